@@ -1,0 +1,193 @@
+/*
+ * nt_gb300.h -- C ABI of the GB300 (sm_103a) kernels behind the analytic
+ * NNGP/NTK path of neural-tangents (nt.stax kernel_fn, nt.batch,
+ * nt.predict.gradient_descent_mse).
+ *
+ * Conventions
+ *   - Every entry point returns 0 on success or a positive NTG_ERR_* code;
+ *     ntg_last_error() returns a message for the calling thread.
+ *   - `stream` is a cudaStream_t passed as void* (0 = legacy default stream).
+ *   - All buffers are device pointers to contiguous float32 arrays unless a
+ *     comment says float64; the caller owns every buffer. Work is enqueued
+ *     on `stream`; no entry point synchronises unless its comment says so.
+ *   - Kernel tensors use the reference's zipped layout: a pair tensor
+ *     (nngp, ntk) is [B, A, A', C, C'] with B = N1*N2 pairs in row-major
+ *     (n1, n2) order; a per-sample tensor (cov1, cov2) is [N, A, A', C, C'].
+ *     One spatial dimension is passed as C = 1; no spatial dimension
+ *     (fully-connected kernels) as A = C = 1.
+ *   - A "variance" operand is the diagonal of a pre-activation per-sample
+ *     kernel, addressed as base + n*s_n + a*s_a + c*s_c.
+ */
+#ifndef NT_GB300_H_
+#define NT_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  NTG_OK = 0,
+  NTG_ERR_INVALID_ARG = 1,
+  NTG_ERR_CUDA = 2,
+  NTG_ERR_UNSUPPORTED = 3,
+  NTG_ERR_NOT_POSITIVE_DEFINITE = 4,
+  NTG_ERR_WAIT_TIMEOUT = 5,
+  NTG_ERR_NO_DEVICE_SCRATCH = 6
+};
+
+enum { NTG_ACT_NONE = 0, NTG_ACT_ABRELU = 1, NTG_ACT_ERF = 2 };
+enum { NTG_PAD_ZERO = 0, NTG_PAD_CIRCULAR = 1 };
+
+/* Activation rule applied to (nngp, ntk) given var1 (first sample) and var2
+ * (second sample).  ABRelu(a, b): neural_tangents/_src/stax/elementwise.py:403-477
+ * (Relu = ABRelu(0, 1)).  Erf(a, b, c): elementwise.py:47-114.
+ * `compensated` = 1 evaluates var1*var2 - q^2 as an exact two-product
+ * difference (accurate near correlation +-1); 0 follows the plain float32
+ * formula of the reference. `stabilize` > 0 is the do_stabilize factor
+ * (ABRelu only; elementwise.py:431-436, 462-466). */
+typedef struct {
+  int32_t kind;
+  float a, b, c;
+  int32_t compensated;
+  float stabilize;
+} ntg_act_t;
+
+/* Affine rule of Dense / Conv on an (unscaled) propagated kernel u:
+ *   nngp_out = w2 * u + b2
+ *   ntk_out  = ntk_w2 * u_ntk + ntk_nn * (nn_scaled ? nngp_out : u) + ntk_c
+ * NTK parameterisation: ntk_w2 = W^2, ntk_nn = 1, nn_scaled = 1, ntk_c = 0
+ * (neural_tangents/_src/stax/linear.py:906-911, 1394-1398); standard:
+ * ntk_nn = fan_in / s0, nn_scaled = 0, ntk_c = (b_std given) (linear.py:912-919,
+ * 1400-1406). */
+typedef struct {
+  float w2, b2;
+  float ntk_w2, ntk_nn, ntk_c;
+  int32_t nn_scaled;
+} ntg_affine_t;
+
+/* Strided view of per-sample variances (diagonal of a per-sample kernel). */
+typedef struct {
+  const float* base;
+  int64_t s_n, s_a, s_c;
+} ntg_var_t;
+
+/* ---- library ---------------------------------------------------------- */
+const char* ntg_last_error(void);
+const char* ntg_version(void);
+/* Number of sm_103a kernels launched by this library since load (all threads). */
+uint64_t ntg_launch_count(void);
+
+/* ---- input kernels (requirements.py:518-638, 641-830) ---------------- */
+/* Flat inputs x1 [N1, D], x2 [N2, D] -> nngp [N1, N2] = x1 x2^T / D.
+ * precision 0: FP32 CUDA cores; 1: split BF16 hi+lo products on tcgen05
+ * tensor cores with FP32 accumulation. Replaces requirements.py:548,564. */
+int ntg_gram(void* stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
+             int64_t d, float* nngp, int32_t precision);
+/* Per-row sum(x^2)/D -> cov [N] (requirements.py:518-526, 572-582). */
+int ntg_cov_diag(void* stream, const float* x, int64_t n, int64_t d, float* cov);
+/* Image inputs x1 [N1, A, C, K], x2 [N2, A, C, K] (NHWC, K channels) ->
+ * full-spatial nngp [N1, N2, A, A, C, C] = sum_k x1 x2 / K
+ * (requirements.py:542-553). With x2 == x1 and pairs == 0 writes the
+ * per-sample cov [N, A, A, C, C] (requirements.py:529-539). */
+int ntg_input_fs(void* stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
+                 int64_t a, int64_t c, int64_t k, int32_t pairs, float* out);
+
+/* ---- Conv / Dense / activations on materialised kernels --------------- */
+/* Full-spatial shared-weight convolution rule (linear.py:1321-1424,
+ * 3115-3207, 3341-3378) on a [B, A, A, C, C] kernel, fused with the affine
+ * rule and an optional activation epilogue.  Filter (fh, fw), strides
+ * (sh, sw), low padding (ph, pw); output spatial size (ao, co); pad_mode
+ * NTG_PAD_ZERO (SAME/VALID) or NTG_PAD_CIRCULAR.  in_ntk may be NULL (the
+ * scalar-zero NTK of an input kernel, or no NTK).  out_ntk may be NULL.
+ * For act.kind != NONE, var1/var2 are the pre-activation variances of the
+ * OUTPUT (diagonal of the convolved per-sample kernels) and n2 > 0 maps pair
+ * b to samples (b / n2, b % n2); n2 == 0 means per-sample (b, b). */
+int ntg_conv_fs(void* stream, const float* in_nngp, const float* in_ntk,
+                float* out_nngp, float* out_ntk, int64_t batch, int64_t n2,
+                int64_t a, int64_t c, int32_t fh, int32_t fw, int32_t sh, int32_t sw,
+                int32_t ph, int32_t pw, int64_t ao, int64_t co, int32_t pad_mode,
+                ntg_affine_t aff, ntg_act_t act, ntg_var_t var1, ntg_var_t var2);
+/* First Conv fused with the input Gram: x1 [N1, A, C, K], x2 [N2, A, C, K]
+ * -> conv(x1 x2^T / K) with affine + activation, written as [N1*N2, A, A, C, C]
+ * (3x3 / stride 1 / SAME / zero padding). ntk_out = nngp_out before the
+ * activation, as for an input kernel whose NTK is the scalar zero. */
+int ntg_conv_input_fs(void* stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
+                      int64_t a, int64_t c, int64_t k, float* out_nngp, float* out_ntk,
+                      ntg_affine_t aff, ntg_act_t act, ntg_var_t var1, ntg_var_t var2);
+/* Diagonal-spatial convolution (linear.py:3381-3437): [B, A, C] box filter. */
+int ntg_conv_ds(void* stream, const float* in_nngp, const float* in_ntk, float* out_nngp,
+                float* out_ntk, int64_t batch, int64_t a, int64_t c, int32_t fh, int32_t fw,
+                int32_t sh, int32_t sw, int32_t ph, int32_t pw, int64_t ao, int64_t co,
+                int32_t pad_mode, ntg_affine_t aff);
+/* Elementwise Dense rule and/or activation on [B, M] kernels (M spatial
+ * entries per pair; spatial index m -> (a, a', c, c') of an [A, A, C, C]
+ * block, or (a, c) of [A, C] when diag_spatial != 0).  var1/var2 give the
+ * pre-activation variances (after the affine when has_affine). */
+int ntg_affine_act(void* stream, const float* in_nngp, const float* in_ntk, float* out_nngp,
+                   float* out_ntk, int64_t batch, int64_t n2, int64_t a, int64_t c,
+                   int32_t diag_spatial, int32_t has_affine, ntg_affine_t aff, ntg_act_t act,
+                   ntg_var_t var1, ntg_var_t var2);
+/* max |x| over n entries -> out[0] (do_stabilize factor, elementwise.py:431-436). */
+int ntg_max_abs(void* stream, const float* x, int64_t n, float* out);
+
+/* ---- pooling / readout ------------------------------------------------ */
+/* AvgPool / SumPool rule (linear.py:1631-1664, 3499-3572) on [B, A, A, C, C]
+ * (diag_spatial = 0) or [B, A, C] (diag_spatial = 1): reduce_window with
+ * window (wa, wc), strides (sa, sc), low padding (pa, pc), zero or circular
+ * padding; scale = 1/prod(window) (average), 1 (sum); normalize_edges = 1
+ * divides by the in-bounds window size instead. diag_spatial average pooling
+ * applies the normalisation twice (linear.py:1653-1657). */
+int ntg_pool(void* stream, const float* in, float* out, int64_t batch, int64_t a, int64_t c,
+             int32_t wa, int32_t wc, int32_t sa, int32_t sc, int32_t pa, int32_t pc,
+             int64_t ao, int64_t co, int32_t pad_mode, int32_t diag_spatial, int32_t average,
+             int32_t normalize_edges);
+/* Mean (average = 1) or sum over all m entries of each of B rows: [B, M] -> [B]
+ * (GlobalAvgPool / GlobalSumPool, linear.py:1771-1801). `post_scale`
+ * multiplies the result (1/M_extra for the diagonal-spatial case). */
+int ntg_global_pool(void* stream, const float* in, float* out, int64_t batch, int64_t m,
+                    int32_t average, float post_scale);
+/* Flatten rule on a full-spatial kernel (linear.py:1865-1899): mean of the
+ * spatial diagonal K[b, a, a, c, c] -> [B]. */
+int ntg_flatten_fs(void* stream, const float* in, float* out, int64_t batch, int64_t a,
+                   int64_t c);
+
+/* ---- fused whole-network kernel per pair ------------------------------ */
+/* A chain program: `nseg` spatial segments of sizes s0, s0/2, ...; segment
+ * i holds nconv[i] layers of [3x3 SAME Conv + activation]; an AvgPool(2,2)
+ * stride 2 separates segments; readout 0 = mean over all spatial entries
+ * (GlobalAvgPool, or AvgPools down to 1x1 then Flatten), 1 = Flatten
+ * (mean of the spatial diagonal). Layers are numbered in order; conv layer
+ * l has affine aff[l] and activation act[l]; its pre-activation variances
+ * for sample n start at var1 + n*var_stride + var_off[l] as an s_i x s_i
+ * map (same for var2). */
+#define NTG_CHAIN_MAX_SEG 4
+#define NTG_CHAIN_MAX_LAYERS 16
+typedef struct {
+  int32_t nseg;
+  int32_t s0;
+  int32_t channels;
+  int32_t readout;
+  int32_t nconv[NTG_CHAIN_MAX_SEG];
+  ntg_affine_t aff[NTG_CHAIN_MAX_LAYERS];
+  ntg_act_t act[NTG_CHAIN_MAX_LAYERS];
+  int64_t var_off[NTG_CHAIN_MAX_LAYERS];
+  int64_t var_stride;
+} ntg_chain_t;
+/* Fused Myrtle-family kernel: inputs x1 [N1, s0, s0, K], x2 [N2, s0, s0, K]
+ * (NHWC); writes the readout nngp/ntk [N1, N2] (before the layers that
+ * follow the readout). Pairs (i, j) with i in [r0, r0+n1), j in [c0, c0+n2)
+ * of the x1 / x2 arrays; out has row stride ld_out. Replaces the per-layer
+ * chain of linear.py:1321-1424 / elementwise.py:423-477 / linear.py:1631-1664
+ * / 1771-1801 / 1865-1899 for that network family. */
+int ntg_chain_fwd(void* stream, const ntg_chain_t* prog, const float* x1, const float* x2,
+                  int64_t r0, int64_t n1, int64_t c0, int64_t n2, const float* var1,
+                  const float* var2, float* out_nngp, float* out_ntk, int64_t ld_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NT_GB300_H_ */

@@ -1,0 +1,135 @@
+"""ctypes binding of libntgb300.so (the C ABI declared in include/nt_gb300.h).
+
+The library is loaded from this package directory. On a CUDA machine a
+missing or unloadable library is an error: there is no CPU fallback for any
+kernel of this package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, 'libntgb300.so')
+
+NTG_ACT_NONE, NTG_ACT_ABRELU, NTG_ACT_ERF = 0, 1, 2
+NTG_PAD_ZERO, NTG_PAD_CIRCULAR = 0, 1
+CHAIN_MAX_SEG, CHAIN_MAX_LAYERS = 4, 16
+
+ERRORS = {
+    1: 'invalid argument', 2: 'CUDA error', 3: 'unsupported', 4: 'not positive definite',
+    5: 'wait timeout', 6: 'no device scratch',
+}
+
+
+class Act(C.Structure):
+    _fields_ = [('kind', C.c_int32), ('a', C.c_float), ('b', C.c_float), ('c', C.c_float),
+                ('compensated', C.c_int32), ('stabilize', C.c_float)]
+
+
+class Affine(C.Structure):
+    _fields_ = [('w2', C.c_float), ('b2', C.c_float), ('ntk_w2', C.c_float),
+                ('ntk_nn', C.c_float), ('ntk_c', C.c_float), ('nn_scaled', C.c_int32)]
+
+
+class Var(C.Structure):
+    _fields_ = [('base', C.c_void_p), ('s_n', C.c_int64), ('s_a', C.c_int64),
+                ('s_c', C.c_int64)]
+
+
+class Chain(C.Structure):
+    _fields_ = [('nseg', C.c_int32), ('s0', C.c_int32), ('channels', C.c_int32),
+                ('readout', C.c_int32), ('nconv', C.c_int32 * CHAIN_MAX_SEG),
+                ('aff', Affine * CHAIN_MAX_LAYERS), ('act', Act * CHAIN_MAX_LAYERS),
+                ('var_off', C.c_int64 * CHAIN_MAX_LAYERS), ('var_stride', C.c_int64)]
+
+
+_P, _I64, _I32, _F = C.c_void_p, C.c_int64, C.c_int32, C.c_float
+
+SIGNATURES = {
+    'ntg_last_error': ([], C.c_char_p),
+    'ntg_version': ([], C.c_char_p),
+    'ntg_launch_count': ([], C.c_uint64),
+    'ntg_gram': ([_P, _P, _P, _I64, _I64, _I64, _P, _I32], C.c_int),
+    'ntg_cov_diag': ([_P, _P, _I64, _I64, _P], C.c_int),
+    'ntg_input_fs': ([_P, _P, _P, _I64, _I64, _I64, _I64, _I64, _I32, _P], C.c_int),
+    'ntg_conv_fs': ([_P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, _I32, _I32, _I32, _I32,
+                     _I32, _I32, _I64, _I64, _I32, Affine, Act, Var, Var], C.c_int),
+    'ntg_conv_input_fs': ([_P, _P, _P, _I64, _I64, _I64, _I64, _I64, _P, _P, Affine, Act, Var,
+                           Var], C.c_int),
+    'ntg_conv_ds': ([_P, _P, _P, _P, _P, _I64, _I64, _I64, _I32, _I32, _I32, _I32, _I32, _I32,
+                     _I64, _I64, _I32, Affine], C.c_int),
+    'ntg_affine_act': ([_P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, _I32, _I32, Affine, Act,
+                        Var, Var], C.c_int),
+    'ntg_max_abs': ([_P, _P, _I64, _P], C.c_int),
+    'ntg_pool': ([_P, _P, _P, _I64, _I64, _I64, _I32, _I32, _I32, _I32, _I32, _I32, _I64, _I64,
+                  _I32, _I32, _I32, _I32], C.c_int),
+    'ntg_global_pool': ([_P, _P, _P, _I64, _I64, _I32, _F], C.c_int),
+    'ntg_flatten_fs': ([_P, _P, _P, _I64, _I64, _I64], C.c_int),
+    'ntg_chain_fwd': ([_P, C.POINTER(Chain), _P, _P, _I64, _I64, _I64, _I64, _P, _P, _P, _P,
+                       _I64], C.c_int),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load() -> C.CDLL:
+    """Loads the library (building it first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            from . import _build
+            _build.build()
+        lib = C.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(lib, name, None)
+            if fn is None:
+                raise RuntimeError(f'{LIB_PATH} does not export {name}')
+            fn.argtypes = args
+            fn.restype = res
+        _lib = lib
+    return _lib
+
+
+class NtgError(RuntimeError):
+    pass
+
+
+def call(name: str, *args) -> None:
+    """Calls an entry point; raises NtgError with the library message on failure."""
+    lib = load()
+    rc = getattr(lib, name)(*args)
+    if rc != 0:
+        msg = lib.ntg_last_error().decode()
+        raise NtgError(f'{name} failed ({ERRORS.get(rc, rc)}): {msg}')
+
+
+def launch_count() -> int:
+    return int(load().ntg_launch_count())
+
+
+def stream() -> int:
+    """The current torch CUDA stream as a raw cudaStream_t value."""
+    return torch.cuda.current_stream().cuda_stream
+
+
+def ptr(t) -> int | None:
+    if t is None:
+        return None
+    if not t.is_cuda or t.dtype != torch.float32 or not t.is_contiguous():
+        raise ValueError('nt_gb300 kernels take contiguous float32 CUDA tensors')
+    return t.data_ptr()
+
+
+def require_cuda() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError('nt_gb300 needs a CUDA device (sm_103a); there is no CPU fallback')
+    return torch.device('cuda', torch.cuda.current_device())

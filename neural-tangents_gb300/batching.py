@@ -1,0 +1,104 @@
+"""nt_gb300.batch -- tiled evaluation of kernel functions (neural_tangents/_src/batching.py:76-132).
+
+``batch(kernel_fn, batch_size)`` returns a function with ``kernel_fn``'s
+signature that evaluates the N1 x N2 kernel in tiles of at most
+``batch_size`` rows and columns. Unlike the reference (batching.py:647-679),
+N1 and N2 need not be multiples of ``batch_size``: the edge tiles are ragged.
+For networks the fused chain kernel covers, the whole grid is one launch of
+that kernel (the per-sample chains run once per sample, in ``batch_size``
+chunks) and ``batch_size`` only bounds the per-sample working set.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _chain
+from .kernel import Kernel, analytic_kernel
+from .stax import KernelFn, _Ctx, _as_input, _normalize_get
+
+
+def _tiles(n: int, b: int):
+    return [(s, min(b, n - s)) for s in range(0, n, b)]
+
+
+def batch(kernel_fn, batch_size: int = 0, device_count: int = -1, store_on_device: bool = True):
+    """batching.py:76-132 (one device: serial tiling)."""
+    if device_count not in (-1, 0, 1):
+        raise NotImplementedError('nt_gb300 runs on one GPU; device_count must be -1, 0 or 1')
+
+    def batched(x1, x2=None, get=None, *, precision='fp32', **kwargs):
+        if isinstance(x1, Kernel):
+            return kernel_fn(x1, x2, get, **kwargs)
+        x1t = _as_input(x1)
+        x2t = None if x2 is None else _as_input(x2)
+        names, single = _normalize_get(get)
+        ctx = _Ctx(precision)
+        bs = batch_size or max(x1t.shape[0], (x2t if x2t is not None else x1t).shape[0])
+        if isinstance(kernel_fn, KernelFn) and not kwargs.get('diagonal_spatial'):
+            plan = _chain.plan_chain(kernel_fn.specs, tuple(x1t.shape), False)
+            if plan is not None and (x2t is None or x2t.shape[1:] == x1t.shape[1:]):
+                old = _chain.SELF_CHUNK
+                _chain.SELF_CHUNK = max(1, min(old, bs))
+                try:
+                    k = _chain.run_fused(plan, x1t, x2t, ctx)
+                finally:
+                    _chain.SELF_CHUNK = old
+                k = kernel_fn.apply_kernel(k, ctx, specs=plan.post)
+                if names is not None and 'ntk' not in names:
+                    k = k.replace(ntk=None)
+                return _select(k, names, single)
+        xb = x1t if x2t is None else x2t
+        n1, n2 = x1t.shape[0], xb.shape[0]
+        rows = []
+        for r0, rn in _tiles(n1, bs):
+            cols = []
+            for c0, cn in _tiles(n2, bs):
+                out = kernel_fn(x1t[r0:r0 + rn], xb[c0:c0 + cn], get, precision=precision,
+                                **kwargs)
+                if not store_on_device:
+                    out = _to_cpu(out)
+                cols.append(out)
+            rows.append(cols)
+        return _assemble(rows, names, single)
+
+    batched.__name__ = getattr(kernel_fn, '__name__', 'kernel_fn')
+    return batched
+
+
+def _to_cpu(out):
+    if isinstance(out, torch.Tensor):
+        return out.cpu()
+    if isinstance(out, tuple):
+        return type(out)(*[None if v is None else v.cpu() for v in out])
+    return out
+
+
+def _select(k: Kernel, names, single):
+    if names is None:
+        return k
+    vals = tuple(getattr(k, n) for n in names)
+    return vals[0] if single is not None else analytic_kernel(names, vals)
+
+
+def _cat_grid(grid):
+    return torch.cat([torch.cat(row, dim=1) for row in grid], dim=0)
+
+
+def _assemble(rows, names, single):
+    if names is None:
+        raise NotImplementedError('batch(get=None) is not supported; pass get=("nngp", "ntk")')
+    if single is not None:
+        return _cat_grid(rows)
+    vals = []
+    for idx, n in enumerate(names):
+        grid = [[c[idx] for c in row] for row in rows]
+        if n in ('nngp', 'ntk'):
+            vals.append(_cat_grid(grid))
+        elif n == 'cov1':
+            vals.append(torch.cat([row[0] for row in grid], dim=0))
+        elif n == 'cov2':
+            vals.append(torch.cat(grid[0], dim=0))
+        else:
+            vals.append(grid[0][0])
+    return analytic_kernel(names, tuple(vals))

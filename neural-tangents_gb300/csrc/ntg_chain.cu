@@ -1,0 +1,431 @@
+// Fused whole-network NNGP/NTK kernel for the Myrtle conv-net family on sm_103a.
+//
+// One CTA computes one (x1[i], x2[j]) pair end to end: first-layer Gram ->
+// [3x3 SAME Conv + activation] x n0 -> AvgPool(2) -> [Conv + act] x n1 ->
+// AvgPool(2) -> ... -> readout (mean of all spatial entries, or the mean of the
+// spatial diagonal).  Nothing but the two readout scalars reaches HBM.
+//
+// Data layout.  The full-spatial kernel K[h, h', w, w'] of a pair is walked
+// along its "lines": a line is the set of planes (h, h + delta) for a fixed
+// delta; every Conv rule only couples planes of the same line
+// (K'[h,h',..] = sum_d K[h+d, h'+d, ..]).  Inside a plane the (w, w') square is
+// stored skewed: row r = (w' - w) mod S, column c = w, so the w-direction
+// stencil neighbours (w +- 1, w' +- 1) are column neighbours of the same row
+// (a row holds two diagonals of the square, split at c = S - r).  A thread owns
+// EPT consecutive columns of one row in every plane of a line; the h-direction
+// stencil is a 3-plane register ring, the w-direction one two warp shuffles.
+// AvgPool(2) couples lines 2m-1, 2m, 2m+1 into pooled line m; pooled lines
+// accumulate in shared memory and a completed pooled line is processed by the
+// next segment right away, so the per-pair working set stays on chip.
+#include "ntg_common.cuh"
+
+namespace ntg {
+namespace {
+
+constexpr int NT = 256;
+
+struct ChainCtx {
+  const float4* img1;  // [S0*S0] pixels, channels padded to 4
+  const float4* img2;
+  float* stage;        // [2 buffers][2 tensors][S0*S0]
+  float inv_k;
+  float acc_q, acc_t;  // per-thread readout partial sums
+  int readout;
+};
+
+__device__ __forceinline__ float wshift_left(float v) {
+  return __shfl_up_sync(0xffffffffu, v, 1);
+}
+__device__ __forceinline__ float wshift_right(float v) {
+  return __shfl_down_sync(0xffffffffu, v, 1);
+}
+
+__device__ __forceinline__ void zero_slot(float* q, float* t, int n) {
+  for (int i = threadIdx.x; i < n; i += NT) {
+    q[i] = 0.f;
+    t[i] = 0.f;
+  }
+}
+
+// Processes line `delta` of a segment of size S with NC conv layers.
+// FIRST: level-0 input is the first-layer Gram of the two images (its NTK is
+// the scalar zero of an input kernel); otherwise it is pooled line
+// `in_q/in_t` ([S][S*S], scaled by 1/16 for the AvgPool normalisation).
+// LAST: the final level feeds the readout sums, otherwise it is average-pooled
+// into the line slots of segment `seg + 1`.
+// `vmaps` holds this segment's variance maps, layer k at vmaps + 2*k*S*S
+// (sample 1) and + S*S more (sample 2); `out_slots` is the next segment's
+// slot region ([parity][tensor][S/2][S/2 * S/2]).
+template <int S, int NC, bool FIRST, bool LAST>
+__device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg, int lbase,
+                                             const float* vmaps, float* out_slots, int delta,
+                                             const float* in_q, const float* in_t) {
+  constexpr int EPT = (S * S >= NT) ? (S * S / NT) : 1;
+  constexpr int TPR = S / EPT;
+  constexpr int ACTIVE = S * S / EPT;
+  static_assert(TPR <= 32 && 32 % TPR == 0, "rows must tile warps");
+  static_assert(ACTIVE % 32 == 0 && ACTIVE <= NT, "whole warps");
+  const int tid = threadIdx.x;
+  const bool on = tid < ACTIVE;
+  const int r = on ? tid / TPR : 0;
+  const int c0 = on ? (tid % TPR) * EPT : 0;
+  const int lo = delta < 0 ? -delta : 0;
+  const int hi = delta < 0 ? S : S - delta;
+
+  bool ml[EPT], mr[EPT];
+  int wp[EPT];
+#pragma unroll
+  for (int u = 0; u < EPT; ++u) {
+    int c = c0 + u;
+    ml[u] = c >= 1 && c != S - r;
+    mr[u] = c <= S - 2 && c != S - 1 - r;
+    wp[u] = (c + r) & (S - 1);
+  }
+
+  // Ring of the last two planes of every level (level 0 = input).
+  float Aq[NC + 1][EPT], Bq[NC + 1][EPT], At[NC + 1][EPT], Bt[NC + 1][EPT];
+#pragma unroll
+  for (int k = 0; k <= NC; ++k)
+#pragma unroll
+    for (int u = 0; u < EPT; ++u) Aq[k][u] = Bq[k][u] = At[k][u] = Bt[k][u] = 0.f;
+
+  int buf = 0;
+  __syncthreads();
+  for (int s = lo; s < hi + NC; ++s) {
+    float nq[EPT], nt[EPT];
+    // ---- level 0 at plane s ----
+#pragma unroll
+    for (int u = 0; u < EPT; ++u) nq[u] = nt[u] = 0.f;
+    if (on && s < hi) {
+      if (FIRST) {
+        const float4* x1r = cx.img1 + s * S;
+        const float4* x2r = cx.img2 + (s + delta) * S;
+#pragma unroll
+        for (int u = 0; u < EPT; ++u) {
+          float4 a = x1r[c0 + u], b = x2r[wp[u]];
+          float g = fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)));
+          nq[u] = g * cx.inv_k;
+        }
+      } else {
+        const float* pq = in_q + s * S * S + r * S + c0;
+        const float* pt = in_t + s * S * S + r * S + c0;
+#pragma unroll
+        for (int u = 0; u < EPT; ++u) {
+          nq[u] = pq[u] * 0.0625f;
+          nt[u] = pt[u] * 0.0625f;
+        }
+      }
+    }
+    // ---- conv layers: level k+1 at plane s-k-1 ----
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      const int p = s - k - 1;
+      const int l = lbase + k;
+      const bool has_t = !(FIRST && k == 0);
+      float hq[EPT], ht[EPT];
+#pragma unroll
+      for (int u = 0; u < EPT; ++u) {
+        hq[u] = (Aq[k][u] + Bq[k][u]) + nq[u];
+        ht[u] = has_t ? (At[k][u] + Bt[k][u]) + nt[u] : 0.f;
+      }
+      const float lq = wshift_left(hq[EPT - 1]), rq = wshift_right(hq[0]);
+      const float lt = has_t ? wshift_left(ht[EPT - 1]) : 0.f;
+      const float rt = has_t ? wshift_right(ht[0]) : 0.f;
+      float oq[EPT], ot[EPT];
+      const bool in_line = p >= lo && p < hi;
+      const ntg_affine_t& af = pg.aff[l];
+      const ntg_act_t& ac = pg.act[l];
+#pragma unroll
+      for (int u = 0; u < EPT; ++u) {
+        float xl = (u > 0) ? hq[u - 1] : lq;
+        float xr = (u < EPT - 1) ? hq[u + 1] : rq;
+        float cq = ((ml[u] ? xl : 0.f) + hq[u]) + (mr[u] ? xr : 0.f);
+        float ct = 0.f;
+        if (has_t) {
+          float yl = (u > 0) ? ht[u - 1] : lt;
+          float yr = (u < EPT - 1) ? ht[u + 1] : rt;
+          ct = ((ml[u] ? yl : 0.f) + ht[u]) + (mr[u] ? yr : 0.f);
+        }
+        const float inv9 = 1.f / 9.f;
+        float q, t = 0.f;
+        apply_affine(af, cq * inv9, ct * inv9, true, q, t);
+        if (ac.kind != NTG_ACT_NONE && on && in_line) {
+          const float* vm = vmaps + 2 * k * S * S;
+          float v1 = vm[p * S + c0 + u];
+          float v2 = vm[S * S + (p + delta) * S + wp[u]];
+          apply_act(ac, q, t, v1, v2);
+        }
+        oq[u] = in_line ? q : 0.f;
+        ot[u] = in_line ? t : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < EPT; ++u) {
+        Aq[k][u] = Bq[k][u];
+        Bq[k][u] = nq[u];
+        At[k][u] = Bt[k][u];
+        Bt[k][u] = nt[u];
+        nq[u] = oq[u];
+        nt[u] = ot[u];
+      }
+    }
+    // ---- emit the last level at plane p = s - NC ----
+    const int p = s - NC;
+    if (p < lo || p >= hi) continue;
+    if (LAST) {
+      if (on) {
+        if (cx.readout == 0) {
+#pragma unroll
+          for (int u = 0; u < EPT; ++u) {
+            cx.acc_q += nq[u];
+            cx.acc_t += nt[u];
+          }
+        } else if (delta == 0 && r == 0) {
+#pragma unroll
+          for (int u = 0; u < EPT; ++u) {
+            cx.acc_q += nq[u];
+            cx.acc_t += nt[u];
+          }
+        }
+      }
+    } else {
+      float* sq = cx.stage + (2 * buf) * (S * S);
+      float* st = sq + S * S;
+      if (on) {
+#pragma unroll
+        for (int u = 0; u < EPT; ++u) {
+          sq[(c0 + u) * S + wp[u]] = nq[u];
+          st[(c0 + u) * S + wp[u]] = nt[u];
+        }
+      }
+      __syncthreads();
+      constexpr int H = S / 2;
+      if (tid < H * H) {
+        const int rho = tid / H, kap = tid % H;
+        const int j = kap, jp = (kap + rho) & (H - 1);
+        const int o0 = (2 * j) * S + 2 * jp, o1 = o0 + S;
+        float vq = (sq[o0] + sq[o0 + 1]) + (sq[o1] + sq[o1 + 1]);
+        float vt = (st[o0] + st[o0 + 1]) + (st[o1] + st[o1 + 1]);
+        const int I = p >> 1;
+        const int m = ((p + delta) >> 1) - I;
+        const int par = m & 1;
+        float* dq = out_slots + (2 * par) * (H * H * H) + I * H * H + tid;
+        float* dt = dq + H * H * H;
+        *dq += vq;
+        *dt += vt;
+      }
+      buf ^= 1;
+    }
+  }
+  __syncthreads();
+}
+
+template <int S, bool LAST>
+__device__ __forceinline__ void process_pooled_line(ChainCtx& cx, const ntg_chain_t& pg, int ncv,
+                                                    int lbase, const float* vmaps,
+                                                    const float* in_slots, float* out_slots,
+                                                    int m) {
+  const float* q = in_slots + (2 * (m & 1)) * (S * S * S);
+  const float* t = q + S * S * S;
+  switch (ncv) {
+    case 0: process_line<S, 0, false, LAST>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
+    case 1: process_line<S, 1, false, LAST>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
+    case 2: process_line<S, 2, false, LAST>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
+    default: process_line<S, 3, false, LAST>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
+  }
+}
+
+// Segment sizes 32 -> 16 -> 8 (nseg <= 3); segment 0 has N0 conv layers.
+template <int N0>
+__global__ void __launch_bounds__(NT, 1)
+    chain_fwd_kernel(const __grid_constant__ ntg_chain_t pg, const float* __restrict__ x1,
+                     const float* __restrict__ x2, int64_t r0, int64_t n1, int64_t c0,
+                     int64_t n2, const float* __restrict__ var1, const float* __restrict__ var2,
+                     float* __restrict__ out_q, float* __restrict__ out_t, int64_t ld_out) {
+  constexpr int S0 = 32, S1 = 16, S2 = 8;
+  extern __shared__ __align__(16) float smem[];
+  const int64_t pair = blockIdx.x;
+  const int64_t i = pair / n2, j = pair - (pair / n2) * n2;
+  const int64_t gi = r0 + i, gj = c0 + j;
+  const int K = pg.channels;
+  const int nseg = pg.nseg;
+
+  ChainCtx cx;
+  float4* img1 = reinterpret_cast<float4*>(smem);
+  float4* img2 = img1 + S0 * S0;
+  float* p = reinterpret_cast<float*>(img2 + S0 * S0);
+  // per-layer variance maps of both samples, segment by segment
+  float* vseg[3] = {nullptr, nullptr, nullptr};
+  {
+    int l = 0;
+    for (int sgi = 0; sgi < nseg; ++sgi) {
+      const int S = S0 >> sgi;
+      vseg[sgi] = p;
+      for (int k = 0; k < pg.nconv[sgi]; ++k, ++l) {
+        const float* g1 = var1 + gi * pg.var_stride + pg.var_off[l];
+        const float* g2 = var2 + gj * pg.var_stride + pg.var_off[l];
+        for (int e = threadIdx.x; e < S * S; e += NT) {
+          p[e] = __ldg(g1 + e);
+          p[S * S + e] = __ldg(g2 + e);
+        }
+        p += 2 * S * S;
+      }
+    }
+  }
+  float* slots1 = p;
+  if (nseg > 1) p += 4 * S1 * S1 * S1;
+  float* slots2 = p;
+  if (nseg > 2) p += 4 * S2 * S2 * S2;
+  cx.stage = p;
+  p += 4 * S0 * S0;
+  float* red = p;  // 2 * NT/32 floats
+
+  // images, channels padded to 4
+  const float* im1 = x1 + gi * S0 * S0 * K;
+  const float* im2 = x2 + gj * S0 * S0 * K;
+  for (int e = threadIdx.x; e < S0 * S0; e += NT) {
+    float a[4] = {0.f, 0.f, 0.f, 0.f}, b[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int k = 0; k < K; ++k) {
+      a[k] = __ldg(im1 + e * K + k);
+      b[k] = __ldg(im2 + e * K + k);
+    }
+    img1[e] = make_float4(a[0], a[1], a[2], a[3]);
+    img2[e] = make_float4(b[0], b[1], b[2], b[3]);
+  }
+  cx.img1 = img1;
+  cx.img2 = img2;
+  cx.inv_k = 1.f / (float)K;
+  cx.acc_q = cx.acc_t = 0.f;
+  cx.readout = pg.readout;
+  __syncthreads();
+
+  const int lb1 = pg.nconv[0];
+  const int lb2 = lb1 + (nseg > 1 ? pg.nconv[1] : 0);
+  const int nc1 = nseg > 1 ? pg.nconv[1] : 0;
+  const int nc2 = nseg > 2 ? pg.nconv[2] : 0;
+  for (int d0 = -(S0 - 1); d0 <= S0 - 1; ++d0) {
+    if (nseg > 1 && (d0 & 1)) {
+      const int m = (d0 + 1) / 2;
+      if (m <= S1 - 1) {
+        float* z = slots1 + (2 * (m & 1)) * (S1 * S1 * S1);
+        zero_slot(z, z + S1 * S1 * S1, S1 * S1 * S1);
+      }
+    }
+    if (nseg == 1)
+      process_line<S0, N0, true, true>(cx, pg, 0, vseg[0], nullptr, d0, nullptr, nullptr);
+    else
+      process_line<S0, N0, true, false>(cx, pg, 0, vseg[0], slots1, d0, nullptr, nullptr);
+    if (nseg > 1 && (d0 & 1)) {
+      const int m1 = (d0 - 1) / 2;
+      if (m1 >= -(S1 - 1)) {
+        if (nseg > 2 && (m1 & 1)) {
+          const int m = (m1 + 1) / 2;
+          if (m <= S2 - 1) {
+            float* z = slots2 + (2 * (m & 1)) * (S2 * S2 * S2);
+            zero_slot(z, z + S2 * S2 * S2, S2 * S2 * S2);
+          }
+        }
+        if (nseg == 2)
+          process_pooled_line<S1, true>(cx, pg, nc1, lb1, vseg[1], slots1, nullptr, m1);
+        else
+          process_pooled_line<S1, false>(cx, pg, nc1, lb1, vseg[1], slots1, slots2, m1);
+        if (nseg > 2 && (m1 & 1)) {
+          const int m2 = (m1 - 1) / 2;
+          if (m2 >= -(S2 - 1))
+            process_pooled_line<S2, true>(cx, pg, nc2, lb2, vseg[2], slots2, nullptr, m2);
+        }
+      }
+    }
+  }
+
+  // block reduction of the readout sums
+  float aq = cx.acc_q, at = cx.acc_t;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    aq += __shfl_xor_sync(0xffffffffu, aq, o);
+    at += __shfl_xor_sync(0xffffffffu, at, o);
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    red[warp] = aq;
+    red[NT / 32 + warp] = at;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float sq = 0.f, st = 0.f;
+    for (int w = 0; w < NT / 32; ++w) {
+      sq += red[w];
+      st += red[NT / 32 + w];
+    }
+    const int Sl = S0 >> (nseg - 1);
+    const float cnt = pg.readout == 0 ? (float)Sl * Sl * Sl * Sl : (float)Sl * Sl;
+    out_q[i * ld_out + j] = sq / cnt;
+    if (out_t) out_t[i * ld_out + j] = st / cnt;
+  }
+}
+
+size_t chain_smem_bytes(const ntg_chain_t& pg) {
+  size_t f = 2 * 32 * 32 * 4;  // images (float4)
+  for (int sgi = 0; sgi < pg.nseg; ++sgi) {
+    size_t S = 32 >> sgi;
+    f += 2 * S * S * pg.nconv[sgi];
+    if (sgi > 0) f += 4 * S * S * S;
+  }
+  f += 4 * 32 * 32;  // staging
+  f += 2 * NT / 32;
+  return f * sizeof(float);
+}
+
+}  // namespace
+}  // namespace ntg
+
+using namespace ntg;
+
+extern "C" int ntg_chain_fwd(void* stream, const ntg_chain_t* prog, const float* x1,
+                             const float* x2, int64_t r0, int64_t n1, int64_t c0, int64_t n2,
+                             const float* var1, const float* var2, float* out_q, float* out_t,
+                             int64_t ld_out) {
+  NTG_REQUIRE(prog && x1 && x2 && var1 && var2 && out_q, "ntg_chain_fwd: null pointer");
+  const ntg_chain_t& pg = *prog;
+  NTG_REQUIRE(pg.s0 == 32, "ntg_chain_fwd: the fused chain needs 32x32 inputs");
+  NTG_REQUIRE(pg.nseg >= 1 && pg.nseg <= 3, "ntg_chain_fwd: 1 to 3 segments");
+  NTG_REQUIRE(pg.channels >= 1 && pg.channels <= 4, "ntg_chain_fwd: 1 to 4 input channels");
+  NTG_REQUIRE(pg.nconv[0] >= 1 && pg.nconv[0] <= 3, "ntg_chain_fwd: 1 to 3 convs in segment 0");
+  int nl = 0;
+  for (int s = 0; s < pg.nseg; ++s) {
+    NTG_REQUIRE(pg.nconv[s] >= 0 && pg.nconv[s] <= 3, "ntg_chain_fwd: 0 to 3 convs per segment");
+    nl += pg.nconv[s];
+  }
+  NTG_REQUIRE(nl <= NTG_CHAIN_MAX_LAYERS, "ntg_chain_fwd: too many layers");
+  NTG_REQUIRE(pg.readout == 0 || pg.readout == 1, "ntg_chain_fwd: readout must be 0 or 1");
+  NTG_REQUIRE(n1 > 0 && n2 > 0 && r0 >= 0 && c0 >= 0 && ld_out >= n2, "ntg_chain_fwd: bad tile");
+  NTG_REQUIRE(n1 * n2 < (1ll << 31), "ntg_chain_fwd: tile too large");
+  size_t sm = chain_smem_bytes(pg);
+  cudaStream_t s = as_stream(stream);
+  cudaError_t e = cudaSuccess;
+  switch (pg.nconv[0]) {
+    case 1:
+      e = cudaFuncSetAttribute(chain_fwd_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)sm);
+      if (e == cudaSuccess)
+        chain_fwd_kernel<1><<<(unsigned)(n1 * n2), NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1,
+                                                                 var2, out_q, out_t, ld_out);
+      break;
+    case 2:
+      e = cudaFuncSetAttribute(chain_fwd_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)sm);
+      if (e == cudaSuccess)
+        chain_fwd_kernel<2><<<(unsigned)(n1 * n2), NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1,
+                                                                 var2, out_q, out_t, ld_out);
+      break;
+    default:
+      e = cudaFuncSetAttribute(chain_fwd_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)sm);
+      if (e == cudaSuccess)
+        chain_fwd_kernel<3><<<(unsigned)(n1 * n2), NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1,
+                                                                 var2, out_q, out_t, ld_out);
+      break;
+  }
+  if (e != cudaSuccess) return fail(NTG_ERR_CUDA, std::string("ntg_chain_fwd: ") + cudaGetErrorString(e));
+  note_launch();
+  return check_launch("ntg_chain_fwd");
+}

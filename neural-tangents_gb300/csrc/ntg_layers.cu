@@ -1,0 +1,654 @@
+// Materialised layer rules of the analytic NNGP/NTK path on sm_103a:
+// input covariances, the full-spatial Conv stencil (with the Dense/Conv affine
+// rule and the ABRelu/Erf epilogue fused in), elementwise Dense/activation,
+// pooling and the Flatten / GlobalAvgPool readouts.
+#include <cstdio>
+
+#include "ntg_common.cuh"
+
+namespace ntg {
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ void pair_of(int64_t b, int64_t n2, int64_t& i1, int64_t& i2) {
+  if (n2 > 0) {
+    i1 = b / n2;
+    i2 = b - i1 * n2;
+  } else {
+    i1 = b;
+    i2 = b;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Flat Gram on CUDA cores: out[i, j] = sum_d x1[i, d] x2[j, d] / D.
+// 64x64 output tile per CTA, 16x16 threads, 4x4 outputs per thread.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) gram_simt_kernel(const float* __restrict__ x1,
+                                                        const float* __restrict__ x2,
+                                                        int64_t n1, int64_t n2, int64_t d,
+                                                        float inv_d, float* __restrict__ out) {
+  __shared__ float As[16][64 + 4];
+  __shared__ float Bs[16][64 + 4];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t row0 = (int64_t)blockIdx.y * 64, col0 = (int64_t)blockIdx.x * 64;
+  float acc[4][4] = {};
+  for (int64_t k0 = 0; k0 < d; k0 += 16) {
+    for (int idx = threadIdx.x; idx < 16 * 64; idx += 256) {
+      int r = idx / 16, kk = idx % 16;
+      int64_t gi = row0 + r, gk = k0 + kk;
+      As[kk][r] = (gi < n1 && gk < d) ? __ldg(x1 + gi * d + gk) : 0.f;
+      int64_t gj = col0 + r;
+      Bs[kk][r] = (gj < n2 && gk < d) ? __ldg(x2 + gj * d + gk) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      float a[4], bb[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = As[kk][ty * 4 + u];
+        bb[u] = Bs[kk][tx * 4 + u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], bb[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      int64_t gi = row0 + ty * 4 + u, gj = col0 + tx * 4 + v;
+      if (gi < n1 && gj < n2) out[gi * n2 + gj] = acc[u][v] * inv_d;
+    }
+}
+
+__global__ void cov_diag_kernel(const float* __restrict__ x, int64_t n, int64_t d, float inv_d,
+                                float* __restrict__ cov) {
+  int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  float s = 0.f;
+  for (int64_t k = lane; k < d; k += 32) {
+    float v = __ldg(x + row * d + k);
+    s = fmaf(v, v, s);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) cov[row] = s * inv_d;
+}
+
+// ---------------------------------------------------------------------------
+// Full-spatial input covariance: out[b, a, a', c, c'] = sum_k x1[a,c,k] x2[a',c',k] / K
+// One CTA per (b, a) row; loops over a'.
+// ---------------------------------------------------------------------------
+__global__ void input_fs_kernel(const float* __restrict__ x1, const float* __restrict__ x2,
+                                int64_t batch, int64_t n2, int64_t A, int64_t C, int64_t K,
+                                float inv_k, float* __restrict__ out) {
+  int64_t blk = blockIdx.x;
+  int64_t b = blk / A, a = blk - b * A;
+  if (b >= batch) return;
+  int64_t i1, i2;
+  pair_of(b, n2, i1, i2);
+  const float* r1 = x1 + ((i1 * A + a) * C) * K;
+  const float* img2 = x2 + i2 * A * C * K;
+  float* o = out + ((b * A + a) * A) * C * C;
+  int64_t plane = C * C;
+  for (int64_t idx = threadIdx.x; idx < A * plane; idx += blockDim.x) {
+    int64_t ap = idx / plane, rem = idx - ap * plane;
+    int64_t c = rem / C, cp = rem - c * C;
+    const float* p1 = r1 + c * K;
+    const float* p2 = img2 + (ap * C + cp) * K;
+    float s = 0.f;
+    for (int64_t k = 0; k < K; ++k) s = fmaf(__ldg(p1 + k), __ldg(p2 + k), s);
+    o[idx] = s * inv_k;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// General full-spatial conv rule: one thread per output entry.
+// ---------------------------------------------------------------------------
+struct ConvGeom {
+  int64_t batch, n2, A, C, Ao, Co;
+  int fh, fw, sh, sw, ph, pw, circular;
+};
+
+__device__ __forceinline__ bool wrap_index(int64_t& i, int64_t n, int circular) {
+  if (i >= 0 && i < n) return true;
+  if (!circular) return false;
+  i %= n;
+  if (i < 0) i += n;
+  return true;
+}
+
+__global__ void conv_fs_general_kernel(const float* __restrict__ in_q,
+                                       const float* __restrict__ in_t, float* __restrict__ out_q,
+                                       float* __restrict__ out_t, ConvGeom g, ntg_affine_t aff,
+                                       ntg_act_t act, ntg_var_t var1, ntg_var_t var2) {
+  const int64_t plane_o = g.Co * g.Co;
+  const int64_t per_b = g.Ao * g.Ao * plane_o;
+  const int64_t total = g.batch * per_b;
+  const float inv = 1.f / (float)(g.fh * g.fw);
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b = idx / per_b, r = idx - b * per_b;
+    int64_t i = r / (g.Ao * plane_o);
+    r -= i * g.Ao * plane_o;
+    int64_t ip = r / plane_o;
+    r -= ip * plane_o;
+    int64_t j = r / g.Co, jp = r - j * g.Co;
+    const float* bq = in_q + b * g.A * g.A * g.C * g.C;
+    const float* bt = in_t ? in_t + b * g.A * g.A * g.C * g.C : nullptr;
+    float sq = 0.f, st = 0.f;
+    for (int d = 0; d < g.fh; ++d) {
+      int64_t ia = i * g.sh + d - g.ph, iap = ip * g.sh + d - g.ph;
+      if (!wrap_index(ia, g.A, g.circular) || !wrap_index(iap, g.A, g.circular)) continue;
+      for (int e = 0; e < g.fw; ++e) {
+        int64_t jc = j * g.sw + e - g.pw, jcp = jp * g.sw + e - g.pw;
+        if (!wrap_index(jc, g.C, g.circular) || !wrap_index(jcp, g.C, g.circular)) continue;
+        int64_t off = ((ia * g.A + iap) * g.C + jc) * g.C + jcp;
+        sq += __ldg(bq + off);
+        if (bt) st += __ldg(bt + off);
+      }
+    }
+    float q, t = 0.f;
+    apply_affine(aff, sq * inv, st * inv, out_t != nullptr, q, t);
+    if (act.kind != NTG_ACT_NONE) {
+      int64_t i1, i2;
+      pair_of(b, g.n2, i1, i2);
+      float v1 = var_at(var1, i1, i, j), v2 = var_at(var2, i2, ip, jp);
+      apply_act(act, q, t, v1, v2);
+    }
+    out_q[idx] = q;
+    if (out_t) out_t[idx] = t;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 3x3 / stride 1 / SAME / zero-padding conv rule streamed along the spatial
+// diagonals of the (A, A') plane grid.  Output plane (i, i+delta) needs input
+// planes (i-1, i-1+delta), (i, i+delta), (i+1, i+1+delta): every input plane
+// of a diagonal line is read once, the 3-plane A-direction sum stays in
+// registers, and the C-direction diagonal sum goes through a zero-haloed
+// shared-memory tile.  C*C <= 1024 entries per plane, 4 per thread.
+// FROM_X computes the input planes from the NHWC images (first-layer Gram).
+// ---------------------------------------------------------------------------
+template <bool FROM_X, bool HAS_T>
+__global__ void __launch_bounds__(kThreads)
+    conv3_line_kernel(const float* __restrict__ in_q, const float* __restrict__ in_t,
+                      const float* __restrict__ x1, const float* __restrict__ x2, int64_t K,
+                      float inv_k, float* __restrict__ out_q, float* __restrict__ out_t,
+                      int64_t batch, int64_t n2, int A, int C, ntg_affine_t aff, ntg_act_t act,
+                      ntg_var_t var1, ntg_var_t var2) {
+  extern __shared__ float smem[];
+  const int P = C + 2;                 // haloed row pitch
+  float* hq[2] = {smem, smem + P * P};  // double-buffered A-sums
+  float* ht[2] = {smem + 2 * P * P, smem + 3 * P * P};
+  const int nlines = 2 * A - 1;
+  const int64_t b = blockIdx.x / nlines;
+  const int delta = (int)(blockIdx.x - b * nlines) - (A - 1);
+  if (b >= batch) return;
+  const int i_lo = delta < 0 ? -delta : 0;
+  const int i_hi = delta < 0 ? A : A - delta;
+  const int plane = C * C;
+  const int64_t pair_stride = (int64_t)A * A * plane;
+
+  for (int idx = threadIdx.x; idx < 4 * P * P; idx += blockDim.x) smem[idx] = 0.f;
+
+  int64_t i1, i2;
+  pair_of(b, n2, i1, i2);
+  const int e0 = threadIdx.x * 4;
+  const bool active = e0 < plane;
+  const int c = active ? e0 / C : 0;
+  const int cp0 = active ? e0 - c * C : 0;
+
+  // Loads input plane at line position i (zero outside the line).
+  auto load = [&](int i, float (&q)[4], float (&t)[4]) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) q[u] = t[u] = 0.f;
+    if (!active || i < i_lo || i >= i_hi) return;
+    if (FROM_X) {
+      const float* p1 = x1 + (((i1 * A + i) * C + c) * K);
+      const float* p2 = x2 + (((i2 * A + i + delta) * C + cp0) * K);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        float s = 0.f;
+        for (int64_t k = 0; k < K; ++k) s = fmaf(__ldg(p1 + k), __ldg(p2 + u * K + k), s);
+        q[u] = s * inv_k;
+      }
+    } else {
+      int64_t off = b * pair_stride + ((int64_t)i * A + i + delta) * plane + e0;
+      float4 v = __ldg(reinterpret_cast<const float4*>(in_q + off));
+      q[0] = v.x; q[1] = v.y; q[2] = v.z; q[3] = v.w;
+      if (HAS_T) {
+        float4 w = __ldg(reinterpret_cast<const float4*>(in_t + off));
+        t[0] = w.x; t[1] = w.y; t[2] = w.z; t[3] = w.w;
+      }
+    }
+  };
+
+  float qm[4], tm[4], q0[4], t0[4], qp[4], tp[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) qm[u] = tm[u] = 0.f;
+  load(i_lo, q0, t0);
+  __syncthreads();
+  const float inv9 = 1.f / 9.f;
+  int buf = 0;
+  for (int i = i_lo; i < i_hi; ++i) {
+    load(i + 1, qp, tp);
+    if (active) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        int o = (c + 1) * P + (cp0 + u + 1);
+        hq[buf][o] = (qm[u] + q0[u]) + qp[u];
+        if (HAS_T) ht[buf][o] = (tm[u] + t0[u]) + tp[u];
+      }
+    }
+    __syncthreads();
+    if (active) {
+      float vq[4], vt[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        int o = (c + 1) * P + (cp0 + u + 1);
+        float sq = (hq[buf][o - P - 1] + hq[buf][o]) + hq[buf][o + P + 1];
+        float st = HAS_T ? (ht[buf][o - P - 1] + ht[buf][o]) + ht[buf][o + P + 1] : 0.f;
+        float q, t = 0.f;
+        apply_affine(aff, sq * inv9, st * inv9, out_t != nullptr, q, t);
+        if (act.kind != NTG_ACT_NONE) {
+          float v1 = var_at(var1, i1, i, c), v2 = var_at(var2, i2, i + delta, cp0 + u);
+          apply_act(act, q, t, v1, v2);
+        }
+        vq[u] = q;
+        vt[u] = t;
+      }
+      int64_t off = b * pair_stride + ((int64_t)i * A + i + delta) * plane + e0;
+      *reinterpret_cast<float4*>(out_q + off) = make_float4(vq[0], vq[1], vq[2], vq[3]);
+      if (out_t) *reinterpret_cast<float4*>(out_t + off) = make_float4(vt[0], vt[1], vt[2], vt[3]);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      qm[u] = q0[u]; tm[u] = t0[u];
+      q0[u] = qp[u]; t0[u] = tp[u];
+    }
+    buf ^= 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Diagonal-spatial conv rule: [B, A, C] box filter (linear.py:3381-3437).
+// ---------------------------------------------------------------------------
+__global__ void conv_ds_kernel(const float* __restrict__ in_q, const float* __restrict__ in_t,
+                               float* __restrict__ out_q, float* __restrict__ out_t, ConvGeom g,
+                               ntg_affine_t aff) {
+  const int64_t per_b = g.Ao * g.Co;
+  const int64_t total = g.batch * per_b;
+  const float inv = 1.f / (float)(g.fh * g.fw);
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b = idx / per_b, r = idx - b * per_b;
+    int64_t i = r / g.Co, j = r - i * g.Co;
+    float sq = 0.f, st = 0.f;
+    for (int d = 0; d < g.fh; ++d) {
+      int64_t ia = i * g.sh + d - g.ph;
+      if (!wrap_index(ia, g.A, g.circular)) continue;
+      for (int e = 0; e < g.fw; ++e) {
+        int64_t jc = j * g.sw + e - g.pw;
+        if (!wrap_index(jc, g.C, g.circular)) continue;
+        int64_t off = (b * g.A + ia) * g.C + jc;
+        sq += __ldg(in_q + off);
+        if (in_t) st += __ldg(in_t + off);
+      }
+    }
+    float q, t = 0.f;
+    apply_affine(aff, sq * inv, st * inv, out_t != nullptr, q, t);
+    out_q[idx] = q;
+    if (out_t) out_t[idx] = t;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Elementwise affine + activation on [B, M].
+// ---------------------------------------------------------------------------
+__global__ void affine_act_kernel(const float* __restrict__ in_q, const float* __restrict__ in_t,
+                                  float* __restrict__ out_q, float* __restrict__ out_t,
+                                  int64_t batch, int64_t n2, int64_t A, int64_t C, int diag,
+                                  int has_affine, ntg_affine_t aff, ntg_act_t act,
+                                  ntg_var_t var1, ntg_var_t var2) {
+  const int64_t M = diag ? A * C : A * A * C * C;
+  const int64_t total = batch * M;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b = idx / M, m = idx - b * M;
+    float q = in_q[idx];
+    float t = in_t ? in_t[idx] : 0.f;
+    if (has_affine) {
+      float q2, t2 = 0.f;
+      apply_affine(aff, q, t, out_t != nullptr, q2, t2);
+      q = q2;
+      t = t2;
+    }
+    if (act.kind != NTG_ACT_NONE) {
+      int64_t a1, a2, c1, c2;
+      if (diag) {
+        a1 = a2 = m / C;
+        c1 = c2 = m - a1 * C;
+      } else {
+        int64_t r = m;
+        c2 = r % C; r /= C;
+        c1 = r % C; r /= C;
+        a2 = r % A;
+        a1 = r / A;
+      }
+      int64_t i1, i2;
+      pair_of(b, n2, i1, i2);
+      apply_act(act, q, t, var_at(var1, i1, a1, c1), var_at(var2, i2, a2, c2));
+    }
+    out_q[idx] = q;
+    if (out_t) out_t[idx] = t;
+  }
+}
+
+__global__ void max_abs_kernel(const float* __restrict__ x, int64_t n, unsigned int* out) {
+  float m = 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(x[i]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+// ---------------------------------------------------------------------------
+// Pooling (reduce_window sum over the doubled window) and readouts.
+// ---------------------------------------------------------------------------
+struct PoolGeom {
+  int64_t batch, A, C, Ao, Co;
+  int wa, wc, sa, sc, pa, pc, circular, diag, average, normalize_edges;
+};
+
+__global__ void pool_kernel(const float* __restrict__ in, float* __restrict__ out, PoolGeom g) {
+  const int64_t per_b = g.diag ? g.Ao * g.Co : g.Ao * g.Ao * g.Co * g.Co;
+  const int64_t in_b = g.diag ? g.A * g.C : g.A * g.A * g.C * g.C;
+  const int64_t total = g.batch * per_b;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b = idx / per_b, r = idx - b * per_b;
+    const float* src = in + b * in_b;
+    float s = 0.f;
+    int count = 0;
+    if (g.diag) {
+      int64_t i = r / g.Co, j = r - i * g.Co;
+      for (int u = 0; u < g.wa; ++u) {
+        int64_t ia = i * g.sa + u - g.pa;
+        if (!wrap_index(ia, g.A, g.circular)) continue;
+        for (int v = 0; v < g.wc; ++v) {
+          int64_t jc = j * g.sc + v - g.pc;
+          if (!wrap_index(jc, g.C, g.circular)) continue;
+          s += __ldg(src + ia * g.C + jc);
+          ++count;
+        }
+      }
+    } else {
+      int64_t jp = r % g.Co; r /= g.Co;
+      int64_t j = r % g.Co; r /= g.Co;
+      int64_t ip = r % g.Ao;
+      int64_t i = r / g.Ao;
+      for (int u = 0; u < g.wa; ++u) {
+        int64_t ia = i * g.sa + u - g.pa;
+        if (!wrap_index(ia, g.A, g.circular)) continue;
+        for (int up = 0; up < g.wa; ++up) {
+          int64_t iap = ip * g.sa + up - g.pa;
+          if (!wrap_index(iap, g.A, g.circular)) continue;
+          for (int v = 0; v < g.wc; ++v) {
+            int64_t jc = j * g.sc + v - g.pc;
+            if (!wrap_index(jc, g.C, g.circular)) continue;
+            const float* row = src + ((ia * g.A + iap) * g.C + jc) * g.C;
+            for (int vp = 0; vp < g.wc; ++vp) {
+              int64_t jcp = jp * g.sc + vp - g.pc;
+              if (!wrap_index(jcp, g.C, g.circular)) continue;
+              s += __ldg(row + jcp);
+              ++count;
+            }
+          }
+        }
+      }
+    }
+    if (g.average) {
+      float norm;
+      if (g.normalize_edges) {
+        norm = (float)count;
+      } else {
+        norm = g.diag ? (float)(g.wa * g.wc) : (float)(g.wa * g.wa * g.wc * g.wc);
+      }
+      s = s / norm;
+      if (g.diag) s = s / norm;
+    }
+    out[idx] = s;
+  }
+}
+
+__global__ void global_pool_kernel(const float* __restrict__ in, float* __restrict__ out,
+                                   int64_t m, int average, float post_scale) {
+  const float* row = in + (int64_t)blockIdx.x * m;
+  float s = 0.f;
+  for (int64_t k = threadIdx.x; k < m; k += blockDim.x) s += __ldg(row + k);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ float part[32];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) {
+      if (average) s = s / (float)m;
+      out[blockIdx.x] = s * post_scale;
+    }
+  }
+}
+
+__global__ void flatten_fs_kernel(const float* __restrict__ in, float* __restrict__ out,
+                                  int64_t A, int64_t C) {
+  const float* src = in + (int64_t)blockIdx.x * A * A * C * C;
+  float s = 0.f;
+  for (int64_t k = threadIdx.x; k < A * C; k += blockDim.x) {
+    int64_t a = k / C, c = k - a * C;
+    s += __ldg(src + ((a * A + a) * C + c) * C + c);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  __shared__ float part[32];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) out[blockIdx.x] = s / (float)(A * C);
+  }
+}
+
+int grid_for(int64_t total, int threads = kThreads) {
+  int64_t g = ceil_div(total, threads);
+  if (g > (int64_t)152 * 64) g = (int64_t)152 * 64;
+  return (int)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+}  // namespace ntg
+
+using namespace ntg;
+
+extern "C" int ntg_gram(void* stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
+                        int64_t d, float* nngp, int32_t precision) {
+  NTG_REQUIRE(x1 && x2 && nngp, "ntg_gram: null pointer");
+  NTG_REQUIRE(n1 > 0 && n2 > 0 && d > 0, "ntg_gram: sizes must be positive");
+  if (precision == 1) {
+    return gram_tc(as_stream(stream), x1, x2, n1, n2, d, nngp);
+  }
+  NTG_REQUIRE(precision == 0, "ntg_gram: precision must be 0 or 1");
+  NTG_REQUIRE(ceil_div(n1, 64) <= 65535, "ntg_gram: n1 too large");
+  dim3 grid((unsigned)ceil_div(n2, 64), (unsigned)ceil_div(n1, 64));
+  gram_simt_kernel<<<grid, 256, 0, as_stream(stream)>>>(x1, x2, n1, n2, d, 1.f / (float)d, nngp);
+  note_launch();
+  return check_launch("ntg_gram");
+}
+
+extern "C" int ntg_cov_diag(void* stream, const float* x, int64_t n, int64_t d, float* cov) {
+  NTG_REQUIRE(x && cov, "ntg_cov_diag: null pointer");
+  NTG_REQUIRE(n > 0 && d > 0, "ntg_cov_diag: sizes must be positive");
+  cov_diag_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, as_stream(stream)>>>(x, n, d,
+                                                                           1.f / (float)d, cov);
+  note_launch();
+  return check_launch("ntg_cov_diag");
+}
+
+extern "C" int ntg_input_fs(void* stream, const float* x1, const float* x2, int64_t n1,
+                            int64_t n2, int64_t a, int64_t c, int64_t k, int32_t pairs,
+                            float* out) {
+  NTG_REQUIRE(x1 && out, "ntg_input_fs: null pointer");
+  NTG_REQUIRE(n1 > 0 && a > 0 && c > 0 && k > 0, "ntg_input_fs: sizes must be positive");
+  int64_t batch = pairs ? n1 * n2 : n1;
+  NTG_REQUIRE(!pairs || (x2 && n2 > 0), "ntg_input_fs: pairs mode needs x2 and n2 > 0");
+  const float* xb = pairs ? x2 : x1;
+  int64_t blocks = batch * a;
+  NTG_REQUIRE(blocks < (1ll << 31), "ntg_input_fs: grid too large");
+  input_fs_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(
+      x1, xb, batch, pairs ? n2 : 0, a, c, k, 1.f / (float)k, out);
+  note_launch();
+  return check_launch("ntg_input_fs");
+}
+
+extern "C" int ntg_conv_fs(void* stream, const float* in_q, const float* in_t, float* out_q,
+                           float* out_t, int64_t batch, int64_t n2, int64_t a, int64_t c,
+                           int32_t fh, int32_t fw, int32_t sh, int32_t sw, int32_t ph, int32_t pw,
+                           int64_t ao, int64_t co, int32_t pad_mode, ntg_affine_t aff,
+                           ntg_act_t act, ntg_var_t var1, ntg_var_t var2) {
+  NTG_REQUIRE(in_q && out_q, "ntg_conv_fs: null pointer");
+  NTG_REQUIRE(batch > 0 && a > 0 && c > 0 && ao > 0 && co > 0, "ntg_conv_fs: bad sizes");
+  NTG_REQUIRE(fh > 0 && fw > 0 && sh > 0 && sw > 0 && ph >= 0 && pw >= 0,
+              "ntg_conv_fs: bad filter geometry");
+  NTG_REQUIRE(act.kind == NTG_ACT_NONE || (var1.base && var2.base),
+              "ntg_conv_fs: activation needs var1/var2");
+  cudaStream_t s = as_stream(stream);
+  const bool line_ok = fh == 3 && fw == 3 && sh == 1 && sw == 1 && ph == 1 && pw == 1 &&
+                       ao == a && co == c && pad_mode == NTG_PAD_ZERO && c % 4 == 0 &&
+                       c * c <= 4 * kThreads && a <= 4096;
+  if (line_ok) {
+    int64_t blocks = batch * (2 * a - 1);
+    NTG_REQUIRE(blocks < (1ll << 31), "ntg_conv_fs: grid too large");
+    size_t sm = sizeof(float) * 4 * (c + 2) * (c + 2);
+    if (in_t)
+      conv3_line_kernel<false, true><<<(unsigned)blocks, kThreads, sm, s>>>(
+          in_q, in_t, nullptr, nullptr, 0, 0.f, out_q, out_t, batch, n2, (int)a, (int)c, aff, act,
+          var1, var2);
+    else
+      conv3_line_kernel<false, false><<<(unsigned)blocks, kThreads, sm, s>>>(
+          in_q, nullptr, nullptr, nullptr, 0, 0.f, out_q, out_t, batch, n2, (int)a, (int)c, aff,
+          act, var1, var2);
+  } else {
+    ConvGeom g{batch, n2, a, c, ao, co, fh, fw, sh, sw, ph, pw, pad_mode == NTG_PAD_CIRCULAR};
+    int64_t total = batch * ao * ao * co * co;
+    conv_fs_general_kernel<<<grid_for(total), kThreads, 0, s>>>(in_q, in_t, out_q, out_t, g, aff,
+                                                                 act, var1, var2);
+  }
+  note_launch();
+  return check_launch("ntg_conv_fs");
+}
+
+extern "C" int ntg_conv_input_fs(void* stream, const float* x1, const float* x2, int64_t n1,
+                                 int64_t n2, int64_t a, int64_t c, int64_t k, float* out_q,
+                                 float* out_t, ntg_affine_t aff, ntg_act_t act, ntg_var_t var1,
+                                 ntg_var_t var2) {
+  NTG_REQUIRE(x1 && x2 && out_q, "ntg_conv_input_fs: null pointer");
+  NTG_REQUIRE(n1 > 0 && n2 > 0 && a > 0 && c > 0 && k > 0, "ntg_conv_input_fs: bad sizes");
+  NTG_REQUIRE(c % 4 == 0 && c * c <= 4 * kThreads, "ntg_conv_input_fs: needs C % 4 == 0, C <= 32");
+  NTG_REQUIRE(act.kind == NTG_ACT_NONE || (var1.base && var2.base),
+              "ntg_conv_input_fs: activation needs var1/var2");
+  int64_t batch = n1 * n2;
+  int64_t blocks = batch * (2 * a - 1);
+  NTG_REQUIRE(blocks < (1ll << 31), "ntg_conv_input_fs: grid too large");
+  size_t sm = sizeof(float) * 4 * (c + 2) * (c + 2);
+  conv3_line_kernel<true, false><<<(unsigned)blocks, kThreads, sm, as_stream(stream)>>>(
+      nullptr, nullptr, x1, x2, k, 1.f / (float)k, out_q, out_t, batch, n2, (int)a, (int)c, aff,
+      act, var1, var2);
+  note_launch();
+  return check_launch("ntg_conv_input_fs");
+}
+
+extern "C" int ntg_conv_ds(void* stream, const float* in_q, const float* in_t, float* out_q,
+                           float* out_t, int64_t batch, int64_t a, int64_t c, int32_t fh,
+                           int32_t fw, int32_t sh, int32_t sw, int32_t ph, int32_t pw, int64_t ao,
+                           int64_t co, int32_t pad_mode, ntg_affine_t aff) {
+  NTG_REQUIRE(in_q && out_q, "ntg_conv_ds: null pointer");
+  NTG_REQUIRE(batch > 0 && a > 0 && c > 0 && ao > 0 && co > 0, "ntg_conv_ds: bad sizes");
+  ConvGeom g{batch, 0, a, c, ao, co, fh, fw, sh, sw, ph, pw, pad_mode == NTG_PAD_CIRCULAR};
+  conv_ds_kernel<<<grid_for(batch * ao * co), kThreads, 0, as_stream(stream)>>>(in_q, in_t, out_q,
+                                                                              out_t, g, aff);
+  note_launch();
+  return check_launch("ntg_conv_ds");
+}
+
+extern "C" int ntg_affine_act(void* stream, const float* in_q, const float* in_t, float* out_q,
+                              float* out_t, int64_t batch, int64_t n2, int64_t a, int64_t c,
+                              int32_t diag_spatial, int32_t has_affine, ntg_affine_t aff,
+                              ntg_act_t act, ntg_var_t var1, ntg_var_t var2) {
+  NTG_REQUIRE(in_q && out_q, "ntg_affine_act: null pointer");
+  NTG_REQUIRE(batch > 0 && a > 0 && c > 0, "ntg_affine_act: bad sizes");
+  NTG_REQUIRE(act.kind == NTG_ACT_NONE || (var1.base && var2.base),
+              "ntg_affine_act: activation needs var1/var2");
+  int64_t m = diag_spatial ? a * c : a * a * c * c;
+  affine_act_kernel<<<grid_for(batch * m), kThreads, 0, as_stream(stream)>>>(
+      in_q, in_t, out_q, out_t, batch, n2, a, c, diag_spatial, has_affine, aff, act, var1, var2);
+  note_launch();
+  return check_launch("ntg_affine_act");
+}
+
+extern "C" int ntg_max_abs(void* stream, const float* x, int64_t n, float* out) {
+  NTG_REQUIRE(x && out && n > 0, "ntg_max_abs: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  if (cudaMemsetAsync(out, 0, sizeof(float), s) != cudaSuccess)
+    return check_launch("ntg_max_abs memset");
+  max_abs_kernel<<<grid_for(n), kThreads, 0, s>>>(x, n, reinterpret_cast<unsigned int*>(out));
+  note_launch();
+  return check_launch("ntg_max_abs");
+}
+
+extern "C" int ntg_pool(void* stream, const float* in, float* out, int64_t batch, int64_t a,
+                        int64_t c, int32_t wa, int32_t wc, int32_t sa, int32_t sc, int32_t pa,
+                        int32_t pc, int64_t ao, int64_t co, int32_t pad_mode,
+                        int32_t diag_spatial, int32_t average, int32_t normalize_edges) {
+  NTG_REQUIRE(in && out, "ntg_pool: null pointer");
+  NTG_REQUIRE(batch > 0 && a > 0 && c > 0 && ao > 0 && co > 0, "ntg_pool: bad sizes");
+  NTG_REQUIRE(wa > 0 && wc > 0 && sa > 0 && sc > 0 && pa >= 0 && pc >= 0, "ntg_pool: bad window");
+  PoolGeom g{batch, a, c, ao, co, wa, wc, sa, sc, pa, pc, pad_mode == NTG_PAD_CIRCULAR,
+             diag_spatial, average, normalize_edges};
+  int64_t total = diag_spatial ? batch * ao * co : batch * ao * ao * co * co;
+  pool_kernel<<<grid_for(total), kThreads, 0, as_stream(stream)>>>(in, out, g);
+  note_launch();
+  return check_launch("ntg_pool");
+}
+
+extern "C" int ntg_global_pool(void* stream, const float* in, float* out, int64_t batch,
+                               int64_t m, int32_t average, float post_scale) {
+  NTG_REQUIRE(in && out && batch > 0 && m > 0, "ntg_global_pool: bad arguments");
+  NTG_REQUIRE(batch < (1ll << 31), "ntg_global_pool: batch too large");
+  global_pool_kernel<<<(unsigned)batch, kThreads, 0, as_stream(stream)>>>(in, out, m, average,
+                                                                          post_scale);
+  note_launch();
+  return check_launch("ntg_global_pool");
+}
+
+extern "C" int ntg_flatten_fs(void* stream, const float* in, float* out, int64_t batch,
+                              int64_t a, int64_t c) {
+  NTG_REQUIRE(in && out && batch > 0 && a > 0 && c > 0, "ntg_flatten_fs: bad arguments");
+  NTG_REQUIRE(batch < (1ll << 31), "ntg_flatten_fs: batch too large");
+  flatten_fs_kernel<<<(unsigned)batch, kThreads, 0, as_stream(stream)>>>(in, out, a, c);
+  note_launch();
+  return check_launch("ntg_flatten_fs");
+}

@@ -1,0 +1,239 @@
+"""GPU parity: the sm_103a kernels against the float64 oracle on the same inputs.
+
+Tolerance: the plain-FP32 path must match the float64 oracle within a
+relative error of 1e-5 on readout kernels ([N1, N2] outputs) and within
+1e-5 of the largest entry on full spatial kernels.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import nt_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+
+
+def rel_err(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-30))
+
+
+def elem_rel_err(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-30)))
+
+
+def cpu(t):
+    return t.detach().cpu().numpy() if isinstance(t, torch.Tensor) else np.asarray(t)
+
+
+def both(nt, layers_fn, x1, x2, get=('nngp', 'ntk', 'cov1', 'cov2'), **kw):
+    s = nt.stax
+    _, _, kf = s.serial(*layers_fn(s))
+    ko = o.serial(*layers_fn(o))
+    got = kf(x1, x2, get, **kw)
+    want = ko(x1, x2, get)
+    return [cpu(g) for g in got], list(want)
+
+
+def fcn_layers(m):
+    return [m.Dense(512, W_std=1.5, b_std=0.05), m.Relu(), m.Dense(512, W_std=1.5, b_std=0.05),
+            m.Relu(), m.Dense(1, W_std=1.5, b_std=0.05)]
+
+
+def normalized_rows(rng, n, d):
+    x = rng.standard_normal((n, d)).astype(np.float32)
+    return (x / np.linalg.norm(x, axis=1, keepdims=True) * math.sqrt(d)).astype(np.float32)
+
+
+def test_fcn_config(nt):
+    rng0, rng1 = np.random.default_rng(0), np.random.default_rng(1)
+    x1, x2 = normalized_rows(rng0, 64, 784), normalized_rows(rng1, 48, 784)
+    got, want = both(nt, fcn_layers, x1, x2)
+    for g, w in zip(got, want):
+        assert elem_rel_err(g, w) < RTOL
+
+
+def test_fcn_erf_and_abrelu(nt):
+    rng = np.random.default_rng(2)
+    x1, x2 = rng.standard_normal((16, 20)), rng.standard_normal((12, 20))
+    lay = lambda m: [m.Dense(3, 1.3, 0.2), m.Erf(0.7, 1.2, 0.1), m.Dense(3, 0.9, 0.3),
+                     m.ABRelu(-0.3, 1.1), m.Dense(1, 1.1)]
+    got, want = both(nt, lay, x1, x2)
+    for g, w in zip(got, want):
+        assert elem_rel_err(g, w) < RTOL
+    got, want = both(nt, lay, x1, None, get=('nngp', 'ntk', 'cov1'))
+    for g, w in zip(got, want):
+        assert elem_rel_err(g, w) < RTOL
+
+
+CONV_CASES = [
+    dict(filter_shape=(3, 3), padding='SAME'),
+    dict(filter_shape=(3, 3), padding='VALID'),
+    dict(filter_shape=(2, 3), strides=(2, 1), padding='SAME'),
+    dict(filter_shape=(3, 2), padding='CIRCULAR'),
+]
+
+
+@pytest.mark.parametrize('case', CONV_CASES)
+def test_conv_relu_full_spatial(nt, case):
+    rng = np.random.default_rng(3)
+    x1, x2 = rng.standard_normal((2, 8, 8, 3)), rng.standard_normal((3, 8, 8, 3))
+    lay = lambda m: [m.Conv(4, W_std=1.4, b_std=0.1, **case), m.Relu(),
+                     m.Conv(4, W_std=1.2, b_std=0.05, **case)]
+    got, want = both(nt, lay, x1, x2)
+    for g, w in zip(got, want):
+        assert g.shape == w.shape
+        assert rel_err(g, w) < RTOL
+
+
+def test_conv_nonsquare_reversal_layout(nt):
+    rng = np.random.default_rng(4)
+    x1, x2 = rng.standard_normal((2, 6, 4, 2)), rng.standard_normal((2, 6, 4, 2))
+    lay = lambda m: [m.Conv(2, (3, 3), padding='SAME', W_std=1.1), m.Relu()]
+    s = nt.stax
+    k = s.serial(*lay(s))[2](x1, x2)
+    ko = o.serial(*lay(o))(x1, x2)
+    assert k.is_reversed == ko.is_reversed is True
+    assert tuple(k.nngp.shape) == ko.nngp.shape == (2, 2, 4, 4, 6, 6)
+    assert rel_err(cpu(k.nngp), ko.nngp) < RTOL
+
+
+@pytest.mark.parametrize('pool', ['avg_same_norm', 'avg_same', 'sum_valid', 'avg_valid'])
+def test_pools(nt, pool):
+    rng = np.random.default_rng(5)
+    x1, x2 = rng.standard_normal((2, 7, 6, 2)), rng.standard_normal((2, 7, 6, 2))
+    mk = {
+        'avg_same_norm': lambda m: m.AvgPool((2, 3), (1, 2), 'SAME', normalize_edges=True),
+        'avg_same': lambda m: m.AvgPool((2, 2), (2, 2), 'SAME'),
+        'sum_valid': lambda m: m.SumPool((2, 2), (1, 1), 'VALID'),
+        'avg_valid': lambda m: m.AvgPool((3, 2), (2, 2), 'VALID'),
+    }[pool]
+    lay = lambda m: [m.Conv(2, (3, 3), padding='SAME', W_std=1.2, b_std=0.1), m.Relu(), mk(m),
+                     m.Conv(2, (3, 3), padding='SAME', W_std=1.1)]
+    got, want = both(nt, lay, x1, x2)
+    for g, w in zip(got, want):
+        assert rel_err(g, w) < RTOL
+
+
+@pytest.mark.parametrize('readout', ['flatten', 'gap', 'gsp'])
+def test_readouts(nt, readout):
+    rng = np.random.default_rng(6)
+    x1, x2 = rng.standard_normal((3, 6, 6, 3)), rng.standard_normal((2, 6, 6, 3))
+    ro = {'flatten': lambda m: m.Flatten(), 'gap': lambda m: m.GlobalAvgPool(),
+          'gsp': lambda m: m.GlobalSumPool()}[readout]
+    lay = lambda m: [m.Conv(2, (3, 3), padding='SAME', W_std=1.3, b_std=0.2), m.Relu(), ro(m),
+                     m.Dense(1, 1.1, 0.1)]
+    got, want = both(nt, lay, x1, x2)
+    for g, w in zip(got, want):
+        assert elem_rel_err(g, w) < RTOL
+
+
+def test_diagonal_spatial_network(nt):
+    rng = np.random.default_rng(7)
+    x1, x2 = rng.standard_normal((3, 6, 5, 2)), rng.standard_normal((2, 6, 5, 2))
+    lay = lambda m: [m.Conv(2, (3, 3), padding='SAME', W_std=1.3, b_std=0.2), m.Erf(),
+                     m.Conv(2, (3, 3), padding='SAME', W_std=1.1), m.Relu(), m.Flatten(),
+                     m.Dense(1, 1.2)]
+    s = nt.stax
+    assert bool(s.serial(*lay(s))[2].diagonal)
+    got, want = both(nt, lay, x1, x2)
+    for g, w in zip(got, want):
+        assert elem_rel_err(g, w) < RTOL
+
+
+def test_one_spatial_dim(nt):
+    rng = np.random.default_rng(8)
+    x1, x2 = rng.standard_normal((2, 9, 3)), rng.standard_normal((3, 9, 3))
+    lay = lambda m: [m.Conv(2, (3,), padding='SAME', W_std=1.3, b_std=0.2), m.Relu(),
+                     m.AvgPool((2,), (2,)), m.Conv(2, (2,), padding='VALID', W_std=1.1)]
+    got, want = both(nt, lay, x1, x2)
+    for g, w in zip(got, want):
+        assert rel_err(g, w) < RTOL
+
+
+def myrtle(m, depth, readout='flatten'):
+    f = {5: [2, 1, 1], 7: [2, 2, 2], 10: [3, 3, 3]}[depth]
+    conv = lambda: m.Conv(1, (3, 3), padding='SAME', W_std=math.sqrt(2.), b_std=0.)
+    L = []
+    for _ in range(f[0]):
+        L += [conv(), m.Relu()]
+    L += [m.AvgPool((2, 2), (2, 2))]
+    for _ in range(f[1]):
+        L += [conv(), m.Relu()]
+    L += [m.AvgPool((2, 2), (2, 2))]
+    for _ in range(f[2]):
+        L += [conv(), m.Relu()]
+    if readout == 'flatten':
+        L += [m.AvgPool((2, 2), (2, 2))] * 3 + [m.Flatten(), m.Dense(10, math.sqrt(2.), 0.)]
+    else:
+        L += [m.GlobalAvgPool(), m.Dense(10, math.sqrt(2.), 0.)]
+    return L
+
+
+@pytest.fixture(scope='module')
+def cifar_like():
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((5, 32, 32, 3)).astype(np.float32)
+    x = (x - x.mean(axis=(0, 1, 2))) / x.std(axis=(0, 1, 2))
+    return x[:3], x[3:]
+
+
+def test_myrtle5_fused_chain_vs_oracle(nt, cifar_like):
+    x1, x2 = cifar_like
+    got, want = both(nt, lambda m: myrtle(m, 5), x1, x2)
+    for g, w in zip(got, want):
+        assert elem_rel_err(g, w) < RTOL
+
+
+def test_myrtle5_symmetric_call(nt, cifar_like):
+    x1, _ = cifar_like
+    got, want = both(nt, lambda m: myrtle(m, 5), x1, None, get=('nngp', 'ntk', 'cov1'))
+    for g, w in zip(got, want):
+        assert elem_rel_err(g, w) < RTOL
+    np.testing.assert_allclose(np.diag(got[0]), got[2], rtol=2e-6)
+
+
+def test_fused_chain_matches_layer_by_layer(nt, cifar_like):
+    """The fused kernel and the materialised per-layer kernels agree."""
+    from nt_gb300 import _chain
+    x1, x2 = cifar_like
+    s = nt.stax
+    _, _, kf = s.serial(*myrtle(s, 10, 'gap'))
+    fused = kf(x1, x2, ('nngp', 'ntk'))
+    assert _chain.plan_chain(kf.specs, x1.shape, False) is not None
+    from nt_gb300.stax import _Ctx, _input_kernel, _as_input
+    ctx = _Ctx('fp32')
+    k = _input_kernel(_as_input(x1), _as_input(x2), False, True, False, ctx)
+    k = kf.apply_kernel(k, ctx)
+    assert rel_err(cpu(fused.nngp), cpu(k.nngp)) < 2e-6
+    assert rel_err(cpu(fused.ntk), cpu(k.ntk)) < 2e-6
+
+
+def test_batch_ragged_equals_unbatched(nt, cifar_like):
+    x1, x2 = cifar_like
+    xa = np.concatenate([x1, x2])
+    s = nt.stax
+    _, _, kf = s.serial(s.Conv(1, (3, 3), padding='SAME', W_std=1.5), s.Relu(), s.Flatten(),
+                        s.Dense(1, 1.2, 0.1))
+    full = kf(xa, xa[:4], ('nngp', 'ntk'))
+    bt = nt.batch(kf, batch_size=2)(xa, xa[:4], ('nngp', 'ntk'))
+    np.testing.assert_allclose(cpu(bt.nngp), cpu(full.nngp), rtol=1e-6)
+    np.testing.assert_allclose(cpu(bt.ntk), cpu(full.ntk), rtol=1e-6)
+    _, _, km = s.serial(*myrtle(s, 5))
+    a = km(xa, None, 'ntk')
+    b = nt.batch(km, batch_size=2)(xa, None, 'ntk')
+    np.testing.assert_allclose(cpu(b), cpu(a), rtol=1e-6)
+
+
+def test_activation_needs_gaussian_input(nt):
+    s = nt.stax
+    _, _, kf = s.serial(s.Relu())
+    with pytest.raises(ValueError, match='Gaussian'):
+        kf(np.ones((2, 3)), None)

@@ -1,0 +1,192 @@
+"""Pins the CPU oracle to the reference's own known-answer and identity tests.
+
+The reference (neural-tangents 0.6.6) ships no golden vectors; its tests pin
+the analytic kernels by closed forms and identities. Each test below re-runs
+one of them against the oracle, citing the reference test it restates, plus
+closed forms derived from the mathematics.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import nt_oracle as o
+
+
+def test_avg_pool_all_ones_kat():
+    """tests/stax/stax_test.py:494-539."""
+    X1, X2 = np.ones((4, 2, 3, 2)), np.ones((3, 2, 3, 2))
+    ker = o.serial(o.AvgPool((2, 2), (1, 1), 'SAME', normalize_edges=False))(X1, X2)
+    kn = o.serial(o.AvgPool((2, 2), (1, 1), 'SAME', normalize_edges=True))(X1, X2)
+    np.testing.assert_allclose(kn.nngp, np.ones_like(kn.nngp))
+    np.testing.assert_allclose(kn.cov1, np.ones_like(kn.cov1))
+    np.testing.assert_allclose(kn.cov2, np.ones_like(kn.cov2))
+    out_unnorm = np.array([[1., 1., 0.5], [0.5, 0.5, 0.25]])
+    ku = np.transpose(np.outer(out_unnorm, out_unnorm).reshape(2, 3, 2, 3), (0, 2, 1, 3))
+    np.testing.assert_allclose(ker.nngp, np.broadcast_to(ku[None, None], ker.nngp.shape))
+    np.testing.assert_allclose(ker.cov1, np.broadcast_to(ku[None], ker.cov1.shape))
+    np.testing.assert_allclose(ker.cov2, np.broadcast_to(ku[None], ker.cov2.shape))
+
+
+@pytest.mark.parametrize('same_inputs', [True, False])
+@pytest.mark.parametrize('do_stabilize', [True, False])
+def test_ab_relu_identities(same_inputs, do_stabilize):
+    """tests/stax/elementwise_test.py:541-636."""
+    rng = np.random.default_rng(1)
+    X0_1 = rng.standard_normal((3, 2))
+    X0_2 = None if same_inputs else rng.standard_normal((4, 2))
+    fc = o.Dense(5, 1, 0)
+    relu = o.serial(fc, o.Relu())(X0_1, X0_2)
+    for a, b in [(0, 1), (0, -1), (-1, 0), (1, 0)]:
+        k = o.serial(fc, o.ABRelu(a, b, do_stabilize))(X0_1, X0_2)
+        np.testing.assert_allclose(k.nngp, relu.nngp, rtol=1e-12)
+        np.testing.assert_allclose(k.ntk, relu.ntk, rtol=1e-12)
+    for a in [-5, -1, -0.5, 0, 0.5, 1, 5]:
+        kid = o.serial(fc, o.Identity())(X0_1 * a, None if X0_2 is None else X0_2 * a)
+        kab = o.serial(fc, o.ABRelu(a, a, do_stabilize))(X0_1, X0_2)
+        np.testing.assert_allclose(kab.nngp, kid.nngp, rtol=1e-10, atol=1e-12)
+        np.testing.assert_allclose(kab.cov1, kid.cov1, rtol=1e-10, atol=1e-12)
+    for a in [-2, -1, 0, 1, 2]:
+        kl = o.serial(fc, o.LeakyRelu(a, do_stabilize))(X0_1, X0_2)
+        ka = o.serial(fc, o.ABRelu(a, 1))(X0_1, X0_2)
+        np.testing.assert_allclose(kl.nngp, ka.nngp, rtol=1e-10)
+    np.testing.assert_allclose(o.serial(fc, o.Abs())(X0_1, X0_2).ntk,
+                               o.serial(fc, o.ABRelu(-1, 1))(X0_1, X0_2).ntk, rtol=1e-12)
+
+
+def test_relu_arccos_closed_form():
+    """Cho & Saul degree-1 arc-cosine kernel for Dense(W=1) -> Relu."""
+    rng = np.random.default_rng(3)
+    x1, x2 = rng.standard_normal((5, 7)), rng.standard_normal((4, 7))
+    k = o.serial(o.Dense(3, 1., None), o.Relu())(x1, x2)
+    q11 = np.sum(x1 ** 2, 1) / 7
+    q22 = np.sum(x2 ** 2, 1) / 7
+    q12 = x1 @ x2.T / 7
+    norm = np.sqrt(np.outer(q11, q22))
+    th = np.arccos(np.clip(q12 / norm, -1, 1))
+    nngp = norm / (2 * np.pi) * (np.sin(th) + (np.pi - th) * np.cos(th))
+    np.testing.assert_allclose(k.nngp, nngp, rtol=1e-12)
+    np.testing.assert_allclose(k.ntk, q12 * (np.pi - th) / (2 * np.pi), rtol=1e-12)
+    np.testing.assert_allclose(k.cov1, q11 / 2, rtol=1e-12)
+
+
+def test_erf_arcsine_closed_form():
+    """Williams' arcsine kernel for Dense(W=1) -> Erf."""
+    rng = np.random.default_rng(4)
+    x1, x2 = rng.standard_normal((5, 6)), rng.standard_normal((3, 6))
+    k = o.serial(o.Dense(3, 1., None), o.Erf())(x1, x2)
+    q11 = np.sum(x1 ** 2, 1) / 6
+    q22 = np.sum(x2 ** 2, 1) / 6
+    q12 = x1 @ x2.T / 6
+    nngp = 2 / np.pi * np.arcsin(2 * q12 / np.sqrt(np.outer(1 + 2 * q11, 1 + 2 * q22)))
+    np.testing.assert_allclose(k.nngp, nngp, rtol=1e-12)
+
+
+def test_serial_composition():
+    """tests/stax/stax_test.py:636-687: serial(B, B) == B o B."""
+    rng = np.random.default_rng(5)
+    x1, x2 = rng.standard_normal((2, 8, 8, 3)), rng.standard_normal((3, 8, 8, 3))
+    B = [o.Conv(1, (3, 3), padding='SAME', W_std=1.3, b_std=0.2), o.Relu()]
+    kbb = o.serial(*B, *B)(x1, x2)
+    kb = o.serial(*B)(x1, x2)
+    kb2 = o.serial(*B).apply_to_kernel(kb)
+    np.testing.assert_allclose(kbb.nngp, kb2.nngp, rtol=1e-12)
+    np.testing.assert_allclose(kbb.ntk, kb2.ntk, rtol=1e-12)
+
+
+def _conv_expectation(x1, x2, W_std, b_std, fs=3):
+    """E[f(x1)[h,w] f(x2)[h',w']] of one SAME conv layer, written out directly."""
+    n1, H, W, C = x1.shape
+    n2 = x2.shape[0]
+    p = fs // 2
+    X1 = np.pad(x1, ((0, 0), (p, p), (p, p), (0, 0)))
+    X2 = np.pad(x2, ((0, 0), (p, p), (p, p), (0, 0)))
+    out = np.zeros((n1, n2, H, H, W, W))
+    for h in range(H):
+        for hp in range(H):
+            for w in range(W):
+                for wp in range(W):
+                    acc = 0.
+                    for d in range(fs):
+                        for e in range(fs):
+                            acc = acc + np.einsum('ac,bc->ab', X1[:, h + d, w + e],
+                                                  X2[:, hp + d, wp + e])
+                    out[:, :, h, hp, w, wp] = W_std ** 2 * acc / (C * fs * fs) + b_std ** 2
+    return out
+
+
+def test_conv_rule_is_the_exact_covariance_of_a_conv_layer():
+    """Conv full-spatial rule (linear.py:1321-1424) == direct expectation; layout is
+    reversed after one Conv (is_reversed, linear.py:1344-1349)."""
+    rng = np.random.default_rng(6)
+    x1, x2 = rng.standard_normal((2, 5, 4, 3)), rng.standard_normal((2, 5, 4, 3))
+    k = o.serial(o.Conv(7, (3, 3), padding='SAME', W_std=1.7, b_std=0.3))(x1, x2)
+    assert k.is_reversed
+    direct = _conv_expectation(x1, x2, 1.7, 0.3)
+    np.testing.assert_allclose(o.reverse_zipped(k.nngp, 2), direct, rtol=1e-12)
+    np.testing.assert_allclose(k.ntk, k.nngp, rtol=1e-12)
+
+
+def test_relu_conv_monte_carlo():
+    """Analytic Conv->Relu->Conv kernel vs a width-4096 finite network (MC)."""
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal((2, 4, 4, 2))
+    k = o.serial(o.Conv(1, (3, 3), padding='SAME', W_std=1.5, b_std=0.1), o.Relu(),
+                 o.Conv(1, (3, 3), padding='SAME', W_std=1.2, b_std=0.2))(x, None)
+    width = 4096
+    H = W = 4
+
+    def conv(z, cin, cout, W_std, b_std):
+        Wt = rng.standard_normal((3, 3, cin, cout)) * W_std / math.sqrt(cin * 9)
+        b = rng.standard_normal(cout) * b_std
+        zp = np.pad(z, ((0, 0), (1, 1), (1, 1), (0, 0)))
+        out = np.zeros(z.shape[:3] + (cout,))
+        for d in range(3):
+            for e in range(3):
+                out += zp[:, d:d + H, e:e + W] @ Wt[d, e]
+        return out + b
+
+    y = conv(np.maximum(conv(x, 2, width, 1.5, 0.1), 0), width, width, 1.2, 0.2)
+    emp = np.einsum('ahwc,bgvc->abhgwv', y, y) / width
+    ana = k.nngp if not k.is_reversed else o.reverse_zipped(k.nngp, 2)
+    assert np.abs(emp - ana).max() < 0.15 * np.abs(ana).max()
+
+
+def test_flatten_vs_global_avg_pool():
+    """Flatten averages the spatial diagonal, GlobalAvgPool all entries (linear.py:1777-1882)."""
+    rng = np.random.default_rng(8)
+    x = rng.standard_normal((2, 4, 4, 3))
+    base = [o.Conv(1, (3, 3), padding='SAME', W_std=1.1), o.Relu()]
+    kf = o.serial(*base, o.Flatten())(x, None)
+    kg = o.serial(*base, o.GlobalAvgPool())(x, None)
+    kc = o.serial(*base)(x, None)
+    full = kc.nngp
+    np.testing.assert_allclose(kg.nngp, full.mean(axis=(2, 3, 4, 5)), rtol=1e-12)
+    diag = np.einsum('abhhww->abhw', full).mean(axis=(2, 3))
+    np.testing.assert_allclose(kf.nngp, diag, rtol=1e-12)
+
+
+def test_cholesky_equals_eigh_infinite_time():
+    """tests/predict_test.py:396-428."""
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal((20, 5))
+    xt = rng.standard_normal((7, 5))
+    kf = o.serial(o.Dense(1, 1.5, 0.1), o.Relu(), o.Dense(1, 1.5, 0.1))
+    ktt = kf(x, None, 'ntk')
+    kts = kf(xt, x, 'ntk')
+    y = rng.standard_normal((20, 3))
+    pf = o.gradient_descent_mse(ktt, y, diag_reg=1e-3)
+    a = pf(None, 0., 0., kts)
+    b = pf(np.inf, 0., 0., kts)
+    np.testing.assert_allclose(a[1], b[1], rtol=1e-8, atol=1e-10)
+    np.testing.assert_allclose(a[0], y)
+
+
+def test_myrtle5_readout_flatten_equals_mean_after_pools():
+    """AvgPool(2,2) down to 1x1 followed by Flatten is the mean of the 8^4 entries."""
+    rng = np.random.default_rng(10)
+    x = rng.standard_normal((1, 8, 8, 3))
+    base = [o.Conv(1, (3, 3), padding='SAME', W_std=1.4), o.Relu()]
+    k1 = o.serial(*base, *[o.AvgPool((2, 2), (2, 2))] * 3, o.Flatten())(x, None)
+    k2 = o.serial(*base, o.GlobalAvgPool())(x, None)
+    np.testing.assert_allclose(k1.nngp, k2.nngp, rtol=1e-12)
