@@ -35,7 +35,10 @@ def batch(kernel_fn, batch_size: int = 0, device_count: int = -1, store_on_devic
         names, single = _normalize_get(get)
         ctx = _Ctx(precision)
         bs = batch_size or max(x1t.shape[0], (x2t if x2t is not None else x1t).shape[0])
-        if isinstance(kernel_fn, KernelFn) and not kwargs.get('diagonal_spatial'):
+        ds = kwargs.get('diagonal_spatial')
+        if isinstance(kernel_fn, KernelFn):
+            ds = bool(kernel_fn.diagonal) if ds is None else bool(ds)
+        if isinstance(kernel_fn, KernelFn) and not ds:
             plan = _chain.plan_chain(kernel_fn.specs, tuple(x1t.shape), False)
             if plan is not None and (x2t is None or x2t.shape[1:] == x1t.shape[1:]):
                 old = _chain.SELF_CHUNK

@@ -67,19 +67,19 @@ __global__ void __launch_bounds__(256) gram_simt_kernel(const float* __restrict_
     }
 }
 
+// Per-row sum(x^2)/D, accumulated in the same order as the Gram kernel above so
+// that cov[i] equals a Gram diagonal entry bit for bit.
 __global__ void cov_diag_kernel(const float* __restrict__ x, int64_t n, int64_t d, float inv_d,
                                 float* __restrict__ cov) {
-  int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-  int lane = threadIdx.x & 31;
+  int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= n) return;
+  const float* p = x + row * d;
   float s = 0.f;
-  for (int64_t k = lane; k < d; k += 32) {
-    float v = __ldg(x + row * d + k);
+  for (int64_t k = 0; k < d; ++k) {
+    float v = __ldg(p + k);
     s = fmaf(v, v, s);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) cov[row] = s * inv_d;
+  cov[row] = s * inv_d;
 }
 
 // ---------------------------------------------------------------------------
@@ -367,7 +367,7 @@ __global__ void max_abs_kernel(const float* __restrict__ x, int64_t n, unsigned 
 // ---------------------------------------------------------------------------
 struct PoolGeom {
   int64_t batch, A, C, Ao, Co;
-  int wa, wc, sa, sc, pa, pc, circular, diag, average, normalize_edges;
+  int wa, wc, sa, sc, pa, pc, circular, diag, average, normalize_edges, pool2;
 };
 
 __global__ void pool_kernel(const float* __restrict__ in, float* __restrict__ out, PoolGeom g) {
@@ -392,6 +392,20 @@ __global__ void pool_kernel(const float* __restrict__ in, float* __restrict__ ou
           ++count;
         }
       }
+    } else if (g.pool2) {
+      // AvgPool(2, 2) / stride 2 / VALID: the window is summed plane by plane
+      // in the order the fused chain kernel accumulates it (planes (1,0),
+      // (0,0), (1,1), (0,1) of the (a, a') window), so both paths round alike.
+      int64_t jp = r % g.Co; r /= g.Co;
+      int64_t j = r % g.Co; r /= g.Co;
+      int64_t ip = r % g.Ao;
+      int64_t i = r / g.Ao;
+      auto plane = [&](int u, int up) {
+        const float* pl = src + (((2 * i + u) * g.A + 2 * ip + up) * g.C + 2 * j) * g.C + 2 * jp;
+        return (__ldg(pl) + __ldg(pl + 1)) + (__ldg(pl + g.C) + __ldg(pl + g.C + 1));
+      };
+      s = ((plane(1, 0) + plane(0, 0)) + plane(1, 1)) + plane(0, 1);
+      count = 16;
     } else {
       int64_t jp = r % g.Co; r /= g.Co;
       int64_t j = r % g.Co; r /= g.Co;
@@ -502,8 +516,8 @@ extern "C" int ntg_gram(void* stream, const float* x1, const float* x2, int64_t 
 extern "C" int ntg_cov_diag(void* stream, const float* x, int64_t n, int64_t d, float* cov) {
   NTG_REQUIRE(x && cov, "ntg_cov_diag: null pointer");
   NTG_REQUIRE(n > 0 && d > 0, "ntg_cov_diag: sizes must be positive");
-  cov_diag_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, as_stream(stream)>>>(x, n, d,
-                                                                           1.f / (float)d, cov);
+  cov_diag_kernel<<<(unsigned)ceil_div(n, 128), 128, 0, as_stream(stream)>>>(x, n, d,
+                                                                             1.f / (float)d, cov);
   note_launch();
   return check_launch("ntg_cov_diag");
 }
@@ -626,8 +640,10 @@ extern "C" int ntg_pool(void* stream, const float* in, float* out, int64_t batch
   NTG_REQUIRE(in && out, "ntg_pool: null pointer");
   NTG_REQUIRE(batch > 0 && a > 0 && c > 0 && ao > 0 && co > 0, "ntg_pool: bad sizes");
   NTG_REQUIRE(wa > 0 && wc > 0 && sa > 0 && sc > 0 && pa >= 0 && pc >= 0, "ntg_pool: bad window");
+  const int pool2 = !diag_spatial && wa == 2 && wc == 2 && sa == 2 && sc == 2 && pa == 0 &&
+                    pc == 0 && 2 * ao <= a && 2 * co <= c;
   PoolGeom g{batch, a, c, ao, co, wa, wc, sa, sc, pa, pc, pad_mode == NTG_PAD_CIRCULAR,
-             diag_spatial, average, normalize_edges};
+             diag_spatial, average, normalize_edges, pool2};
   int64_t total = diag_spatial ? batch * ao * co : batch * ao * ao * co * co;
   pool_kernel<<<grid_for(total), kThreads, 0, as_stream(stream)>>>(in, out, g);
   note_launch();

@@ -519,7 +519,12 @@ def _input_kernel(x1: torch.Tensor, x2: Optional[torch.Tensor], diagonal_spatial
     xb = x1 if x2 is None else x2
     if x1.ndim == 2:
         nngp = O.gram(x1, xb, prec)
-        cov1 = O.cov_diag(x1)
+        if x2 is None:
+            # the self covariances are the Gram diagonal itself, so that a self
+            # pair has var1 * var2 - nngp^2 == 0 exactly
+            cov1 = torch.diagonal(nngp).contiguous()
+        else:
+            cov1 = O.cov_diag(x1)
         cov2 = None if x2 is None else O.cov_diag(x2)
     elif diagonal_spatial:
         kk = x1.shape[-1]
