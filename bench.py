@@ -1,0 +1,418 @@
+"""Myrtle-5 NNGP+NTK throughput on GB300 (entries/s).
+
+Workload: the full-spatial Myrtle-5 kernel (notebook definition: Conv3x3+Relu
+x2, AvgPool, Conv+Relu, AvgPool, Conv+Relu, AvgPool x3, Flatten, Dense;
+W_std = sqrt(2), b_std = 0) over 2000 synthetic CIFAR-shaped inputs
+[2000, 32, 32, 3] (iid N(0, 1), standardised per channel, seed 0), computed as
+a 2000 x 2000 nngp+ntk kernel through nt.batch(batch_size=100). One step is
+one 100 x 100 tile of that grid (10,000 kernel entries, including the
+per-sample chains of the tile's 200 inputs). Steps walk the tile grid in
+row-major order; under torchrun rank r takes tiles r, r+N, ... (weak scaling).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line. `value` is device-timed throughput (inputs resident);
+`e2e` is the same metric through the public API from pinned host buffers
+with host<->device copies inside the timed region; `--impl reference` times
+the CPU restatement of the reference's kernel rules (oracle/nt_oracle.py,
+float32, one process per host core) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_SAMPLES, TILE, IMG = 2000, 100, (32, 32, 3)
+# Algorithmic HBM bytes per kernel entry of the layer-by-layer Myrtle-5 schedule
+# (f32 nngp+ntk, every layer tensor written once and read once):
+# (10 * 32^4 + 8 * 16^4 + 8 * 8^4) floats.
+BYTES_PER_ENTRY = (10 * 32 ** 4 + 8 * 16 ** 4 + 8 * 8 ** 4) * 4
+# FP32 operations per entry of the fused kernel, counted from its source per
+# full-spatial element: Gram 4 FMA + 1 MUL; per conv+act layer 4 adds (A
+# direction) + 4 adds (C direction) x 2 tensors, affine 4, ABRelu rule ~40.
+FLOPS_PER_ELEM_LAYER = 4 * 2 + 4 * 2 + 4 + 40
+
+
+def myrtle5(m):
+    conv = lambda: m.Conv(1, (3, 3), padding='SAME', W_std=math.sqrt(2.), b_std=0.)
+    layers = [conv(), m.Relu(), conv(), m.Relu(), m.AvgPool((2, 2), (2, 2)), conv(), m.Relu(),
+              m.AvgPool((2, 2), (2, 2)), conv(), m.Relu()]
+    layers += [m.AvgPool((2, 2), (2, 2))] * 3 + [m.Flatten(), m.Dense(10, math.sqrt(2.), 0.)]
+    return layers
+
+
+def make_inputs(n=N_SAMPLES, seed=0):
+    x = np.random.default_rng(seed).standard_normal((n,) + IMG).astype(np.float32)
+    x = (x - x.mean(axis=(0, 1, 2))) / x.std(axis=(0, 1, 2))
+    return x.astype(np.float32)
+
+
+def tiles(n_tiles_side):
+    return [(r, c) for r in range(n_tiles_side) for c in range(n_tiles_side)]
+
+
+def dist_env():
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return ws, rank, local
+
+
+class Clocks:
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    QUERY = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.gpu), f'--query-gpu={self.QUERY}',
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ''
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = [r.split(',') for r in (self.out or '').strip().splitlines() if r.strip()]
+        sm, mx, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for name, v in zip(names, r[5:9]):
+                    if v.strip().lower() == 'active':
+                        reasons.add(name)
+            except (ValueError, IndexError):
+                continue
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': mx,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def flush_l2(buf):
+    buf.add_(1.0)  # 256 MiB write: larger than the 126 MB L2
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    import nt_gb300 as nt
+    from nt_gb300 import _chain, _lib, stax
+    from nt_gb300.stax import _Ctx
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    dev = torch.device('cuda', torch.cuda.current_device())
+    x = make_inputs()
+    xd = torch.from_numpy(x).to(dev)
+    _, _, kf = stax.serial(*myrtle5(stax))
+    plan = _chain.plan_chain(kf.specs, tuple(xd.shape), False)
+    assert plan is not None, 'Myrtle-5 must take the fused chain path'
+    n_side = N_SAMPLES // TILE
+    grid = tiles(n_side)
+    total_steps = args.warmup + args.steps
+    mine = [grid[(rank + ws * s) % len(grid)] for s in range(total_steps)]
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    out_q = torch.empty((TILE, TILE), device=dev)
+    out_t = torch.empty((TILE, TILE), device=dev)
+
+    def step(rc, precision='fp32'):
+        r, c = rc
+        ctx = _Ctx(precision)
+        k = _chain.run_fused(plan, xd[r * TILE:(r + 1) * TILE], xd[c * TILE:(c + 1) * TILE], ctx,
+                             out=(out_q, out_t))
+        kf.apply_kernel(k, ctx, specs=plan.post)
+
+    stream = torch.cuda.current_stream()
+    for s in range(args.warmup):
+        step(mine[s])
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    launches0 = _lib.launch_count()
+    with Clocks(local) as clk:
+        for s in range(args.steps):
+            flush_l2(flush)
+            ev[s][0].record(stream)
+            step(mine[args.warmup + s])
+            ev[s][1].record(stream)
+        torch.cuda.synchronize()
+    launches = _lib.launch_count() - launches0
+    if ws > 1:
+        dist.barrier()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    t = torch.tensor([ms], device=dev)
+    if ws > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    entries = TILE * TILE * args.steps * ws
+    value = entries / (ms_max / 1e3)
+
+    # Dominant kernel alone: the fused chain launch of one tile, CUDA events on
+    # the launching stream, L2 flushed before each launch.
+    pg = _chain._program(plan, 3, _Ctx('fp32'))
+    xa, xb = xd[:TILE], xd[TILE:2 * TILE]
+    var1, _ = _chain.self_chain(xa, plan, _Ctx('fp32'))
+    var2, _ = _chain.self_chain(xb, plan, _Ctx('fp32'))
+    from nt_gb300 import _ops as O
+    kt = []
+    for i in range(4):
+        flush_l2(flush)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        O.chain_fwd(pg, xa, xb, 0, TILE, 0, TILE, var1, var2, out_q, out_t, TILE)
+        b.record(stream)
+        torch.cuda.synchronize()
+        if i:
+            kt.append(a.elapsed_time(b))
+    chain_ms = statistics.median(kt)
+    achieved_gbs = BYTES_PER_ENTRY * TILE * TILE / (chain_ms / 1e3) / 1e9
+    flops_entry = (5 * 32 ** 4 + FLOPS_PER_ELEM_LAYER * (2 * 32 ** 4 + 16 ** 4 + 8 ** 4))
+    achieved_tflops = flops_entry * TILE * TILE / (chain_ms / 1e3) / 1e12
+
+    # Materialised per-layer stencil (conv + Relu epilogue) on a 16 x 16 tile at S = 32.
+    st_gbs = stencil_roofline(torch, O, dev)
+
+    # Mixed precision (compensated) variant of the same step and its error vs plain.
+    torch.cuda.synchronize()
+    em = []
+    for s in range(min(args.steps, 5)):
+        flush_l2(flush)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step(mine[args.warmup + s], 'mixed')
+        b.record(stream)
+        torch.cuda.synchronize()
+        em.append(a.elapsed_time(b))
+    mixed_value = TILE * TILE / (statistics.mean(em) / 1e3)
+
+    # End to end through the public API: pinned host inputs, results read back.
+    xh = torch.from_numpy(x).pin_memory()
+    batched = nt.batch(kf, batch_size=TILE)
+    e2e_times = []
+    for s in range(args.steps):
+        r, c = mine[args.warmup + s]
+        h1 = xh[r * TILE:(r + 1) * TILE]
+        h2 = xh[c * TILE:(c + 1) * TILE]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = batched(h1, h2, ('nngp', 'ntk'))
+        q, tt = res.nngp.cpu(), res.ntk.cpu()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_value = TILE * TILE / statistics.mean(e2e_times)
+    h2d = 2 * TILE * int(np.prod(IMG)) * 4
+    d2h = 2 * TILE * TILE * 4
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+    except OSError:
+        pass
+    hbm_peak = peaks.get('hbm_gbs', 6800.0)
+    peak_note = 'of measured' if 'hbm_gbs' in peaks else 'of fallback'
+    clocks = clk.summary()
+    line = {
+        'metric': 'Myrtle-5 NTK entries/s mixed vs plain FP32 (<=1e-4 vs FP64); fwd+bwd ms',
+        'value': round(value, 1), 'unit': 'entries/s', 'n_gpus': ws, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': round(ms_max / args.steps, 3),
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+        'data': 'synthetic: iid N(0,1) [2000,32,32,3], standardised per channel, seed 0',
+        'config': {'workload': 'Myrtle-5 full-spatial nngp+ntk, 2000x2000 via '
+                               'nt.batch(batch_size=100); step = one 100x100 tile',
+                   'n_samples': N_SAMPLES, 'batch_size': TILE, 'input': list(IMG),
+                   'precision': 'fp32 (plain)', 'l2': 'flushed before every step (256 MiB write)',
+                   'path': 'fused chain kernel (ntg_chain_fwd) + per-sample chains'},
+        'mixed': {'value': round(mixed_value, 1), 'unit': 'entries/s',
+                  'precision': 'compensated var1*var2 - q^2'},
+        'e2e': {'value': round(e2e_value, 1), 'unit': 'entries/s', 'h2d_bytes_per_step': h2d,
+                'd2h_bytes_per_step': d2h, 'api': 'nt.batch(kernel_fn, 100)(x1, x2, get)'},
+        'roofline': {'bound': 'hbm', 'achieved': round(achieved_gbs, 1), 'peak': hbm_peak,
+                     'unit': 'GB/s', 'frac': round(achieved_gbs / hbm_peak, 3), 'traffic': None,
+                     'kernel': 'chain_fwd_kernel', 'kernel_ms': round(chain_ms, 3),
+                     'bytes_per_entry': BYTES_PER_ENTRY,
+                     'note': f'{peak_note}; algorithmic bytes of the layer-by-layer schedule; '
+                             'the fused kernel keeps them on chip'},
+        'compute': {'bound': 'fp32', 'achieved_tflops': round(achieved_tflops, 2),
+                    'flops_per_entry': flops_entry},
+        'stencil_roofline': st_gbs,
+        'gpu_launches': int(launches),
+        'clocks': clocks,
+    }
+    if args.cpu_baseline and rank == 0 and ws == 1:
+        line['cpu_baseline'] = cpu_baseline(x, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def stencil_roofline(torch, O, dev):
+    """Materialised 3x3 conv + Relu rule on [B, 32, 32, 32, 32] pairs (HBM-bound)."""
+    from nt_gb300 import _lib as L
+    B = 256
+    q = torch.rand((B, 32, 32, 32, 32), device=dev) + 1.
+    t = torch.rand_like(q)
+    var = torch.rand((B, 32, 32), device=dev) + 2.
+    v = L.Var(var.data_ptr(), 32 * 32, 32, 1)
+    aff = O.affine(2., 0., 2.)
+    act = L.Act(L.NTG_ACT_ABRELU, 0., 1., 0., 0, 0.)
+    outs = None
+    ts = []
+    for i in range(4):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        outs = O.conv_fs(q, t, B, 1, 32, 32, 3, 3, 1, 1, 1, 1, 32, 32, False, aff, act, v, v,
+                         True, (B,))
+        b.record()
+        torch.cuda.synchronize()
+        if i:
+            ts.append(a.elapsed_time(b))
+    del outs
+    ms = statistics.median(ts)
+    nbytes = 4 * q.numel() * 4  # read nngp, ntk; write nngp, ntk
+    gbs = nbytes / (ms / 1e3) / 1e9
+    return {'kernel': 'conv3_line_kernel', 'pairs': B, 'bytes': nbytes, 'ms': round(ms, 3),
+            'achieved': round(gbs, 1), 'unit': 'GB/s'}
+
+
+REF_TILE = 4
+
+
+def _ref_tile(args):
+    """A REF_TILE x REF_TILE block of kernel entries (nngp, ntk) from the float32 oracle."""
+    x1, x2 = args
+    sys.path.insert(0, ROOT)
+    from oracle import nt_oracle as o
+    kf = o.serial(*myrtle5(o))
+    nngp, ntk = kf(x1, x2, ('nngp', 'ntk'), dtype=np.float32)
+    return nngp.size
+
+
+def cpu_baseline(x, seconds=15.0, procs=None):
+    """Times the oracle (float32) on tiles of the same workload, one process per core."""
+    import multiprocessing as mp
+    procs = procs or os.cpu_count() or 1
+    ctx = mp.get_context('spawn')
+    done = 0
+    b = REF_TILE
+    with ctx.Pool(procs) as pool:
+        pool.map(_ref_tile, [(x[:b], x[b:2 * b])] * procs)  # warm the workers
+        t0 = time.perf_counter()
+        i = 0
+        while time.perf_counter() - t0 < seconds:
+            batch = [(x[(i + k) * b % 2000:][:b], x[(1000 + (i + 2 * k) * b) % 2000:][:b])
+                     for k in range(procs)]
+            done += sum(pool.map(_ref_tile, batch))
+            i += procs
+        el = time.perf_counter() - t0
+    return {'value': round(done / el, 3), 'unit': 'entries/s', 'cores': procs, 'kind': 'port',
+            'sample': f'{done} Myrtle-5 entries of the 2000x2000 grid as {b}x{b} tiles (nngp+ntk '
+                      f'and the tiles\' per-sample chains), float32 oracle, {procs} processes, '
+                      f'{el:.1f} s'}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    x = make_inputs()
+    procs = os.cpu_count() or 1
+    per_step = []
+    for s in range(args.warmup + args.steps):
+        r = cpu_baseline(x, seconds=args.ref_step_seconds, procs=procs)
+        if s >= args.warmup:
+            per_step.append(r['value'])
+    value = statistics.mean(per_step)
+    line = {
+        'impl': 'reference', 'metric': 'Myrtle-5 NTK entries/s mixed vs plain FP32 (<=1e-4 vs '
+                                       'FP64); fwd+bwd ms',
+        'value': round(value, 3), 'unit': 'entries/s', 'n_gpus': ws, 'steps': args.steps,
+        'warmup': args.warmup, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32', 'data': 'synthetic: iid N(0,1) [2000,32,32,3], standardised, seed 0',
+        'config': {'workload': 'Myrtle-5 full-spatial nngp+ntk, 2000x2000 via '
+                               'nt.batch(batch_size=100); step = a bounded sample of pairs',
+                   'n_samples': N_SAMPLES, 'batch_size': TILE},
+        'cpu_baseline': {'value': round(value, 3), 'unit': 'entries/s', 'cores': procs,
+                         'kind': 'port',
+                         'sample': f'{args.ref_step_seconds:.0f} s of {REF_TILE}x{REF_TILE} tiles per step, float32 '
+                                   'restatement of the reference rules (oracle/nt_oracle.py); '
+                                   'the JAX reference is not installable here'},
+        'e2e': {'value': round(value, 3), 'unit': 'entries/s', 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line))
+
+
+def profile_tile(p: int):
+    """One fused-chain launch on a p x p tile (a small case for ncu captures)."""
+    import torch
+    from nt_gb300 import _chain, _ops as O, stax
+    from nt_gb300.stax import _Ctx
+    x = torch.from_numpy(make_inputs(2 * p)).cuda()
+    _, _, kf = stax.serial(*myrtle5(stax))
+    plan = _chain.plan_chain(kf.specs, tuple(x.shape), False)
+    ctx = _Ctx('fp32')
+    var, _ = _chain.self_chain(x, plan, ctx)
+    pg = _chain._program(plan, 3, ctx)
+    oq = torch.empty((p, p), device='cuda')
+    ot = torch.empty((p, p), device='cuda')
+    O.chain_fwd(pg, x[:p], x[p:], 0, p, 0, p, var[:p].contiguous(), var[p:].contiguous(), oq, ot, p)
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_tile': p, 'nngp_mean': float(oq.mean()), 'ntk_mean': float(ot.mean())}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--profile-tile', type=int, default=0)
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=20)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='gb300', choices=['gb300', 'reference'])
+    ap.add_argument('--no-cpu-baseline', dest='cpu_baseline', action='store_false')
+    ap.add_argument('--cpu-seconds', type=float, default=15.0)
+    ap.add_argument('--ref-step-seconds', type=float, default=5.0)
+    args = ap.parse_args()
+    if args.profile_tile:
+        profile_tile(args.profile_tile)
+    elif args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == '__main__':
+    main()
