@@ -22,11 +22,12 @@
 namespace ntg {
 namespace {
 
-constexpr int NT = 256;
+constexpr int NT = 512;
 
 struct ChainCtx {
-  const float4* img1;  // [S0*S0] pixels, channels padded to 4
-  const float4* img2;
+  const float* img1;  // [K][S0*S0] channel planes
+  const float* img2;
+  int K;
   float* stage;        // [2 buffers][2 tensors][S0*S0]
   float inv_k;
   float acc_q, acc_t;  // per-thread readout partial sums
@@ -82,6 +83,10 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
     wp[u] = (c + r) & (S - 1);
   }
 
+  ActC acs[NC > 0 ? NC : 1];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) acs[k] = act_consts(pg.act[lbase + k]);
+
   // Ring of the last two planes of every level (level 0 = input).
   float Aq[NC + 1][EPT], Bq[NC + 1][EPT], At[NC + 1][EPT], Bt[NC + 1][EPT];
 #pragma unroll
@@ -98,14 +103,24 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
     for (int u = 0; u < EPT; ++u) nq[u] = nt[u] = 0.f;
     if (on && s < hi) {
       if (FIRST) {
-        const float4* x1r = cx.img1 + s * S;
-        const float4* x2r = cx.img2 + (s + delta) * S;
+        // first-layer Gram of the two images, channel by channel in the same
+        // order as ntg_input_fs, so that both paths round alike
+        const float* x1r = cx.img1 + s * S + c0;
+        const float* x2r = cx.img2 + (s + delta) * S;
+        float g[EPT];
 #pragma unroll
-        for (int u = 0; u < EPT; ++u) {
-          float4 a = x1r[c0 + u], b = x2r[wp[u]];
-          float g = fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)));
-          nq[u] = g * cx.inv_k;
+        for (int u = 0; u < EPT; ++u) g[u] = 0.f;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (k < cx.K) {
+            const float* a = x1r + k * (S * S);
+            const float* b = x2r + k * (S * S);
+#pragma unroll
+            for (int u = 0; u < EPT; ++u) g[u] = fmaf(a[u], b[wp[u]], g[u]);
+          }
         }
+#pragma unroll
+        for (int u = 0; u < EPT; ++u) nq[u] = g[u] * cx.inv_k;
       } else {
         const float* pq = in_q + s * S * S + r * S + c0;
         const float* pt = in_t + s * S * S + r * S + c0;
@@ -134,7 +149,7 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
       float oq[EPT], ot[EPT];
       const bool in_line = p >= lo && p < hi;
       const ntg_affine_t& af = pg.aff[l];
-      const ntg_act_t& ac = pg.act[l];
+      const ActC& ac = acs[k];
 #pragma unroll
       for (int u = 0; u < EPT; ++u) {
         float xl = (u > 0) ? hq[u - 1] : lq;
@@ -153,7 +168,7 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
           const float* vm = vmaps + 2 * k * S * S;
           float v1 = vm[p * S + c0 + u];
           float v2 = vm[S * S + (p + delta) * S + wp[u]];
-          apply_act(ac, q, t, v1, v2);
+          act_apply(ac, q, t, v1, v2);
         }
         oq[u] = in_line ? q : 0.f;
         ot[u] = in_line ? t : 0.f;
@@ -250,9 +265,9 @@ __global__ void __launch_bounds__(NT, 1)
   const int nseg = pg.nseg;
 
   ChainCtx cx;
-  float4* img1 = reinterpret_cast<float4*>(smem);
-  float4* img2 = img1 + S0 * S0;
-  float* p = reinterpret_cast<float*>(img2 + S0 * S0);
+  float* img1 = smem;                 // [4][S0*S0]
+  float* img2 = img1 + 4 * S0 * S0;
+  float* p = img2 + 4 * S0 * S0;
   // per-layer variance maps of both samples, segment by segment
   float* vseg[3] = {nullptr, nullptr, nullptr};
   {
@@ -279,20 +294,18 @@ __global__ void __launch_bounds__(NT, 1)
   p += 4 * S0 * S0;
   float* red = p;  // 2 * NT/32 floats
 
-  // images, channels padded to 4
+  // images as channel planes
   const float* im1 = x1 + gi * S0 * S0 * K;
   const float* im2 = x2 + gj * S0 * S0 * K;
   for (int e = threadIdx.x; e < S0 * S0; e += NT) {
-    float a[4] = {0.f, 0.f, 0.f, 0.f}, b[4] = {0.f, 0.f, 0.f, 0.f};
     for (int k = 0; k < K; ++k) {
-      a[k] = __ldg(im1 + e * K + k);
-      b[k] = __ldg(im2 + e * K + k);
+      img1[k * S0 * S0 + e] = __ldg(im1 + e * K + k);
+      img2[k * S0 * S0 + e] = __ldg(im2 + e * K + k);
     }
-    img1[e] = make_float4(a[0], a[1], a[2], a[3]);
-    img2[e] = make_float4(b[0], b[1], b[2], b[3]);
   }
   cx.img1 = img1;
   cx.img2 = img2;
+  cx.K = K;
   cx.inv_k = 1.f / (float)K;
   cx.acc_q = cx.acc_t = 0.f;
   cx.readout = pg.readout;
@@ -364,7 +377,7 @@ __global__ void __launch_bounds__(NT, 1)
 }
 
 size_t chain_smem_bytes(const ntg_chain_t& pg) {
-  size_t f = 2 * 32 * 32 * 4;  // images (float4)
+  size_t f = 2 * 4 * 32 * 32;  // images (4 channel planes each)
   for (int sgi = 0; sgi < pg.nseg; ++sgi) {
     size_t S = 32 >> sgi;
     f += 2 * S * S * pg.nconv[sgi];

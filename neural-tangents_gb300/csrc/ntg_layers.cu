@@ -133,6 +133,7 @@ __global__ void conv_fs_general_kernel(const float* __restrict__ in_q,
   const int64_t per_b = g.Ao * g.Ao * plane_o;
   const int64_t total = g.batch * per_b;
   const float inv = 1.f / (float)(g.fh * g.fw);
+  const ActC ac = act_consts(act);
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     int64_t b = idx / per_b, r = idx - b * per_b;
@@ -161,7 +162,7 @@ __global__ void conv_fs_general_kernel(const float* __restrict__ in_q,
       int64_t i1, i2;
       pair_of(b, g.n2, i1, i2);
       float v1 = var_at(var1, i1, i, j), v2 = var_at(var2, i2, ip, jp);
-      apply_act(act, q, t, v1, v2);
+      act_apply(ac, q, t, v1, v2);
     }
     out_q[idx] = q;
     if (out_t) out_t[idx] = t;
@@ -201,6 +202,7 @@ __global__ void __launch_bounds__(kThreads)
 
   int64_t i1, i2;
   pair_of(b, n2, i1, i2);
+  const ActC ac = act_consts(act);
   const int e0 = threadIdx.x * 4;
   const bool active = e0 < plane;
   const int c = active ? e0 / C : 0;
@@ -260,7 +262,7 @@ __global__ void __launch_bounds__(kThreads)
         apply_affine(aff, sq * inv9, st * inv9, out_t != nullptr, q, t);
         if (act.kind != NTG_ACT_NONE) {
           float v1 = var_at(var1, i1, i, c), v2 = var_at(var2, i2, i + delta, cp0 + u);
-          apply_act(act, q, t, v1, v2);
+          act_apply(ac, q, t, v1, v2);
         }
         vq[u] = q;
         vt[u] = t;
@@ -320,6 +322,7 @@ __global__ void affine_act_kernel(const float* __restrict__ in_q, const float* _
                                   ntg_var_t var1, ntg_var_t var2) {
   const int64_t M = diag ? A * C : A * A * C * C;
   const int64_t total = batch * M;
+  const ActC ac = act_consts(act);
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     int64_t b = idx / M, m = idx - b * M;
@@ -345,7 +348,7 @@ __global__ void affine_act_kernel(const float* __restrict__ in_q, const float* _
       }
       int64_t i1, i2;
       pair_of(b, n2, i1, i2);
-      apply_act(act, q, t, var_at(var1, i1, a1, c1), var_at(var2, i2, a2, c2));
+      act_apply(ac, q, t, var_at(var1, i1, a1, c1), var_at(var2, i2, a2, c2));
     }
     out_q[idx] = q;
     if (out_t) out_t[idx] = t;
