@@ -54,8 +54,8 @@ __device__ __forceinline__ void zero_slot(float* q, float* t, int n) {
 // `in_q/in_t` ([S][S*S], scaled by 1/16 for the AvgPool normalisation).
 // LAST: the final level feeds the readout sums, otherwise it is average-pooled
 // into the line slots of segment `seg + 1`.
-// `vmaps` holds this segment's variance maps, layer k at vmaps + 2*k*S*S
-// (sample 1) and + S*S more (sample 2); `out_slots` is the next segment's
+// `vmaps` holds this segment's variance maps, layer k at vmaps + 4*k*S*S:
+// var1, var2, sqrt(var1), sqrt(var2) as S x S maps; `out_slots` is the next segment's
 // slot region ([parity][tensor][S/2][S/2 * S/2]).
 template <int S, int NC, bool FIRST, bool LAST>
 __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg, int lbase,
@@ -73,13 +73,15 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
   const int lo = delta < 0 ? -delta : 0;
   const int hi = delta < 0 ? S : S - delta;
 
-  bool ml[EPT], mr[EPT];
+  // 1/0 weights of the left / right C-direction stencil neighbours (zero at
+  // the row ends and at the split between the row's two diagonals)
+  float ml[EPT], mr[EPT];
   int wp[EPT];
 #pragma unroll
   for (int u = 0; u < EPT; ++u) {
     int c = c0 + u;
-    ml[u] = c >= 1 && c != S - r;
-    mr[u] = c <= S - 2 && c != S - 1 - r;
+    ml[u] = (c >= 1 && c != S - r) ? 1.f : 0.f;
+    mr[u] = (c <= S - 2 && c != S - 1 - r) ? 1.f : 0.f;
     wp[u] = (c + r) & (S - 1);
   }
 
@@ -147,31 +149,34 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
       const float lt = has_t ? wshift_left(ht[EPT - 1]) : 0.f;
       const float rt = has_t ? wshift_right(ht[0]) : 0.f;
       float oq[EPT], ot[EPT];
-      const bool in_line = p >= lo && p < hi;
-      const ntg_affine_t& af = pg.aff[l];
-      const ActC& ac = acs[k];
+      const bool in_line = p >= lo && p < hi;  // uniform across the CTA
+      if (in_line) {
+        const ntg_affine_t& af = pg.aff[l];
+        const ActC& ac = acs[k];
+        const float* vm = vmaps + 4 * k * S * S;
 #pragma unroll
-      for (int u = 0; u < EPT; ++u) {
-        float xl = (u > 0) ? hq[u - 1] : lq;
-        float xr = (u < EPT - 1) ? hq[u + 1] : rq;
-        float cq = ((ml[u] ? xl : 0.f) + hq[u]) + (mr[u] ? xr : 0.f);
-        float ct = 0.f;
-        if (has_t) {
-          float yl = (u > 0) ? ht[u - 1] : lt;
-          float yr = (u < EPT - 1) ? ht[u + 1] : rt;
-          ct = ((ml[u] ? yl : 0.f) + ht[u]) + (mr[u] ? yr : 0.f);
+        for (int u = 0; u < EPT; ++u) {
+          const float xl = (u > 0) ? hq[u - 1] : lq;
+          const float xr = (u < EPT - 1) ? hq[u + 1] : rq;
+          const float cq = fmaf(mr[u], xr, fmaf(ml[u], xl, hq[u]));
+          float ct = 0.f;
+          if (has_t) {
+            const float yl = (u > 0) ? ht[u - 1] : lt;
+            const float yr = (u < EPT - 1) ? ht[u + 1] : rt;
+            ct = fmaf(mr[u], yr, fmaf(ml[u], yl, ht[u]));
+          }
+          float q, t = 0.f;
+          apply_affine(af, cq, ct, true, q, t, 1.f / 9.f);
+          if (ac.kind != NTG_ACT_NONE && on) {
+            const int i1 = p * S + c0 + u, i2 = (p + delta) * S + wp[u];
+            act_apply(ac, q, t, vm[i1], vm[S * S + i2], vm[2 * S * S + i1], vm[3 * S * S + i2]);
+          }
+          oq[u] = q;
+          ot[u] = t;
         }
-        const float inv9 = 1.f / 9.f;
-        float q, t = 0.f;
-        apply_affine(af, cq * inv9, ct * inv9, true, q, t);
-        if (ac.kind != NTG_ACT_NONE && on && in_line) {
-          const float* vm = vmaps + 2 * k * S * S;
-          float v1 = vm[p * S + c0 + u];
-          float v2 = vm[S * S + (p + delta) * S + wp[u]];
-          act_apply(ac, q, t, v1, v2);
-        }
-        oq[u] = in_line ? q : 0.f;
-        ot[u] = in_line ? t : 0.f;
+      } else {
+#pragma unroll
+        for (int u = 0; u < EPT; ++u) oq[u] = ot[u] = 0.f;
       }
 #pragma unroll
       for (int u = 0; u < EPT; ++u) {
@@ -234,6 +239,154 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
   __syncthreads();
 }
 
+// Segment-0 line processor for 32x32 inputs: process_line<32, NC, true,
+// LAST> with each thread's two elements held as one packed f32x2 pair.
+// Thread t owns columns 2(t % 16), 2(t % 16) + 1 of skewed row t / 16. The
+// per-lane operation sequence equals the scalar path's, so the result is bit
+// for bit the same as process_line's and as the materialised layer kernels'.
+template <int NC, bool LAST>
+__device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, const float* vmaps,
+                                         float* out_slots, int delta) {
+  constexpr int S = 32;
+  static_assert(NT == 512, "two columns per thread");
+  const int tid = threadIdx.x;
+  const int r = tid >> 4, c0 = (tid & 15) * 2;
+  const int lo = delta < 0 ? -delta : 0;
+  const int hi = delta < 0 ? S : S - delta;
+  const P2 ML = p2((c0 >= 1 && c0 != S - r) ? 1.f : 0.f, (c0 + 1 != S - r) ? 1.f : 0.f);
+  const P2 MR = p2((c0 != S - 1 - r) ? 1.f : 0.f,
+                   (c0 + 1 <= S - 2 && c0 + 1 != S - 1 - r) ? 1.f : 0.f);
+  const int wp0 = (c0 + r) & (S - 1), wp1 = (c0 + 1 + r) & (S - 1);
+  const P2 zero = p2s(0.f);
+
+  ActC acs[NC];
+  P2 W2[NC], B2[NC], TW[NC], TN[NC], TC[NC];
+  bool nns[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) {
+    acs[k] = act_consts(pg.act[k]);
+    const ntg_affine_t& f = pg.aff[k];
+    W2[k] = p2s(f.w2 * (1.f / 9.f));
+    B2[k] = p2s(f.b2);
+    TW[k] = p2s(f.ntk_w2 * (1.f / 9.f));
+    TN[k] = p2s(f.ntk_nn);
+    TC[k] = p2s(f.ntk_c);
+    nns[k] = f.nn_scaled != 0;
+  }
+  const P2 INV9 = p2s(1.f / 9.f);
+  const P2 INVK = p2s(cx.inv_k);
+
+  P2 Aq[NC], Bq[NC], At[NC], Bt[NC];
+#pragma unroll
+  for (int k = 0; k < NC; ++k) Aq[k] = Bq[k] = At[k] = Bt[k] = zero;
+
+  int buf = 0;
+  __syncthreads();
+  for (int s = lo; s < hi + NC; ++s) {
+    P2 nq = zero, nt = zero;
+    if (s < hi) {
+      const float* x1r = cx.img1 + s * S + c0;
+      const float* x2r = cx.img2 + (s + delta) * S;
+      P2 g = zero;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (k < cx.K) {
+          const float* b = x2r + k * (S * S);
+          g = fma2(p2ld(x1r + k * (S * S)), p2(b[wp0], b[wp1]), g);
+        }
+      }
+      nq = mul2(g, INVK);
+    }
+#pragma unroll
+    for (int k = 0; k < NC; ++k) {
+      const int p = s - k - 1;
+      const bool has_t = k > 0;
+      const P2 hq = add2(add2(Aq[k], Bq[k]), nq);
+      const P2 ht = has_t ? add2(add2(At[k], Bt[k]), nt) : zero;
+      float h0, h1, e0 = 0.f, e1 = 0.f;
+      p2u(hq, h0, h1);
+      const float lq = wshift_left(h1), rq = wshift_right(h0);
+      const P2 cq = fma2(MR, p2(h1, rq), fma2(ML, p2(lq, h0), hq));
+      P2 ct = zero;
+      if (has_t) {
+        p2u(ht, e0, e1);
+        const float lt = wshift_left(e1), rt = wshift_right(e0);
+        ct = fma2(MR, p2(e1, rt), fma2(ML, p2(lt, e0), ht));
+      }
+      P2 oq = zero, ot = zero;
+      if (p >= lo && p < hi) {  // uniform across the CTA
+        P2 q = fma2(W2[k], cq, B2[k]);
+        const P2 nn = nns[k] ? q : mul2(cq, INV9);
+        P2 t = fma2(TW[k], ct, fma2(TN[k], nn, TC[k]));
+        const ActC& ac = acs[k];
+        if (ac.kind != NTG_ACT_NONE) {
+          const float* vm = vmaps + 4 * k * S * S;
+          const int i1 = p * S + c0, i2 = (p + delta) * S;
+          const P2 v1 = p2ld(vm + i1), sv1 = p2ld(vm + 2 * S * S + i1);
+          const float* v2r = vm + S * S + i2;
+          const float* s2r = vm + 3 * S * S + i2;
+          if (ac.kind == NTG_ACT_ABRELU && ac.stab <= 0.f) {
+            abrelu2(ac, q, t, v1, p2(v2r[wp0], v2r[wp1]), sv1, p2(s2r[wp0], s2r[wp1]));
+          } else {
+            float qa, qb, ta, tb, va, vb, sa, sb;
+            p2u(q, qa, qb);
+            p2u(t, ta, tb);
+            p2u(v1, va, vb);
+            p2u(sv1, sa, sb);
+            act_apply(ac, qa, ta, va, v2r[wp0], sa, s2r[wp0]);
+            act_apply(ac, qb, tb, vb, v2r[wp1], sb, s2r[wp1]);
+            q = p2(qa, qb);
+            t = p2(ta, tb);
+          }
+        }
+        oq = q;
+        ot = t;
+      }
+      Aq[k] = Bq[k];
+      Bq[k] = nq;
+      At[k] = Bt[k];
+      Bt[k] = nt;
+      nq = oq;
+      nt = ot;
+    }
+    const int p = s - NC;
+    if (p < lo || p >= hi) continue;
+    float q0, q1, t0, t1;
+    p2u(nq, q0, q1);
+    p2u(nt, t0, t1);
+    if (LAST) {
+      if (cx.readout == 0 || (delta == 0 && r == 0)) {
+        cx.acc_q += q0 + q1;
+        cx.acc_t += t0 + t1;
+      }
+    } else {
+      float* sq = cx.stage + (2 * buf) * (S * S);
+      float* st = sq + S * S;
+      sq[c0 * S + wp0] = q0;
+      sq[(c0 + 1) * S + wp1] = q1;
+      st[c0 * S + wp0] = t0;
+      st[(c0 + 1) * S + wp1] = t1;
+      __syncthreads();
+      constexpr int H = S / 2;
+      if (tid < H * H) {
+        const int rho = tid / H, kap = tid % H;
+        const int j = kap, jp = (kap + rho) & (H - 1);
+        const int o0 = (2 * j) * S + 2 * jp, o1 = o0 + S;
+        const float vq = (sq[o0] + sq[o0 + 1]) + (sq[o1] + sq[o1 + 1]);
+        const float vt = (st[o0] + st[o0 + 1]) + (st[o1] + st[o1 + 1]);
+        const int I = p >> 1;
+        const int m = ((p + delta) >> 1) - I;
+        float* dq = out_slots + (2 * (m & 1)) * (H * H * H) + I * H * H + tid;
+        float* dt = dq + H * H * H;
+        *dq += vq;
+        *dt += vt;
+      }
+      buf ^= 1;
+    }
+  }
+  __syncthreads();
+}
+
 template <int S, bool LAST>
 __device__ __forceinline__ void process_pooled_line(ChainCtx& cx, const ntg_chain_t& pg, int ncv,
                                                     int lbase, const float* vmaps,
@@ -279,10 +432,13 @@ __global__ void __launch_bounds__(NT, 1)
         const float* g1 = var1 + gi * pg.var_stride + pg.var_off[l];
         const float* g2 = var2 + gj * pg.var_stride + pg.var_off[l];
         for (int e = threadIdx.x; e < S * S; e += NT) {
-          p[e] = __ldg(g1 + e);
-          p[S * S + e] = __ldg(g2 + e);
+          const float a = __ldg(g1 + e), b = __ldg(g2 + e);
+          p[e] = a;
+          p[S * S + e] = b;
+          p[2 * S * S + e] = sqrtf(a);
+          p[3 * S * S + e] = sqrtf(b);
         }
-        p += 2 * S * S;
+        p += 4 * S * S;
       }
     }
   }
@@ -324,9 +480,9 @@ __global__ void __launch_bounds__(NT, 1)
       }
     }
     if (nseg == 1)
-      process_line<S0, N0, true, true>(cx, pg, 0, vseg[0], nullptr, d0, nullptr, nullptr);
+      line_s32<N0, true>(cx, pg, vseg[0], nullptr, d0);
     else
-      process_line<S0, N0, true, false>(cx, pg, 0, vseg[0], slots1, d0, nullptr, nullptr);
+      line_s32<N0, false>(cx, pg, vseg[0], slots1, d0);
     if (nseg > 1 && (d0 & 1)) {
       const int m1 = (d0 - 1) / 2;
       if (m1 >= -(S1 - 1)) {
@@ -380,7 +536,7 @@ size_t chain_smem_bytes(const ntg_chain_t& pg) {
   size_t f = 2 * 4 * 32 * 32;  // images (4 channel planes each)
   for (int sgi = 0; sgi < pg.nseg; ++sgi) {
     size_t S = 32 >> sgi;
-    f += 2 * S * S * pg.nconv[sgi];
+    f += 4 * S * S * pg.nconv[sgi];
     if (sgi > 0) f += 4 * S * S * S;
   }
   f += 4 * 32 * 32;  // staging

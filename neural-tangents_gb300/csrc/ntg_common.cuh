@@ -91,15 +91,45 @@ __device__ __forceinline__ float atan2_xpos(float y, float x) {
   return copysignf(th, y);
 }
 
-// atan2(s, q) for s >= 0 (angle in [0, pi]); returns `fill` when s == q == 0
-// (the fill_zero convention of elementwise.py:1293-1301).
-__device__ __forceinline__ float atan2_ypos(float s, float q, float fill) {
-  const float aq = fabsf(q);
-  const float mx = fmaxf(aq, s), mn = fminf(aq, s);
-  float th = atan_unit(mn * rcp_approx(mx));
-  th = (s > aq) ? (0.5f * kPi - th) : th;
-  th = (q < 0.f) ? (kPi - th) : th;
-  return (mx == 0.f) ? fill : th;
+// Packed float pairs on the sm_100-family f32x2 datapath: one instruction
+// operates on two independent lanes, each rounded exactly as the scalar
+// instruction would round it.
+struct P2 {
+  unsigned long long v;
+};
+__device__ __forceinline__ P2 p2(float a, float b) {
+  P2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ P2 p2s(float a) { return p2(a, a); }
+__device__ __forceinline__ void p2u(P2 x, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(x.v));
+}
+__device__ __forceinline__ P2 p2ld(const float* ptr) {  // 8-byte aligned shared/global
+  P2 r;
+  r.v = *reinterpret_cast<const unsigned long long*>(ptr);
+  return r;
+}
+__device__ __forceinline__ P2 add2(P2 a, P2 b) {
+  P2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d.v) : "l"(a.v), "l"(b.v));
+  return d;
+}
+__device__ __forceinline__ P2 sub2(P2 a, P2 b) {
+  P2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d.v) : "l"(a.v), "l"(b.v));
+  return d;
+}
+__device__ __forceinline__ P2 mul2(P2 a, P2 b) {
+  P2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d.v) : "l"(a.v), "l"(b.v));
+  return d;
+}
+__device__ __forceinline__ P2 fma2(P2 a, P2 b, P2 c) {
+  P2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+  return d;
 }
 
 // Per-layer activation constants, computed once per layer (uniform).
@@ -107,8 +137,9 @@ struct ActC {
   int kind;
   int comp;
   float factor, half;  // ABRelu: (a-b)^2 / (2 pi), (a^2 + b^2) / 2
+  float f2, h_neg, h_zero;  // 2 factor, half - pi factor, half - pi/2 factor
   float a2, b2, c2;    // Erf: a^2, b^2, c^2
-  float stab, inv_stab;
+  float stab;
 };
 
 __device__ __forceinline__ ActC act_consts(const ntg_act_t& act) {
@@ -118,31 +149,42 @@ __device__ __forceinline__ ActC act_consts(const ntg_act_t& act) {
   const float amb = act.a - act.b;
   c.factor = __fdiv_rn(__fmul_rn(amb, amb), 2.f * kPi);
   c.half = 0.5f * (__fmul_rn(act.a, act.a) + __fmul_rn(act.b, act.b));
+  c.f2 = 2.f * c.factor;
+  c.h_neg = fmaf(-kPi, c.factor, c.half);
+  c.h_zero = fmaf(-0.5f * kPi, c.factor, c.half);
   c.a2 = __fmul_rn(act.a, act.a);
   c.b2 = __fmul_rn(act.b, act.b);
   c.c2 = __fmul_rn(act.c, act.c);
   c.stab = act.stabilize;
-  c.inv_stab = act.stabilize > 0.f ? __fdiv_rn(1.f, act.stabilize) : 1.f;
   return c;
 }
 
 // ABRelu(a, b) rule, elementwise.py:447-455:
 //   s = sqrt(max(prod - q^2, 0)); theta = atan2(s, q) (pi/2 if both 0)
 //   dot = (a^2 + b^2)/2 - (a-b)^2/(2 pi) theta; q' = (a-b)^2/(2 pi) s + dot q; ntk' = ntk dot
+// theta comes from the half-angle identities
+//   theta = 2 atan(s / (n + q)) for q >= 0,  theta = pi - 2 atan(s / (n - q)) for q < 0,
+// n = sqrt(v1) sqrt(v2) >= |q|, whose arguments lie in [0, 1] and carry no
+// cancellation near correlation +-1. sv1, sv2 are sqrt(v1), sqrt(v2).
 // Erf(a, b, c) rule, elementwise.py:67-112 (k *= b first, a*k + c last):
 //   prod = (1 + 2 v1)(1 + 2 v2); s = sqrt(max(prod - 4q^2, 0));
 //   q' = 2/pi atan2(2q, s); ntk' = ntk (4/pi) / s
-__device__ __forceinline__ void act_apply(const ActC& c, float& q, float& t, float v1, float v2) {
+__device__ __forceinline__ void act_apply(const ActC& c, float& q, float& t, float v1, float v2,
+                                          float sv1, float sv2) {
   if (c.kind == NTG_ACT_ABRELU) {
+    float n = __fmul_rn(sv1, sv2);
     if (c.stab > 0.f) {
       q = __fdiv_rn(q, c.stab);
       v1 = __fdiv_rn(v1, c.stab);
       v2 = __fdiv_rn(v2, c.stab);
+      n = __fdiv_rn(n, c.stab);
     }
     const float d = prod_minus_sq(v1, v2, q, c.comp);
     const float s = sqrt_approx(fmaxf(d, 0.f));
-    const float th = atan2_ypos(s, q, 0.5f * kPi);
-    const float dot = fmaf(-c.factor, th, c.half);
+    const float den = n + fabsf(q);
+    const float p = atan_unit(s * rcp_approx(den));
+    float dot = (q < 0.f) ? fmaf(c.f2, p, c.h_neg) : fmaf(-c.f2, p, c.half);
+    dot = (den == 0.f) ? c.h_zero : dot;
     float qo = fmaf(c.factor, s, __fmul_rn(dot, q));
     if (c.stab > 0.f) qo = __fmul_rn(qo, c.stab);
     q = qo;
@@ -161,13 +203,61 @@ __device__ __forceinline__ void act_apply(const ActC& c, float& q, float& t, flo
   }
 }
 
-// Affine rule on an unscaled propagated value u (nngp) and u_t (ntk).
+// The ABRelu branch of act_apply (do_stabilize off) on a packed pair, with
+// the same operation sequence per lane.
+__device__ __forceinline__ void abrelu2(const ActC& c, P2& q, P2& t, P2 v1, P2 v2, P2 sv1,
+                                        P2 sv2) {
+  const P2 n = mul2(sv1, sv2);
+  const P2 pr = mul2(v1, v2), qq = mul2(q, q);
+  P2 d = sub2(pr, qq);
+  if (c.comp) {
+    const P2 m1 = p2s(-1.f);
+    const P2 pe = fma2(v1, v2, mul2(pr, m1)), qe = fma2(q, q, mul2(qq, m1));
+    d = add2(d, sub2(pe, qe));
+  }
+  float d0, d1, q0, q1, n0, n1;
+  p2u(d, d0, d1);
+  p2u(q, q0, q1);
+  p2u(n, n0, n1);
+  const float s0 = sqrt_approx(fmaxf(d0, 0.f)), s1 = sqrt_approx(fmaxf(d1, 0.f));
+  const float den0 = n0 + fabsf(q0), den1 = n1 + fabsf(q1);
+  const P2 sp = p2(s0, s1);
+  const P2 r = mul2(sp, p2(rcp_approx(den0), rcp_approx(den1)));
+  const P2 z = mul2(r, r);
+  P2 pp = fma2(p2s(-0.00405457f), z, p2s(0.02186296f));
+  pp = fma2(pp, z, p2s(-0.05591233f));
+  pp = fma2(pp, z, p2s(0.09642197f));
+  pp = fma2(pp, z, p2s(-0.13908629f));
+  pp = fma2(pp, z, p2s(0.19946566f));
+  pp = fma2(pp, z, p2s(-0.3332986f));
+  pp = fma2(pp, z, p2s(0.99999934f));
+  pp = mul2(pp, r);
+  const P2 dneg = fma2(p2s(c.f2), pp, p2s(c.h_neg));
+  const P2 dpos = fma2(p2s(-c.f2), pp, p2s(c.half));
+  float a0, a1, b0, b1;
+  p2u(dneg, a0, a1);
+  p2u(dpos, b0, b1);
+  float dot0 = (q0 < 0.f) ? a0 : b0, dot1 = (q1 < 0.f) ? a1 : b1;
+  dot0 = (den0 == 0.f) ? c.h_zero : dot0;
+  dot1 = (den1 == 0.f) ? c.h_zero : dot1;
+  const P2 dot = p2(dot0, dot1);
+  q = fma2(p2s(c.factor), sp, mul2(dot, q));
+  t = mul2(t, dot);
+}
+
+__device__ __forceinline__ void act_apply(const ActC& c, float& q, float& t, float v1, float v2) {
+  act_apply(c, q, t, v1, v2, sqrtf(v1), sqrtf(v2));
+}
+
+// Affine rule on an unscaled propagated sum u (nngp) and u_t (ntk) whose
+// stencil normalisation `scale` (1 / filter size) is folded into the weights.
 __device__ __forceinline__ void apply_affine(const ntg_affine_t& f, float u, float ut,
-                                             bool has_ntk, float& q, float& t) {
-  q = __fadd_rn(__fmul_rn(f.w2, u), f.b2);
+                                             bool has_ntk, float& q, float& t,
+                                             float scale = 1.f) {
+  q = fmaf(f.w2 * scale, u, f.b2);
   if (has_ntk) {
-    float nn = f.nn_scaled ? q : u;
-    t = __fadd_rn(__fadd_rn(__fmul_rn(f.ntk_w2, ut), __fmul_rn(f.ntk_nn, nn)), f.ntk_c);
+    float nn = f.nn_scaled ? q : u * scale;
+    t = fmaf(f.ntk_w2 * scale, ut, fmaf(f.ntk_nn, nn, f.ntk_c));
   }
 }
 

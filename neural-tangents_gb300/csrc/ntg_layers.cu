@@ -157,7 +157,7 @@ __global__ void conv_fs_general_kernel(const float* __restrict__ in_q,
       }
     }
     float q, t = 0.f;
-    apply_affine(aff, sq * inv, st * inv, out_t != nullptr, q, t);
+    apply_affine(aff, sq, st, out_t != nullptr, q, t, inv);
     if (act.kind != NTG_ACT_NONE) {
       int64_t i1, i2;
       pair_of(b, g.n2, i1, i2);
@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(kThreads)
         float sq = (hq[buf][o - P - 1] + hq[buf][o]) + hq[buf][o + P + 1];
         float st = HAS_T ? (ht[buf][o - P - 1] + ht[buf][o]) + ht[buf][o + P + 1] : 0.f;
         float q, t = 0.f;
-        apply_affine(aff, sq * inv9, st * inv9, out_t != nullptr, q, t);
+        apply_affine(aff, sq, st, out_t != nullptr, q, t, inv9);
         if (act.kind != NTG_ACT_NONE) {
           float v1 = var_at(var1, i1, i, c), v2 = var_at(var2, i2, i + delta, cp0 + u);
           act_apply(ac, q, t, v1, v2);
@@ -306,7 +306,7 @@ __global__ void conv_ds_kernel(const float* __restrict__ in_q, const float* __re
       }
     }
     float q, t = 0.f;
-    apply_affine(aff, sq * inv, st * inv, out_t != nullptr, q, t);
+    apply_affine(aff, sq, st, out_t != nullptr, q, t, inv);
     out_q[idx] = q;
     if (out_t) out_t[idx] = t;
   }
