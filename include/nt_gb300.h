@@ -86,6 +86,10 @@ uint64_t ntg_launch_count(void);
  * tensor cores with FP32 accumulation. Replaces requirements.py:548,564. */
 int ntg_gram(void* stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
              int64_t d, float* nngp, int32_t precision);
+/* C [m, n] = A [m, k] B [k, n] in FP32 (C += A B when accumulate != 0): the
+ * tensordot(k_test_train, solve(...)) of predict.py:172-174. */
+int ntg_gemm(void* stream, const float* a, const float* b, float* c, int64_t m, int64_t n,
+             int64_t k, int32_t accumulate);
 /* Per-row sum(x^2)/D -> cov [N] (requirements.py:518-526, 572-582). */
 int ntg_cov_diag(void* stream, const float* x, int64_t n, int64_t d, float* cov);
 /* Image inputs x1 [N1, A, C, K], x2 [N2, A, C, K] (NHWC, K channels) ->
@@ -185,6 +189,28 @@ typedef struct {
 int ntg_chain_fwd(void* stream, const ntg_chain_t* prog, const float* x1, const float* x2,
                   int64_t r0, int64_t n1, int64_t c0, int64_t n2, const float* var1,
                   const float* var2, float* out_nngp, float* out_ntk, int64_t ld_out);
+
+/* ---- kernel regression (predict.gradient_descent_mse, t = None) -------- */
+/* Factor A = K + lambda I = L L^T in FP32 (predict.py:1224-1258 with
+ * cho_factor). K is the [n, n] float32 train-train kernel; lambda =
+ * diag_reg * trace(K) / n, or diag_reg when absolute != 0. L receives the
+ * lower factor ([n, n], upper triangle zeroed). lambda points to two device
+ * doubles: [0] receives lambda, [1] the trace of K. A non-positive pivot
+ * writes its 1-based column to *info (device int, 0 = success); the caller
+ * reads it back. */
+int ntg_chol_factor(void* stream, const float* A, int64_t n, double diag_reg, int32_t absolute,
+                    float* L, double* lambda, int* info);
+/* Bytes of device workspace ntg_chol_solve needs for refinement. */
+size_t ntg_chol_workspace_bytes(int64_t n, int64_t m);
+/* X = (K + lambda I)^{-1} B for B [n, m] (m <= 128): FP32 triangular solves
+ * with L, then `refine_iters` steps of iterative refinement whose residual
+ * B - (K + lambda I) X is accumulated in FP64 (predict.py:1235-1258 with
+ * cho_solve). `workspace` must hold ntg_chol_workspace_bytes(n, m) bytes when
+ * refine_iters > 0 or final_residual != NULL; final_residual (device double,
+ * optional) receives max |residual| of the returned X. */
+int ntg_chol_solve(void* stream, const float* A, const float* L, const double* lambda, int64_t n,
+                   const float* B, int64_t m, float* X, int32_t refine_iters, void* workspace,
+                   size_t workspace_bytes, double* final_residual);
 
 #ifdef __cplusplus
 }

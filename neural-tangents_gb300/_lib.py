@@ -54,6 +54,7 @@ SIGNATURES = {
     'ntg_version': ([], C.c_char_p),
     'ntg_launch_count': ([], C.c_uint64),
     'ntg_gram': ([_P, _P, _P, _I64, _I64, _I64, _P, _I32], C.c_int),
+    'ntg_gemm': ([_P, _P, _P, _P, _I64, _I64, _I64, _I32], C.c_int),
     'ntg_cov_diag': ([_P, _P, _I64, _I64, _P], C.c_int),
     'ntg_input_fs': ([_P, _P, _P, _I64, _I64, _I64, _I64, _I64, _I32, _P], C.c_int),
     'ntg_conv_fs': ([_P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, _I32, _I32, _I32, _I32,
@@ -71,6 +72,9 @@ SIGNATURES = {
     'ntg_flatten_fs': ([_P, _P, _P, _I64, _I64, _I64], C.c_int),
     'ntg_chain_fwd': ([_P, C.POINTER(Chain), _P, _P, _I64, _I64, _I64, _I64, _P, _P, _P, _P,
                        _I64], C.c_int),
+    'ntg_chol_factor': ([_P, _P, _I64, C.c_double, _I32, _P, _P, _P], C.c_int),
+    'ntg_chol_workspace_bytes': ([_I64, _I64], C.c_size_t),
+    'ntg_chol_solve': ([_P, _P, _P, _P, _I64, _P, _I64, _P, _I32, _P, C.c_size_t, _P], C.c_int),
 }
 
 _lib = None

@@ -67,6 +67,50 @@ __global__ void __launch_bounds__(256) gram_simt_kernel(const float* __restrict_
     }
 }
 
+// C[M, N] = A[M, K] B[K, N] (+ C_in when accumulate): 64x64 tiles, 4x4 per thread.
+__global__ void __launch_bounds__(256) gemm_nn_kernel(const float* __restrict__ A,
+                                                      const float* __restrict__ B,
+                                                      float* __restrict__ Cm, int64_t M, int64_t N,
+                                                      int64_t K, int accumulate) {
+  __shared__ float As[16][64 + 4];
+  __shared__ float Bs[16][64 + 4];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t row0 = (int64_t)blockIdx.y * 64, col0 = (int64_t)blockIdx.x * 64;
+  float acc[4][4] = {};
+  for (int64_t k0 = 0; k0 < K; k0 += 16) {
+    for (int idx = threadIdx.x; idx < 16 * 64; idx += 256) {
+      int r = idx / 16, kk = idx % 16;
+      int64_t gi = row0 + r, gk = k0 + kk;
+      As[kk][r] = (gi < M && gk < K) ? __ldg(A + gi * K + gk) : 0.f;
+      int kb = idx / 64, cb = idx % 64;
+      int64_t gkb = k0 + kb, gj = col0 + cb;
+      Bs[kb][cb] = (gkb < K && gj < N) ? __ldg(B + gkb * N + gj) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      float a[4], bb[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = As[kk][ty * 4 + u];
+        bb[u] = Bs[kk][tx * 4 + u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], bb[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      int64_t gi = row0 + ty * 4 + u, gj = col0 + tx * 4 + v;
+      if (gi < M && gj < N) Cm[gi * N + gj] = accumulate ? Cm[gi * N + gj] + acc[u][v] : acc[u][v];
+    }
+}
+
 // Per-row sum(x^2)/D, accumulated in the same order as the Gram kernel above so
 // that cov[i] equals a Gram diagonal entry bit for bit.
 __global__ void cov_diag_kernel(const float* __restrict__ x, int64_t n, int64_t d, float inv_d,
@@ -514,6 +558,17 @@ extern "C" int ntg_gram(void* stream, const float* x1, const float* x2, int64_t 
   gram_simt_kernel<<<grid, 256, 0, as_stream(stream)>>>(x1, x2, n1, n2, d, 1.f / (float)d, nngp);
   note_launch();
   return check_launch("ntg_gram");
+}
+
+extern "C" int ntg_gemm(void* stream, const float* a, const float* b, float* c, int64_t m,
+                        int64_t n, int64_t k, int32_t accumulate) {
+  NTG_REQUIRE(a && b && c, "ntg_gemm: null pointer");
+  NTG_REQUIRE(m > 0 && n > 0 && k > 0, "ntg_gemm: sizes must be positive");
+  NTG_REQUIRE(ceil_div(m, 64) <= 65535, "ntg_gemm: m too large");
+  dim3 grid((unsigned)ceil_div(n, 64), (unsigned)ceil_div(m, 64));
+  gemm_nn_kernel<<<grid, 256, 0, as_stream(stream)>>>(a, b, c, m, n, k, accumulate);
+  note_launch();
+  return check_launch("ntg_gemm");
 }
 
 extern "C" int ntg_cov_diag(void* stream, const float* x, int64_t n, int64_t d, float* cov) {

@@ -1,1 +1,145 @@
-"""nt_gb300.predict -- kernel-regression consumers (neural_tangents/_src/predict.py)."""
+"""nt_gb300.predict -- closed-form kernel regression (neural_tangents/_src/predict.py).
+
+``gradient_descent_mse(k_train_train, y_train, ...)`` keeps the reference
+signature (predict.py:71-278) and returns ``predict_fn(t=None, fx_train_0=0.,
+fx_test_0=None, k_test_train=None)``. ``t=None`` (infinite time) is the
+Cholesky path: an FP32 Cholesky of K + lambda I on the GPU, FP32 triangular
+solves and FP64 iterative refinement (`refine_iters`, default 2; 0 gives the
+plain FP32 solve), all in libntgb300.so. The factorisation is computed once
+and cached, as the reference caches it (predict.py:163). Finite ``t`` uses the
+eigendecomposition of predict.py:185-229 through torch.linalg.eigh (a cuSOLVER
+library call) in float64. Only 2-D ``k_train_train`` with ``trace_axes=(-1,)``
+is supported.
+"""
+from __future__ import annotations
+
+import warnings
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+
+def _dev(x, dtype=torch.float32) -> torch.Tensor:
+    dev = L.require_cuda()
+    if isinstance(x, torch.Tensor):
+        return x.to(device=dev, dtype=dtype).contiguous()
+    return torch.as_tensor(np.asarray(x), dtype=dtype, device=dev).contiguous()
+
+
+def _gemm(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    out = torch.empty((a.shape[0], b.shape[1]), device=a.device, dtype=torch.float32)
+    L.call('ntg_gemm', L.stream(), L.ptr(a), L.ptr(b), L.ptr(out), a.shape[0], b.shape[1],
+           a.shape[1], 0)
+    return out
+
+
+class CholeskySolver:
+    """Cached factorisation of K + lambda I (predict.py:1224-1258)."""
+
+    def __init__(self, k: torch.Tensor, diag_reg: float, absolute: bool, refine_iters: int = 2):
+        n = k.shape[0]
+        if k.ndim != 2 or k.shape[1] != n:
+            raise NotImplementedError('nt_gb300 supports a 2-D square k_train_train')
+        self.k, self.n, self.refine = k, n, int(refine_iters)
+        self.L = torch.empty_like(k)
+        self.lam = torch.zeros((2,), device=k.device, dtype=torch.float64)
+        info = torch.zeros((1,), device=k.device, dtype=torch.int32)
+        L.call('ntg_chol_factor', L.stream(), L.ptr(k), n, float(diag_reg), int(bool(absolute)),
+               L.ptr(self.L), self.lam.data_ptr(), info.data_ptr())
+        self.info = int(info.item())
+        if self.info:
+            warnings.warn(f'k_train_train + diag_reg * I is not positive definite (pivot '
+                          f'{self.info}); the solution is NaN, as jax.scipy.linalg.cho_solve '
+                          f'would return.')
+        self.residual = None
+
+    def solve(self, b: torch.Tensor) -> torch.Tensor:
+        b = b.reshape(self.n, -1).contiguous()
+        if self.info:
+            return torch.full_like(b, float('nan'))
+        out = torch.empty_like(b)
+        ws_bytes = int(L.load().ntg_chol_workspace_bytes(self.n, min(b.shape[1], 128)))
+        ws = torch.empty((ws_bytes,), device=b.device, dtype=torch.uint8)
+        res = torch.zeros((1,), device=b.device, dtype=torch.float64)
+        for c0 in range(0, b.shape[1], 128):
+            bc = b[:, c0:c0 + 128].contiguous()
+            xc = torch.empty_like(bc)
+            L.call('ntg_chol_solve', L.stream(), L.ptr(self.k), L.ptr(self.L),
+                   self.lam.data_ptr(), self.n, L.ptr(bc), bc.shape[1], L.ptr(xc), self.refine,
+                   ws.data_ptr(), ws_bytes, res.data_ptr())
+            out[:, c0:c0 + 128] = xc
+        self.residual = res
+        return out
+
+
+def gradient_descent_mse(k_train_train, y_train, learning_rate: float = 1.,
+                         diag_reg: float = 0., diag_reg_absolute_scale: bool = False,
+                         trace_axes=(-1,), refine_iters: int = 2):
+    """predict.py:71-278."""
+    if tuple(trace_axes) not in ((-1,), (1,)):
+        raise NotImplementedError('nt_gb300 supports trace_axes=(-1,)')
+    k = _dev(k_train_train)
+    y = _dev(y_train)
+    if y.ndim == 1:
+        raise ValueError('y_train must have a trailing output axis')
+    state = {}
+
+    def solver() -> CholeskySolver:
+        if 'chol' not in state:
+            state['chol'] = CholeskySolver(k, diag_reg, diag_reg_absolute_scale, refine_iters)
+        return state['chol']
+
+    def eig():
+        if 'eig' not in state:
+            a = k.double()
+            n = a.shape[0]
+            reg = diag_reg if diag_reg_absolute_scale else diag_reg * torch.trace(a) / n
+            a = a + reg * torch.eye(n, device=a.device, dtype=a.dtype)
+            state['eig'] = torch.linalg.eigh(a)
+        return state['eig']
+
+    def predict_fn(t=None, fx_train_0=0., fx_test_0=None, k_test_train=None):
+        if fx_test_0 is not None and k_test_train is None:
+            raise ValueError('`k_test_train` must be specified when `fx_test_0` is not `None`.')
+        if t is None:
+            fx_train_t = y
+            if fx_test_0 is None:
+                return fx_train_t
+            rhs = y if fx_train_0 is None else y - _as_like(fx_train_0, y)
+            x = solver().solve(rhs)
+            fx_test_t = _as_like(fx_test_0, None) + _gemm(_dev(k_test_train), x)
+            if fx_train_0 is None:
+                return fx_test_t
+            return fx_train_t, fx_test_t
+        evals, evecs = eig()
+        tt = torch.as_tensor(np.asarray(t, dtype=np.float64), device=k.device) * learning_rate
+        yd = y.double()
+        rhs = -yd if fx_train_0 is None else _as_like(fx_train_0, y).double() - yd
+        proj = evecs.T @ rhs
+        tshape = tuple(tt.shape)
+        tf = tt.reshape(-1, 1)
+        expm1 = torch.expm1(-torch.clamp(evals, min=0)[None] * tf / y.numel())
+        outs = []
+        if fx_train_0 is not None:
+            dfx = torch.einsum('ji,ti,ik->tjk', evecs, expm1, proj)
+            outs.append((_as_like(fx_train_0, y).double() + dfx).reshape(tshape + y.shape).float())
+        if fx_test_0 is not None:
+            inv = expm1 / torch.abs(evals)[None]
+            dfx = torch.einsum('ji,ti,ik->tjk', evecs, inv, proj)
+            kt = _dev(k_test_train).double()
+            test = _as_like(fx_test_0, None).double() + torch.einsum('sj,tjk->tsk', kt, dfx)
+            outs.append(test.reshape(tshape + (kt.shape[0], y.shape[1])).float())
+        if len(outs) == 2:
+            return tuple(outs)
+        return outs[0] if outs else y
+
+    return predict_fn
+
+
+def _as_like(v, like: Optional[torch.Tensor]):
+    if isinstance(v, (int, float)):
+        return v
+    return _dev(v)
