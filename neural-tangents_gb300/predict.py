@@ -117,7 +117,7 @@ def gradient_descent_mse(k_train_train, y_train, learning_rate: float = 1.,
         evals, evecs = eig()
         tt = torch.as_tensor(np.asarray(t, dtype=np.float64), device=k.device) * learning_rate
         yd = y.double()
-        rhs = -yd if fx_train_0 is None else _as_like(fx_train_0, y).double() - yd
+        rhs = -yd if fx_train_0 is None else _t64(fx_train_0, y) - yd
         proj = evecs.T @ rhs
         tshape = tuple(tt.shape)
         tf = tt.reshape(-1, 1)
@@ -125,12 +125,12 @@ def gradient_descent_mse(k_train_train, y_train, learning_rate: float = 1.,
         outs = []
         if fx_train_0 is not None:
             dfx = torch.einsum('ji,ti,ik->tjk', evecs, expm1, proj)
-            outs.append((_as_like(fx_train_0, y).double() + dfx).reshape(tshape + y.shape).float())
+            outs.append((_t64(fx_train_0, y) + dfx).reshape(tshape + y.shape).float())
         if fx_test_0 is not None:
             inv = expm1 / torch.abs(evals)[None]
             dfx = torch.einsum('ji,ti,ik->tjk', evecs, inv, proj)
             kt = _dev(k_test_train).double()
-            test = _as_like(fx_test_0, None).double() + torch.einsum('sj,tjk->tsk', kt, dfx)
+            test = _t64(fx_test_0, y) + torch.einsum('sj,tjk->tsk', kt, dfx)
             outs.append(test.reshape(tshape + (kt.shape[0], y.shape[1])).float())
         if len(outs) == 2:
             return tuple(outs)
@@ -143,3 +143,9 @@ def _as_like(v, like: Optional[torch.Tensor]):
     if isinstance(v, (int, float)):
         return v
     return _dev(v)
+
+
+def _t64(v, like: torch.Tensor) -> torch.Tensor:
+    if isinstance(v, (int, float)):
+        return torch.tensor(float(v), dtype=torch.float64, device=like.device)
+    return _dev(v, torch.float64)

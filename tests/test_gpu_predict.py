@@ -40,11 +40,12 @@ def test_fcn_config_end_to_end(nt):
     np.testing.assert_allclose(fx_train.cpu().numpy(), want[0], rtol=1e-6)
     got = fx_test.cpu().numpy()
     assert np.max(np.abs(got - want[1])) / np.max(np.abs(want[1])) < 1e-4
-    # the solve itself, on the same float32 kernel, matches a float64 solve to ~1e-6
+    # the refined solve on the same float32 kernel, followed by the float32
+    # k_test_train product, matches a float64 solve to ~1e-5
     k64 = ktt.double().cpu().numpy()
     a = k64 + 1e-4 * np.trace(k64) / 256 * np.eye(256)
     exact = kts.double().cpu().numpy() @ sla.cho_solve(sla.cho_factor(a), y)
-    assert np.max(np.abs(got - exact)) / np.max(np.abs(exact)) < 2e-6
+    assert np.max(np.abs(got - exact)) / np.max(np.abs(exact)) < 1e-5
 
 
 def test_cholesky_equals_eigh_at_infinite_time(nt):
