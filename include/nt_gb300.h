@@ -212,6 +212,24 @@ int ntg_chol_solve(void* stream, const float* A, const float* L, const double* l
                    const float* B, int64_t m, float* X, int32_t refine_iters, void* workspace,
                    size_t workspace_bytes, double* final_residual);
 
+/* No counterpart in the reference. ntg_chol_solve without a caller workspace,
+ * for callers that cannot allocate device memory where they call the solve
+ * (a handler inside a captured CUDA graph, a server that reserved all device
+ * memory up front). The refinement workspace is a fixed device array of
+ * NTG_NOALLOC_SCRATCH_BYTES owned by the library: each GPU that loads the
+ * library holds it until the process exits, and the call fails with
+ * NTG_ERR_INVALID_ARG when ntg_chol_workspace_bytes(n, m) exceeds it (about
+ * n * m <= 87,000). The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture. All calls share the array: calls that overlap on the GPU (other
+ * streams, other threads) race and must be serialised by the caller. No
+ * cudaMalloc, cudaFree or allocating library routine is called. Arguments
+ * and results are those of ntg_chol_solve. */
+#define NTG_NOALLOC_SCRATCH_BYTES (1u << 20)
+int ntg_chol_solve_noalloc(void* stream, const float* A, const float* L, const double* lambda,
+                           int64_t n, const float* B, int64_t m, float* X, int32_t refine_iters,
+                           double* final_residual);
+
 #ifdef __cplusplus
 }
 #endif

@@ -75,6 +75,7 @@ SIGNATURES = {
     'ntg_chol_factor': ([_P, _P, _I64, C.c_double, _I32, _P, _P, _P], C.c_int),
     'ntg_chol_workspace_bytes': ([_I64, _I64], C.c_size_t),
     'ntg_chol_solve': ([_P, _P, _P, _P, _I64, _P, _I64, _P, _I32, _P, C.c_size_t, _P], C.c_int),
+    'ntg_chol_solve_noalloc': ([_P, _P, _P, _P, _I64, _P, _I64, _P, _I32, _P], C.c_int),
 }
 
 _lib = None
