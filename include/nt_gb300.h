@@ -81,11 +81,16 @@ const char* ntg_version(void);
 uint64_t ntg_launch_count(void);
 
 /* ---- input kernels (requirements.py:518-638, 641-830) ---------------- */
-/* Flat inputs x1 [N1, D], x2 [N2, D] -> nngp [N1, N2] = x1 x2^T / D.
- * precision 0: FP32 CUDA cores; 1: split BF16 hi+lo products on tcgen05
- * tensor cores with FP32 accumulation. Replaces requirements.py:548,564. */
+/* Flat inputs x1 [N1, D], x2 [N2, D] -> nngp [N1, N2] = x1 x2^T / D
+ * (requirements.py:542-564). precision 0: FP32 on CUDA cores (workspace
+ * unused, may be NULL); 1: x = hi + lo split into BF16, hi1 hi2^T + hi1 lo2^T
+ * + lo1 hi2^T on the tcgen05 tensor cores with FP32 accumulation, fed by TMA;
+ * needs ntg_gram_workspace_bytes(n1, n2, d) bytes of workspace, whose first
+ * int32 is set non-zero if a bounded pipeline wait ran out (read it back to
+ * check). */
 int ntg_gram(void* stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
-             int64_t d, float* nngp, int32_t precision);
+             int64_t d, float* nngp, int32_t precision, void* workspace, size_t workspace_bytes);
+size_t ntg_gram_workspace_bytes(int64_t n1, int64_t n2, int64_t d);
 /* C [m, n] = A [m, k] B [k, n] in FP32 (C += A B when accumulate != 0): the
  * tensordot(k_test_train, solve(...)) of predict.py:172-174. */
 int ntg_gemm(void* stream, const float* a, const float* b, float* c, int64_t m, int64_t n,

@@ -60,9 +60,19 @@ def spatial_ac(t: torch.Tensor, bnd: int, diag: bool) -> tuple[int, int]:
 
 
 def gram(x1: torch.Tensor, x2: torch.Tensor, precision: int = 0) -> torch.Tensor:
-    out = torch.empty((x1.shape[0], x2.shape[0]), device=x1.device, dtype=torch.float32)
-    L.call('ntg_gram', L.stream(), L.ptr(x1), L.ptr(x2), x1.shape[0], x2.shape[0], x1.shape[1],
-           L.ptr(out), precision)
+    """x1 x2^T / D; precision 1 runs the split-BF16 tcgen05 tensor-core kernel."""
+    n1, n2, d = x1.shape[0], x2.shape[0], x1.shape[1]
+    out = torch.empty((n1, n2), device=x1.device, dtype=torch.float32)
+    ws, nbytes = None, 0
+    if precision == 1:
+        nbytes = int(L.load().ntg_gram_workspace_bytes(n1, n2, d))
+        ws = torch.empty((nbytes,), device=x1.device, dtype=torch.uint8)
+    L.call('ntg_gram', L.stream(), L.ptr(x1), L.ptr(x2), n1, n2, d, L.ptr(out), precision,
+           None if ws is None else ws.data_ptr(), nbytes)
+    if precision == 1:
+        code = int(ws[:4].view(torch.int32).item())
+        if code:
+            raise L.NtgError(f'ntg_gram: tensor-core pipeline wait timed out (code {code})')
     return out
 
 

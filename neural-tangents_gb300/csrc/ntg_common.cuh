@@ -21,7 +21,8 @@ void note_launch(uint64_t n = 1);
 
 // Tensor-core (tcgen05) split-precision Gram; defined in ntg_gram_tc.cu.
 int gram_tc(cudaStream_t stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
-            int64_t d, float* out);
+            int64_t d, float* out, void* workspace, size_t ws_bytes);
+size_t gram_tc_workspace(int64_t n1, int64_t n2, int64_t d);
 
 #define NTG_REQUIRE(cond, msg)                                   \
   do {                                                           \

@@ -1,8 +1,301 @@
-// Split-precision Gram x1 x2^T / D on the tcgen05 tensor cores (sm_103a).
+// Split-precision Gram x1 x2^T / D on the sm_103a tensor cores (tcgen05).
+//
+// Each float32 input is split into bf16 hi = bf16(x) and lo = bf16(x - hi);
+// x1 x2^T ~ hi1 hi2^T + hi1 lo2^T + lo1 hi2^T, the three products accumulated
+// in FP32 in tensor memory (the lo lo^T term is below float32 resolution of
+// the sum). Tiles: 128 x 128 outputs per CTA, K chunks of 64 bf16 (one 128-byte
+// swizzled row) moved by TMA into a 3-stage shared-memory ring; one thread
+// issues tcgen05.mma (M=128, N=128, K=16) and tcgen05.commit frees each stage;
+// four warps drain the accumulator with tcgen05.ld. Every mbarrier wait is
+// bounded: a wait that runs out sets the error word and the CTA winds down.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+#include <string>
+
 #include "ntg_common.cuh"
 
 namespace ntg {
-int gram_tc(cudaStream_t, const float*, const float*, int64_t, int64_t, int64_t, float*) {
-  return fail(NTG_ERR_UNSUPPORTED, "ntg_gram: tensor-core path not built");
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 64;
+constexpr int STAGES = 3;
+constexpr int TILE_BYTES = BM * BK * 2;       // one operand tile: 16 KB
+constexpr int STAGE_BYTES = 4 * TILE_BYTES;   // A_hi, A_lo, B_hi, B_lo
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr uint32_t TMEM_COLS = 128;
+constexpr uint64_t WAIT_LIMIT = 1ull << 20;   // about a second of polling
+
+__global__ void split_bf16_kernel(const float* __restrict__ x, int64_t n, int64_t d,
+                                  int64_t npad, int64_t dpad, __nv_bfloat16* __restrict__ hi,
+                                  __nv_bfloat16* __restrict__ lo) {
+  const int64_t total = npad * dpad;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = idx / dpad, c = idx - r * dpad;
+    const float v = (r < n && c < d) ? __ldg(x + r * d + c) : 0.f;
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    hi[idx] = h;
+    lo[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
+  }
 }
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+// Bounded wait for the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (uint64_t it = 0; it < WAIT_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar,
+                                            int32_t x, int32_t y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
+      : "memory");
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row
+// groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);        // start address
+  d |= (uint64_t)1 << 16;                        // leading byte offset (unused for SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset
+  d |= (uint64_t)1 << 46;                        // descriptor version
+  d |= (uint64_t)2 << 61;                        // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D F32, A/B BF16, both K-major, M=128, N=128.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(IDESC), "r"(acc));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(128, 1)
+    gram_tc_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
+                   const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
+                   float* __restrict__ out, int64_t n1, int64_t n2, int64_t dpad, float inv_d,
+                   int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  // 1024-byte alignment for the swizzled tiles
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  // bars[0..S): full, bars[S..2S): empty, bars[2S]: accumulator ready
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
+  const int nk = (int)(dpad / BK);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(smem_u32(&bars[s]), 1);
+      mbar_init(smem_u32(&bars[STAGES + s]), 1);
+    }
+    mbar_init(smem_u32(&bars[2 * STAGES]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+  bool ok = true;
+
+  if (warp == 0 && lane == 0) {
+    // TMA producer
+    for (int kc = 0; kc < nk && ok; ++kc) {
+      const int s = kc % STAGES;
+      if (kc >= STAGES) ok = mbar_wait(smem_u32(&bars[STAGES + s]), ((kc / STAGES) - 1) & 1);
+      if (!ok) break;
+      const uint32_t full = smem_u32(&bars[s]);
+      uint8_t* st = smem + s * STAGE_BYTES;
+      mbar_expect_tx(full, STAGE_BYTES);
+      const int32_t x = kc * BK;
+      tma_load_2d(smem_u32(st), &ta_hi, full, x, (int32_t)m0);
+      tma_load_2d(smem_u32(st + TILE_BYTES), &ta_lo, full, x, (int32_t)m0);
+      tma_load_2d(smem_u32(st + 2 * TILE_BYTES), &tb_hi, full, x, (int32_t)n0);
+      tma_load_2d(smem_u32(st + 3 * TILE_BYTES), &tb_lo, full, x, (int32_t)n0);
+    }
+    if (!ok) atomicExch(err, 1);
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    for (int kc = 0; kc < nk && ok; ++kc) {
+      const int s = kc % STAGES;
+      ok = mbar_wait(smem_u32(&bars[s]), (kc / STAGES) & 1);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+      const uint32_t a_hi = st, a_lo = st + TILE_BYTES, b_hi = st + 2 * TILE_BYTES,
+                     b_lo = st + 3 * TILE_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk) {
+        const uint32_t off = kk * 32;  // 16 bf16 along K
+        mma_bf16(tmem, smem_desc(a_hi + off), smem_desc(b_hi + off), (kc | kk) ? 1u : 0u);
+        mma_bf16(tmem, smem_desc(a_hi + off), smem_desc(b_lo + off), 1u);
+        mma_bf16(tmem, smem_desc(a_lo + off), smem_desc(b_hi + off), 1u);
+      }
+      mma_commit(smem_u32(&bars[STAGES + s]));  // frees the stage once these MMAs finish
+    }
+    mma_commit(smem_u32(&bars[2 * STAGES]));  // accumulator complete
+    if (!ok) atomicExch(err, 2);
+  }
+  __syncwarp();
+
+  // Epilogue: warp w drains TMEM lanes 32 (w % 4) .. + 31 (rows of the tile).
+  const bool ready = mbar_wait(smem_u32(&bars[2 * STAGES]), 0);
+  if (!ready && lane == 0) atomicExch(err, 3);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ready) {
+    const int rq = warp & 3;
+    const int64_t row = m0 + rq * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      uint32_t v[32];
+      const uint32_t taddr = tmem + ((uint32_t)(rq * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
+          "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
+          "%28, %29, %30, %31}, [%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+            "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
+            "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+            "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
+            "=r"(v[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < n1) {
+        float* o = out + row * n2 + n0 + c0;
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (n0 + c0 + j < n2) o[j] = __uint_as_float(v[j]) * inv_d;
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS));
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+int make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t dpad) {
+  auto fn = encode_fn();
+  if (!fn) return fail(NTG_ERR_CUDA, "ntg_gram: cuTensorMapEncodeTiled unavailable");
+  cuuint64_t dims[2] = {(cuuint64_t)dpad, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(dpad * 2)};
+  cuuint32_t box[2] = {BK, BM};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
+                  box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(NTG_ERR_CUDA, "ntg_gram: cuTensorMapEncodeTiled failed");
+  return NTG_OK;
+}
+
+}  // namespace
+
+size_t gram_tc_workspace(int64_t n1, int64_t n2, int64_t d) {
+  const int64_t dpad = ceil_div(d, BK) * BK;
+  const int64_t p1 = ceil_div(n1, BM) * BM, p2 = ceil_div(n2, BN) * BN;
+  return (size_t)(2 * (p1 + p2) * dpad) * sizeof(__nv_bfloat16) + 256 + 256;
+}
+
+int gram_tc(cudaStream_t s, const float* x1, const float* x2, int64_t n1, int64_t n2, int64_t d,
+            float* out, void* workspace, size_t ws_bytes) {
+  NTG_REQUIRE(workspace && ws_bytes >= gram_tc_workspace(n1, n2, d),
+              "ntg_gram: precision 1 needs ntg_gram_workspace_bytes(n1, n2, d) of workspace");
+  NTG_REQUIRE(ceil_div(n1, BM) <= 65535, "ntg_gram: n1 too large");
+  const int64_t dpad = ceil_div(d, BK) * BK;
+  const int64_t p1 = ceil_div(n1, BM) * BM, p2 = ceil_div(n2, BN) * BN;
+  uint8_t* ws = static_cast<uint8_t*>(workspace);
+  int* err = reinterpret_cast<int*>(ws);
+  __nv_bfloat16* a_hi = reinterpret_cast<__nv_bfloat16*>(ws + 256);
+  __nv_bfloat16* a_lo = a_hi + p1 * dpad;
+  __nv_bfloat16* b_hi = a_lo + p1 * dpad;
+  __nv_bfloat16* b_lo = b_hi + p2 * dpad;
+  if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return check_launch("ntg_gram memset");
+  auto grid = [](int64_t n) { return (unsigned)std::min<int64_t>(ceil_div(n, 256), 152 * 32); };
+  split_bf16_kernel<<<grid(p1 * dpad), 256, 0, s>>>(x1, n1, d, p1, dpad, a_hi, a_lo);
+  split_bf16_kernel<<<grid(p2 * dpad), 256, 0, s>>>(x2, n2, d, p2, dpad, b_hi, b_lo);
+  note_launch(2);
+  CUtensorMap m[4];
+  int rc;
+  if ((rc = make_map(&m[0], a_hi, p1, dpad)) || (rc = make_map(&m[1], a_lo, p1, dpad)) ||
+      (rc = make_map(&m[2], b_hi, p2, dpad)) || (rc = make_map(&m[3], b_lo, p2, dpad)))
+    return rc;
+  static std::once_flag attr_once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(attr_once, [] {
+    attr_err = cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    SMEM_BYTES);
+  });
+  if (attr_err != cudaSuccess)
+    return fail(NTG_ERR_CUDA, std::string("ntg_gram: ") + cudaGetErrorString(attr_err));
+  dim3 g((unsigned)(p2 / BN), (unsigned)(p1 / BM));
+  gram_tc_kernel<<<g, 128, SMEM_BYTES, s>>>(m[0], m[1], m[2], m[3], out, n1, n2, dpad,
+                                            1.f / (float)d, err);
+  note_launch();
+  return check_launch("ntg_gram (tcgen05)");
+}
+
 }  // namespace ntg

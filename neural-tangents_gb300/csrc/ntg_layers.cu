@@ -545,12 +545,17 @@ int grid_for(int64_t total, int threads = kThreads) {
 
 using namespace ntg;
 
+extern "C" size_t ntg_gram_workspace_bytes(int64_t n1, int64_t n2, int64_t d) {
+  return gram_tc_workspace(n1, n2, d);
+}
+
 extern "C" int ntg_gram(void* stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
-                        int64_t d, float* nngp, int32_t precision) {
+                        int64_t d, float* nngp, int32_t precision, void* workspace,
+                        size_t workspace_bytes) {
   NTG_REQUIRE(x1 && x2 && nngp, "ntg_gram: null pointer");
   NTG_REQUIRE(n1 > 0 && n2 > 0 && d > 0, "ntg_gram: sizes must be positive");
   if (precision == 1) {
-    return gram_tc(as_stream(stream), x1, x2, n1, n2, d, nngp);
+    return gram_tc(as_stream(stream), x1, x2, n1, n2, d, nngp, workspace, workspace_bytes);
   }
   NTG_REQUIRE(precision == 0, "ntg_gram: precision must be 0 or 1");
   NTG_REQUIRE(ceil_div(n1, 64) <= 65535, "ntg_gram: n1 too large");

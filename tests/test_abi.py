@@ -46,7 +46,7 @@ def test_version_and_error_channel(lib):
     lib.ntg_gram.restype = ctypes.c_int
     # invalid arguments are rejected on the host before any CUDA call
     rc = lib.ntg_gram(None, None, None, ctypes.c_int64(1), ctypes.c_int64(1), ctypes.c_int64(1),
-                      None, 0)
+                      None, 0, None, ctypes.c_size_t(0))
     assert rc == 1
     assert b'null pointer' in lib.ntg_last_error()
 
