@@ -206,6 +206,7 @@ def run_gpu(args):
 
     # Materialised per-layer stencil (conv + Relu epilogue) on a 16 x 16 tile at S = 32.
     st_gbs = stencil_roofline(torch, O, dev)
+    gram_tc = gram_roofline(torch, O, dev)
 
     # Mixed precision (compensated) variant of the same step and its error vs plain.
     torch.cuda.synchronize()
@@ -269,6 +270,7 @@ def run_gpu(args):
         'compute': {'bound': 'fp32', 'achieved_tflops': round(achieved_tflops, 2),
                     'flops_per_entry': flops_entry},
         'stencil_roofline': st_gbs,
+        'gram_tc': gram_tc,
         'gpu_launches': int(launches),
         'clocks': clocks,
     }
@@ -307,6 +309,25 @@ def stencil_roofline(torch, O, dev):
     gbs = nbytes / (ms / 1e3) / 1e9
     return {'kernel': 'conv3_line_kernel', 'pairs': B, 'bytes': nbytes, 'ms': round(ms, 3),
             'achieved': round(gbs, 1), 'unit': 'GB/s'}
+
+
+def gram_roofline(torch, O, dev):
+    """tcgen05 split-BF16 Gram of the NLL configuration, X [4096, 3072]: X X^T / D."""
+    x = torch.randn((4096, 3072), device=dev)
+    ts = []
+    for i in range(4):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        O.gram(x, x, 1)
+        b.record()
+        torch.cuda.synchronize()
+        if i:
+            ts.append(a.elapsed_time(b))
+    ms = statistics.median(ts)
+    flops = 2 * 4096 * 4096 * 3072
+    return {'kernel': 'gram_tc_kernel (+ bf16 split)', 'shape': [4096, 4096, 3072], 'ms': round(ms, 3),
+            'tflops_fp32_equivalent': round(flops / (ms / 1e3) / 1e12, 1),
+            'tensor_tflops_issued': round(3 * flops / (ms / 1e3) / 1e12, 1), 'unit': 'TFLOP/s'}
 
 
 REF_TILE = 4
