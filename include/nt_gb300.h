@@ -217,6 +217,60 @@ int ntg_chol_solve(void* stream, const float* A, const float* L, const double* l
                    const float* B, int64_t m, float* X, int32_t refine_iters, void* workspace,
                    size_t workspace_bytes, double* final_residual);
 
+/* ---- adjoints (reverse mode; the jax.custom_vjp backward rules) -------- */
+/* Derivative conventions follow the reference's custom JVPs: the square root
+ * of elementwise.py:1278-1290 has derivative 0 at arguments <= 1e-30, and the
+ * arctan2 of :1293-1310 divides by max(x^2 + y^2, 1e-30). */
+/* VJP of the activation rule on [B, M] kernels (layout as ntg_affine_act):
+ * q, t are the pre-activation nngp/ntk (t may be NULL), gq, gt the output
+ * cotangents (either may be NULL); writes the cotangents of q (oq) and t (ot,
+ * may be NULL) and ADDS the variance cotangents into gvar1 / gvar2 (compact
+ * [n, A, C] device arrays; NULL to skip). */
+int ntg_act_bwd(void* stream, const float* q, const float* t, const float* gq, const float* gt,
+                float* oq, float* ot, int64_t batch, int64_t n2, int64_t a, int64_t c,
+                int32_t diag_spatial, ntg_act_t act, ntg_var_t var1, ntg_var_t var2,
+                float* gvar1, float* gvar2);
+/* Cotangents of the unscaled stencil sums U, Ut of an affine rule evaluated
+ * as q = aff.w2 * scale * U + b2, t = ntk_w2 * scale * Ut + ... (n entries). */
+int ntg_affine_bwd(void* stream, const float* gq, const float* gt, float* gu, float* gut,
+                   int64_t n, ntg_affine_t aff, float scale);
+/* Hyperparameter cotangent sums of an NTK-parameterised affine rule from its
+ * outputs (q, t) and their cotangents: out[0] += d/d(W^2), out[1] += d/d(b^2)
+ * (two device doubles, accumulated). */
+int ntg_affine_hyper_bwd(void* stream, const float* q, const float* t, const float* gq,
+                         const float* gt, int64_t n, float w2, float b2, double* out);
+/* Transpose of the Conv stencil sum (full spatial [B, A, A, C, C] or diagonal
+ * spatial [B, A, C]): geometry as ntg_conv_fs. */
+int ntg_stencil_bwd(void* stream, const float* gu, float* gin, int64_t batch, int64_t a,
+                    int64_t c, int32_t fh, int32_t fw, int32_t sh, int32_t sw, int32_t ph,
+                    int32_t pw, int64_t ao, int64_t co, int32_t pad_mode, int32_t diag_spatial);
+/* Transpose of ntg_pool (windows up to 6 per axis). */
+int ntg_pool_bwd(void* stream, const float* gout, float* gin, int64_t batch, int64_t a, int64_t c,
+                 int32_t wa, int32_t wc, int32_t sa, int32_t sc, int32_t pa, int32_t pc,
+                 int64_t ao, int64_t co, int32_t pad_mode, int32_t diag_spatial, int32_t average,
+                 int32_t normalize_edges);
+/* Transpose of the readouts: gin[b, m] = gout[b] * scale on all m entries
+ * (global pooling) or only on the spatial diagonal (flatten_fs = 1, Flatten). */
+int ntg_readout_bwd(void* stream, const float* gout, float* gin, int64_t batch, int64_t a,
+                    int64_t c, int32_t flatten_fs, int64_t m, float scale);
+/* Image cotangents through ntg_input_fs: ADDS into gx [nself, A, C, K]; side 0
+ * treats the cotangent g as indexed by (self, other) pairs, side 1 as
+ * (other, self); n2 == 0 for the per-sample covariance (pairs (i, i)). */
+int ntg_input_fs_bwd(void* stream, const float* g, const float* x_other, float* gx,
+                     int64_t nself, int64_t nother, int64_t n2, int64_t a, int64_t c, int64_t k,
+                     int32_t side);
+/* C [m, n] (+)= alpha op(A) B, op(A) = A [m, k] or, trans_a != 0, A^T with A [k, m]
+ * (flat Gram adjoint). */
+int ntg_gemm_ex(void* stream, const float* a, const float* b, float* c, int64_t m, int64_t n,
+                int64_t k, int32_t trans_a, float alpha, int32_t accumulate);
+/* dst[i*s_n + a*s_a + c*s_c] += src[i, a, c]: folds variance cotangents
+ * [n, A, C] into the diagonal of a per-sample kernel cotangent. */
+int ntg_diag_add(void* stream, const float* src, float* dst, int64_t n, int64_t a, int64_t c,
+                 int64_t s_n, int64_t s_a, int64_t s_c);
+/* gx [n, d] += 2 gcov[i] x[i, :] / d (adjoint of ntg_cov_diag). */
+int ntg_cov_diag_bwd(void* stream, const float* gcov, const float* x, float* gx, int64_t n,
+                     int64_t d);
+
 /* No counterpart in the reference. ntg_chol_solve without a caller workspace,
  * for callers that cannot allocate device memory where they call the solve
  * (a handler inside a captured CUDA graph, a server that reserved all device

@@ -1,0 +1,511 @@
+"""Reverse-mode differentiation of kernel_fn: one torch.autograd.Function per
+layer rule, the counterpart of a ``jax.custom_vjp`` pair. Each forward calls
+the layer's sm_103a kernels, each backward its hand-written adjoint kernels
+(csrc/ntg_bwd.cu); gradients flow to the inputs x1, x2 and to W_std / b_std
+given as tensors. Scope: full-spatial or flat kernels, NTK parameterisation.
+"""
+from __future__ import annotations
+
+import math
+from typing import Optional
+
+import torch
+
+from . import _lib as L
+from . import _ops as O
+from .kernel import Kernel, from_physical, to_physical
+
+
+def _e(dev) -> torch.Tensor:
+    return torch.empty(0, device=dev)
+
+
+def _opt(t: Optional[torch.Tensor]) -> Optional[torch.Tensor]:
+    return None if t is None or t.numel() == 0 else t
+
+
+def _zero_ntk(t: Optional[torch.Tensor]) -> bool:
+    return t is not None and t.ndim == 0
+
+
+def _ac(x: torch.Tensor, bnd: int) -> tuple[int, int]:
+    sp = x.shape[bnd:]
+    if len(sp) == 0:
+        return 1, 1
+    if len(sp) == 2:
+        return sp[0], 1
+    return sp[0], sp[2]
+
+
+def _as4(x: Optional[torch.Tensor], bnd: int):
+    """View a kernel as [lead, A, A, C, C] (C = 1 for one spatial dimension)."""
+    if x is None:
+        return None
+    a, c = _ac(x, bnd)
+    return x.reshape(tuple(x.shape[:bnd]) + (a, a, c, c))
+
+
+def _batch(x: torch.Tensor, bnd: int) -> int:
+    return int(math.prod(x.shape[:bnd]))
+
+
+def _f(x) -> float:
+    return float(x.item()) if isinstance(x, torch.Tensor) else float(x)
+
+
+# ---------------------------------------------------------------------------
+class InputFn(torch.autograd.Function):
+    """requirements.py:641-830: inputs -> (nngp, cov1, cov2)."""
+
+    @staticmethod
+    def forward(ctx, x1, x2):
+        x2o = _opt(x2)
+        xb = x1 if x2o is None else x2o
+        if x1.ndim == 2:
+            nngp = O.gram(x1, xb, 0)
+            cov1 = torch.diagonal(nngp).contiguous() if x2o is None else O.cov_diag(x1)
+            cov2 = _e(x1.device) if x2o is None else O.cov_diag(x2o)
+        else:
+            y1 = x1 if x1.ndim == 4 else x1.unsqueeze(2)
+            yb = xb if xb.ndim == 4 else xb.unsqueeze(2)
+            nngp = O.input_fs(y1, yb)
+            cov1 = O.input_fs(y1, None)
+            cov2 = _e(x1.device) if x2o is None else O.input_fs(yb, None)
+            if x1.ndim == 3:
+                a = x1.shape[1]
+                nngp = nngp.reshape(nngp.shape[0], nngp.shape[1], a, a)
+                cov1 = cov1.reshape(cov1.shape[0], a, a)
+                if x2o is not None:
+                    cov2 = cov2.reshape(cov2.shape[0], a, a)
+        ctx.save_for_backward(x1, x2)
+        return nngp, cov1, cov2
+
+    @staticmethod
+    def backward(ctx, gn, gc1, gc2):
+        x1, x2 = ctx.saved_tensors
+        x2o = _opt(x2)
+        s = L.stream()
+        gx1 = torch.zeros_like(x1)
+        gx2 = None if x2o is None else torch.zeros_like(x2o)
+        gn = gn.contiguous()
+        if x1.ndim == 2:
+            n1, d = x1.shape
+            xb = x1 if x2o is None else x2o
+            n2 = xb.shape[0]
+            L.call('ntg_gemm_ex', s, L.ptr(gn), L.ptr(xb), L.ptr(gx1), n1, d, n2, 0, 1. / d, 1)
+            L.call('ntg_gemm_ex', s, L.ptr(gn), L.ptr(x1),
+                   L.ptr(gx1 if x2o is None else gx2), n2, d, n1, 1, 1. / d, 1)
+            L.call('ntg_cov_diag_bwd', s, L.ptr(gc1.contiguous()), L.ptr(x1), L.ptr(gx1), n1, d)
+            if x2o is not None:
+                L.call('ntg_cov_diag_bwd', s, L.ptr(gc2.contiguous()), L.ptr(x2o), L.ptr(gx2),
+                       n2, d)
+            return gx1, gx2
+        y1 = x1 if x1.ndim == 4 else x1.unsqueeze(2)
+        yb = None if x2o is None else (x2o if x2o.ndim == 4 else x2o.unsqueeze(2))
+        gy1 = gx1 if x1.ndim == 4 else gx1.unsqueeze(2)
+        gyb = None if gx2 is None else (gx2 if x2o.ndim == 4 else gx2.unsqueeze(2))
+        n1, a, c, k = y1.shape
+        other = y1 if yb is None else yb
+        n2 = other.shape[0]
+        L.call('ntg_input_fs_bwd', s, L.ptr(gn), L.ptr(other), L.ptr(gy1), n1, n2, n2, a, c, k, 0)
+        L.call('ntg_input_fs_bwd', s, L.ptr(gn), L.ptr(y1), L.ptr(gy1 if yb is None else gyb),
+               n2, n1, n2, a, c, k, 1)
+        for gcv, yy, gg in ((gc1, y1, gy1), (gc2, yb, gyb)):
+            if yy is None:
+                continue
+            gcv = gcv.contiguous()
+            m = yy.shape[0]
+            L.call('ntg_input_fs_bwd', s, L.ptr(gcv), L.ptr(yy), L.ptr(gg), m, m, 0, a, c, k, 0)
+            L.call('ntg_input_fs_bwd', s, L.ptr(gcv), L.ptr(yy), L.ptr(gg), m, m, 0, a, c, k, 1)
+        return gx1, gx2
+
+
+# ---------------------------------------------------------------------------
+def _hyper(outs, grads, w2, b2, dev):
+    acc = torch.zeros(2, device=dev, dtype=torch.float64)
+    s = L.stream()
+    for (q, t), (gq, gt) in zip(outs, grads):
+        if q is None or gq is None:
+            continue
+        L.call('ntg_affine_hyper_bwd', s, L.ptr(q), None if t is None else L.ptr(t),
+               L.ptr(gq.contiguous()), None if gt is None else L.ptr(gt.contiguous()),
+               q.numel(), w2, b2, acc.data_ptr())
+    return acc
+
+
+class AffineFn(torch.autograd.Function):
+    """Dense rule (linear.py:899-926) on all four tensors, NTK parameterisation."""
+
+    @staticmethod
+    def forward(ctx, w2t, b2t, q, t, c1, c2):
+        w2, b2 = _f(w2t), _f(b2t)
+        aff = O.affine(w2, b2, w2)
+        zero_t = _zero_ntk(t)
+        c2o = _opt(c2)
+
+        def aa(x, xt, want_t, bnd):
+            a, c = _ac(x, bnd)
+            return O.affine_act(x.contiguous(), xt, _batch(x, bnd), 0, a, c, False, True, aff,
+                                O.NO_ACT, O.NO_VAR, O.NO_VAR, want_t)
+
+        qn, tn = aa(q, None if zero_t else t.contiguous(), True, 2)
+        c1n, _ = aa(c1, None, False, 1)
+        c2n = _e(q.device) if c2o is None else aa(c2o, None, False, 1)[0]
+        ctx.save_for_backward(qn, tn, c1n, c2n)
+        ctx.w2, ctx.b2, ctx.zero_t = w2, b2, zero_t
+        return qn, tn, c1n, c2n
+
+    @staticmethod
+    def backward(ctx, gq, gt, gc1, gc2):
+        qn, tn, c1n, c2n = ctx.saved_tensors
+        w2, b2 = ctx.w2, ctx.b2
+        aff = O.affine(w2, b2, w2)
+        s = L.stream()
+
+        def bwd(g, gtt, n):
+            gu = torch.empty(n, device=qn.device)
+            gut = torch.empty(n, device=qn.device) if gtt is not None else None
+            L.call('ntg_affine_bwd', s, None if g is None else L.ptr(g.contiguous()),
+                   None if gtt is None else L.ptr(gtt.contiguous()), L.ptr(gu),
+                   None if gut is None else L.ptr(gut), n, aff, 1.)
+            return gu, gut
+
+        gu, gut = bwd(gq, gt, qn.numel())
+        gc1i = bwd(gc1, None, c1n.numel())[0].reshape(c1n.shape)
+        gc2i = None if c2n.numel() == 0 else bwd(gc2, None, c2n.numel())[0].reshape(c2n.shape)
+        acc = _hyper([(qn, tn), (c1n, None), (_opt(c2n), None)], [(gq, gt), (gc1, None),
+                     (gc2 if c2n.numel() else None, None)], w2, b2, qn.device)
+        gw2 = acc[0].float()
+        gb2 = acc[1].float()
+        return (gw2, gb2, gu.reshape(qn.shape), None if ctx.zero_t else gut.reshape(qn.shape),
+                gc1i, gc2i)
+
+
+class ConvFn(torch.autograd.Function):
+    """Full-spatial Conv rule (linear.py:1321-1424), NTK parameterisation."""
+
+    @staticmethod
+    def forward(ctx, w2t, b2t, q, t, c1, c2, geom):
+        w2, b2 = _f(w2t), _f(b2t)
+        aff = O.affine(w2, b2, w2)
+        fh, fw, sh, sw, ph, pw, ao, co, circ, nsp = geom
+        zero_t = _zero_ntk(t)
+        c2o = _opt(c2)
+
+        def conv(x, xt, want_t, bnd):
+            x4 = _as4(x.contiguous(), bnd)
+            a, c = _ac(x, bnd)
+            n2 = 0 if bnd == 1 else x.shape[1]
+            lead = tuple(x.shape[:bnd])
+            r = O.conv_fs(x4, None if xt is None else _as4(xt.contiguous(), bnd),
+                          _batch(x, bnd), n2, a, c, fh, fw, sh, sw, ph, pw, ao, co, circ, aff,
+                          O.NO_ACT, O.NO_VAR, O.NO_VAR, want_t, lead)
+            if nsp == 1:
+                r = tuple(None if y is None else y.reshape(lead + (ao, ao)) for y in r)
+            return r
+
+        qn, tn = conv(q, None if zero_t else t, True, 2)
+        c1n = conv(c1, None, False, 1)[0]
+        c2n = _e(q.device) if c2o is None else conv(c2o, None, False, 1)[0]
+        ctx.save_for_backward(qn, tn, c1n, c2n)
+        ctx.meta = (w2, b2, zero_t, geom, tuple(q.shape), tuple(c1.shape),
+                    None if c2o is None else tuple(c2o.shape))
+        return qn, tn, c1n, c2n
+
+    @staticmethod
+    def backward(ctx, gq, gt, gc1, gc2):
+        qn, tn, c1n, c2n = ctx.saved_tensors
+        w2, b2, zero_t, geom, qs, c1s, c2s = ctx.meta
+        fh, fw, sh, sw, ph, pw, ao, co, circ, nsp = geom
+        aff = O.affine(w2, b2, w2)
+        scale = 1. / (fh * fw)
+        s = L.stream()
+        dev = qn.device
+
+        def back(g, gtt, in_shape, bnd):
+            n = int(math.prod(g.shape)) if g is not None else int(math.prod(gtt.shape))
+            gu = torch.empty(n, device=dev)
+            gut = torch.empty(n, device=dev) if gtt is not None else None
+            L.call('ntg_affine_bwd', s, None if g is None else L.ptr(g.contiguous()),
+                   None if gtt is None else L.ptr(gtt.contiguous()), L.ptr(gu),
+                   None if gut is None else L.ptr(gut), n, aff, scale)
+            lead = in_shape[:bnd]
+            a = in_shape[bnd]
+            c = in_shape[bnd + 2] if nsp == 2 else 1
+            batch = int(math.prod(lead))
+            outs = []
+            for gg in (gu, gut):
+                if gg is None:
+                    outs.append(None)
+                    continue
+                gin = torch.empty(in_shape, device=dev)
+                L.call('ntg_stencil_bwd', s, L.ptr(gg), L.ptr(gin), batch, a, c, fh, fw, sh, sw,
+                       ph, pw, ao, co, int(circ), 0)
+                outs.append(gin)
+            return outs
+
+        gqi, gti = back(gq, None if zero_t else gt, qs, 2)
+        gc1i = back(gc1, None, c1s, 1)[0]
+        gc2i = None if c2s is None else back(gc2, None, c2s, 1)[0]
+        acc = _hyper([(qn, tn), (c1n, None), (_opt(c2n), None)], [(gq, gt), (gc1, None),
+                     (gc2 if c2s is not None else None, None)], w2, b2, dev)
+        return acc[0].float(), acc[1].float(), gqi, gti, gc1i, gc2i, None
+
+
+# ---------------------------------------------------------------------------
+def _diag_view(cov: torch.Tensor) -> L.Var:
+    return O.var_view(_as4(cov, 1) if cov.ndim > 1 else cov, False)
+
+
+class ActFn(torch.autograd.Function):
+    """Activation rule (elementwise.py:423-477 ABRelu, :67-112 Erf) on all four tensors."""
+
+    @staticmethod
+    def forward(ctx, q, t, c1, c2, act):
+        c2o = _opt(c2)
+        zero_t = _zero_ntk(t)
+        a, c = _ac(q, 2)
+        q4, c14 = _as4(q.contiguous(), 2), _as4(c1.contiguous(), 1)
+        c24 = None if c2o is None else _as4(c2o.contiguous(), 1)
+        v1 = _diag_view(c14)
+        v2 = _diag_view(c24 if c24 is not None else c14)
+        n1, n2 = q.shape[0], q.shape[1]
+        t4 = None if zero_t else _as4(t.contiguous(), 2)
+        qn, tn = O.affine_act(q4, t4, n1 * n2, n2, a, c, False, False, O.IDENTITY_AFFINE, act, v1,
+                              v2, not zero_t)
+
+        def self_act(cv):
+            vv = _diag_view(cv)
+            return O.affine_act(cv, None, cv.shape[0], 0, a, c, False, False, O.IDENTITY_AFFINE,
+                                act, vv, vv, False)[0]
+
+        c1n = self_act(c14)
+        c2n = _e(q.device) if c24 is None else self_act(c24)
+        ctx.save_for_backward(q, t if not zero_t else _e(q.device), c1, c2)
+        ctx.act, ctx.zero_t = act, zero_t
+        tout = t.clone() if zero_t else tn.reshape(q.shape)
+        return (qn.reshape(q.shape), tout, c1n.reshape(c1.shape),
+                c2n if c2o is None else c2n.reshape(c2o.shape))
+
+    @staticmethod
+    def backward(ctx, gq, gt, gc1, gc2):
+        q, t, c1, c2 = ctx.saved_tensors
+        act, zero_t = ctx.act, ctx.zero_t
+        c2o = _opt(c2)
+        s = L.stream()
+        a, c = _ac(q, 2)
+        n1, n2 = q.shape[0], q.shape[1]
+        q4, c14 = _as4(q.contiguous(), 2), _as4(c1.contiguous(), 1)
+        c24 = None if c2o is None else _as4(c2o.contiguous(), 1)
+        v1 = _diag_view(c14)
+        v2 = _diag_view(c24 if c24 is not None else c14)
+        gd1 = torch.zeros((n1, a, c), device=q.device)
+        gd2 = gd1 if c24 is None else torch.zeros((c24.shape[0], a, c), device=q.device)
+        gqi = torch.empty_like(q4)
+        gti = None if zero_t else torch.empty_like(q4)
+        t4 = None if zero_t else _as4(t.contiguous(), 2)
+        L.call('ntg_act_bwd', s, L.ptr(q4), None if t4 is None else L.ptr(t4),
+               None if gq is None else L.ptr(_as4(gq.contiguous(), 2)),
+               None if (gt is None or zero_t) else L.ptr(_as4(gt.contiguous(), 2)),
+               L.ptr(gqi), None if gti is None else L.ptr(gti), n1 * n2, n2, a, c, 0, act, v1, v2,
+               gd1.data_ptr(), gd2.data_ptr())
+
+        def self_back(cv, gcv, gd):
+            vv = _diag_view(cv)
+            out = torch.empty_like(cv)
+            L.call('ntg_act_bwd', s, L.ptr(cv), None,
+                   None if gcv is None else L.ptr(_as4(gcv.contiguous(), 1) if cv.ndim > 1 else
+                                                  gcv.contiguous()),
+                   None, L.ptr(out), None, cv.shape[0], 0, a, c, 0, act, vv, vv,
+                   gd.data_ptr(), gd.data_ptr())
+            L.call('ntg_diag_add', s, gd.data_ptr(), L.ptr(out), cv.shape[0], a, c, vv.s_n, vv.s_a,
+                   vv.s_c)
+            return out
+
+        # The pair VJP has already added its variance cotangents into gd1/gd2;
+        # each self VJP adds its own and folds the total into its diagonal.
+        gc1i = self_back(c14, gc1, gd1).reshape(c1.shape)
+        gc2i = None if c24 is None else self_back(c24, gc2, gd2).reshape(c2o.shape)
+        return (gqi.reshape(q.shape), None if zero_t else gti.reshape(q.shape), gc1i, gc2i, None)
+
+
+# ---------------------------------------------------------------------------
+class PoolFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, q, t, c1, c2, geom):
+        a, c, wa, wc, sa, sc, pa, pc, ao, co, circ, avg, ne, two_d = geom
+
+        def run(x, bnd):
+            if x is None or x.ndim == 0 or x.numel() == 0:
+                return x
+            lead = tuple(x.shape[:bnd])
+            shape = lead + ((ao, ao, co, co) if two_d else (ao, ao))
+            return O.pool(x.contiguous(), int(math.prod(lead)), a, c, wa, wc, sa, sc, pa, pc, ao,
+                          co, circ, False, avg, ne, shape)
+
+        ctx.geom = geom
+        ctx.shapes = [None if x is None else tuple(x.shape) for x in (q, t, c1, c2)]
+        return run(q, 2), run(t, 2), run(c1, 1), run(c2, 1)
+
+    @staticmethod
+    def backward(ctx, gq, gt, gc1, gc2):
+        a, c, wa, wc, sa, sc, pa, pc, ao, co, circ, avg, ne, two_d = ctx.geom
+        s = L.stream()
+        outs = []
+        for g, shp, bnd in zip((gq, gt, gc1, gc2), ctx.shapes, (2, 2, 1, 1)):
+            if g is None or shp is None or len(shp) == 0 or int(math.prod(shp)) == 0:
+                outs.append(None)
+                continue
+            gin = torch.empty(shp, device=g.device)
+            L.call('ntg_pool_bwd', s, L.ptr(g.contiguous()), L.ptr(gin),
+                   int(math.prod(shp[:bnd])), a, c, wa, wc, sa, sc, pa, pc, ao, co, int(circ), 0,
+                   int(avg), int(ne))
+            outs.append(gin)
+        return (*outs, None)
+
+
+class ReadoutFn(torch.autograd.Function):
+    """GlobalAvgPool / GlobalSumPool (linear.py:1771-1801) and Flatten (:1865-1899)."""
+
+    @staticmethod
+    def forward(ctx, q, t, c1, c2, kind):
+        def run(x, bnd):
+            if x is None or x.ndim <= bnd or x.numel() == 0:
+                return x
+            if kind == 'flatten':
+                a, c = _ac(x, bnd)
+                return O.flatten_fs(_as4(x.contiguous(), bnd), bnd, a, c)
+            return O.global_pool(x.contiguous(), bnd, kind == 'avg', 1.)
+
+        ctx.kind = kind
+        ctx.shapes = [None if x is None else tuple(x.shape) for x in (q, t, c1, c2)]
+        return run(q, 2), run(t, 2), run(c1, 1), run(c2, 1)
+
+    @staticmethod
+    def backward(ctx, gq, gt, gc1, gc2):
+        s = L.stream()
+        outs = []
+        for g, shp, bnd in zip((gq, gt, gc1, gc2), ctx.shapes, (2, 2, 1, 1)):
+            if g is None or shp is None or len(shp) <= bnd or int(math.prod(shp)) == 0:
+                outs.append(g if (shp is not None and len(shp) <= bnd) else None)
+                continue
+            m = int(math.prod(shp[bnd:]))
+            a = shp[bnd]
+            c = shp[bnd + 2] if len(shp) == bnd + 4 else 1
+            gin = torch.empty(shp, device=g.device)
+            if ctx.kind == 'flatten':
+                L.call('ntg_readout_bwd', s, L.ptr(g.contiguous()), L.ptr(gin),
+                       int(math.prod(shp[:bnd])), a, c, 1, m, 1. / (a * c))
+            else:
+                L.call('ntg_readout_bwd', s, L.ptr(g.contiguous()), L.ptr(gin),
+                       int(math.prod(shp[:bnd])), a, c, 0, m, 1. / m if ctx.kind == 'avg' else 1.)
+            outs.append(gin)
+        return (*outs, None)
+
+
+# ---------------------------------------------------------------------------
+def needs_grad(specs, *xs) -> bool:
+    if not torch.is_grad_enabled():
+        return False
+    if any(isinstance(x, torch.Tensor) and x.requires_grad for x in xs):
+        return True
+    for sp in specs:
+        for key in ('W_std', 'b_std'):
+            v = sp.params.get(key)
+            if isinstance(v, torch.Tensor) and v.requires_grad:
+                return True
+    return False
+
+
+def _sq(v, dev):
+    if v is None:
+        return torch.zeros((), device=dev)
+    if isinstance(v, torch.Tensor):
+        return (v.to(dev, torch.float32) ** 2).reshape(())
+    return torch.tensor(float(v) ** 2, device=dev)
+
+
+def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: bool) -> Kernel:
+    """kernel_fn(x1, x2) through the differentiable layer Functions."""
+    from .stax import Padding, _act_struct, _Ctx, _pads
+    dev = x1.device
+    ctx = _Ctx('fp32')
+    if x1.ndim > 4:
+        raise NotImplementedError('nt_gb300 supports at most two spatial dimensions')
+    if specs and specs[0].channel_axis_none and x1.ndim > 2:
+        x1 = x1.reshape(x1.shape[0], -1)
+        x2 = None if x2 is None else x2.reshape(x2.shape[0], -1)
+    shape1 = tuple(x1.shape)
+    shape2 = shape1 if x2 is None else tuple(x2.shape)
+    q, c1, c2 = InputFn.apply(x1, _e(dev) if x2 is None else x2)
+    t = torch.zeros((), device=dev) if compute_ntk else None
+    is_gaussian, is_reversed = False, False
+    for sp in specs:
+        p = sp.params
+        if sp.kind == 'identity':
+            pass
+        elif sp.kind in ('dense', 'conv'):
+            if p['parameterization'] != 'ntk':
+                raise NotImplementedError('gradients need the NTK parameterisation')
+            w2, b2 = _sq(p['W_std'], dev), _sq(p['b_std'], dev)
+            tt = t if t is not None else torch.zeros((), device=dev)
+            if sp.kind == 'dense':
+                q, tt, c1, c2 = AffineFn.apply(w2, b2, q, tt, c1, c2)
+            else:
+                nsp = len(p['filter_shape'])
+                if nsp > 2:
+                    raise NotImplementedError('Conv with 1 or 2 spatial dimensions')
+                a, c = _ac(q, 2)
+                fh, sh = p['filter_shape'][0], p['strides'][0]
+                fw, sw = (p['filter_shape'][1], p['strides'][1]) if nsp == 2 else (1, 1)
+                ph, ao = _pads(a, fh, sh, p['padding'])
+                pw, co = _pads(c, fw, sw, p['padding']) if nsp == 2 else (0, 1)
+                geom = (fh, fw, sh, sw, ph, pw, ao, co, p['padding'] == Padding.CIRCULAR, nsp)
+                q, tt, c1, c2 = ConvFn.apply(w2, b2, q, tt, c1, c2, geom)
+                is_reversed = not is_reversed
+            t = tt if t is not None else None
+            is_gaussian = True
+        elif sp.kind == 'act':
+            if not is_gaussian:
+                raise ValueError('The input to the activation function must be Gaussian, '
+                                 'i.e. a random affine transform is required before the '
+                                 'activation function.')
+            if p.get('do_stabilize'):
+                raise NotImplementedError('do_stabilize is not differentiable here')
+            tt = t if t is not None else torch.zeros((), device=dev)
+            q, tt, c1, c2 = ActFn.apply(q, tt, c1, c2, _act_struct(p, ctx))
+            t = tt if t is not None else None
+            is_gaussian = False
+        elif sp.kind == 'pool':
+            a, c = _ac(q, 2)
+            ws, st = p['window_shape'], p['strides']
+            two_d = len(ws) == 2
+            wa, sa = ws[0], st[0]
+            wc, sc = (ws[1], st[1]) if two_d else (1, 1)
+            pa, ao = _pads(a, wa, sa, p['padding'])
+            pc, co = _pads(c, wc, sc, p['padding']) if two_d else (0, 1)
+            ne = bool(p['normalize_edges']) and p['padding'] == Padding.SAME
+            geom = (a, c, wa, wc, sa, sc, pa, pc, ao, co, p['padding'] == Padding.CIRCULAR,
+                    p['pool'] == 'avg', ne, two_d)
+            tt = t if (t is not None and t.ndim > 0) else None
+            q, tt2, c1, c2 = PoolFn.apply(q, tt, c1, c2, geom)
+            t = tt2 if tt is not None else t
+        elif sp.kind in ('gpool', 'flatten'):
+            kind = 'flatten' if sp.kind == 'flatten' else p['pool']
+            tt = t if (t is not None and t.ndim > 0) else None
+            q, tt2, c1, c2 = ReadoutFn.apply(q, tt, c1, c2, kind)
+            t = tt2 if tt is not None else t
+            is_reversed = False
+            if sp.kind == 'flatten':
+                is_gaussian = False
+        else:
+            raise NotImplementedError(sp.kind)
+        shape1, shape2 = sp.shape_fn(shape1), sp.shape_fn(shape2)
+    c2o = _opt(c2)
+    return Kernel(nngp=from_physical(q, 2, is_reversed, False),
+                  ntk=from_physical(t, 2, is_reversed, False) if compute_ntk else None,
+                  cov1=from_physical(c1, 1, is_reversed, False),
+                  cov2=None if c2o is None else from_physical(c2o, 1, is_reversed, False),
+                  x1_is_x2=x2 is None, is_gaussian=is_gaussian, is_reversed=is_reversed,
+                  is_input=False, diagonal_batch=True, diagonal_spatial=False, shape1=shape1,
+                  shape2=shape2)

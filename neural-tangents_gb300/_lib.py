@@ -73,6 +73,19 @@ SIGNATURES = {
     'ntg_flatten_fs': ([_P, _P, _P, _I64, _I64, _I64], C.c_int),
     'ntg_chain_fwd': ([_P, C.POINTER(Chain), _P, _P, _I64, _I64, _I64, _I64, _P, _P, _P, _P,
                        _I64], C.c_int),
+    'ntg_act_bwd': ([_P, _P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, _I32, Act, Var, Var, _P,
+                     _P], C.c_int),
+    'ntg_affine_bwd': ([_P, _P, _P, _P, _P, _I64, Affine, _F], C.c_int),
+    'ntg_affine_hyper_bwd': ([_P, _P, _P, _P, _P, _I64, _F, _F, _P], C.c_int),
+    'ntg_stencil_bwd': ([_P, _P, _P, _I64, _I64, _I64, _I32, _I32, _I32, _I32, _I32, _I32, _I64,
+                         _I64, _I32, _I32], C.c_int),
+    'ntg_pool_bwd': ([_P, _P, _P, _I64, _I64, _I64, _I32, _I32, _I32, _I32, _I32, _I32, _I64,
+                      _I64, _I32, _I32, _I32, _I32], C.c_int),
+    'ntg_readout_bwd': ([_P, _P, _P, _I64, _I64, _I64, _I32, _I64, _F], C.c_int),
+    'ntg_input_fs_bwd': ([_P, _P, _P, _P, _I64, _I64, _I64, _I64, _I64, _I64, _I32], C.c_int),
+    'ntg_gemm_ex': ([_P, _P, _P, _P, _I64, _I64, _I64, _I32, _F, _I32], C.c_int),
+    'ntg_cov_diag_bwd': ([_P, _P, _P, _P, _I64, _I64], C.c_int),
+    'ntg_diag_add': ([_P, _P, _P, _I64, _I64, _I64, _I64, _I64, _I64], C.c_int),
     'ntg_chol_factor': ([_P, _P, _I64, C.c_double, _I32, _P, _P, _P], C.c_int),
     'ntg_chol_workspace_bytes': ([_I64, _I64], C.c_size_t),
     'ntg_chol_solve': ([_P, _P, _P, _P, _I64, _P, _I64, _P, _I32, _P, C.c_size_t, _P], C.c_int),

@@ -1,0 +1,626 @@
+// Adjoints (vector-Jacobian products) of the layer rules, for reverse-mode
+// differentiation of kernel_fn with respect to its inputs and to W_std / b_std.
+// The derivative conventions follow the reference's custom JVPs:
+// _sqrt (elementwise.py:1278-1290) has derivative 0 where its argument is
+// <= 1e-30, and _arctan2 (:1293-1310) divides by max(x^2 + y^2, 1e-30).
+#include <cstdio>
+
+#include "ntg_common.cuh"
+
+namespace ntg {
+namespace {
+
+constexpr int kT = 256;
+
+__device__ __forceinline__ void pair_of(int64_t b, int64_t n2, int64_t& i1, int64_t& i2) {
+  if (n2 > 0) {
+    i1 = b / n2;
+    i2 = b - i1 * n2;
+  } else {
+    i1 = b;
+    i2 = b;
+  }
+}
+
+struct VarGrad {
+  float* base;
+  int64_t s_n, s_a, s_c;
+};
+
+__device__ __forceinline__ void vg_add(const VarGrad& g, int64_t n, int64_t a, int64_t c, float v) {
+  if (g.base && v != 0.f) atomicAdd(g.base + n * g.s_n + a * g.s_a + c * g.s_c, v);
+}
+
+// VJP of the activation rule at one entry: given the pre-activation (q, t) and
+// variances (v1, v2) and the output cotangents (gq, gt), returns the
+// cotangents of q, t, v1, v2.
+__device__ __forceinline__ void act_vjp(const ntg_act_t& act, float q, float t, float v1,
+                                        float v2, float gq, float gt, float& oq, float& ot,
+                                        float& ov1, float& ov2) {
+  const float tol = 1e-30f;
+  if (act.kind == NTG_ACT_ABRELU) {
+    const float a = act.a, b = act.b;
+    const float factor = (a - b) * (a - b) / (2.f * kPi);
+    const float half = 0.5f * (a * a + b * b);
+    const float d = v1 * v2 - q * q;
+    const float s = sqrtf(fmaxf(d, 0.f));
+    const float th = (s == 0.f && q == 0.f) ? 0.5f * kPi : atan2f(s, q);
+    const float dot = half - factor * th;
+    // q' = factor s + dot q ; t' = t dot ; dot = half - factor th
+    const float g_dot = q * gq + t * gt;
+    float g_s = factor * gq;
+    float g_q = dot * gq;
+    ot = dot * gt;
+    const float g_th = -factor * g_dot;
+    const float den = fmaxf(s * s + q * q, tol);
+    g_s += g_th * (q / den);
+    g_q -= g_th * (s / den);
+    const float g_d = (d > tol) ? g_s / (2.f * sqrtf(fmaxf(d, tol))) : 0.f;
+    g_q -= 2.f * q * g_d;
+    ov1 = g_d * v2;
+    ov2 = g_d * v1;
+    oq = g_q;
+  } else if (act.kind == NTG_ACT_ERF) {
+    const float a2 = act.a * act.a, b2 = act.b * act.b;
+    const float qb = b2 * q, tb = b2 * t;
+    const float d1 = 1.f + 2.f * b2 * v1, d2 = 1.f + 2.f * b2 * v2;
+    const float y = 2.f * qb;
+    const float dd = d1 * d2 - y * y;
+    const float s = sqrtf(fmaxf(dd, 0.f));
+    const float gq2 = a2 * gq, gt2 = a2 * gt;
+    const float dot = (4.f / kPi) / s;
+    const float g_tb = dot * gt2;
+    const float g_dot = tb * gt2;
+    float g_s = -(4.f / kPi) / (s * s) * g_dot;
+    const float g_phi = (2.f / kPi) * gq2;
+    const float den = s * s + y * y;  // jnp.arctan2 derivative
+    const float g_y = den > 0.f ? g_phi * s / den : 0.f;
+    g_s += den > 0.f ? -g_phi * y / den : 0.f;
+    float g_qb = 2.f * g_y;
+    const float g_dd = (dd > tol) ? g_s / (2.f * sqrtf(fmaxf(dd, tol))) : 0.f;
+    g_qb -= 2.f * y * g_dd * 2.f;  // d(y^2)/dqb = 2 y * 2
+    const float g_d1 = g_dd * d2, g_d2 = g_dd * d1;
+    oq = b2 * g_qb;
+    ot = b2 * g_tb;
+    ov1 = b2 * 2.f * g_d1;
+    ov2 = b2 * 2.f * g_d2;
+  } else {
+    oq = gq;
+    ot = gt;
+    ov1 = ov2 = 0.f;
+  }
+}
+
+// Activation VJP over [B, M] kernels; variance cotangents are accumulated
+// atomically into gvar1 / gvar2 (same addressing as var1 / var2).
+__global__ void act_bwd_kernel(const float* __restrict__ q, const float* __restrict__ t,
+                               const float* __restrict__ gq, const float* __restrict__ gt,
+                               float* __restrict__ oq, float* __restrict__ ot, int64_t batch,
+                               int64_t n2, int64_t A, int64_t C, int diag, ntg_act_t act,
+                               ntg_var_t var1, ntg_var_t var2, VarGrad gv1, VarGrad gv2) {
+  const int64_t M = diag ? A * C : A * A * C * C;
+  const int64_t total = batch * M;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = idx / M, m = idx - b * M;
+    int64_t a1, a2, c1, c2;
+    if (diag) {
+      a1 = a2 = m / C;
+      c1 = c2 = m - a1 * C;
+    } else {
+      int64_t r = m;
+      c2 = r % C; r /= C;
+      c1 = r % C; r /= C;
+      a2 = r % A;
+      a1 = r / A;
+    }
+    int64_t i1, i2;
+    pair_of(b, n2, i1, i2);
+    const float v1 = var_at(var1, i1, a1, c1), v2 = var_at(var2, i2, a2, c2);
+    float rq, rt, rv1, rv2;
+    act_vjp(act, q[idx], t ? t[idx] : 0.f, v1, v2, gq ? gq[idx] : 0.f, gt ? gt[idx] : 0.f, rq,
+            rt, rv1, rv2);
+    oq[idx] = rq;
+    if (ot) ot[idx] = rt;
+    vg_add(gv1, i1, a1, c1, rv1);
+    vg_add(gv2, i2, a2, c2, rv2);
+  }
+}
+
+// Cotangent of the unscaled stencil sums of a conv/dense affine rule:
+//   q = w2 s U + b2,  t = tw2 s Ut + nn_w (nn_scaled ? q : s U) + c
+// gives  gU = s (w2 (gq + [nn_scaled] nn_w gt) + [!nn_scaled] nn_w gt),  gUt = tw2 s gt.
+__global__ void affine_bwd_kernel(const float* __restrict__ gq, const float* __restrict__ gt,
+                                  float* __restrict__ gu, float* __restrict__ gut, int64_t n,
+                                  ntg_affine_t f, float scale) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float a = gq ? gq[i] : 0.f, b = gt ? gt[i] : 0.f;
+    const float gqq = a + (f.nn_scaled ? f.ntk_nn * b : 0.f);
+    gu[i] = scale * (f.w2 * gqq + (f.nn_scaled ? 0.f : f.ntk_nn * b));
+    if (gut) gut[i] = scale * f.ntk_w2 * b;
+  }
+}
+
+// Sums for the W^2 / b^2 cotangents of an NTK-parameterised affine rule from
+// its outputs: q = W^2 X + b^2, t = W^2 Y + q  =>  dq/dW^2 = X = (q - b^2) / W^2,
+// dt/dW^2 = Y + X = (t - b^2) / W^2, dq/db^2 = dt/db^2 = 1.
+// out[0] += sum(gq X + gt (t - b^2)/W^2), out[1] += sum(gq + gt).
+__global__ void affine_hyper_kernel(const float* __restrict__ q, const float* __restrict__ t,
+                                    const float* __restrict__ gq, const float* __restrict__ gt,
+                                    int64_t n, float w2, float b2, double* __restrict__ out) {
+  double sw = 0.0, sb = 0.0;
+  const float inv = w2 != 0.f ? 1.f / w2 : 0.f;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float g1 = gq ? gq[i] : 0.f;
+    const float g2 = (gt && t) ? gt[i] : 0.f;
+    sw += (double)g1 * (double)((q[i] - b2) * inv);
+    if (g2 != 0.f) sw += (double)g2 * (double)((t[i] - b2) * inv);
+    sb += (double)g1 + (double)g2;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    sw += __shfl_xor_sync(0xffffffffu, sw, o);
+    sb += __shfl_xor_sync(0xffffffffu, sb, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(out, sw);
+    atomicAdd(out + 1, sb);
+  }
+}
+
+__device__ __forceinline__ bool wrap_idx(int64_t& i, int64_t n, int circular) {
+  if (i >= 0 && i < n) return true;
+  if (!circular) return false;
+  i %= n;
+  if (i < 0) i += n;
+  return true;
+}
+
+// Outputs i in [0, no) whose window offset `off` lands on input x:
+// i*s + off - p == x (zero padding) or == x mod n (circular). At most 3.
+__device__ __forceinline__ int candidates(int64_t x, int off, int s, int p, int64_t n, int64_t no,
+                                          int circular, int64_t out[3]) {
+  int cnt = 0;
+  const int k0 = circular ? -1 : 0, k1 = circular ? 1 : 0;
+  for (int k = k0; k <= k1; ++k) {
+    const int64_t pp = x + p + k * n - off;  // = i * s
+    if (pp < 0 || pp % s) continue;
+    const int64_t i = pp / s;
+    if (i < no) out[cnt++] = i;
+  }
+  return cnt;
+}
+
+// Transpose of the full-spatial stencil sum U[o] = sum_{d,e} in[o*s + d - p]:
+// gin[a, a', c, c'] = sum of gU over every output whose window holds (a, a', c, c')
+// (the same offset d on both A axes and e on both C axes).
+__global__ void stencil_t_kernel(const float* __restrict__ gu, float* __restrict__ gin,
+                                 int64_t batch, int64_t A, int64_t C, int64_t Ao, int64_t Co,
+                                 int fh, int fw, int sh, int sw, int ph, int pw, int circular) {
+  const int64_t per_b = A * A * C * C;
+  const int64_t total = batch * per_b;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b = idx / per_b, r = idx - b * per_b;
+    const int64_t cp = r % C; r /= C;
+    const int64_t c = r % C; r /= C;
+    const int64_t ap = r % A;
+    const int64_t a = r / A;
+    const float* g = gu + b * Ao * Ao * Co * Co;
+    float s = 0.f;
+    int64_t ia[3], iap[3], jc[3], jcp[3];
+    for (int d = 0; d < fh; ++d) {
+      const int na = candidates(a, d, sh, ph, A, Ao, circular, ia);
+      const int nap = candidates(ap, d, sh, ph, A, Ao, circular, iap);
+      for (int x = 0; x < na; ++x)
+        for (int y = 0; y < nap; ++y)
+          for (int e = 0; e < fw; ++e) {
+            const int nc = candidates(c, e, sw, pw, C, Co, circular, jc);
+            const int ncp = candidates(cp, e, sw, pw, C, Co, circular, jcp);
+            for (int u = 0; u < nc; ++u)
+              for (int v = 0; v < ncp; ++v)
+                s += g[((ia[x] * Ao + iap[y]) * Co + jc[u]) * Co + jcp[v]];
+          }
+    }
+    gin[idx] = s;
+  }
+}
+
+// Same for a 3x3 / stride 1 / SAME / zero-padded stencil: its transpose is the
+// same 3x3 diagonal box sum.
+__global__ void stencil3_t_kernel(const float* __restrict__ gu, float* __restrict__ gin,
+                                  int64_t batch, int64_t A, int64_t C) {
+  const int64_t per_b = A * A * C * C;
+  const int64_t total = batch * per_b;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b = idx / per_b, r = idx - b * per_b;
+    const int64_t cp = r % C; r /= C;
+    const int64_t c = r % C; r /= C;
+    const int64_t ap = r % A;
+    const int64_t a = r / A;
+    const float* g = gu + b * per_b;
+    float s = 0.f;
+    for (int d = -1; d <= 1; ++d) {
+      const int64_t ia = a + d, iap = ap + d;
+      if (ia < 0 || ia >= A || iap < 0 || iap >= A) continue;
+      for (int e = -1; e <= 1; ++e) {
+        const int64_t jc = c + e, jcp = cp + e;
+        if (jc < 0 || jc >= C || jcp < 0 || jcp >= C) continue;
+        s += g[((ia * A + iap) * C + jc) * C + jcp];
+      }
+    }
+    gin[idx] = s;
+  }
+}
+
+// Diagonal-spatial stencil transpose on [B, A, C].
+__global__ void stencil_ds_t_kernel(const float* __restrict__ gu, float* __restrict__ gin,
+                                    int64_t batch, int64_t A, int64_t C, int64_t Ao, int64_t Co,
+                                    int fh, int fw, int sh, int sw, int ph, int pw,
+                                    int circular) {
+  const int64_t total = batch * A * C;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = idx / (A * C), r = idx - b * A * C;
+    const int64_t a = r / C, c = r - a * C;
+    float s = 0.f;
+    int64_t ia[3], jc[3];
+    for (int d = 0; d < fh; ++d) {
+      const int na = candidates(a, d, sh, ph, A, Ao, circular, ia);
+      for (int x = 0; x < na; ++x)
+        for (int e = 0; e < fw; ++e) {
+          const int nc = candidates(c, e, sw, pw, C, Co, circular, jc);
+          for (int u = 0; u < nc; ++u) s += gu[(b * Ao + ia[x]) * Co + jc[u]];
+        }
+    }
+    gin[idx] = s;
+  }
+}
+
+__device__ __forceinline__ int inbounds(int64_t o, int w, int s, int p, int64_t n) {
+  int cnt = 0;
+  for (int u = 0; u < w; ++u) {
+    const int64_t x = o * s + u - p;
+    if (x >= 0 && x < n) ++cnt;
+  }
+  return cnt;
+}
+
+// Transpose of the pooling rule: every input entry collects the cotangents of
+// the outputs whose window holds it, scaled as in the forward (window offsets
+// are independent on each of the four axes).
+__global__ void pool_t_kernel(const float* __restrict__ gout, float* __restrict__ gin,
+                              int64_t batch, int64_t A, int64_t C, int64_t Ao, int64_t Co, int wa,
+                              int wc, int sa, int sc, int pa, int pc, int circular, int diag,
+                              int average, int normalize_edges) {
+  const int64_t per_b = diag ? A * C : A * A * C * C;
+  const int64_t total = batch * per_b;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b = idx / per_b, r = idx - b * per_b;
+    int64_t a, ap, c, cp;
+    if (diag) {
+      a = ap = r / C;
+      c = cp = r - a * C;
+    } else {
+      cp = r % C; r /= C;
+      c = r % C; r /= C;
+      ap = r % A;
+      a = r / A;
+    }
+    // candidate output indices per axis (over all window offsets)
+    int64_t ca[8], cap[8], cc[8], ccp[8];
+    int na = 0, nap = 0, nc = 0, ncp = 0;
+    int64_t tmp[3];
+    for (int u = 0; u < wa && na < 6; ++u) {
+      int k = candidates(a, u, sa, pa, A, Ao, circular, tmp);
+      for (int x = 0; x < k && na < 8; ++x) ca[na++] = tmp[x];
+    }
+    for (int v = 0; v < wc && nc < 6; ++v) {
+      int k = candidates(c, v, sc, pc, C, Co, circular, tmp);
+      for (int x = 0; x < k && nc < 8; ++x) cc[nc++] = tmp[x];
+    }
+    if (!diag) {
+      for (int u = 0; u < wa && nap < 6; ++u) {
+        int k = candidates(ap, u, sa, pa, A, Ao, circular, tmp);
+        for (int x = 0; x < k && nap < 8; ++x) cap[nap++] = tmp[x];
+      }
+      for (int v = 0; v < wc && ncp < 6; ++v) {
+        int k = candidates(cp, v, sc, pc, C, Co, circular, tmp);
+        for (int x = 0; x < k && ncp < 8; ++x) ccp[ncp++] = tmp[x];
+      }
+    } else {
+      nap = ncp = 1;
+      cap[0] = ccp[0] = 0;
+    }
+    float s = 0.f;
+    const int64_t ob = diag ? b * Ao * Co : b * Ao * Ao * Co * Co;
+    const float full = diag ? (float)(wa * wc) : (float)(wa * wa * wc * wc);
+    for (int x = 0; x < na; ++x)
+      for (int y = 0; y < nap; ++y)
+        for (int u = 0; u < nc; ++u)
+          for (int v = 0; v < ncp; ++v) {
+            const int64_t i = ca[x], ip = cap[y], j = cc[u], jp = ccp[v];
+            float g = diag ? gout[ob + i * Co + j] : gout[ob + ((i * Ao + ip) * Co + j) * Co + jp];
+            if (average) {
+              float norm = full;
+              if (normalize_edges) {
+                int cnt = inbounds(i, wa, sa, pa, A) * inbounds(j, wc, sc, pc, C);
+                if (!diag) cnt *= inbounds(ip, wa, sa, pa, A) * inbounds(jp, wc, sc, pc, C);
+                norm = (float)cnt;
+              }
+              g = g / norm;
+              if (diag) g = g / norm;
+            }
+            s += g;
+          }
+    gin[idx] = s;
+  }
+}
+
+// Broadcast of a readout cotangent: gin[b, m] = gout[b] * scale (mean or sum),
+// or, for Flatten on a full-spatial kernel, only on the spatial diagonal.
+__global__ void readout_t_kernel(const float* __restrict__ gout, float* __restrict__ gin,
+                                 int64_t batch, int64_t A, int64_t C, int flatten_fs,
+                                 int64_t m, float scale) {
+  const int64_t total = batch * m;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = idx / m, r = idx - b * m;
+    float v = gout[b] * scale;
+    if (flatten_fs) {
+      const int64_t cp = r % C, c = (r / C) % C, ap = (r / (C * C)) % A, a = r / (A * C * C);
+      if (a != ap || c != cp) v = 0.f;
+    }
+    gin[idx] = v;
+  }
+}
+
+// Cotangent of the image inputs through the full-spatial input covariance
+// G[b, h, h', w, w'] = sum_k x1[i1, h, w, k] x2[i2, h', w', k] / K:
+//   side 0: gx1[i1, h, w, k] += sum_{pairs with i1, h', w'} G'[..] x2[i2, h', w', k] / K
+//   side 1: gx2[i2, h', w', k] += sum_{pairs with i2, h, w} G'[..] x1[i1, h, w, k] / K
+// One CTA per (sample, row); n2 == 0 means per-sample pairs (i, i).
+__global__ void input_fs_t_kernel(const float* __restrict__ g, const float* __restrict__ xo,
+                                  float* __restrict__ gx, int64_t nself, int64_t nother,
+                                  int64_t n2, int64_t A, int64_t C, int64_t K, int side,
+                                  float inv_k) {
+  const int64_t i = blockIdx.x / A, h = blockIdx.x % A;
+  if (i >= nself) return;
+  extern __shared__ float acc[];  // [C][K]
+  for (int64_t e = threadIdx.x; e < C * K; e += blockDim.x) acc[e] = 0.f;
+  __syncthreads();
+  const int64_t plane = C * C;
+  const int64_t partners = n2 > 0 ? nother : 1;
+  for (int64_t pj = 0; pj < partners; ++pj) {
+    const int64_t j = n2 > 0 ? pj : i;
+    const int64_t b = n2 > 0 ? (side == 0 ? i * n2 + j : j * n2 + i) : i;
+    for (int64_t hp = 0; hp < A; ++hp) {
+      const float* pl = side == 0 ? g + ((b * A + h) * A + hp) * plane
+                                  : g + ((b * A + hp) * A + h) * plane;
+      const float* xr = xo + ((j * A + hp) * C) * K;
+      for (int64_t e = threadIdx.x; e < C * K; e += blockDim.x) {
+        const int64_t w = e / K, k = e - w * K;
+        float s = 0.f;
+        for (int64_t wp = 0; wp < C; ++wp) {
+          const float gv = side == 0 ? pl[w * C + wp] : pl[wp * C + w];
+          s = fmaf(gv, __ldg(xr + wp * K + k), s);
+        }
+        acc[e] += s;
+      }
+    }
+  }
+  __syncthreads();
+  for (int64_t e = threadIdx.x; e < C * K; e += blockDim.x) {
+    const int64_t w = e / K, k = e - w * K;
+    atomicAdd(gx + ((i * A + h) * C + w) * K + k, acc[e] * inv_k);
+  }
+}
+
+// C[m, n] (+)= alpha * op(A) B with op(A) = A [m, k] or A^T (A stored [k, m]).
+__global__ void __launch_bounds__(256) gemm_ex_kernel(const float* __restrict__ A,
+                                                      const float* __restrict__ B,
+                                                      float* __restrict__ Cm, int64_t M, int64_t N,
+                                                      int64_t K, int trans_a, float alpha,
+                                                      int accumulate) {
+  __shared__ float As[16][64 + 4];
+  __shared__ float Bs[16][64 + 4];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t row0 = (int64_t)blockIdx.y * 64, col0 = (int64_t)blockIdx.x * 64;
+  float acc[4][4] = {};
+  for (int64_t k0 = 0; k0 < K; k0 += 16) {
+    for (int idx = threadIdx.x; idx < 16 * 64; idx += 256) {
+      if (trans_a) {
+        const int kk = idx / 64, r = idx % 64;
+        const int64_t gk = k0 + kk, gi = row0 + r;
+        As[kk][r] = (gi < M && gk < K) ? __ldg(A + gk * M + gi) : 0.f;
+      } else {
+        const int r = idx / 16, kk = idx % 16;
+        const int64_t gi = row0 + r, gk = k0 + kk;
+        As[kk][r] = (gi < M && gk < K) ? __ldg(A + gi * K + gk) : 0.f;
+      }
+      const int kb = idx / 64, cb = idx % 64;
+      const int64_t gkb = k0 + kb, gj = col0 + cb;
+      Bs[kb][cb] = (gkb < K && gj < N) ? __ldg(B + gkb * N + gj) : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      float a[4], bb[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        a[u] = As[kk][ty * 4 + u];
+        bb[u] = Bs[kk][tx * 4 + u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], bb[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int64_t gi = row0 + ty * 4 + u, gj = col0 + tx * 4 + v;
+      if (gi < M && gj < N) {
+        const float r = alpha * acc[u][v];
+        Cm[gi * N + gj] = accumulate ? Cm[gi * N + gj] + r : r;
+      }
+    }
+}
+
+// gx[i, :] += 2 gcov[i] x[i, :] / D (adjoint of cov_i = |x_i|^2 / D).
+__global__ void cov_diag_t_kernel(const float* __restrict__ gcov, const float* __restrict__ x,
+                                  float* __restrict__ gx, int64_t n, int64_t d, float two_over_d) {
+  const int64_t total = n * d;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    gx[idx] += two_over_d * gcov[idx / d] * x[idx];
+}
+
+// dst[n, a, a, c, c] (strided diagonal view) += src[n, a, c].
+__global__ void diag_add_kernel(const float* __restrict__ src, float* __restrict__ dst, int64_t n,
+                                int64_t A, int64_t C, int64_t s_n, int64_t s_a, int64_t s_c) {
+  const int64_t total = n * A * C;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx / (A * C), r = idx - i * A * C, a = r / C, c = r - a * C;
+    dst[i * s_n + a * s_a + c * s_c] += src[idx];
+  }
+}
+
+int grid_for(int64_t n) {
+  int64_t g = (n + kT - 1) / kT;
+  if (g > 152 * 64) g = 152 * 64;
+  return (int)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+}  // namespace ntg
+
+using namespace ntg;
+
+extern "C" int ntg_act_bwd(void* stream, const float* q, const float* t, const float* gq,
+                           const float* gt, float* oq, float* ot, int64_t batch, int64_t n2,
+                           int64_t a, int64_t c, int32_t diag_spatial, ntg_act_t act,
+                           ntg_var_t var1, ntg_var_t var2, float* gvar1, float* gvar2) {
+  NTG_REQUIRE(q && oq && var1.base && var2.base, "ntg_act_bwd: null pointer");
+  NTG_REQUIRE(batch > 0 && a > 0 && c > 0, "ntg_act_bwd: bad sizes");
+  NTG_REQUIRE(act.kind != NTG_ACT_ABRELU || act.stabilize <= 0.f,
+              "ntg_act_bwd: do_stabilize is not differentiable here");
+  // variance cotangents are compact [n, A, C] arrays
+  VarGrad g1{gvar1, a * c, c, 1}, g2{gvar2, a * c, c, 1};
+  const int64_t m = diag_spatial ? a * c : a * a * c * c;
+  act_bwd_kernel<<<grid_for(batch * m), kT, 0, as_stream(stream)>>>(
+      q, t, gq, gt, oq, ot, batch, n2, a, c, diag_spatial, act, var1, var2, g1, g2);
+  note_launch();
+  return check_launch("ntg_act_bwd");
+}
+
+extern "C" int ntg_affine_bwd(void* stream, const float* gq, const float* gt, float* gu,
+                              float* gut, int64_t n, ntg_affine_t aff, float scale) {
+  NTG_REQUIRE(gu && n > 0, "ntg_affine_bwd: bad arguments");
+  affine_bwd_kernel<<<grid_for(n), kT, 0, as_stream(stream)>>>(gq, gt, gu, gut, n, aff, scale);
+  note_launch();
+  return check_launch("ntg_affine_bwd");
+}
+
+extern "C" int ntg_affine_hyper_bwd(void* stream, const float* q, const float* t,
+                                    const float* gq, const float* gt, int64_t n, float w2,
+                                    float b2, double* out) {
+  NTG_REQUIRE(q && out && n > 0, "ntg_affine_hyper_bwd: bad arguments");
+  affine_hyper_kernel<<<grid_for(n), kT, 0, as_stream(stream)>>>(q, t, gq, gt, n, w2, b2, out);
+  note_launch();
+  return check_launch("ntg_affine_hyper_bwd");
+}
+
+extern "C" int ntg_stencil_bwd(void* stream, const float* gu, float* gin, int64_t batch, int64_t a,
+                               int64_t c, int32_t fh, int32_t fw, int32_t sh, int32_t sw,
+                               int32_t ph, int32_t pw, int64_t ao, int64_t co, int32_t pad_mode,
+                               int32_t diag_spatial) {
+  NTG_REQUIRE(gu && gin && batch > 0 && a > 0 && c > 0, "ntg_stencil_bwd: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  if (diag_spatial) {
+    stencil_ds_t_kernel<<<grid_for(batch * a * c), kT, 0, s>>>(
+        gu, gin, batch, a, c, ao, co, fh, fw, sh, sw, ph, pw, pad_mode == NTG_PAD_CIRCULAR);
+  } else if (fh == 3 && fw == 3 && sh == 1 && sw == 1 && ph == 1 && pw == 1 && ao == a &&
+             co == c && pad_mode == NTG_PAD_ZERO) {
+    stencil3_t_kernel<<<grid_for(batch * a * a * c * c), kT, 0, s>>>(gu, gin, batch, a, c);
+  } else {
+    stencil_t_kernel<<<grid_for(batch * a * a * c * c), kT, 0, s>>>(
+        gu, gin, batch, a, c, ao, co, fh, fw, sh, sw, ph, pw, pad_mode == NTG_PAD_CIRCULAR);
+  }
+  note_launch();
+  return check_launch("ntg_stencil_bwd");
+}
+
+extern "C" int ntg_pool_bwd(void* stream, const float* gout, float* gin, int64_t batch, int64_t a,
+                            int64_t c, int32_t wa, int32_t wc, int32_t sa, int32_t sc, int32_t pa,
+                            int32_t pc, int64_t ao, int64_t co, int32_t pad_mode,
+                            int32_t diag_spatial, int32_t average, int32_t normalize_edges) {
+  NTG_REQUIRE(gout && gin && batch > 0, "ntg_pool_bwd: bad arguments");
+  NTG_REQUIRE(wa <= 6 && wc <= 6, "ntg_pool_bwd: windows up to 6 per axis");
+  const int64_t total = diag_spatial ? batch * a * c : batch * a * a * c * c;
+  pool_t_kernel<<<grid_for(total), kT, 0, as_stream(stream)>>>(
+      gout, gin, batch, a, c, ao, co, wa, wc, sa, sc, pa, pc, pad_mode == NTG_PAD_CIRCULAR,
+      diag_spatial, average, normalize_edges);
+  note_launch();
+  return check_launch("ntg_pool_bwd");
+}
+
+extern "C" int ntg_readout_bwd(void* stream, const float* gout, float* gin, int64_t batch,
+                               int64_t a, int64_t c, int32_t flatten_fs, int64_t m, float scale) {
+  NTG_REQUIRE(gout && gin && batch > 0 && m > 0, "ntg_readout_bwd: bad arguments");
+  readout_t_kernel<<<grid_for(batch * m), kT, 0, as_stream(stream)>>>(gout, gin, batch, a, c,
+                                                                      flatten_fs, m, scale);
+  note_launch();
+  return check_launch("ntg_readout_bwd");
+}
+
+extern "C" int ntg_input_fs_bwd(void* stream, const float* g, const float* x_other, float* gx,
+                                int64_t nself, int64_t nother, int64_t n2, int64_t a, int64_t c,
+                                int64_t k, int32_t side) {
+  NTG_REQUIRE(g && x_other && gx && nself > 0 && a > 0 && c > 0 && k > 0,
+              "ntg_input_fs_bwd: bad arguments");
+  const size_t sm = sizeof(float) * c * k;
+  NTG_REQUIRE(sm <= 48 * 1024, "ntg_input_fs_bwd: C * K too large");
+  input_fs_t_kernel<<<(unsigned)(nself * a), 128, sm, as_stream(stream)>>>(
+      g, x_other, gx, nself, nother, n2, a, c, k, side, 1.f / (float)k);
+  note_launch();
+  return check_launch("ntg_input_fs_bwd");
+}
+
+extern "C" int ntg_gemm_ex(void* stream, const float* a, const float* b, float* c, int64_t m,
+                           int64_t n, int64_t k, int32_t trans_a, float alpha,
+                           int32_t accumulate) {
+  NTG_REQUIRE(a && b && c && m > 0 && n > 0 && k > 0, "ntg_gemm_ex: bad arguments");
+  NTG_REQUIRE(ceil_div(m, 64) <= 65535, "ntg_gemm_ex: m too large");
+  dim3 grid((unsigned)ceil_div(n, 64), (unsigned)ceil_div(m, 64));
+  gemm_ex_kernel<<<grid, 256, 0, as_stream(stream)>>>(a, b, c, m, n, k, trans_a, alpha,
+                                                      accumulate);
+  note_launch();
+  return check_launch("ntg_gemm_ex");
+}
+
+extern "C" int ntg_cov_diag_bwd(void* stream, const float* gcov, const float* x, float* gx,
+                                int64_t n, int64_t d) {
+  NTG_REQUIRE(gcov && x && gx && n > 0 && d > 0, "ntg_cov_diag_bwd: bad arguments");
+  cov_diag_t_kernel<<<grid_for(n * d), kT, 0, as_stream(stream)>>>(gcov, x, gx, n, d,
+                                                                   2.f / (float)d);
+  note_launch();
+  return check_launch("ntg_cov_diag_bwd");
+}
+
+extern "C" int ntg_diag_add(void* stream, const float* src, float* dst, int64_t n, int64_t a,
+                            int64_t c, int64_t s_n, int64_t s_a, int64_t s_c) {
+  NTG_REQUIRE(src && dst && n > 0 && a > 0 && c > 0, "ntg_diag_add: bad arguments");
+  diag_add_kernel<<<grid_for(n * a * c), kT, 0, as_stream(stream)>>>(src, dst, n, a, c, s_n, s_a,
+                                                                     s_c);
+  note_launch();
+  return check_launch("ntg_diag_add");
+}

@@ -618,7 +618,15 @@ class KernelFn:
             compute_ntk = names is None or 'ntk' in names
             x1 = _as_input(x1_or_kernel)
             x2t = None if x2 is None else _as_input(x2)
-            from . import _chain
+            from . import _autograd, _chain
+            if _autograd.needs_grad(self.specs, x1, x2t):
+                if ds:
+                    raise NotImplementedError('gradients of diagonal_spatial kernels')
+                k = _autograd.run_ad(self.specs, x1, x2t, compute_ntk)
+                if names is None:
+                    return k
+                vals = tuple(getattr(k, n) for n in names)
+                return vals[0] if single is not None else analytic_kernel(names, vals)
             k = _chain.try_fused(self, x1, x2t, ds, compute_ntk, ctx)
             if k is None:
                 cnone = bool(self.specs) and self.specs[0].channel_axis_none

@@ -1,0 +1,106 @@
+"""Gradients of kernel_fn (hand-written adjoints) against central finite
+differences of the float64 oracle (h = 1e-3), the check of the reference's own
+autodiff tests (tests/stax/elementwise_test.py:639-732, 782-934)."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import nt_oracle as o
+
+pytestmark = pytest.mark.gpu
+H = 1e-3
+
+
+def fd(f, x, idx, h=H):
+    xp, xm = x.copy(), x.copy()
+    xp[idx] += h
+    xm[idx] -= h
+    return (f(xp) - f(xm)) / (2 * h)
+
+
+def test_fcn_hyper_gradients(nt):
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((12, 30))
+    wq, wt = rng.standard_normal((12, 12)), rng.standard_normal((12, 12))
+    hp = np.array([1.3, 0.1, 1.6, 0.15, 1.1, 0.05])  # (W, b) of three Dense layers
+
+    def layers(m, h):
+        return [m.Dense(8, h[0], h[1]), m.Relu(), m.Dense(8, h[2], h[3]), m.Erf(),
+                m.Dense(1, h[4], h[5])]
+
+    def loss_oracle(h):
+        q, t = o.serial(*layers(o, h))(x, None, ('nngp', 'ntk'))
+        return float(np.sum(wq * q) + np.sum(wt * t))
+
+    ht = [torch.tensor(v, device='cuda', requires_grad=True) for v in hp]
+    q, t = nt.stax.serial(*layers(nt.stax, ht))[2](x, None, ('nngp', 'ntk'))
+    loss = (torch.from_numpy(wq).float().cuda() * q).sum() + \
+        (torch.from_numpy(wt).float().cuda() * t).sum()
+    loss.backward()
+    got = np.array([v.grad.item() for v in ht])
+    want = np.array([fd(loss_oracle, hp, i) for i in range(len(hp))])
+    np.testing.assert_allclose(got, want, rtol=2e-3, atol=2e-3 * np.abs(want).max())
+
+
+@pytest.mark.parametrize('readout', ['flatten', 'gap'])
+def test_conv_input_gradients(nt, readout):
+    rng = np.random.default_rng(1)
+    x1 = rng.standard_normal((2, 6, 6, 2))
+    x2 = rng.standard_normal((3, 6, 6, 2))
+    wq, wt = rng.standard_normal((2, 3)), rng.standard_normal((2, 3))
+
+    def layers(m):
+        ro = m.Flatten() if readout == 'flatten' else m.GlobalAvgPool()
+        return [m.Conv(2, (3, 3), padding='SAME', W_std=1.4, b_std=0.1), m.Relu(),
+                m.AvgPool((2, 2), (2, 2)), m.Conv(2, (2, 2), padding='SAME', W_std=1.2, b_std=0.2),
+                m.Erf(), ro, m.Dense(1, 1.1, 0.05)]
+
+    def loss_oracle(a, b):
+        q, t = o.serial(*layers(o))(a, b, ('nngp', 'ntk'))
+        return float(np.sum(wq * q) + np.sum(wt * t))
+
+    t1 = torch.tensor(x1, dtype=torch.float32, device='cuda', requires_grad=True)
+    t2 = torch.tensor(x2, dtype=torch.float32, device='cuda', requires_grad=True)
+    q, t = nt.stax.serial(*layers(nt.stax))[2](t1, t2, ('nngp', 'ntk'))
+    loss = (torch.from_numpy(wq).float().cuda() * q).sum() + \
+        (torch.from_numpy(wt).float().cuda() * t).sum()
+    loss.backward()
+    g1, g2 = t1.grad.cpu().numpy(), t2.grad.cpu().numpy()
+    scale = max(np.abs(g1).max(), np.abs(g2).max())
+    for idx in [(0, 0, 0, 0), (1, 3, 2, 1), (0, 5, 5, 1), (1, 2, 4, 0)]:
+        want = fd(lambda a: loss_oracle(a, x2), x1, idx)
+        assert abs(g1[idx] - want) < 3e-3 * scale, (idx, g1[idx], want)
+    for idx in [(0, 1, 1, 0), (2, 4, 0, 1), (1, 5, 3, 0)]:
+        want = fd(lambda b: loss_oracle(x1, b), x2, idx)
+        assert abs(g2[idx] - want) < 3e-3 * scale, (idx, g2[idx], want)
+
+
+def test_symmetric_call_gradient(nt):
+    """x2 = None: both factors of every covariance depend on x1."""
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal((3, 5, 5, 2))
+    w = rng.standard_normal((3, 3))
+
+    def layers(m):
+        return [m.Conv(1, (3, 3), padding='SAME', W_std=1.3, b_std=0.1), m.Relu(),
+                m.GlobalAvgPool(), m.Dense(1, 1.2, 0.1)]
+
+    def loss_oracle(a):
+        return float(np.sum(w * o.serial(*layers(o))(a, None, 'ntk')))
+
+    tx = torch.tensor(x, dtype=torch.float32, device='cuda', requires_grad=True)
+    k = nt.stax.serial(*layers(nt.stax))[2](tx, None, 'ntk')
+    (torch.from_numpy(w).float().cuda() * k).sum().backward()
+    g = tx.grad.cpu().numpy()
+    for idx in [(0, 0, 0, 0), (1, 2, 3, 1), (2, 4, 4, 0)]:
+        want = fd(loss_oracle, x, idx)
+        assert abs(g[idx] - want) < 3e-3 * np.abs(g).max(), (idx, g[idx], want)
+
+
+def test_zero_input_gradient_is_finite(nt):
+    """tests/stax/elementwise_test.py:949-1036 (issue 123): zero inputs give finite gradients."""
+    x = torch.zeros((2, 4), device='cuda', requires_grad=True)
+    q = nt.stax.serial(nt.stax.Dense(3, 1., 0.), nt.stax.Relu(), nt.stax.Dense(1))[2](x, None, 'nngp')
+    q.sum().backward()
+    assert torch.isfinite(x.grad).all()
+    assert (x.grad == 0).all()
