@@ -222,10 +222,10 @@ class ConvFn(torch.autograd.Function):
         s = L.stream()
         dev = qn.device
 
-        def back(g, gtt, in_shape, bnd):
+        def back(g, gtt, in_shape, bnd, want_t_in=True):
             n = int(math.prod(g.shape)) if g is not None else int(math.prod(gtt.shape))
             gu = torch.empty(n, device=dev)
-            gut = torch.empty(n, device=dev) if gtt is not None else None
+            gut = torch.empty(n, device=dev) if (gtt is not None and want_t_in) else None
             L.call('ntg_affine_bwd', s, None if g is None else L.ptr(g.contiguous()),
                    None if gtt is None else L.ptr(gtt.contiguous()), L.ptr(gu),
                    None if gut is None else L.ptr(gut), n, aff, scale)
@@ -244,7 +244,9 @@ class ConvFn(torch.autograd.Function):
                 outs.append(gin)
             return outs
 
-        gqi, gti = back(gq, None if zero_t else gt, qs, 2)
+        # the output NTK's cotangent reaches the input nngp through ntk_out = nngp_out + ...
+        # even when the input NTK is the scalar zero of an input kernel
+        gqi, gti = back(gq, gt, qs, 2, not zero_t)
         gc1i = back(gc1, None, c1s, 1)[0]
         gc2i = None if c2s is None else back(gc2, None, c2s, 1)[0]
         acc = _hyper([(qn, tn), (c1n, None), (_opt(c2n), None)], [(gq, gt), (gc1, None),
