@@ -271,6 +271,16 @@ int ntg_diag_add(void* stream, const float* src, float* dst, int64_t n, int64_t 
 int ntg_cov_diag_bwd(void* stream, const float* gcov, const float* x, float* gx, int64_t n,
                      int64_t d);
 
+/* log det(L L^T) = 2 sum log L_ii of a factor from ntg_chol_factor -> out[0]. */
+int ntg_chol_logdet(void* stream, const float* L, int64_t n, double* out);
+/* Cotangent of the Gaussian-process negative log-likelihood
+ * 1/2 tr(Y^T A^{-1} Y) + m/2 log det A + const with A = K + lambda I:
+ * out = g (-1/2 alpha alpha^T + m/2 A^{-1}) (alpha = A^{-1} Y [n, m], kinv = A^{-1}),
+ * plus reg_over_n * trace(out) on the diagonal when lambda = diag_reg trace(K) / n
+ * (reg_over_n = diag_reg / n; 0 for an absolute regulariser). tr: device double. */
+int ntg_nll_grad(void* stream, const float* kinv, const float* alpha, int64_t n, int64_t m,
+                 float g, double reg_over_n, float* out, double* tr);
+
 /* No counterpart in the reference. ntg_chol_solve without a caller workspace,
  * for callers that cannot allocate device memory where they call the solve
  * (a handler inside a captured CUDA graph, a server that reserved all device

@@ -87,6 +87,8 @@ SIGNATURES = {
     'ntg_cov_diag_bwd': ([_P, _P, _P, _P, _I64, _I64], C.c_int),
     'ntg_diag_add': ([_P, _P, _P, _I64, _I64, _I64, _I64, _I64, _I64], C.c_int),
     'ntg_chol_factor': ([_P, _P, _I64, C.c_double, _I32, _P, _P, _P], C.c_int),
+    'ntg_chol_logdet': ([_P, _P, _I64, _P], C.c_int),
+    'ntg_nll_grad': ([_P, _P, _P, _I64, _I64, _F, C.c_double, _P, _P], C.c_int),
     'ntg_chol_workspace_bytes': ([_I64, _I64], C.c_size_t),
     'ntg_chol_solve': ([_P, _P, _P, _P, _I64, _P, _I64, _P, _I32, _P, C.c_size_t, _P], C.c_int),
     'ntg_chol_solve_noalloc': ([_P, _P, _P, _P, _I64, _P, _I64, _P, _I32, _P], C.c_int),
@@ -122,10 +124,29 @@ class NtgError(RuntimeError):
     pass
 
 
+_pinned = threading.local()
+
+
+def _keep(t) -> None:
+    lst = getattr(_pinned, 'tensors', None)
+    if lst is None:
+        lst = _pinned.tensors = []
+    lst.append(t)
+
+
 def call(name: str, *args) -> None:
-    """Calls an entry point; raises NtgError with the library message on failure."""
+    """Calls an entry point; raises NtgError with the library message on failure.
+
+    Tensors whose pointers were taken by ptr() since the previous call stay
+    referenced until this call has enqueued its work: a temporary such as
+    ptr(x.contiguous()) would otherwise return its memory to the caching
+    allocator before the kernel that reads it is launched, and the next
+    temporary of the same argument list could take over that block."""
     lib = load()
-    rc = getattr(lib, name)(*args)
+    try:
+        rc = getattr(lib, name)(*args)
+    finally:
+        _pinned.tensors = []
     if rc != 0:
         msg = lib.ntg_last_error().decode()
         raise NtgError(f'{name} failed ({ERRORS.get(rc, rc)}): {msg}')
@@ -145,6 +166,7 @@ def ptr(t) -> int | None:
         return None
     if not t.is_cuda or t.dtype != torch.float32 or not t.is_contiguous():
         raise ValueError('nt_gb300 kernels take contiguous float32 CUDA tensors')
+    _keep(t)
     return t.data_ptr()
 
 

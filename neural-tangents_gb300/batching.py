@@ -22,8 +22,76 @@ def _tiles(n: int, b: int):
     return [(s, min(b, n - s)) for s in range(0, n, b)]
 
 
+class _CheckpointedKernel(torch.autograd.Function):
+    """nngp/ntk over the whole grid with a recompute-per-tile backward.
+
+    The forward keeps nothing but the inputs; the backward re-evaluates each
+    tile through the differentiable layer rules and back-propagates that
+    tile's cotangents, so at most one tile's layer tensors are alive at once.
+    """
+
+    @staticmethod
+    def forward(ctx, x1, x2, kfn, bs, precision):
+        x2o = None if x2.numel() == 0 else x2
+        with torch.no_grad():
+            res = _forward_grid(kfn, x1, x2o, bs, precision)
+        ctx.save_for_backward(x1, x2)
+        ctx.kfn, ctx.bs = kfn, bs
+        return res.nngp, res.ntk
+
+    @staticmethod
+    def backward(ctx, gq, gt):
+        from . import _autograd
+        x1, x2 = ctx.saved_tensors
+        x2o = None if x2.numel() == 0 else x2
+        xb = x1 if x2o is None else x2o
+        gx1 = torch.zeros_like(x1)
+        gxb = gx1 if x2o is None else torch.zeros_like(x2o)
+        bs = ctx.bs
+        for r0, rn in _tiles(x1.shape[0], bs):
+            for c0, cn in _tiles(xb.shape[0], bs):
+                with torch.enable_grad():
+                    a = x1[r0:r0 + rn].detach().requires_grad_(True)
+                    b = xb[c0:c0 + cn].detach().requires_grad_(True)
+                    k = _autograd.run_ad(ctx.kfn.specs, a, b, True)
+                    outs, grads = [], []
+                    for o, g in ((k.nngp, gq), (k.ntk, gt)):
+                        if g is not None:
+                            outs.append(o)
+                            grads.append(g[r0:r0 + rn, c0:c0 + cn])
+                    torch.autograd.backward(outs, grads)
+                gx1[r0:r0 + rn] += a.grad
+                gxb[c0:c0 + cn] += b.grad
+        return gx1, (None if x2o is None else gxb), None, None, None
+
+
+def _forward_grid(kernel_fn, x1t, x2t, bs, precision):
+    ctx = _Ctx(precision)
+    plan = _chain.plan_chain(kernel_fn.specs, tuple(x1t.shape), bool(kernel_fn.diagonal))
+    if plan is not None and (x2t is None or x2t.shape[1:] == x1t.shape[1:]):
+        old = _chain.SELF_CHUNK
+        _chain.SELF_CHUNK = max(1, min(old, bs))
+        try:
+            k = _chain.run_fused(plan, x1t, x2t, ctx)
+        finally:
+            _chain.SELF_CHUNK = old
+        return kernel_fn.apply_kernel(k, ctx, specs=plan.post)
+    xb = x1t if x2t is None else x2t
+    rows = []
+    for r0, rn in _tiles(x1t.shape[0], bs):
+        cols = []
+        for c0, cn in _tiles(xb.shape[0], bs):
+            cols.append(kernel_fn(x1t[r0:r0 + rn], xb[c0:c0 + cn], ('nngp', 'ntk'),
+                                  precision=precision))
+        rows.append(cols)
+    return _assemble(rows, ('nngp', 'ntk'), None)
+
+
 def batch(kernel_fn, batch_size: int = 0, device_count: int = -1, store_on_device: bool = True):
-    """batching.py:76-132 (one device: serial tiling)."""
+    """batching.py:76-132 (one device: serial tiling).
+
+    With inputs that require grad, the returned nngp/ntk carry a checkpointed
+    backward (one tile of layer tensors recomputed at a time)."""
     if device_count not in (-1, 0, 1):
         raise NotImplementedError('nt_gb300 runs on one GPU; device_count must be -1, 0 or 1')
 
@@ -35,6 +103,15 @@ def batch(kernel_fn, batch_size: int = 0, device_count: int = -1, store_on_devic
         names, single = _normalize_get(get)
         ctx = _Ctx(precision)
         bs = batch_size or max(x1t.shape[0], (x2t if x2t is not None else x1t).shape[0])
+        if isinstance(kernel_fn, KernelFn) and torch.is_grad_enabled() and (
+                x1t.requires_grad or (x2t is not None and x2t.requires_grad)):
+            if names is None or not set(names) <= {'nngp', 'ntk'}:
+                raise NotImplementedError('differentiable batch() returns nngp and ntk')
+            q, t = _CheckpointedKernel.apply(
+                x1t, x2t if x2t is not None else torch.empty(0, device=x1t.device), kernel_fn,
+                bs, precision)
+            vals = tuple(q if n == 'nngp' else t for n in names)
+            return vals[0] if single is not None else analytic_kernel(names, vals)
         ds = kwargs.get('diagonal_spatial')
         if isinstance(kernel_fn, KernelFn):
             ds = bool(kernel_fn.diagonal) if ds is None else bool(ds)

@@ -260,6 +260,47 @@ __global__ void accumulate_kernel(double* __restrict__ x, const float* __restric
   }
 }
 
+__global__ void logdet_kernel(const float* __restrict__ L, int64_t n, double* __restrict__ out) {
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += log((double)L[i * n + i]);
+  __shared__ double part[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+    out[0] = 2.0 * t;
+  }
+}
+
+// out = g (-1/2 alpha alpha^T + m/2 Kinv); trace(out) accumulated into tr[0].
+__global__ void nll_grad_kernel(const float* __restrict__ kinv, const float* __restrict__ alpha,
+                                int64_t n, int64_t m, float g, float* __restrict__ out,
+                                double* __restrict__ tr) {
+  const int64_t total = n * n;
+  double ltr = 0.0;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx / n, j = idx - i * n;
+    float aa = 0.f;
+    for (int64_t c = 0; c < m; ++c) aa = fmaf(alpha[i * m + c], alpha[j * m + c], aa);
+    const float v = g * (-0.5f * aa + 0.5f * (float)m * kinv[idx]);
+    out[idx] = v;
+    if (i == j) ltr += (double)v;
+  }
+  if (ltr != 0.0) atomicAdd(tr, ltr);
+}
+
+__global__ void add_diag_kernel(float* __restrict__ a, int64_t n, const double* __restrict__ tr,
+                                double scale) {
+  const float v = (float)(scale * tr[0]);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    a[i * n + i] += v;
+}
+
 int grid1(int64_t n) {
   int64_t g = (n + 255) / 256;
   return (int)(g > 152 * 32 ? 152 * 32 : (g < 1 ? 1 : g));
@@ -362,4 +403,25 @@ extern "C" int ntg_chol_solve(void* stream, const float* A, const float* L, cons
           cudaSuccess)
     return check_launch("ntg_chol_solve residual copy");
   return check_launch("ntg_chol_solve");
+}
+
+extern "C" int ntg_chol_logdet(void* stream, const float* L, int64_t n, double* out) {
+  NTG_REQUIRE(L && out && n > 0, "ntg_chol_logdet: bad arguments");
+  logdet_kernel<<<1, 1024, 0, as_stream(stream)>>>(L, n, out);
+  note_launch();
+  return check_launch("ntg_chol_logdet");
+}
+
+extern "C" int ntg_nll_grad(void* stream, const float* kinv, const float* alpha, int64_t n,
+                            int64_t m, float g, double reg_over_n, float* out, double* tr) {
+  NTG_REQUIRE(kinv && alpha && out && tr && n > 0 && m > 0, "ntg_nll_grad: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  if (cudaMemsetAsync(tr, 0, sizeof(double), s) != cudaSuccess) return check_launch("ntg_nll_grad");
+  nll_grad_kernel<<<grid1(n * n), 256, 0, s>>>(kinv, alpha, n, m, g, out, tr);
+  note_launch();
+  if (reg_over_n != 0.0) {
+    add_diag_kernel<<<grid1(n), 256, 0, s>>>(out, n, tr, reg_over_n);
+    note_launch();
+  }
+  return check_launch("ntg_nll_grad");
 }

@@ -13,6 +13,7 @@ is supported.
 """
 from __future__ import annotations
 
+import math
 import warnings
 from typing import Optional
 
@@ -149,3 +150,48 @@ def _t64(v, like: torch.Tensor) -> torch.Tensor:
     if isinstance(v, (int, float)):
         return torch.tensor(float(v), dtype=torch.float64, device=like.device)
     return _dev(v, torch.float64)
+
+
+class _NLL(torch.autograd.Function):
+    """1/2 tr(Y^T A^{-1} Y) + m/2 log det A + n m/2 log 2 pi, A = K + lambda I."""
+
+    @staticmethod
+    def forward(ctx, k, y, diag_reg, absolute, refine_iters):
+        k = k.contiguous()
+        n, m = y.shape
+        solver = CholeskySolver(k, diag_reg, absolute, refine_iters)
+        alpha = solver.solve(y)
+        ld = torch.zeros(1, device=k.device, dtype=torch.float64)
+        L.call('ntg_chol_logdet', L.stream(), L.ptr(solver.L), n, ld.data_ptr())
+        quad = _gemm(y.reshape(1, -1).contiguous(), alpha.reshape(-1, 1).contiguous())
+        nll = 0.5 * quad.reshape(()).double() + 0.5 * m * ld[0] + 0.5 * n * m * math.log(2 * math.pi)
+        ctx.solver, ctx.alpha, ctx.meta = solver, alpha, (diag_reg, absolute, n, m)
+        return nll.float()
+
+    @staticmethod
+    def backward(ctx, g):
+        diag_reg, absolute, n, m = ctx.meta
+        solver, alpha = ctx.solver, ctx.alpha
+        eye = torch.zeros((n, n), device=alpha.device)
+        eye.view(-1)[::n + 1] = 1.
+        kinv = solver.solve(eye)
+        out = torch.empty((n, n), device=alpha.device)
+        tr = torch.zeros(1, device=alpha.device, dtype=torch.float64)
+        L.call('ntg_nll_grad', L.stream(), L.ptr(kinv), L.ptr(alpha.contiguous()), n, m,
+               float(g.item()), 0. if absolute else diag_reg / n, L.ptr(out), tr.data_ptr())
+        return out, alpha * g, None, None, None
+
+
+def negative_log_likelihood(k_train_train, y_train, diag_reg: float = 0.,
+                            diag_reg_absolute_scale: bool = False, refine_iters: int = 2):
+    """NNGP negative log marginal likelihood, differentiable with respect to the kernel.
+
+    A helper for hyper-parameter learning (not part of the reference's predict
+    module): 1/2 tr(Y^T A^{-1} Y) + m/2 log det A + n m/2 log(2 pi) with
+    A = K + diag_reg * trace(K) / n * I (or diag_reg * I when absolute), on the
+    Cholesky kernels of this module; its backward is the Cholesky adjoint
+    g (-1/2 alpha alpha^T + m/2 A^{-1}).
+    """
+    k = k_train_train if isinstance(k_train_train, torch.Tensor) else _dev(k_train_train)
+    y = _dev(y_train)
+    return _NLL.apply(k, y, float(diag_reg), bool(diag_reg_absolute_scale), int(refine_iters))
