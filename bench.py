@@ -207,6 +207,7 @@ def run_gpu(args):
     # Materialised per-layer stencil (conv + Relu epilogue) on a 16 x 16 tile at S = 32.
     st_gbs = stencil_roofline(torch, O, dev)
     gram_tc = gram_roofline(torch, O, dev)
+    fwd_bwd = fwd_bwd_timing(torch, nt, kf, xd)
 
     # Mixed precision (compensated) variant of the same step and its error vs plain.
     torch.cuda.synchronize()
@@ -271,6 +272,7 @@ def run_gpu(args):
                     'flops_per_entry': flops_entry},
         'stencil_roofline': st_gbs,
         'gram_tc': gram_tc,
+        'fwd_bwd': fwd_bwd,
         'gpu_launches': int(launches),
         'clocks': clocks,
     }
@@ -309,6 +311,29 @@ def stencil_roofline(torch, O, dev):
     gbs = nbytes / (ms / 1e3) / 1e9
     return {'kernel': 'conv3_line_kernel', 'pairs': B, 'bytes': nbytes, 'ms': round(ms, 3),
             'achieved': round(gbs, 1), 'unit': 'GB/s'}
+
+
+def fwd_bwd_timing(torch, nt, kf, xd, n_t=16, n_s=8, bs=8):
+    """Myrtle-5 NTK forward + backward with respect to a support set: the gradient of
+    sum(w * K(x_t, x_s)) by x_s through nt.batch's checkpointed tiles (the
+    recompute-per-tile adjoint path)."""
+    xt = xd[:n_t].contiguous()
+    w = torch.randn((n_t, n_s), device=xd.device)
+    batched = nt.batch(kf, batch_size=bs)
+    ts = []
+    for i in range(3):
+        xs = xd[1000:1000 + n_s].clone().requires_grad_(True)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        k = batched(xt, xs, 'ntk')
+        (w * k).sum().backward()
+        b.record()
+        torch.cuda.synchronize()
+        if i:
+            ts.append(a.elapsed_time(b))
+    ms = statistics.mean(ts)
+    return {'ms': round(ms, 2), 'pairs': n_t * n_s, 'entries_per_s': round(n_t * n_s / (ms / 1e3), 1),
+            'config': f'Myrtle-5 ntk fwd + d/dx_s, x_t [{n_t}], x_s [{n_s}], batch_size {bs}'}
 
 
 def gram_roofline(torch, O, dev):
