@@ -58,8 +58,6 @@ def make_inputs(n=N_SAMPLES, seed=0):
     return x.astype(np.float32)
 
 
-def tiles(n_tiles_side):
-    return [(r, c) for r in range(n_tiles_side) for c in range(n_tiles_side)]
 
 
 def dist_env():
@@ -139,10 +137,9 @@ def run_gpu(args):
     _, _, kf = stax.serial(*myrtle5(stax))
     plan = _chain.plan_chain(kf.specs, tuple(xd.shape), False)
     assert plan is not None, 'Myrtle-5 must take the fused chain path'
-    n_side = N_SAMPLES // TILE
-    grid = tiles(n_side)
-    total_steps = args.warmup + args.steps
-    mine = [grid[(rank + ws * s) % len(grid)] for s in range(total_steps)]
+    from nt_gb300.batching import rank_tiles, tile_grid
+    grid = [(r0 // TILE, c0 // TILE) for r0, _, c0, _ in tile_grid(N_SAMPLES, N_SAMPLES, TILE)]
+    mine = rank_tiles(grid, ws, rank, args.warmup + args.steps)
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
     out_q = torch.empty((TILE, TILE), device=dev)
     out_t = torch.empty((TILE, TILE), device=dev)

@@ -22,6 +22,21 @@ def _tiles(n: int, b: int):
     return [(s, min(b, n - s)) for s in range(0, n, b)]
 
 
+def tile_grid(n1: int, n2: int, b: int):
+    """Row-major (r0, rn, c0, cn) tiles of an n1 x n2 kernel, ragged at the edges."""
+    return [(r0, rn, c0, cn) for r0, rn in _tiles(n1, b) for c0, cn in _tiles(n2, b)]
+
+
+def rank_tiles(tiles, world_size: int, rank: int, steps=None):
+    """Tiles of one rank when the grid is sharded across ranks (tile k -> rank k % world_size,
+    batching.py:505-644 shards x1 rows the same way). Every tile of the grid is independent, so
+    the ranks exchange no data; with `steps`, the list wraps to that length."""
+    mine = [t for k, t in enumerate(tiles) if k % world_size == rank]
+    if steps is None:
+        return mine
+    return [tiles[(rank + world_size * s) % len(tiles)] for s in range(steps)]
+
+
 class _CheckpointedKernel(torch.autograd.Function):
     """nngp/ntk over the whole grid with a recompute-per-tile backward.
 
