@@ -281,10 +281,10 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def stencil_roofline(torch, O, dev):
+def stencil_roofline(torch, O, dev, pairs=256, reps=4):
     """Materialised 3x3 conv + Relu rule on [B, 32, 32, 32, 32] pairs (HBM-bound)."""
     from nt_gb300 import _lib as L
-    B = 256
+    B = pairs
     q = torch.rand((B, 32, 32, 32, 32), device=dev) + 1.
     t = torch.rand_like(q)
     var = torch.rand((B, 32, 32), device=dev) + 2.
@@ -293,7 +293,7 @@ def stencil_roofline(torch, O, dev):
     act = L.Act(L.NTG_ACT_ABRELU, 0., 1., 0., 0, 0.)
     outs = None
     ts = []
-    for i in range(4):
+    for i in range(reps):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
         outs = O.conv_fs(q, t, B, 1, 32, 32, 3, 3, 1, 1, 1, 1, 32, 32, False, aff, act, v, v,
@@ -303,7 +303,7 @@ def stencil_roofline(torch, O, dev):
         if i:
             ts.append(a.elapsed_time(b))
     del outs
-    ms = statistics.median(ts)
+    ms = statistics.median(ts) if ts else float('nan')
     nbytes = 4 * q.numel() * 4  # read nngp, ntk; write nngp, ntk
     gbs = nbytes / (ms / 1e3) / 1e9
     return {'kernel': 'conv3_line_kernel', 'pairs': B, 'bytes': nbytes, 'ms': round(ms, 3),
@@ -438,9 +438,18 @@ def profile_tile(p: int):
     print(json.dumps({'profile_tile': p, 'nngp_mean': float(oq.mean()), 'ntk_mean': float(ot.mean())}))
 
 
+def profile_stencil(pairs: int):
+    """One materialised conv+ReLU stencil launch on `pairs` 32^4 pairs (ncu small case)."""
+    import torch
+    from nt_gb300 import _ops as O
+    st = stencil_roofline(torch, O, torch.device('cuda'), pairs=pairs, reps=1)
+    print(json.dumps({'profile_stencil': pairs, **st}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--profile-tile', type=int, default=0)
+    ap.add_argument('--profile-stencil', type=int, default=0)
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=3)
@@ -451,6 +460,8 @@ def main():
     args = ap.parse_args()
     if args.profile_tile:
         profile_tile(args.profile_tile)
+    elif args.profile_stencil:
+        profile_stencil(args.profile_stencil)
     elif args.impl == 'reference':
         run_reference(args)
     else:

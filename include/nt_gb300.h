@@ -79,6 +79,9 @@ const char* ntg_last_error(void);
 const char* ntg_version(void);
 /* Number of sm_103a kernels launched by this library since load (all threads). */
 uint64_t ntg_launch_count(void);
+/* Reads and clears the device error word of the streamed kernels (synchronous):
+ * NTG_ERR_WAIT_TIMEOUT if a bounded pipeline wait ran out since the last call. */
+int ntg_device_status(void);
 
 /* ---- input kernels (requirements.py:518-638, 641-830) ---------------- */
 /* Flat inputs x1 [N1, D], x2 [N2, D] -> nngp [N1, N2] = x1 x2^T / D

@@ -53,6 +53,7 @@ SIGNATURES = {
     'ntg_last_error': ([], C.c_char_p),
     'ntg_version': ([], C.c_char_p),
     'ntg_launch_count': ([], C.c_uint64),
+    'ntg_device_status': ([], C.c_int),
     'ntg_gram': ([_P, _P, _P, _I64, _I64, _I64, _P, _I32, _P, C.c_size_t], C.c_int),
     'ntg_gram_workspace_bytes': ([_I64, _I64, _I64], C.c_size_t),
     'ntg_gemm': ([_P, _P, _P, _P, _I64, _I64, _I64, _I32], C.c_int),

@@ -435,8 +435,8 @@ __global__ void __launch_bounds__(NT, 1)
           const float a = __ldg(g1 + e), b = __ldg(g2 + e);
           p[e] = a;
           p[S * S + e] = b;
-          p[2 * S * S + e] = sqrtf(a);
-          p[3 * S * S + e] = sqrtf(b);
+          p[2 * S * S + e] = sqrt_var(a);
+          p[3 * S * S + e] = sqrt_var(b);
         }
         p += 4 * S * S;
       }

@@ -246,8 +246,12 @@ __device__ __forceinline__ void abrelu2(const ActC& c, P2& q, P2& t, P2 v1, P2 v
   t = mul2(t, dot);
 }
 
+// sqrt(var) as every kernel of the library evaluates it (one approximate
+// square root), so that the fused and the materialised paths round alike.
+__device__ __forceinline__ float sqrt_var(float v) { return sqrt_approx(fmaxf(v, 0.f)); }
+
 __device__ __forceinline__ void act_apply(const ActC& c, float& q, float& t, float v1, float v2) {
-  act_apply(c, q, t, v1, v2, sqrtf(v1), sqrtf(v2));
+  act_apply(c, q, t, v1, v2, sqrt_var(v1), sqrt_var(v2));
 }
 
 // Affine rule on an unscaled propagated sum u (nngp) and u_t (ntk) whose

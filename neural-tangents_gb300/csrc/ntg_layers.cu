@@ -3,6 +3,7 @@
 // rule and the ABRelu/Erf epilogue fused in), elementwise Dense/activation,
 // pooling and the Flatten / GlobalAvgPool readouts.
 #include <cstdio>
+#include <string>
 
 #include "ntg_common.cuh"
 
@@ -325,6 +326,212 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ---------------------------------------------------------------------------
+// Same rule with the input planes of a line streamed through a 4-stage
+// shared-memory ring by bulk asynchronous copies (cp.async.bulk, completion on
+// an mbarrier): one thread keeps up to 3 planes of both tensors in flight while
+// the CTA works on the current one. Waits are bounded; a wait that runs out
+// raises the library's device error word and the line is left unwritten.
+// ---------------------------------------------------------------------------
+constexpr int kRing = 4;
+constexpr uint32_t kLineWaitLimit = 1u << 20;
+
+__device__ int g_device_error = 0;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
+  for (uint32_t it = 0; it < kLineWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+template <bool HAS_T>
+__global__ void __launch_bounds__(kThreads)
+    conv3_line_bulk_kernel(const float* __restrict__ in_q, const float* __restrict__ in_t,
+                           float* __restrict__ out_q, float* __restrict__ out_t, int64_t batch,
+                           int64_t n2, int A, int C, ntg_affine_t aff, ntg_act_t act,
+                           ntg_var_t var1, ntg_var_t var2) {
+  extern __shared__ __align__(128) float smem[];
+  const int plane = C * C;
+  const int P = C + 2;
+  float* ring_q = smem;                          // [kRing][plane]
+  float* ring_t = ring_q + kRing * plane;        // [kRing][plane]
+  float* hq[2] = {ring_t + kRing * plane, ring_t + kRing * plane + P * P};
+  float* ht[2] = {hq[1] + P * P, hq[1] + 2 * P * P};
+  uint64_t* bars = reinterpret_cast<uint64_t*>(hq[1] + 3 * P * P);
+  const int nlines = 2 * A - 1;
+  const int64_t b = blockIdx.x / nlines;
+  const int delta = (int)(blockIdx.x - b * nlines) - (A - 1);
+  if (b >= batch) return;
+  const int i_lo = delta < 0 ? -delta : 0;
+  const int i_hi = delta < 0 ? A : A - delta;
+  const int len = i_hi - i_lo;
+  const int64_t pair_stride = (int64_t)A * A * plane;
+  const uint32_t bytes = (uint32_t)(plane * sizeof(float)) * (HAS_T ? 2u : 1u);
+
+  for (int idx = threadIdx.x; idx < 4 * P * P; idx += blockDim.x) hq[0][idx] = 0.f;
+  if (threadIdx.x == 0) {
+    for (int sl = 0; sl < kRing; ++sl)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[sl])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  auto issue = [&](int j) {  // plane j of the line (0-based) into slot j % kRing
+    const int i = i_lo + j;
+    const int sl = j % kRing;
+    const uint32_t bar = smem_addr(&bars[sl]);
+    const int64_t off = b * pair_stride + ((int64_t)i * A + i + delta) * plane;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_addr(ring_q + sl * plane)), "l"(in_q + off), "r"((uint32_t)(plane * 4)),
+        "r"(bar)
+        : "memory");
+    if (HAS_T)
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+          ::"r"(smem_addr(ring_t + sl * plane)), "l"(in_t + off), "r"((uint32_t)(plane * 4)),
+          "r"(bar)
+          : "memory");
+  };
+  if (threadIdx.x == 0)
+    for (int j = 0; j < kRing && j < len; ++j) issue(j);
+
+  int64_t i1, i2;
+  pair_of(b, n2, i1, i2);
+  const ActC ac = act_consts(act);
+  const int e0 = threadIdx.x * 4;
+  const bool active = e0 < plane;
+  const int c = active ? e0 / C : 0;
+  const int cp0 = active ? e0 - c * C : 0;
+  bool ok = true;
+
+  // reads plane j (0-based) of the line from its ring slot (zero outside)
+  auto take = [&](int j, float (&q)[4], float (&t)[4]) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) q[u] = t[u] = 0.f;
+    if (j < 0 || j >= len) return;
+    const int sl = j % kRing;
+    if (!bar_wait(smem_addr(&bars[sl]), (uint32_t)((j / kRing) & 1))) {
+      ok = false;
+      return;
+    }
+    if (!active) return;
+    const float4 v = *reinterpret_cast<const float4*>(ring_q + sl * plane + e0);
+    q[0] = v.x; q[1] = v.y; q[2] = v.z; q[3] = v.w;
+    if (HAS_T) {
+      const float4 w = *reinterpret_cast<const float4*>(ring_t + sl * plane + e0);
+      t[0] = w.x; t[1] = w.y; t[2] = w.z; t[3] = w.w;
+    }
+  };
+
+  float qm[4], tm[4], q0[4], t0[4], qp[4], tp[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) qm[u] = tm[u] = 0.f;
+  take(0, q0, t0);
+  const float inv9 = 1.f / 9.f;
+  int buf = 0;
+  for (int j = 0; j < len; ++j) {
+    take(j + 1, qp, tp);
+    const int i = i_lo + j;
+    if (active) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int o = (c + 1) * P + (cp0 + u + 1);
+        hq[buf][o] = (qm[u] + q0[u]) + qp[u];
+        if (HAS_T) ht[buf][o] = (tm[u] + t0[u]) + tp[u];
+      }
+    }
+    __syncthreads();
+    // Plane j was read by every thread before the previous barrier, so its slot
+    // takes plane j + kRing now: up to three planes stay in flight.
+    if (threadIdx.x == 0 && j + kRing < len) issue(j + kRing);
+    if (active && ok) {
+      float sq[4], st[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int o = (c + 1) * P + (cp0 + u + 1);
+        sq[u] = (hq[buf][o - P - 1] + hq[buf][o]) + hq[buf][o + P + 1];
+        st[u] = HAS_T ? (ht[buf][o - P - 1] + ht[buf][o]) + ht[buf][o + P + 1] : 0.f;
+      }
+      // affine rule on packed pairs (same rounding as apply_affine)
+      const P2 W2 = p2s(aff.w2 * inv9), B2 = p2s(aff.b2);
+      const P2 TW = p2s(aff.ntk_w2 * inv9), TN = p2s(aff.ntk_nn), TC = p2s(aff.ntk_c);
+      P2 q[2], t[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const P2 cq = p2(sq[2 * h], sq[2 * h + 1]), ct = p2(st[2 * h], st[2 * h + 1]);
+        q[h] = fma2(W2, cq, B2);
+        const P2 nn = aff.nn_scaled ? q[h] : mul2(cq, p2s(inv9));
+        t[h] = fma2(TW, ct, fma2(TN, nn, TC));
+      }
+      if (act.kind != NTG_ACT_NONE) {
+        const float v1 = var1.base[i1 * var1.s_n + (int64_t)i * var1.s_a + (int64_t)c * var1.s_c];
+        const float sv1 = sqrt_var(v1);
+        const float* v2r = var2.base + i2 * var2.s_n + (int64_t)(i + delta) * var2.s_a;
+        float v2[4], sv2[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          v2[u] = __ldg(v2r + (int64_t)(cp0 + u) * var2.s_c);
+          sv2[u] = sqrt_var(v2[u]);
+        }
+        if (act.kind == NTG_ACT_ABRELU && act.stabilize <= 0.f) {
+#pragma unroll
+          for (int h = 0; h < 2; ++h)
+            abrelu2(ac, q[h], t[h], p2s(v1), p2(v2[2 * h], v2[2 * h + 1]), p2s(sv1),
+                    p2(sv2[2 * h], sv2[2 * h + 1]));
+        } else {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            float qa, qb, ta, tb;
+            p2u(q[h], qa, qb);
+            p2u(t[h], ta, tb);
+            act_apply(ac, qa, ta, v1, v2[2 * h], sv1, sv2[2 * h]);
+            act_apply(ac, qb, tb, v1, v2[2 * h + 1], sv1, sv2[2 * h + 1]);
+            q[h] = p2(qa, qb);
+            t[h] = p2(ta, tb);
+          }
+        }
+      }
+      float vq[4], vt[4];
+      p2u(q[0], vq[0], vq[1]);
+      p2u(q[1], vq[2], vq[3]);
+      p2u(t[0], vt[0], vt[1]);
+      p2u(t[1], vt[2], vt[3]);
+      float* oq = out_q + b * pair_stride + ((int64_t)i * A + i + delta) * plane + e0;
+      *reinterpret_cast<float4*>(oq) = make_float4(vq[0], vq[1], vq[2], vq[3]);
+      if (out_t) {
+        float* ot = out_t + b * pair_stride + ((int64_t)i * A + i + delta) * plane + e0;
+        *reinterpret_cast<float4*>(ot) = make_float4(vt[0], vt[1], vt[2], vt[3]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      qm[u] = q0[u]; tm[u] = t0[u];
+      q0[u] = qp[u]; t0[u] = tp[u];
+    }
+    buf ^= 1;
+  }
+  if (!ok && threadIdx.x == 0) {
+    atomicExch(&g_device_error, NTG_ERR_WAIT_TIMEOUT);
+    // let every issued copy land (bounded) before the CTA's shared memory is released
+    for (int j = 0; j < len; ++j) bar_wait(smem_addr(&bars[j % kRing]), (uint32_t)((j / kRing) & 1));
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Diagonal-spatial conv rule: [B, A, C] box filter (linear.py:3381-3437).
 // ---------------------------------------------------------------------------
 __global__ void conv_ds_kernel(const float* __restrict__ in_q, const float* __restrict__ in_t,
@@ -616,7 +823,30 @@ extern "C" int ntg_conv_fs(void* stream, const float* in_q, const float* in_t, f
   const bool line_ok = fh == 3 && fw == 3 && sh == 1 && sw == 1 && ph == 1 && pw == 1 &&
                        ao == a && co == c && pad_mode == NTG_PAD_ZERO && c % 4 == 0 &&
                        c * c <= 4 * kThreads && a <= 4096;
-  if (line_ok) {
+  const bool aligned = ((reinterpret_cast<uintptr_t>(in_q) | reinterpret_cast<uintptr_t>(in_t) |
+                         reinterpret_cast<uintptr_t>(out_q) | reinterpret_cast<uintptr_t>(out_t)) &
+                        15) == 0;
+  if (line_ok && aligned) {
+    int64_t blocks = batch * (2 * a - 1);
+    NTG_REQUIRE(blocks < (1ll << 31), "ntg_conv_fs: grid too large");
+    const size_t sm = sizeof(float) * (2 * kRing * c * c + 4 * (c + 2) * (c + 2)) +
+                      sizeof(uint64_t) * kRing;
+    cudaError_t e;
+    if (in_t) {
+      e = cudaFuncSetAttribute(conv3_line_bulk_kernel<true>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e == cudaSuccess)
+        conv3_line_bulk_kernel<true><<<(unsigned)blocks, kThreads, sm, s>>>(
+            in_q, in_t, out_q, out_t, batch, n2, (int)a, (int)c, aff, act, var1, var2);
+    } else {
+      e = cudaFuncSetAttribute(conv3_line_bulk_kernel<false>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e == cudaSuccess)
+        conv3_line_bulk_kernel<false><<<(unsigned)blocks, kThreads, sm, s>>>(
+            in_q, nullptr, out_q, out_t, batch, n2, (int)a, (int)c, aff, act, var1, var2);
+    }
+    if (e != cudaSuccess) return fail(NTG_ERR_CUDA, std::string("ntg_conv_fs: ") + cudaGetErrorString(e));
+  } else if (line_ok) {
     int64_t blocks = batch * (2 * a - 1);
     NTG_REQUIRE(blocks < (1ll << 31), "ntg_conv_fs: grid too large");
     size_t sm = sizeof(float) * 4 * (c + 2) * (c + 2);
@@ -730,4 +960,15 @@ extern "C" int ntg_flatten_fs(void* stream, const float* in, float* out, int64_t
   flatten_fs_kernel<<<(unsigned)batch, kThreads, 0, as_stream(stream)>>>(in, out, a, c);
   note_launch();
   return check_launch("ntg_flatten_fs");
+}
+
+extern "C" int ntg_device_status(void) {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_device_error, sizeof(int)) != cudaSuccess)
+    return check_launch("ntg_device_status");
+  const int zero = 0;
+  if (v != 0 && cudaMemcpyToSymbol(g_device_error, &zero, sizeof(int)) != cudaSuccess)
+    return check_launch("ntg_device_status");
+  if (v != 0) return fail(v, "a bounded device wait ran out in a streamed kernel");
+  return NTG_OK;
 }
