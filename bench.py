@@ -306,7 +306,7 @@ def stencil_roofline(torch, O, dev, pairs=256, reps=4):
     ms = statistics.median(ts) if ts else float('nan')
     nbytes = 4 * q.numel() * 4  # read nngp, ntk; write nngp, ntk
     gbs = nbytes / (ms / 1e3) / 1e9
-    return {'kernel': 'conv3_line_kernel', 'pairs': B, 'bytes': nbytes, 'ms': round(ms, 3),
+    return {'kernel': 'conv3_skew_kernel', 'pairs': B, 'bytes': nbytes, 'ms': round(ms, 3),
             'achieved': round(gbs, 1), 'unit': 'GB/s'}
 
 

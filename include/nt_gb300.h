@@ -83,6 +83,16 @@ uint64_t ntg_launch_count(void);
  * NTG_ERR_WAIT_TIMEOUT if a bounded pipeline wait ran out since the last call. */
 int ntg_device_status(void);
 
+/* ---- tuning (process-wide, thread-safe) --------------------------------- */
+/* Launch parameters an autotuner may change (no counterpart in the reference,
+ * where XLA chooses its own). Values are checked; results do not depend on them.
+ *   NTG_TUNE_STENCIL_RING: input planes in flight per CTA of the 32 x 32
+ *     full-spatial stencil of ntg_conv_fs — 2, 3, 4 (default) or 6. */
+enum { NTG_TUNE_STENCIL_RING = 0, NTG_TUNE_COUNT = 1 };
+int ntg_tune_set(int32_t knob, int32_t value);
+/* Current value of a knob, or -1 for an unknown knob. */
+int32_t ntg_tune_get(int32_t knob);
+
 /* ---- input kernels (requirements.py:518-638, 641-830) ---------------- */
 /* Flat inputs x1 [N1, D], x2 [N2, D] -> nngp [N1, N2] = x1 x2^T / D
  * (requirements.py:542-564). precision 0: FP32 on CUDA cores (workspace

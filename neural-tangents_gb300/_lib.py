@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, 'libntgb300.so')
 
 NTG_ACT_NONE, NTG_ACT_ABRELU, NTG_ACT_ERF = 0, 1, 2
 NTG_PAD_ZERO, NTG_PAD_CIRCULAR = 0, 1
+NTG_TUNE_STENCIL_RING = 0
 CHAIN_MAX_SEG, CHAIN_MAX_LAYERS = 4, 16
 
 ERRORS = {
@@ -54,6 +55,8 @@ SIGNATURES = {
     'ntg_version': ([], C.c_char_p),
     'ntg_launch_count': ([], C.c_uint64),
     'ntg_device_status': ([], C.c_int),
+    'ntg_tune_set': ([_I32, _I32], C.c_int),
+    'ntg_tune_get': ([_I32], C.c_int32),
     'ntg_gram': ([_P, _P, _P, _I64, _I64, _I64, _P, _I32, _P, C.c_size_t], C.c_int),
     'ntg_gram_workspace_bytes': ([_I64, _I64, _I64], C.c_size_t),
     'ntg_gemm': ([_P, _P, _P, _P, _I64, _I64, _I64, _I32], C.c_int),

@@ -27,6 +27,10 @@ int check_launch(const char* what) {
 
 void note_launch(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+static std::atomic<int32_t> g_tune[NTG_TUNE_COUNT] = {{4}};
+
+int32_t tune(int32_t knob) { return g_tune[knob].load(std::memory_order_relaxed); }
+
 }  // namespace ntg
 
 extern "C" const char* ntg_last_error(void) { return ntg::g_last_error.c_str(); }
@@ -35,4 +39,20 @@ extern "C" const char* ntg_version(void) { return "nt_gb300 0.1.0 (sm_103a)"; }
 
 extern "C" uint64_t ntg_launch_count(void) {
   return ntg::g_launches.load(std::memory_order_relaxed);
+}
+
+extern "C" int ntg_tune_set(int32_t knob, int32_t value) {
+  if (knob == NTG_TUNE_STENCIL_RING) {
+    if (value != 2 && value != 3 && value != 4 && value != 6)
+      return ntg::fail(NTG_ERR_INVALID_ARG, "ntg_tune_set: stencil ring must be 2, 3, 4 or 6");
+  } else {
+    return ntg::fail(NTG_ERR_INVALID_ARG, "ntg_tune_set: unknown knob");
+  }
+  ntg::g_tune[knob].store(value, std::memory_order_relaxed);
+  return NTG_OK;
+}
+
+extern "C" int32_t ntg_tune_get(int32_t knob) {
+  if (knob < 0 || knob >= NTG_TUNE_COUNT) return -1;
+  return ntg::tune(knob);
 }

@@ -18,6 +18,7 @@ void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
 int check_launch(const char* what);
 void note_launch(uint64_t n = 1);
+int32_t tune(int32_t knob);  // current value of an NTG_TUNE_* knob
 
 // Tensor-core (tcgen05) split-precision Gram; defined in ntg_gram_tc.cu.
 int gram_tc(cudaStream_t stream, const float* x1, const float* x2, int64_t n1, int64_t n2,

@@ -532,6 +532,261 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ---------------------------------------------------------------------------
+// The same rule for 32 x 32 planes, each thread on a run of a *skewed* row:
+// thread (r, w0) owns the elements (w, (w + r) mod 32) for w = w0 .. w0 + 3,
+// so the w-direction stencil neighbours (w - 1, w' - 1) and (w + 1, w' + 1)
+// are the row neighbours w -/+ 1 — a register, or one shuffle at the ends of
+// the run — masked to zero where w' wraps around. Input planes stream in
+// through the bulk-copy ring; results are written into a double-buffered
+// staging plane and leave by bulk stores, so each plane costs one barrier and
+// no shared-memory halo. Bank-conflict free: for a fixed element slot the 32
+// lanes of a warp touch 32 distinct banks (w0 + r distinct mod 32). The sums
+// run in the same order as conv3_line_kernel's, so both round alike.
+// ---------------------------------------------------------------------------
+constexpr int kSkewC = 32;
+constexpr int kSkewPlane = kSkewC * kSkewC;
+constexpr int kSkewVars = 192;  // per plane: v1[32] | sqrt v1[32] | v2[64] | sqrt v2[64]
+
+template <int RING>
+constexpr size_t skew_smem_bytes() {
+  return sizeof(float) * (2 * RING * kSkewPlane + 4 * kSkewPlane + 2 * kSkewVars) +
+         sizeof(uint64_t) * RING;
+}
+
+__device__ __forceinline__ void bulk_store(float* gdst, const float* ssrc, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst),
+               "r"(smem_addr(ssrc)), "r"(bytes)
+               : "memory");
+}
+
+template <bool HAS_T, int RING>
+__global__ void __launch_bounds__(kThreads)
+    conv3_skew_kernel(const float* __restrict__ in_q, const float* __restrict__ in_t,
+                      float* __restrict__ out_q, float* __restrict__ out_t, int64_t batch,
+                      int64_t n2, int A, ntg_affine_t aff, ntg_act_t act, ntg_var_t var1,
+                      ntg_var_t var2) {
+  extern __shared__ __align__(128) float smem[];
+  __shared__ int s_err;
+  float* ring_q = smem;                           // [RING][plane]
+  float* ring_t = ring_q + RING * kSkewPlane;     // [RING][plane]
+  float* stage_q = ring_t + RING * kSkewPlane;    // [2][plane]
+  float* stage_t = stage_q + 2 * kSkewPlane;      // [2][plane]
+  float* vrow = stage_t + 2 * kSkewPlane;         // [2][kSkewVars]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(vrow + 2 * kSkewVars);
+  const int nlines = 2 * A - 1;
+  const int64_t b = blockIdx.x / nlines;
+  const int delta = (int)(blockIdx.x - b * nlines) - (A - 1);
+  if (b >= batch) return;
+  const int i_lo = delta < 0 ? -delta : 0;
+  const int len = (delta < 0 ? A : A - delta) - i_lo;
+  const int64_t pair_stride = (int64_t)A * A * kSkewPlane;
+  const uint32_t bytes = (uint32_t)(kSkewPlane * sizeof(float)) * (HAS_T ? 2u : 1u);
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int w0 = (lane & 7) * 4;
+  const int r = (tid >> 5) * 4 + (lane >> 3);
+  const bool has_act = act.kind != NTG_ACT_NONE;
+
+  int u[4];
+  float mL[4], mR[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int w = w0 + k, wq = (w + r) & (kSkewC - 1);
+    u[k] = w * kSkewC + wq;
+    mL[k] = (w >= 1 && wq >= 1) ? 1.f : 0.f;
+    mR[k] = (w <= kSkewC - 2 && wq <= kSkewC - 2) ? 1.f : 0.f;
+  }
+  int64_t i1, i2;
+  pair_of(b, n2, i1, i2);
+
+  // variance rows of plane j (row i = i_lo + j): v1 at (i, w), v2 at (i + delta, w')
+  auto load_vars = [&](int j) {
+    const int i = i_lo + j;
+    float* vb = vrow + (j & 1) * kSkewVars;
+    if (tid < kSkewC) {
+      const float v =
+          __ldg(var1.base + i1 * var1.s_n + (int64_t)i * var1.s_a + (int64_t)tid * var1.s_c);
+      vb[tid] = v;
+      vb[32 + tid] = sqrt_var(v);
+    } else if (tid < 3 * kSkewC) {
+      const int x = tid - kSkewC;
+      const float v = __ldg(var2.base + i2 * var2.s_n + (int64_t)(i + delta) * var2.s_a +
+                            (int64_t)(x & (kSkewC - 1)) * var2.s_c);
+      vb[64 + x] = v;
+      vb[128 + x] = sqrt_var(v);
+    }
+  };
+
+  if (tid == 0) {
+    s_err = 0;
+    for (int sl = 0; sl < RING; ++sl)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[sl])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (has_act) load_vars(0);
+  __syncthreads();
+
+  auto issue = [&](int p) {  // plane p of the line into slot p % RING
+    const int i = i_lo + p;
+    const int sl = p % RING;
+    const uint32_t bar = smem_addr(&bars[sl]);
+    const int64_t off = b * pair_stride + ((int64_t)i * A + i + delta) * kSkewPlane;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_addr(ring_q + sl * kSkewPlane)), "l"(in_q + off), "r"(kSkewPlane * 4u),
+        "r"(bar)
+        : "memory");
+    if (HAS_T)
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+          ::"r"(smem_addr(ring_t + sl * kSkewPlane)), "l"(in_t + off), "r"(kSkewPlane * 4u),
+          "r"(bar)
+          : "memory");
+  };
+  int next = 0;  // next plane thread 0 issues
+  if (tid == 0)
+    for (; next < RING && next < len; ++next) issue(next);
+
+  // plane p of the line from its ring slot, in this thread's skewed order (zero outside)
+  auto take = [&](int p, float (&q)[4], float (&t)[4]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) q[k] = t[k] = 0.f;
+    if (p >= len) return;
+    const int sl = p % RING;
+    if (!s_err && !bar_wait(smem_addr(&bars[sl]), (uint32_t)((p / RING) & 1))) s_err = 1;
+    const float* sq = ring_q + sl * kSkewPlane;
+    const float* st = ring_t + sl * kSkewPlane;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      q[k] = sq[u[k]];
+      if (HAS_T) t[k] = st[u[k]];
+    }
+  };
+
+  const float inv9 = 1.f / 9.f;
+  const ActC ac = act_consts(act);
+  const P2 W2 = p2s(aff.w2 * inv9), B2 = p2s(aff.b2);
+  const P2 TW = p2s(aff.ntk_w2 * inv9), TN = p2s(aff.ntk_nn), TC = p2s(aff.ntk_c);
+  float qm[4], tm[4], q0[4], t0[4], qp[4], tp[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) qm[k] = tm[k] = 0.f;
+  take(0, q0, t0);
+  for (int j = 0; j < len; ++j) {
+    take(j + 1, qp, tp);
+    if (has_act && j + 1 < len) load_vars(j + 1);  // read after the next barrier
+    const int i = i_lo + j;
+    float hq[4], ht[4], sq[4], st[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      hq[k] = (qm[k] + q0[k]) + qp[k];
+      ht[k] = HAS_T ? (tm[k] + t0[k]) + tp[k] : 0.f;
+    }
+    {
+      const float lq = __shfl_up_sync(0xffffffffu, hq[3], 1, 8);
+      const float rq = __shfl_down_sync(0xffffffffu, hq[0], 1, 8);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float L = k == 0 ? lq : hq[k - 1], R = k == 3 ? rq : hq[k + 1];
+        sq[k] = fmaf(R, mR[k], fmaf(L, mL[k], hq[k]));
+      }
+    }
+    if (HAS_T) {
+      const float lt = __shfl_up_sync(0xffffffffu, ht[3], 1, 8);
+      const float rt = __shfl_down_sync(0xffffffffu, ht[0], 1, 8);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float L = k == 0 ? lt : ht[k - 1], R = k == 3 ? rt : ht[k + 1];
+        st[k] = fmaf(R, mR[k], fmaf(L, mL[k], ht[k]));
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) st[k] = 0.f;
+    }
+    // affine rule on packed pairs (same rounding as apply_affine)
+    P2 q[2], t[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const P2 cq = p2(sq[2 * h], sq[2 * h + 1]), ct = p2(st[2 * h], st[2 * h + 1]);
+      q[h] = fma2(W2, cq, B2);
+      const P2 nn = aff.nn_scaled ? q[h] : mul2(cq, p2s(inv9));
+      t[h] = fma2(TW, ct, fma2(TN, nn, TC));
+    }
+    if (has_act) {
+      const float* vb = vrow + (j & 1) * kSkewVars;
+      const float4 v1 = *reinterpret_cast<const float4*>(vb + w0);
+      const float4 s1 = *reinterpret_cast<const float4*>(vb + 32 + w0);
+      float v2[4], s2[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        v2[k] = vb[64 + w0 + r + k];
+        s2[k] = vb[128 + w0 + r + k];
+      }
+      if (act.kind == NTG_ACT_ABRELU && act.stabilize <= 0.f) {
+        abrelu2(ac, q[0], t[0], p2(v1.x, v1.y), p2(v2[0], v2[1]), p2(s1.x, s1.y),
+                p2(s2[0], s2[1]));
+        abrelu2(ac, q[1], t[1], p2(v1.z, v1.w), p2(v2[2], v2[3]), p2(s1.z, s1.w),
+                p2(s2[2], s2[3]));
+      } else {
+        const float a1[4] = {v1.x, v1.y, v1.z, v1.w}, b1[4] = {s1.x, s1.y, s1.z, s1.w};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          float qa, qb, ta, tb;
+          p2u(q[h], qa, qb);
+          p2u(t[h], ta, tb);
+          act_apply(ac, qa, ta, a1[2 * h], v2[2 * h], b1[2 * h], s2[2 * h]);
+          act_apply(ac, qb, tb, a1[2 * h + 1], v2[2 * h + 1], b1[2 * h + 1], s2[2 * h + 1]);
+          q[h] = p2(qa, qb);
+          t[h] = p2(ta, tb);
+        }
+      }
+    }
+    float* gq = stage_q + (j & 1) * kSkewPlane;
+    float* gt = stage_t + (j & 1) * kSkewPlane;
+    {
+      float vq[4], vt[4];
+      p2u(q[0], vq[0], vq[1]);
+      p2u(q[1], vq[2], vq[3]);
+      p2u(t[0], vt[0], vt[1]);
+      p2u(t[1], vt[2], vt[3]);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        gq[u[k]] = vq[k];
+        if (out_t) gt[u[k]] = vt[k];
+      }
+    }
+    // staging writes -> visible to the bulk-copy engine; the store of plane j - 1
+    // has finished reading its buffer before anyone writes it again (plane j + 1)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      const int64_t off = b * pair_stride + ((int64_t)i * A + i + delta) * kSkewPlane;
+      bulk_store(out_q + off, gq, kSkewPlane * 4u);
+      if (out_t) bulk_store(out_t + off, gt, kSkewPlane * 4u);
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      // plane j + 1 has been read by every thread: its slot takes plane j + 1 + RING
+      if (!s_err)
+        for (; next < len && next <= j + 1 + RING; ++next) issue(next);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      qm[k] = q0[k]; tm[k] = t0[k];
+      q0[k] = qp[k]; t0[k] = tp[k];
+    }
+  }
+  if (tid == 0) {
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    if (s_err) {
+      atomicExch(&g_device_error, NTG_ERR_WAIT_TIMEOUT);
+      // let every issued copy land (bounded) before the CTA's shared memory is released
+      for (int p = next > RING ? next - RING : 0; p < next; ++p)
+        bar_wait(smem_addr(&bars[p % RING]), (uint32_t)((p / RING) & 1));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Diagonal-spatial conv rule: [B, A, C] box filter (linear.py:3381-3437).
 // ---------------------------------------------------------------------------
 __global__ void conv_ds_kernel(const float* __restrict__ in_q, const float* __restrict__ in_t,
@@ -808,6 +1063,28 @@ extern "C" int ntg_input_fs(void* stream, const float* x1, const float* x2, int6
   return check_launch("ntg_input_fs");
 }
 
+template <int RING>
+cudaError_t launch_skew(cudaStream_t s, int64_t blocks, const float* in_q, const float* in_t,
+                        float* out_q, float* out_t, int64_t batch, int64_t n2, int64_t a,
+                        ntg_affine_t aff, ntg_act_t act, ntg_var_t var1, ntg_var_t var2) {
+  constexpr size_t sm = skew_smem_bytes<RING>();
+  cudaError_t e;
+  if (in_t) {
+    e = cudaFuncSetAttribute(conv3_skew_kernel<true, RING>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e == cudaSuccess)
+      conv3_skew_kernel<true, RING><<<(unsigned)blocks, kThreads, sm, s>>>(
+          in_q, in_t, out_q, out_t, batch, n2, (int)a, aff, act, var1, var2);
+  } else {
+    e = cudaFuncSetAttribute(conv3_skew_kernel<false, RING>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e == cudaSuccess)
+      conv3_skew_kernel<false, RING><<<(unsigned)blocks, kThreads, sm, s>>>(
+          in_q, nullptr, out_q, out_t, batch, n2, (int)a, aff, act, var1, var2);
+  }
+  return e;
+}
+
 extern "C" int ntg_conv_fs(void* stream, const float* in_q, const float* in_t, float* out_q,
                            float* out_t, int64_t batch, int64_t n2, int64_t a, int64_t c,
                            int32_t fh, int32_t fw, int32_t sh, int32_t sw, int32_t ph, int32_t pw,
@@ -826,7 +1103,18 @@ extern "C" int ntg_conv_fs(void* stream, const float* in_q, const float* in_t, f
   const bool aligned = ((reinterpret_cast<uintptr_t>(in_q) | reinterpret_cast<uintptr_t>(in_t) |
                          reinterpret_cast<uintptr_t>(out_q) | reinterpret_cast<uintptr_t>(out_t)) &
                         15) == 0;
-  if (line_ok && aligned) {
+  if (line_ok && aligned && c == kSkewC) {
+    int64_t blocks = batch * (2 * a - 1);
+    NTG_REQUIRE(blocks < (1ll << 31), "ntg_conv_fs: grid too large");
+    cudaError_t e;
+    switch (tune(NTG_TUNE_STENCIL_RING)) {
+      case 2: e = launch_skew<2>(s, blocks, in_q, in_t, out_q, out_t, batch, n2, a, aff, act, var1, var2); break;
+      case 3: e = launch_skew<3>(s, blocks, in_q, in_t, out_q, out_t, batch, n2, a, aff, act, var1, var2); break;
+      case 6: e = launch_skew<6>(s, blocks, in_q, in_t, out_q, out_t, batch, n2, a, aff, act, var1, var2); break;
+      default: e = launch_skew<4>(s, blocks, in_q, in_t, out_q, out_t, batch, n2, a, aff, act, var1, var2); break;
+    }
+    if (e != cudaSuccess) return fail(NTG_ERR_CUDA, std::string("ntg_conv_fs: ") + cudaGetErrorString(e));
+  } else if (line_ok && aligned) {
     int64_t blocks = batch * (2 * a - 1);
     NTG_REQUIRE(blocks < (1ll << 31), "ntg_conv_fs: grid too large");
     const size_t sm = sizeof(float) * (2 * kRing * c * c + 4 * (c + 2) * (c + 2)) +

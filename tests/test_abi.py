@@ -59,3 +59,14 @@ def test_python_binding_signatures_cover_header():
     spec.loader.exec_module(mod)
     missing = [s for s in declared_symbols() if s not in mod.SIGNATURES]
     assert not missing, missing
+
+
+def test_tuning_knobs_are_checked(lib):
+    lib.ntg_tune_get.restype = ctypes.c_int32
+    lib.ntg_tune_set.restype = ctypes.c_int
+    assert lib.ntg_tune_get(0) == 4            # stencil ring default
+    assert lib.ntg_tune_get(99) == -1
+    assert lib.ntg_tune_set(0, 5) == 1         # not a supported ring depth
+    assert lib.ntg_tune_set(7, 1) == 1         # unknown knob
+    assert lib.ntg_tune_set(0, 6) == 0 and lib.ntg_tune_get(0) == 6
+    assert lib.ntg_tune_set(0, 4) == 0 and lib.ntg_tune_get(0) == 4
