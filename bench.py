@@ -446,10 +446,22 @@ def profile_stencil(pairs: int):
     print(json.dumps({'profile_stencil': pairs, **st}))
 
 
+def profile_fwd_bwd(n_s: int):
+    """The fwd+bwd measurement alone: x_t [2 n_s], x_s [n_s], tiles of n_s (launch lists)."""
+    import torch
+    import nt_gb300 as nt
+    from nt_gb300 import stax
+    _, _, kf = stax.serial(*myrtle5(stax))
+    x = torch.from_numpy(make_inputs(2000)).cuda()
+    r = fwd_bwd_timing(torch, nt, kf, x, n_t=2 * n_s, n_s=n_s, bs=n_s)
+    print(json.dumps({'profile_fwd_bwd': n_s, **r}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--profile-tile', type=int, default=0)
     ap.add_argument('--profile-stencil', type=int, default=0)
+    ap.add_argument('--profile-fwd-bwd', type=int, default=0)
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=3)
@@ -462,6 +474,8 @@ def main():
         profile_tile(args.profile_tile)
     elif args.profile_stencil:
         profile_stencil(args.profile_stencil)
+    elif args.profile_fwd_bwd:
+        profile_fwd_bwd(args.profile_fwd_bwd)
     elif args.impl == 'reference':
         run_reference(args)
     else:

@@ -173,10 +173,12 @@ class AffineFn(torch.autograd.Function):
         gu, gut = bwd(gq, gt, qn.numel())
         gc1i = bwd(gc1, None, c1n.numel())[0].reshape(c1n.shape)
         gc2i = None if c2n.numel() == 0 else bwd(gc2, None, c2n.numel())[0].reshape(c2n.shape)
-        acc = _hyper([(qn, tn), (c1n, None), (_opt(c2n), None)], [(gq, gt), (gc1, None),
-                     (gc2 if c2n.numel() else None, None)], w2, b2, qn.device)
-        gw2 = acc[0].float()
-        gb2 = acc[1].float()
+        if ctx.needs_input_grad[0] or ctx.needs_input_grad[1]:
+            acc = _hyper([(qn, tn), (c1n, None), (_opt(c2n), None)], [(gq, gt), (gc1, None),
+                         (gc2 if c2n.numel() else None, None)], w2, b2, qn.device)
+            gw2, gb2 = acc[0].float(), acc[1].float()
+        else:
+            gw2 = gb2 = None
         return (gw2, gb2, gu.reshape(qn.shape), None if ctx.zero_t else gut.reshape(qn.shape),
                 gc1i, gc2i)
 
@@ -244,14 +246,57 @@ class ConvFn(torch.autograd.Function):
                 outs.append(gin)
             return outs
 
+        def back_symmetric(g, gtt, in_shape, bnd):
+            # A stride-1 window centred on its output (odd filter, padding (f - 1) / 2, same
+            # size) is its own transpose, so the adjoint is the forward stencil kernel with
+            # the roles of the two tensors exchanged:
+            #   g_nngp_in = s (W^2 Sum g + W^2 Sum g_ntk),  g_ntk_in = s W^2 Sum g_ntk.
+            lead = tuple(in_shape[:bnd])
+            a = in_shape[bnd]
+            c = in_shape[bnd + 2] if nsp == 2 else 1
+            n2 = 0 if bnd == 1 else in_shape[1]
+            batch = int(math.prod(lead))
+
+            def four(x):
+                return None if x is None else _as4(x.contiguous(), bnd)
+
+            if gtt is None:
+                oq, _ = O.conv_fs(four(g), None, batch, n2, a, c, fh, fw, sh, sw, ph, pw, ao, co,
+                                  circ, O.affine(w2, 0., 0., 0., 0., False), O.NO_ACT, O.NO_VAR,
+                                  O.NO_VAR, False, lead)
+                return [oq.reshape(in_shape), None]
+            gti_, gqi_ = O.conv_fs(four(gtt), four(g), batch, n2, a, c, fh, fw, sh, sw, ph, pw, ao,
+                                   co, circ, O.affine(w2, 0., w2, w2, 0., False), O.NO_ACT,
+                                   O.NO_VAR, O.NO_VAR, True, lead)
+            return [gqi_.reshape(in_shape), gti_.reshape(in_shape)]
+
+        symmetric = (sh == 1 and sw == 1 and fh % 2 == 1 and fw % 2 == 1 and
+                     2 * ph + 1 == fh and 2 * pw + 1 == fw and ao == qs[2] and
+                     (nsp == 1 or co == qs[4]))
         # the output NTK's cotangent reaches the input nngp through ntk_out = nngp_out + ...
         # even when the input NTK is the scalar zero of an input kernel
-        gqi, gti = back(gq, gt, qs, 2, not zero_t)
-        gc1i = back(gc1, None, c1s, 1)[0]
-        gc2i = None if c2s is None else back(gc2, None, c2s, 1)[0]
-        acc = _hyper([(qn, tn), (c1n, None), (_opt(c2n), None)], [(gq, gt), (gc1, None),
-                     (gc2 if c2s is not None else None, None)], w2, b2, dev)
-        return acc[0].float(), acc[1].float(), gqi, gti, gc1i, gc2i, None
+        if symmetric and (gq is not None or gt is not None):
+            gqi, gti = back_symmetric(gq if gq is not None else torch.zeros_like(gt), gt, qs, 2)
+            gti = None if zero_t else gti
+        else:
+            gqi, gti = back(gq, gt, qs, 2, not zero_t)
+        if symmetric and gc1 is not None:
+            gc1i = back_symmetric(gc1, None, c1s, 1)[0]
+        else:
+            gc1i = back(gc1, None, c1s, 1)[0]
+        if c2s is None:
+            gc2i = None
+        elif symmetric and gc2 is not None:
+            gc2i = back_symmetric(gc2, None, c2s, 1)[0]
+        else:
+            gc2i = back(gc2, None, c2s, 1)[0]
+        if ctx.needs_input_grad[0] or ctx.needs_input_grad[1]:
+            acc = _hyper([(qn, tn), (c1n, None), (_opt(c2n), None)], [(gq, gt), (gc1, None),
+                         (gc2 if c2s is not None else None, None)], w2, b2, dev)
+            gw2, gb2 = acc[0].float(), acc[1].float()
+        else:
+            gw2 = gb2 = None
+        return gw2, gb2, gqi, gti, gc1i, gc2i, None
 
 
 # ---------------------------------------------------------------------------

@@ -127,6 +127,179 @@ __global__ void act_bwd_kernel(const float* __restrict__ q, const float* __restr
   }
 }
 
+// act_vjp with the library's one-instruction square roots and reciprocals and
+// its arc tangent: the angle atan2(s, q) comes from the half-angle identities
+// theta = 2 atan(s / (r + q)) (q >= 0), pi - 2 atan(s / (r - q)) (q < 0),
+// r = |(q, s)|, and pi / 2 where s = q = 0 — the same derivative conventions
+// as act_vjp (tolerance 1e-30 in the arctan2 and sqrt derivatives).
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+__device__ __forceinline__ void act_vjp_fast(const ntg_act_t& act, const ActC& c, float q,
+                                             float t, float v1, float v2, float gq, float gt,
+                                             float& oq, float& ot, float& ov1, float& ov2) {
+  const float tol = 1e-30f;
+  if (act.kind == NTG_ACT_ABRELU) {
+    const float d = prod_minus_sq(v1, v2, q, c.comp);
+    const float s = sqrt_approx(fmaxf(d, 0.f));
+    const float den2 = fmaf(s, s, q * q);
+    const float r = sqrt_approx(den2);
+    const float hd = r + fabsf(q);
+    const float p = atan_unit(s * rcp_approx(hd));
+    float th = (q < 0.f) ? fmaf(-2.f, p, kPi) : 2.f * p;
+    th = (hd == 0.f) ? 0.5f * kPi : th;
+    const float dot = fmaf(-c.factor, th, c.half);
+    const float g_dot = fmaf(q, gq, t * gt);
+    float g_s = c.factor * gq;
+    float g_q = dot * gq;
+    ot = dot * gt;
+    const float g_th = -c.factor * g_dot;
+    const float inv = rcp_approx(fmaxf(den2, tol));
+    g_s = fmaf(g_th * q, inv, g_s);
+    g_q = fmaf(-g_th * s, inv, g_q);
+    const float g_d = (d > tol) ? 0.5f * g_s * rsqrt_approx(d) : 0.f;
+    g_q = fmaf(-2.f * q, g_d, g_q);
+    ov1 = g_d * v2;
+    ov2 = g_d * v1;
+    oq = g_q;
+  } else if (act.kind == NTG_ACT_ERF) {
+    const float qb = c.b2 * q, tb = c.b2 * t;
+    const float d1 = fmaf(2.f * c.b2, v1, 1.f), d2 = fmaf(2.f * c.b2, v2, 1.f);
+    const float y = 2.f * qb;
+    const float dd = prod_minus_sq(d1, d2, y, c.comp);
+    const float s = sqrt_approx(fmaxf(dd, 0.f));
+    const float gq2 = c.a2 * gq, gt2 = c.a2 * gt;
+    const float rs = rcp_approx(s);
+    const float dot = (4.f / kPi) * rs;
+    const float g_tb = dot * gt2;
+    const float g_dot = tb * gt2;
+    float g_s = -(4.f / kPi) * rs * rs * g_dot;
+    const float g_phi = (2.f / kPi) * gq2;
+    const float den = fmaf(s, s, y * y);
+    const float iden = den > 0.f ? rcp_approx(den) : 0.f;
+    const float g_y = g_phi * s * iden;
+    g_s = fmaf(-g_phi * y, iden, g_s);
+    float g_qb = 2.f * g_y;
+    const float g_dd = (dd > tol) ? 0.5f * g_s * rsqrt_approx(dd) : 0.f;
+    g_qb = fmaf(-4.f * y, g_dd, g_qb);
+    oq = c.b2 * g_qb;
+    ot = c.b2 * g_tb;
+    ov1 = c.b2 * 2.f * (g_dd * d2);
+    ov2 = c.b2 * 2.f * (g_dd * d1);
+  } else {
+    oq = gq;
+    ot = gt;
+    ov1 = ov2 = 0.f;
+  }
+}
+
+// Activation VJP on full-spatial [B, A, A, C, C] kernels with C a power of two
+// in [4, 32] and A^2 C^2 a multiple of 1024: a CTA takes chunks of 1024
+// consecutive entries (one pair; 4 entries per thread, vector loads). The
+// variance cotangents of a chunk are summed by warp shuffles and shared-memory
+// atomics per (plane, row) for var1 and per (plane, column) for var2, and
+// leave with one global atomic per key instead of one per entry.
+__global__ void __launch_bounds__(kT)
+    act_bwd_fs_kernel(const float* __restrict__ q, const float* __restrict__ t,
+                      const float* __restrict__ gq, const float* __restrict__ gt,
+                      float* __restrict__ oq, float* __restrict__ ot, int64_t batch, int64_t n2,
+                      int A, int C, ntg_act_t act, ntg_var_t var1, ntg_var_t var2, VarGrad gv1,
+                      VarGrad gv2) {
+  __shared__ float s1[256], s2[256];
+  const int64_t M = (int64_t)A * A * C * C;
+  const int64_t chunks = batch * (M / 1024);
+  const ActC ac = act_consts(act);
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int nkeys = 1024 / C;
+  const int seg = C / 4;                                // lanes per row
+  const int pseg = C * C / 4 < 32 ? C * C / 4 : 32;     // lanes per plane within a warp
+  for (int64_t ch = blockIdx.x; ch < chunks; ch += gridDim.x) {
+    for (int k = tid; k < nkeys; k += kT) s1[k] = s2[k] = 0.f;
+    __syncthreads();
+    const int64_t base = ch * 1024;
+    const int64_t b = base / M;
+    const int64_t m0 = base - b * M;
+    const int64_t e = base + 4 * tid;
+    const int64_t m = m0 + 4 * tid;
+    const int wq = (int)(m % C);
+    const int64_t row = m / C;
+    const int w = (int)(row % C);
+    const int64_t pl = row / C;
+    const int hq = (int)(pl % A), h = (int)(pl / A);
+    int64_t i1, i2;
+    pair_of(b, n2, i1, i2);
+    const float v1 = var_at(var1, i1, h, w);
+    const float4 Q = *reinterpret_cast<const float4*>(q + e);
+    const float4 T = t ? *reinterpret_cast<const float4*>(t + e) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 GQ = gq ? *reinterpret_cast<const float4*>(gq + e) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 GT = gt ? *reinterpret_cast<const float4*>(gt + e) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float qa[4] = {Q.x, Q.y, Q.z, Q.w}, ta[4] = {T.x, T.y, T.z, T.w};
+    const float ga[4] = {GQ.x, GQ.y, GQ.z, GQ.w}, gb[4] = {GT.x, GT.y, GT.z, GT.w};
+    float rq[4], rt[4], r2[4], r1 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float v2 = var_at(var2, i2, hq, wq + k);
+      float o1;
+      act_vjp_fast(act, ac, qa[k], ta[k], v1, v2, ga[k], gb[k], rq[k], rt[k], o1, r2[k]);
+      r1 += o1;
+    }
+    *reinterpret_cast<float4*>(oq + e) = make_float4(rq[0], rq[1], rq[2], rq[3]);
+    if (ot) *reinterpret_cast<float4*>(ot + e) = make_float4(rt[0], rt[1], rt[2], rt[3]);
+    // var1 key: the row (4 tid / C) of the chunk; var2 key: (plane of the chunk, column)
+    for (int o = 1; o < seg; o <<= 1) r1 += __shfl_xor_sync(0xffffffffu, r1, o);
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      for (int o = seg; o < pseg; o <<= 1) r2[k] += __shfl_xor_sync(0xffffffffu, r2[k], o);
+    if ((lane & (seg - 1)) == 0) atomicAdd(&s1[(4 * tid) / C], r1);
+    if ((lane & (pseg - 1)) < seg) {
+      const int kb = ((4 * tid) / (C * C)) * C + wq;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) atomicAdd(&s2[kb + k], r2[k]);
+    }
+    __syncthreads();
+    for (int k = tid; k < nkeys; k += kT) {
+      const int64_t rr = m0 / C + k;                 // (h, h', w) of row k
+      const int64_t pp = m0 / ((int64_t)C * C) + k / C;  // (h, h') of key k
+      if (gv1.base && s1[k] != 0.f)
+        atomicAdd(gv1.base + i1 * gv1.s_n + (rr / C / A) * gv1.s_a + (rr % C) * gv1.s_c, s1[k]);
+      if (gv2.base && s2[k] != 0.f)
+        atomicAdd(gv2.base + i2 * gv2.s_n + (pp % A) * gv2.s_a + (k % C) * gv2.s_c, s2[k]);
+    }
+    __syncthreads();
+  }
+}
+
+// Transpose of a pooling rule with full, non-overlapping windows (stride ==
+// window, no padding, A and C multiples of the window): every input entry
+// takes its window's cotangent times the forward's weight (1 / window size for
+// the average, 1 for the sum). Four entries per thread, vector stores.
+__global__ void __launch_bounds__(kT)
+    pool_t_block_kernel(const float* __restrict__ gout, float* __restrict__ gin, int64_t batch,
+                        int A, int C, int wa, int wc, float weight) {
+  const int Ao = A / wa, Co = C / wc;
+  const int64_t per_b = (int64_t)A * A * C * C;
+  const int64_t n4 = batch * per_b / 4;
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n4;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t idx = 4 * v;
+    const int64_t b = idx / per_b;
+    int64_t r = idx - b * per_b;
+    const int cp = (int)(r % C); r /= C;
+    const int c = (int)(r % C); r /= C;
+    const int ap = (int)(r % A);
+    const int a = (int)(r / A);
+    const float* g = gout + b * (int64_t)Ao * Ao * Co * Co +
+                     (((int64_t)(a / wa) * Ao + ap / wa) * Co + c / wc) * Co;
+    float o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) o[k] = __ldg(g + (cp + k) / wc) * weight;
+    *reinterpret_cast<float4*>(gin + idx) = make_float4(o[0], o[1], o[2], o[3]);
+  }
+}
+
 // Cotangent of the unscaled stencil sums of a conv/dense affine rule:
 //   q = w2 s U + b2,  t = tw2 s Ut + nn_w (nn_scaled ? q : s U) + c
 // gives  gU = s (w2 (gq + [nn_scaled] nn_w gt) + [!nn_scaled] nn_w gt),  gUt = tw2 s gt.
@@ -149,16 +322,18 @@ __global__ void affine_bwd_kernel(const float* __restrict__ gq, const float* __r
 __global__ void affine_hyper_kernel(const float* __restrict__ q, const float* __restrict__ t,
                                     const float* __restrict__ gq, const float* __restrict__ gt,
                                     int64_t n, float w2, float b2, double* __restrict__ out) {
-  double sw = 0.0, sb = 0.0;
+  // FP32 partial sums per thread (a few hundred terms each), FP64 across threads
+  float fw = 0.f, fb = 0.f;
   const float inv = w2 != 0.f ? 1.f / w2 : 0.f;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const float g1 = gq ? gq[i] : 0.f;
     const float g2 = (gt && t) ? gt[i] : 0.f;
-    sw += (double)g1 * (double)((q[i] - b2) * inv);
-    if (g2 != 0.f) sw += (double)g2 * (double)((t[i] - b2) * inv);
-    sb += (double)g1 + (double)g2;
+    fw = fmaf(g1, (q[i] - b2) * inv, fw);
+    if (g2 != 0.f) fw = fmaf(g2, (t[i] - b2) * inv, fw);
+    fb += g1 + g2;
   }
+  double sw = fw, sb = fb;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     sw += __shfl_xor_sync(0xffffffffu, sw, o);
@@ -516,8 +691,20 @@ extern "C" int ntg_act_bwd(void* stream, const float* q, const float* t, const f
   // variance cotangents are compact [n, A, C] arrays
   VarGrad g1{gvar1, a * c, c, 1}, g2{gvar2, a * c, c, 1};
   const int64_t m = diag_spatial ? a * c : a * a * c * c;
-  act_bwd_kernel<<<grid_for(batch * m), kT, 0, as_stream(stream)>>>(
-      q, t, gq, gt, oq, ot, batch, n2, a, c, diag_spatial, act, var1, var2, g1, g2);
+  const bool pow2 = c >= 4 && c <= 32 && (c & (c - 1)) == 0;
+  const bool aligned = ((reinterpret_cast<uintptr_t>(q) | reinterpret_cast<uintptr_t>(t) |
+                         reinterpret_cast<uintptr_t>(gq) | reinterpret_cast<uintptr_t>(gt) |
+                         reinterpret_cast<uintptr_t>(oq) | reinterpret_cast<uintptr_t>(ot)) &
+                        15) == 0;
+  if (!diag_spatial && pow2 && m % 1024 == 0 && aligned && a <= (1 << 20)) {
+    const int64_t chunks = batch * (m / 1024);
+    const int grid = (int)(chunks < 152 * 8 ? chunks : 152 * 8);
+    act_bwd_fs_kernel<<<grid, kT, 0, as_stream(stream)>>>(q, t, gq, gt, oq, ot, batch, n2,
+                                                          (int)a, (int)c, act, var1, var2, g1, g2);
+  } else {
+    act_bwd_kernel<<<grid_for(batch * m), kT, 0, as_stream(stream)>>>(
+        q, t, gq, gt, oq, ot, batch, n2, a, c, diag_spatial, act, var1, var2, g1, g2);
+  }
   note_launch();
   return check_launch("ntg_act_bwd");
 }
@@ -566,6 +753,16 @@ extern "C" int ntg_pool_bwd(void* stream, const float* gout, float* gin, int64_t
   NTG_REQUIRE(gout && gin && batch > 0, "ntg_pool_bwd: bad arguments");
   NTG_REQUIRE(wa <= 6 && wc <= 6, "ntg_pool_bwd: windows up to 6 per axis");
   const int64_t total = diag_spatial ? batch * a * c : batch * a * a * c * c;
+  const bool blocks = !diag_spatial && pa == 0 && pc == 0 && sa == wa && sc == wc &&
+                      a % wa == 0 && c % wc == 0 && ao == a / wa && co == c / wc && c % 4 == 0 &&
+                      ((reinterpret_cast<uintptr_t>(gin) & 15) == 0);
+  if (blocks) {
+    const float weight = average ? 1.f / (float)(wa * wa * wc * wc) : 1.f;
+    pool_t_block_kernel<<<grid_for(total / 4), kT, 0, as_stream(stream)>>>(
+        gout, gin, batch, (int)a, (int)c, wa, wc, weight);
+    note_launch();
+    return check_launch("ntg_pool_bwd");
+  }
   pool_t_kernel<<<grid_for(total), kT, 0, as_stream(stream)>>>(
       gout, gin, batch, a, c, ao, co, wa, wc, sa, sc, pa, pc, pad_mode == NTG_PAD_CIRCULAR,
       diag_spatial, average, normalize_edges);

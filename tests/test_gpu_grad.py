@@ -153,3 +153,79 @@ def test_batched_checkpointed_backward_equals_unbatched(nt):
     b = xs.clone().requires_grad_(True)
     (w * nt.batch(kf, batch_size=2)(xt, b, 'ntk')).sum().backward()
     torch.testing.assert_close(b.grad, a.grad, rtol=1e-4, atol=1e-6)
+
+
+def test_conv_input_gradients_power_of_two_planes(nt):
+    """8 x 8 images: the vectorised activation VJP (C a power of two), the block
+    pooling transpose and the stencil-as-its-own-transpose path."""
+    rng = np.random.default_rng(4)
+    x1 = rng.standard_normal((2, 8, 8, 3))
+    x2 = rng.standard_normal((2, 8, 8, 3))
+    wq, wt = rng.standard_normal((2, 2)), rng.standard_normal((2, 2))
+
+    def layers(m):
+        return [m.Conv(2, (3, 3), padding='SAME', W_std=1.4, b_std=0.1), m.Relu(),
+                m.Conv(2, (3, 3), padding='SAME', W_std=1.3, b_std=0.0), m.Relu(),
+                m.AvgPool((2, 2), (2, 2)), m.Conv(2, (3, 3), padding='SAME', W_std=1.2, b_std=0.2),
+                m.Erf(), m.GlobalAvgPool(), m.Dense(1, 1.1, 0.05)]
+
+    def loss_oracle(a, b):
+        q, t = o.serial(*layers(o))(a, b, ('nngp', 'ntk'))
+        return float(np.sum(wq * q) + np.sum(wt * t))
+
+    t1 = torch.tensor(x1, dtype=torch.float32, device='cuda', requires_grad=True)
+    t2 = torch.tensor(x2, dtype=torch.float32, device='cuda', requires_grad=True)
+    q, t = nt.stax.serial(*layers(nt.stax))[2](t1, t2, ('nngp', 'ntk'))
+    loss = (torch.from_numpy(wq).float().cuda() * q).sum() + \
+        (torch.from_numpy(wt).float().cuda() * t).sum()
+    loss.backward()
+    g1, g2 = t1.grad.cpu().numpy(), t2.grad.cpu().numpy()
+    scale = max(np.abs(g1).max(), np.abs(g2).max())
+    for idx in [(0, 0, 0, 0), (1, 3, 2, 1), (0, 7, 7, 2), (1, 4, 5, 0)]:
+        want = fd(lambda a: loss_oracle(a, x2), x1, idx)
+        assert abs(g1[idx] - want) < 3e-3 * scale, (idx, g1[idx], want)
+    for idx in [(0, 1, 1, 0), (1, 6, 0, 2)]:
+        want = fd(lambda b: loss_oracle(x1, b), x2, idx)
+        assert abs(g2[idx] - want) < 3e-3 * scale, (idx, g2[idx], want)
+
+
+@pytest.mark.parametrize('kind', ['relu', 'erf'])
+def test_vectorised_activation_vjp_matches_elementwise_kernel(nt, kind):
+    """ntg_act_bwd on 16-byte aligned buffers (chunked kernel with reduced variance
+    cotangents) against the same call on buffers offset by one float (the
+    elementwise kernel with one atomic per entry)."""
+    from nt_gb300 import _lib as L
+    g = torch.Generator(device='cuda').manual_seed(11)
+    n1, n2, A, C = 2, 3, 8, 8
+    shp = (n1 * n2, A, A, C, C)
+    cov = torch.rand((n1 + n2, A, A, C, C), device='cuda', generator=g) * 0.2
+    # positive diagonal (variances) well above the cross terms
+    for a in range(A):
+        for c in range(C):
+            cov[:, a, a, c, c] += 2.
+    v1 = L.Var(cov[:n1].data_ptr(), A * A * C * C, A * C * C + C * C, C + 1)
+    v2 = L.Var(cov[n1:].data_ptr(), A * A * C * C, A * C * C + C * C, C + 1)
+    act = (L.Act(L.NTG_ACT_ABRELU, 0., 1., 0., 0, 0.) if kind == 'relu' else
+           L.Act(L.NTG_ACT_ERF, 1., 1., 0., 0, 0.))
+    ins = [torch.rand(shp, device='cuda', generator=g) * 2 - 1 for _ in range(4)]
+
+    def run(offset):
+        bufs = []
+        for x in ins + [None, None]:
+            raw = torch.empty(x.numel() + 1 if x is not None else ins[0].numel() + 1, device='cuda')
+            v = raw[offset:offset + ins[0].numel()].view(shp)
+            if x is not None:
+                v.copy_(x)
+            bufs.append(v)
+        gd1 = torch.zeros((n1, A, C), device='cuda')
+        gd2 = torch.zeros((n2, A, C), device='cuda')
+        L.call('ntg_act_bwd', L.stream(), L.ptr(bufs[0]), L.ptr(bufs[1]), L.ptr(bufs[2]),
+               L.ptr(bufs[3]), L.ptr(bufs[4]), L.ptr(bufs[5]), n1 * n2, n2, A, C, 0, act, v1, v2,
+               gd1.data_ptr(), gd2.data_ptr())
+        torch.cuda.synchronize()
+        return bufs[4].clone(), bufs[5].clone(), gd1, gd2
+
+    fast, slow = run(0), run(1)
+    for a, b in zip(fast, slow):
+        err = float((a - b).abs().max() / b.abs().max())
+        assert err < 2e-5, err
