@@ -199,76 +199,90 @@ __device__ __forceinline__ void act_vjp_fast(const ntg_act_t& act, const ActC& c
 // Activation VJP on full-spatial [B, A, A, C, C] kernels with C a power of two
 // in [4, 32] and A^2 C^2 a multiple of 1024: a CTA takes chunks of 1024
 // consecutive entries (one pair; 4 entries per thread, vector loads). The
-// variance cotangents of a chunk are summed by warp shuffles and shared-memory
-// atomics per (plane, row) for var1 and per (plane, column) for var2, and
-// leave with one global atomic per key instead of one per entry.
+// variances a chunk reads are staged in shared memory one chunk ahead; its
+// variance cotangents are summed by warp shuffles and shared-memory atomics per
+// (plane, row) for var1 and per (plane, column) for var2 and leave with one
+// global atomic per key instead of one per entry. Double-buffered shared arrays
+// leave one barrier per chunk.
 __global__ void __launch_bounds__(kT)
     act_bwd_fs_kernel(const float* __restrict__ q, const float* __restrict__ t,
                       const float* __restrict__ gq, const float* __restrict__ gt,
                       float* __restrict__ oq, float* __restrict__ ot, int64_t batch, int64_t n2,
                       int A, int C, ntg_act_t act, ntg_var_t var1, ntg_var_t var2, VarGrad gv1,
                       VarGrad gv2) {
-  __shared__ float s1[256], s2[256];
+  __shared__ __align__(16) float sv[2][2][256];  // [buffer][v1 | v2][key]
+  __shared__ float sg[2][2][256];                // [buffer][g v1 | g v2][key]
   const int64_t M = (int64_t)A * A * C * C;
   const int64_t chunks = batch * (M / 1024);
   const ActC ac = act_consts(act);
   const int tid = threadIdx.x, lane = tid & 31;
   const int nkeys = 1024 / C;
-  const int seg = C / 4;                                // lanes per row
-  const int pseg = C * C / 4 < 32 ? C * C / 4 : 32;     // lanes per plane within a warp
-  for (int64_t ch = blockIdx.x; ch < chunks; ch += gridDim.x) {
-    for (int k = tid; k < nkeys; k += kT) s1[k] = s2[k] = 0.f;
-    __syncthreads();
-    const int64_t base = ch * 1024;
-    const int64_t b = base / M;
-    const int64_t m0 = base - b * M;
-    const int64_t e = base + 4 * tid;
-    const int64_t m = m0 + 4 * tid;
-    const int wq = (int)(m % C);
-    const int64_t row = m / C;
-    const int w = (int)(row % C);
-    const int64_t pl = row / C;
-    const int hq = (int)(pl % A), h = (int)(pl / A);
+  const int seg = C / 4;                             // lanes per row
+  const int pseg = C * C / 4 < 32 ? C * C / 4 : 32;  // lanes per plane within a warp
+  auto stage = [&](int64_t ch, int buf) {
+    const int64_t base = ch * 1024, b = base / M, m0 = base - b * M;
     int64_t i1, i2;
     pair_of(b, n2, i1, i2);
-    const float v1 = var_at(var1, i1, h, w);
+    for (int k = tid; k < nkeys; k += kT) {
+      const int64_t rr = m0 / C + k;
+      const int64_t pp = m0 / ((int64_t)C * C) + k / C;
+      sv[buf][0][k] = var_at(var1, i1, rr / C / A, rr % C);
+      sv[buf][1][k] = var_at(var2, i2, pp % A, k % C);
+    }
+  };
+  for (int k = tid; k < 2 * 2 * 256; k += kT) (&sg[0][0][0])[k] = 0.f;
+  if (blockIdx.x < chunks) stage(blockIdx.x, 0);
+  __syncthreads();
+  const int k1 = (4 * tid) / C;
+  const int k2 = ((4 * tid) / (C * C)) * C + (4 * tid) % C;
+  int it = 0;
+  for (int64_t ch = blockIdx.x; ch < chunks; ch += gridDim.x, ++it) {
+    const int cur = it & 1;
+    if (ch + gridDim.x < chunks) stage(ch + gridDim.x, cur ^ 1);
+    const int64_t e = ch * 1024 + 4 * tid;
     const float4 Q = *reinterpret_cast<const float4*>(q + e);
     const float4 T = t ? *reinterpret_cast<const float4*>(t + e) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 GQ = gq ? *reinterpret_cast<const float4*>(gq + e) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 GT = gt ? *reinterpret_cast<const float4*>(gt + e) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float qa[4] = {Q.x, Q.y, Q.z, Q.w}, ta[4] = {T.x, T.y, T.z, T.w};
     const float ga[4] = {GQ.x, GQ.y, GQ.z, GQ.w}, gb[4] = {GT.x, GT.y, GT.z, GT.w};
+    const float v1 = sv[cur][0][k1];
+    const float4 V2 = *reinterpret_cast<const float4*>(&sv[cur][1][k2]);
+    const float v2[4] = {V2.x, V2.y, V2.z, V2.w};
     float rq[4], rt[4], r2[4], r1 = 0.f;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const float v2 = var_at(var2, i2, hq, wq + k);
       float o1;
-      act_vjp_fast(act, ac, qa[k], ta[k], v1, v2, ga[k], gb[k], rq[k], rt[k], o1, r2[k]);
+      act_vjp_fast(act, ac, qa[k], ta[k], v1, v2[k], ga[k], gb[k], rq[k], rt[k], o1, r2[k]);
       r1 += o1;
     }
     *reinterpret_cast<float4*>(oq + e) = make_float4(rq[0], rq[1], rq[2], rq[3]);
     if (ot) *reinterpret_cast<float4*>(ot + e) = make_float4(rt[0], rt[1], rt[2], rt[3]);
-    // var1 key: the row (4 tid / C) of the chunk; var2 key: (plane of the chunk, column)
     for (int o = 1; o < seg; o <<= 1) r1 += __shfl_xor_sync(0xffffffffu, r1, o);
 #pragma unroll
     for (int k = 0; k < 4; ++k)
       for (int o = seg; o < pseg; o <<= 1) r2[k] += __shfl_xor_sync(0xffffffffu, r2[k], o);
-    if ((lane & (seg - 1)) == 0) atomicAdd(&s1[(4 * tid) / C], r1);
+    if ((lane & (seg - 1)) == 0) atomicAdd(&sg[cur][0][k1], r1);
     if ((lane & (pseg - 1)) < seg) {
-      const int kb = ((4 * tid) / (C * C)) * C + wq;
 #pragma unroll
-      for (int k = 0; k < 4; ++k) atomicAdd(&s2[kb + k], r2[k]);
+      for (int k = 0; k < 4; ++k) atomicAdd(&sg[cur][1][k2 + k], r2[k]);
     }
     __syncthreads();
+    // flush this chunk's sums; the buffer is accumulated again two chunks later
+    const int64_t base = ch * 1024, b = base / M, m0 = base - b * M;
+    int64_t i1, i2;
+    pair_of(b, n2, i1, i2);
     for (int k = tid; k < nkeys; k += kT) {
-      const int64_t rr = m0 / C + k;                 // (h, h', w) of row k
-      const int64_t pp = m0 / ((int64_t)C * C) + k / C;  // (h, h') of key k
-      if (gv1.base && s1[k] != 0.f)
-        atomicAdd(gv1.base + i1 * gv1.s_n + (rr / C / A) * gv1.s_a + (rr % C) * gv1.s_c, s1[k]);
-      if (gv2.base && s2[k] != 0.f)
-        atomicAdd(gv2.base + i2 * gv2.s_n + (pp % A) * gv2.s_a + (k % C) * gv2.s_c, s2[k]);
+      const float a1 = sg[cur][0][k], a2 = sg[cur][1][k];
+      sg[cur][0][k] = 0.f;
+      sg[cur][1][k] = 0.f;
+      const int64_t rr = m0 / C + k;
+      const int64_t pp = m0 / ((int64_t)C * C) + k / C;
+      if (gv1.base && a1 != 0.f)
+        atomicAdd(gv1.base + i1 * gv1.s_n + (rr / C / A) * gv1.s_a + (rr % C) * gv1.s_c, a1);
+      if (gv2.base && a2 != 0.f)
+        atomicAdd(gv2.base + i2 * gv2.s_n + (pp % A) * gv2.s_a + (k % C) * gv2.s_c, a2);
     }
-    __syncthreads();
   }
 }
 

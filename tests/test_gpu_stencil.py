@@ -98,3 +98,39 @@ def test_stencil32_nngp_only(nt):
     assert ot is None
     wq, _ = reference(q, None, var, 2., 0.1, True)
     assert float((oq.double() - wq).abs().max() / wq.abs().max()) < RTOL
+
+
+@pytest.mark.parametrize('kind', ['relu', 'erf', 'none'])
+def test_affine_act_vectorised_matches_elementwise(nt, kind):
+    """ntg_affine_act on 16-byte aligned full-spatial buffers (chunked kernel with
+    staged variances) and on buffers offset by one float (the elementwise kernel):
+    the same operations per entry, so the results are bit-identical."""
+    from nt_gb300 import _lib as L, _ops as O
+    g = torch.Generator(device='cuda').manual_seed(13)
+    n1, n2, A, C = 2, 3, 8, 16
+    shp = (n1 * n2, A, A, C, C)
+    cov = torch.rand((n1 + n2, A, A, C, C), device='cuda', generator=g) * 0.2 + 1.
+    v1 = L.Var(cov[:n1].data_ptr(), A * A * C * C, A * C * C + C * C, C + 1)
+    v2 = L.Var(cov[n1:].data_ptr(), A * A * C * C, A * C * C + C * C, C + 1)
+    act = {'relu': L.Act(L.NTG_ACT_ABRELU, 0., 1., 0., 0, 0.),
+           'erf': L.Act(L.NTG_ACT_ERF, 1., 1., 0., 0, 0.),
+           'none': L.Act(L.NTG_ACT_NONE, 0., 0., 0., 0, 0.)}[kind]
+    q = torch.rand(shp, device='cuda', generator=g) * 2 - 1
+    t = torch.rand(shp, device='cuda', generator=g)
+    aff = O.affine(1.7, 0.1, 1.7)
+
+    def run(offset):
+        bufs = []
+        for x in (q, t, None, None):
+            raw = torch.empty(q.numel() + 1, device='cuda')
+            v = raw[offset:offset + q.numel()].view(shp)
+            if x is not None:
+                v.copy_(x)
+            bufs.append(v)
+        L.call('ntg_affine_act', L.stream(), L.ptr(bufs[0]), L.ptr(bufs[1]), L.ptr(bufs[2]),
+               L.ptr(bufs[3]), n1 * n2, n2, A, C, 0, 1, aff, act, v1, v2)
+        torch.cuda.synchronize()
+        return bufs[2].clone(), bufs[3].clone()
+
+    fast, slow = run(0), run(1)
+    assert torch.equal(fast[0], slow[0]) and torch.equal(fast[1], slow[1])
