@@ -272,6 +272,15 @@ int ntg_readout_bwd(void* stream, const float* gout, float* gin, int64_t batch, 
 int ntg_input_fs_bwd(void* stream, const float* g, const float* x_other, float* gx,
                      int64_t nself, int64_t nother, int64_t n2, int64_t a, int64_t c, int64_t k,
                      int32_t side);
+/* Both image cotangents of the full-spatial input covariance in one pass over
+ * its cotangent g (requirements.py:641-830, the _cov of an image pair): gx1 +=
+ * dG/dx1 contracted with g, gx2 += dG/dx2 (pairs g [N1, N2, A, A, C, C]); with
+ * n2 == 0 the per-sample covariances g [N1, A, A, C, C] of x1 with itself, both
+ * terms into gx1 (x2, gx2 unused). Equivalent to the two side calls of
+ * ntg_input_fs_bwd. */
+int ntg_input_fs_bwd2(void* stream, const float* g, const float* x1, const float* x2,
+                      float* gx1, float* gx2, int64_t n1, int64_t n2, int64_t a, int64_t c,
+                      int64_t k);
 /* C [m, n] (+)= alpha op(A) B, op(A) = A [m, k] or, trans_a != 0, A^T with A [k, m]
  * (flat Gram adjoint). */
 int ntg_gemm_ex(void* stream, const float* a, const float* b, float* c, int64_t m, int64_t n,

@@ -107,16 +107,13 @@ class InputFn(torch.autograd.Function):
         n1, a, c, k = y1.shape
         other = y1 if yb is None else yb
         n2 = other.shape[0]
-        L.call('ntg_input_fs_bwd', s, L.ptr(gn), L.ptr(other), L.ptr(gy1), n1, n2, n2, a, c, k, 0)
-        L.call('ntg_input_fs_bwd', s, L.ptr(gn), L.ptr(y1), L.ptr(gy1 if yb is None else gyb),
-               n2, n1, n2, a, c, k, 1)
+        L.call('ntg_input_fs_bwd2', s, L.ptr(gn), L.ptr(y1), L.ptr(other), L.ptr(gy1),
+               L.ptr(gy1 if yb is None else gyb), n1, n2, a, c, k)
         for gcv, yy, gg in ((gc1, y1, gy1), (gc2, yb, gyb)):
             if yy is None:
                 continue
-            gcv = gcv.contiguous()
-            m = yy.shape[0]
-            L.call('ntg_input_fs_bwd', s, L.ptr(gcv), L.ptr(yy), L.ptr(gg), m, m, 0, a, c, k, 0)
-            L.call('ntg_input_fs_bwd', s, L.ptr(gcv), L.ptr(yy), L.ptr(gg), m, m, 0, a, c, k, 1)
+            L.call('ntg_input_fs_bwd2', s, L.ptr(gcv.contiguous()), L.ptr(yy), None, L.ptr(gg),
+                   None, yy.shape[0], 0, a, c, k)
         return gx1, gx2
 
 

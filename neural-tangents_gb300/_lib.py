@@ -87,6 +87,7 @@ SIGNATURES = {
                       _I64, _I32, _I32, _I32, _I32], C.c_int),
     'ntg_readout_bwd': ([_P, _P, _P, _I64, _I64, _I64, _I32, _I64, _F], C.c_int),
     'ntg_input_fs_bwd': ([_P, _P, _P, _P, _I64, _I64, _I64, _I64, _I64, _I64, _I32], C.c_int),
+    'ntg_input_fs_bwd2': ([_P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, _I64], C.c_int),
     'ntg_gemm_ex': ([_P, _P, _P, _P, _I64, _I64, _I64, _I32, _F, _I32], C.c_int),
     'ntg_cov_diag_bwd': ([_P, _P, _P, _P, _I64, _I64], C.c_int),
     'ntg_diag_add': ([_P, _P, _P, _I64, _I64, _I64, _I64, _I64, _I64], C.c_int),

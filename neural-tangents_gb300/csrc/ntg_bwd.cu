@@ -609,6 +609,111 @@ __global__ void input_fs_t_kernel(const float* __restrict__ g, const float* __re
   }
 }
 
+// Both image cotangents of the full-spatial input covariance in one pass over
+// its cotangent G, for 32 x 32 planes and K <= 4 channels:
+//   gx1[i1, h, w, k]   += sum_{i2, h', w'} G[i1, i2, h, h', w, w'] x2[i2, h', w', k] / K
+//   gx2[i2, h', w', k] += sum_{i1, h, w}   G[i1, i2, h, h', w, w'] x1[i1, h, w, k] / K
+// One CTA per (i1, h) streams its planes (i2, h') once, two planes of G
+// prefetched in registers; the gx1 sums stay in registers until the end, the
+// gx2 sums of each plane are reduced by shuffles and shared-memory atomics and
+// leave with 32 K global atomics. n2 == 0: per-sample covariances
+// G[i, h, h', w, w'] of x1 with itself (x2 = x1, gx2 = gx1).
+constexpr int kIfC = 32;
+
+template <int K>
+__global__ void __launch_bounds__(256)
+    input_fs_t2_kernel(const float* __restrict__ g, const float* __restrict__ x1,
+                       const float* __restrict__ x2, float* __restrict__ gx1,
+                       float* __restrict__ gx2, int64_t n1, int64_t n2, int A, float inv_k) {
+  constexpr int C = kIfC;
+  __shared__ __align__(16) float xs[2][C * 4];  // x2[i2, h', :, :], channels padded to 4
+  __shared__ float cs[2][C * 4];                // gx2 sums of a plane [w'][k]
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int64_t i1 = blockIdx.x / A;
+  const int h = (int)(blockIdx.x % A);
+  if (i1 >= n1) return;
+  const bool self = n2 == 0;
+  const float* xo = self ? x1 : x2;
+  float* go = self ? gx1 : gx2;
+  const int64_t np = (self ? 1 : n2) * A;
+  const int w = tid >> 3, wq0 = (tid & 7) * 4;
+  float xr[K], acc[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    xr[k] = __ldg(x1 + ((i1 * A + h) * C + w) * K + k);
+    acc[k] = 0.f;
+  }
+  auto plane_ptr = [&](int64_t p) {
+    const int64_t i2 = self ? i1 : p / A;
+    const int64_t b = self ? i1 : i1 * n2 + i2;
+    return g + (((b * A + h) * A + p % A) * C + w) * C + wq0;
+  };
+  auto stage = [&](int64_t p, int buf) {
+    const int64_t i2 = self ? i1 : p / A;
+    const float* src = xo + ((i2 * A + p % A) * C) * K;
+    if (tid < C * 4) {
+      const int wq = tid >> 2, k = tid & 3;
+      xs[buf][tid] = k < K ? __ldg(src + wq * K + k) : 0.f;
+    }
+  };
+  for (int e = tid; e < 2 * C * 4; e += 256) (&cs[0][0])[e] = 0.f;
+  stage(0, 0);
+  float4 G0 = *reinterpret_cast<const float4*>(plane_ptr(0));
+  float4 G1 = np > 1 ? *reinterpret_cast<const float4*>(plane_ptr(1)) : G0;
+  __syncthreads();
+  for (int64_t p = 0; p < np; ++p) {
+    const int cur = (int)(p & 1);
+    const float4 G2 = p + 2 < np ? *reinterpret_cast<const float4*>(plane_ptr(p + 2)) : G1;
+    if (p + 1 < np) stage(p + 1, cur ^ 1);
+    const float ga[4] = {G0.x, G0.y, G0.z, G0.w};
+    float cp[4][K];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float4 X = *reinterpret_cast<const float4*>(&xs[cur][(wq0 + j) * 4]);
+      const float xv[4] = {X.x, X.y, X.z, X.w};
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        acc[k] = fmaf(ga[j], xv[k], acc[k]);
+        cp[j][k] = ga[j] * xr[k];
+      }
+    }
+    // sums over the 4 rows w of this warp, then over the 8 warps in shared memory
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        cp[j][k] += __shfl_xor_sync(0xffffffffu, cp[j][k], 8);
+        cp[j][k] += __shfl_xor_sync(0xffffffffu, cp[j][k], 16);
+      }
+    if (lane < 8) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int k = 0; k < K; ++k) atomicAdd(&cs[cur][(wq0 + j) * 4 + k], cp[j][k]);
+    }
+    __syncthreads();
+    if (tid < C * K) {
+      const int wq = tid / K, k = tid - (tid / K) * K;
+      const float v = cs[cur][wq * 4 + k];
+      cs[cur][wq * 4 + k] = 0.f;
+      const int64_t i2 = self ? i1 : p / A;
+      atomicAdd(go + ((i2 * A + p % A) * C + wq) * K + k, v * inv_k);
+    }
+    G0 = G1;
+    G1 = G2;
+  }
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], 1);
+    acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], 2);
+    acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], 4);
+  }
+  if ((lane & 7) == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) atomicAdd(gx1 + ((i1 * A + h) * C + w) * K + k, acc[k] * inv_k);
+  }
+}
+
 // C[m, n] (+)= alpha * op(A) B with op(A) = A [m, k] or A^T (A stored [k, m]).
 __global__ void __launch_bounds__(256) gemm_ex_kernel(const float* __restrict__ A,
                                                       const float* __restrict__ B,
@@ -804,6 +909,41 @@ extern "C" int ntg_input_fs_bwd(void* stream, const float* g, const float* x_oth
       g, x_other, gx, nself, nother, n2, a, c, k, side, 1.f / (float)k);
   note_launch();
   return check_launch("ntg_input_fs_bwd");
+}
+
+extern "C" int ntg_input_fs_bwd2(void* stream, const float* g, const float* x1,
+                                 const float* x2, float* gx1, float* gx2, int64_t n1, int64_t n2,
+                                 int64_t a, int64_t c, int64_t k) {
+  NTG_REQUIRE(g && x1 && gx1 && n1 > 0 && n2 >= 0 && a > 0 && c > 0 && k > 0,
+              "ntg_input_fs_bwd2: bad arguments");
+  NTG_REQUIRE(n2 == 0 || (x2 && gx2), "ntg_input_fs_bwd2: pairs need x2 and gx2");
+  cudaStream_t s = as_stream(stream);
+  const bool fast = c == kIfC && k <= 4 && a <= (1 << 16) && n1 * a < (1ll << 31) &&
+                    (reinterpret_cast<uintptr_t>(g) & 15) == 0;
+  if (fast) {
+    const unsigned grid = (unsigned)(n1 * a);
+    const float inv_k = 1.f / (float)k;
+    switch (k) {
+      case 1: input_fs_t2_kernel<1><<<grid, 256, 0, s>>>(g, x1, x2, gx1, gx2, n1, n2, (int)a, inv_k); break;
+      case 2: input_fs_t2_kernel<2><<<grid, 256, 0, s>>>(g, x1, x2, gx1, gx2, n1, n2, (int)a, inv_k); break;
+      case 3: input_fs_t2_kernel<3><<<grid, 256, 0, s>>>(g, x1, x2, gx1, gx2, n1, n2, (int)a, inv_k); break;
+      default: input_fs_t2_kernel<4><<<grid, 256, 0, s>>>(g, x1, x2, gx1, gx2, n1, n2, (int)a, inv_k); break;
+    }
+    note_launch();
+    return check_launch("ntg_input_fs_bwd2");
+  }
+  const size_t sm = sizeof(float) * c * k;
+  NTG_REQUIRE(sm <= 48 * 1024, "ntg_input_fs_bwd2: C * K too large");
+  const float inv_k = 1.f / (float)k;
+  if (n2 == 0) {
+    input_fs_t_kernel<<<(unsigned)(n1 * a), 128, sm, s>>>(g, x1, gx1, n1, n1, 0, a, c, k, 0, inv_k);
+    input_fs_t_kernel<<<(unsigned)(n1 * a), 128, sm, s>>>(g, x1, gx1, n1, n1, 0, a, c, k, 1, inv_k);
+  } else {
+    input_fs_t_kernel<<<(unsigned)(n1 * a), 128, sm, s>>>(g, x2, gx1, n1, n2, n2, a, c, k, 0, inv_k);
+    input_fs_t_kernel<<<(unsigned)(n2 * a), 128, sm, s>>>(g, x1, gx2, n2, n1, n2, a, c, k, 1, inv_k);
+  }
+  note_launch(2);
+  return check_launch("ntg_input_fs_bwd2");
 }
 
 extern "C" int ntg_gemm_ex(void* stream, const float* a, const float* b, float* c, int64_t m,

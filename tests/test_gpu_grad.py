@@ -229,3 +229,42 @@ def test_vectorised_activation_vjp_matches_elementwise_kernel(nt, kind):
     for a, b in zip(fast, slow):
         err = float((a - b).abs().max() / b.abs().max())
         assert err < 2e-5, err
+
+
+@pytest.mark.parametrize('pairs', [True, False])
+def test_input_covariance_adjoint_single_pass(nt, pairs):
+    """ntg_input_fs_bwd2 on 32 x 32 planes (one pass over G for both image
+    cotangents) against the same call with G offset by one float (the per-side
+    kernels), and against a float64 torch contraction."""
+    from nt_gb300 import _lib as L
+    g = torch.Generator(device='cuda').manual_seed(17)
+    n1, n2, A, C, K = 3, 2, 32, 32, 3
+    x1 = torch.randn((n1, A, C, K), device='cuda', generator=g)
+    x2 = torch.randn((n2, A, C, K), device='cuda', generator=g)
+    shp = (n1, n2, A, A, C, C) if pairs else (n1, A, A, C, C)
+    G = torch.randn(shp, device='cuda', generator=g)
+
+    def run(offset):
+        raw = torch.empty(G.numel() + 1, device='cuda')
+        gv = raw[offset:offset + G.numel()].view(shp)
+        gv.copy_(G)
+        gx1 = torch.zeros_like(x1)
+        gx2 = torch.zeros_like(x2)
+        L.call('ntg_input_fs_bwd2', L.stream(), L.ptr(gv), L.ptr(x1),
+               L.ptr(x2) if pairs else None, L.ptr(gx1), L.ptr(gx2) if pairs else None, n1,
+               n2 if pairs else 0, A, C, K)
+        torch.cuda.synchronize()
+        return gx1, gx2
+
+    fast, slow = run(0), run(1)
+    Gd, a, b = G.double(), x1.double(), x2.double()
+    if pairs:
+        want1 = torch.einsum('ijhHwW,jHWk->ihwk', Gd, b) / K
+        want2 = torch.einsum('ijhHwW,ihwk->jHWk', Gd, a) / K
+    else:
+        want1 = (torch.einsum('ihHwW,iHWk->ihwk', Gd, a) + torch.einsum('ihHwW,ihwk->iHWk', Gd, a)) / K
+        want2 = torch.zeros_like(b)
+    for got, ref, want in ((fast[0], slow[0], want1), (fast[1], slow[1], want2)):
+        scale = float(want.abs().max()) if float(want.abs().max()) > 0 else 1.
+        assert float((got.double() - want).abs().max()) / scale < 1e-5
+        assert float((got - ref).abs().max()) / scale < 1e-5
