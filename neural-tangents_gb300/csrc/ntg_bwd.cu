@@ -212,34 +212,45 @@ __global__ void __launch_bounds__(kT)
                       VarGrad gv2) {
   __shared__ __align__(16) float sv[2][2][256];  // [buffer][v1 | v2][key]
   __shared__ float sg[2][2][256];                // [buffer][g v1 | g v2][key]
-  const int64_t M = (int64_t)A * A * C * C;
-  const int64_t chunks = batch * (M / 1024);
+  const int64_t M = (int64_t)A * A * C * C;  // < 2^31 (checked by the host)
+  const int P = (int)(M / 1024);              // chunks per pair
+  const int64_t chunks = batch * P;
   const ActC ac = act_consts(act);
   const int tid = threadIdx.x, lane = tid & 31;
-  const int nkeys = 1024 / C;
+  const int lc = __ffs(C) - 1;                       // log2 C
+  const int nkeys = 1024 >> lc;
   const int seg = C / 4;                             // lanes per row
   const int pseg = C * C / 4 < 32 ? C * C / 4 : 32;  // lanes per plane within a warp
-  auto stage = [&](int64_t ch, int buf) {
-    const int64_t base = ch * 1024, b = base / M, m0 = base - b * M;
+  // chunk ch = b * P + j: pair b, entries [1024 j, 1024 j + 1024) of that pair
+  auto stage = [&](int64_t b, int j, int buf) {
     int64_t i1, i2;
     pair_of(b, n2, i1, i2);
+    const int r0 = (j * 1024) >> lc, p0 = (j * 1024) >> (2 * lc);
     for (int k = tid; k < nkeys; k += kT) {
-      const int64_t rr = m0 / C + k;
-      const int64_t pp = m0 / ((int64_t)C * C) + k / C;
-      sv[buf][0][k] = var_at(var1, i1, rr / C / A, rr % C);
-      sv[buf][1][k] = var_at(var2, i2, pp % A, k % C);
+      const int rr = r0 + k, pp = p0 + (k >> lc);
+      sv[buf][0][k] = var_at(var1, i1, (rr >> lc) / A, rr & (C - 1));
+      sv[buf][1][k] = var_at(var2, i2, pp % A, k & (C - 1));
     }
   };
   for (int k = tid; k < 2 * 2 * 256; k += kT) (&sg[0][0][0])[k] = 0.f;
-  if (blockIdx.x < chunks) stage(blockIdx.x, 0);
+  int64_t b = blockIdx.x / P;
+  int j = (int)(blockIdx.x - b * P);
+  if (blockIdx.x < chunks) stage(b, j, 0);
   __syncthreads();
-  const int k1 = (4 * tid) / C;
-  const int k2 = ((4 * tid) / (C * C)) * C + (4 * tid) % C;
+  const int k1 = (4 * tid) >> lc;
+  const int k2 = (((4 * tid) >> (2 * lc)) << lc) + ((4 * tid) & (C - 1));
+  const int step_b = (int)(gridDim.x / P), step_j = (int)(gridDim.x - (int64_t)step_b * P);
   int it = 0;
   for (int64_t ch = blockIdx.x; ch < chunks; ch += gridDim.x, ++it) {
     const int cur = it & 1;
-    if (ch + gridDim.x < chunks) stage(ch + gridDim.x, cur ^ 1);
-    const int64_t e = ch * 1024 + 4 * tid;
+    int64_t bn = b + step_b;
+    int jn = j + step_j;
+    if (jn >= P) {
+      jn -= P;
+      ++bn;
+    }
+    if (ch + gridDim.x < chunks) stage(bn, jn, cur ^ 1);
+    const int64_t e = b * M + (int64_t)j * 1024 + 4 * tid;
     const float4 Q = *reinterpret_cast<const float4*>(q + e);
     const float4 T = t ? *reinterpret_cast<const float4*>(t + e) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 GQ = gq ? *reinterpret_cast<const float4*>(gq + e) : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -269,20 +280,23 @@ __global__ void __launch_bounds__(kT)
     }
     __syncthreads();
     // flush this chunk's sums; the buffer is accumulated again two chunks later
-    const int64_t base = ch * 1024, b = base / M, m0 = base - b * M;
     int64_t i1, i2;
     pair_of(b, n2, i1, i2);
+    const int r0 = (j * 1024) >> lc, p0 = (j * 1024) >> (2 * lc);
     for (int k = tid; k < nkeys; k += kT) {
       const float a1 = sg[cur][0][k], a2 = sg[cur][1][k];
       sg[cur][0][k] = 0.f;
       sg[cur][1][k] = 0.f;
-      const int64_t rr = m0 / C + k;
-      const int64_t pp = m0 / ((int64_t)C * C) + k / C;
+      const int rr = r0 + k, pp = p0 + (k >> lc);
       if (gv1.base && a1 != 0.f)
-        atomicAdd(gv1.base + i1 * gv1.s_n + (rr / C / A) * gv1.s_a + (rr % C) * gv1.s_c, a1);
+        atomicAdd(gv1.base + i1 * gv1.s_n + (int64_t)((rr >> lc) / A) * gv1.s_a +
+                      (int64_t)(rr & (C - 1)) * gv1.s_c, a1);
       if (gv2.base && a2 != 0.f)
-        atomicAdd(gv2.base + i2 * gv2.s_n + (pp % A) * gv2.s_a + (k % C) * gv2.s_c, a2);
+        atomicAdd(gv2.base + i2 * gv2.s_n + (int64_t)(pp % A) * gv2.s_a +
+                      (int64_t)(k & (C - 1)) * gv2.s_c, a2);
     }
+    b = bn;
+    j = jn;
   }
 }
 
@@ -614,11 +628,18 @@ __global__ void input_fs_t_kernel(const float* __restrict__ g, const float* __re
 //   gx1[i1, h, w, k]   += sum_{i2, h', w'} G[i1, i2, h, h', w, w'] x2[i2, h', w', k] / K
 //   gx2[i2, h', w', k] += sum_{i1, h, w}   G[i1, i2, h, h', w, w'] x1[i1, h, w, k] / K
 // One CTA per (i1, h) streams its planes (i2, h') once, two planes of G
-// prefetched in registers; the gx1 sums stay in registers until the end, the
-// gx2 sums of each plane are reduced by shuffles and shared-memory atomics and
-// leave with 32 K global atomics. n2 == 0: per-sample covariances
+// prefetched in registers; the gx1 sums stay in registers until the end. The
+// gx2 sums of a plane are reduced over a warp's rows by shuffles, written per
+// warp to shared memory and summed over the warps by 32 K threads, which add
+// them to gx2 with one global atomic each. Plane coordinates advance
+// incrementally (no divisions in the loop). n2 == 0: per-sample covariances
 // G[i, h, h', w, w'] of x1 with itself (x2 = x1, gx2 = gx1).
 constexpr int kIfC = 32;
+
+struct PlaneIt {  // (i2, h') of a plane in the order the CTA streams them
+  int64_t i2;
+  int hq;
+};
 
 template <int K>
 __global__ void __launch_bounds__(256)
@@ -626,9 +647,9 @@ __global__ void __launch_bounds__(256)
                        const float* __restrict__ x2, float* __restrict__ gx1,
                        float* __restrict__ gx2, int64_t n1, int64_t n2, int A, float inv_k) {
   constexpr int C = kIfC;
-  __shared__ __align__(16) float xs[2][C * 4];  // x2[i2, h', :, :], channels padded to 4
-  __shared__ float cs[2][C * 4];                // gx2 sums of a plane [w'][k]
-  const int tid = threadIdx.x, lane = tid & 31;
+  __shared__ __align__(16) float xs[2][C * 4];      // x2[i2, h', :, :], channels padded to 4
+  __shared__ __align__(16) float cw[2][8][C * 4];   // per-warp gx2 sums of a plane [w'][k]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t i1 = blockIdx.x / A;
   const int h = (int)(blockIdx.x % A);
   if (i1 >= n1) return;
@@ -643,41 +664,53 @@ __global__ void __launch_bounds__(256)
     xr[k] = __ldg(x1 + ((i1 * A + h) * C + w) * K + k);
     acc[k] = 0.f;
   }
-  auto plane_ptr = [&](int64_t p) {
-    const int64_t i2 = self ? i1 : p / A;
-    const int64_t b = self ? i1 : i1 * n2 + i2;
-    return g + (((b * A + h) * A + p % A) * C + w) * C + wq0;
+  auto advance = [&](PlaneIt& it) {
+    if (++it.hq == A) {
+      it.hq = 0;
+      ++it.i2;
+    }
   };
-  auto stage = [&](int64_t p, int buf) {
-    const int64_t i2 = self ? i1 : p / A;
-    const float* src = xo + ((i2 * A + p % A) * C) * K;
+  // G + offset of this thread's 4 entries in plane (i2, h')
+  auto gptr = [&](const PlaneIt& it) {
+    const int64_t b = self ? i1 : i1 * n2 + it.i2;
+    return g + ((b * A + h) * A + it.hq) * (int64_t)(C * C) + w * C + wq0;
+  };
+  auto stage = [&](const PlaneIt& it, int buf) {
     if (tid < C * 4) {
+      const float* src = xo + ((it.i2 * A + it.hq) * C) * K;
       const int wq = tid >> 2, k = tid & 3;
       xs[buf][tid] = k < K ? __ldg(src + wq * K + k) : 0.f;
     }
   };
-  for (int e = tid; e < 2 * C * 4; e += 256) (&cs[0][0])[e] = 0.f;
-  stage(0, 0);
-  float4 G0 = *reinterpret_cast<const float4*>(plane_ptr(0));
-  float4 G1 = np > 1 ? *reinterpret_cast<const float4*>(plane_ptr(1)) : G0;
+  PlaneIt p0{self ? i1 : 0, 0}, p1 = p0, p2;
+  advance(p1);
+  p2 = p1;
+  advance(p2);
+  stage(p0, 0);
+  float4 G0 = *reinterpret_cast<const float4*>(gptr(p0));
+  float4 G1 = np > 1 ? *reinterpret_cast<const float4*>(gptr(p1)) : G0;
   __syncthreads();
   for (int64_t p = 0; p < np; ++p) {
     const int cur = (int)(p & 1);
-    const float4 G2 = p + 2 < np ? *reinterpret_cast<const float4*>(plane_ptr(p + 2)) : G1;
-    if (p + 1 < np) stage(p + 1, cur ^ 1);
+    const float4 G2 = p + 2 < np ? *reinterpret_cast<const float4*>(gptr(p2)) : G1;
+    if (p + 1 < np) stage(p1, cur ^ 1);
     const float ga[4] = {G0.x, G0.y, G0.z, G0.w};
-    float cp[4][K];
+    float cp[4][4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const float4 X = *reinterpret_cast<const float4*>(&xs[cur][(wq0 + j) * 4]);
       const float xv[4] = {X.x, X.y, X.z, X.w};
 #pragma unroll
-      for (int k = 0; k < K; ++k) {
-        acc[k] = fmaf(ga[j], xv[k], acc[k]);
-        cp[j][k] = ga[j] * xr[k];
+      for (int k = 0; k < 4; ++k) {
+        if (k < K) {
+          acc[k] = fmaf(ga[j], xv[k], acc[k]);
+          cp[j][k] = ga[j] * xr[k];
+        } else {
+          cp[j][k] = 0.f;
+        }
       }
     }
-    // sums over the 4 rows w of this warp, then over the 8 warps in shared memory
+    // sums over the 4 rows w of this warp (lanes 8 apart), then one row per warp
 #pragma unroll
     for (int j = 0; j < 4; ++j)
 #pragma unroll
@@ -688,19 +721,22 @@ __global__ void __launch_bounds__(256)
     if (lane < 8) {
 #pragma unroll
       for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int k = 0; k < K; ++k) atomicAdd(&cs[cur][(wq0 + j) * 4 + k], cp[j][k]);
+        *reinterpret_cast<float4*>(&cw[cur][warp][(wq0 + j) * 4]) =
+            make_float4(cp[j][0], cp[j][1], cp[j][2], cp[j][3]);
     }
     __syncthreads();
     if (tid < C * K) {
       const int wq = tid / K, k = tid - (tid / K) * K;
-      const float v = cs[cur][wq * 4 + k];
-      cs[cur][wq * 4 + k] = 0.f;
-      const int64_t i2 = self ? i1 : p / A;
-      atomicAdd(go + ((i2 * A + p % A) * C + wq) * K + k, v * inv_k);
+      float v = 0.f;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v += cw[cur][u][wq * 4 + k];
+      atomicAdd(go + ((p0.i2 * A + p0.hq) * C + wq) * K + k, v * inv_k);
     }
     G0 = G1;
     G1 = G2;
+    p0 = p1;
+    p1 = p2;
+    advance(p2);
   }
 #pragma unroll
   for (int k = 0; k < K; ++k) {
@@ -815,7 +851,7 @@ extern "C" int ntg_act_bwd(void* stream, const float* q, const float* t, const f
                          reinterpret_cast<uintptr_t>(gq) | reinterpret_cast<uintptr_t>(gt) |
                          reinterpret_cast<uintptr_t>(oq) | reinterpret_cast<uintptr_t>(ot)) &
                         15) == 0;
-  if (!diag_spatial && pow2 && m % 1024 == 0 && aligned && a <= (1 << 20)) {
+  if (!diag_spatial && pow2 && m % 1024 == 0 && aligned && m < (1ll << 31)) {
     const int64_t chunks = batch * (m / 1024);
     const int grid = (int)(chunks < 152 * 8 ? chunks : 152 * 8);
     act_bwd_fs_kernel<<<grid, kT, 0, as_stream(stream)>>>(q, t, gq, gt, oq, ot, batch, n2,

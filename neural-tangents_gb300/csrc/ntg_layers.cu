@@ -872,37 +872,49 @@ __global__ void __launch_bounds__(kThreads)
                          int64_t n2, int A, int C, int has_affine, ntg_affine_t aff,
                          ntg_act_t act, ntg_var_t var1, ntg_var_t var2) {
   __shared__ __align__(16) float sv[2][4][256];  // [buffer][v1 | sqrt v1 | v2 | sqrt v2][key]
-  const int64_t M = (int64_t)A * A * C * C;
-  const int64_t chunks = batch * (M / 1024);
+  const int64_t M = (int64_t)A * A * C * C;  // < 2^31 (checked by the host)
+  const int P = (int)(M / 1024);              // chunks per pair
+  const int64_t chunks = batch * P;
   const ActC ac = act_consts(act);
   const bool has_act = act.kind != NTG_ACT_NONE;
   const int tid = threadIdx.x;
-  const int nkeys = 1024 / C;
-  // keys of a chunk: rows (plane, w) for var1 at (h, w); (plane, w') for var2 at (h', w')
-  auto stage = [&](int64_t ch, int buf) {
-    const int64_t base = ch * 1024, b = base / M, m0 = base - b * M;
+  const int lc = __ffs(C) - 1;  // log2 C
+  const int nkeys = 1024 >> lc;
+  // keys of chunk (b, j): rows (plane, w) for var1 at (h, w); (plane, w') for var2 at (h', w')
+  auto stage = [&](int64_t b, int j, int buf) {
     int64_t i1, i2;
     pair_of(b, n2, i1, i2);
+    const int r0 = (j * 1024) >> lc, p0 = (j * 1024) >> (2 * lc);
     for (int k = tid; k < nkeys; k += kThreads) {
-      const int64_t rr = m0 / C + k;
-      const int64_t pp = m0 / ((int64_t)C * C) + k / C;
-      const float v1 = var_at(var1, i1, rr / C / A, rr % C);
-      const float v2 = var_at(var2, i2, pp % A, k % C);
+      const int rr = r0 + k, pp = p0 + (k >> lc);
+      const float v1 = var_at(var1, i1, (rr >> lc) / A, rr & (C - 1));
+      const float v2 = var_at(var2, i2, pp % A, k & (C - 1));
       sv[buf][0][k] = v1;
       sv[buf][1][k] = sqrt_var(v1);
       sv[buf][2][k] = v2;
       sv[buf][3][k] = sqrt_var(v2);
     }
   };
-  if (has_act && blockIdx.x < chunks) stage(blockIdx.x, 0);
+  int64_t b = blockIdx.x / P;
+  int j = (int)(blockIdx.x - b * P);
+  if (has_act && blockIdx.x < chunks) stage(b, j, 0);
   __syncthreads();
-  const int k1 = (4 * tid) / C;
-  const int k2 = ((4 * tid) / (C * C)) * C + (4 * tid) % C;
+  const int k1 = (4 * tid) >> lc;
+  const int k2 = (((4 * tid) >> (2 * lc)) << lc) + ((4 * tid) & (C - 1));
+  const int step_b = (int)(gridDim.x / P), step_j = (int)(gridDim.x - (int64_t)step_b * P);
   int it = 0;
   for (int64_t ch = blockIdx.x; ch < chunks; ch += gridDim.x, ++it) {
     const int cur = it & 1;
-    if (has_act && ch + gridDim.x < chunks) stage(ch + gridDim.x, cur ^ 1);  // read next round
-    const int64_t e = ch * 1024 + 4 * tid;
+    int64_t bn = b + step_b;
+    int jn = j + step_j;
+    if (jn >= P) {
+      jn -= P;
+      ++bn;
+    }
+    if (has_act && ch + gridDim.x < chunks) stage(bn, jn, cur ^ 1);  // read next round
+    const int64_t e = b * M + (int64_t)j * 1024 + 4 * tid;
+    b = bn;
+    j = jn;
     const float4 Q = *reinterpret_cast<const float4*>(in_q + e);
     const float4 T = in_t ? *reinterpret_cast<const float4*>(in_t + e)
                           : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1271,7 +1283,7 @@ extern "C" int ntg_affine_act(void* stream, const float* in_q, const float* in_t
   const bool aligned = ((reinterpret_cast<uintptr_t>(in_q) | reinterpret_cast<uintptr_t>(in_t) |
                          reinterpret_cast<uintptr_t>(out_q) | reinterpret_cast<uintptr_t>(out_t)) &
                         15) == 0;
-  if (!diag_spatial && pow2 && m % 1024 == 0 && aligned && a <= (1 << 20)) {
+  if (!diag_spatial && pow2 && m % 1024 == 0 && aligned && m < (1ll << 31)) {
     const int64_t chunks = batch * (m / 1024);
     const int grid = (int)(chunks < 152 * 8 ? chunks : 152 * 8);
     affine_act_fs_kernel<<<grid, kThreads, 0, as_stream(stream)>>>(
