@@ -308,23 +308,26 @@ __global__ void __launch_bounds__(kT)
     pool_t_block_kernel(const float* __restrict__ gout, float* __restrict__ gin, int64_t batch,
                         int A, int C, int wa, int wc, float weight) {
   const int Ao = A / wa, Co = C / wc;
-  const int64_t per_b = (int64_t)A * A * C * C;
-  const int64_t n4 = batch * per_b / 4;
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n4;
-       v += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t idx = 4 * v;
-    const int64_t b = idx / per_b;
-    int64_t r = idx - b * per_b;
-    const int cp = (int)(r % C); r /= C;
-    const int c = (int)(r % C); r /= C;
-    const int ap = (int)(r % A);
-    const int a = (int)(r / A);
-    const float* g = gout + b * (int64_t)Ao * Ao * Co * Co +
-                     (((int64_t)(a / wa) * Ao + ap / wa) * Co + c / wc) * Co;
-    float o[4];
+  const int per_b = A * A * C * C;  // < 2^31 (checked by the host)
+  const int n4 = per_b / 4;
+  for (int64_t b = blockIdx.y; b < batch; b += gridDim.y) {
+    const float* gb = gout + b * (int64_t)Ao * Ao * Co * Co;
+    float* ib = gin + b * (int64_t)per_b;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n4; v += gridDim.x * blockDim.x) {
+      const int idx = 4 * v;
+      int r = idx;
+      const int cp = r % C;
+      r /= C;
+      const int c = r % C;
+      r /= C;
+      const int ap = r % A;
+      const int a = r / A;
+      const float* g = gb + (((a / wa) * Ao + ap / wa) * Co + c / wc) * Co;
+      float o[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) o[k] = __ldg(g + (cp + k) / wc) * weight;
-    *reinterpret_cast<float4*>(gin + idx) = make_float4(o[0], o[1], o[2], o[3]);
+      for (int k = 0; k < 4; ++k) o[k] = __ldg(g + (cp + k) / wc) * weight;
+      *reinterpret_cast<float4*>(ib + idx) = make_float4(o[0], o[1], o[2], o[3]);
+    }
   }
 }
 
@@ -910,10 +913,15 @@ extern "C" int ntg_pool_bwd(void* stream, const float* gout, float* gin, int64_t
   const int64_t total = diag_spatial ? batch * a * c : batch * a * a * c * c;
   const bool blocks = !diag_spatial && pa == 0 && pc == 0 && sa == wa && sc == wc &&
                       a % wa == 0 && c % wc == 0 && ao == a / wa && co == c / wc && c % 4 == 0 &&
+                      a * a * c * c < (1ll << 31) &&
                       ((reinterpret_cast<uintptr_t>(gin) & 15) == 0);
   if (blocks) {
     const float weight = average ? 1.f / (float)(wa * wa * wc * wc) : 1.f;
-    pool_t_block_kernel<<<grid_for(total / 4), kT, 0, as_stream(stream)>>>(
+    const int64_t n4 = a * a * c * c / 4;
+    int64_t gx = ceil_div(n4, kT);
+    const int64_t gy = batch < 65535 ? batch : 65535;
+    while (gx * gy > 152 * 64 && gx > 1) gx = ceil_div(gx, 2);
+    pool_t_block_kernel<<<dim3((unsigned)gx, (unsigned)gy), kT, 0, as_stream(stream)>>>(
         gout, gin, batch, (int)a, (int)c, wa, wc, weight);
     note_launch();
     return check_launch("ntg_pool_bwd");

@@ -154,6 +154,56 @@ __global__ void input_fs_kernel(const float* __restrict__ x1, const float* __res
   }
 }
 
+// The same for C a power of two in [4, 32] and K <= 4 channels: the row x1[i1, a]
+// and the image x2[i2] are staged in shared memory (channels padded to 4), each
+// thread writes 4 consecutive entries with one vector store; the same
+// multiply-add order per entry as input_fs_kernel.
+__global__ void __launch_bounds__(256)
+    input_fs_vec_kernel(const float* __restrict__ x1, const float* __restrict__ x2,
+                        int64_t batch, int64_t n2, int A, int C, int K, float inv_k,
+                        float* __restrict__ out) {
+  extern __shared__ __align__(16) float xsm[];  // x1 row [C][4] | x2 image [A * C][4]
+  float* r1 = xsm;
+  float* im2 = xsm + 4 * C;
+  const int64_t b = blockIdx.x / A;
+  const int a = (int)(blockIdx.x - b * A);
+  if (b >= batch) return;
+  int64_t i1, i2;
+  pair_of(b, n2, i1, i2);
+  const float* src1 = x1 + ((i1 * A + a) * C) * K;
+  const float* src2 = x2 + i2 * (int64_t)A * C * K;
+  for (int e = threadIdx.x; e < 4 * C; e += blockDim.x) {
+    const int c = e >> 2, k = e & 3;
+    r1[e] = k < K ? __ldg(src1 + c * K + k) : 0.f;
+  }
+  for (int e = threadIdx.x; e < 4 * A * C; e += blockDim.x) {
+    const int pos = e >> 2, k = e & 3;
+    im2[e] = k < K ? __ldg(src2 + (int64_t)pos * K + k) : 0.f;
+  }
+  __syncthreads();
+  const int lc = __ffs(C) - 1;
+  float* o = out + (b * A + a) * (int64_t)A * C * C;
+  const int n4 = (A * C * C) >> 2;
+  for (int v = threadIdx.x; v < n4; v += blockDim.x) {
+    const int idx = 4 * v;
+    const int cp0 = idx & (C - 1), c = (idx >> lc) & (C - 1), ap = idx >> (2 * lc);
+    const float4 u = *reinterpret_cast<const float4*>(r1 + 4 * c);
+    const float ua[4] = {u.x, u.y, u.z, u.w};
+    float r[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float4 x = *reinterpret_cast<const float4*>(im2 + 4 * (ap * C + cp0 + j));
+      const float xa[4] = {x.x, x.y, x.z, x.w};
+      float sacc = 0.f;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (k < K) sacc = fmaf(ua[k], xa[k], sacc);
+      r[j] = sacc * inv_k;
+    }
+    *reinterpret_cast<float4*>(o + idx) = make_float4(r[0], r[1], r[2], r[3]);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // General full-spatial conv rule: one thread per output entry.
 // ---------------------------------------------------------------------------
@@ -1138,8 +1188,15 @@ extern "C" int ntg_input_fs(void* stream, const float* x1, const float* x2, int6
   const float* xb = pairs ? x2 : x1;
   int64_t blocks = batch * a;
   NTG_REQUIRE(blocks < (1ll << 31), "ntg_input_fs: grid too large");
-  input_fs_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(
-      x1, xb, batch, pairs ? n2 : 0, a, c, k, 1.f / (float)k, out);
+  const size_t vec_sm = sizeof(float) * 4 * (c + a * c);
+  if (c >= 4 && c <= 32 && (c & (c - 1)) == 0 && k <= 4 && vec_sm <= 48 * 1024 &&
+      (reinterpret_cast<uintptr_t>(out) & 15) == 0) {
+    input_fs_vec_kernel<<<(unsigned)blocks, 256, vec_sm, as_stream(stream)>>>(
+        x1, xb, batch, pairs ? n2 : 0, (int)a, (int)c, (int)k, 1.f / (float)k, out);
+  } else {
+    input_fs_kernel<<<(unsigned)blocks, 256, 0, as_stream(stream)>>>(
+        x1, xb, batch, pairs ? n2 : 0, a, c, k, 1.f / (float)k, out);
+  }
   note_launch();
   return check_launch("ntg_input_fs");
 }

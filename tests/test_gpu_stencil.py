@@ -134,3 +134,51 @@ def test_affine_act_vectorised_matches_elementwise(nt, kind):
 
     fast, slow = run(0), run(1)
     assert torch.equal(fast[0], slow[0]) and torch.equal(fast[1], slow[1])
+
+
+@pytest.mark.parametrize('pairs', [True, False])
+def test_input_covariance_vectorised_matches_elementwise(nt, pairs):
+    """ntg_input_fs with a 16-byte aligned output (staged, vectorised kernel) and
+    with the output offset by one float (one thread per entry): bit-identical."""
+    from nt_gb300 import _lib as L
+    g = torch.Generator(device='cuda').manual_seed(19)
+    n1, n2, A, C, K = 3, 2, 32, 32, 3
+    x1 = torch.randn((n1, A, C, K), device='cuda', generator=g)
+    x2 = torch.randn((n2, A, C, K), device='cuda', generator=g)
+    shp = (n1, n2, A, A, C, C) if pairs else (n1, A, A, C, C)
+    numel = int(torch.tensor(shp).prod())
+
+    def run(offset):
+        raw = torch.empty(numel + 1, device='cuda')
+        out = raw[offset:offset + numel].view(shp)
+        L.call('ntg_input_fs', L.stream(), L.ptr(x1), L.ptr(x2) if pairs else None, n1,
+               n2 if pairs else 0, A, C, K, int(pairs), L.ptr(out))
+        torch.cuda.synchronize()
+        return out.clone()
+
+    fast, slow = run(0), run(1)
+    assert torch.equal(fast, slow)
+    want = (torch.einsum('ihwk,jHWk->ijhHwW', x1.double(), x2.double()) if pairs else
+            torch.einsum('ihwk,iHWk->ihHwW', x1.double(), x1.double())) / K
+    assert float((fast.double() - want).abs().max() / want.abs().max()) < 1e-6
+
+
+def test_pool_transpose_block_matches_general(nt):
+    """ntg_pool_bwd for AvgPool(2, 2) on full-spatial kernels: the block kernel
+    (aligned output) against the general transpose (output offset by one float)."""
+    from nt_gb300 import _lib as L
+    g = torch.Generator(device='cuda').manual_seed(23)
+    B, A, C = 5, 16, 16
+    gout = torch.randn((B, A // 2, A // 2, C // 2, C // 2), device='cuda', generator=g)
+    numel = B * A * A * C * C
+
+    def run(offset):
+        raw = torch.empty(numel + 1, device='cuda')
+        gin = raw[offset:offset + numel].view(B, A, A, C, C)
+        L.call('ntg_pool_bwd', L.stream(), L.ptr(gout), L.ptr(gin), B, A, C, 2, 2, 2, 2, 0, 0,
+               A // 2, C // 2, 0, 0, 1, 0)
+        torch.cuda.synchronize()
+        return gin.clone()
+
+    fast, slow = run(0), run(1)
+    assert torch.equal(fast, slow)
