@@ -204,7 +204,10 @@ def run_gpu(args):
     # Materialised per-layer stencil (conv + Relu epilogue) on a 16 x 16 tile at S = 32.
     st_gbs = stencil_roofline(torch, O, dev)
     gram_tc = gram_roofline(torch, O, dev)
-    fwd_bwd = fwd_bwd_timing(torch, nt, kf, xd)
+    fb32, g32 = fwd_bwd_timing(torch, nt, kf, xd, precision='fp32')
+    fbmx, gmx = fwd_bwd_timing(torch, nt, kf, xd, precision='mixed')
+    fbmx['grad_rel_diff_vs_fp32'] = float((gmx - g32).abs().max() / g32.abs().max())
+    fwd_bwd = {'ms': fbmx['ms'], 'fp32': fb32, 'mixed': fbmx}
 
     # Mixed precision (compensated) variant of the same step and its error vs plain.
     torch.cuda.synchronize()
@@ -310,27 +313,40 @@ def stencil_roofline(torch, O, dev, pairs=256, reps=4):
             'achieved': round(gbs, 1), 'unit': 'GB/s'}
 
 
-def fwd_bwd_timing(torch, nt, kf, xd, n_t=16, n_s=8, bs=8):
-    """Myrtle-5 NTK forward + backward with respect to a support set: the gradient of
-    sum(w * K(x_t, x_s)) by x_s through nt.batch's checkpointed tiles (the
-    recompute-per-tile adjoint path)."""
+def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=16, precision='fp32', reps=2):
+    """Kernel-ridge loss of the Myrtle-5 NTK, ||y_t - K_ts (K_ss + 1e-6 tr(K_ss)/n I)^-1 y_s||^2,
+    and its gradient with respect to the support set x_s (forward through nt.batch's fused
+    grid, backward through its checkpointed tiles and the hand-written adjoints; the solve
+    and its adjoint on the library's Cholesky kernels). A bounded sample of the
+    [200]-support / [2000]-target configuration: x_s [n_s], x_t [n_t] from the synthetic
+    inputs, one-hot labels over 10 classes (seed 2)."""
+    from nt_gb300 import predict
+    g = torch.Generator(device='cpu').manual_seed(2)
+    ys = torch.nn.functional.one_hot(torch.randint(0, 10, (n_s,), generator=g), 10).float().cuda()
+    yt = torch.nn.functional.one_hot(torch.randint(0, 10, (n_t,), generator=g), 10).float().cuda()
     xt = xd[:n_t].contiguous()
-    w = torch.randn((n_t, n_s), device=xd.device)
     batched = nt.batch(kf, batch_size=bs)
-    ts = []
-    for i in range(3):
+    ts, grad = [], None
+    for i in range(reps + 1):
         xs = xd[1000:1000 + n_s].clone().requires_grad_(True)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
-        k = batched(xt, xs, 'ntk')
-        (w * k).sum().backward()
+        kss = batched(xs, None, 'ntk', precision=precision)
+        kts = batched(xt, xs, 'ntk', precision=precision)
+        alpha = predict.kernel_ridge_solve(kss, ys, diag_reg=1e-6)
+        loss = ((yt - predict.matmul(kts, alpha)) ** 2).sum()
+        loss.backward()
         b.record()
         torch.cuda.synchronize()
         if i:
             ts.append(a.elapsed_time(b))
+        grad = xs.grad
     ms = statistics.mean(ts)
-    return {'ms': round(ms, 2), 'pairs': n_t * n_s, 'entries_per_s': round(n_t * n_s / (ms / 1e3), 1),
-            'config': f'Myrtle-5 ntk fwd + d/dx_s, x_t [{n_t}], x_s [{n_s}], batch_size {bs}'}
+    entries = n_s * n_s + n_t * n_s
+    return {'ms': round(ms, 2), 'entries': entries,
+            'entries_per_s': round(entries / (ms / 1e3), 1), 'precision': precision,
+            'config': f'Myrtle-5 NTK kernel-ridge loss, d/dx_s; x_s [{n_s}], x_t [{n_t}], '
+                      f'nt.batch(batch_size={bs})'}, grad
 
 
 def gram_roofline(torch, O, dev):
@@ -447,13 +463,13 @@ def profile_stencil(pairs: int):
 
 
 def profile_fwd_bwd(n_s: int):
-    """The fwd+bwd measurement alone: x_t [2 n_s], x_s [n_s], tiles of n_s (launch lists)."""
+    """The fwd+bwd measurement alone: x_s [n_s], x_t [2 n_s], tiles of 16 (launch lists)."""
     import torch
     import nt_gb300 as nt
     from nt_gb300 import stax
     _, _, kf = stax.serial(*myrtle5(stax))
     x = torch.from_numpy(make_inputs(2000)).cuda()
-    r = fwd_bwd_timing(torch, nt, kf, x, n_t=2 * n_s, n_s=n_s, bs=n_s)
+    r, _ = fwd_bwd_timing(torch, nt, kf, x, n_t=2 * n_s, n_s=n_s, bs=16, reps=1)
     print(json.dumps({'profile_fwd_bwd': n_s, **r}))
 
 

@@ -469,11 +469,13 @@ def _sq(v, dev):
     return torch.tensor(float(v) ** 2, device=dev)
 
 
-def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: bool) -> Kernel:
-    """kernel_fn(x1, x2) through the differentiable layer Functions."""
+def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: bool,
+           precision: str = 'fp32') -> Kernel:
+    """kernel_fn(x1, x2) through the differentiable layer Functions ('mixed': the
+    compensated var1 var2 - q^2 in the activation rules and their VJPs)."""
     from .stax import Padding, _act_struct, _Ctx, _pads
     dev = x1.device
-    ctx = _Ctx('fp32')
+    ctx = _Ctx(precision)
     if x1.ndim > 4:
         raise NotImplementedError('nt_gb300 supports at most two spatial dimensions')
     if specs and specs[0].channel_axis_none and x1.ndim > 2:

@@ -51,7 +51,7 @@ class _CheckpointedKernel(torch.autograd.Function):
         with torch.no_grad():
             res = _forward_grid(kfn, x1, x2o, bs, precision)
         ctx.save_for_backward(x1, x2)
-        ctx.kfn, ctx.bs = kfn, bs
+        ctx.kfn, ctx.bs, ctx.precision = kfn, bs, precision
         return res.nngp, res.ntk
 
     @staticmethod
@@ -63,17 +63,25 @@ class _CheckpointedKernel(torch.autograd.Function):
         gx1 = torch.zeros_like(x1)
         gxb = gx1 if x2o is None else torch.zeros_like(x2o)
         bs = ctx.bs
+        symmetric = x2o is None
         for r0, rn in _tiles(x1.shape[0], bs):
             for c0, cn in _tiles(xb.shape[0], bs):
+                # K(x, x) is symmetric: the tile (c, r) is the transpose of the tile (r, c),
+                # so each off-diagonal pair of tiles is recomputed once, with both cotangents
+                if symmetric and c0 < r0:
+                    continue
                 with torch.enable_grad():
                     a = x1[r0:r0 + rn].detach().requires_grad_(True)
                     b = xb[c0:c0 + cn].detach().requires_grad_(True)
-                    k = _autograd.run_ad(ctx.kfn.specs, a, b, True)
+                    k = _autograd.run_ad(ctx.kfn.specs, a, b, True, ctx.precision)
                     outs, grads = [], []
                     for o, g in ((k.nngp, gq), (k.ntk, gt)):
                         if g is not None:
+                            gg = g[r0:r0 + rn, c0:c0 + cn]
+                            if symmetric and c0 > r0:
+                                gg = gg + g[c0:c0 + cn, r0:r0 + rn].transpose(0, 1)
                             outs.append(o)
-                            grads.append(g[r0:r0 + rn, c0:c0 + cn])
+                            grads.append(gg)
                     torch.autograd.backward(outs, grads)
                 gx1[r0:r0 + rn] += a.grad
                 gxb[c0:c0 + cn] += b.grad

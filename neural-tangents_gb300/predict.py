@@ -195,3 +195,69 @@ def negative_log_likelihood(k_train_train, y_train, diag_reg: float = 0.,
     k = k_train_train if isinstance(k_train_train, torch.Tensor) else _dev(k_train_train)
     y = _dev(y_train)
     return _NLL.apply(k, y, float(diag_reg), bool(diag_reg_absolute_scale), int(refine_iters))
+
+
+class _RidgeSolve(torch.autograd.Function):
+    """alpha = A^{-1} Y, A = K + lambda I; backward: gY = A^{-1} g,
+    gK = -gY alpha^T - [relative lambda] (r / n) <gY, alpha> I."""
+
+    @staticmethod
+    def forward(ctx, k, y, diag_reg, absolute, refine_iters):
+        k = k.contiguous()
+        y2 = y.reshape(y.shape[0], -1).contiguous()
+        solver = CholeskySolver(k, diag_reg, absolute, refine_iters)
+        alpha = solver.solve(y2)
+        ctx.solver, ctx.alpha, ctx.meta = solver, alpha, (diag_reg, absolute, tuple(y.shape))
+        return alpha.reshape(y.shape)
+
+    @staticmethod
+    def backward(ctx, g):
+        diag_reg, absolute, yshape = ctx.meta
+        solver, alpha = ctx.solver, ctx.alpha
+        n = alpha.shape[0]
+        gy = solver.solve(g.reshape(n, -1).contiguous())
+        gk = torch.empty((n, n), device=alpha.device)
+        L.call('ntg_gemm_ex', L.stream(), L.ptr(gy), L.ptr(alpha.t().contiguous()), L.ptr(gk), n,
+               n, alpha.shape[1], 0, -1., 0)
+        if not absolute and diag_reg:
+            gk.diagonal().sub_((diag_reg / n) * (gy.double() * alpha.double()).sum().float())
+        return gk, gy.reshape(yshape), None, None, None
+
+
+def kernel_ridge_solve(k_train_train, y_train, diag_reg: float = 0.,
+                       diag_reg_absolute_scale: bool = False, refine_iters: int = 2):
+    """(K + diag_reg * trace(K) / n * I)^{-1} y on this module's Cholesky kernels,
+    differentiable with respect to K and y (a helper for kernel-ridge losses such
+    as the support-set objective of dataset distillation; the reference computes
+    the same solve inside gradient_descent_mse, predict.py:1235-1258). The
+    backward reuses the cached factorisation: gY = A^{-1} g, gK = -gY alpha^T
+    (minus the trace term of a relative diag_reg)."""
+    k = k_train_train if isinstance(k_train_train, torch.Tensor) else _dev(k_train_train)
+    y = y_train if isinstance(y_train, torch.Tensor) else _dev(y_train)
+    return _RidgeSolve.apply(k, y, float(diag_reg), bool(diag_reg_absolute_scale),
+                             int(refine_iters))
+
+
+class _MatMul(torch.autograd.Function):
+    """a @ b on the library's FP32 GEMM, with its two adjoint GEMMs."""
+
+    @staticmethod
+    def forward(ctx, a, b):
+        a, b = a.contiguous(), b.contiguous()
+        ctx.save_for_backward(a, b)
+        return _gemm(a, b)
+
+    @staticmethod
+    def backward(ctx, g):
+        a, b = ctx.saved_tensors
+        g = g.contiguous()
+        ga = _gemm(g, b.t().contiguous())
+        gb = torch.empty_like(b)
+        L.call('ntg_gemm_ex', L.stream(), L.ptr(a), L.ptr(g), L.ptr(gb), b.shape[0], b.shape[1],
+               a.shape[0], 1, 1., 0)
+        return ga, gb
+
+
+def matmul(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """Differentiable a @ b for float32 CUDA matrices on the library's GEMM kernels."""
+    return _MatMul.apply(a, b)

@@ -622,7 +622,7 @@ class KernelFn:
             if _autograd.needs_grad(self.specs, x1, x2t):
                 if ds:
                     raise NotImplementedError('gradients of diagonal_spatial kernels')
-                k = _autograd.run_ad(self.specs, x1, x2t, compute_ntk)
+                k = _autograd.run_ad(self.specs, x1, x2t, compute_ntk, precision)
                 if names is None:
                     return k
                 vals = tuple(getattr(k, n) for n in names)

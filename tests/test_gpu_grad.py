@@ -268,3 +268,49 @@ def test_input_covariance_adjoint_single_pass(nt, pairs):
         scale = float(want.abs().max()) if float(want.abs().max()) > 0 else 1.
         assert float((got.double() - want).abs().max()) / scale < 1e-5
         assert float((got - ref).abs().max()) / scale < 1e-5
+
+
+def test_batched_symmetric_backward_equals_unbatched(nt):
+    """nt.batch(x, None) recomputes each off-diagonal pair of tiles once, with the
+    cotangents of both; the input gradient equals one untiled evaluation."""
+    rng = np.random.default_rng(6)
+    xs = torch.tensor(rng.standard_normal((5, 8, 8, 3)), dtype=torch.float32, device='cuda')
+    w = torch.tensor(rng.standard_normal((5, 5)), dtype=torch.float32, device='cuda')
+    s = nt.stax
+    kf = s.serial(s.Conv(1, (3, 3), padding='SAME', W_std=1.4, b_std=0.1), s.Relu(),
+                  s.AvgPool((2, 2), (2, 2)), s.Conv(1, (3, 3), padding='SAME', W_std=1.4),
+                  s.Relu(), s.GlobalAvgPool(), s.Dense(1, 1.3, 0.))[2]
+    for precision in ('fp32', 'mixed'):
+        a = xs.clone().requires_grad_(True)
+        (w * kf(a, None, 'ntk', precision=precision)).sum().backward()
+        b = xs.clone().requires_grad_(True)
+        (w * nt.batch(kf, batch_size=2)(b, None, 'ntk', precision=precision)).sum().backward()
+        torch.testing.assert_close(b.grad, a.grad, rtol=1e-4, atol=1e-6)
+
+
+def test_kernel_ridge_solve_gradients(nt):
+    """predict.kernel_ridge_solve (Cholesky kernels, relative diag_reg) and
+    predict.matmul: gradients with respect to K, y and the test kernel against
+    float64 torch autograd of the same expressions."""
+    rng = np.random.default_rng(8)
+    n, m, nt_ = 40, 3, 25
+    f = rng.standard_normal((n, 60))
+    k = torch.tensor(f @ f.T / 60, device='cuda')
+    y = torch.tensor(rng.standard_normal((n, m)), device='cuda')
+    kt = torch.tensor(rng.standard_normal((nt_, n)), device='cuda')
+    yt = torch.tensor(rng.standard_normal((nt_, m)), device='cuda')
+
+    def loss64(kk, yy, ktt):
+        a = kk + 1e-2 * torch.trace(kk) / n * torch.eye(n, device='cuda', dtype=kk.dtype)
+        alpha = torch.linalg.solve(a, yy)
+        return ((yt.double() - ktt @ alpha) ** 2).sum()
+
+    leaves64 = [v.double().clone().requires_grad_(True) for v in (k, y, kt)]
+    loss64(*leaves64).backward()
+    leaves = [v.float().clone().requires_grad_(True) for v in (k, y, kt)]
+    alpha = nt.predict.kernel_ridge_solve(leaves[0], leaves[1], diag_reg=1e-2)
+    loss = ((yt.float() - nt.predict.matmul(leaves[2], alpha)) ** 2).sum()
+    loss.backward()
+    for got, want in zip(leaves, leaves64):
+        err = float((got.grad.double() - want.grad).abs().max() / want.grad.abs().max())
+        assert err < 1e-4, err
