@@ -208,6 +208,8 @@ def run_gpu(args):
     fbmx, gmx = fwd_bwd_timing(torch, nt, kf, xd, precision='mixed')
     fbmx['grad_rel_diff_vs_fp32'] = float((gmx - g32).abs().max() / g32.abs().max())
     fwd_bwd = {'ms': fbmx['ms'], 'fp32': fb32, 'mixed': fbmx}
+    side = {'myrtle10': myrtle10_timing(torch, nt, xd), 'cholesky': cholesky_timing(torch, O, dev),
+            'nll': nll_timing(torch, nt, dev)}
 
     # Mixed precision (compensated) variant of the same step and its error vs plain.
     torch.cuda.synchronize()
@@ -273,6 +275,7 @@ def run_gpu(args):
         'stencil_roofline': st_gbs,
         'gram_tc': gram_tc,
         'fwd_bwd': fwd_bwd,
+        'side': side,
         'gpu_launches': int(launches),
         'clocks': clocks,
     }
@@ -347,6 +350,90 @@ def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=16, precision='fp32', 
             'entries_per_s': round(entries / (ms / 1e3), 1), 'precision': precision,
             'config': f'Myrtle-5 NTK kernel-ridge loss, d/dx_s; x_s [{n_s}], x_t [{n_t}], '
                       f'nt.batch(batch_size={bs})'}, grad
+
+
+def myrtle10(m):
+    """Myrtle-10: Conv3x3+Relu blocks [3, 3, 3] separated by AvgPool(2, 2), GlobalAvgPool, Dense."""
+    conv = lambda: m.Conv(1, (3, 3), padding='SAME', W_std=2 ** .5, b_std=0.)
+    layers = []
+    for i, n in enumerate((3, 3, 3)):
+        for _ in range(n):
+            layers += [conv(), m.Relu()]
+        if i < 2:
+            layers += [m.AvgPool((2, 2), (2, 2))]
+    return layers + [m.GlobalAvgPool(), m.Dense(10, 2 ** .5, 0.)]
+
+
+def _timed(torch, fn, reps=3):
+    ts = []
+    for i in range(reps + 1):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        torch.cuda.synchronize()
+        if i:
+            ts.append(a.elapsed_time(b))
+    return statistics.median(ts)
+
+
+def myrtle10_timing(torch, nt, xd, n1=128, n2=200):
+    """Myrtle-10 nngp+ntk on a ragged 128 x 200 block of the synthetic inputs (one fused
+    launch over the block plus the per-sample chains of its 328 inputs), plain and mixed."""
+    from nt_gb300 import stax
+    _, _, kf = stax.serial(*myrtle10(stax))
+    x1, x2 = xd[:n1].contiguous(), xd[n1:n1 + n2].contiguous()
+    out = {'config': f'Myrtle-10 [3,3,3] + GlobalAvgPool, block {n1} x {n2}'}
+    for prec in ('fp32', 'mixed'):
+        ms = _timed(torch, lambda: kf(x1, x2, ('nngp', 'ntk'), precision=prec))
+        out[prec] = {'ms': round(ms, 2), 'entries_per_s': round(n1 * n2 / (ms / 1e3), 1)}
+    return out
+
+
+def cholesky_timing(torch, O, dev, n=5000, m=10):
+    """predict.gradient_descent_mse at t = None for n = 5000 training points and 10 one-hot
+    targets: FP32 Cholesky of K + 1e-4 tr(K)/n I, FP32 triangular solves, two FP64 refinement
+    steps, and the test prediction for 100 points. K is a synthetic SPD kernel (the Gram of
+    iid N(0,1) features of width 6144)."""
+    from nt_gb300 import predict
+    g = torch.Generator(device='cpu').manual_seed(2)
+    x = torch.randn((n, 6144), device=dev)
+    k = O.gram(x, x, 0)
+    y = torch.nn.functional.one_hot(torch.randint(0, 10, (n,), generator=g), m).float().to(dev)
+    kts = k[:100].contiguous()
+    res = {}
+
+    def run():
+        pred = predict.gradient_descent_mse(k, y, diag_reg=1e-4)
+        res['out'] = pred(None, 0., 0., kts)
+
+    ms = _timed(torch, run)
+    return {'n': n, 'targets': m, 'ms': round(ms, 2),
+            'flops': round(n ** 3 / 3 / 1e9, 1), 'unit_flops': 'GFLOP (factorisation)'}
+
+
+def nll_timing(torch, nt, dev):
+    """NNGP negative log marginal likelihood of a depth-3 FCN (Dense+Relu x 3, Dense) on
+    X [4096, 3072], Y [4096, 10] (iid N(0,1)) and its gradient with respect to the shared
+    (W_std, b_std): input Gram, layer rules and their adjoints, Cholesky and its adjoint."""
+    from nt_gb300 import predict, stax
+    x = torch.randn((4096, 3072), device=dev)
+    y = torch.randn((4096, 10), device=dev)
+    out = {'config': 'depth-3 FCN NNGP NLL, X [4096, 3072], d/d(W_std, b_std)'}
+    for prec in ('fp32', 'mixed'):
+        w = torch.tensor(1.5, device=dev, requires_grad=True)
+        b = torch.tensor(0.1, device=dev, requires_grad=True)
+        kf = stax.serial(stax.Dense(512, w, b), stax.Relu(), stax.Dense(512, w, b), stax.Relu(),
+                         stax.Dense(512, w, b), stax.Relu(), stax.Dense(1, w, b))[2]
+
+        def run():
+            w.grad = b.grad = None
+            k = kf(x, None, 'nngp', precision=prec)
+            predict.negative_log_likelihood(k, y, diag_reg=1e-4).backward()
+
+        ms = _timed(torch, run)
+        out[prec] = {'ms': round(ms, 2), 'grad': [float(w.grad), float(b.grad)]}
+    return out
 
 
 def gram_roofline(torch, O, dev):

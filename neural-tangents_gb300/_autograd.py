@@ -58,11 +58,11 @@ class InputFn(torch.autograd.Function):
     """requirements.py:641-830: inputs -> (nngp, cov1, cov2)."""
 
     @staticmethod
-    def forward(ctx, x1, x2):
+    def forward(ctx, x1, x2, gram_precision=0):
         x2o = _opt(x2)
         xb = x1 if x2o is None else x2o
         if x1.ndim == 2:
-            nngp = O.gram(x1, xb, 0)
+            nngp = O.gram(x1, xb, gram_precision)
             cov1 = torch.diagonal(nngp).contiguous() if x2o is None else O.cov_diag(x1)
             cov2 = _e(x1.device) if x2o is None else O.cov_diag(x2o)
         else:
@@ -99,7 +99,7 @@ class InputFn(torch.autograd.Function):
             if x2o is not None:
                 L.call('ntg_cov_diag_bwd', s, L.ptr(gc2.contiguous()), L.ptr(x2o), L.ptr(gx2),
                        n2, d)
-            return gx1, gx2
+            return gx1, gx2, None
         y1 = x1 if x1.ndim == 4 else x1.unsqueeze(2)
         yb = None if x2o is None else (x2o if x2o.ndim == 4 else x2o.unsqueeze(2))
         gy1 = gx1 if x1.ndim == 4 else gx1.unsqueeze(2)
@@ -114,7 +114,7 @@ class InputFn(torch.autograd.Function):
                 continue
             L.call('ntg_input_fs_bwd2', s, L.ptr(gcv.contiguous()), L.ptr(yy), None, L.ptr(gg),
                    None, yy.shape[0], 0, a, c, k)
-        return gx1, gx2
+        return gx1, gx2, None
 
 
 # ---------------------------------------------------------------------------
@@ -483,7 +483,7 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
         x2 = None if x2 is None else x2.reshape(x2.shape[0], -1)
     shape1 = tuple(x1.shape)
     shape2 = shape1 if x2 is None else tuple(x2.shape)
-    q, c1, c2 = InputFn.apply(x1, _e(dev) if x2 is None else x2)
+    q, c1, c2 = InputFn.apply(x1, _e(dev) if x2 is None else x2, ctx.gram_precision)
     t = torch.zeros((), device=dev) if compute_ntk else None
     is_gaussian, is_reversed = False, False
     for sp in specs:

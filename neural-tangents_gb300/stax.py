@@ -92,6 +92,11 @@ class _Ctx:
     def compensated(self) -> int:
         return 1 if self.precision == 'mixed' else 0
 
+    @property
+    def gram_precision(self) -> int:
+        """ntg_gram precision: 1 (split-BF16 tcgen05) for the mixed form."""
+        return 1 if self.precision == 'mixed' else 0
+
 
 def _act_struct(p: dict, ctx: _Ctx, stabilize: float = 0.) -> L.Act:
     if p['fn'] == 'abrelu':

@@ -237,3 +237,26 @@ def test_activation_needs_gaussian_input(nt):
     _, _, kf = s.serial(s.Relu())
     with pytest.raises(ValueError, match='Gaussian'):
         kf(np.ones((2, 3)), None)
+
+
+@pytest.mark.parametrize('depth,readout', [(10, 'gap'), (7, 'flatten')])
+def test_myrtle_deeper_fused_chain_vs_oracle(nt, cifar_like, depth, readout):
+    """Myrtle-10 ([3, 3, 3] + GlobalAvgPool) and Myrtle-7 on the fused kernel against the
+    float64 oracle: plain FP32 within 1e-5, the mixed form within 1e-4."""
+    x1, x2 = cifar_like
+    s = nt.stax
+    _, _, kf = s.serial(*myrtle(s, depth, readout))
+    want = o.serial(*myrtle(o, depth, readout))(x1[:2], x2, ('nngp', 'ntk'))
+    plain = kf(x1[:2], x2, ('nngp', 'ntk'))
+    mixed = kf(x1[:2], x2, ('nngp', 'ntk'), precision='mixed')
+    for g, w in zip(plain, want):
+        assert elem_rel_err(cpu(g), w) < RTOL
+    for g, w in zip(mixed, want):
+        assert elem_rel_err(cpu(g), w) < 1e-4
+
+
+def test_myrtle5_mixed_vs_oracle(nt, cifar_like):
+    x1, x2 = cifar_like
+    got, want = both(nt, lambda m: myrtle(m, 5), x1, x2, get=('nngp', 'ntk'), precision='mixed')
+    for g, w in zip(got, want):
+        assert elem_rel_err(g, w) < 1e-4
