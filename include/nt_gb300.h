@@ -220,12 +220,12 @@ int ntg_chol_factor(void* stream, const float* A, int64_t n, double diag_reg, in
                     float* L, double* lambda, int* info);
 /* Bytes of device workspace ntg_chol_solve needs for refinement. */
 size_t ntg_chol_workspace_bytes(int64_t n, int64_t m);
-/* X = (K + lambda I)^{-1} B for B [n, m] (m <= 128): FP32 triangular solves
- * with L, then `refine_iters` steps of iterative refinement whose residual
+/* X = (K + lambda I)^{-1} B for B [n, m]: blocked FP32 triangular solves with
+ * L, then `refine_iters` steps of iterative refinement whose residual
  * B - (K + lambda I) X is accumulated in FP64 (predict.py:1235-1258 with
  * cho_solve). `workspace` must hold ntg_chol_workspace_bytes(n, m) bytes when
  * refine_iters > 0 or final_residual != NULL; final_residual (device double,
- * optional) receives max |residual| of the returned X. */
+ * optional) receives max |residual| of the returned X (one more FP64 residual). */
 int ntg_chol_solve(void* stream, const float* A, const float* L, const double* lambda, int64_t n,
                    const float* B, int64_t m, float* X, int32_t refine_iters, void* workspace,
                    size_t workspace_bytes, double* final_residual);

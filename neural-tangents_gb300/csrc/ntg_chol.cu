@@ -148,9 +148,9 @@ __global__ void __launch_bounds__(256) syrk_update_kernel(float* __restrict__ L,
 }
 
 // Triangular solves L y = b (forward) and L^T x = y (backward) for m right-hand
-// sides, in blocks of TB rows: a single CTA solves the diagonal block (one warp
-// per right-hand side), then a wide kernel applies that block to every other
-// row with coalesced reads of L.
+// sides, in blocks of TB rows: the diagonal block is solved for all columns by
+// ceil(m / 32) CTAs (one warp per column), then a tiled FP32 GEMM subtracts the
+// solved block from every remaining row block.
 constexpr int TB = 64;
 
 __global__ void trsv_diag_kernel(const float* __restrict__ L, int64_t n, float* __restrict__ X,
@@ -163,7 +163,8 @@ __global__ void trsv_diag_kernel(const float* __restrict__ L, int64_t n, float* 
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int64_t c = warp; c < m; c += nw) {
+  const int64_t c_end = imin64(m, (int64_t)(blockIdx.x + 1) * 32);
+  for (int64_t c = (int64_t)blockIdx.x * 32 + warp; c < c_end; c += nw) {
     float x0 = lane < nb ? X[(r0 + lane) * m + c] : 0.f;
     float x1 = lane + 32 < nb ? X[(r0 + lane + 32) * m + c] : 0.f;
     if (!transpose) {
@@ -190,59 +191,103 @@ __global__ void trsv_diag_kernel(const float* __restrict__ L, int64_t n, float* 
   }
 }
 
-// forward: rows rr >= r0 + nb:  X[rr] -= L[rr, block] X[block]   (one warp per row)
-// backward: rows rr < r0:       X[rr] -= L[block, rr]^T X[block] (one thread per row)
-__global__ void trsv_update_kernel(const float* __restrict__ L, int64_t n, float* __restrict__ X,
-                                   int64_t m, int64_t r0, int transpose) {
-  extern __shared__ float xb[];  // [TB][m] solved block
-  const int nb = (int)imin64(TB, n - r0);
-  for (int64_t idx = threadIdx.x; idx < (int64_t)nb * m; idx += blockDim.x)
-    xb[idx] = X[(r0 + idx / m) * m + idx % m];
-  __syncthreads();
-  if (!transpose) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int64_t rr = r0 + nb + (int64_t)blockIdx.x * nw + warp;
-    if (rr >= n) return;
-    const float l0 = lane < nb ? L[rr * n + r0 + lane] : 0.f;
-    const float l1 = lane + 32 < nb ? L[rr * n + r0 + lane + 32] : 0.f;
-    for (int64_t c = 0; c < m; ++c) {
-      float sacc = l0 * (lane < nb ? xb[lane * m + c] : 0.f);
-      if (lane + 32 < nb) sacc = fmaf(l1, xb[(lane + 32) * m + c], sacc);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
-      if (lane == 0) X[rr * m + c] -= sacc;
+// X[row0 + i, j] -= sum_{k < nb} A(i, k) X[r0 + k, j] over 64 x 64 tiles of (i, j):
+//   forward   A(i, k) = L[row0 + i, r0 + k]   (rows after the block)
+//   transpose A(i, k) = L[r0 + k, row0 + i]   (rows before the block)
+__global__ void __launch_bounds__(256)
+    trsm_update_kernel(const float* __restrict__ L, int64_t n, float* __restrict__ X, int64_t m,
+                       int64_t r0, int nb, int64_t row0, int64_t rows, int transpose) {
+  __shared__ __align__(16) float As[TB][64 + 4];  // [k][i]
+  __shared__ __align__(16) float Bs[TB][64 + 4];  // [k][j]
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t i0 = (int64_t)blockIdx.y * 64, j0 = (int64_t)blockIdx.x * 64;
+  for (int idx = threadIdx.x; idx < TB * 64; idx += 256) {
+    if (!transpose) {
+      const int i = idx / TB, k = idx % TB;
+      As[k][i] = (i0 + i < rows && k < nb) ? L[(row0 + i0 + i) * n + r0 + k] : 0.f;
+    } else {
+      const int k = idx / 64, i = idx % 64;
+      As[k][i] = (i0 + i < rows && k < nb) ? L[(r0 + k) * n + row0 + i0 + i] : 0.f;
     }
-  } else {
-    const int64_t rr = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (rr >= r0) return;
-    for (int64_t c = 0; c < m; ++c) {
-      float sacc = 0.f;
-      for (int i = 0; i < nb; ++i) sacc = fmaf(L[(r0 + i) * n + rr], xb[i * m + c], sacc);
-      X[rr * m + c] -= sacc;
+    const int k = idx / 64, j = idx % 64;
+    Bs[k][j] = (k < nb && j0 + j < m) ? X[(r0 + k) * m + j0 + j] : 0.f;
+  }
+  __syncthreads();
+  float acc[4][4] = {};
+  for (int k = 0; k < nb; ++k) {
+    const float4 a = *reinterpret_cast<const float4*>(&As[k][ty * 4]);
+    const float4 b = *reinterpret_cast<const float4*>(&Bs[k][tx * 4]);
+    const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(av[u], bv[v], acc[u][v]);
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int64_t i = i0 + ty * 4 + u;
+    if (i >= rows) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int64_t j = j0 + tx * 4 + v;
+      if (j < m) X[(row0 + i) * m + j] -= acc[u][v];
     }
   }
 }
 
-// r = b - (A + lambda I) x in FP64; one warp per row, all m columns.
-__global__ void residual_kernel(const float* __restrict__ A, int64_t n, const double* lambda,
-                                const float* __restrict__ B, const double* __restrict__ X,
-                                int64_t m, float* __restrict__ R, double* __restrict__ rnorm) {
-  const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-  const int lane = threadIdx.x & 31;
-  if (row >= n) return;
-  const float* ar = A + row * n;
-  for (int64_t c = 0; c < m; ++c) {
-    double s = 0.0;
-    for (int64_t j = lane; j < n; j += 32) s = fma((double)ar[j], X[j * m + c], s);
+// R = B - (A + lambda I) X in FP64 over 64 x 64 tiles of (row, column), X [n, m]
+// in FP64; max |R| into rnorm.
+__global__ void __launch_bounds__(256)
+    residual_kernel(const float* __restrict__ A, int64_t n, const double* lambda,
+                    const float* __restrict__ B, const double* __restrict__ X, int64_t m,
+                    float* __restrict__ R, double* __restrict__ rnorm) {
+  __shared__ double As[16][64 + 1];  // [k][i]
+  __shared__ double Xs[16][64 + 1];  // [k][j]
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t i0 = (int64_t)blockIdx.y * 64, j0 = (int64_t)blockIdx.x * 64;
+  double acc[4][4] = {};
+  for (int64_t k0 = 0; k0 < n; k0 += 16) {
+    for (int idx = threadIdx.x; idx < 16 * 64; idx += 256) {
+      const int i = idx / 16, k = idx % 16;
+      As[k][i] = (i0 + i < n && k0 + k < n) ? (double)A[(i0 + i) * n + k0 + k] : 0.0;
+      const int kk = idx / 64, j = idx % 64;
+      Xs[kk][j] = (k0 + kk < n && j0 + j < m) ? X[(k0 + kk) * m + j0 + j] : 0.0;
+    }
+    __syncthreads();
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) {
-      const double r = (double)B[row * m + c] - s - lambda[0] * X[row * m + c];
-      R[row * m + c] = (float)r;
-      atomicMax(reinterpret_cast<unsigned long long*>(rnorm),
-                (unsigned long long)__double_as_longlong(fabs(r)));
+    for (int k = 0; k < 16; ++k) {
+      double av[4], bv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        av[u] = As[k][ty * 4 + u];
+        bv[u] = Xs[k][tx * 4 + u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) acc[u][v] = fma(av[u], bv[v], acc[u][v]);
+    }
+    __syncthreads();
+  }
+  double rmax = 0.0;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int64_t i = i0 + ty * 4 + u;
+    if (i >= n) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int64_t j = j0 + tx * 4 + v;
+      if (j >= m) continue;
+      const double r = (double)B[i * m + j] - acc[u][v] - lambda[0] * X[i * m + j];
+      R[i * m + j] = (float)r;
+      rmax = fmax(rmax, fabs(r));
     }
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+  if ((threadIdx.x & 31) == 0 && rmax > 0.0)
+    atomicMax(reinterpret_cast<unsigned long long*>(rnorm),
+              (unsigned long long)__double_as_longlong(rmax));
 }
 
 __global__ void to_double_kernel(const float* __restrict__ a, double* __restrict__ b, int64_t n) {
@@ -308,16 +353,17 @@ int grid1(int64_t n) {
 
 int trsv(cudaStream_t s, const float* L, int64_t n, float* X, int64_t m, int transpose) {
   const int64_t nblk = ceil_div(n, TB);
-  const size_t sm = sizeof(float) * TB * m;
   for (int64_t bb = 0; bb < nblk; ++bb) {
     const int64_t blk = transpose ? nblk - 1 - bb : bb;
     const int64_t r0 = blk * TB;
-    trsv_diag_kernel<<<1, 256, 0, s>>>(L, n, X, m, r0, transpose);
-    const int64_t rows = transpose ? r0 : n - imin64(n, r0 + TB);
+    const int nb = (int)imin64(TB, n - r0);
+    trsv_diag_kernel<<<(unsigned)ceil_div(m, 32), 256, 0, s>>>(L, n, X, m, r0, transpose);
     note_launch();
+    const int64_t row0 = transpose ? 0 : r0 + nb;
+    const int64_t rows = transpose ? r0 : n - row0;
     if (rows > 0) {
-      const unsigned g = (unsigned)(transpose ? ceil_div(rows, 256) : ceil_div(rows, 8));
-      trsv_update_kernel<<<g, 256, sm, s>>>(L, n, X, m, r0, transpose);
+      dim3 grid((unsigned)ceil_div(m, 64), (unsigned)ceil_div(rows, 64));
+      trsm_update_kernel<<<grid, 256, 0, s>>>(L, n, X, m, r0, nb, row0, rows, transpose);
       note_launch();
     }
   }
@@ -368,7 +414,8 @@ extern "C" int ntg_chol_solve(void* stream, const float* A, const float* L, cons
   NTG_REQUIRE(A && L && lambda && B && X, "ntg_chol_solve: null pointer");
   NTG_REQUIRE(n > 0 && m > 0, "ntg_chol_solve: sizes must be positive");
   NTG_REQUIRE(refine_iters >= 0 && refine_iters <= 16, "ntg_chol_solve: 0..16 refinement steps");
-  NTG_REQUIRE(m <= 128, "ntg_chol_solve: at most 128 right-hand sides per call");
+  NTG_REQUIRE(ceil_div(m, 64) <= 65535 && ceil_div(m, 32) <= (1ll << 31) - 1,
+              "ntg_chol_solve: too many right-hand sides");
   cudaStream_t s = as_stream(stream);
   if (cudaMemcpyAsync(X, B, sizeof(float) * n * m, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
     return check_launch("ntg_chol_solve copy");
@@ -385,10 +432,14 @@ extern "C" int ntg_chol_solve(void* stream, const float* A, const float* L, cons
   float* r32 = reinterpret_cast<float*>(ws + 256 + sizeof(double) * n * m);
   to_double_kernel<<<grid1(n * m), 256, 0, s>>>(X, x64, n * m);
   note_launch();
+  const dim3 rgrid((unsigned)ceil_div(m, 64), (unsigned)ceil_div(n, 64));
+  // refine_iters residual + correction rounds, then the residual of the result
+  // only when the caller asks for its norm
   for (int it = 0; it <= refine_iters; ++it) {
+    if (it == refine_iters && !final_residual) break;
     if (cudaMemsetAsync(rnorm, 0, sizeof(double), s) != cudaSuccess)
       return check_launch("ntg_chol_solve memset");
-    residual_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(A, n, lambda, B, x64, m, r32, rnorm);
+    residual_kernel<<<rgrid, 256, 0, s>>>(A, n, lambda, B, x64, m, r32, rnorm);
     note_launch();
     if (it == refine_iters) break;
     rc = trsv(s, L, n, r32, m, 0);

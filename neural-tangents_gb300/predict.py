@@ -57,27 +57,34 @@ class CholeskySolver:
                           f'would return.')
         self.residual = None
 
-    def solve(self, b: torch.Tensor, refine_iters: Optional[int] = None) -> torch.Tensor:
-        """A^{-1} b; refine_iters overrides the solver's FP64 refinement steps."""
+    COLS = 2048  # right-hand sides per ntg_chol_solve call (bounds the FP64 workspace)
+
+    def solve(self, b: torch.Tensor, refine_iters: Optional[int] = None,
+              residual: bool = True) -> torch.Tensor:
+        """A^{-1} b; refine_iters overrides the solver's FP64 refinement steps;
+        residual=False skips the final FP64 residual kept in self.residual."""
         refine = self.refine if refine_iters is None else int(refine_iters)
         b = b.reshape(self.n, -1).contiguous()
         if self.info:
             return torch.full_like(b, float('nan'))
         out = torch.empty_like(b)
-        if refine:
-            ws_bytes = int(L.load().ntg_chol_workspace_bytes(self.n, min(b.shape[1], 128)))
+        cols = min(b.shape[1], self.COLS)
+        if refine or residual:
+            ws_bytes = int(L.load().ntg_chol_workspace_bytes(self.n, cols))
             ws = torch.empty((ws_bytes,), device=b.device, dtype=torch.uint8)
-            res = torch.zeros((1,), device=b.device, dtype=torch.float64)
-        else:  # plain FP32 solve: no workspace, no residual
-            ws_bytes, ws, res = 0, None, None
-        for c0 in range(0, b.shape[1], 128):
-            bc = b[:, c0:c0 + 128].contiguous()
-            xc = torch.empty_like(bc)
+        else:  # plain FP32 solve: no workspace
+            ws_bytes, ws = 0, None
+        res = torch.zeros((1,), device=b.device, dtype=torch.float64) if residual else None
+        single = b.shape[1] <= cols
+        for c0 in range(0, b.shape[1], cols):
+            bc = b if single else b[:, c0:c0 + cols].contiguous()
+            xc = out if single else torch.empty_like(bc)
             L.call('ntg_chol_solve', L.stream(), L.ptr(self.k), L.ptr(self.L),
                    self.lam.data_ptr(), self.n, L.ptr(bc), bc.shape[1], L.ptr(xc), refine,
                    None if ws is None else ws.data_ptr(), ws_bytes,
                    None if res is None else res.data_ptr())
-            out[:, c0:c0 + 128] = xc
+            if not single:
+                out[:, c0:c0 + cols] = xc
         if res is not None:
             self.residual = res
         return out
@@ -184,7 +191,7 @@ class _NLL(torch.autograd.Function):
         # A^{-1} for the log-determinant term, refined like the solve itself: on the
         # ill-conditioned kernels of wide, deep FCNs the plain FP32 inverse moves this
         # gradient term by tens of percent
-        kinv = solver.solve(eye)
+        kinv = solver.solve(eye, residual=False)
         out = torch.empty((n, n), device=alpha.device)
         tr = torch.zeros(1, device=alpha.device, dtype=torch.float64)
         L.call('ntg_nll_grad', L.stream(), L.ptr(kinv), L.ptr(alpha.contiguous()), n, m,
@@ -225,7 +232,7 @@ class _RidgeSolve(torch.autograd.Function):
         diag_reg, absolute, yshape = ctx.meta
         solver, alpha = ctx.solver, ctx.alpha
         n = alpha.shape[0]
-        gy = solver.solve(g.reshape(n, -1).contiguous())
+        gy = solver.solve(g.reshape(n, -1).contiguous(), residual=False)
         gk = torch.empty((n, n), device=alpha.device)
         L.call('ntg_gemm_ex', L.stream(), L.ptr(gy), L.ptr(alpha.t().contiguous()), L.ptr(gk), n,
                n, alpha.shape[1], 0, -1., 0)

@@ -60,7 +60,7 @@ def test_cholesky_equals_eigh_at_infinite_time(nt):
     np.testing.assert_allclose(a, b, rtol=2e-4, atol=2e-5)
 
 
-@pytest.mark.parametrize('n,m', [(33, 1), (100, 10), (1000, 7), (2048, 10)])
+@pytest.mark.parametrize('n,m', [(33, 1), (100, 10), (1000, 7), (2048, 10), (300, 2500), (517, 129)])
 def test_solve_sizes_and_refinement(nt, n, m):
     rng = np.random.default_rng(n)
     g = rng.standard_normal((n, n + 5)).astype(np.float32)
