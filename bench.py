@@ -560,11 +560,22 @@ def profile_fwd_bwd(n_s: int):
     print(json.dumps({'profile_fwd_bwd': n_s, **r}))
 
 
+def profile_gram(n: int):
+    """One split-BF16 tcgen05 Gram X X^T / D of X [n, 3072] (ncu small case)."""
+    import torch
+    from nt_gb300 import _ops as O
+    x = torch.randn((n, 3072), device='cuda')
+    g = O.gram(x, x, 1)
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_gram': n, 'mean': float(g.mean())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--profile-tile', type=int, default=0)
     ap.add_argument('--profile-stencil', type=int, default=0)
     ap.add_argument('--profile-fwd-bwd', type=int, default=0)
+    ap.add_argument('--profile-gram', type=int, default=0)
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=3)
@@ -579,6 +590,8 @@ def main():
         profile_stencil(args.profile_stencil)
     elif args.profile_fwd_bwd:
         profile_fwd_bwd(args.profile_fwd_bwd)
+    elif args.profile_gram:
+        profile_gram(args.profile_gram)
     elif args.impl == 'reference':
         run_reference(args)
     else:

@@ -290,6 +290,44 @@ __global__ void __launch_bounds__(256)
               (unsigned long long)__double_as_longlong(rmax));
 }
 
+// The same residual for few right-hand sides (m <= 16): one warp per row reads
+// that row of A once and keeps the m FP64 dot products in registers.
+template <int MR>
+__global__ void __launch_bounds__(256)
+    residual_rows_kernel(const float* __restrict__ A, int64_t n, const double* lambda,
+                         const float* __restrict__ B, const double* __restrict__ X, int64_t m,
+                         float* __restrict__ R, double* __restrict__ rnorm) {
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float* ar = A + row * n;
+  double acc[MR];
+#pragma unroll
+  for (int c = 0; c < MR; ++c) acc[c] = 0.0;
+  for (int64_t j = lane; j < n; j += 32) {
+    const double a = (double)ar[j];
+    const double* xr = X + j * m;
+#pragma unroll
+    for (int c = 0; c < MR; ++c)
+      if (c < m) acc[c] = fma(a, xr[c], acc[c]);
+  }
+  double rmax = 0.0;
+#pragma unroll
+  for (int c = 0; c < MR; ++c) {
+    double v = acc[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (c < m && lane == 0) {
+      const double r = (double)B[row * m + c] - v - lambda[0] * X[row * m + c];
+      R[row * m + c] = (float)r;
+      rmax = fmax(rmax, fabs(r));
+    }
+  }
+  if (lane == 0 && rmax > 0.0)
+    atomicMax(reinterpret_cast<unsigned long long*>(rnorm),
+              (unsigned long long)__double_as_longlong(rmax));
+}
+
 __global__ void to_double_kernel(const float* __restrict__ a, double* __restrict__ b, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -439,7 +477,14 @@ extern "C" int ntg_chol_solve(void* stream, const float* A, const float* L, cons
     if (it == refine_iters && !final_residual) break;
     if (cudaMemsetAsync(rnorm, 0, sizeof(double), s) != cudaSuccess)
       return check_launch("ntg_chol_solve memset");
-    residual_kernel<<<rgrid, 256, 0, s>>>(A, n, lambda, B, x64, m, r32, rnorm);
+    if (m <= 4)
+      residual_rows_kernel<4><<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(A, n, lambda, B, x64, m,
+                                                                      r32, rnorm);
+    else if (m <= 16)
+      residual_rows_kernel<16><<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(A, n, lambda, B, x64, m,
+                                                                       r32, rnorm);
+    else
+      residual_kernel<<<rgrid, 256, 0, s>>>(A, n, lambda, B, x64, m, r32, rnorm);
     note_launch();
     if (it == refine_iters) break;
     rc = trsv(s, L, n, r32, m, 0);
