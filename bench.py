@@ -208,7 +208,8 @@ def run_gpu(args):
     fbmx, gmx = fwd_bwd_timing(torch, nt, kf, xd, precision='mixed')
     fbmx['grad_rel_diff_vs_fp32'] = float((gmx - g32).abs().max() / g32.abs().max())
     fwd_bwd = {'ms': fbmx['ms'], 'fp32': fb32, 'mixed': fbmx}
-    side = {'myrtle10': myrtle10_timing(torch, nt, xd), 'cholesky': cholesky_timing(torch, O, dev),
+    side = {'symmetric_grid': symmetric_grid_timing(torch, nt, kf, xd),
+            'myrtle10': myrtle10_timing(torch, nt, xd), 'cholesky': cholesky_timing(torch, O, dev),
             'nll': nll_timing(torch, nt, dev)}
 
     # Mixed precision (compensated) variant of the same step and its error vs plain.
@@ -388,6 +389,17 @@ def myrtle10_timing(torch, nt, xd, n1=128, n2=200):
         ms = _timed(torch, lambda: kf(x1, x2, ('nngp', 'ntk'), precision=prec))
         out[prec] = {'ms': round(ms, 2), 'entries_per_s': round(n1 * n2 / (ms / 1e3), 1)}
     return out
+
+
+def symmetric_grid_timing(torch, nt, kf, xd, n=1000):
+    """K(x, x) over n inputs through nt.batch(kernel_fn, 100)(x, None): the fused kernel
+    evaluates the pairs i <= j once (one persistent launch over the triangle) and mirrors
+    them; entries/s counts all n^2 entries of the result."""
+    x = xd[:n].contiguous()
+    batched = nt.batch(kf, batch_size=100)
+    ms = _timed(torch, lambda: batched(x, None, ('nngp', 'ntk')), reps=2)
+    return {'n': n, 'ms': round(ms, 2), 'entries_per_s': round(n * n / (ms / 1e3), 1),
+            'config': f'Myrtle-5 K(x, x), x [{n}], nt.batch(batch_size=100), symmetric grid'}
 
 
 def cholesky_timing(torch, O, dev, n=5000, m=10):

@@ -207,6 +207,13 @@ typedef struct {
 int ntg_chain_fwd(void* stream, const ntg_chain_t* prog, const float* x1, const float* x2,
                   int64_t r0, int64_t n1, int64_t c0, int64_t n2, const float* var1,
                   const float* var2, float* out_nngp, float* out_ntk, int64_t ld_out);
+/* The same network on the square tile of x rows [r0, r0 + n) with themselves
+ * (kernel_fn(x, None)): only the pairs i <= j are evaluated, each result is
+ * written at (i, j) and (j, i) of out [n, ld_out] — half the work of
+ * ntg_chain_fwd(x, x), and an exactly symmetric output. No counterpart in the
+ * reference, which evaluates every pair. */
+int ntg_chain_fwd_sym(void* stream, const ntg_chain_t* prog, const float* x, int64_t r0,
+                      int64_t n, const float* var, float* out_q, float* out_t, int64_t ld_out);
 
 /* ---- kernel regression (predict.gradient_descent_mse, t = None) -------- */
 /* Factor A = K + lambda I = L L^T in FP32 (predict.py:1224-1258 with

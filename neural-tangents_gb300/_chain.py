@@ -218,7 +218,11 @@ def run_fused(plan: ChainPlan, x1: torch.Tensor, x2: Optional[torch.Tensor], ctx
         out_t = torch.empty((n1, n2), device=x1.device, dtype=torch.float32)
     else:
         out_q, out_t = out
-    O.chain_fwd(pg, x1, xb, 0, n1, 0, n2, var1, var2, out_q, out_t, n2)
+    if x2 is None:
+        # K(x, x): the pairs i <= j once, mirrored (one launch over the triangle)
+        O.chain_fwd_sym(pg, x1, 0, n1, var1, out_q, out_t, n2)
+    else:
+        O.chain_fwd(pg, x1, xb, 0, n1, 0, n2, var1, var2, out_q, out_t, n2)
     shape1 = tuple(x1.shape)
     shape2 = tuple(xb.shape)
     for s in plan.spatial:

@@ -403,17 +403,28 @@ __device__ __forceinline__ void process_pooled_line(ChainCtx& cx, const ntg_chai
 }
 
 // Segment sizes 32 -> 16 -> 8 (nseg <= 3); segment 0 has N0 conv layers.
+// Pair p of the upper triangle (i <= j) of an n x n grid, row by row.
+__device__ __forceinline__ void tri_pair(int64_t p, int64_t n, int64_t& i, int64_t& j) {
+  auto start = [&](int64_t r) { return r * n - (r * (r - 1)) / 2; };  // first pair of row r
+  const double b = 2.0 * (double)n + 1.0;
+  int64_t r = (int64_t)floor((b - sqrt(fmax(b * b - 8.0 * (double)p, 0.0))) * 0.5);
+  if (r < 0) r = 0;
+  if (r > n - 1) r = n - 1;
+  while (r > 0 && start(r) > p) --r;
+  while (r + 1 < n && start(r + 1) <= p) ++r;
+  i = r;
+  j = r + (p - start(r));
+}
+
 template <int N0>
-__global__ void __launch_bounds__(NT, 1)
-    chain_fwd_kernel(const __grid_constant__ ntg_chain_t pg, const float* __restrict__ x1,
-                     const float* __restrict__ x2, int64_t r0, int64_t n1, int64_t c0,
-                     int64_t n2, const float* __restrict__ var1, const float* __restrict__ var2,
-                     float* __restrict__ out_q, float* __restrict__ out_t, int64_t ld_out) {
+__device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* __restrict__ x1,
+                                           const float* __restrict__ x2, int64_t gi, int64_t gj,
+                                           const float* __restrict__ var1,
+                                           const float* __restrict__ var2,
+                                           float* __restrict__ out_q, float* __restrict__ out_t,
+                                           int64_t o1, int64_t o2) {
   constexpr int S0 = 32, S1 = 16, S2 = 8;
   extern __shared__ __align__(16) float smem[];
-  const int64_t pair = blockIdx.x;
-  const int64_t i = pair / n2, j = pair - (pair / n2) * n2;
-  const int64_t gi = r0 + i, gj = c0 + j;
   const int K = pg.channels;
   const int nseg = pg.nseg;
 
@@ -527,9 +538,35 @@ __global__ void __launch_bounds__(NT, 1)
     }
     const int Sl = S0 >> (nseg - 1);
     const float cnt = pg.readout == 0 ? (float)Sl * Sl * Sl * Sl : (float)Sl * Sl;
-    out_q[i * ld_out + j] = sq / cnt;
-    if (out_t) out_t[i * ld_out + j] = st / cnt;
+    out_q[o1] = sq / cnt;
+    if (out_t) out_t[o1] = st / cnt;
+    if (o2 >= 0) {
+      out_q[o2] = sq / cnt;
+      if (out_t) out_t[o2] = st / cnt;
+    }
   }
+}
+
+// One CTA per pair of the tile, or (sym != 0) per pair i <= j of the upper
+// triangle of a square tile of x1 with itself, the result written at (i, j) and
+// (j, i); per pair the CTA runs the whole network.
+template <int N0>
+__global__ void __launch_bounds__(NT, 1)
+    chain_fwd_kernel(const __grid_constant__ ntg_chain_t pg, const float* __restrict__ x1,
+                     const float* __restrict__ x2, int64_t r0, int64_t n1, int64_t c0,
+                     int64_t n2, const float* __restrict__ var1, const float* __restrict__ var2,
+                     float* __restrict__ out_q, float* __restrict__ out_t, int64_t ld_out,
+                     int sym) {
+  const int64_t pair = blockIdx.x;
+  int64_t i, j;
+  if (sym) {
+    tri_pair(pair, n1, i, j);
+  } else {
+    i = pair / n2;
+    j = pair - i * n2;
+  }
+  chain_pair<N0>(pg, x1, x2, r0 + i, c0 + j, var1, var2, out_q, out_t, i * ld_out + j,
+                 sym && i != j ? j * ld_out + i : -1);
 }
 
 size_t chain_smem_bytes(const ntg_chain_t& pg) {
@@ -549,25 +586,31 @@ size_t chain_smem_bytes(const ntg_chain_t& pg) {
 
 using namespace ntg;
 
-extern "C" int ntg_chain_fwd(void* stream, const ntg_chain_t* prog, const float* x1,
-                             const float* x2, int64_t r0, int64_t n1, int64_t c0, int64_t n2,
-                             const float* var1, const float* var2, float* out_q, float* out_t,
-                             int64_t ld_out) {
-  NTG_REQUIRE(prog && x1 && x2 && var1 && var2 && out_q, "ntg_chain_fwd: null pointer");
+namespace {
+
+int launch_chain(const char* who, void* stream, const ntg_chain_t* prog, const float* x1,
+                 const float* x2, int64_t r0, int64_t n1, int64_t c0, int64_t n2,
+                 const float* var1, const float* var2, float* out_q, float* out_t, int64_t ld_out,
+                 int sym) {
+  const std::string w(who);
+  NTG_REQUIRE(prog && x1 && x2 && var1 && var2 && out_q, w + ": null pointer");
   const ntg_chain_t& pg = *prog;
-  NTG_REQUIRE(pg.s0 == 32, "ntg_chain_fwd: the fused chain needs 32x32 inputs");
-  NTG_REQUIRE(pg.nseg >= 1 && pg.nseg <= 3, "ntg_chain_fwd: 1 to 3 segments");
-  NTG_REQUIRE(pg.channels >= 1 && pg.channels <= 4, "ntg_chain_fwd: 1 to 4 input channels");
-  NTG_REQUIRE(pg.nconv[0] >= 1 && pg.nconv[0] <= 3, "ntg_chain_fwd: 1 to 3 convs in segment 0");
+  NTG_REQUIRE(pg.s0 == 32, w + ": the fused chain needs 32x32 inputs");
+  NTG_REQUIRE(pg.nseg >= 1 && pg.nseg <= 3, w + ": 1 to 3 segments");
+  NTG_REQUIRE(pg.channels >= 1 && pg.channels <= 4, w + ": 1 to 4 input channels");
+  NTG_REQUIRE(pg.nconv[0] >= 1 && pg.nconv[0] <= 3, w + ": 1 to 3 convs in segment 0");
   int nl = 0;
-  for (int s = 0; s < pg.nseg; ++s) {
-    NTG_REQUIRE(pg.nconv[s] >= 0 && pg.nconv[s] <= 3, "ntg_chain_fwd: 0 to 3 convs per segment");
-    nl += pg.nconv[s];
+  for (int sg = 0; sg < pg.nseg; ++sg) {
+    NTG_REQUIRE(pg.nconv[sg] >= 0 && pg.nconv[sg] <= 3, w + ": 0 to 3 convs per segment");
+    nl += pg.nconv[sg];
   }
-  NTG_REQUIRE(nl <= NTG_CHAIN_MAX_LAYERS, "ntg_chain_fwd: too many layers");
-  NTG_REQUIRE(pg.readout == 0 || pg.readout == 1, "ntg_chain_fwd: readout must be 0 or 1");
-  NTG_REQUIRE(n1 > 0 && n2 > 0 && r0 >= 0 && c0 >= 0 && ld_out >= n2, "ntg_chain_fwd: bad tile");
-  NTG_REQUIRE(n1 * n2 < (1ll << 31), "ntg_chain_fwd: tile too large");
+  NTG_REQUIRE(nl <= NTG_CHAIN_MAX_LAYERS, w + ": too many layers");
+  NTG_REQUIRE(pg.readout == 0 || pg.readout == 1, w + ": readout must be 0 or 1");
+  NTG_REQUIRE(n1 > 0 && n2 > 0 && r0 >= 0 && c0 >= 0 && ld_out >= n2, w + ": bad tile");
+  NTG_REQUIRE(n1 <= (1ll << 24) && n2 <= (1ll << 24), w + ": tile too large");
+  const int64_t total = sym ? n1 * (n1 + 1) / 2 : n1 * n2;
+  NTG_REQUIRE(total < (1ll << 31), w + ": too many pairs for one launch");
+  const unsigned grid = (unsigned)total;  // one CTA per pair
   size_t sm = chain_smem_bytes(pg);
   cudaStream_t s = as_stream(stream);
   cudaError_t e = cudaSuccess;
@@ -576,25 +619,42 @@ extern "C" int ntg_chain_fwd(void* stream, const ntg_chain_t* prog, const float*
       e = cudaFuncSetAttribute(chain_fwd_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sm);
       if (e == cudaSuccess)
-        chain_fwd_kernel<1><<<(unsigned)(n1 * n2), NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1,
-                                                                 var2, out_q, out_t, ld_out);
+        chain_fwd_kernel<1><<<grid, NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1, var2,
+                                                 out_q, out_t, ld_out, sym);
       break;
     case 2:
       e = cudaFuncSetAttribute(chain_fwd_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sm);
       if (e == cudaSuccess)
-        chain_fwd_kernel<2><<<(unsigned)(n1 * n2), NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1,
-                                                                 var2, out_q, out_t, ld_out);
+        chain_fwd_kernel<2><<<grid, NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1, var2,
+                                                 out_q, out_t, ld_out, sym);
       break;
     default:
       e = cudaFuncSetAttribute(chain_fwd_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)sm);
       if (e == cudaSuccess)
-        chain_fwd_kernel<3><<<(unsigned)(n1 * n2), NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1,
-                                                                 var2, out_q, out_t, ld_out);
+        chain_fwd_kernel<3><<<grid, NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1, var2,
+                                                 out_q, out_t, ld_out, sym);
       break;
   }
-  if (e != cudaSuccess) return fail(NTG_ERR_CUDA, std::string("ntg_chain_fwd: ") + cudaGetErrorString(e));
+  if (e != cudaSuccess) return fail(NTG_ERR_CUDA, w + ": " + cudaGetErrorString(e));
   note_launch();
-  return check_launch("ntg_chain_fwd");
+  return check_launch(who);
+}
+
+}  // namespace
+
+extern "C" int ntg_chain_fwd(void* stream, const ntg_chain_t* prog, const float* x1,
+                             const float* x2, int64_t r0, int64_t n1, int64_t c0, int64_t n2,
+                             const float* var1, const float* var2, float* out_q, float* out_t,
+                             int64_t ld_out) {
+  return launch_chain("ntg_chain_fwd", stream, prog, x1, x2, r0, n1, c0, n2, var1, var2, out_q,
+                      out_t, ld_out, 0);
+}
+
+extern "C" int ntg_chain_fwd_sym(void* stream, const ntg_chain_t* prog, const float* x,
+                                 int64_t r0, int64_t n, const float* var, float* out_q,
+                                 float* out_t, int64_t ld_out) {
+  return launch_chain("ntg_chain_fwd_sym", stream, prog, x, x, r0, n, r0, n, var, var, out_q,
+                      out_t, ld_out, 1);
 }

@@ -260,3 +260,19 @@ def test_myrtle5_mixed_vs_oracle(nt, cifar_like):
     got, want = both(nt, lambda m: myrtle(m, 5), x1, x2, get=('nngp', 'ntk'), precision='mixed')
     for g, w in zip(got, want):
         assert elem_rel_err(g, w) < 1e-4
+
+
+def test_symmetric_grid_is_mirrored_triangle(nt):
+    """kernel_fn(x, None) on the fused path evaluates the pairs i <= j once and mirrors
+    them: the result is exactly symmetric and matches kernel_fn(x, x) (every pair
+    evaluated) to float32 rounding."""
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((7, 32, 32, 3)).astype(np.float32)
+    s = nt.stax
+    _, _, kf = s.serial(*myrtle(s, 5))
+    sym = kf(x, None, ('nngp', 'ntk'))
+    full = kf(x, x.copy(), ('nngp', 'ntk'))
+    for a, b in zip(sym, full):
+        a, b = cpu(a), cpu(b)
+        assert np.array_equal(a, a.T)
+        assert rel_err(a, b) < 2e-6
