@@ -317,7 +317,7 @@ def stencil_roofline(torch, O, dev, pairs=256, reps=4):
             'achieved': round(gbs, 1), 'unit': 'GB/s'}
 
 
-def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=16, precision='fp32', reps=2):
+def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=64, precision='fp32', reps=2):
     """Kernel-ridge loss of the Myrtle-5 NTK, ||y_t - K_ts (K_ss + 1e-6 tr(K_ss)/n I)^-1 y_s||^2,
     and its gradient with respect to the support set x_s (forward through nt.batch's fused
     grid, backward through its checkpointed tiles and the hand-written adjoints; the solve
@@ -347,10 +347,12 @@ def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=16, precision='fp32', 
         grad = xs.grad
     ms = statistics.mean(ts)
     entries = n_s * n_s + n_t * n_s
+    tile = nt.tune.recompute_tile(kf, tuple(xs.shape), precision)
     return {'ms': round(ms, 2), 'entries': entries,
             'entries_per_s': round(entries / (ms / 1e3), 1), 'precision': precision,
+            'recompute_tile': min(tile, bs),
             'config': f'Myrtle-5 NTK kernel-ridge loss, d/dx_s; x_s [{n_s}], x_t [{n_t}], '
-                      f'nt.batch(batch_size={bs})'}, grad
+                      f'nt.batch(batch_size={bs}), autotuned recompute tile'}, grad
 
 
 def myrtle10(m):
@@ -562,13 +564,13 @@ def profile_stencil(pairs: int):
 
 
 def profile_fwd_bwd(n_s: int):
-    """The fwd+bwd measurement alone: x_s [n_s], x_t [2 n_s], tiles of 16 (launch lists)."""
+    """The fwd+bwd measurement alone: x_s [n_s], x_t [2 n_s], batch_size n_s (launch lists)."""
     import torch
     import nt_gb300 as nt
     from nt_gb300 import stax
     _, _, kf = stax.serial(*myrtle5(stax))
     x = torch.from_numpy(make_inputs(2000)).cuda()
-    r, _ = fwd_bwd_timing(torch, nt, kf, x, n_t=2 * n_s, n_s=n_s, bs=16, reps=1)
+    r, _ = fwd_bwd_timing(torch, nt, kf, x, n_t=2 * n_s, n_s=n_s, bs=n_s, reps=1)
     print(json.dumps({'profile_fwd_bwd': n_s, **r}))
 
 

@@ -10,6 +10,8 @@ chunks) and ``batch_size`` only bounds the per-sample working set.
 """
 from __future__ import annotations
 
+from typing import Optional
+
 import numpy as np
 import torch
 
@@ -110,11 +112,15 @@ def _forward_grid(kernel_fn, x1t, x2t, bs, precision):
     return _assemble(rows, ('nngp', 'ntk'), None)
 
 
-def batch(kernel_fn, batch_size: int = 0, device_count: int = -1, store_on_device: bool = True):
+def batch(kernel_fn, batch_size: int = 0, device_count: int = -1, store_on_device: bool = True,
+          recompute_tile: Optional[int] = None):
     """batching.py:76-132 (one device: serial tiling).
 
     With inputs that require grad, the returned nngp/ntk carry a checkpointed
-    backward (one tile of layer tensors recomputed at a time)."""
+    backward (one tile of layer tensors recomputed at a time). Its tile is
+    ``recompute_tile`` rows/columns when given, else the autotuned one
+    (``tune.recompute_tile``: the fastest probe within the memory budget), never
+    more than ``batch_size`` (not in the reference, whose backward is XLA's)."""
     if device_count not in (-1, 0, 1):
         raise NotImplementedError('nt_gb300 runs on one GPU; device_count must be -1, 0 or 1')
 
@@ -130,9 +136,13 @@ def batch(kernel_fn, batch_size: int = 0, device_count: int = -1, store_on_devic
                 x1t.requires_grad or (x2t is not None and x2t.requires_grad)):
             if names is None or not set(names) <= {'nngp', 'ntk'}:
                 raise NotImplementedError('differentiable batch() returns nngp and ntk')
+            tile = recompute_tile
+            if tile is None:
+                from . import tune
+                tile = tune.recompute_tile(kernel_fn, tuple(x1t.shape), precision)
             q, t = _CheckpointedKernel.apply(
                 x1t, x2t if x2t is not None else torch.empty(0, device=x1t.device), kernel_fn,
-                bs, precision)
+                max(1, min(bs, int(tile))), precision)
             vals = tuple(q if n == 'nngp' else t for n in names)
             return vals[0] if single is not None else analytic_kernel(names, vals)
         ds = kwargs.get('diagonal_spatial')

@@ -1,6 +1,8 @@
 """Gradients of kernel_fn (hand-written adjoints) against central finite
 differences of the float64 oracle (h = 1e-3), the check of the reference's own
 autodiff tests (tests/stax/elementwise_test.py:639-732, 782-934)."""
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -314,3 +316,29 @@ def test_kernel_ridge_solve_gradients(nt):
     for got, want in zip(leaves, leaves64):
         err = float((got.grad.double() - want.grad).abs().max() / want.grad.abs().max())
         assert err < 1e-4, err
+
+
+def test_autotuned_recompute_tile(nt, tmp_path, monkeypatch):
+    """tune.recompute_tile picks one of its candidates from timed probes, caches it,
+    and the batched backward with the tuned tile equals one with an explicit tile."""
+    import importlib
+    monkeypatch.setenv('NT_GB300_TUNE_CACHE', str(tmp_path / 'tune.json'))
+    tune = importlib.reload(nt.tune)
+    s = nt.stax
+    kf = s.serial(s.Conv(1, (3, 3), padding='SAME', W_std=1.4), s.Relu(),
+                  s.AvgPool((2, 2), (2, 2)), s.Conv(1, (3, 3), padding='SAME', W_std=1.4),
+                  s.Relu(), s.GlobalAvgPool(), s.Dense(1, 1.3, 0.))[2]
+    t = tune.recompute_tile(kf, (1, 8, 8, 3), 'fp32', candidates=(2, 4, 8))
+    assert t in (2, 4, 8)
+    assert os.path.exists(tmp_path / 'tune.json')
+    assert tune.recompute_tile(kf, (1, 8, 8, 3), 'fp32', candidates=(2, 4, 8)) == t
+    rng = np.random.default_rng(9)
+    xs = torch.tensor(rng.standard_normal((9, 8, 8, 3)), dtype=torch.float32, device='cuda')
+    xt = torch.tensor(rng.standard_normal((5, 8, 8, 3)), dtype=torch.float32, device='cuda')
+    grads = []
+    for tile in (None, 3):
+        a = xs.clone().requires_grad_(True)
+        nt.batch(kf, batch_size=8, recompute_tile=tile)(xt, a, 'ntk').sum().backward()
+        grads.append(a.grad)
+    torch.testing.assert_close(grads[0], grads[1], rtol=1e-4, atol=1e-6)
+    tune.clear()
