@@ -7,7 +7,7 @@ hand-written CUDA library libntgb300.so behind include/nt_gb300.h.
 from . import stax  # noqa: F401
 from . import predict  # noqa: F401
 from . import tune  # noqa: F401
-from .batching import batch  # noqa: F401
+from .batching import batch, CapturedBatch  # noqa: F401
 from .kernel import Kernel  # noqa: F401
 
 __version__ = '0.1.0'

@@ -203,8 +203,12 @@ def try_fused(kfn, x1: torch.Tensor, x2: Optional[torch.Tensor], diagonal_spatia
 
 
 def run_fused(plan: ChainPlan, x1: torch.Tensor, x2: Optional[torch.Tensor], ctx: _Ctx,
-              out: Optional[tuple] = None, rows=None, cols=None, selfs=None) -> Kernel:
-    """Readout Kernel of the chain for all pairs of x1 x x2 (x2 None: x1 x x1)."""
+              out: Optional[tuple] = None, rows=None, cols=None, selfs=None,
+              x1_is_x2: Optional[bool] = None) -> Kernel:
+    """Readout Kernel of the chain for all pairs of x1 x x2 (x2 None: x1 x x1).
+
+    ``x1_is_x2`` given skips the element-wise comparison of x1 and x2 (a host
+    synchronisation, not allowed while a CUDA graph is being captured)."""
     pg = _program(plan, x1.shape[-1], ctx)
     if selfs is None:
         var1, cov1 = self_chain(x1, plan, ctx)
@@ -228,6 +232,7 @@ def run_fused(plan: ChainPlan, x1: torch.Tensor, x2: Optional[torch.Tensor], ctx
     for s in plan.spatial:
         shape1, shape2 = s.shape_fn(shape1), s.shape_fn(shape2)
     return Kernel(nngp=out_q, ntk=out_t, cov1=cov1, cov2=cov2,
-                  x1_is_x2=x2 is None or bool(torch.equal(x1, x2)), is_gaussian=plan.is_gaussian,
+                  x1_is_x2=(x2 is None or bool(torch.equal(x1, x2))) if x1_is_x2 is None
+                  else bool(x1_is_x2), is_gaussian=plan.is_gaussian,
                   is_reversed=False, is_input=False, diagonal_batch=True, diagonal_spatial=False,
                   shape1=shape1, shape2=shape2)

@@ -215,3 +215,63 @@ def _assemble(rows, names, single):
         else:
             vals.append(grid[0][0])
     return analytic_kernel(names, tuple(vals))
+
+
+class CapturedBatch:
+    """``batch(kernel_fn, batch_size)(x1, x2, get)`` for fixed input shapes, captured
+    once as a CUDA graph and replayed: for serving, where the same shapes come back
+    and the host-side work of a call (per-sample chains, launches, allocations)
+    would otherwise be repeated. Only networks on the fused chain path (whose
+    forward has no host synchronisation) can be captured. A call copies the inputs
+    into the graph's static buffers, replays, and returns the graph's static
+    output tensors, which the next call overwrites (clone them to keep them).
+    Not in the reference (XLA compiles, it does not capture)."""
+
+    def __init__(self, kernel_fn, x1_shape, x2_shape=None, get=('nngp', 'ntk'),
+                 batch_size: int = 0, precision: str = 'fp32'):
+        from . import _lib as L
+        dev = L.require_cuda()
+        if not isinstance(kernel_fn, KernelFn):
+            raise TypeError('CapturedBatch needs a kernel_fn from nt_gb300.stax.serial')
+        self.names, self.single = _normalize_get(get)
+        if self.names is None or not set(self.names) <= {'nngp', 'ntk'}:
+            raise NotImplementedError('CapturedBatch returns nngp and/or ntk')
+        self.plan = _chain.plan_chain(kernel_fn.specs, tuple(x1_shape), False)
+        if self.plan is None or bool(kernel_fn.diagonal) or (
+                x2_shape is not None and tuple(x2_shape[1:]) != tuple(x1_shape[1:])):
+            raise NotImplementedError('CapturedBatch needs a network on the fused chain path')
+        self.kernel_fn, self.precision = kernel_fn, precision
+        self.bs = batch_size or max(x1_shape[0], (x2_shape or x1_shape)[0])
+        self.x1 = torch.zeros(tuple(x1_shape), device=dev)
+        self.x2 = None if x2_shape is None else torch.zeros(tuple(x2_shape), device=dev)
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(2):  # warm-up: library load, kernel attributes, allocator pools
+                self._run()
+        torch.cuda.current_stream().wait_stream(side)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph, capture_error_mode='thread_local'):
+            self.out = self._run()
+
+    def _run(self):
+        ctx = _Ctx(self.precision)
+        old = _chain.SELF_CHUNK
+        _chain.SELF_CHUNK = max(1, min(old, self.bs))
+        try:
+            k = _chain.run_fused(self.plan, self.x1, self.x2, ctx, x1_is_x2=self.x2 is None)
+        finally:
+            _chain.SELF_CHUNK = old
+        k = self.kernel_fn.apply_kernel(k, ctx, specs=self.plan.post)
+        return _select(k, self.names, self.single)
+
+    def __call__(self, x1, x2=None):
+        self.x1.copy_(_as_input(x1), non_blocking=True)
+        if self.x2 is not None:
+            if x2 is None:
+                raise ValueError('this capture was made with x2')
+            self.x2.copy_(_as_input(x2), non_blocking=True)
+        elif x2 is not None:
+            raise ValueError('this capture was made with x2=None')
+        self.graph.replay()
+        return self.out

@@ -276,3 +276,22 @@ def test_symmetric_grid_is_mirrored_triangle(nt):
         a, b = cpu(a), cpu(b)
         assert np.array_equal(a, a.T)
         assert rel_err(a, b) < 2e-6
+
+
+@pytest.mark.parametrize('with_x2', [True, False])
+def test_captured_batch_replays_eager_results(nt, with_x2):
+    """CapturedBatch: one CUDA-graph capture of the fused batch, replayed on new inputs,
+    gives the eager nt.batch results bit for bit."""
+    rng = np.random.default_rng(12)
+    s = nt.stax
+    _, _, kf = s.serial(*myrtle(s, 5))
+    shape1, shape2 = (6, 32, 32, 3), (5, 32, 32, 3)
+    cap = nt.CapturedBatch(kf, shape1, shape2 if with_x2 else None, ('nngp', 'ntk'),
+                           batch_size=4)
+    for seed in range(2):
+        x1 = torch.tensor(rng.standard_normal(shape1), dtype=torch.float32, device='cuda')
+        x2 = torch.tensor(rng.standard_normal(shape2), dtype=torch.float32, device='cuda')
+        got = cap(x1, x2 if with_x2 else None)
+        want = nt.batch(kf, batch_size=4)(x1, x2 if with_x2 else None, ('nngp', 'ntk'))
+        for g, w in zip(got, want):
+            assert torch.equal(g, w)
