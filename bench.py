@@ -4,10 +4,14 @@ Workload: the full-spatial Myrtle-5 kernel (notebook definition: Conv3x3+Relu
 x2, AvgPool, Conv+Relu, AvgPool, Conv+Relu, AvgPool x3, Flatten, Dense;
 W_std = sqrt(2), b_std = 0) over 2000 synthetic CIFAR-shaped inputs
 [2000, 32, 32, 3] (iid N(0, 1), standardised per channel, seed 0), computed as
-a 2000 x 2000 nngp+ntk kernel through nt.batch(batch_size=100). One step is
-one 100 x 100 tile of that grid (10,000 kernel entries, including the
-per-sample chains of the tile's 200 inputs). Steps walk the tile grid in
-row-major order; under torchrun rank r takes tiles r, r+N, ... (weak scaling).
+the 2000 x 2000 nngp+ntk kernel K(x, x) through nt.batch(batch_size=100).
+Because K(x, x) is symmetric, the job is the per-sample chains of the 2000
+inputs plus the upper triangle of the 20 x 20 tile grid: 20 diagonal tiles
+(pairs i <= j) and 190 off-diagonal tiles whose results are also written at
+the mirrored position, 210 tiles in all. Step k is tile k of the triangle plus
+1/210 of the per-sample chains; each step is credited 2000^2 / 210 entries, so
+`value` is the throughput of the whole job. Steps are spread evenly over the
+triangle; under torchrun rank r takes tiles r, r+N, ... (weak scaling).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -137,19 +141,47 @@ def run_gpu(args):
     _, _, kf = stax.serial(*myrtle5(stax))
     plan = _chain.plan_chain(kf.specs, tuple(xd.shape), False)
     assert plan is not None, 'Myrtle-5 must take the fused chain path'
-    from nt_gb300.batching import rank_tiles, tile_grid
-    grid = [(r0 // TILE, c0 // TILE) for r0, _, c0, _ in tile_grid(N_SAMPLES, N_SAMPLES, TILE)]
-    mine = rank_tiles(grid, ws, rank, args.warmup + args.steps)
+    from nt_gb300 import _ops as O
+    from nt_gb300.kernel import Kernel
+    # The job is K(x, x) over the 2000 inputs, as nt.batch(kf, 100)(x, None) computes it: the
+    # per-sample chains of the 2000 inputs and the upper triangle of the 20 x 20 tile grid
+    # (20 diagonal tiles with only i <= j evaluated, 190 off-diagonal tiles written at (i, j)
+    # and (j, i)). Step k is tile k of the triangle plus the per-sample chains of samples
+    # [k N / 210, (k + 1) N / 210): the 210 steps are the whole job, each credited N^2 / 210
+    # entries. Steps are spread evenly over a rank's share of the tiles (tile k -> rank k % N).
+    nt_ = N_SAMPLES // TILE
+    tiles = [(r, c) for r in range(nt_) for c in range(r, nt_)]
+    njob = len(tiles)
+    slices = [(k * N_SAMPLES // njob, (k + 1) * N_SAMPLES // njob) for k in range(njob)]
+    mine_all = list(range(rank, njob, ws))
+    total_steps = args.warmup + args.steps
+    mine = [mine_all[(s * len(mine_all)) // total_steps % len(mine_all)] for s in range(total_steps)]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
-    out_q = torch.empty((TILE, TILE), device=dev)
-    out_t = torch.empty((TILE, TILE), device=dev)
+    ctx32 = _Ctx('fp32')
+    var_all, cov_all = _chain.self_chain(xd, plan, ctx32)
+    out_q = torch.empty((N_SAMPLES, N_SAMPLES), device=dev)
+    out_t = torch.empty((N_SAMPLES, N_SAMPLES), device=dev)
+    shape_out = tuple(xd.shape)
+    for sp in plan.spatial:
+        shape_out = sp.shape_fn(shape_out)
 
-    def step(rc, precision='fp32'):
-        r, c = rc
+    def step(k, precision='fp32'):
         ctx = _Ctx(precision)
-        k = _chain.run_fused(plan, xd[r * TILE:(r + 1) * TILE], xd[c * TILE:(c + 1) * TILE], ctx,
-                             out=(out_q, out_t))
-        kf.apply_kernel(k, ctx, specs=plan.post)
+        a, b = slices[k]
+        v, cr = _chain.self_chain(xd[a:b], plan, ctx)
+        var_all[a:b].copy_(v)
+        cov_all[a:b].copy_(cr)
+        r, c = tiles[k]
+        pg = _chain._program(plan, 3, ctx)
+        O.chain_fwd_sym(pg, xd, r * TILE, TILE, c * TILE, TILE, var_all, out_q, out_t, N_SAMPLES)
+        # the layers after the readout (Dense) on the tile
+        rs, cs = slice(r * TILE, (r + 1) * TILE), slice(c * TILE, (c + 1) * TILE)
+        kt = Kernel(nngp=out_q[rs, cs].contiguous(), ntk=out_t[rs, cs].contiguous(),
+                    cov1=cov_all[rs], cov2=cov_all[cs], x1_is_x2=False,
+                    is_gaussian=plan.is_gaussian, is_reversed=False, is_input=False,
+                    diagonal_batch=True, diagonal_spatial=False, shape1=shape_out,
+                    shape2=shape_out)
+        kf.apply_kernel(kt, ctx, specs=plan.post)
 
     stream = torch.cuda.current_stream()
     for s in range(args.warmup):
@@ -176,22 +208,19 @@ def run_gpu(args):
     if ws > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     ms_max = float(t.item())
-    entries = TILE * TILE * args.steps * ws
+    per_step = N_SAMPLES * N_SAMPLES / njob
+    entries = per_step * args.steps * ws
     value = entries / (ms_max / 1e3)
 
-    # Dominant kernel alone: the fused chain launch of one tile, CUDA events on
-    # the launching stream, L2 flushed before each launch.
+    # Dominant kernel alone: the fused chain launch of one off-diagonal tile (10 000 pairs
+    # evaluated), CUDA events on the launching stream, L2 flushed before each launch.
     pg = _chain._program(plan, 3, _Ctx('fp32'))
-    xa, xb = xd[:TILE], xd[TILE:2 * TILE]
-    var1, _ = _chain.self_chain(xa, plan, _Ctx('fp32'))
-    var2, _ = _chain.self_chain(xb, plan, _Ctx('fp32'))
-    from nt_gb300 import _ops as O
     kt = []
     for i in range(4):
         flush_l2(flush)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        O.chain_fwd(pg, xa, xb, 0, TILE, 0, TILE, var1, var2, out_q, out_t, TILE)
+        O.chain_fwd_sym(pg, xd, 0, TILE, TILE, TILE, var_all, out_q, out_t, N_SAMPLES)
         b.record(stream)
         torch.cuda.synchronize()
         if i:
@@ -223,24 +252,20 @@ def run_gpu(args):
         b.record(stream)
         torch.cuda.synchronize()
         em.append(a.elapsed_time(b))
-    mixed_value = TILE * TILE / (statistics.mean(em) / 1e3)
+    mixed_value = per_step / (statistics.mean(em) / 1e3)
 
-    # End to end through the public API: pinned host inputs, results read back.
+    # End to end through the public API: the whole job nt.batch(kf, 100)(x, None) from pinned
+    # host inputs, nngp and ntk read back to the host.
     xh = torch.from_numpy(x).pin_memory()
     batched = nt.batch(kf, batch_size=TILE)
-    e2e_times = []
-    for s in range(args.steps):
-        r, c = mine[args.warmup + s]
-        h1 = xh[r * TILE:(r + 1) * TILE]
-        h2 = xh[c * TILE:(c + 1) * TILE]
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        res = batched(h1, h2, ('nngp', 'ntk'))
-        q, tt = res.nngp.cpu(), res.ntk.cpu()
-        e2e_times.append(time.perf_counter() - t0)
-    e2e_value = TILE * TILE / statistics.mean(e2e_times)
-    h2d = 2 * TILE * int(np.prod(IMG)) * 4
-    d2h = 2 * TILE * TILE * 4
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = batched(xh, None, ('nngp', 'ntk'))
+    q, tt = res.nngp.cpu(), res.ntk.cpu()
+    e2e_s = time.perf_counter() - t0
+    e2e_value = N_SAMPLES * N_SAMPLES / e2e_s
+    h2d = N_SAMPLES * int(np.prod(IMG)) * 4
+    d2h = 2 * N_SAMPLES * N_SAMPLES * 4
 
     peaks = {}
     try:
@@ -256,15 +281,20 @@ def run_gpu(args):
         'warmup': args.warmup, 'ms_per_step': round(ms_max / args.steps, 3),
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
         'data': 'synthetic: iid N(0,1) [2000,32,32,3], standardised per channel, seed 0',
-        'config': {'workload': 'Myrtle-5 full-spatial nngp+ntk, 2000x2000 via '
-                               'nt.batch(batch_size=100); step = one 100x100 tile',
+        'config': {'workload': 'Myrtle-5 full-spatial nngp+ntk K(x, x), x [2000, 32, 32, 3], '
+                               'nt.batch(batch_size=100); the job is the per-sample chains and '
+                               'the upper triangle of the 20x20 tile grid (210 tiles, '
+                               'off-diagonal tiles mirrored); step = one tile of the triangle '
+                               'plus 1/210 of the per-sample chains, credited 2000^2/210 entries',
                    'n_samples': N_SAMPLES, 'batch_size': TILE, 'input': list(IMG),
                    'precision': 'fp32 (plain)', 'l2': 'flushed before every step (256 MiB write)',
-                   'path': 'fused chain kernel (ntg_chain_fwd) + per-sample chains'},
+                   'path': 'fused chain kernel (ntg_chain_fwd_sym) + per-sample chains'},
         'mixed': {'value': round(mixed_value, 1), 'unit': 'entries/s',
                   'precision': 'compensated var1*var2 - q^2'},
         'e2e': {'value': round(e2e_value, 1), 'unit': 'entries/s', 'h2d_bytes_per_step': h2d,
-                'd2h_bytes_per_step': d2h, 'api': 'nt.batch(kernel_fn, 100)(x1, x2, get)'},
+                'd2h_bytes_per_step': d2h, 'api': 'nt.batch(kernel_fn, 100)(x, None, get)',
+                'note': 'one call of the whole 2000x2000 job from pinned host memory, '
+                        f'{e2e_s:.2f} s; bytes are per job'},
         'roofline': {'bound': 'hbm', 'achieved': round(achieved_gbs, 1), 'peak': hbm_peak,
                      'unit': 'GB/s', 'frac': round(achieved_gbs / hbm_peak, 3), 'traffic': None,
                      'kernel': 'chain_fwd_kernel', 'kernel_ms': round(chain_ms, 3),

@@ -207,13 +207,16 @@ typedef struct {
 int ntg_chain_fwd(void* stream, const ntg_chain_t* prog, const float* x1, const float* x2,
                   int64_t r0, int64_t n1, int64_t c0, int64_t n2, const float* var1,
                   const float* var2, float* out_nngp, float* out_ntk, int64_t ld_out);
-/* The same network on the square tile of x rows [r0, r0 + n) with themselves
- * (kernel_fn(x, None)): only the pairs i <= j are evaluated, each result is
- * written at (i, j) and (j, i) of out [n, ld_out] — half the work of
- * ntg_chain_fwd(x, x), and an exactly symmetric output. No counterpart in the
+/* The same network for K(x, x), whose pairs (i, j) and (j, i) are equal: the
+ * pairs (i, j) of x with itself for i in [r0, r0 + n1), j in [c0, c0 + n2) — a
+ * diagonal tile (r0 == c0, n1 == n2: only i <= j evaluated) or a tile whose row
+ * and column ranges are disjoint — each result written at (i, j) and (j, i) of
+ * out, the whole kernel [., ld_out] (element (0, 0) at out). Half the work of
+ * evaluating every pair, and an exactly symmetric output. No counterpart in the
  * reference, which evaluates every pair. */
 int ntg_chain_fwd_sym(void* stream, const ntg_chain_t* prog, const float* x, int64_t r0,
-                      int64_t n, const float* var, float* out_q, float* out_t, int64_t ld_out);
+                      int64_t n1, int64_t c0, int64_t n2, const float* var, float* out_q,
+                      float* out_t, int64_t ld_out);
 
 /* ---- kernel regression (predict.gradient_descent_mse, t = None) -------- */
 /* Factor A = K + lambda I = L L^T in FP32 (predict.py:1224-1258 with

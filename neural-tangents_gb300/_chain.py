@@ -224,7 +224,7 @@ def run_fused(plan: ChainPlan, x1: torch.Tensor, x2: Optional[torch.Tensor], ctx
         out_q, out_t = out
     if x2 is None:
         # K(x, x): the pairs i <= j once, mirrored (one launch over the triangle)
-        O.chain_fwd_sym(pg, x1, 0, n1, var1, out_q, out_t, n2)
+        O.chain_fwd_sym(pg, x1, 0, n1, 0, n1, var1, out_q, out_t, n2)
     else:
         O.chain_fwd(pg, x1, xb, 0, n1, 0, n2, var1, var2, out_q, out_t, n2)
     shape1 = tuple(x1.shape)

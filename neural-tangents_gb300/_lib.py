@@ -77,7 +77,8 @@ SIGNATURES = {
     'ntg_flatten_fs': ([_P, _P, _P, _I64, _I64, _I64], C.c_int),
     'ntg_chain_fwd': ([_P, C.POINTER(Chain), _P, _P, _I64, _I64, _I64, _I64, _P, _P, _P, _P,
                        _I64], C.c_int),
-    'ntg_chain_fwd_sym': ([_P, C.POINTER(Chain), _P, _I64, _I64, _P, _P, _P, _I64], C.c_int),
+    'ntg_chain_fwd_sym': ([_P, C.POINTER(Chain), _P, _I64, _I64, _I64, _I64, _P, _P, _P, _I64],
+                          C.c_int),
     'ntg_act_bwd': ([_P, _P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, _I32, Act, Var, Var, _P,
                      _P], C.c_int),
     'ntg_affine_bwd': ([_P, _P, _P, _P, _P, _I64, Affine, _F], C.c_int),

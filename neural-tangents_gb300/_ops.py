@@ -174,8 +174,10 @@ def chain_fwd(prog: L.Chain, x1, x2, r0, n1, c0, n2, var1, var2, out_q, out_t, l
            ld_out)
 
 
-def chain_fwd_sym(prog: L.Chain, x, r0, n, var, out_q, out_t, ld_out):
-    """Upper triangle of the tile of x rows [r0, r0 + n) with themselves, mirrored."""
+def chain_fwd_sym(prog: L.Chain, x, r0, n1, c0, n2, var, out_q, out_t, ld_out):
+    """Pairs (r0.., c0..) of x with itself, each written at (i, j) and (j, i) of the
+    whole kernel out [., ld_out]; the tile is diagonal (only i <= j evaluated) or
+    has disjoint row and column ranges."""
     import ctypes
-    L.call('ntg_chain_fwd_sym', L.stream(), ctypes.byref(prog), L.ptr(x), r0, n, L.ptr(var),
-           out_q.data_ptr(), None if out_t is None else out_t.data_ptr(), ld_out)
+    L.call('ntg_chain_fwd_sym', L.stream(), ctypes.byref(prog), L.ptr(x), r0, n1, c0, n2,
+           L.ptr(var), out_q.data_ptr(), None if out_t is None else out_t.data_ptr(), ld_out)

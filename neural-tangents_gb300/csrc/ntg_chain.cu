@@ -547,9 +547,12 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
   }
 }
 
-// One CTA per pair of the tile, or (sym != 0) per pair i <= j of the upper
-// triangle of a square tile of x1 with itself, the result written at (i, j) and
-// (j, i); per pair the CTA runs the whole network.
+// One CTA per pair. sym == 0: the pairs (r0 + i, c0 + j) of x1 x x2, result at
+// out[i * ld + j] (out points at the tile). sym == 1: the pairs i <= j of the
+// square tile of x1 with itself (r0 == c0, n1 == n2); sym == 2: all pairs of a
+// tile of x1 with itself whose row and column ranges are disjoint. For sym != 0
+// out points at element (0, 0) of the whole kernel and each result is written at
+// (gi, gj) and (gj, gi).
 template <int N0>
 __global__ void __launch_bounds__(NT, 1)
     chain_fwd_kernel(const __grid_constant__ ntg_chain_t pg, const float* __restrict__ x1,
@@ -559,14 +562,18 @@ __global__ void __launch_bounds__(NT, 1)
                      int sym) {
   const int64_t pair = blockIdx.x;
   int64_t i, j;
-  if (sym) {
+  if (sym == 1) {
     tri_pair(pair, n1, i, j);
   } else {
     i = pair / n2;
     j = pair - i * n2;
   }
-  chain_pair<N0>(pg, x1, x2, r0 + i, c0 + j, var1, var2, out_q, out_t, i * ld_out + j,
-                 sym && i != j ? j * ld_out + i : -1);
+  const int64_t gi = r0 + i, gj = c0 + j;
+  if (sym == 0)
+    chain_pair<N0>(pg, x1, x2, gi, gj, var1, var2, out_q, out_t, i * ld_out + j, -1);
+  else
+    chain_pair<N0>(pg, x1, x2, gi, gj, var1, var2, out_q, out_t, gi * ld_out + gj,
+                   gi != gj ? gj * ld_out + gi : -1);
 }
 
 size_t chain_smem_bytes(const ntg_chain_t& pg) {
@@ -606,9 +613,11 @@ int launch_chain(const char* who, void* stream, const ntg_chain_t* prog, const f
   }
   NTG_REQUIRE(nl <= NTG_CHAIN_MAX_LAYERS, w + ": too many layers");
   NTG_REQUIRE(pg.readout == 0 || pg.readout == 1, w + ": readout must be 0 or 1");
-  NTG_REQUIRE(n1 > 0 && n2 > 0 && r0 >= 0 && c0 >= 0 && ld_out >= n2, w + ": bad tile");
+  NTG_REQUIRE(n1 > 0 && n2 > 0 && r0 >= 0 && c0 >= 0, w + ": bad tile");
+  NTG_REQUIRE(sym ? ld_out >= (r0 + n1 > c0 + n2 ? r0 + n1 : c0 + n2) : ld_out >= n2,
+              w + ": ld_out smaller than the kernel");
   NTG_REQUIRE(n1 <= (1ll << 24) && n2 <= (1ll << 24), w + ": tile too large");
-  const int64_t total = sym ? n1 * (n1 + 1) / 2 : n1 * n2;
+  const int64_t total = sym == 1 ? n1 * (n1 + 1) / 2 : n1 * n2;
   NTG_REQUIRE(total < (1ll << 31), w + ": too many pairs for one launch");
   const unsigned grid = (unsigned)total;  // one CTA per pair
   size_t sm = chain_smem_bytes(pg);
@@ -653,8 +662,17 @@ extern "C" int ntg_chain_fwd(void* stream, const ntg_chain_t* prog, const float*
 }
 
 extern "C" int ntg_chain_fwd_sym(void* stream, const ntg_chain_t* prog, const float* x,
-                                 int64_t r0, int64_t n, const float* var, float* out_q,
-                                 float* out_t, int64_t ld_out) {
-  return launch_chain("ntg_chain_fwd_sym", stream, prog, x, x, r0, n, r0, n, var, var, out_q,
-                      out_t, ld_out, 1);
+                                 int64_t r0, int64_t n1, int64_t c0, int64_t n2, const float* var,
+                                 float* out_q, float* out_t, int64_t ld_out) {
+  int sym;
+  if (r0 == c0 && n1 == n2) {
+    sym = 1;
+  } else if (r0 + n1 <= c0 || c0 + n2 <= r0) {
+    sym = 2;
+  } else {
+    return fail(NTG_ERR_INVALID_ARG,
+                "ntg_chain_fwd_sym: the row and column ranges must be equal or disjoint");
+  }
+  return launch_chain("ntg_chain_fwd_sym", stream, prog, x, x, r0, n1, c0, n2, var, var, out_q,
+                      out_t, ld_out, sym);
 }
