@@ -1,5 +1,8 @@
 """nt_gb300.predict -- closed-form kernel regression (neural_tangents/_src/predict.py).
 
+``gp_inference`` and ``gradient_descent_mse_ensemble`` (predict.py:566-1005) give the
+NNGP / NTK / NTKGP posterior and the infinite-ensemble predictions on the same kernels.
+
 ``gradient_descent_mse(k_train_train, y_train, ...)`` keeps the reference
 signature (predict.py:71-278) and returns ``predict_fn(t=None, fx_train_0=0.,
 fx_test_0=None, k_test_train=None)``. ``t=None`` (infinite time) is the
@@ -13,6 +16,7 @@ is supported.
 """
 from __future__ import annotations
 
+import collections
 import math
 import warnings
 from typing import Optional
@@ -278,3 +282,224 @@ class _MatMul(torch.autograd.Function):
 def matmul(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     """Differentiable a @ b for float32 CUDA matrices on the library's GEMM kernels."""
     return _MatMul.apply(a, b)
+
+
+# ---------------------------------------------------------------------------
+# Posterior of the NNGP / NTK / NTKGP and the infinite ensemble
+# (predict.py:566-745, 753-1005)
+# ---------------------------------------------------------------------------
+
+Gaussian = collections.namedtuple('Gaussian', 'mean covariance')
+
+
+def _kattr(k, g):
+    """A field of a kernel container (Kernel, AnalyticKernel, dict) or the array itself."""
+    if isinstance(k, dict):
+        return k[g]
+    if hasattr(k, g):
+        return getattr(k, g)
+    return k
+
+
+def _has(k, g) -> bool:
+    return (g in k) if isinstance(k, dict) else hasattr(k, g)
+
+
+def _names(get):
+    if get is None:
+        return ('nngp', 'ntk')
+    if isinstance(get, str):
+        return (get.lower(),)
+    return tuple(g.lower() for g in get)
+
+
+def _gaussians(get, names, out):
+    if isinstance(get, str):
+        return out[names[0]]
+    return collections.namedtuple('Gaussians', names)(*[out[g] for g in names])
+
+
+def gp_inference(k_train_train, y_train, diag_reg: float = 0.,
+                 diag_reg_absolute_scale: bool = False, trace_axes=(-1,), refine_iters: int = 2):
+    """predict.py:566-745: ``predict_fn(get, k_test_train, k_test_test)`` with the
+    NNGP / NTK / NTKGP posterior mean and, given ``k_test_test``, covariance.
+
+    Every solve runs on this module's Cholesky kernels (FP32 factorisation cached per
+    kernel, blocked triangular solves with FP64 refinement) and every product on its
+    GEMM kernel; 2-D kernels with ``trace_axes=(-1,)``."""
+    if tuple(trace_axes) not in ((-1,), (1,)):
+        raise NotImplementedError('nt_gb300 supports trace_axes=(-1,)')
+    y = _dev(y_train)
+    solvers = {}
+
+    def solve(g: str):
+        if g not in solvers:
+            solvers[g] = CholeskySolver(_dev(_kattr(k_train_train, g)), diag_reg,
+                                        diag_reg_absolute_scale, refine_iters)
+        return solvers[g]
+
+    k_inv_y = {}
+
+    def predict_fn(get=None, k_test_train=None, k_test_test=None):
+        names = _names(get)
+        out = {}
+        for g in names:
+            k = 'ntk' if g == 'ntkgp' else g
+            k_dd = _dev(_kattr(k_train_train, k))
+            k_td = None if k_test_train is None else _dev(_kattr(k_test_train, k))
+            if k_td is None:
+                mean = y
+            else:
+                if k not in k_inv_y:
+                    k_inv_y[k] = solve(k).solve(y, residual=False)
+                mean = _gemm(k_td, k_inv_y[k].reshape(y.shape[0], -1)).reshape(
+                    (k_td.shape[0],) + tuple(y.shape[1:]))
+            if k_test_test is None:
+                out[g] = mean
+                continue
+            if k_td is None:
+                out[g] = Gaussian(mean, torch.zeros_like(k_dd))
+                continue
+            if g == 'ntk' and (not _has(k_train_train, 'nngp') or not _has(k_test_train, 'nngp')):
+                raise ValueError(
+                    'If `"ntk" in get`, and `k_test_test is not None`, and `k_test_train is not '
+                    'None`, i.e. you request the NTK posterior covariance on the test set, you '
+                    'need both NTK and NNGP train-train and test-train matrices contained in '
+                    '`k_test_train` and `k_train_train`. Hence they must be `namedtuple`s with '
+                    '`nngp` and `ntk` attributes.')
+            g_init = 'nngp' if g != 'ntkgp' else 'ntk'
+            k_td_g_inv_y = solve(k).solve(_dev(_kattr(k_test_train, g_init)).t().contiguous(),
+                                          residual=False)
+            k_tt = _dev(_kattr(k_test_test, g_init))
+            if g in ('nngp', 'ntkgp'):
+                cov = k_tt - _gemm(k_td, k_td_g_inv_y)
+            elif g == 'ntk':
+                term_1 = solve(g).solve(k_td.t().contiguous(), residual=False)
+                nngp_dd = _dev(_kattr(k_train_train, 'nngp'))
+                cov = _gemm(term_1.t().contiguous(), _gemm(nngp_dd, term_1))
+                term_2 = _gemm(k_td, k_td_g_inv_y)
+                cov = cov - (term_2 + term_2.t()) + k_tt
+            else:
+                raise ValueError(g)
+            out[g] = Gaussian(mean, cov)
+        return _gaussians(get, names, out)
+
+    return predict_fn
+
+
+def _dependency(names, compute_cov):
+    """predict.py _get_dependency."""
+    for g in names:
+        if g not in ('nngp', 'ntk'):
+            raise NotImplementedError(
+                'Can only get either "nngp" or "ntk" predictions, got %s.' % g)
+    dep = ()
+    if 'nngp' in names or ('ntk' in names and compute_cov):
+        dep += ('nngp',)
+    if 'ntk' in names:
+        dep += ('ntk',)
+    return dep
+
+
+def gradient_descent_mse_ensemble(kernel_fn, x_train, y_train, learning_rate: float = 1.,
+                                  diag_reg: float = 0., diag_reg_absolute_scale: bool = False,
+                                  trace_axes=(-1,), **kernel_fn_train_train_kwargs):
+    """predict.py:753-1005: ``predict_fn(t=None, x_test=None, get=None, compute_cov=False)``,
+    the mean (and covariance) of the infinite ensemble of infinite-width networks
+    trained by gradient flow on the MSE loss. ``t=None`` is the Cholesky path of
+    ``gp_inference`` (this library's kernels); finite ``t`` uses the eigendecomposition of
+    the regularised train-train kernel (``torch.linalg.eigh`` in FP64) and the expm1
+    spectral functions of predict.py:1277-1294, contracted in FP64."""
+    if tuple(trace_axes) not in ((-1,), (1,)):
+        raise NotImplementedError('nt_gb300 supports trace_axes=(-1,)')
+    y = _dev(y_train)
+    k_dd = {}
+
+    def k_train(dep):
+        missing = tuple(g for g in dep if g not in k_dd)
+        if len(missing) == 1:
+            k_dd[missing[0]] = _dev(kernel_fn(x_train, None, missing[0],
+                                              **kernel_fn_train_train_kwargs))
+        elif missing:
+            k = kernel_fn(x_train, None, missing, **kernel_fn_train_train_kwargs)
+            for g in missing:
+                k_dd[g] = _dev(getattr(k, g))
+        return {g: k_dd[g] for g in dep}
+
+    eig = {}
+
+    def eigenspace(g):
+        if g not in eig:
+            a = k_train((g,))[g].double()
+            n = a.shape[0]
+            reg = diag_reg if diag_reg_absolute_scale else diag_reg * torch.trace(a) / n
+            eig[g] = torch.linalg.eigh(a + reg * torch.eye(n, device=a.device, dtype=a.dtype))
+        return eig[g]
+
+    inf_cache = {}
+
+    def predict_fn(t=None, x_test=None, get=None, compute_cov: bool = False,
+                   **kernel_fn_test_test_kwargs):
+        names = _names(get)
+        dep = _dependency(names, compute_cov)
+        kd = k_train(dep)
+        kw_tt = {**kernel_fn_train_train_kwargs, **kernel_fn_test_test_kwargs}
+        if x_test is None:
+            k_td = None
+            nngp_tt = True if compute_cov else None
+        else:
+            k = kernel_fn(x_test, x_train, dep if len(dep) > 1 else dep[0], **kw_tt)
+            k_td = {g: _dev(getattr(k, g) if len(dep) > 1 else k) for g in dep}
+            nngp_tt = _dev(kernel_fn(x_test, None, 'nngp', **kw_tt)) if compute_cov else None
+        if t is None:
+            if dep not in inf_cache:
+                inf_cache[dep] = gp_inference(kd, y, diag_reg, diag_reg_absolute_scale)
+            return inf_cache[dep](get=get, k_test_train=k_td, k_test_test=nngp_tt)
+        tt = torch.as_tensor(np.asarray(t, np.float64), device=y.device) * learning_rate
+        t_shape = tuple(tt.shape)
+        tf = tt.reshape(-1, 1)
+        y64 = y.double()
+        norm = y.numel()
+        out = {}
+        for g in names:
+            evals, evecs = eigenspace(g)
+            ev = evals[None, :]
+            pos = torch.clamp(ev, min=0.)
+            neg_expm1 = -torch.expm1(-pos * tf / norm)
+            neg_inv = neg_expm1 / torch.abs(ev)
+            proj = evecs.t() @ y64                                   # [i, m]
+            if k_td is None:
+                mean = torch.einsum('ji,ti,im->tjm', evecs, neg_expm1, proj)
+            else:
+                ktd = k_td[g].double()
+                mean = torch.einsum('lj,ji,ti,im->tlm', ktd, evecs, neg_inv, proj)
+            mean = mean.reshape(t_shape + tuple(mean.shape[1:])).float()
+            if nngp_tt is None:
+                out[g] = mean
+                continue
+            nngp_dd = kd['nngp'].double()
+            if k_td is None:
+                if g == 'nngp':
+                    cov = torch.einsum('ji,ti,ki->tjk', evecs,
+                                       pos * torch.exp(-2 * pos * tf / norm), evecs)
+                else:
+                    ex = torch.einsum('mi,ti,ki->tmk', evecs, torch.exp(-pos * tf / norm), evecs)
+                    cov = torch.einsum('tmk,kl,tnl->tmn', ex, nngp_dd, ex)
+            else:
+                tt_k = nngp_tt.double()[None]
+                if g == 'nngp':
+                    neg_inv2 = -torch.expm1(-pos * 2 * tf / norm) / torch.abs(ev)
+                    a = ktd @ evecs                                    # [m, i]
+                    cov = tt_k - torch.einsum('mi,ti,li->tml', a, neg_inv2, a)
+                else:
+                    b = evecs.t() @ ktd.t()                            # [i, l]
+                    term_1 = torch.einsum('mi,ti,il->tml', evecs, neg_inv, b)
+                    c = evecs.t() @ k_td['nngp'].double().t()         # [i, l]
+                    term_2 = torch.einsum('mi,ti,il->tml', ktd @ evecs, neg_inv, c)
+                    term_2 = term_2 + term_2.transpose(1, 2)
+                    cov = torch.einsum('tji,jk,tkl->til', term_1, nngp_dd, term_1) - term_2 + tt_k
+            cov = cov.reshape(t_shape + tuple(cov.shape[1:])).float()
+            out[g] = Gaussian(mean, cov)
+        return _gaussians(get, names, out)
+
+    return predict_fn

@@ -20,7 +20,8 @@ What it restates (paths are inside the neural-tangents 0.6.6 project):
   ``:1250-1310`` ``_elementwise`` / ``_sqrt`` / ``_arctan2``.
 * ``neural_tangents/_src/utils/kernel.py:426-441`` Kernel scalar algebra.
 * ``neural_tangents/_src/predict.py:71-278`` ``gradient_descent_mse``,
-  ``:1180-1258`` eigen / Cholesky helpers.
+  ``:566-745`` ``gp_inference``, ``:753-1005`` ``gradient_descent_mse_ensemble``,
+  ``:1180-1294`` eigen / Cholesky / expm1 helpers.
 
 Parity pinning. The reference ships no stored golden vectors and cannot be
 imported in this environment (it needs jax/jaxlib). This restatement is pinned
@@ -38,6 +39,7 @@ under ``tests/golden/`` are outputs of this restatement, regenerated by
 """
 from __future__ import annotations
 
+import collections
 import dataclasses
 import enum
 import math
@@ -783,5 +785,180 @@ def gradient_descent_mse(k_train_train, y_train, learning_rate=1., diag_reg=0.,
         if out_train is not None and out_test is not None:
             return out_train, out_test
         return out_test if out_train is None else out_train
+
+    return predict_fn
+
+
+# ---------------------------------------------------------------------------
+# Gaussian-process inference and the infinite ensemble (predict.py:566-1005)
+# ---------------------------------------------------------------------------
+Gaussian = collections.namedtuple('Gaussian', 'mean covariance')
+
+
+def _kattr(k, g):
+    """predict.py _get_attr: a field of a kernel container, or the array itself."""
+    if isinstance(k, dict):
+        return k[g]
+    if hasattr(k, g):
+        return getattr(k, g)
+    return k
+
+
+def _has(k, g) -> bool:
+    return (g in k) if isinstance(k, dict) else hasattr(k, g)
+
+
+def _canonical_get(get):
+    if get is None:
+        return None, ('nngp', 'ntk')
+    if isinstance(get, str):
+        return get, (get,)
+    return None, tuple(get)
+
+
+def _as_gaussians(get, names, out):
+    """utils.get_namedtuple('Gaussians'): one value for a string `get`, else a
+    namedtuple of the requested fields in order."""
+    if isinstance(get, str):
+        return out[get]
+    return collections.namedtuple('Gaussians', names)(*[out[g] for g in names])
+
+
+def gp_inference(k_train_train, y_train, diag_reg=0., diag_reg_absolute_scale=False):
+    """predict.py:566-745 with trace_axes=(-1,) and 2-D kernels: the NNGP / NTK /
+    NTKGP posterior mean and, given k_test_test, covariance."""
+    import scipy.linalg as sla
+    y = np.asarray(y_train, np.float64)
+    factors = {}
+
+    def solve(g):
+        if g not in factors:
+            a = _add_diagonal_regularizer(np.asarray(_kattr(k_train_train, g), np.float64),
+                                          diag_reg, diag_reg_absolute_scale)
+            factors[g] = sla.cho_factor(a, lower=False)
+        return lambda b: sla.cho_solve(factors[g], b)
+
+    def predict_fn(get=None, k_test_train=None, k_test_test=None):
+        _, names = _canonical_get(get)
+        out = {}
+        for g in names:
+            k = 'ntk' if g == 'ntkgp' else g
+            k_dd = np.asarray(_kattr(k_train_train, k), np.float64)
+            k_td = None if k_test_train is None else np.asarray(_kattr(k_test_train, k),
+                                                                  np.float64)
+            mean = y if k_td is None else k_td @ solve(k)(y)
+            if k_test_test is None:
+                out[g] = mean
+                continue
+            if k_td is None:
+                out[g] = Gaussian(mean, np.zeros_like(k_dd))
+                continue
+            if g == 'ntk' and (not _has(k_train_train, 'nngp') or
+                               not _has(k_test_train, 'nngp')):
+                raise ValueError('the NTK posterior covariance needs the NNGP kernels too')
+            g_init = 'nngp' if g != 'ntkgp' else 'ntk'
+            k_td_g_inv_y = solve(k)(np.asarray(_kattr(k_test_train, g_init), np.float64).T)
+            k_tt = np.asarray(_kattr(k_test_test, g_init), np.float64)
+            if g in ('nngp', 'ntkgp'):
+                cov = k_tt - k_td @ k_td_g_inv_y
+            else:
+                term_1 = solve(g)(k_td.T)
+                nngp_dd = np.asarray(_kattr(k_train_train, 'nngp'), np.float64)
+                cov = term_1.T @ (nngp_dd @ term_1)
+                term_2 = k_td @ k_td_g_inv_y
+                cov = cov - (term_2 + term_2.T) + k_tt
+            out[g] = Gaussian(mean, cov)
+        return _as_gaussians(get, names, out)
+
+    return predict_fn
+
+
+def _dependency(names, compute_cov):
+    """predict.py _get_dependency."""
+    dep = ()
+    if 'nngp' in names or ('ntk' in names and compute_cov):
+        dep += ('nngp',)
+    if 'ntk' in names:
+        dep += ('ntk',)
+    return dep
+
+
+def gradient_descent_mse_ensemble(kernel_fn, x_train, y_train, learning_rate=1., diag_reg=0.,
+                                  diag_reg_absolute_scale=False):
+    """predict.py:753-1005 with trace_axes=(-1,): mean (and covariance) of the
+    infinite ensemble trained by gradient flow on the MSE loss, at times t
+    (eigendecomposition, expm1 spectral functions of predict.py:1277-1294) or at
+    t=None (gp_inference, Cholesky)."""
+    y = np.asarray(y_train, np.float64)
+    k_dd = {}
+    eig = {}
+
+    def k_train(g):
+        if g not in k_dd:
+            k_dd[g] = np.asarray(kernel_fn(x_train, None, g), np.float64)
+        return k_dd[g]
+
+    def eigenspace(g):
+        if g not in eig:
+            a = _add_diagonal_regularizer(k_train(g), diag_reg, diag_reg_absolute_scale)
+            eig[g] = np.linalg.eigh(a)
+        return eig[g]
+
+    def predict_fn(t=None, x_test=None, get=None, compute_cov=False):
+        _, names = _canonical_get(get)
+        dep = _dependency(names, compute_cov)
+        kd = {g: k_train(g) for g in dep}
+        if x_test is None:
+            k_td = None
+            nngp_tt = True if compute_cov else None
+        else:
+            k_td = {g: np.asarray(kernel_fn(x_test, x_train, g), np.float64) for g in dep}
+            nngp_tt = (np.asarray(kernel_fn(x_test, None, 'nngp'), np.float64)
+                       if compute_cov else None)
+        if t is None:
+            return gp_inference(kd, y, diag_reg, diag_reg_absolute_scale)(
+                get=get, k_test_train=k_td, k_test_test=nngp_tt)
+        t = np.asarray(t, np.float64) * learning_rate
+        t_shape = t.shape
+        tf = t.reshape(-1, 1)
+        norm = y.size
+        out = {}
+        for g in names:
+            evals, evecs = eigenspace(g)
+            ev = evals[None, :]
+            pos = np.maximum(ev, 0.)
+            neg_expm1 = -np.expm1(-pos * tf / norm)
+            neg_inv = neg_expm1 / np.abs(ev)
+            if k_td is None:
+                mean = np.einsum('ji,ti,ki,kl->tjl', evecs, neg_expm1, evecs, y)
+            else:
+                ktd = k_td[g]
+                mean = np.einsum('lj,ji,ti,ki,km->tlm', ktd, evecs, neg_inv, evecs, y)
+            mean = mean.reshape(t_shape + mean.shape[1:])
+            if nngp_tt is None:
+                out[g] = mean
+                continue
+            nngp_dd = kd['nngp']
+            if k_td is None:
+                if g == 'nngp':
+                    cov = np.einsum('ji,ti,ki->tjk', evecs, pos * np.exp(-2 * pos * tf / norm),
+                                    evecs)
+                else:
+                    ex = np.einsum('mi,ti,ki->tmk', evecs, np.exp(-pos * tf / norm), evecs)
+                    cov = np.einsum('tmk,kl,tnl->tmn', ex, nngp_dd, ex)
+            else:
+                tt = nngp_tt[None]
+                if g == 'nngp':
+                    neg_inv2 = -np.expm1(-pos * 2 * tf / norm) / np.abs(ev)
+                    cov = tt - np.einsum('mj,ji,ti,ki,lk->tml', ktd, evecs, neg_inv2, evecs, ktd)
+                else:
+                    term_1 = np.einsum('mi,ti,ki,lk->tml', evecs, neg_inv, evecs, ktd)
+                    term_2 = np.einsum('mj,ji,ti,ki,lk->tml', ktd, evecs, neg_inv, evecs,
+                                       k_td['nngp'])
+                    term_2 = term_2 + np.swapaxes(term_2, 1, 2)
+                    cov = np.einsum('tji,jk,tkl->til', term_1, nngp_dd, term_1) - term_2 + tt
+            cov = cov.reshape(t_shape + cov.shape[1:])
+            out[g] = Gaussian(mean, cov)
+        return _as_gaussians(get, names, out)
 
     return predict_fn

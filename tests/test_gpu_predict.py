@@ -95,3 +95,61 @@ def test_finite_time_matches_oracle(nt):
         2.5, 0., 0., ktt.double().cpu().numpy())
     for g, w in zip(got, want):
         np.testing.assert_allclose(g.cpu().numpy(), w, rtol=1e-4, atol=1e-6)
+
+
+def _leaves(x):
+    if isinstance(x, tuple):
+        return [a for v in x for a in _leaves(v)]
+    if isinstance(x, torch.Tensor):
+        return [x.detach().double().cpu().numpy()]
+    return [np.asarray(x, np.float64)]
+
+
+def _ens_setup(nt):
+    rng = np.random.default_rng(31)
+    x_train = rng.standard_normal((40, 12))
+    x_test = rng.standard_normal((15, 12))
+    y_train = rng.standard_normal((40, 3))
+    lay = lambda m: [m.Dense(64, 1.5, 0.2), m.Erf(), m.Dense(64, 1.3, 0.1), m.Relu(),
+                     m.Dense(3, 1.2, 0.1)]
+    return (nt.stax.serial(*lay(nt.stax))[2], o.serial(*lay(o)), x_train, x_test, y_train)
+
+
+@pytest.mark.parametrize('get', ['nngp', 'ntk', ('ntk', 'nngp'), None])
+@pytest.mark.parametrize('compute_cov', [False, True])
+def test_gradient_descent_mse_ensemble_vs_oracle(nt, get, compute_cov):
+    """predict.gradient_descent_mse_ensemble at t = None (Cholesky kernels) and at finite and
+    infinite t (eigendecomposition) against the float64 oracle, on the train and a test set."""
+    kf, ko, x_train, x_test, y_train = _ens_setup(nt)
+    pred = nt.predict.gradient_descent_mse_ensemble(kf, x_train, y_train, diag_reg=1e-3)
+    want_pred = o.gradient_descent_mse_ensemble(ko, x_train, y_train, diag_reg=1e-3)
+    for x in (None, x_test):
+        for t in (None, 0.5, np.array([1., 10.]), np.inf):
+            got = _leaves(pred(t, x, get, compute_cov))
+            want = _leaves(want_pred(t, x, get, compute_cov))
+            assert len(got) == len(want)
+            for g, w in zip(got, want):
+                assert g.shape == w.shape
+                scale = max(np.abs(w).max(), 1e-12)
+                assert np.abs(g - w).max() / scale < 1e-4, (x is None, t)
+
+
+def test_gp_inference_ntkgp_and_errors(nt):
+    """predict.gp_inference: the NNGP / NTK / NTKGP posteriors against the oracle, and the
+    reference's ValueError for an NTK covariance without the NNGP kernels."""
+    kf, ko, x_train, x_test, y_train = _ens_setup(nt)
+    k_dd = kf(x_train, None, ('nngp', 'ntk'))
+    k_td = kf(x_test, x_train, ('nngp', 'ntk'))
+    k_tt = kf(x_test, None, ('nngp', 'ntk'))
+    ok_dd = dict(zip(('nngp', 'ntk'), ko(x_train, None, ('nngp', 'ntk'))))
+    ok_td = dict(zip(('nngp', 'ntk'), ko(x_test, x_train, ('nngp', 'ntk'))))
+    ok_tt = dict(zip(('nngp', 'ntk'), ko(x_test, None, ('nngp', 'ntk'))))
+    gp = nt.predict.gp_inference(k_dd, y_train, diag_reg=1e-3)
+    want = o.gp_inference(ok_dd, y_train, diag_reg=1e-3)
+    for get in (('nngp', 'ntk', 'ntkgp'), 'ntkgp'):
+        for g, w in zip(_leaves(gp(get, k_td, k_tt)), _leaves(want(get, ok_td, ok_tt))):
+            assert np.abs(g - w).max() / max(np.abs(w).max(), 1e-12) < 1e-4
+    with pytest.raises(ValueError):
+        nt.predict.gp_inference({'ntk': k_dd.ntk}, y_train)(get='ntk',
+                                                           k_test_train={'ntk': k_td.ntk},
+                                                           k_test_test=k_tt.nngp)

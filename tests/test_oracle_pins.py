@@ -190,3 +190,84 @@ def test_myrtle5_readout_flatten_equals_mean_after_pools():
     k1 = o.serial(*base, *[o.AvgPool((2, 2), (2, 2))] * 3, o.Flatten())(x, None)
     k2 = o.serial(*base, o.GlobalAvgPool())(x, None)
     np.testing.assert_allclose(k1.nngp, k2.nngp, rtol=1e-12)
+
+
+# ---------------------------------------------------------------------------
+# gp_inference / gradient_descent_mse_ensemble pins (tests/predict_test.py)
+# ---------------------------------------------------------------------------
+def _leaves(x):
+    if isinstance(x, tuple):
+        return [a for v in x for a in _leaves(v)]
+    return [np.asarray(x, np.float64)]
+
+
+def _fcn_ens_setup():
+    rng = np.random.default_rng(21)
+    x_train = rng.standard_normal((10, 5))
+    x_test = rng.standard_normal((6, 5))
+    y_train = rng.standard_normal((10, 3))
+    kf = o.serial(o.Dense(16, 1.5, 0.2), o.Erf(), o.Dense(3, 1.2, 0.1))
+    return kf, x_train, x_test, y_train
+
+
+@pytest.mark.parametrize('get', ['nngp', 'ntk', ('nngp', 'ntk')])
+def test_ensemble_infinite_time_agreement(get):
+    """predict_test.py:396-428: t = inf (eigh) equals t = None (Cholesky), with covariance."""
+    kf, x_train, x_test, y_train = _fcn_ens_setup()
+    pred = o.gradient_descent_mse_ensemble(kf, x_train, y_train, diag_reg=1e-6)
+    for x in (None, x_test):
+        fin = pred(t=np.inf, x_test=x, get=get, compute_cov=True)
+        inf = pred(t=None, x_test=x, get=get, compute_cov=True)
+        for a, b in zip(_leaves(fin), _leaves(inf)):
+            np.testing.assert_allclose(a, b, rtol=1e-5, atol=1e-6)
+
+
+def test_ensemble_zero_time_agreement():
+    """predict_test.py:437-491: at t = 0 the mean is 0 and the covariance the prior NNGP."""
+    kf, x_train, x_test, y_train = _fcn_ens_setup()
+    pred = o.gradient_descent_mse_ensemble(kf, x_train, y_train, diag_reg=1e-7)
+    for x in (None, x_test):
+        out = pred(t=0., x_test=x, get=('ntk', 'nngp'), compute_cov=True)
+        prior = kf(x_train if x is None else x, None, 'nngp')
+        for g in out:
+            np.testing.assert_allclose(g.mean, 0., atol=1e-12)
+            # the regularised train-train matrix enters the NNGP train-set covariance: diag_reg
+            # (1e-7 of the mean trace) is the only difference
+            np.testing.assert_allclose(g.covariance, prior, rtol=1e-6, atol=1e-6)
+
+
+def test_ensemble_covariance_symmetric_psd():
+    """predict_test.py:586-620: posterior covariances are symmetric positive semi-definite."""
+    kf, x_train, x_test, y_train = _fcn_ens_setup()
+    pred = o.gradient_descent_mse_ensemble(kf, x_train, y_train)
+    ts = np.logspace(-3, 3, 5)
+    for get in ('nngp', 'ntk'):
+        for x in (None, x_test):
+            for t in (None, ts):
+                cov = pred(t=t, x_test=x, get=get, compute_cov=True).covariance
+                np.testing.assert_allclose(cov, np.swapaxes(cov, -1, -2), atol=1e-10)
+                assert np.min(np.linalg.eigvalsh(cov)) > -1e-4
+
+
+def test_gp_inference_matches_ensemble_and_ntkgp_is_nngp_with_ntk():
+    """predict_test.py:704-824: gp_inference equals the ensemble at t = None, and NTKGP is the
+    NNGP posterior computed with the NTK in place of the NNGP."""
+    kf, x_train, x_test, y_train = _fcn_ens_setup()
+    k_dd = dict(zip(('nngp', 'ntk'), kf(x_train, None, ('nngp', 'ntk'))))
+    k_td = dict(zip(('nngp', 'ntk'), kf(x_test, x_train, ('nngp', 'ntk'))))
+    k_tt = dict(zip(('nngp', 'ntk'), kf(x_test, None, ('nngp', 'ntk'))))
+    gp = o.gp_inference(k_dd, y_train, diag_reg=1e-5)
+    ens = o.gradient_descent_mse_ensemble(kf, x_train, y_train, diag_reg=1e-5)
+    a = gp(get=('nngp', 'ntk'), k_test_train=k_td, k_test_test=k_tt['nngp'])
+    b = ens(None, x_test, ('nngp', 'ntk'), True)
+    for ga, gb in zip(a, b):
+        np.testing.assert_allclose(ga.mean, gb.mean, rtol=1e-10)
+        np.testing.assert_allclose(ga.covariance, gb.covariance, rtol=1e-9, atol=1e-12)
+    ntkgp = gp(get='ntkgp', k_test_train=k_td, k_test_test=k_tt)
+    only_ntk = o.gp_inference({'nngp': k_dd['ntk']}, y_train, diag_reg=1e-5)(
+        get='nngp', k_test_train={'nngp': k_td['ntk']}, k_test_test=k_tt['ntk'])
+    np.testing.assert_allclose(ntkgp.mean, only_ntk.mean, rtol=1e-12)
+    np.testing.assert_allclose(ntkgp.covariance, only_ntk.covariance, rtol=1e-12)
+    with pytest.raises(ValueError):
+        o.gp_inference({'ntk': k_dd['ntk']}, y_train)(get='ntk', k_test_train={'ntk': k_td['ntk']},
+                                                      k_test_test=k_tt['nngp'])
