@@ -253,6 +253,16 @@ int ntg_act_bwd(void* stream, const float* q, const float* t, const float* gq, c
                 float* oq, float* ot, int64_t batch, int64_t n2, int64_t a, int64_t c,
                 int32_t diag_spatial, ntg_act_t act, ntg_var_t var1, ntg_var_t var2,
                 float* gvar1, float* gvar2);
+/* The activation VJP of ntg_act_bwd composed with the transpose of the
+ * AvgPool((2, 2), (2, 2)) that follows it (linear.py:1631-1664): the output
+ * cotangents are those of the pooled kernels [B, A/2, A/2, C/2, C/2]; each entry
+ * takes its window's cotangent / 16 without the [B, A, A, C, C] cotangent being
+ * written. Full-spatial only, C a power of two in [4, 32], A even. No reference
+ * counterpart (XLA differentiates the two layers separately). */
+int ntg_act_pool_bwd(void* stream, const float* q, const float* t, const float* gq_pooled,
+                     const float* gt_pooled, float* oq, float* ot, int64_t batch, int64_t n2,
+                     int64_t a, int64_t c, ntg_act_t act, ntg_var_t var1, ntg_var_t var2,
+                     float* gvar1, float* gvar2);
 /* Cotangents of the unscaled stencil sums U, Ut of an affine rule evaluated
  * as q = aff.w2 * scale * U + b2, t = ntk_w2 * scale * Ut + ... (n entries). */
 int ntg_affine_bwd(void* stream, const float* gq, const float* gt, float* gu, float* gut,

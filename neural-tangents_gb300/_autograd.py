@@ -373,6 +373,77 @@ class ActFn(torch.autograd.Function):
         return (gqi.reshape(q.shape), None if zero_t else gti.reshape(q.shape), gc1i, gc2i, None)
 
 
+class ActPoolFn(torch.autograd.Function):
+    """Activation followed by AvgPool((2, 2), (2, 2)) on full-spatial kernels: the forward
+    is the two rules; the backward applies the activation VJP to the pooled cotangents
+    directly (ntg_act_pool_bwd), so the unpooled cotangent is never written."""
+
+    @staticmethod
+    def forward(ctx, q, t, c1, c2, act, pool_geom):
+        qa, ta, c1a, c2a = ActFn.forward(ctx, q, t, c1, c2, act)
+        ctx.pool_geom = pool_geom
+        ctx.pool_shapes = [None if x is None else tuple(x.shape) for x in (qa, ta, c1a, c2a)]
+
+        def run(x, bnd):
+            if x is None or x.ndim == 0 or x.numel() == 0:
+                return x
+            a, c, wa, wc, sa, sc, pa, pc, ao, co, circ, avg, ne, two_d = pool_geom
+            lead = tuple(x.shape[:bnd])
+            return O.pool(x.contiguous(), int(math.prod(lead)), a, c, wa, wc, sa, sc, pa, pc, ao,
+                          co, circ, False, avg, ne, lead + (ao, ao, co, co))
+
+        return run(qa, 2), run(ta, 2), run(c1a, 1), run(c2a, 1)
+
+    @staticmethod
+    def backward(ctx, gq, gt, gc1, gc2):
+        q, t, c1, c2 = ctx.saved_tensors
+        act, zero_t = ctx.act, ctx.zero_t
+        c2o = _opt(c2)
+        s = L.stream()
+        a, c = _ac(q, 2)
+        n1, n2 = q.shape[0], q.shape[1]
+        q4, c14 = _as4(q.contiguous(), 2), _as4(c1.contiguous(), 1)
+        c24 = None if c2o is None else _as4(c2o.contiguous(), 1)
+        v1 = _diag_view(c14)
+        v2 = _diag_view(c24 if c24 is not None else c14)
+        gd1 = torch.zeros((n1, a, c), device=q.device)
+        gd2 = gd1 if c24 is None else torch.zeros((c24.shape[0], a, c), device=q.device)
+        gqi = torch.empty_like(q4)
+        gti = None if zero_t else torch.empty_like(q4)
+        t4 = None if zero_t else _as4(t.contiguous(), 2)
+        L.call('ntg_act_pool_bwd', s, L.ptr(q4), None if t4 is None else L.ptr(t4),
+               None if gq is None else L.ptr(gq.contiguous()),
+               None if (gt is None or zero_t) else L.ptr(gt.contiguous()),
+               L.ptr(gqi), None if gti is None else L.ptr(gti), n1 * n2, n2, a, c, act, v1, v2,
+               gd1.data_ptr(), gd2.data_ptr())
+
+        def self_back(cv, gcv, gd):
+            vv = _diag_view(cv)
+            out = torch.empty_like(cv)
+            L.call('ntg_act_pool_bwd', s, L.ptr(cv), None,
+                   None if gcv is None else L.ptr(gcv.contiguous()), None, L.ptr(out), None,
+                   cv.shape[0], 0, a, c, act, vv, vv, gd.data_ptr(), gd.data_ptr())
+            L.call('ntg_diag_add', s, gd.data_ptr(), L.ptr(out), cv.shape[0], a, c, vv.s_n,
+                   vv.s_a, vv.s_c)
+            return out
+
+        gc1i = self_back(c14, gc1, gd1).reshape(c1.shape)
+        gc2i = None if c24 is None else self_back(c24, gc2, gd2).reshape(c2o.shape)
+        return (gqi.reshape(q.shape), None if zero_t else gti.reshape(q.shape), gc1i, gc2i, None,
+                None)
+
+
+def act_pool_fusable(q: torch.Tensor, pool_geom) -> bool:
+    """Whether ActPoolFn's fused backward applies: full-spatial [N1, N2, A, A, C, C] with C a
+    power of two in [4, 32], AvgPool((2, 2), (2, 2)) without padding."""
+    if q.ndim != 6:
+        return False
+    a, c, wa, wc, sa, sc, pa, pc, ao, co, circ, avg, ne, two_d = pool_geom
+    return (two_d and avg and not ne and (wa, wc, sa, sc, pa, pc) == (2, 2, 2, 2, 0, 0) and
+            a % 2 == 0 and c in (4, 8, 16, 32) and (a * a * c * c) % 1024 == 0 and
+            ao == a // 2 and co == c // 2)
+
+
 # ---------------------------------------------------------------------------
 class PoolFn(torch.autograd.Function):
     @staticmethod
@@ -469,6 +540,23 @@ def _sq(v, dev):
     return torch.tensor(float(v) ** 2, device=dev)
 
 
+def _pool_geom(q: torch.Tensor, sp):
+    """(a, c, windows, strides, pads, output sizes, circular, average, normalize_edges, two_d)
+    of a pooling layer applied to the pair kernel q."""
+    from .stax import Padding, _pads
+    p = sp.params
+    a, c = _ac(q, 2)
+    ws, st = p['window_shape'], p['strides']
+    two_d = len(ws) == 2
+    wa, sa = ws[0], st[0]
+    wc, sc = (ws[1], st[1]) if two_d else (1, 1)
+    pa, ao = _pads(a, wa, sa, p['padding'])
+    pc, co = _pads(c, wc, sc, p['padding']) if two_d else (0, 1)
+    ne = bool(p['normalize_edges']) and p['padding'] == Padding.SAME
+    return (a, c, wa, wc, sa, sc, pa, pc, ao, co, p['padding'] == Padding.CIRCULAR,
+            p['pool'] == 'avg', ne, two_d)
+
+
 def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: bool,
            precision: str = 'fp32') -> Kernel:
     """kernel_fn(x1, x2) through the differentiable layer Functions ('mixed': the
@@ -486,9 +574,12 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
     q, c1, c2 = InputFn.apply(x1, _e(dev) if x2 is None else x2, ctx.gram_precision)
     t = torch.zeros((), device=dev) if compute_ntk else None
     is_gaussian, is_reversed = False, False
-    for sp in specs:
+    skip_next = False
+    for idx, sp in enumerate(specs):
         p = sp.params
-        if sp.kind == 'identity':
+        if skip_next:  # a pooling folded into the activation before it
+            skip_next = False
+        elif sp.kind == 'identity':
             pass
         elif sp.kind in ('dense', 'conv'):
             if p['parameterization'] != 'ntk':
@@ -519,20 +610,17 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
             if p.get('do_stabilize'):
                 raise NotImplementedError('do_stabilize is not differentiable here')
             tt = t if t is not None else torch.zeros((), device=dev)
-            q, tt, c1, c2 = ActFn.apply(q, tt, c1, c2, _act_struct(p, ctx))
+            nxt = specs[idx + 1] if idx + 1 < len(specs) else None
+            geom = _pool_geom(q, nxt) if (nxt is not None and nxt.kind == 'pool') else None
+            if geom is not None and act_pool_fusable(q, geom) and t is not None and tt.ndim > 0:
+                q, tt, c1, c2 = ActPoolFn.apply(q, tt, c1, c2, _act_struct(p, ctx), geom)
+                skip_next = True
+            else:
+                q, tt, c1, c2 = ActFn.apply(q, tt, c1, c2, _act_struct(p, ctx))
             t = tt if t is not None else None
             is_gaussian = False
         elif sp.kind == 'pool':
-            a, c = _ac(q, 2)
-            ws, st = p['window_shape'], p['strides']
-            two_d = len(ws) == 2
-            wa, sa = ws[0], st[0]
-            wc, sc = (ws[1], st[1]) if two_d else (1, 1)
-            pa, ao = _pads(a, wa, sa, p['padding'])
-            pc, co = _pads(c, wc, sc, p['padding']) if two_d else (0, 1)
-            ne = bool(p['normalize_edges']) and p['padding'] == Padding.SAME
-            geom = (a, c, wa, wc, sa, sc, pa, pc, ao, co, p['padding'] == Padding.CIRCULAR,
-                    p['pool'] == 'avg', ne, two_d)
+            geom = _pool_geom(q, sp)
             tt = t if (t is not None and t.ndim > 0) else None
             q, tt2, c1, c2 = PoolFn.apply(q, tt, c1, c2, geom)
             t = tt2 if tt is not None else t

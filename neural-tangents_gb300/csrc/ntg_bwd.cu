@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(kT)
                       const float* __restrict__ gq, const float* __restrict__ gt,
                       float* __restrict__ oq, float* __restrict__ ot, int64_t batch, int64_t n2,
                       int A, int C, ntg_act_t act, ntg_var_t var1, ntg_var_t var2, VarGrad gv1,
-                      VarGrad gv2) {
+                      VarGrad gv2, int pooled, float pool_w) {
   __shared__ __align__(16) float sv[2][2][256];  // [buffer][v1 | v2][key]
   __shared__ float sg[2][2][256];                // [buffer][g v1 | g v2][key]
   const int64_t M = (int64_t)A * A * C * C;  // < 2^31 (checked by the host)
@@ -253,8 +253,23 @@ __global__ void __launch_bounds__(kT)
     const int64_t e = b * M + (int64_t)j * 1024 + 4 * tid;
     const float4 Q = *reinterpret_cast<const float4*>(q + e);
     const float4 T = t ? *reinterpret_cast<const float4*>(t + e) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 GQ = gq ? *reinterpret_cast<const float4*>(gq + e) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 GT = gt ? *reinterpret_cast<const float4*>(gt + e) : make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 GQ, GT;
+    if (!pooled) {
+      GQ = gq ? *reinterpret_cast<const float4*>(gq + e) : make_float4(0.f, 0.f, 0.f, 0.f);
+      GT = gt ? *reinterpret_cast<const float4*>(gt + e) : make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+      // cotangent of the AvgPool(2, 2) output, taken at the window of each entry
+      const int m = j * 1024 + 4 * tid;
+      const int row = m >> lc, pl = row >> lc;
+      const int wq = m & (C - 1), w = row & (C - 1), hq = pl % A, h = pl / A;
+      const int Ao = A >> 1, Co = C >> 1;
+      const int64_t o = b * ((int64_t)Ao * Ao * Co * Co) +
+                        ((int64_t)((h >> 1) * Ao + (hq >> 1)) * Co + (w >> 1)) * Co + (wq >> 1);
+      const float a0 = gq ? __ldg(gq + o) * pool_w : 0.f, a1 = gq ? __ldg(gq + o + 1) * pool_w : 0.f;
+      const float c0 = gt ? __ldg(gt + o) * pool_w : 0.f, c1 = gt ? __ldg(gt + o + 1) * pool_w : 0.f;
+      GQ = make_float4(a0, a0, a1, a1);
+      GT = make_float4(c0, c0, c1, c1);
+    }
     const float qa[4] = {Q.x, Q.y, Q.z, Q.w}, ta[4] = {T.x, T.y, T.z, T.w};
     const float ga[4] = {GQ.x, GQ.y, GQ.z, GQ.w}, gb[4] = {GT.x, GT.y, GT.z, GT.w};
     const float v1 = sv[cur][0][k1];
@@ -858,13 +873,41 @@ extern "C" int ntg_act_bwd(void* stream, const float* q, const float* t, const f
     const int64_t chunks = batch * (m / 1024);
     const int grid = (int)(chunks < 152 * 8 ? chunks : 152 * 8);
     act_bwd_fs_kernel<<<grid, kT, 0, as_stream(stream)>>>(q, t, gq, gt, oq, ot, batch, n2,
-                                                          (int)a, (int)c, act, var1, var2, g1, g2);
+                                                          (int)a, (int)c, act, var1, var2, g1, g2,
+                                                          0, 0.f);
   } else {
     act_bwd_kernel<<<grid_for(batch * m), kT, 0, as_stream(stream)>>>(
         q, t, gq, gt, oq, ot, batch, n2, a, c, diag_spatial, act, var1, var2, g1, g2);
   }
   note_launch();
   return check_launch("ntg_act_bwd");
+}
+
+extern "C" int ntg_act_pool_bwd(void* stream, const float* q, const float* t,
+                                const float* gq_pooled, const float* gt_pooled, float* oq,
+                                float* ot, int64_t batch, int64_t n2, int64_t a, int64_t c,
+                                ntg_act_t act, ntg_var_t var1, ntg_var_t var2, float* gvar1,
+                                float* gvar2) {
+  NTG_REQUIRE(q && oq && var1.base && var2.base, "ntg_act_pool_bwd: null pointer");
+  NTG_REQUIRE(batch > 0 && a > 0 && c > 0, "ntg_act_pool_bwd: bad sizes");
+  NTG_REQUIRE(act.kind != NTG_ACT_ABRELU || act.stabilize <= 0.f,
+              "ntg_act_pool_bwd: do_stabilize is not differentiable here");
+  const int64_t m = a * a * c * c;
+  const bool pow2 = c >= 4 && c <= 32 && (c & (c - 1)) == 0;
+  const bool aligned = ((reinterpret_cast<uintptr_t>(q) | reinterpret_cast<uintptr_t>(t) |
+                         reinterpret_cast<uintptr_t>(oq) | reinterpret_cast<uintptr_t>(ot)) &
+                        15) == 0;
+  NTG_REQUIRE(pow2 && a % 2 == 0 && m % 1024 == 0 && aligned && m < (1ll << 31),
+              "ntg_act_pool_bwd: needs C a power of two in [4, 32], even A, 16-byte aligned "
+              "buffers and A^2 C^2 a multiple of 1024");
+  VarGrad g1{gvar1, a * c, c, 1}, g2{gvar2, a * c, c, 1};
+  const int64_t chunks = batch * (m / 1024);
+  const int grid = (int)(chunks < 152 * 8 ? chunks : 152 * 8);
+  act_bwd_fs_kernel<<<grid, kT, 0, as_stream(stream)>>>(q, t, gq_pooled, gt_pooled, oq, ot, batch,
+                                                        n2, (int)a, (int)c, act, var1, var2, g1,
+                                                        g2, 1, 1.f / 16.f);
+  note_launch();
+  return check_launch("ntg_act_pool_bwd");
 }
 
 extern "C" int ntg_affine_bwd(void* stream, const float* gq, const float* gt, float* gu,
