@@ -136,6 +136,15 @@ int ntg_conv_fs(void* stream, const float* in_nngp, const float* in_ntk,
  * -> conv(x1 x2^T / K) with affine + activation, written as [N1*N2, A, A, C, C]
  * (3x3 / stride 1 / SAME / zero padding). ntk_out = nngp_out before the
  * activation, as for an input kernel whose NTK is the scalar zero. */
+/* ntg_conv_fs for a 3x3 / stride 1 / SAME / zero-padded conv on 32 x 32 planes
+ * followed by an activation, also writing the conv output before the activation
+ * (pre_q, pre_t) that the activation's VJP needs: one pass instead of a conv and
+ * an activation pass. NTG_ERR_UNSUPPORTED for other shapes or unaligned buffers
+ * (run ntg_conv_fs and ntg_affine_act then). No reference counterpart. */
+int ntg_conv_act_fs(void* stream, const float* in_q, const float* in_t, float* out_q,
+                    float* out_t, float* pre_q, float* pre_t, int64_t batch, int64_t n2,
+                    int64_t a, int64_t c, ntg_affine_t aff, ntg_act_t act, ntg_var_t var1,
+                    ntg_var_t var2);
 int ntg_conv_input_fs(void* stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
                       int64_t a, int64_t c, int64_t k, float* out_nngp, float* out_ntk,
                       ntg_affine_t aff, ntg_act_t act, ntg_var_t var1, ntg_var_t var2);

@@ -433,6 +433,99 @@ class ActPoolFn(torch.autograd.Function):
                 None)
 
 
+class _SubCtx:
+    """The ctx fields another Function's backward reads, for composing rules."""
+
+    def __init__(self, saved, **fields):
+        self.saved_tensors = saved
+        self.__dict__.update(fields)
+
+
+class ConvActFn(torch.autograd.Function):
+    """Conv (3x3, stride 1, SAME, 32 x 32 planes) followed by an activation, and optionally by
+    AvgPool((2, 2), (2, 2)): the pair kernels take one pass (ntg_conv_act_fs writes the
+    activated kernels and the conv output the activation's VJP needs); the per-sample
+    kernels take the conv, then the activation with their own variances. The backward is
+    the activation VJP (pooled cotangent read directly when the pool is fused) followed by
+    the conv's."""
+
+    @staticmethod
+    def forward(ctx, w2t, b2t, q, t, c1, c2, geom, act, pool_geom):
+        w2, b2 = _f(w2t), _f(b2t)
+        aff = O.affine(w2, b2, w2)
+        fh, fw, sh, sw, ph, pw, ao, co, circ, nsp = geom
+        zero_t = _zero_ntk(t)
+        c2o = _opt(c2)
+        dev = q.device
+
+        def conv_self(x):
+            x4 = _as4(x.contiguous(), 1)
+            a, c = _ac(x, 1)
+            return O.conv_fs(x4, None, x.shape[0], 0, a, c, fh, fw, sh, sw, ph, pw, ao, co, circ,
+                             aff, O.NO_ACT, O.NO_VAR, O.NO_VAR, False, (x.shape[0],))[0]
+
+        c1p = conv_self(c1)
+        c2p = _e(dev) if c2o is None else conv_self(c2o)
+        v1 = _diag_view(c1p)
+        v2 = _diag_view(c2p if c2o is not None else c1p)
+        n1, n2, a = q.shape[0], q.shape[1], q.shape[2]
+        c = q.shape[4]
+        q4 = _as4(q.contiguous(), 2)
+        t4 = None if zero_t else _as4(t.contiguous(), 2)
+        shape = (n1, n2, a, a, c, c)
+        qp, tp = torch.empty(shape, device=dev), torch.empty(shape, device=dev)
+        qa, ta = torch.empty(shape, device=dev), torch.empty(shape, device=dev)
+        L.call('ntg_conv_act_fs', L.stream(), L.ptr(q4), None if t4 is None else L.ptr(t4),
+               L.ptr(qa), L.ptr(ta), L.ptr(qp), L.ptr(tp), n1 * n2, n2, a, c, aff, act, v1, v2)
+
+        def act_self(cv):
+            vv = _diag_view(cv)
+            return O.affine_act(cv, None, cv.shape[0], 0, a, c, False, False, O.IDENTITY_AFFINE,
+                                act, vv, vv, False)[0]
+
+        c1a = act_self(c1p)
+        c2a = _e(dev) if c2o is None else act_self(c2p)
+        ctx.save_for_backward(qp, tp, c1p, c2p)
+        ctx.conv_meta = (w2, b2, zero_t, geom, tuple(q.shape), tuple(c1.shape),
+                         None if c2o is None else tuple(c2o.shape))
+        ctx.act, ctx.pool_geom = act, pool_geom
+        outs = [qa, ta, c1a, c2a]
+        if pool_geom is not None:
+            pa_, pc_ = pool_geom[6], pool_geom[7]
+            ao2, co2 = pool_geom[8], pool_geom[9]
+
+            def pool(x, bnd):
+                if x.numel() == 0:
+                    return x
+                lead = tuple(x.shape[:bnd])
+                return O.pool(x.contiguous(), int(math.prod(lead)), a, c, 2, 2, 2, 2, pa_, pc_,
+                              ao2, co2, False, False, True, False, lead + (ao2, ao2, co2, co2))
+
+            outs = [pool(outs[0], 2), pool(outs[1], 2), pool(outs[2], 1), pool(outs[3], 1)]
+        return tuple(outs)
+
+    @staticmethod
+    def backward(ctx, gq, gt, gc1, gc2):
+        qp, tp, c1p, c2p = ctx.saved_tensors
+        act_ctx = _SubCtx((qp, tp, c1p, c2p), act=ctx.act, zero_t=False)
+        if ctx.pool_geom is not None:
+            g = ActPoolFn.backward(act_ctx, gq, gt, gc1, gc2)
+        else:
+            g = ActFn.backward(act_ctx, gq, gt, gc1, gc2)
+        conv_ctx = _SubCtx((qp, tp, c1p, c2p), meta=ctx.conv_meta,
+                           needs_input_grad=ctx.needs_input_grad[:2] + (True,) * 5)
+        r = ConvFn.backward(conv_ctx, g[0], g[1], g[2], g[3])
+        return r[0], r[1], r[2], r[3], r[4], r[5], None, None, None
+
+
+def conv_act_fusable(q: torch.Tensor, geom) -> bool:
+    """Whether ConvActFn applies: pair kernels [N1, N2, 32, 32, 32, 32] and a 3x3 / stride 1 /
+    SAME / zero-padded conv."""
+    fh, fw, sh, sw, ph, pw, ao, co, circ, nsp = geom
+    return (q.ndim == 6 and nsp == 2 and q.shape[2] == 32 and q.shape[4] == 32 and
+            (fh, fw, sh, sw, ph, pw) == (3, 3, 1, 1, 1, 1) and ao == 32 and co == 32 and not circ)
+
+
 def act_pool_fusable(q: torch.Tensor, pool_geom) -> bool:
     """Whether ActPoolFn's fused backward applies: full-spatial [N1, N2, A, A, C, C] with C a
     power of two in [4, 32], AvgPool((2, 2), (2, 2)) without padding."""
@@ -543,9 +636,13 @@ def _sq(v, dev):
 def _pool_geom(q: torch.Tensor, sp):
     """(a, c, windows, strides, pads, output sizes, circular, average, normalize_edges, two_d)
     of a pooling layer applied to the pair kernel q."""
+    a, c = _ac(q, 2)
+    return _pool_geom_sizes(a, c, sp)
+
+
+def _pool_geom_sizes(a: int, c: int, sp):
     from .stax import Padding, _pads
     p = sp.params
-    a, c = _ac(q, 2)
     ws, st = p['window_shape'], p['strides']
     two_d = len(ws) == 2
     wa, sa = ws[0], st[0]
@@ -574,11 +671,11 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
     q, c1, c2 = InputFn.apply(x1, _e(dev) if x2 is None else x2, ctx.gram_precision)
     t = torch.zeros((), device=dev) if compute_ntk else None
     is_gaussian, is_reversed = False, False
-    skip_next = False
+    skip_next = 0
     for idx, sp in enumerate(specs):
         p = sp.params
-        if skip_next:  # a pooling folded into the activation before it
-            skip_next = False
+        if skip_next:  # layers folded into the rule before them
+            skip_next -= 1
         elif sp.kind == 'identity':
             pass
         elif sp.kind in ('dense', 'conv'):
@@ -598,6 +695,23 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
                 ph, ao = _pads(a, fh, sh, p['padding'])
                 pw, co = _pads(c, fw, sw, p['padding']) if nsp == 2 else (0, 1)
                 geom = (fh, fw, sh, sw, ph, pw, ao, co, p['padding'] == Padding.CIRCULAR, nsp)
+                nxt = specs[idx + 1] if idx + 1 < len(specs) else None
+                nxt2 = specs[idx + 2] if idx + 2 < len(specs) else None
+                if (nxt is not None and nxt.kind == 'act' and not nxt.params.get('do_stabilize')
+                        and conv_act_fusable(q, geom)):
+                    pool_geom = None
+                    if nxt2 is not None and nxt2.kind == 'pool':
+                        pg = _pool_geom_sizes(32, 32, nxt2)
+                        if act_pool_fusable(q, pg):
+                            pool_geom = pg
+                    q, tt, c1, c2 = ConvActFn.apply(w2, b2, q, tt, c1, c2, geom,
+                                                    _act_struct(nxt.params, ctx), pool_geom)
+                    skip_next = 2 if pool_geom is not None else 1
+                    is_gaussian = False
+                    shape1, shape2 = sp.shape_fn(shape1), sp.shape_fn(shape2)
+                    is_reversed = not is_reversed
+                    t = tt if t is not None else None
+                    continue
                 q, tt, c1, c2 = ConvFn.apply(w2, b2, q, tt, c1, c2, geom)
                 is_reversed = not is_reversed
             t = tt if t is not None else None
@@ -614,7 +728,7 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
             geom = _pool_geom(q, nxt) if (nxt is not None and nxt.kind == 'pool') else None
             if geom is not None and act_pool_fusable(q, geom) and t is not None and tt.ndim > 0:
                 q, tt, c1, c2 = ActPoolFn.apply(q, tt, c1, c2, _act_struct(p, ctx), geom)
-                skip_next = True
+                skip_next = 1
             else:
                 q, tt, c1, c2 = ActFn.apply(q, tt, c1, c2, _act_struct(p, ctx))
             t = tt if t is not None else None

@@ -64,6 +64,8 @@ SIGNATURES = {
     'ntg_input_fs': ([_P, _P, _P, _I64, _I64, _I64, _I64, _I64, _I32, _P], C.c_int),
     'ntg_conv_fs': ([_P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, _I32, _I32, _I32, _I32,
                      _I32, _I32, _I64, _I64, _I32, Affine, Act, Var, Var], C.c_int),
+    'ntg_conv_act_fs': ([_P, _P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, Affine, Act, Var,
+                         Var], C.c_int),
     'ntg_conv_input_fs': ([_P, _P, _P, _I64, _I64, _I64, _I64, _I64, _P, _P, Affine, Act, Var,
                            Var], C.c_int),
     'ntg_conv_ds': ([_P, _P, _P, _P, _P, _I64, _I64, _I64, _I32, _I32, _I32, _I32, _I32, _I32,

@@ -598,9 +598,20 @@ constexpr int kSkewPlane = kSkewC * kSkewC;
 constexpr int kSkewVars = 192;  // per plane: v1[32] | sqrt v1[32] | v2[64] | sqrt v2[64]
 
 template <int RING>
-constexpr size_t skew_smem_bytes() {
+__host__ __device__ constexpr size_t skew_smem_bytes() {
   return sizeof(float) * (2 * RING * kSkewPlane + 4 * kSkewPlane + 2 * kSkewVars) +
          sizeof(uint64_t) * RING;
+}
+
+// start (bytes, 128-aligned) of the optional pre-activation staging planes
+template <int RING>
+__host__ __device__ constexpr size_t skew_pre_offset() {
+  return (skew_smem_bytes<RING>() + 127) / 128 * 128;
+}
+
+template <int RING>
+__host__ __device__ constexpr size_t skew_smem_bytes_pre() {
+  return skew_pre_offset<RING>() + sizeof(float) * 4 * kSkewPlane;
 }
 
 __device__ __forceinline__ void bulk_store(float* gdst, const float* ssrc, uint32_t bytes) {
@@ -614,7 +625,7 @@ __global__ void __launch_bounds__(kThreads)
     conv3_skew_kernel(const float* __restrict__ in_q, const float* __restrict__ in_t,
                       float* __restrict__ out_q, float* __restrict__ out_t, int64_t batch,
                       int64_t n2, int A, ntg_affine_t aff, ntg_act_t act, ntg_var_t var1,
-                      ntg_var_t var2) {
+                      ntg_var_t var2, float* __restrict__ pre_q, float* __restrict__ pre_t) {
   extern __shared__ __align__(128) float smem[];
   __shared__ int s_err;
   float* ring_q = smem;                           // [RING][plane]
@@ -623,6 +634,9 @@ __global__ void __launch_bounds__(kThreads)
   float* stage_t = stage_q + 2 * kSkewPlane;      // [2][plane]
   float* vrow = stage_t + 2 * kSkewPlane;         // [2][kSkewVars]
   uint64_t* bars = reinterpret_cast<uint64_t*>(vrow + 2 * kSkewVars);
+  // with pre_q: staging of the pre-activation planes [2][plane] x 2 after the barriers
+  float* stage_pq = reinterpret_cast<float*>(smem) + skew_pre_offset<RING>() / sizeof(float);
+  float* stage_pt = stage_pq + 2 * kSkewPlane;
   const int nlines = 2 * A - 1;
   const int64_t b = blockIdx.x / nlines;
   const int delta = (int)(blockIdx.x - b * nlines) - (A - 1);
@@ -762,6 +776,20 @@ __global__ void __launch_bounds__(kThreads)
       const P2 nn = aff.nn_scaled ? q[h] : mul2(cq, p2s(inv9));
       t[h] = fma2(TW, ct, fma2(TN, nn, TC));
     }
+    if (pre_q) {  // the conv output before the activation, for the activation's VJP
+      float* pq = stage_pq + (j & 1) * kSkewPlane;
+      float* pt = stage_pt + (j & 1) * kSkewPlane;
+      float vq[4], vt[4];
+      p2u(q[0], vq[0], vq[1]);
+      p2u(q[1], vq[2], vq[3]);
+      p2u(t[0], vt[0], vt[1]);
+      p2u(t[1], vt[2], vt[3]);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        pq[u[k]] = vq[k];
+        if (pre_t) pt[u[k]] = vt[k];
+      }
+    }
     if (has_act) {
       const float* vb = vrow + (j & 1) * kSkewVars;
       const float4 v1 = *reinterpret_cast<const float4*>(vb + w0);
@@ -814,6 +842,10 @@ __global__ void __launch_bounds__(kThreads)
       const int64_t off = b * pair_stride + ((int64_t)i * A + i + delta) * kSkewPlane;
       bulk_store(out_q + off, gq, kSkewPlane * 4u);
       if (out_t) bulk_store(out_t + off, gt, kSkewPlane * 4u);
+      if (pre_q) {
+        bulk_store(pre_q + off, stage_pq + (j & 1) * kSkewPlane, kSkewPlane * 4u);
+        if (pre_t) bulk_store(pre_t + off, stage_pt + (j & 1) * kSkewPlane, kSkewPlane * 4u);
+      }
       asm volatile("cp.async.bulk.commit_group;" ::: "memory");
       // plane j + 1 has been read by every thread: its slot takes plane j + 1 + RING
       if (!s_err)
@@ -1204,21 +1236,23 @@ extern "C" int ntg_input_fs(void* stream, const float* x1, const float* x2, int6
 template <int RING>
 cudaError_t launch_skew(cudaStream_t s, int64_t blocks, const float* in_q, const float* in_t,
                         float* out_q, float* out_t, int64_t batch, int64_t n2, int64_t a,
-                        ntg_affine_t aff, ntg_act_t act, ntg_var_t var1, ntg_var_t var2) {
-  constexpr size_t sm = skew_smem_bytes<RING>();
+                        ntg_affine_t aff, ntg_act_t act, ntg_var_t var1, ntg_var_t var2,
+                        float* pre_q = nullptr, float* pre_t = nullptr) {
+  const size_t sm = pre_q ? skew_smem_bytes_pre<RING>() : skew_smem_bytes<RING>();
+  const size_t sm_max = skew_smem_bytes_pre<RING>();
   cudaError_t e;
   if (in_t) {
     e = cudaFuncSetAttribute(conv3_skew_kernel<true, RING>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
     if (e == cudaSuccess)
       conv3_skew_kernel<true, RING><<<(unsigned)blocks, kThreads, sm, s>>>(
-          in_q, in_t, out_q, out_t, batch, n2, (int)a, aff, act, var1, var2);
+          in_q, in_t, out_q, out_t, batch, n2, (int)a, aff, act, var1, var2, pre_q, pre_t);
   } else {
     e = cudaFuncSetAttribute(conv3_skew_kernel<false, RING>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
     if (e == cudaSuccess)
       conv3_skew_kernel<false, RING><<<(unsigned)blocks, kThreads, sm, s>>>(
-          in_q, nullptr, out_q, out_t, batch, n2, (int)a, aff, act, var1, var2);
+          in_q, nullptr, out_q, out_t, batch, n2, (int)a, aff, act, var1, var2, pre_q, pre_t);
   }
   return e;
 }
@@ -1292,6 +1326,36 @@ extern "C" int ntg_conv_fs(void* stream, const float* in_q, const float* in_t, f
   }
   note_launch();
   return check_launch("ntg_conv_fs");
+}
+
+extern "C" int ntg_conv_act_fs(void* stream, const float* in_q, const float* in_t,
+                               float* out_q, float* out_t, float* pre_q, float* pre_t,
+                               int64_t batch, int64_t n2, int64_t a, int64_t c, ntg_affine_t aff,
+                               ntg_act_t act, ntg_var_t var1, ntg_var_t var2) {
+  NTG_REQUIRE(in_q && out_q && pre_q, "ntg_conv_act_fs: null pointer");
+  NTG_REQUIRE(!out_t == !pre_t, "ntg_conv_act_fs: out_t and pre_t go together");
+  NTG_REQUIRE(batch > 0 && a > 0 && a <= 4096, "ntg_conv_act_fs: bad sizes");
+  NTG_REQUIRE(act.kind == NTG_ACT_NONE || (var1.base && var2.base),
+              "ntg_conv_act_fs: activation needs var1/var2");
+  const bool aligned = ((reinterpret_cast<uintptr_t>(in_q) | reinterpret_cast<uintptr_t>(in_t) |
+                         reinterpret_cast<uintptr_t>(out_q) | reinterpret_cast<uintptr_t>(out_t) |
+                         reinterpret_cast<uintptr_t>(pre_q) | reinterpret_cast<uintptr_t>(pre_t)) &
+                        15) == 0;
+  if (c != kSkewC || !aligned)
+    return fail(NTG_ERR_UNSUPPORTED,
+                "ntg_conv_act_fs: needs 32 x 32 planes and 16-byte aligned buffers");
+  const int64_t blocks = batch * (2 * a - 1);
+  NTG_REQUIRE(blocks < (1ll << 31), "ntg_conv_act_fs: grid too large");
+  cudaError_t e;
+  switch (tune(NTG_TUNE_STENCIL_RING)) {
+    case 2: e = launch_skew<2>(as_stream(stream), blocks, in_q, in_t, out_q, out_t, batch, n2, a, aff, act, var1, var2, pre_q, pre_t); break;
+    case 3: e = launch_skew<3>(as_stream(stream), blocks, in_q, in_t, out_q, out_t, batch, n2, a, aff, act, var1, var2, pre_q, pre_t); break;
+    case 6: e = launch_skew<6>(as_stream(stream), blocks, in_q, in_t, out_q, out_t, batch, n2, a, aff, act, var1, var2, pre_q, pre_t); break;
+    default: e = launch_skew<4>(as_stream(stream), blocks, in_q, in_t, out_q, out_t, batch, n2, a, aff, act, var1, var2, pre_q, pre_t); break;
+  }
+  if (e != cudaSuccess) return fail(NTG_ERR_CUDA, std::string("ntg_conv_act_fs: ") + cudaGetErrorString(e));
+  note_launch();
+  return check_launch("ntg_conv_act_fs");
 }
 
 extern "C" int ntg_conv_input_fs(void* stream, const float* x1, const float* x2, int64_t n1,

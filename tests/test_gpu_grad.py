@@ -342,3 +342,38 @@ def test_autotuned_recompute_tile(nt, tmp_path, monkeypatch):
         grads.append(a.grad)
     torch.testing.assert_close(grads[0], grads[1], rtol=1e-4, atol=1e-6)
     tune.clear()
+
+
+def test_conv_act_pool_fused_gradients_32x32(nt):
+    """32 x 32 images: conv + ReLU (+ AvgPool) fused in one pass (ConvActFn with
+    ntg_conv_act_fs and ntg_act_pool_bwd) against central finite differences of the
+    float64 oracle."""
+    rng = np.random.default_rng(14)
+    x1 = rng.standard_normal((1, 32, 32, 2))
+    x2 = rng.standard_normal((2, 32, 32, 2))
+    wq, wt = rng.standard_normal((1, 2)), rng.standard_normal((1, 2))
+
+    def layers(m):
+        return [m.Conv(1, (3, 3), padding='SAME', W_std=1.4, b_std=0.1), m.Relu(),
+                m.Conv(1, (3, 3), padding='SAME', W_std=1.3, b_std=0.0), m.Relu(),
+                m.AvgPool((2, 2), (2, 2)), m.Conv(1, (3, 3), padding='SAME', W_std=1.2),
+                m.Erf(), m.GlobalAvgPool(), m.Dense(1, 1.1, 0.05)]
+
+    def loss_oracle(a, b):
+        q, t = o.serial(*layers(o))(a, b, ('nngp', 'ntk'))
+        return float(np.sum(wq * q) + np.sum(wt * t))
+
+    t1 = torch.tensor(x1, dtype=torch.float32, device='cuda', requires_grad=True)
+    t2 = torch.tensor(x2, dtype=torch.float32, device='cuda', requires_grad=True)
+    q, t = nt.stax.serial(*layers(nt.stax))[2](t1, t2, ('nngp', 'ntk'))
+    loss = (torch.from_numpy(wq).float().cuda() * q).sum() + \
+        (torch.from_numpy(wt).float().cuda() * t).sum()
+    loss.backward()
+    g1, g2 = t1.grad.cpu().numpy(), t2.grad.cpu().numpy()
+    scale = max(np.abs(g1).max(), np.abs(g2).max())
+    for idx in [(0, 0, 0, 0), (0, 13, 21, 1), (0, 31, 31, 0)]:
+        want = fd(lambda a: loss_oracle(a, x2), x1, idx)
+        assert abs(g1[idx] - want) < 3e-3 * scale, (idx, g1[idx], want)
+    for idx in [(1, 7, 30, 1)]:
+        want = fd(lambda b: loss_oracle(x1, b), x2, idx)
+        assert abs(g2[idx] - want) < 3e-3 * scale, (idx, g2[idx], want)
