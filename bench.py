@@ -347,7 +347,8 @@ def stencil_roofline(torch, O, dev, pairs=256, reps=4):
             'achieved': round(gbs, 1), 'unit': 'GB/s'}
 
 
-def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=64, precision='fp32', reps=2):
+def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=64, precision='fp32', reps=2,
+                   tile=None):
     """Kernel-ridge loss of the Myrtle-5 NTK, ||y_t - K_ts (K_ss + 1e-6 tr(K_ss)/n I)^-1 y_s||^2,
     and its gradient with respect to the support set x_s (forward through nt.batch's fused
     grid, backward through its checkpointed tiles and the hand-written adjoints; the solve
@@ -359,7 +360,7 @@ def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=64, precision='fp32', 
     ys = torch.nn.functional.one_hot(torch.randint(0, 10, (n_s,), generator=g), 10).float().cuda()
     yt = torch.nn.functional.one_hot(torch.randint(0, 10, (n_t,), generator=g), 10).float().cuda()
     xt = xd[:n_t].contiguous()
-    batched = nt.batch(kf, batch_size=bs)
+    batched = nt.batch(kf, batch_size=bs, recompute_tile=tile)
     ts, grad = [], None
     for i in range(reps + 1):
         xs = xd[1000:1000 + n_s].clone().requires_grad_(True)
@@ -377,7 +378,8 @@ def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=64, precision='fp32', 
         grad = xs.grad
     ms = statistics.mean(ts)
     entries = n_s * n_s + n_t * n_s
-    tile = nt.tune.recompute_tile(kf, tuple(xs.shape), precision)
+    if tile is None:
+        tile = nt.tune.recompute_tile(kf, tuple(xs.shape), precision)
     return {'ms': round(ms, 2), 'entries': entries,
             'entries_per_s': round(entries / (ms / 1e3), 1), 'precision': precision,
             'recompute_tile': min(tile, bs),
@@ -594,13 +596,14 @@ def profile_stencil(pairs: int):
 
 
 def profile_fwd_bwd(n_s: int):
-    """The fwd+bwd measurement alone: x_s [n_s], x_t [2 n_s], batch_size n_s (launch lists)."""
+    """The fwd+bwd measurement alone: x_s [n_s], x_t [2 n_s], batch_size and recompute tile n_s
+    (no autotuning probes in the launch list)."""
     import torch
     import nt_gb300 as nt
     from nt_gb300 import stax
     _, _, kf = stax.serial(*myrtle5(stax))
     x = torch.from_numpy(make_inputs(2000)).cuda()
-    r, _ = fwd_bwd_timing(torch, nt, kf, x, n_t=2 * n_s, n_s=n_s, bs=n_s, reps=1)
+    r, _ = fwd_bwd_timing(torch, nt, kf, x, n_t=2 * n_s, n_s=n_s, bs=n_s, reps=1, tile=n_s)
     print(json.dumps({'profile_fwd_bwd': n_s, **r}))
 
 
