@@ -196,6 +196,62 @@ __device__ __forceinline__ void act_vjp_fast(const ntg_act_t& act, const ActC& c
   }
 }
 
+// act_vjp_fast's ABRelu branch on a packed pair of entries (the f32x2 datapath
+// for the products and sums, scalar square roots, reciprocals and selects).
+__device__ __forceinline__ void abrelu_vjp2(const ActC& c, P2 q, P2 t, P2 v1, P2 v2, P2 gq,
+                                            P2 gt, P2& oq, P2& ot, P2& ov1, P2& ov2) {
+  const float tol = 1e-30f;
+  const P2 pr = mul2(v1, v2), qq = mul2(q, q);
+  P2 d = sub2(pr, qq);
+  if (c.comp) {
+    const P2 m1 = p2s(-1.f);
+    const P2 pe = fma2(v1, v2, mul2(pr, m1)), qe = fma2(q, q, mul2(qq, m1));
+    d = add2(d, sub2(pe, qe));
+  }
+  float d0, d1, q0, q1;
+  p2u(d, d0, d1);
+  p2u(q, q0, q1);
+  const float s0 = sqrt_approx(fmaxf(d0, 0.f)), s1 = sqrt_approx(fmaxf(d1, 0.f));
+  const P2 sp = p2(s0, s1);
+  const P2 den2 = fma2(sp, sp, qq);
+  float e0, e1;
+  p2u(den2, e0, e1);
+  const float hd0 = sqrt_approx(e0) + fabsf(q0), hd1 = sqrt_approx(e1) + fabsf(q1);
+  const P2 r = mul2(sp, p2(rcp_approx(hd0), rcp_approx(hd1)));
+  const P2 z = mul2(r, r);
+  P2 pp = fma2(p2s(-0.00405457f), z, p2s(0.02186296f));
+  pp = fma2(pp, z, p2s(-0.05591233f));
+  pp = fma2(pp, z, p2s(0.09642197f));
+  pp = fma2(pp, z, p2s(-0.13908629f));
+  pp = fma2(pp, z, p2s(0.19946566f));
+  pp = fma2(pp, z, p2s(-0.3332986f));
+  pp = fma2(pp, z, p2s(0.99999934f));
+  pp = mul2(pp, r);
+  float p0, p1;
+  p2u(pp, p0, p1);
+  float th0 = (q0 < 0.f) ? fmaf(-2.f, p0, kPi) : 2.f * p0;
+  float th1 = (q1 < 0.f) ? fmaf(-2.f, p1, kPi) : 2.f * p1;
+  th0 = (hd0 == 0.f) ? 0.5f * kPi : th0;
+  th1 = (hd1 == 0.f) ? 0.5f * kPi : th1;
+  const P2 dot = fma2(p2s(-c.factor), p2(th0, th1), p2s(c.half));
+  const P2 g_dot = fma2(q, gq, mul2(t, gt));
+  P2 g_s = mul2(p2s(c.factor), gq);
+  P2 g_q = mul2(dot, gq);
+  ot = mul2(dot, gt);
+  const P2 g_th = mul2(p2s(-c.factor), g_dot);
+  const P2 inv = p2(rcp_approx(fmaxf(e0, tol)), rcp_approx(fmaxf(e1, tol)));
+  g_s = fma2(mul2(g_th, q), inv, g_s);
+  g_q = fma2(mul2(mul2(g_th, sp), p2s(-1.f)), inv, g_q);
+  float gs0, gs1;
+  p2u(g_s, gs0, gs1);
+  const float gd0 = (d0 > tol) ? 0.5f * gs0 * rsqrt_approx(d0) : 0.f;
+  const float gd1 = (d1 > tol) ? 0.5f * gs1 * rsqrt_approx(d1) : 0.f;
+  const P2 g_d = p2(gd0, gd1);
+  oq = fma2(mul2(p2s(-2.f), q), g_d, g_q);
+  ov1 = mul2(g_d, v2);
+  ov2 = mul2(g_d, v1);
+}
+
 // Activation VJP on full-spatial [B, A, A, C, C] kernels with C a power of two
 // in [4, 32] and A^2 C^2 a multiple of 1024: a CTA takes chunks of 1024
 // consecutive entries (one pair; 4 entries per thread, vector loads). The
@@ -276,11 +332,27 @@ __global__ void __launch_bounds__(kT)
     const float4 V2 = *reinterpret_cast<const float4*>(&sv[cur][1][k2]);
     const float v2[4] = {V2.x, V2.y, V2.z, V2.w};
     float rq[4], rt[4], r2[4], r1 = 0.f;
+    if (act.kind == NTG_ACT_ABRELU) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      float o1;
-      act_vjp_fast(act, ac, qa[k], ta[k], v1, v2[k], ga[k], gb[k], rq[k], rt[k], o1, r2[k]);
-      r1 += o1;
+      for (int h = 0; h < 2; ++h) {
+        P2 oq2, ot2, o12, o22;
+        abrelu_vjp2(ac, p2(qa[2 * h], qa[2 * h + 1]), p2(ta[2 * h], ta[2 * h + 1]), p2s(v1),
+                    p2(v2[2 * h], v2[2 * h + 1]), p2(ga[2 * h], ga[2 * h + 1]),
+                    p2(gb[2 * h], gb[2 * h + 1]), oq2, ot2, o12, o22);
+        float a0, a1;
+        p2u(oq2, rq[2 * h], rq[2 * h + 1]);
+        p2u(ot2, rt[2 * h], rt[2 * h + 1]);
+        p2u(o12, a0, a1);
+        p2u(o22, r2[2 * h], r2[2 * h + 1]);
+        r1 += a0 + a1;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        float o1;
+        act_vjp_fast(act, ac, qa[k], ta[k], v1, v2[k], ga[k], gb[k], rq[k], rt[k], o1, r2[k]);
+        r1 += o1;
+      }
     }
     *reinterpret_cast<float4*>(oq + e) = make_float4(rq[0], rq[1], rq[2], rq[3]);
     if (ot) *reinterpret_cast<float4*>(ot + e) = make_float4(rt[0], rt[1], rt[2], rt[3]);
