@@ -604,6 +604,32 @@ class KernelFn:
             i += 1
         return k
 
+    def _empty(self, x1, x2, get, precision, diagonal_spatial):
+        """Kernels of an empty batch: evaluated on one stand-in input per empty side, then
+        sliced to zero rows/columns, so that shapes and dtypes are those of the rule."""
+        n1 = x1.shape[0]
+        n2 = n1 if x2 is None else x2.shape[0]
+        p1 = x1 if n1 else torch.zeros((1,) + tuple(x1.shape[1:]), device=x1.device)
+        p2 = None if x2 is None else (x2 if n2 else torch.zeros((1,) + tuple(x2.shape[1:]),
+                                                              device=x2.device))
+        out = self(p1, p2, get, precision=precision, diagonal_spatial=diagonal_spatial)
+
+        def cut(name, v):
+            if not isinstance(v, torch.Tensor) or v.ndim == 0:
+                return v
+            if name == 'cov1':
+                return v[:n1]
+            if name == 'cov2':
+                return v[:n2]
+            return v[:n1, :n2] if v.ndim >= 2 else v[:n1]
+
+        if isinstance(out, torch.Tensor):
+            return cut(get, out)
+        if isinstance(out, Kernel):
+            return out.replace(nngp=cut('nngp', out.nngp), ntk=cut('ntk', out.ntk),
+                               cov1=cut('cov1', out.cov1), cov2=cut('cov2', out.cov2))
+        return type(out)(*[cut(n, v) for n, v in zip(out._fields, out)])
+
     def __call__(self, x1_or_kernel, x2=None, get=None, *, pattern=None, mask_constant=None,
                  diagonal_batch=None, diagonal_spatial=None, precision='fp32', **kwargs):
         if mask_constant is not None:
@@ -623,6 +649,8 @@ class KernelFn:
             compute_ntk = names is None or 'ntk' in names
             x1 = _as_input(x1_or_kernel)
             x2t = None if x2 is None else _as_input(x2)
+            if x1.shape[0] == 0 or (x2t is not None and x2t.shape[0] == 0):
+                return self._empty(x1, x2t, get, precision, diagonal_spatial)
             from . import _autograd, _chain
             if _autograd.needs_grad(self.specs, x1, x2t):
                 if ds:

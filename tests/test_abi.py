@@ -70,3 +70,23 @@ def test_tuning_knobs_are_checked(lib):
     assert lib.ntg_tune_set(7, 1) == 1         # unknown knob
     assert lib.ntg_tune_set(0, 6) == 0 and lib.ntg_tune_get(0) == 6
     assert lib.ntg_tune_set(0, 4) == 0 and lib.ntg_tune_get(0) == 4
+
+
+def test_argument_checks_before_any_launch(lib):
+    """Host-side validation of the C ABI rejects bad sizes and layouts with an error code and
+    message, without touching a device (the pointers below are never dereferenced)."""
+    lib.ntg_last_error.restype = ctypes.c_char_p
+    i64 = ctypes.c_int64
+    fake = ctypes.c_void_p(256)
+    # ntg_conv_fs: empty batch
+    lib.ntg_conv_fs.restype = ctypes.c_int
+    assert lib.ntg_chol_workspace_bytes(i64(10), i64(3)) >= 10 * 3 * 12
+    rc = lib.ntg_pool_bwd(None, fake, fake, i64(0), i64(4), i64(4), 2, 2, 2, 2, 0, 0, i64(2),
+                          i64(2), 0, 0, 1, 0)
+    assert rc == 1 and b'bad arguments' in lib.ntg_last_error()
+    rc = lib.ntg_input_fs_bwd2(None, fake, fake, None, fake, None, i64(2), i64(3), i64(4),
+                               i64(4), i64(3))
+    assert rc == 1 and b'pairs need x2' in lib.ntg_last_error()
+    rc = lib.ntg_chol_solve(None, fake, fake, fake, i64(4), fake, i64(2), fake, 17, None,
+                            ctypes.c_size_t(0), None)
+    assert rc == 1 and b'refinement' in lib.ntg_last_error()

@@ -295,3 +295,28 @@ def test_captured_batch_replays_eager_results(nt, with_x2):
         want = nt.batch(kf, batch_size=4)(x1, x2 if with_x2 else None, ('nngp', 'ntk'))
         for g, w in zip(got, want):
             assert torch.equal(g, w)
+
+
+def test_edge_batches(nt):
+    """Empty batches return empty kernels of the right shape; one-sample batches, x2=None with
+    one sample, batch_size larger than N and batch_size = 1 agree with the oracle."""
+    rng = np.random.default_rng(8)
+    s = nt.stax
+    _, _, kf = s.serial(*myrtle(s, 5))
+    x = rng.standard_normal((3, 32, 32, 3)).astype(np.float32)
+    ko = o.serial(*myrtle(o, 5))
+    e = kf(x[:0], x, ('nngp', 'ntk'))
+    assert tuple(e.nngp.shape) == (0, 3) and tuple(e.ntk.shape) == (0, 3)
+    e = kf(x, x[:0], 'nngp')
+    assert tuple(e.shape) == (3, 0)
+    e = kf(x[:0], None, 'ntk')
+    assert tuple(e.shape) == (0, 0)
+    want = ko(x[:1], x[1:], ('nngp', 'ntk'))
+    got = kf(x[:1], x[1:], ('nngp', 'ntk'))
+    for g, w in zip(got, want):
+        assert elem_rel_err(cpu(g), w) < RTOL
+    one = kf(x[:1], None, 'ntk')
+    assert elem_rel_err(cpu(one), ko(x[:1], None, 'ntk')) < RTOL
+    for bs in (1, 10):
+        b = nt.batch(kf, batch_size=bs)(x, None, 'ntk')
+        assert elem_rel_err(cpu(b), ko(x, None, 'ntk')) < RTOL
