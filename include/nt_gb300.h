@@ -38,7 +38,14 @@ enum {
   NTG_ERR_NO_DEVICE_SCRATCH = 6
 };
 
-enum { NTG_ACT_NONE = 0, NTG_ACT_ABRELU = 1, NTG_ACT_ERF = 2 };
+enum {
+  NTG_ACT_NONE = 0,
+  NTG_ACT_ABRELU = 1,
+  NTG_ACT_ERF = 2,
+  NTG_ACT_SIN = 3,  /* a sin(b x + c) (Cos: c + pi/2), elementwise.py:275-345 */
+  NTG_ACT_RBF = 4,  /* gamma in `a`, elementwise.py:348-400 */
+  NTG_ACT_GELU = 5  /* elementwise.py:195-272 */
+};
 enum { NTG_PAD_ZERO = 0, NTG_PAD_CIRCULAR = 1 };
 
 /* Activation rule applied to (nngp, ntk) given var1 (first sample) and var2

@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, 'libntgb300.so')
 
 NTG_ACT_NONE, NTG_ACT_ABRELU, NTG_ACT_ERF = 0, 1, 2
+NTG_ACT_SIN, NTG_ACT_RBF, NTG_ACT_GELU = 3, 4, 5
 NTG_PAD_ZERO, NTG_PAD_CIRCULAR = 0, 1
 NTG_TUNE_STENCIL_RING = 0
 CHAIN_MAX_SEG, CHAIN_MAX_LAYERS = 4, 16

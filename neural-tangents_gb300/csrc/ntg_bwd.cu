@@ -933,6 +933,8 @@ extern "C" int ntg_act_bwd(void* stream, const float* q, const float* t, const f
   NTG_REQUIRE(batch > 0 && a > 0 && c > 0, "ntg_act_bwd: bad sizes");
   NTG_REQUIRE(act.kind != NTG_ACT_ABRELU || act.stabilize <= 0.f,
               "ntg_act_bwd: do_stabilize is not differentiable here");
+  if (act.kind != NTG_ACT_NONE && act.kind != NTG_ACT_ABRELU && act.kind != NTG_ACT_ERF)
+    return fail(NTG_ERR_UNSUPPORTED, "ntg_act_bwd: adjoints exist for ABRelu and Erf");
   // variance cotangents are compact [n, A, C] arrays
   VarGrad g1{gvar1, a * c, c, 1}, g2{gvar2, a * c, c, 1};
   const int64_t m = diag_spatial ? a * c : a * a * c * c;
@@ -964,6 +966,8 @@ extern "C" int ntg_act_pool_bwd(void* stream, const float* q, const float* t,
   NTG_REQUIRE(batch > 0 && a > 0 && c > 0, "ntg_act_pool_bwd: bad sizes");
   NTG_REQUIRE(act.kind != NTG_ACT_ABRELU || act.stabilize <= 0.f,
               "ntg_act_pool_bwd: do_stabilize is not differentiable here");
+  if (act.kind != NTG_ACT_NONE && act.kind != NTG_ACT_ABRELU && act.kind != NTG_ACT_ERF)
+    return fail(NTG_ERR_UNSUPPORTED, "ntg_act_pool_bwd: adjoints exist for ABRelu and Erf");
   const int64_t m = a * a * c * c;
   const bool pow2 = c >= 4 && c <= 32 && (c & (c - 1)) == 0;
   const bool aligned = ((reinterpret_cast<uintptr_t>(q) | reinterpret_cast<uintptr_t>(t) |

@@ -142,6 +142,7 @@ struct ActC {
   float f2, h_neg, h_zero;  // 2 factor, half - pi factor, half - pi/2 factor
   float a2, b2, c2;    // Erf: a^2, b^2, c^2
   float stab;
+  float ha2, cos2c;    // Sin: a^2 / 2, cos(2 c) (b^2 in b2); Rbf: gamma in ha2
 };
 
 __device__ __forceinline__ ActC act_consts(const ntg_act_t& act) {
@@ -158,6 +159,8 @@ __device__ __forceinline__ ActC act_consts(const ntg_act_t& act) {
   c.b2 = __fmul_rn(act.b, act.b);
   c.c2 = __fmul_rn(act.c, act.c);
   c.stab = act.stabilize;
+  c.ha2 = act.kind == NTG_ACT_RBF ? act.a : 0.5f * c.a2;
+  c.cos2c = cosf(2.f * act.c);
   return c;
 }
 
@@ -202,6 +205,32 @@ __device__ __forceinline__ void act_apply(const ActC& c, float& q, float& t, flo
     const float dot = __fmul_rn(4.f / kPi, rcp_approx(s));
     q = fmaf(c.a2, qo, c.c2);
     t = __fmul_rn(c.a2, __fmul_rn(__fmul_rn(c.b2, t), dot));
+  } else if (c.kind == NTG_ACT_SIN) {
+    // elementwise.py:303-311: s1 = exp(b^2 (q - sum / 2)), s2 = exp(b^2 (-q - sum / 2)) cos 2c
+    const float sum = v1 + v2;
+    const float s1 = expf(c.b2 * fmaf(-0.5f, sum, q));
+    const float s2 = expf(c.b2 * fmaf(-0.5f, sum, -q)) * c.cos2c;
+    t = t * (c.ha2 * c.b2 * (s1 + s2));
+    q = c.ha2 * (s1 - s2);
+  } else if (c.kind == NTG_ACT_RBF) {
+    // elementwise.py:380-384: q' = exp(gamma (2 q - sum)), ntk' = ntk 2 gamma q'
+    const float qo = expf(c.ha2 * fmaf(2.f, q, -(v1 + v2)));
+    t = t * (2.f * c.ha2 * qo);
+    q = qo;
+  } else if (c.kind == NTG_ACT_GELU) {
+    // elementwise.py:230-250 with prod = v1 v2, prod + 1 = (v1 + 1)(v2 + 1)
+    const float prod = v1 * v2;
+    const float pp1 = (v1 + 1.f) * (v2 + 1.f);
+    const float d2 = pp1 - q * q;
+    const float dl = sqrtf(fmaxf(d2, 0.f));
+    const float ang = atan2_xpos(q, dl);
+    float qo = (q * q + prod * d2) / (pp1 * dl);
+    qo = (qo + q * ang) / (2.f * kPi);
+    qo = fmaf(0.25f, q, qo);
+    float first = 1.f / d2 + (1.f - prod) / pp1 + 1.f;
+    first *= q / dl / (2.f * kPi);
+    t = t * (first + (0.25f + ang / (2.f * kPi)));
+    q = qo;
   }
 }
 

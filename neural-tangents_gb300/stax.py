@@ -103,6 +103,12 @@ def _act_struct(p: dict, ctx: _Ctx, stabilize: float = 0.) -> L.Act:
         return L.Act(L.NTG_ACT_ABRELU, p['a'], p['b'], 0., ctx.compensated, stabilize)
     if p['fn'] == 'erf':
         return L.Act(L.NTG_ACT_ERF, p['a'], p['b'], p['c'], ctx.compensated, 0.)
+    if p['fn'] == 'sin':
+        return L.Act(L.NTG_ACT_SIN, p['a'], p['b'], p['c'], 0, 0.)
+    if p['fn'] == 'rbf':
+        return L.Act(L.NTG_ACT_RBF, p['gamma'], 0., 0., 0, 0.)
+    if p['fn'] == 'gelu':
+        return L.Act(L.NTG_ACT_GELU, 0., 0., 0., 0, 0.)
     raise ValueError(p['fn'])
 
 
@@ -439,6 +445,12 @@ def _apply_spec(spec: LayerSpec, params, x: torch.Tensor) -> torch.Tensor:
     if spec.kind == 'act':
         if p['fn'] == 'abrelu':
             return p['a'] * torch.clamp(x, max=0) + p['b'] * torch.clamp(x, min=0)
+        if p['fn'] == 'sin':
+            return p['a'] * torch.sin(p['b'] * x + p['c'])
+        if p['fn'] == 'rbf':
+            return math.sqrt(2.) * torch.sin(math.sqrt(2. * p['gamma']) * x + math.pi / 4)
+        if p['fn'] == 'gelu':
+            return torch.nn.functional.gelu(x, approximate='tanh' if p['approximate'] else 'none')
         return p['a'] * torch.erf(p['b'] * x) + p['c']
     if spec.kind == 'pool':
         nsp = len(p['window_shape'])
@@ -757,6 +769,31 @@ def Erf(a: float = 1., b: float = 1., c: float = 0.):
     spec = LayerSpec('act', Diagonal(), dict(fn='erf', a=float(a), b=float(b), c=float(c)),
                      lambda sh: sh)
     return _make_layer(spec, f'Erf({a}, {b}, {c})')
+
+
+def Sin(a: float = 1., b: float = 1., c: float = 0.):
+    """elementwise.py:275-328: a sin(b x + c)."""
+    spec = LayerSpec('act', Diagonal(), dict(fn='sin', a=float(a), b=float(b), c=float(c)),
+                     lambda sh: sh)
+    return _make_layer(spec, f'Sin({a}, {b}, {c})')
+
+
+def Cos(a: float = 1., b: float = 1., c: float = 0.):
+    """elementwise.py:331-345: Sin with the phase shifted by pi / 2."""
+    return Sin(a=a, b=b, c=c + math.pi / 2)
+
+
+def Rbf(gamma: float = 1.0):
+    """elementwise.py:348-400: sqrt(2) sin(sqrt(2 gamma) x + pi / 4)."""
+    spec = LayerSpec('act', Diagonal(), dict(fn='rbf', gamma=float(gamma)), lambda sh: sh)
+    return _make_layer(spec, f'Rbf({gamma})')
+
+
+def Gelu(approximate: bool = False):
+    """elementwise.py:195-272 (the kernel does not depend on `approximate`)."""
+    spec = LayerSpec('act', Diagonal(), dict(fn='gelu', approximate=bool(approximate)),
+                     lambda sh: sh)
+    return _make_layer(spec, 'Gelu')
 
 
 def _pool(kind, window_shape, strides, padding, normalize_edges, batch_axis, channel_axis):

@@ -17,6 +17,7 @@ What it restates (paths are inside the neural-tangents 0.6.6 project):
   ``:1631-1664`` / ``:3499-3572`` pooling, ``:1771-1801`` global pooling,
   ``:1865-1899`` Flatten.
 * ``neural_tangents/_src/stax/elementwise.py:67-112`` Erf, ``:423-477`` ABRelu,
+  ``:195-272`` Gelu, ``:275-345`` Sin / Cos, ``:348-400`` Rbf,
   ``:1250-1310`` ``_elementwise`` / ``_sqrt`` / ``_arctan2``.
 * ``neural_tangents/_src/utils/kernel.py:426-441`` Kernel scalar algebra.
 * ``neural_tangents/_src/predict.py:71-278`` ``gradient_descent_mse``,
@@ -435,21 +436,21 @@ def _get_diagonal(cov, diagonal_spatial):
     return diagonal_between(cov, 1)
 
 
-def _outer_prods(cov1, cov2, diagonal_spatial):
-    """requirements.py:1077-1117 with op=mul, diagonal batch."""
+def _outer_prods(cov1, cov2, diagonal_spatial, op=np.multiply):
+    """requirements.py:1077-1117 (op = mul or add), diagonal batch."""
     d1 = _get_diagonal(cov1, diagonal_spatial)
     d2 = _get_diagonal(cov2, diagonal_spatial)
     if diagonal_spatial:
         # requirements.py:1108: the outer product runs over the batch axis only.
-        prod12 = d1[:, None] * (d1 if d2 is None else d2)[None, :]
+        prod12 = op(d1[:, None], (d1 if d2 is None else d2)[None, :])
     else:
-        prod12 = outer_prod(d1, d1 if d2 is None else d2, 0)
+        prod12 = outer_prod(d1, d1 if d2 is None else d2, 0, op)
     if diagonal_spatial:
-        prod11 = d1 * d1
-        prod22 = None if d2 is None else d2 * d2
+        prod11 = op(d1, d1)
+        prod22 = None if d2 is None else op(d2, d2)
     else:
-        prod11 = outer_prod(d1, d1, 1)
-        prod22 = None if d2 is None else outer_prod(d2, d2, 1)
+        prod11 = outer_prod(d1, d1, 1, op)
+        prod22 = None if d2 is None else outer_prod(d2, d2, 1, op)
     return prod11, prod12, (prod11 if prod22 is None else prod22)
 
 
@@ -558,6 +559,106 @@ def Erf(a=1., b=1., c=0.):
         k = k.replace(cov1=cov1, nngp=nngp, cov2=cov2, ntk=ntk)
         return k.mul(a).add(c)
     return _elementwise(f'Erf({a},{b},{c})', rule)
+
+
+def Sin(a=1., b=1., c=0.):
+    """elementwise.py:275-328: a sin(b x + c)."""
+    def rule(k: Kernel) -> Kernel:
+        cov1, nngp, cov2, ntk = k.cov1, k.nngp, k.cov2, k.ntk
+        sum11, sum12, sum22 = _outer_prods(cov1, cov2, k.diagonal_spatial, np.add)
+        half_a_square = a ** 2 / 2.
+
+        def nngp_ntk_fn(q, sum_, t=None):
+            s1 = np.exp(b ** 2 * (-0.5 * sum_ + q))
+            s2 = np.exp(b ** 2 * (-0.5 * sum_ - q)) * np.cos(2 * c)
+            q_out = half_a_square * (s1 - s2)
+            if t is not None:
+                t = t * (half_a_square * b ** 2 * (s1 + s2))
+            return q_out, t
+
+        def nngp_fn_diag(q):
+            return half_a_square * (1. - np.exp(-2 * b ** 2 * q) * np.cos(2 * c))
+
+        nngp, ntk = nngp_ntk_fn(nngp, sum12, ntk)
+        if k.diagonal_spatial:
+            cov1 = nngp_fn_diag(cov1)
+            cov2 = None if cov2 is None else nngp_fn_diag(cov2)
+        else:
+            cov1, _ = nngp_ntk_fn(cov1, sum11)
+            if cov2 is not None:
+                cov2, _ = nngp_ntk_fn(cov2, sum22)
+        return k.replace(cov1=cov1, nngp=nngp, cov2=cov2, ntk=ntk)
+    return _elementwise(f'Sin({a},{b},{c})', rule)
+
+
+def Cos(a=1., b=1., c=0.):
+    """elementwise.py:331-345: Sin with the phase shifted by pi / 2."""
+    return Sin(a=a, b=b, c=c + np.pi / 2)
+
+
+def Rbf(gamma=1.0):
+    """elementwise.py:348-400: dual activation of the normalised RBF kernel."""
+    def rule(k: Kernel) -> Kernel:
+        cov1, nngp, cov2, ntk = k.cov1, k.nngp, k.cov2, k.ntk
+        sum11, sum12, sum22 = _outer_prods(cov1, cov2, k.diagonal_spatial, np.add)
+
+        def nngp_ntk_fn(q, sum_, t=None):
+            q_out = np.exp(gamma * (-sum_ + 2 * q))
+            if t is not None:
+                t = t * (2 * gamma * q_out)
+            return q_out, t
+
+        nngp, ntk = nngp_ntk_fn(nngp, sum12, ntk)
+        if k.diagonal_spatial:
+            cov1 = np.ones_like(cov1)
+            cov2 = None if cov2 is None else np.ones_like(cov2)
+        else:
+            cov1, _ = nngp_ntk_fn(cov1, sum11)
+            if cov2 is not None:
+                cov2, _ = nngp_ntk_fn(cov2, sum22)
+        return k.replace(cov1=cov1, nngp=nngp, cov2=cov2, ntk=ntk)
+    return _elementwise(f'Rbf({gamma})', rule)
+
+
+def Gelu(approximate=False):
+    """elementwise.py:195-272 (the kernel does not depend on `approximate`)."""
+    def rule(k: Kernel) -> Kernel:
+        cov1, nngp, cov2, ntk = k.cov1, k.nngp, k.cov2, k.ntk
+        p1_11, p1_12, p1_22 = _outer_prods(cov1 + 1, None if cov2 is None else cov2 + 1,
+                                           k.diagonal_spatial)
+        p11, p12, p22 = _outer_prods(cov1, cov2, k.diagonal_spatial)
+
+        def nngp_ntk_fn(q, prod, prod_plus_1, t=None):
+            delta_squared = prod_plus_1 - q ** 2
+            delta = _sqrt(delta_squared)
+            angles = np.arctan2(q, delta)
+            q_out = (q ** 2 + prod * delta_squared) / (prod_plus_1 * delta)
+            q_out = q_out + q * angles
+            q_out = q_out / (2 * np.pi)
+            q_out = q_out + 0.25 * q
+            if t is not None:
+                second = 0.25 + angles / (2 * np.pi)
+                first = 1 / delta_squared + (1 - prod) / prod_plus_1 + 1
+                first = first * (q / delta / (2. * np.pi))
+                t = t * (first + second)
+            return q_out, t
+
+        def nngp_fn_diag(q):
+            root = np.sqrt(1. + 2. * q)
+            out = q / ((q + 1.) * root)
+            out = out + np.arctan2(q, root) / 2
+            return (out / np.pi + 0.25) * q
+
+        nngp, ntk = nngp_ntk_fn(nngp, p12, p1_12, ntk)
+        if k.diagonal_spatial:
+            cov1 = nngp_fn_diag(cov1)
+            cov2 = None if cov2 is None else nngp_fn_diag(cov2)
+        else:
+            cov1, _ = nngp_ntk_fn(cov1, p11, p1_11)
+            if cov2 is not None:
+                cov2, _ = nngp_ntk_fn(cov2, p22, p1_22)
+        return k.replace(cov1=cov1, nngp=nngp, cov2=cov2, ntk=ntk)
+    return _elementwise('Gelu', rule)
 
 
 def Identity():

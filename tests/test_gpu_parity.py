@@ -320,3 +320,34 @@ def test_edge_batches(nt):
     for bs in (1, 10):
         b = nt.batch(kf, batch_size=bs)(x, None, 'ntk')
         assert elem_rel_err(cpu(b), ko(x, None, 'ntk')) < RTOL
+
+
+@pytest.mark.parametrize('act', ['gelu', 'sin', 'cos', 'rbf'])
+def test_more_dual_activations_vs_oracle(nt, act, cifar_like):
+    """Gelu, Sin, Cos and Rbf (elementwise.py:195-400) as epilogues of the Dense rule (flat
+    inputs), of the materialised conv rule, and inside the fused whole-network kernel."""
+    def mk(m):
+        return {'gelu': m.Gelu(), 'sin': m.Sin(1.2, 0.8, 0.3), 'cos': m.Cos(0.9, 1.1, -0.2),
+                'rbf': m.Rbf(0.4)}[act]
+
+    rng = np.random.default_rng(33)
+    xf1, xf2 = rng.standard_normal((6, 20)), rng.standard_normal((5, 20))
+    got, want = both(nt, lambda m: [m.Dense(8, 1.3, 0.1), mk(m), m.Dense(1, 1.1, 0.05)],
+                     xf1, xf2)
+    for g, w in zip(got, want):
+        assert elem_rel_err(g, w) < RTOL
+    xc1, xc2 = rng.standard_normal((2, 6, 6, 2)), rng.standard_normal((3, 6, 6, 2))
+    got, want = both(nt, lambda m: [m.Conv(2, (3, 3), padding='SAME', W_std=1.2, b_std=0.1),
+                                    mk(m), m.GlobalAvgPool(), m.Dense(1, 1.1, 0.)], xc1, xc2)
+    for g, w in zip(got, want):
+        assert rel_err(g, w) < RTOL
+    x1, x2 = cifar_like
+    lay = lambda m: [m.Conv(1, (3, 3), padding='SAME', W_std=1.3), mk(m),
+                     m.AvgPool((2, 2), (2, 2)), m.Conv(1, (3, 3), padding='SAME', W_std=1.2),
+                     mk(m), m.GlobalAvgPool(), m.Dense(1, 1.0, 0.)]
+    from nt_gb300 import _chain
+    kf = nt.stax.serial(*lay(nt.stax))[2]
+    assert _chain.plan_chain(kf.specs, x1.shape, False) is not None
+    got, want = both(nt, lay, x1[:2], x2, get=('nngp', 'ntk'))
+    for g, w in zip(got, want):
+        assert elem_rel_err(g, w) < RTOL

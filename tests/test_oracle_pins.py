@@ -271,3 +271,47 @@ def test_gp_inference_matches_ensemble_and_ntkgp_is_nngp_with_ntk():
     with pytest.raises(ValueError):
         o.gp_inference({'ntk': k_dd['ntk']}, y_train)(get='ntk', k_test_train={'ntk': k_td['ntk']},
                                                       k_test_test=k_tt['nngp'])
+
+
+# ---------------------------------------------------------------------------
+# Gelu / Sin / Cos / Rbf (elementwise.py:195-400): Gaussian expectations by Monte Carlo,
+# the check of the reference's elementwise tests (tests/stax/elementwise_test.py)
+# ---------------------------------------------------------------------------
+def _phi_pairs():
+    from scipy.special import ndtr
+    r2 = np.sqrt(2.)
+    return [
+        (o.Sin(1.3, 0.7, 0.2), lambda x: 1.3 * np.sin(0.7 * x + 0.2),
+         lambda x: 1.3 * 0.7 * np.cos(0.7 * x + 0.2)),
+        (o.Cos(0.9, 1.1, -0.3), lambda x: 0.9 * np.cos(1.1 * x - 0.3),
+         lambda x: -0.9 * 1.1 * np.sin(1.1 * x - 0.3)),
+        (o.Rbf(0.6), lambda x: r2 * np.sin(np.sqrt(1.2) * x + np.pi / 4),
+         lambda x: r2 * np.sqrt(1.2) * np.cos(np.sqrt(1.2) * x + np.pi / 4)),
+        (o.Gelu(), lambda x: x * ndtr(x),
+         lambda x: ndtr(x) + x * np.exp(-x * x / 2) / np.sqrt(2 * np.pi)),
+    ]
+
+
+@pytest.mark.parametrize('case', range(4))
+def test_dual_activations_match_gaussian_expectations(case):
+    layer, phi, dphi = _phi_pairs()[case]
+    rng = np.random.default_rng(40 + case)
+    x = rng.standard_normal((2, 6))
+    kf = o.serial(o.Dense(1, 1.1, 0.3), layer)
+    q, t = kf(x[:1], x[1:], ('nngp', 'ntk'))
+    c1, c2 = kf(x[:1], None, 'nngp'), kf(x[1:], None, 'nngp')
+    pre = o.serial(o.Dense(1, 1.1, 0.3))
+    v1 = float(pre(x[:1], None, 'nngp')[0, 0])
+    v2 = float(pre(x[1:], None, 'nngp')[0, 0])
+    qq = float(pre(x[:1], x[1:], 'nngp')[0, 0])
+    tt = float(pre(x[:1], x[1:], 'ntk')[0, 0])
+    n = 4_000_000
+    z = rng.standard_normal((n, 2))
+    l = np.linalg.cholesky(np.array([[v1, qq], [qq, v2]]))
+    u = z @ l.T
+    for got, samples in ((q[0, 0], phi(u[:, 0]) * phi(u[:, 1])),
+                         (t[0, 0], tt * dphi(u[:, 0]) * dphi(u[:, 1])),
+                         (c1[0, 0], phi(np.sqrt(v1) * z[:, 0]) ** 2),
+                         (c2[0, 0], phi(np.sqrt(v2) * z[:, 1]) ** 2)):
+        mean, err = samples.mean(), samples.std() / np.sqrt(n)
+        assert abs(got - mean) < 6 * err + 1e-12, (got, mean, err)
