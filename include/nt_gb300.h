@@ -42,7 +42,8 @@ enum {
   NTG_ACT_NONE = 0,
   NTG_ACT_ABRELU = 1,
   NTG_ACT_ERF = 2,
-  NTG_ACT_SIN = 3,  /* a sin(b x + c) (Cos: c + pi/2), elementwise.py:275-345 */
+  NTG_ACT_SIN = 3,  /* a sin(b x + c) (Cos: c + pi/2), elementwise.py:275-345; the `c`
+                       field of ntg_act_t carries cos(2 c) */
   NTG_ACT_RBF = 4,  /* gamma in `a`, elementwise.py:348-400 */
   NTG_ACT_GELU = 5  /* elementwise.py:195-272 */
 };

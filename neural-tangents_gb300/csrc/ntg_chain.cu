@@ -169,7 +169,7 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
           apply_affine(af, cq, ct, true, q, t, 1.f / 9.f);
           if (ac.kind != NTG_ACT_NONE && on) {
             const int i1 = p * S + c0 + u, i2 = (p + delta) * S + wp[u];
-            act_apply(ac, q, t, vm[i1], vm[S * S + i2], vm[2 * S * S + i1], vm[3 * S * S + i2]);
+            act_apply<false>(ac, q, t, vm[i1], vm[S * S + i2], vm[2 * S * S + i1], vm[3 * S * S + i2]);
           }
           oq[u] = q;
           ot[u] = t;
@@ -333,8 +333,8 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
             p2u(t, ta, tb);
             p2u(v1, va, vb);
             p2u(sv1, sa, sb);
-            act_apply(ac, qa, ta, va, v2r[wp0], sa, s2r[wp0]);
-            act_apply(ac, qb, tb, vb, v2r[wp1], sb, s2r[wp1]);
+            act_apply<false>(ac, qa, ta, va, v2r[wp0], sa, s2r[wp0]);
+            act_apply<false>(ac, qb, tb, vb, v2r[wp1], sb, s2r[wp1]);
             q = p2(qa, qb);
             t = p2(ta, tb);
           }
@@ -612,6 +612,10 @@ int launch_chain(const char* who, void* stream, const ntg_chain_t* prog, const f
     nl += pg.nconv[sg];
   }
   NTG_REQUIRE(nl <= NTG_CHAIN_MAX_LAYERS, w + ": too many layers");
+  for (int l = 0; l < nl; ++l)
+    NTG_REQUIRE(pg.act[l].kind == NTG_ACT_NONE || pg.act[l].kind == NTG_ACT_ABRELU ||
+                    pg.act[l].kind == NTG_ACT_ERF,
+                w + ": the fused chain carries the ABRelu and Erf rules only");
   NTG_REQUIRE(pg.readout == 0 || pg.readout == 1, w + ": readout must be 0 or 1");
   NTG_REQUIRE(n1 > 0 && n2 > 0 && r0 >= 0 && c0 >= 0, w + ": bad tile");
   NTG_REQUIRE(sym ? ld_out >= (r0 + n1 > c0 + n2 ? r0 + n1 : c0 + n2) : ld_out >= n2,

@@ -140,9 +140,8 @@ struct ActC {
   int comp;
   float factor, half;  // ABRelu: (a-b)^2 / (2 pi), (a^2 + b^2) / 2
   float f2, h_neg, h_zero;  // 2 factor, half - pi factor, half - pi/2 factor
-  float a2, b2, c2;    // Erf: a^2, b^2, c^2
+  float a2, b2, c2;    // Erf: a^2, b^2, c^2; Sin: a^2 / 2, b^2, cos(2 c); Rbf: gamma in a2
   float stab;
-  float ha2, cos2c;    // Sin: a^2 / 2, cos(2 c) (b^2 in b2); Rbf: gamma in ha2
 };
 
 __device__ __forceinline__ ActC act_consts(const ntg_act_t& act) {
@@ -159,9 +158,46 @@ __device__ __forceinline__ ActC act_consts(const ntg_act_t& act) {
   c.b2 = __fmul_rn(act.b, act.b);
   c.c2 = __fmul_rn(act.c, act.c);
   c.stab = act.stabilize;
-  c.ha2 = act.kind == NTG_ACT_RBF ? act.a : 0.5f * c.a2;
-  c.cos2c = cosf(2.f * act.c);
+  if (act.kind == NTG_ACT_SIN) {
+    c.a2 = 0.5f * c.a2;
+    c.c2 = act.c;  // the caller passes cos(2 c)
+  } else if (act.kind == NTG_ACT_RBF) {
+    c.a2 = act.a;
+  }
   return c;
+}
+
+// Sin / Rbf / Gelu rules. Kernels instantiate act_apply<false> to leave them out:
+// compiled into the fused chain kernel, their library calls slow its ReLU path.
+__device__ __forceinline__ void act_apply_rare(const ActC& c, float& q, float& t, float v1,
+                                            float v2) {
+  if (c.kind == NTG_ACT_SIN) {
+    // elementwise.py:303-311: s1 = exp(b^2 (q - sum / 2)), s2 = exp(b^2 (-q - sum / 2)) cos 2c
+    const float sum = v1 + v2;
+    const float s1 = expf(c.b2 * fmaf(-0.5f, sum, q));
+    const float s2 = expf(c.b2 * fmaf(-0.5f, sum, -q)) * c.c2;
+    t = t * (c.a2 * c.b2 * (s1 + s2));
+    q = c.a2 * (s1 - s2);
+  } else if (c.kind == NTG_ACT_RBF) {
+    // elementwise.py:380-384: q' = exp(gamma (2 q - sum)), ntk' = ntk 2 gamma q'
+    const float qo = expf(c.a2 * fmaf(2.f, q, -(v1 + v2)));
+    t = t * (2.f * c.a2 * qo);
+    q = qo;
+  } else if (c.kind == NTG_ACT_GELU) {
+    // elementwise.py:230-250 with prod = v1 v2, prod + 1 = (v1 + 1)(v2 + 1)
+    const float prod = v1 * v2;
+    const float pp1 = (v1 + 1.f) * (v2 + 1.f);
+    const float d2 = pp1 - q * q;
+    const float dl = sqrtf(fmaxf(d2, 0.f));
+    const float ang = atan2_xpos(q, dl);
+    float qo = (q * q + prod * d2) / (pp1 * dl);
+    qo = (qo + q * ang) / (2.f * kPi);
+    qo = fmaf(0.25f, q, qo);
+    float first = 1.f / d2 + (1.f - prod) / pp1 + 1.f;
+    first *= q / dl / (2.f * kPi);
+    t = t * (first + (0.25f + ang / (2.f * kPi)));
+    q = qo;
+  }
 }
 
 // ABRelu(a, b) rule, elementwise.py:447-455:
@@ -174,6 +210,7 @@ __device__ __forceinline__ ActC act_consts(const ntg_act_t& act) {
 // Erf(a, b, c) rule, elementwise.py:67-112 (k *= b first, a*k + c last):
 //   prod = (1 + 2 v1)(1 + 2 v2); s = sqrt(max(prod - 4q^2, 0));
 //   q' = 2/pi atan2(2q, s); ntk' = ntk (4/pi) / s
+template <bool RARE = true>
 __device__ __forceinline__ void act_apply(const ActC& c, float& q, float& t, float v1, float v2,
                                           float sv1, float sv2) {
   if (c.kind == NTG_ACT_ABRELU) {
@@ -205,32 +242,8 @@ __device__ __forceinline__ void act_apply(const ActC& c, float& q, float& t, flo
     const float dot = __fmul_rn(4.f / kPi, rcp_approx(s));
     q = fmaf(c.a2, qo, c.c2);
     t = __fmul_rn(c.a2, __fmul_rn(__fmul_rn(c.b2, t), dot));
-  } else if (c.kind == NTG_ACT_SIN) {
-    // elementwise.py:303-311: s1 = exp(b^2 (q - sum / 2)), s2 = exp(b^2 (-q - sum / 2)) cos 2c
-    const float sum = v1 + v2;
-    const float s1 = expf(c.b2 * fmaf(-0.5f, sum, q));
-    const float s2 = expf(c.b2 * fmaf(-0.5f, sum, -q)) * c.cos2c;
-    t = t * (c.ha2 * c.b2 * (s1 + s2));
-    q = c.ha2 * (s1 - s2);
-  } else if (c.kind == NTG_ACT_RBF) {
-    // elementwise.py:380-384: q' = exp(gamma (2 q - sum)), ntk' = ntk 2 gamma q'
-    const float qo = expf(c.ha2 * fmaf(2.f, q, -(v1 + v2)));
-    t = t * (2.f * c.ha2 * qo);
-    q = qo;
-  } else if (c.kind == NTG_ACT_GELU) {
-    // elementwise.py:230-250 with prod = v1 v2, prod + 1 = (v1 + 1)(v2 + 1)
-    const float prod = v1 * v2;
-    const float pp1 = (v1 + 1.f) * (v2 + 1.f);
-    const float d2 = pp1 - q * q;
-    const float dl = sqrtf(fmaxf(d2, 0.f));
-    const float ang = atan2_xpos(q, dl);
-    float qo = (q * q + prod * d2) / (pp1 * dl);
-    qo = (qo + q * ang) / (2.f * kPi);
-    qo = fmaf(0.25f, q, qo);
-    float first = 1.f / d2 + (1.f - prod) / pp1 + 1.f;
-    first *= q / dl / (2.f * kPi);
-    t = t * (first + (0.25f + ang / (2.f * kPi)));
-    q = qo;
+  } else if (RARE && c.kind >= NTG_ACT_SIN) {
+    act_apply_rare(c, q, t, v1, v2);
   }
 }
 
@@ -281,7 +294,7 @@ __device__ __forceinline__ void abrelu2(const ActC& c, P2& q, P2& t, P2 v1, P2 v
 __device__ __forceinline__ float sqrt_var(float v) { return sqrt_approx(fmaxf(v, 0.f)); }
 
 __device__ __forceinline__ void act_apply(const ActC& c, float& q, float& t, float v1, float v2) {
-  act_apply(c, q, t, v1, v2, sqrt_var(v1), sqrt_var(v2));
+  act_apply<true>(c, q, t, v1, v2, sqrt_var(v1), sqrt_var(v2));
 }
 
 // Affine rule on an unscaled propagated sum u (nngp) and u_t (ntk) whose

@@ -103,8 +103,8 @@ def _act_struct(p: dict, ctx: _Ctx, stabilize: float = 0.) -> L.Act:
         return L.Act(L.NTG_ACT_ABRELU, p['a'], p['b'], 0., ctx.compensated, stabilize)
     if p['fn'] == 'erf':
         return L.Act(L.NTG_ACT_ERF, p['a'], p['b'], p['c'], ctx.compensated, 0.)
-    if p['fn'] == 'sin':
-        return L.Act(L.NTG_ACT_SIN, p['a'], p['b'], p['c'], 0, 0.)
+    if p['fn'] == 'sin':  # the kernels take cos(2 c), computed here in double precision
+        return L.Act(L.NTG_ACT_SIN, p['a'], p['b'], math.cos(2. * p['c']), 0, 0.)
     if p['fn'] == 'rbf':
         return L.Act(L.NTG_ACT_RBF, p['gamma'], 0., 0., 0, 0.)
     if p['fn'] == 'gelu':

@@ -325,7 +325,8 @@ def test_edge_batches(nt):
 @pytest.mark.parametrize('act', ['gelu', 'sin', 'cos', 'rbf'])
 def test_more_dual_activations_vs_oracle(nt, act, cifar_like):
     """Gelu, Sin, Cos and Rbf (elementwise.py:195-400) as epilogues of the Dense rule (flat
-    inputs), of the materialised conv rule, and inside the fused whole-network kernel."""
+    inputs) and of the materialised conv rule, on 6x6 and on 32x32 images (the latter take
+    the per-layer kernels: the fused whole-network kernel carries ReLU and Erf only)."""
     def mk(m):
         return {'gelu': m.Gelu(), 'sin': m.Sin(1.2, 0.8, 0.3), 'cos': m.Cos(0.9, 1.1, -0.2),
                 'rbf': m.Rbf(0.4)}[act]
@@ -347,7 +348,7 @@ def test_more_dual_activations_vs_oracle(nt, act, cifar_like):
                      mk(m), m.GlobalAvgPool(), m.Dense(1, 1.0, 0.)]
     from nt_gb300 import _chain
     kf = nt.stax.serial(*lay(nt.stax))[2]
-    assert _chain.plan_chain(kf.specs, x1.shape, False) is not None
+    assert _chain.plan_chain(kf.specs, x1.shape, False) is None
     got, want = both(nt, lay, x1[:2], x2, get=('nngp', 'ntk'))
     for g, w in zip(got, want):
         assert elem_rel_err(g, w) < RTOL
