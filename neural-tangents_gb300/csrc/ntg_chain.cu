@@ -569,11 +569,9 @@ __global__ void __launch_bounds__(NT, 1)
     j = pair - i * n2;
   }
   const int64_t gi = r0 + i, gj = c0 + j;
-  if (sym == 0)
-    chain_pair<N0>(pg, x1, x2, gi, gj, var1, var2, out_q, out_t, i * ld_out + j, -1);
-  else
-    chain_pair<N0>(pg, x1, x2, gi, gj, var1, var2, out_q, out_t, gi * ld_out + gj,
-                   gi != gj ? gj * ld_out + gi : -1);
+  const int64_t o1 = sym ? gi * ld_out + gj : i * ld_out + j;
+  const int64_t o2 = (sym && gi != gj) ? gj * ld_out + gi : -1;
+  chain_pair<N0>(pg, x1, x2, gi, gj, var1, var2, out_q, out_t, o1, o2);
 }
 
 size_t chain_smem_bytes(const ntg_chain_t& pg) {
