@@ -387,13 +387,18 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
   __syncthreads();
 }
 
-template <int S, bool LAST>
+// NCT >= 0: the segment's conv count is known at compile time (one instantiation).
+template <int S, bool LAST, int NCT = -1>
 __device__ __forceinline__ void process_pooled_line(ChainCtx& cx, const ntg_chain_t& pg, int ncv,
                                                     int lbase, const float* vmaps,
                                                     const float* in_slots, float* out_slots,
                                                     int m) {
   const float* q = in_slots + (2 * (m & 1)) * (S * S * S);
   const float* t = q + S * S * S;
+  if constexpr (NCT >= 0) {
+    process_line<S, NCT, false, LAST>(cx, pg, lbase, vmaps, out_slots, m, q, t);
+    return;
+  }
   switch (ncv) {
     case 0: process_line<S, 0, false, LAST>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
     case 1: process_line<S, 1, false, LAST>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
@@ -416,7 +421,9 @@ __device__ __forceinline__ void tri_pair(int64_t p, int64_t n, int64_t& i, int64
   j = r + (p - start(r));
 }
 
-template <int N0>
+// NSEG > 0: segment count and conv counts N1, N2 fixed at compile time (the common
+// Myrtle shapes), so that only the code this network runs is in the kernel.
+template <int N0, int NSEG, int N1, int N2>
 __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* __restrict__ x1,
                                            const float* __restrict__ x2, int64_t gi, int64_t gj,
                                            const float* __restrict__ var1,
@@ -426,7 +433,7 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
   constexpr int S0 = 32, S1 = 16, S2 = 8;
   extern __shared__ __align__(16) float smem[];
   const int K = pg.channels;
-  const int nseg = pg.nseg;
+  const int nseg = NSEG > 0 ? NSEG : pg.nseg;
 
   ChainCtx cx;
   float* img1 = smem;                 // [4][S0*S0]
@@ -478,10 +485,10 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
   cx.readout = pg.readout;
   __syncthreads();
 
-  const int lb1 = pg.nconv[0];
-  const int lb2 = lb1 + (nseg > 1 ? pg.nconv[1] : 0);
-  const int nc1 = nseg > 1 ? pg.nconv[1] : 0;
-  const int nc2 = nseg > 2 ? pg.nconv[2] : 0;
+  const int lb1 = N0;
+  const int nc1 = NSEG > 0 ? (NSEG > 1 ? N1 : 0) : (nseg > 1 ? pg.nconv[1] : 0);
+  const int nc2 = NSEG > 0 ? (NSEG > 2 ? N2 : 0) : (nseg > 2 ? pg.nconv[2] : 0);
+  const int lb2 = lb1 + nc1;
   for (int d0 = -(S0 - 1); d0 <= S0 - 1; ++d0) {
     if (nseg > 1 && (d0 & 1)) {
       const int m = (d0 + 1) / 2;
@@ -505,13 +512,16 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
           }
         }
         if (nseg == 2)
-          process_pooled_line<S1, true>(cx, pg, nc1, lb1, vseg[1], slots1, nullptr, m1);
+          process_pooled_line<S1, true, NSEG == 2 ? N1 : -1>(cx, pg, nc1, lb1, vseg[1], slots1,
+                                                            nullptr, m1);
         else
-          process_pooled_line<S1, false>(cx, pg, nc1, lb1, vseg[1], slots1, slots2, m1);
+          process_pooled_line<S1, false, NSEG == 3 ? N1 : -1>(cx, pg, nc1, lb1, vseg[1], slots1,
+                                                             slots2, m1);
         if (nseg > 2 && (m1 & 1)) {
           const int m2 = (m1 - 1) / 2;
           if (m2 >= -(S2 - 1))
-            process_pooled_line<S2, true>(cx, pg, nc2, lb2, vseg[2], slots2, nullptr, m2);
+            process_pooled_line<S2, true, NSEG == 3 ? N2 : -1>(cx, pg, nc2, lb2, vseg[2], slots2,
+                                                              nullptr, m2);
         }
       }
     }
@@ -553,7 +563,7 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
 // tile of x1 with itself whose row and column ranges are disjoint. For sym != 0
 // out points at element (0, 0) of the whole kernel and each result is written at
 // (gi, gj) and (gj, gi).
-template <int N0>
+template <int N0, int NSEG = 0, int N1 = 0, int N2 = 0>
 __global__ void __launch_bounds__(NT, 1)
     chain_fwd_kernel(const __grid_constant__ ntg_chain_t pg, const float* __restrict__ x1,
                      const float* __restrict__ x2, int64_t r0, int64_t n1, int64_t c0,
@@ -571,7 +581,7 @@ __global__ void __launch_bounds__(NT, 1)
   const int64_t gi = r0 + i, gj = c0 + j;
   const int64_t o1 = sym ? gi * ld_out + gj : i * ld_out + j;
   const int64_t o2 = (sym && gi != gj) ? gj * ld_out + gi : -1;
-  chain_pair<N0>(pg, x1, x2, gi, gj, var1, var2, out_q, out_t, o1, o2);
+  chain_pair<N0, NSEG, N1, N2>(pg, x1, x2, gi, gj, var1, var2, out_q, out_t, o1, o2);
 }
 
 size_t chain_smem_bytes(const ntg_chain_t& pg) {
@@ -593,10 +603,24 @@ using namespace ntg;
 
 namespace {
 
+template <int N0, int NSEG, int N1, int N2>
+cudaError_t launch_chain_k(unsigned grid, size_t sm, cudaStream_t s, const ntg_chain_t& pg,
+                           const float* x1, const float* x2, int64_t r0, int64_t n1, int64_t c0,
+                           int64_t n2, const float* var1, const float* var2, float* out_q,
+                           float* out_t, int64_t ld_out, int sym) {
+  cudaError_t e = cudaFuncSetAttribute(chain_fwd_kernel<N0, NSEG, N1, N2>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e == cudaSuccess)
+    chain_fwd_kernel<N0, NSEG, N1, N2><<<grid, NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1,
+                                                            var2, out_q, out_t, ld_out, sym);
+  return e;
+}
+
 int launch_chain(const char* who, void* stream, const ntg_chain_t* prog, const float* x1,
-                 const float* x2, int64_t r0, int64_t n1, int64_t c0, int64_t n2,
+                 const float* x2, int64_t r0, int64_t n1_, int64_t c0, int64_t n2_,
                  const float* var1, const float* var2, float* out_q, float* out_t, int64_t ld_out,
                  int sym) {
+  const int64_t n1 = n1_, n2 = n2_;
   const std::string w(who);
   NTG_REQUIRE(prog && x1 && x2 && var1 && var2 && out_q, w + ": null pointer");
   const ntg_chain_t& pg = *prog;
@@ -624,30 +648,28 @@ int launch_chain(const char* who, void* stream, const ntg_chain_t* prog, const f
   const unsigned grid = (unsigned)total;  // one CTA per pair
   size_t sm = chain_smem_bytes(pg);
   cudaStream_t s = as_stream(stream);
-  cudaError_t e = cudaSuccess;
-  switch (pg.nconv[0]) {
-    case 1:
-      e = cudaFuncSetAttribute(chain_fwd_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)sm);
-      if (e == cudaSuccess)
-        chain_fwd_kernel<1><<<grid, NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1, var2,
-                                                 out_q, out_t, ld_out, sym);
-      break;
-    case 2:
-      e = cudaFuncSetAttribute(chain_fwd_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)sm);
-      if (e == cudaSuccess)
-        chain_fwd_kernel<2><<<grid, NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1, var2,
-                                                 out_q, out_t, ld_out, sym);
-      break;
-    default:
-      e = cudaFuncSetAttribute(chain_fwd_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)sm);
-      if (e == cudaSuccess)
-        chain_fwd_kernel<3><<<grid, NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1, var2,
-                                                 out_q, out_t, ld_out, sym);
-      break;
-  }
+  const int n0 = pg.nconv[0];
+  const int c1 = pg.nseg > 1 ? pg.nconv[1] : -1, c2 = pg.nseg > 2 ? pg.nconv[2] : -1;
+  cudaError_t e;
+  // the Myrtle-5 / -7 / -10 shapes get kernels specialised to their segments
+  if (pg.nseg == 3 && n0 == 2 && c1 == 1 && c2 == 1)
+    e = launch_chain_k<2, 3, 1, 1>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2, out_q,
+                                   out_t, ld_out, sym);
+  else if (pg.nseg == 3 && n0 == 2 && c1 == 2 && c2 == 2)
+    e = launch_chain_k<2, 3, 2, 2>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2, out_q,
+                                   out_t, ld_out, sym);
+  else if (pg.nseg == 3 && n0 == 3 && c1 == 3 && c2 == 3)
+    e = launch_chain_k<3, 3, 3, 3>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2, out_q,
+                                   out_t, ld_out, sym);
+  else if (n0 == 1)
+    e = launch_chain_k<1, 0, 0, 0>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2, out_q,
+                                   out_t, ld_out, sym);
+  else if (n0 == 2)
+    e = launch_chain_k<2, 0, 0, 0>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2, out_q,
+                                   out_t, ld_out, sym);
+  else
+    e = launch_chain_k<3, 0, 0, 0>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2, out_q,
+                                   out_t, ld_out, sym);
   if (e != cudaSuccess) return fail(NTG_ERR_CUDA, w + ": " + cudaGetErrorString(e));
   note_launch();
   return check_launch(who);
