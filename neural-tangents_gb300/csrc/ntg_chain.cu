@@ -57,7 +57,8 @@ __device__ __forceinline__ void zero_slot(float* q, float* t, int n) {
 // `vmaps` holds this segment's variance maps, layer k at vmaps + 4*k*S*S:
 // var1, var2, sqrt(var1), sqrt(var2) as S x S maps; `out_slots` is the next segment's
 // slot region ([parity][tensor][S/2][S/2 * S/2]).
-template <int S, int NC, bool FIRST, bool LAST>
+// RO: the network's activations are all of the ABRelu family (the Erf rule is left out).
+template <int S, int NC, bool FIRST, bool LAST, bool RO = false>
 __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg, int lbase,
                                              const float* vmaps, float* out_slots, int delta,
                                              const float* in_q, const float* in_t) {
@@ -169,7 +170,8 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
           apply_affine(af, cq, ct, true, q, t, 1.f / 9.f);
           if (ac.kind != NTG_ACT_NONE && on) {
             const int i1 = p * S + c0 + u, i2 = (p + delta) * S + wp[u];
-            act_apply<false>(ac, q, t, vm[i1], vm[S * S + i2], vm[2 * S * S + i1], vm[3 * S * S + i2]);
+            act_apply<false, !RO>(ac, q, t, vm[i1], vm[S * S + i2], vm[2 * S * S + i1],
+                                  vm[3 * S * S + i2]);
           }
           oq[u] = q;
           ot[u] = t;
@@ -244,7 +246,7 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
 // Thread t owns columns 2(t % 16), 2(t % 16) + 1 of skewed row t / 16. The
 // per-lane operation sequence equals the scalar path's, so the result is bit
 // for bit the same as process_line's and as the materialised layer kernels'.
-template <int NC, bool LAST>
+template <int NC, bool LAST, bool RO = false>
 __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, const float* vmaps,
                                          float* out_slots, int delta) {
   constexpr int S = 32;
@@ -325,7 +327,7 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
           const P2 v1 = p2ld(vm + i1), sv1 = p2ld(vm + 2 * S * S + i1);
           const float* v2r = vm + S * S + i2;
           const float* s2r = vm + 3 * S * S + i2;
-          if (ac.kind == NTG_ACT_ABRELU && ac.stab <= 0.f) {
+          if (RO || (ac.kind == NTG_ACT_ABRELU && ac.stab <= 0.f)) {
             abrelu2(ac, q, t, v1, p2(v2r[wp0], v2r[wp1]), sv1, p2(s2r[wp0], s2r[wp1]));
           } else {
             float qa, qb, ta, tb, va, vb, sa, sb;
@@ -388,7 +390,7 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
 }
 
 // NCT >= 0: the segment's conv count is known at compile time (one instantiation).
-template <int S, bool LAST, int NCT = -1>
+template <int S, bool LAST, int NCT = -1, bool RO = false>
 __device__ __forceinline__ void process_pooled_line(ChainCtx& cx, const ntg_chain_t& pg, int ncv,
                                                     int lbase, const float* vmaps,
                                                     const float* in_slots, float* out_slots,
@@ -396,14 +398,14 @@ __device__ __forceinline__ void process_pooled_line(ChainCtx& cx, const ntg_chai
   const float* q = in_slots + (2 * (m & 1)) * (S * S * S);
   const float* t = q + S * S * S;
   if constexpr (NCT >= 0) {
-    process_line<S, NCT, false, LAST>(cx, pg, lbase, vmaps, out_slots, m, q, t);
+    process_line<S, NCT, false, LAST, RO>(cx, pg, lbase, vmaps, out_slots, m, q, t);
     return;
   }
   switch (ncv) {
-    case 0: process_line<S, 0, false, LAST>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
-    case 1: process_line<S, 1, false, LAST>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
-    case 2: process_line<S, 2, false, LAST>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
-    default: process_line<S, 3, false, LAST>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
+    case 0: process_line<S, 0, false, LAST, RO>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
+    case 1: process_line<S, 1, false, LAST, RO>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
+    case 2: process_line<S, 2, false, LAST, RO>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
+    default: process_line<S, 3, false, LAST, RO>(cx, pg, lbase, vmaps, out_slots, m, q, t); break;
   }
 }
 
@@ -423,7 +425,7 @@ __device__ __forceinline__ void tri_pair(int64_t p, int64_t n, int64_t& i, int64
 
 // NSEG > 0: segment count and conv counts N1, N2 fixed at compile time (the common
 // Myrtle shapes), so that only the code this network runs is in the kernel.
-template <int N0, int NSEG, int N1, int N2>
+template <int N0, int NSEG, int N1, int N2, bool RO>
 __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* __restrict__ x1,
                                            const float* __restrict__ x2, int64_t gi, int64_t gj,
                                            const float* __restrict__ var1,
@@ -498,9 +500,9 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
       }
     }
     if (nseg == 1)
-      line_s32<N0, true>(cx, pg, vseg[0], nullptr, d0);
+      line_s32<N0, true, RO>(cx, pg, vseg[0], nullptr, d0);
     else
-      line_s32<N0, false>(cx, pg, vseg[0], slots1, d0);
+      line_s32<N0, false, RO>(cx, pg, vseg[0], slots1, d0);
     if (nseg > 1 && (d0 & 1)) {
       const int m1 = (d0 - 1) / 2;
       if (m1 >= -(S1 - 1)) {
@@ -512,15 +514,15 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
           }
         }
         if (nseg == 2)
-          process_pooled_line<S1, true, NSEG == 2 ? N1 : -1>(cx, pg, nc1, lb1, vseg[1], slots1,
+          process_pooled_line<S1, true, NSEG == 2 ? N1 : -1, RO>(cx, pg, nc1, lb1, vseg[1], slots1,
                                                             nullptr, m1);
         else
-          process_pooled_line<S1, false, NSEG == 3 ? N1 : -1>(cx, pg, nc1, lb1, vseg[1], slots1,
+          process_pooled_line<S1, false, NSEG == 3 ? N1 : -1, RO>(cx, pg, nc1, lb1, vseg[1], slots1,
                                                              slots2, m1);
         if (nseg > 2 && (m1 & 1)) {
           const int m2 = (m1 - 1) / 2;
           if (m2 >= -(S2 - 1))
-            process_pooled_line<S2, true, NSEG == 3 ? N2 : -1>(cx, pg, nc2, lb2, vseg[2], slots2,
+            process_pooled_line<S2, true, NSEG == 3 ? N2 : -1, RO>(cx, pg, nc2, lb2, vseg[2], slots2,
                                                               nullptr, m2);
         }
       }
@@ -563,7 +565,7 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
 // tile of x1 with itself whose row and column ranges are disjoint. For sym != 0
 // out points at element (0, 0) of the whole kernel and each result is written at
 // (gi, gj) and (gj, gi).
-template <int N0, int NSEG = 0, int N1 = 0, int N2 = 0>
+template <int N0, int NSEG = 0, int N1 = 0, int N2 = 0, bool RO = false>
 __global__ void __launch_bounds__(NT, 1)
     chain_fwd_kernel(const __grid_constant__ ntg_chain_t pg, const float* __restrict__ x1,
                      const float* __restrict__ x2, int64_t r0, int64_t n1, int64_t c0,
@@ -581,7 +583,7 @@ __global__ void __launch_bounds__(NT, 1)
   const int64_t gi = r0 + i, gj = c0 + j;
   const int64_t o1 = sym ? gi * ld_out + gj : i * ld_out + j;
   const int64_t o2 = (sym && gi != gj) ? gj * ld_out + gi : -1;
-  chain_pair<N0, NSEG, N1, N2>(pg, x1, x2, gi, gj, var1, var2, out_q, out_t, o1, o2);
+  chain_pair<N0, NSEG, N1, N2, RO>(pg, x1, x2, gi, gj, var1, var2, out_q, out_t, o1, o2);
 }
 
 size_t chain_smem_bytes(const ntg_chain_t& pg) {
@@ -603,17 +605,31 @@ using namespace ntg;
 
 namespace {
 
-template <int N0, int NSEG, int N1, int N2>
+template <int N0, int NSEG, int N1, int N2, bool RO = false>
 cudaError_t launch_chain_k(unsigned grid, size_t sm, cudaStream_t s, const ntg_chain_t& pg,
                            const float* x1, const float* x2, int64_t r0, int64_t n1, int64_t c0,
                            int64_t n2, const float* var1, const float* var2, float* out_q,
                            float* out_t, int64_t ld_out, int sym) {
-  cudaError_t e = cudaFuncSetAttribute(chain_fwd_kernel<N0, NSEG, N1, N2>,
+  cudaError_t e = cudaFuncSetAttribute(chain_fwd_kernel<N0, NSEG, N1, N2, RO>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e == cudaSuccess)
-    chain_fwd_kernel<N0, NSEG, N1, N2><<<grid, NT, sm, s>>>(pg, x1, x2, r0, n1, c0, n2, var1,
-                                                            var2, out_q, out_t, ld_out, sym);
+    chain_fwd_kernel<N0, NSEG, N1, N2, RO><<<grid, NT, sm, s>>>(
+        pg, x1, x2, r0, n1, c0, n2, var1, var2, out_q, out_t, ld_out, sym);
   return e;
+}
+
+// The Myrtle shapes: segment-specialised kernels, ReLU-family-only variants where they apply.
+template <int N0, int N1, int N2>
+cudaError_t launch_myrtle(bool relu_only, unsigned grid, size_t sm, cudaStream_t s,
+                          const ntg_chain_t& pg, const float* x1, const float* x2, int64_t r0,
+                          int64_t n1, int64_t c0, int64_t n2, const float* var1,
+                          const float* var2, float* out_q, float* out_t, int64_t ld_out,
+                          int sym) {
+  if (relu_only)
+    return launch_chain_k<N0, 3, N1, N2, true>(grid, sm, s, pg, x1, x2, r0, n1, c0, n2, var1,
+                                               var2, out_q, out_t, ld_out, sym);
+  return launch_chain_k<N0, 3, N1, N2, false>(grid, sm, s, pg, x1, x2, r0, n1, c0, n2, var1,
+                                              var2, out_q, out_t, ld_out, sym);
 }
 
 int launch_chain(const char* who, void* stream, const ntg_chain_t* prog, const float* x1,
@@ -652,15 +668,18 @@ int launch_chain(const char* who, void* stream, const ntg_chain_t* prog, const f
   const int c1 = pg.nseg > 1 ? pg.nconv[1] : -1, c2 = pg.nseg > 2 ? pg.nconv[2] : -1;
   cudaError_t e;
   // the Myrtle-5 / -7 / -10 shapes get kernels specialised to their segments
+  bool relu_only = true;
+  for (int l = 0; l < nl; ++l)
+    relu_only = relu_only && (pg.act[l].kind == NTG_ACT_NONE || pg.act[l].kind == NTG_ACT_ABRELU);
   if (pg.nseg == 3 && n0 == 2 && c1 == 1 && c2 == 1)
-    e = launch_chain_k<2, 3, 1, 1>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2, out_q,
-                                   out_t, ld_out, sym);
+    e = launch_myrtle<2, 1, 1>(relu_only, grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2,
+                               out_q, out_t, ld_out, sym);
   else if (pg.nseg == 3 && n0 == 2 && c1 == 2 && c2 == 2)
-    e = launch_chain_k<2, 3, 2, 2>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2, out_q,
-                                   out_t, ld_out, sym);
+    e = launch_myrtle<2, 2, 2>(relu_only, grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2,
+                               out_q, out_t, ld_out, sym);
   else if (pg.nseg == 3 && n0 == 3 && c1 == 3 && c2 == 3)
-    e = launch_chain_k<3, 3, 3, 3>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2, out_q,
-                                   out_t, ld_out, sym);
+    e = launch_myrtle<3, 3, 3>(relu_only, grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2,
+                               out_q, out_t, ld_out, sym);
   else if (n0 == 1)
     e = launch_chain_k<1, 0, 0, 0>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2, out_q,
                                    out_t, ld_out, sym);

@@ -210,7 +210,7 @@ __device__ __forceinline__ void act_apply_rare(const ActC& c, float& q, float& t
 // Erf(a, b, c) rule, elementwise.py:67-112 (k *= b first, a*k + c last):
 //   prod = (1 + 2 v1)(1 + 2 v2); s = sqrt(max(prod - 4q^2, 0));
 //   q' = 2/pi atan2(2q, s); ntk' = ntk (4/pi) / s
-template <bool RARE = true>
+template <bool RARE = true, bool ERF = true>
 __device__ __forceinline__ void act_apply(const ActC& c, float& q, float& t, float v1, float v2,
                                           float sv1, float sv2) {
   if (c.kind == NTG_ACT_ABRELU) {
@@ -231,7 +231,7 @@ __device__ __forceinline__ void act_apply(const ActC& c, float& q, float& t, flo
     if (c.stab > 0.f) qo = __fmul_rn(qo, c.stab);
     q = qo;
     t = __fmul_rn(t, dot);
-  } else if (c.kind == NTG_ACT_ERF) {
+  } else if (ERF && c.kind == NTG_ACT_ERF) {
     const float qb = __fmul_rn(c.b2, q);
     const float d1 = fmaf(2.f * c.b2, v1, 1.f);
     const float d2 = fmaf(2.f * c.b2, v2, 1.f);
