@@ -248,13 +248,15 @@ __device__ __forceinline__ void act_apply(const ActC& c, float& q, float& t, flo
 }
 
 // The ABRelu branch of act_apply (do_stabilize off) on a packed pair, with
-// the same operation sequence per lane.
+// the same operation sequence per lane. COMP: -1 reads c.comp, 0 / 1 fix the
+// plain / compensated var1 var2 - q^2 at compile time.
+template <int COMP = -1>
 __device__ __forceinline__ void abrelu2(const ActC& c, P2& q, P2& t, P2 v1, P2 v2, P2 sv1,
                                         P2 sv2) {
   const P2 n = mul2(sv1, sv2);
   const P2 pr = mul2(v1, v2), qq = mul2(q, q);
   P2 d = sub2(pr, qq);
-  if (c.comp) {
+  if (COMP == 1 || (COMP < 0 && c.comp)) {
     const P2 m1 = p2s(-1.f);
     const P2 pe = fma2(v1, v2, mul2(pr, m1)), qe = fma2(q, q, mul2(qq, m1));
     d = add2(d, sub2(pe, qe));
