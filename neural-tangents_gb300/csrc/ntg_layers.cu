@@ -620,7 +620,9 @@ __device__ __forceinline__ void bulk_store(float* gdst, const float* ssrc, uint3
                : "memory");
 }
 
-template <bool HAS_T, int RING>
+// ACTK: 1 = the ABRelu family without do_stabilize only (the other rules compiled out),
+// 0 = any activation rule.
+template <bool HAS_T, int RING, int ACTK>
 __global__ void __launch_bounds__(kThreads)
     conv3_skew_kernel(const float* __restrict__ in_q, const float* __restrict__ in_t,
                       float* __restrict__ out_q, float* __restrict__ out_t, int64_t batch,
@@ -800,7 +802,7 @@ __global__ void __launch_bounds__(kThreads)
         v2[k] = vb[64 + w0 + r + k];
         s2[k] = vb[128 + w0 + r + k];
       }
-      if (act.kind == NTG_ACT_ABRELU && act.stabilize <= 0.f) {
+      if (ACTK == 1 || (act.kind == NTG_ACT_ABRELU && act.stabilize <= 0.f)) {
         abrelu2(ac, q[0], t[0], p2(v1.x, v1.y), p2(v2[0], v2[1]), p2(s1.x, s1.y),
                 p2(s2[0], s2[1]));
         abrelu2(ac, q[1], t[1], p2(v1.z, v1.w), p2(v2[2], v2[3]), p2(s1.z, s1.w),
@@ -1233,28 +1235,37 @@ extern "C" int ntg_input_fs(void* stream, const float* x1, const float* x2, int6
   return check_launch("ntg_input_fs");
 }
 
+template <bool HAS_T, int RING, int ACTK>
+cudaError_t launch_skew_k(cudaStream_t s, int64_t blocks, size_t sm, const float* in_q,
+                          const float* in_t, float* out_q, float* out_t, int64_t batch,
+                          int64_t n2, int64_t a, ntg_affine_t aff, ntg_act_t act, ntg_var_t var1,
+                          ntg_var_t var2, float* pre_q, float* pre_t) {
+  cudaError_t e = cudaFuncSetAttribute(conv3_skew_kernel<HAS_T, RING, ACTK>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)skew_smem_bytes_pre<RING>());
+  if (e == cudaSuccess)
+    conv3_skew_kernel<HAS_T, RING, ACTK><<<(unsigned)blocks, kThreads, sm, s>>>(
+        in_q, in_t, out_q, out_t, batch, n2, (int)a, aff, act, var1, var2, pre_q, pre_t);
+  return e;
+}
+
 template <int RING>
 cudaError_t launch_skew(cudaStream_t s, int64_t blocks, const float* in_q, const float* in_t,
                         float* out_q, float* out_t, int64_t batch, int64_t n2, int64_t a,
                         ntg_affine_t aff, ntg_act_t act, ntg_var_t var1, ntg_var_t var2,
                         float* pre_q = nullptr, float* pre_t = nullptr) {
   const size_t sm = pre_q ? skew_smem_bytes_pre<RING>() : skew_smem_bytes<RING>();
-  const size_t sm_max = skew_smem_bytes_pre<RING>();
-  cudaError_t e;
-  if (in_t) {
-    e = cudaFuncSetAttribute(conv3_skew_kernel<true, RING>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
-    if (e == cudaSuccess)
-      conv3_skew_kernel<true, RING><<<(unsigned)blocks, kThreads, sm, s>>>(
-          in_q, in_t, out_q, out_t, batch, n2, (int)a, aff, act, var1, var2, pre_q, pre_t);
-  } else {
-    e = cudaFuncSetAttribute(conv3_skew_kernel<false, RING>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_max);
-    if (e == cudaSuccess)
-      conv3_skew_kernel<false, RING><<<(unsigned)blocks, kThreads, sm, s>>>(
-          in_q, nullptr, out_q, out_t, batch, n2, (int)a, aff, act, var1, var2, pre_q, pre_t);
-  }
-  return e;
+  const bool relu = act.kind == NTG_ACT_NONE ||
+                    (act.kind == NTG_ACT_ABRELU && act.stabilize <= 0.f);
+  if (in_t)
+    return relu ? launch_skew_k<true, RING, 1>(s, blocks, sm, in_q, in_t, out_q, out_t, batch, n2,
+                                               a, aff, act, var1, var2, pre_q, pre_t)
+                : launch_skew_k<true, RING, 0>(s, blocks, sm, in_q, in_t, out_q, out_t, batch, n2,
+                                               a, aff, act, var1, var2, pre_q, pre_t);
+  return relu ? launch_skew_k<false, RING, 1>(s, blocks, sm, in_q, nullptr, out_q, out_t, batch,
+                                              n2, a, aff, act, var1, var2, pre_q, pre_t)
+              : launch_skew_k<false, RING, 0>(s, blocks, sm, in_q, nullptr, out_q, out_t, batch,
+                                              n2, a, aff, act, var1, var2, pre_q, pre_t);
 }
 
 extern "C" int ntg_conv_fs(void* stream, const float* in_q, const float* in_t, float* out_q,
