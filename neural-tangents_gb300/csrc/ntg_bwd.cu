@@ -259,7 +259,9 @@ __device__ __forceinline__ void abrelu_vjp2(const ActC& c, P2 q, P2 t, P2 v1, P2
 // variance cotangents are summed by warp shuffles and shared-memory atomics per
 // (plane, row) for var1 and per (plane, column) for var2 and leave with one
 // global atomic per key instead of one per entry. Double-buffered shared arrays
-// leave one barrier per chunk.
+// leave one barrier per chunk. RELU: the ABRelu rule only (the Erf VJP compiled
+// out); POOLED: the cotangent is that of the AvgPool(2, 2) output (pooled != 0).
+template <bool RELU, bool POOLED>
 __global__ void __launch_bounds__(kT)
     act_bwd_fs_kernel(const float* __restrict__ q, const float* __restrict__ t,
                       const float* __restrict__ gq, const float* __restrict__ gt,
@@ -310,7 +312,7 @@ __global__ void __launch_bounds__(kT)
     const float4 Q = *reinterpret_cast<const float4*>(q + e);
     const float4 T = t ? *reinterpret_cast<const float4*>(t + e) : make_float4(0.f, 0.f, 0.f, 0.f);
     float4 GQ, GT;
-    if (!pooled) {
+    if (!POOLED) {
       GQ = gq ? *reinterpret_cast<const float4*>(gq + e) : make_float4(0.f, 0.f, 0.f, 0.f);
       GT = gt ? *reinterpret_cast<const float4*>(gt + e) : make_float4(0.f, 0.f, 0.f, 0.f);
     } else {
@@ -332,7 +334,7 @@ __global__ void __launch_bounds__(kT)
     const float4 V2 = *reinterpret_cast<const float4*>(&sv[cur][1][k2]);
     const float v2[4] = {V2.x, V2.y, V2.z, V2.w};
     float rq[4], rt[4], r2[4], r1 = 0.f;
-    if (act.kind == NTG_ACT_ABRELU) {
+    if (RELU || act.kind == NTG_ACT_ABRELU) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         P2 oq2, ot2, o12, o22;
@@ -946,9 +948,12 @@ extern "C" int ntg_act_bwd(void* stream, const float* q, const float* t, const f
   if (!diag_spatial && pow2 && m % 1024 == 0 && aligned && m < (1ll << 31)) {
     const int64_t chunks = batch * (m / 1024);
     const int grid = (int)(chunks < 152 * 8 ? chunks : 152 * 8);
-    act_bwd_fs_kernel<<<grid, kT, 0, as_stream(stream)>>>(q, t, gq, gt, oq, ot, batch, n2,
-                                                          (int)a, (int)c, act, var1, var2, g1, g2,
-                                                          0, 0.f);
+    if (act.kind == NTG_ACT_ABRELU)
+      act_bwd_fs_kernel<true, false><<<grid, kT, 0, as_stream(stream)>>>(
+          q, t, gq, gt, oq, ot, batch, n2, (int)a, (int)c, act, var1, var2, g1, g2, 0, 0.f);
+    else
+      act_bwd_fs_kernel<false, false><<<grid, kT, 0, as_stream(stream)>>>(
+          q, t, gq, gt, oq, ot, batch, n2, (int)a, (int)c, act, var1, var2, g1, g2, 0, 0.f);
   } else {
     act_bwd_kernel<<<grid_for(batch * m), kT, 0, as_stream(stream)>>>(
         q, t, gq, gt, oq, ot, batch, n2, a, c, diag_spatial, act, var1, var2, g1, g2);
@@ -979,9 +984,14 @@ extern "C" int ntg_act_pool_bwd(void* stream, const float* q, const float* t,
   VarGrad g1{gvar1, a * c, c, 1}, g2{gvar2, a * c, c, 1};
   const int64_t chunks = batch * (m / 1024);
   const int grid = (int)(chunks < 152 * 8 ? chunks : 152 * 8);
-  act_bwd_fs_kernel<<<grid, kT, 0, as_stream(stream)>>>(q, t, gq_pooled, gt_pooled, oq, ot, batch,
-                                                        n2, (int)a, (int)c, act, var1, var2, g1,
-                                                        g2, 1, 1.f / 16.f);
+  if (act.kind == NTG_ACT_ABRELU)
+    act_bwd_fs_kernel<true, true><<<grid, kT, 0, as_stream(stream)>>>(
+        q, t, gq_pooled, gt_pooled, oq, ot, batch, n2, (int)a, (int)c, act, var1, var2, g1, g2, 1,
+        1.f / 16.f);
+  else
+    act_bwd_fs_kernel<false, true><<<grid, kT, 0, as_stream(stream)>>>(
+        q, t, gq_pooled, gt_pooled, oq, ot, batch, n2, (int)a, (int)c, act, var1, var2, g1, g2, 1,
+        1.f / 16.f);
   note_launch();
   return check_launch("ntg_act_pool_bwd");
 }

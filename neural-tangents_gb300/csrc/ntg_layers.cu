@@ -950,6 +950,7 @@ __global__ void affine_act_kernel(const float* __restrict__ in_q, const float* _
 // per thread, vector loads and stores); the variances a chunk needs, and their
 // square roots, are staged in shared memory one chunk ahead (2 C^-1 1024 loads per
 // chunk instead of 5 per thread). Same operations per entry as affine_act_kernel.
+template <int ACTK>  // 1: no activation or the ABRelu family only; 0: any rule
 __global__ void __launch_bounds__(kThreads)
     affine_act_fs_kernel(const float* __restrict__ in_q, const float* __restrict__ in_t,
                          float* __restrict__ out_q, float* __restrict__ out_t, int64_t batch,
@@ -1018,7 +1019,8 @@ __global__ void __launch_bounds__(kThreads)
       const float4 S2 = *reinterpret_cast<const float4*>(&sv[cur][3][k2]);
       const float v2[4] = {V2.x, V2.y, V2.z, V2.w}, s2[4] = {S2.x, S2.y, S2.z, S2.w};
 #pragma unroll
-      for (int k = 0; k < 4; ++k) act_apply(ac, q[k], t[k], v1, v2[k], s1, s2[k]);
+      for (int k = 0; k < 4; ++k)
+        act_apply<ACTK == 0, ACTK == 0>(ac, q[k], t[k], v1, v2[k], s1, s2[k]);
     }
     *reinterpret_cast<float4*>(out_q + e) = make_float4(q[0], q[1], q[2], q[3]);
     if (out_t) *reinterpret_cast<float4*>(out_t + e) = make_float4(t[0], t[1], t[2], t[3]);
@@ -1418,7 +1420,12 @@ extern "C" int ntg_affine_act(void* stream, const float* in_q, const float* in_t
   if (!diag_spatial && pow2 && m % 1024 == 0 && aligned && m < (1ll << 31)) {
     const int64_t chunks = batch * (m / 1024);
     const int grid = (int)(chunks < 152 * 8 ? chunks : 152 * 8);
-    affine_act_fs_kernel<<<grid, kThreads, 0, as_stream(stream)>>>(
+    const bool relu = act.kind == NTG_ACT_NONE || act.kind == NTG_ACT_ABRELU;
+    if (relu)
+      affine_act_fs_kernel<1><<<grid, kThreads, 0, as_stream(stream)>>>(
+          in_q, in_t, out_q, out_t, batch, n2, (int)a, (int)c, has_affine, aff, act, var1, var2);
+    else
+      affine_act_fs_kernel<0><<<grid, kThreads, 0, as_stream(stream)>>>(
         in_q, in_t, out_q, out_t, batch, n2, (int)a, (int)c, has_affine, aff, act, var1, var2);
   } else {
     affine_act_kernel<<<grid_for(batch * m), kThreads, 0, as_stream(stream)>>>(
