@@ -246,7 +246,7 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
 // Thread t owns columns 2(t % 16), 2(t % 16) + 1 of skewed row t / 16. The
 // per-lane operation sequence equals the scalar path's, so the result is bit
 // for bit the same as process_line's and as the materialised layer kernels'.
-template <int NC, bool LAST, bool RO = false, int COMP = -1>
+template <int NC, bool LAST, bool RO = false, int COMP = -1, int KC = 0>
 __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, const float* vmaps,
                                          float* out_slots, int delta) {
   constexpr int S = 32;
@@ -292,7 +292,7 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
       P2 g = zero;
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        if (k < cx.K) {
+        if (KC > 0 ? k < KC : k < cx.K) {  // KC > 0: channel count fixed at compile time
           const float* b = x2r + k * (S * S);
           g = fma2(p2ld(x1r + k * (S * S)), p2(b[wp0], b[wp1]), g);
         }
@@ -425,7 +425,7 @@ __device__ __forceinline__ void tri_pair(int64_t p, int64_t n, int64_t& i, int64
 
 // NSEG > 0: segment count and conv counts N1, N2 fixed at compile time (the common
 // Myrtle shapes), so that only the code this network runs is in the kernel.
-template <int N0, int NSEG, int N1, int N2, bool RO, int COMP>
+template <int N0, int NSEG, int N1, int N2, bool RO, int COMP, int KC>
 __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* __restrict__ x1,
                                            const float* __restrict__ x2, int64_t gi, int64_t gj,
                                            const float* __restrict__ var1,
@@ -500,9 +500,9 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
       }
     }
     if (nseg == 1)
-      line_s32<N0, true, RO, COMP>(cx, pg, vseg[0], nullptr, d0);
+      line_s32<N0, true, RO, COMP, KC>(cx, pg, vseg[0], nullptr, d0);
     else
-      line_s32<N0, false, RO, COMP>(cx, pg, vseg[0], slots1, d0);
+      line_s32<N0, false, RO, COMP, KC>(cx, pg, vseg[0], slots1, d0);
     if (nseg > 1 && (d0 & 1)) {
       const int m1 = (d0 - 1) / 2;
       if (m1 >= -(S1 - 1)) {
@@ -565,7 +565,8 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
 // tile of x1 with itself whose row and column ranges are disjoint. For sym != 0
 // out points at element (0, 0) of the whole kernel and each result is written at
 // (gi, gj) and (gj, gi).
-template <int N0, int NSEG = 0, int N1 = 0, int N2 = 0, bool RO = false, int COMP = -1>
+template <int N0, int NSEG = 0, int N1 = 0, int N2 = 0, bool RO = false, int COMP = -1,
+          int KC = 0>
 __global__ void __launch_bounds__(NT, 1)
     chain_fwd_kernel(const __grid_constant__ ntg_chain_t pg, const float* __restrict__ x1,
                      const float* __restrict__ x2, int64_t r0, int64_t n1, int64_t c0,
@@ -583,8 +584,8 @@ __global__ void __launch_bounds__(NT, 1)
   const int64_t gi = r0 + i, gj = c0 + j;
   const int64_t o1 = sym ? gi * ld_out + gj : i * ld_out + j;
   const int64_t o2 = (sym && gi != gj) ? gj * ld_out + gi : -1;
-  chain_pair<N0, NSEG, N1, N2, RO, COMP>(pg, x1, x2, gi, gj, var1, var2, out_q, out_t, o1,
-                                          o2);
+  chain_pair<N0, NSEG, N1, N2, RO, COMP, KC>(pg, x1, x2, gi, gj, var1, var2, out_q, out_t,
+                                              o1, o2);
 }
 
 size_t chain_smem_bytes(const ntg_chain_t& pg) {
@@ -606,15 +607,15 @@ using namespace ntg;
 
 namespace {
 
-template <int N0, int NSEG, int N1, int N2, bool RO = false, int COMP = -1>
+template <int N0, int NSEG, int N1, int N2, bool RO = false, int COMP = -1, int KC = 0>
 cudaError_t launch_chain_k(unsigned grid, size_t sm, cudaStream_t s, const ntg_chain_t& pg,
                            const float* x1, const float* x2, int64_t r0, int64_t n1, int64_t c0,
                            int64_t n2, const float* var1, const float* var2, float* out_q,
                            float* out_t, int64_t ld_out, int sym) {
-  cudaError_t e = cudaFuncSetAttribute(chain_fwd_kernel<N0, NSEG, N1, N2, RO, COMP>,
+  cudaError_t e = cudaFuncSetAttribute(chain_fwd_kernel<N0, NSEG, N1, N2, RO, COMP, KC>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e == cudaSuccess)
-    chain_fwd_kernel<N0, NSEG, N1, N2, RO, COMP><<<grid, NT, sm, s>>>(
+    chain_fwd_kernel<N0, NSEG, N1, N2, RO, COMP, KC><<<grid, NT, sm, s>>>(
         pg, x1, x2, r0, n1, c0, n2, var1, var2, out_q, out_t, ld_out, sym);
   return e;
 }
@@ -629,11 +630,21 @@ cudaError_t launch_myrtle(bool relu_only, unsigned grid, size_t sm, cudaStream_t
   if (relu_only) {
     bool comp = false;  // all layers share the precision of one call
     for (int l = 0; l < NTG_CHAIN_MAX_LAYERS; ++l) comp = comp || pg.act[l].compensated != 0;
+    // three input channels (images) get their own instantiation
     if (comp)
-      return launch_chain_k<N0, 3, N1, N2, true, 1>(grid, sm, s, pg, x1, x2, r0, n1, c0, n2,
-                                                    var1, var2, out_q, out_t, ld_out, sym);
-    return launch_chain_k<N0, 3, N1, N2, true, 0>(grid, sm, s, pg, x1, x2, r0, n1, c0, n2, var1,
-                                                  var2, out_q, out_t, ld_out, sym);
+      return pg.channels == 3
+                 ? launch_chain_k<N0, 3, N1, N2, true, 1, 3>(grid, sm, s, pg, x1, x2, r0, n1,
+                                                             c0, n2, var1, var2, out_q, out_t,
+                                                             ld_out, sym)
+                 : launch_chain_k<N0, 3, N1, N2, true, 1>(grid, sm, s, pg, x1, x2, r0, n1, c0,
+                                                          n2, var1, var2, out_q, out_t, ld_out,
+                                                          sym);
+    return pg.channels == 3
+               ? launch_chain_k<N0, 3, N1, N2, true, 0, 3>(grid, sm, s, pg, x1, x2, r0, n1, c0,
+                                                           n2, var1, var2, out_q, out_t, ld_out,
+                                                           sym)
+               : launch_chain_k<N0, 3, N1, N2, true, 0>(grid, sm, s, pg, x1, x2, r0, n1, c0, n2,
+                                                        var1, var2, out_q, out_t, ld_out, sym);
   }
   return launch_chain_k<N0, 3, N1, N2, false>(grid, sm, s, pg, x1, x2, r0, n1, c0, n2, var1,
                                               var2, out_q, out_t, ld_out, sym);
