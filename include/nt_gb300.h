@@ -265,7 +265,9 @@ int ntg_chol_solve(void* stream, const float* A, const float* L, const double* l
  * q, t are the pre-activation nngp/ntk (t may be NULL), gq, gt the output
  * cotangents (either may be NULL); writes the cotangents of q (oq) and t (ot,
  * may be NULL) and ADDS the variance cotangents into gvar1 / gvar2 (compact
- * [n, A, C] device arrays; NULL to skip). */
+ * [n, A, C] device arrays; NULL to skip). Every kind of ntg_act_kind has an
+ * adjoint; the Gelu rule is differentiated with jnp.arctan2's plain derivative,
+ * as the reference writes it (elementwise.py:230-250). */
 int ntg_act_bwd(void* stream, const float* q, const float* t, const float* gq, const float* gt,
                 float* oq, float* ot, int64_t batch, int64_t n2, int64_t a, int64_t c,
                 int32_t diag_spatial, ntg_act_t act, ntg_var_t var1, ntg_var_t var2,

@@ -698,7 +698,7 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
                 nxt = specs[idx + 1] if idx + 1 < len(specs) else None
                 nxt2 = specs[idx + 2] if idx + 2 < len(specs) else None
                 if (nxt is not None and nxt.kind == 'act' and not nxt.params.get('do_stabilize')
-                        and nxt.params['fn'] in ('abrelu', 'erf') and conv_act_fusable(q, geom)):
+                        and conv_act_fusable(q, geom)):
                     pool_geom = None
                     if nxt2 is not None and nxt2.kind == 'pool':
                         pg = _pool_geom_sizes(32, 32, nxt2)
@@ -723,9 +723,6 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
                                  'activation function.')
             if p.get('do_stabilize'):
                 raise NotImplementedError('do_stabilize is not differentiable here')
-            if p['fn'] not in ('abrelu', 'erf'):
-                raise NotImplementedError(f'gradients through {p["fn"]} are not implemented; '
-                                          'adjoints exist for ABRelu/Relu and Erf')
             tt = t if t is not None else torch.zeros((), device=dev)
             nxt = specs[idx + 1] if idx + 1 < len(specs) else None
             geom = _pool_geom(q, nxt) if (nxt is not None and nxt.kind == 'pool') else None

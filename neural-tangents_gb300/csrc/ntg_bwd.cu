@@ -31,6 +31,87 @@ __device__ __forceinline__ void vg_add(const VarGrad& g, int64_t n, int64_t a, i
   if (g.base && v != 0.f) atomicAdd(g.base + n * g.s_n + a * g.s_a + c * g.s_c, v);
 }
 
+// VJPs of the Sin / Rbf / Gelu rules at one entry (the forward rules are
+// act_apply_rare's): reverse mode through the reference's expressions, with
+// _sqrt's derivative 0 where its argument is <= 1e-30 (elementwise.py:1278-1290)
+// and jnp.arctan2's plain derivative in the Gelu rule (elementwise.py:230-250).
+__device__ __forceinline__ void act_vjp_rare(const ActC& c, float q, float t, float v1, float v2,
+                                             float gq, float gt, float& oq, float& ot,
+                                             float& ov1, float& ov2) {
+  if (c.kind == NTG_ACT_SIN) {
+    // q' = A (s1 - s2) = M, t' = t B A (s1 + s2) = t B P with dM/dq = B P, dP/dq = B M and
+    // d/dv1 = d/dv2 = -B / 2 on both (A = a^2 / 2, B = b^2; elementwise.py:303-311)
+    const float sum = v1 + v2;
+    const float s1 = expf(c.b2 * fmaf(-0.5f, sum, q));
+    const float s2 = expf(c.b2 * fmaf(-0.5f, sum, -q)) * c.c2;
+    const float P = c.a2 * (s1 + s2), M = c.a2 * (s1 - s2);
+    const float gP = c.b2 * t * gt;
+    oq = c.b2 * fmaf(gq, P, gP * M);
+    ot = c.b2 * P * gt;
+    ov1 = ov2 = -0.5f * c.b2 * fmaf(gq, M, gP * P);
+  } else if (c.kind == NTG_ACT_RBF) {
+    // q' = exp(g (2 q - v1 - v2)), t' = t 2 g q' (g = gamma; elementwise.py:380-384)
+    const float qo = expf(c.a2 * fmaf(2.f, q, -(v1 + v2)));
+    const float g_qo = fmaf(2.f * c.a2 * t, gt, gq);
+    oq = 2.f * c.a2 * qo * g_qo;
+    ot = 2.f * c.a2 * qo * gt;
+    ov1 = ov2 = -c.a2 * qo * g_qo;
+  } else if (c.kind == NTG_ACT_GELU) {
+    const float tol = 1e-30f;
+    const float prod = v1 * v2;
+    const float pp1 = (v1 + 1.f) * (v2 + 1.f);
+    const float d2 = pp1 - q * q;
+    const float dl = sqrtf(fmaxf(d2, 0.f));
+    const float ang = atan2f(q, dl);
+    const float num = q * q + prod * d2, dn = pp1 * dl;
+    const float first0 = 1.f / d2 + (1.f - prod) / pp1 + 1.f;
+    const float k2pi = 1.f / (2.f * kPi);
+    const float first = first0 * q / dl * k2pi;
+    const float second = 0.25f + ang * k2pi;
+    ot = gt * (first + second);
+    const float g_f = gt * t;  // cotangent of first and of second
+    float g_q = gq * (ang * k2pi + 0.25f);
+    const float g_ang = (g_f + gq * q) * k2pi;
+    const float g_r = gq * k2pi;  // cotangent of num / dn
+    // first = first0 q / dl / (2 pi)
+    const float g_first0 = g_f * q / dl * k2pi;
+    g_q += g_f * first0 / dl * k2pi;
+    float g_dl = -g_f * first0 * q / (dl * dl) * k2pi;
+    // first0 = 1 / d2 + (1 - prod) / pp1 + 1
+    float g_d2 = -g_first0 / (d2 * d2);
+    float g_prod = -g_first0 / pp1;
+    float g_pp1 = -g_first0 * (1.f - prod) / (pp1 * pp1);
+    // num / dn
+    const float g_num = g_r / dn;
+    const float g_dn = -g_r * num / (dn * dn);
+    g_pp1 += g_dn * dl;
+    g_dl += g_dn * pp1;
+    g_q += 2.f * q * g_num;
+    g_prod += g_num * d2;
+    g_d2 += g_num * prod;
+    // ang = arctan2(q, dl)
+    const float den = q * q + dl * dl;
+    g_q += g_ang * dl / den;
+    g_dl -= g_ang * q / den;
+    // dl = _sqrt(d2)
+    g_d2 += (d2 > tol) ? g_dl * 0.5f / dl : 0.f;
+    // d2 = pp1 - q^2
+    g_pp1 += g_d2;
+    g_q -= 2.f * q * g_d2;
+    oq = g_q;
+    ov1 = fmaf(g_pp1, v2 + 1.f, g_prod * v2);
+    ov2 = fmaf(g_pp1, v1 + 1.f, g_prod * v1);
+  } else {
+    oq = gq;
+    ot = gt;
+    ov1 = ov2 = 0.f;
+  }
+}
+
+__device__ __forceinline__ bool act_is_rare(int kind) {
+  return kind == NTG_ACT_SIN || kind == NTG_ACT_RBF || kind == NTG_ACT_GELU;
+}
+
 // VJP of the activation rule at one entry: given the pre-activation (q, t) and
 // variances (v1, v2) and the output cotangents (gq, gt), returns the
 // cotangents of q, t, v1, v2.
@@ -84,6 +165,8 @@ __device__ __forceinline__ void act_vjp(const ntg_act_t& act, float q, float t, 
     ot = b2 * g_tb;
     ov1 = b2 * 2.f * g_d1;
     ov2 = b2 * 2.f * g_d2;
+  } else if (act_is_rare(act.kind)) {
+    act_vjp_rare(act_consts(act), q, t, v1, v2, gq, gt, oq, ot, ov1, ov2);
   } else {
     oq = gq;
     ot = gt;
@@ -138,6 +221,7 @@ __device__ __forceinline__ float rsqrt_approx(float x) {
   return r;
 }
 
+template <bool RARE = false>
 __device__ __forceinline__ void act_vjp_fast(const ntg_act_t& act, const ActC& c, float q,
                                              float t, float v1, float v2, float gq, float gt,
                                              float& oq, float& ot, float& ov1, float& ov2) {
@@ -189,6 +273,8 @@ __device__ __forceinline__ void act_vjp_fast(const ntg_act_t& act, const ActC& c
     ot = c.b2 * g_tb;
     ov1 = c.b2 * 2.f * (g_dd * d2);
     ov2 = c.b2 * 2.f * (g_dd * d1);
+  } else if (RARE && act_is_rare(act.kind)) {
+    act_vjp_rare(c, q, t, v1, v2, gq, gt, oq, ot, ov1, ov2);
   } else {
     oq = gq;
     ot = gt;
@@ -260,8 +346,9 @@ __device__ __forceinline__ void abrelu_vjp2(const ActC& c, P2 q, P2 t, P2 v1, P2
 // (plane, row) for var1 and per (plane, column) for var2 and leave with one
 // global atomic per key instead of one per entry. Double-buffered shared arrays
 // leave one barrier per chunk. RELU: the ABRelu rule only (the Erf VJP compiled
-// out); POOLED: the cotangent is that of the AvgPool(2, 2) output (pooled != 0).
-template <bool RELU, bool POOLED>
+// out); POOLED: the cotangent is that of the AvgPool(2, 2) output (pooled != 0);
+// RARE: the Sin / Rbf / Gelu VJPs compiled in.
+template <bool RELU, bool POOLED, bool RARE = false>
 __global__ void __launch_bounds__(kT)
     act_bwd_fs_kernel(const float* __restrict__ q, const float* __restrict__ t,
                       const float* __restrict__ gq, const float* __restrict__ gt,
@@ -352,7 +439,8 @@ __global__ void __launch_bounds__(kT)
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         float o1;
-        act_vjp_fast(act, ac, qa[k], ta[k], v1, v2[k], ga[k], gb[k], rq[k], rt[k], o1, r2[k]);
+        act_vjp_fast<RARE>(act, ac, qa[k], ta[k], v1, v2[k], ga[k], gb[k], rq[k], rt[k], o1,
+                           r2[k]);
         r1 += o1;
       }
     }
@@ -935,8 +1023,9 @@ extern "C" int ntg_act_bwd(void* stream, const float* q, const float* t, const f
   NTG_REQUIRE(batch > 0 && a > 0 && c > 0, "ntg_act_bwd: bad sizes");
   NTG_REQUIRE(act.kind != NTG_ACT_ABRELU || act.stabilize <= 0.f,
               "ntg_act_bwd: do_stabilize is not differentiable here");
-  if (act.kind != NTG_ACT_NONE && act.kind != NTG_ACT_ABRELU && act.kind != NTG_ACT_ERF)
-    return fail(NTG_ERR_UNSUPPORTED, "ntg_act_bwd: adjoints exist for ABRelu and Erf");
+  if (act.kind < NTG_ACT_NONE || act.kind > NTG_ACT_GELU)
+    return fail(NTG_ERR_UNSUPPORTED, "ntg_act_bwd: unknown activation kind");
+  const bool rare = act.kind >= NTG_ACT_SIN;
   // variance cotangents are compact [n, A, C] arrays
   VarGrad g1{gvar1, a * c, c, 1}, g2{gvar2, a * c, c, 1};
   const int64_t m = diag_spatial ? a * c : a * a * c * c;
@@ -950,6 +1039,9 @@ extern "C" int ntg_act_bwd(void* stream, const float* q, const float* t, const f
     const int grid = (int)(chunks < 152 * 8 ? chunks : 152 * 8);
     if (act.kind == NTG_ACT_ABRELU)
       act_bwd_fs_kernel<true, false><<<grid, kT, 0, as_stream(stream)>>>(
+          q, t, gq, gt, oq, ot, batch, n2, (int)a, (int)c, act, var1, var2, g1, g2, 0, 0.f);
+    else if (rare)
+      act_bwd_fs_kernel<false, false, true><<<grid, kT, 0, as_stream(stream)>>>(
           q, t, gq, gt, oq, ot, batch, n2, (int)a, (int)c, act, var1, var2, g1, g2, 0, 0.f);
     else
       act_bwd_fs_kernel<false, false><<<grid, kT, 0, as_stream(stream)>>>(
@@ -971,8 +1063,8 @@ extern "C" int ntg_act_pool_bwd(void* stream, const float* q, const float* t,
   NTG_REQUIRE(batch > 0 && a > 0 && c > 0, "ntg_act_pool_bwd: bad sizes");
   NTG_REQUIRE(act.kind != NTG_ACT_ABRELU || act.stabilize <= 0.f,
               "ntg_act_pool_bwd: do_stabilize is not differentiable here");
-  if (act.kind != NTG_ACT_NONE && act.kind != NTG_ACT_ABRELU && act.kind != NTG_ACT_ERF)
-    return fail(NTG_ERR_UNSUPPORTED, "ntg_act_pool_bwd: adjoints exist for ABRelu and Erf");
+  if (act.kind < NTG_ACT_NONE || act.kind > NTG_ACT_GELU)
+    return fail(NTG_ERR_UNSUPPORTED, "ntg_act_pool_bwd: unknown activation kind");
   const int64_t m = a * a * c * c;
   const bool pow2 = c >= 4 && c <= 32 && (c & (c - 1)) == 0;
   const bool aligned = ((reinterpret_cast<uintptr_t>(q) | reinterpret_cast<uintptr_t>(t) |
@@ -986,6 +1078,10 @@ extern "C" int ntg_act_pool_bwd(void* stream, const float* q, const float* t,
   const int grid = (int)(chunks < 152 * 8 ? chunks : 152 * 8);
   if (act.kind == NTG_ACT_ABRELU)
     act_bwd_fs_kernel<true, true><<<grid, kT, 0, as_stream(stream)>>>(
+        q, t, gq_pooled, gt_pooled, oq, ot, batch, n2, (int)a, (int)c, act, var1, var2, g1, g2, 1,
+        1.f / 16.f);
+  else if (act.kind >= NTG_ACT_SIN)
+    act_bwd_fs_kernel<false, true, true><<<grid, kT, 0, as_stream(stream)>>>(
         q, t, gq_pooled, gt_pooled, oq, ot, batch, n2, (int)a, (int)c, act, var1, var2, g1, g2, 1,
         1.f / 16.f);
   else

@@ -191,7 +191,7 @@ def test_conv_input_gradients_power_of_two_planes(nt):
         assert abs(g2[idx] - want) < 3e-3 * scale, (idx, g2[idx], want)
 
 
-@pytest.mark.parametrize('kind', ['relu', 'erf'])
+@pytest.mark.parametrize('kind', ['relu', 'erf', 'sin', 'rbf', 'gelu'])
 def test_vectorised_activation_vjp_matches_elementwise_kernel(nt, kind):
     """ntg_act_bwd on 16-byte aligned buffers (chunked kernel with reduced variance
     cotangents) against the same call on buffers offset by one float (the
@@ -207,8 +207,11 @@ def test_vectorised_activation_vjp_matches_elementwise_kernel(nt, kind):
             cov[:, a, a, c, c] += 2.
     v1 = L.Var(cov[:n1].data_ptr(), A * A * C * C, A * C * C + C * C, C + 1)
     v2 = L.Var(cov[n1:].data_ptr(), A * A * C * C, A * C * C + C * C, C + 1)
-    act = (L.Act(L.NTG_ACT_ABRELU, 0., 1., 0., 0, 0.) if kind == 'relu' else
-           L.Act(L.NTG_ACT_ERF, 1., 1., 0., 0, 0.))
+    act = {'relu': L.Act(L.NTG_ACT_ABRELU, 0., 1., 0., 0, 0.),
+           'erf': L.Act(L.NTG_ACT_ERF, 1., 1., 0., 0, 0.),
+           'sin': L.Act(L.NTG_ACT_SIN, 1.2, 0.8, float(np.cos(0.6)), 0, 0.),
+           'rbf': L.Act(L.NTG_ACT_RBF, 0.7, 0., 0., 0, 0.),
+           'gelu': L.Act(L.NTG_ACT_GELU, 0., 0., 0., 0, 0.)}[kind]
     ins = [torch.rand(shp, device='cuda', generator=g) * 2 - 1 for _ in range(4)]
 
     def run(offset):
@@ -375,5 +378,78 @@ def test_conv_act_pool_fused_gradients_32x32(nt):
         want = fd(lambda a: loss_oracle(a, x2), x1, idx)
         assert abs(g1[idx] - want) < 3e-3 * scale, (idx, g1[idx], want)
     for idx in [(1, 7, 30, 1)]:
+        want = fd(lambda b: loss_oracle(x1, b), x2, idx)
+        assert abs(g2[idx] - want) < 3e-3 * scale, (idx, g2[idx], want)
+
+
+def _rare(m, kind):
+    return {'sin': lambda: m.Sin(1.2, 0.8, 0.3), 'cos': lambda: m.Cos(1.0, 1.1, 0.2),
+            'rbf': lambda: m.Rbf(0.7), 'gelu': lambda: m.Gelu()}[kind]()
+
+
+@pytest.mark.parametrize('kind', ['sin', 'cos', 'rbf', 'gelu'])
+def test_rare_activation_fcn_gradients(nt, kind):
+    """Sin / Cos / Rbf / Gelu adjoints (elementwise kernel) in a Dense network:
+    d/d(W_std, b_std) and d/dx against central finite differences of the oracle."""
+    rng = np.random.default_rng(21)
+    x = rng.standard_normal((5, 12)) * 0.8
+    wq, wt = rng.standard_normal((5, 5)), rng.standard_normal((5, 5))
+    hp = np.array([1.2, 0.1, 0.9, 0.2, 1.1, 0.05])
+
+    def layers(m, h):
+        return [m.Dense(8, h[0], h[1]), _rare(m, kind), m.Dense(8, h[2], h[3]), _rare(m, kind),
+                m.Dense(1, h[4], h[5])]
+
+    def loss_oracle(h, xx):
+        q, t = o.serial(*layers(o, h))(xx, None, ('nngp', 'ntk'))
+        return float(np.sum(wq * q) + np.sum(wt * t))
+
+    ht = [torch.tensor(v, device='cuda', requires_grad=True) for v in hp]
+    xt = torch.tensor(x, dtype=torch.float32, device='cuda', requires_grad=True)
+    q, t = nt.stax.serial(*layers(nt.stax, ht))[2](xt, None, ('nngp', 'ntk'))
+    loss = (torch.from_numpy(wq).float().cuda() * q).sum() + \
+        (torch.from_numpy(wt).float().cuda() * t).sum()
+    loss.backward()
+    got = np.array([v.grad.item() for v in ht])
+    want = np.array([fd(lambda h: loss_oracle(h, x), hp, i) for i in range(len(hp))])
+    np.testing.assert_allclose(got, want, rtol=2e-3, atol=2e-3 * np.abs(want).max())
+    gx = xt.grad.cpu().numpy()
+    scale = np.abs(gx).max()
+    for idx in [(0, 0), (2, 7), (4, 11)]:
+        wx = fd(lambda xx: loss_oracle(hp, xx), x, idx)
+        assert abs(gx[idx] - wx) < 3e-3 * scale, (idx, gx[idx], wx)
+
+
+@pytest.mark.parametrize('kind', ['sin', 'rbf', 'gelu'])
+def test_rare_activation_conv_gradients(nt, kind):
+    """8 x 8 images: the chunked activation VJP with the rare rules compiled in, its
+    AvgPool-composed form and, at 4 x 4, the elementwise kernel."""
+    rng = np.random.default_rng(22)
+    x1 = rng.standard_normal((2, 8, 8, 2)) * 0.7
+    x2 = rng.standard_normal((1, 8, 8, 2)) * 0.7
+    wq, wt = rng.standard_normal((2, 1)), rng.standard_normal((2, 1))
+
+    def layers(m):
+        return [m.Conv(2, (3, 3), padding='SAME', W_std=1.2, b_std=0.1), _rare(m, kind),
+                m.Conv(2, (3, 3), padding='SAME', W_std=1.1, b_std=0.0), _rare(m, kind),
+                m.AvgPool((2, 2), (2, 2)), m.Conv(2, (3, 3), padding='SAME', W_std=1.0, b_std=0.2),
+                _rare(m, kind), m.GlobalAvgPool(), m.Dense(1, 1.1, 0.05)]
+
+    def loss_oracle(a, b):
+        q, t = o.serial(*layers(o))(a, b, ('nngp', 'ntk'))
+        return float(np.sum(wq * q) + np.sum(wt * t))
+
+    t1 = torch.tensor(x1, dtype=torch.float32, device='cuda', requires_grad=True)
+    t2 = torch.tensor(x2, dtype=torch.float32, device='cuda', requires_grad=True)
+    q, t = nt.stax.serial(*layers(nt.stax))[2](t1, t2, ('nngp', 'ntk'))
+    loss = (torch.from_numpy(wq).float().cuda() * q).sum() + \
+        (torch.from_numpy(wt).float().cuda() * t).sum()
+    loss.backward()
+    g1, g2 = t1.grad.cpu().numpy(), t2.grad.cpu().numpy()
+    scale = max(np.abs(g1).max(), np.abs(g2).max())
+    for idx in [(0, 0, 0, 0), (1, 3, 2, 1), (0, 7, 7, 1)]:
+        want = fd(lambda a: loss_oracle(a, x2), x1, idx)
+        assert abs(g1[idx] - want) < 3e-3 * scale, (idx, g1[idx], want)
+    for idx in [(0, 4, 5, 0)]:
         want = fd(lambda b: loss_oracle(x1, b), x2, idx)
         assert abs(g2[idx] - want) < 3e-3 * scale, (idx, g2[idx], want)
