@@ -83,8 +83,8 @@ def plan_chain(specs, x_shape, diagonal_spatial: bool) -> Optional[ChainPlan]:
             is_gaussian = True
             if i + 1 < len(spatial) and spatial[i + 1].kind == 'act':
                 act = spatial[i + 1].params
-                if act.get('do_stabilize') or act['fn'] not in ('abrelu', 'erf'):
-                    return None  # the fused kernel carries the ReLU-family and Erf rules
+                if act.get('do_stabilize'):
+                    return None  # the stabilised ABRelu rescales by the pre-activation maximum
                 is_gaussian = False
                 i += 1
             convs.append((p, act, cin))

@@ -57,8 +57,9 @@ __device__ __forceinline__ void zero_slot(float* q, float* t, int n) {
 // `vmaps` holds this segment's variance maps, layer k at vmaps + 4*k*S*S:
 // var1, var2, sqrt(var1), sqrt(var2) as S x S maps; `out_slots` is the next segment's
 // slot region ([parity][tensor][S/2][S/2 * S/2]).
-// RO: the network's activations are all of the ABRelu family (the Erf rule is left out).
-template <int S, int NC, bool FIRST, bool LAST, bool RO = false>
+// RO: which activation rules are compiled in — 0: ABRelu and Erf, 1: the ABRelu
+// family only, 2: every rule (Sin / Rbf / Gelu as well).
+template <int S, int NC, bool FIRST, bool LAST, int RO = 0>
 __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg, int lbase,
                                              const float* vmaps, float* out_slots, int delta,
                                              const float* in_q, const float* in_t) {
@@ -170,8 +171,8 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
           apply_affine(af, cq, ct, true, q, t, 1.f / 9.f);
           if (ac.kind != NTG_ACT_NONE && on) {
             const int i1 = p * S + c0 + u, i2 = (p + delta) * S + wp[u];
-            act_apply<false, !RO>(ac, q, t, vm[i1], vm[S * S + i2], vm[2 * S * S + i1],
-                                  vm[3 * S * S + i2]);
+            act_apply<RO == 2, RO != 1>(ac, q, t, vm[i1], vm[S * S + i2], vm[2 * S * S + i1],
+                                        vm[3 * S * S + i2]);
           }
           oq[u] = q;
           ot[u] = t;
@@ -246,7 +247,7 @@ __device__ __forceinline__ void process_line(ChainCtx& cx, const ntg_chain_t& pg
 // Thread t owns columns 2(t % 16), 2(t % 16) + 1 of skewed row t / 16. The
 // per-lane operation sequence equals the scalar path's, so the result is bit
 // for bit the same as process_line's and as the materialised layer kernels'.
-template <int NC, bool LAST, bool RO = false, int COMP = -1, int KC = 0>
+template <int NC, bool LAST, int RO = 0, int COMP = -1, int KC = 0>
 __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, const float* vmaps,
                                          float* out_slots, int delta) {
   constexpr int S = 32;
@@ -327,7 +328,7 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
           const P2 v1 = p2ld(vm + i1), sv1 = p2ld(vm + 2 * S * S + i1);
           const float* v2r = vm + S * S + i2;
           const float* s2r = vm + 3 * S * S + i2;
-          if (RO || (ac.kind == NTG_ACT_ABRELU && ac.stab <= 0.f)) {
+          if (RO == 1 || (ac.kind == NTG_ACT_ABRELU && ac.stab <= 0.f)) {
             abrelu2<COMP>(ac, q, t, v1, p2(v2r[wp0], v2r[wp1]), sv1, p2(s2r[wp0], s2r[wp1]));
           } else {
             float qa, qb, ta, tb, va, vb, sa, sb;
@@ -335,8 +336,8 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
             p2u(t, ta, tb);
             p2u(v1, va, vb);
             p2u(sv1, sa, sb);
-            act_apply<false>(ac, qa, ta, va, v2r[wp0], sa, s2r[wp0]);
-            act_apply<false>(ac, qb, tb, vb, v2r[wp1], sb, s2r[wp1]);
+            act_apply<RO == 2>(ac, qa, ta, va, v2r[wp0], sa, s2r[wp0]);
+            act_apply<RO == 2>(ac, qb, tb, vb, v2r[wp1], sb, s2r[wp1]);
             q = p2(qa, qb);
             t = p2(ta, tb);
           }
@@ -390,7 +391,7 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
 }
 
 // NCT >= 0: the segment's conv count is known at compile time (one instantiation).
-template <int S, bool LAST, int NCT = -1, bool RO = false>
+template <int S, bool LAST, int NCT = -1, int RO = 0>
 __device__ __forceinline__ void process_pooled_line(ChainCtx& cx, const ntg_chain_t& pg, int ncv,
                                                     int lbase, const float* vmaps,
                                                     const float* in_slots, float* out_slots,
@@ -425,7 +426,7 @@ __device__ __forceinline__ void tri_pair(int64_t p, int64_t n, int64_t& i, int64
 
 // NSEG > 0: segment count and conv counts N1, N2 fixed at compile time (the common
 // Myrtle shapes), so that only the code this network runs is in the kernel.
-template <int N0, int NSEG, int N1, int N2, bool RO, int COMP, int KC>
+template <int N0, int NSEG, int N1, int N2, int RO, int COMP, int KC>
 __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* __restrict__ x1,
                                            const float* __restrict__ x2, int64_t gi, int64_t gj,
                                            const float* __restrict__ var1,
@@ -565,7 +566,7 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
 // tile of x1 with itself whose row and column ranges are disjoint. For sym != 0
 // out points at element (0, 0) of the whole kernel and each result is written at
 // (gi, gj) and (gj, gi).
-template <int N0, int NSEG = 0, int N1 = 0, int N2 = 0, bool RO = false, int COMP = -1,
+template <int N0, int NSEG = 0, int N1 = 0, int N2 = 0, int RO = 0, int COMP = -1,
           int KC = 0>
 __global__ void __launch_bounds__(NT, 1)
     chain_fwd_kernel(const __grid_constant__ ntg_chain_t pg, const float* __restrict__ x1,
@@ -607,7 +608,7 @@ using namespace ntg;
 
 namespace {
 
-template <int N0, int NSEG, int N1, int N2, bool RO = false, int COMP = -1, int KC = 0>
+template <int N0, int NSEG, int N1, int N2, int RO = 0, int COMP = -1, int KC = 0>
 cudaError_t launch_chain_k(unsigned grid, size_t sm, cudaStream_t s, const ntg_chain_t& pg,
                            const float* x1, const float* x2, int64_t r0, int64_t n1, int64_t c0,
                            int64_t n2, const float* var1, const float* var2, float* out_q,
@@ -633,20 +634,20 @@ cudaError_t launch_myrtle(bool relu_only, unsigned grid, size_t sm, cudaStream_t
     // three input channels (images) get their own instantiation
     if (comp)
       return pg.channels == 3
-                 ? launch_chain_k<N0, 3, N1, N2, true, 1, 3>(grid, sm, s, pg, x1, x2, r0, n1,
+                 ? launch_chain_k<N0, 3, N1, N2, 1, 1, 3>(grid, sm, s, pg, x1, x2, r0, n1,
                                                              c0, n2, var1, var2, out_q, out_t,
                                                              ld_out, sym)
-                 : launch_chain_k<N0, 3, N1, N2, true, 1>(grid, sm, s, pg, x1, x2, r0, n1, c0,
+                 : launch_chain_k<N0, 3, N1, N2, 1, 1>(grid, sm, s, pg, x1, x2, r0, n1, c0,
                                                           n2, var1, var2, out_q, out_t, ld_out,
                                                           sym);
     return pg.channels == 3
-               ? launch_chain_k<N0, 3, N1, N2, true, 0, 3>(grid, sm, s, pg, x1, x2, r0, n1, c0,
+               ? launch_chain_k<N0, 3, N1, N2, 1, 0, 3>(grid, sm, s, pg, x1, x2, r0, n1, c0,
                                                            n2, var1, var2, out_q, out_t, ld_out,
                                                            sym)
-               : launch_chain_k<N0, 3, N1, N2, true, 0>(grid, sm, s, pg, x1, x2, r0, n1, c0, n2,
+               : launch_chain_k<N0, 3, N1, N2, 1, 0>(grid, sm, s, pg, x1, x2, r0, n1, c0, n2,
                                                         var1, var2, out_q, out_t, ld_out, sym);
   }
-  return launch_chain_k<N0, 3, N1, N2, false>(grid, sm, s, pg, x1, x2, r0, n1, c0, n2, var1,
+  return launch_chain_k<N0, 3, N1, N2, 0>(grid, sm, s, pg, x1, x2, r0, n1, c0, n2, var1,
                                               var2, out_q, out_t, ld_out, sym);
 }
 
@@ -668,10 +669,12 @@ int launch_chain(const char* who, void* stream, const ntg_chain_t* prog, const f
     nl += pg.nconv[sg];
   }
   NTG_REQUIRE(nl <= NTG_CHAIN_MAX_LAYERS, w + ": too many layers");
-  for (int l = 0; l < nl; ++l)
-    NTG_REQUIRE(pg.act[l].kind == NTG_ACT_NONE || pg.act[l].kind == NTG_ACT_ABRELU ||
-                    pg.act[l].kind == NTG_ACT_ERF,
-                w + ": the fused chain carries the ABRelu and Erf rules only");
+  bool rare = false;  // Sin / Rbf / Gelu: the instances with every rule compiled in
+  for (int l = 0; l < nl; ++l) {
+    NTG_REQUIRE(pg.act[l].kind >= NTG_ACT_NONE && pg.act[l].kind <= NTG_ACT_GELU,
+                w + ": unknown activation kind");
+    rare = rare || pg.act[l].kind >= NTG_ACT_SIN;
+  }
   NTG_REQUIRE(pg.readout == 0 || pg.readout == 1, w + ": readout must be 0 or 1");
   NTG_REQUIRE(n1 > 0 && n2 > 0 && r0 >= 0 && c0 >= 0, w + ": bad tile");
   NTG_REQUIRE(sym ? ld_out >= (r0 + n1 > c0 + n2 ? r0 + n1 : c0 + n2) : ld_out >= n2,
@@ -689,7 +692,14 @@ int launch_chain(const char* who, void* stream, const ntg_chain_t* prog, const f
   bool relu_only = true;
   for (int l = 0; l < nl; ++l)
     relu_only = relu_only && (pg.act[l].kind == NTG_ACT_NONE || pg.act[l].kind == NTG_ACT_ABRELU);
-  if (pg.nseg == 3 && n0 == 2 && c1 == 1 && c2 == 1)
+  if (rare)
+    e = n0 == 1 ? launch_chain_k<1, 0, 0, 0, 2>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1,
+                                                var2, out_q, out_t, ld_out, sym)
+        : n0 == 2 ? launch_chain_k<2, 0, 0, 0, 2>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1,
+                                                  var2, out_q, out_t, ld_out, sym)
+                  : launch_chain_k<3, 0, 0, 0, 2>(grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1,
+                                                  var2, out_q, out_t, ld_out, sym);
+  else if (pg.nseg == 3 && n0 == 2 && c1 == 1 && c2 == 1)
     e = launch_myrtle<2, 1, 1>(relu_only, grid, sm, s, pg, x1, x2, r0, n1_, c0, n2_, var1, var2,
                                out_q, out_t, ld_out, sym);
   else if (pg.nseg == 3 && n0 == 2 && c1 == 2 && c2 == 2)

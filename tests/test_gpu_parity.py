@@ -325,8 +325,8 @@ def test_edge_batches(nt):
 @pytest.mark.parametrize('act', ['gelu', 'sin', 'cos', 'rbf'])
 def test_more_dual_activations_vs_oracle(nt, act, cifar_like):
     """Gelu, Sin, Cos and Rbf (elementwise.py:195-400) as epilogues of the Dense rule (flat
-    inputs) and of the materialised conv rule, on 6x6 and on 32x32 images (the latter take
-    the per-layer kernels: the fused whole-network kernel carries ReLU and Erf only)."""
+    inputs), of the materialised conv rule (6x6 images) and of the fused whole-network kernel
+    (32x32 images; checked against the oracle and against the per-layer kernels)."""
     def mk(m):
         return {'gelu': m.Gelu(), 'sin': m.Sin(1.2, 0.8, 0.3), 'cos': m.Cos(0.9, 1.1, -0.2),
                 'rbf': m.Rbf(0.4)}[act]
@@ -347,8 +347,14 @@ def test_more_dual_activations_vs_oracle(nt, act, cifar_like):
                      m.AvgPool((2, 2), (2, 2)), m.Conv(1, (3, 3), padding='SAME', W_std=1.2),
                      mk(m), m.GlobalAvgPool(), m.Dense(1, 1.0, 0.)]
     from nt_gb300 import _chain
+    from nt_gb300.stax import _Ctx, _input_kernel, _as_input
     kf = nt.stax.serial(*lay(nt.stax))[2]
-    assert _chain.plan_chain(kf.specs, x1.shape, False) is None
+    assert _chain.plan_chain(kf.specs, x1.shape, False) is not None
     got, want = both(nt, lay, x1[:2], x2, get=('nngp', 'ntk'))
     for g, w in zip(got, want):
         assert elem_rel_err(g, w) < RTOL
+    ctx = _Ctx('fp32')
+    k = _input_kernel(_as_input(x1[:2]), _as_input(x2), False, True, False, ctx)
+    k = kf.apply_kernel(k, ctx)
+    assert rel_err(got[0], cpu(k.nngp)) < 2e-6
+    assert rel_err(got[1], cpu(k.ntk)) < 2e-6
