@@ -124,6 +124,12 @@ int ntg_cov_diag(void* stream, const float* x, int64_t n, int64_t d, float* cov)
  * per-sample cov [N, A, A, C, C] (requirements.py:529-539). */
 int ntg_input_fs(void* stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
                  int64_t a, int64_t c, int64_t k, int32_t pairs, float* out);
+/* Diagonal-spatial input covariances (requirements.py:641-830 with
+ * diagonal_spatial = True): x1 [N1, P, K], x2 [N2, P, K] over P spatial
+ * positions -> nngp [N1, N2, P] = sum_k x1 x2 / K; with x2 == NULL and n2 == 0
+ * the per-sample cov [N1, P] (same channel order, so self pairs agree exactly). */
+int ntg_input_ds(void* stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
+                 int64_t p, int64_t k, float* out);
 
 /* ---- Conv / Dense / activations on materialised kernels --------------- */
 /* Full-spatial shared-weight convolution rule (linear.py:1321-1424,
@@ -320,6 +326,11 @@ int ntg_input_fs_bwd(void* stream, const float* g, const float* x_other, float* 
 int ntg_input_fs_bwd2(void* stream, const float* g, const float* x1, const float* x2,
                       float* gx1, float* gx2, int64_t n1, int64_t n2, int64_t a, int64_t c,
                       int64_t k);
+/* Adjoint of ntg_input_ds, ADDING into gx1 [N1, P, K] and gx2 [N2, P, K]:
+ * pairs g [N1, N2, P] (gx2 may be gx1 when x2 is x1), or with n2 == 0 the
+ * per-sample covariances g [N1, P] of x1 (x2, gx2 unused). */
+int ntg_input_ds_bwd(void* stream, const float* g, const float* x1, const float* x2,
+                     float* gx1, float* gx2, int64_t n1, int64_t n2, int64_t p, int64_t k);
 /* C [m, n] (+)= alpha op(A) B, op(A) = A [m, k] or, trans_a != 0, A^T with A [k, m]
  * (flat Gram adjoint). */
 int ntg_gemm_ex(void* stream, const float* a, const float* b, float* c, int64_t m, int64_t n,

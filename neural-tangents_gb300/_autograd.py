@@ -2,7 +2,9 @@
 layer rule, the counterpart of a ``jax.custom_vjp`` pair. Each forward calls
 the layer's sm_103a kernels, each backward its hand-written adjoint kernels
 (csrc/ntg_bwd.cu); gradients flow to the inputs x1, x2 and to W_std / b_std
-given as tensors. Scope: full-spatial or flat kernels, NTK parameterisation.
+given as tensors. Scope: full-spatial, diagonal-spatial (``ds``: kernels
+[N1, N2, *spatial] holding only the (h, h, w, w) entries) or flat kernels, NTK
+parameterisation.
 """
 from __future__ import annotations
 
@@ -49,6 +51,17 @@ def _batch(x: torch.Tensor, bnd: int) -> int:
     return int(math.prod(x.shape[:bnd]))
 
 
+def _positions(x: torch.Tensor, bnd: int) -> int:
+    """Spatial positions of a diagonal-spatial kernel."""
+    return int(math.prod(x.shape[bnd:]))
+
+
+def _ds_var(cov: torch.Tensor) -> L.Var:
+    """The variances of a diagonal-spatial per-sample kernel [N, *spatial]: the kernel itself,
+    viewed as [N, P, 1]."""
+    return L.Var(L.ptr(cov), _positions(cov, 1), 1, 0)
+
+
 def _f(x) -> float:
     return float(x.item()) if isinstance(x, torch.Tensor) else float(x)
 
@@ -58,10 +71,15 @@ class InputFn(torch.autograd.Function):
     """requirements.py:641-830: inputs -> (nngp, cov1, cov2)."""
 
     @staticmethod
-    def forward(ctx, x1, x2, gram_precision=0):
+    def forward(ctx, x1, x2, gram_precision=0, ds=False):
         x2o = _opt(x2)
         xb = x1 if x2o is None else x2o
-        if x1.ndim == 2:
+        ctx.ds = ds and x1.ndim > 2
+        if ctx.ds:
+            nngp = O.input_ds(x1, xb)
+            cov1 = O.input_ds(x1, None)
+            cov2 = _e(x1.device) if x2o is None else O.input_ds(x2o, None)
+        elif x1.ndim == 2:
             nngp = O.gram(x1, xb, gram_precision)
             cov1 = torch.diagonal(nngp).contiguous() if x2o is None else O.cov_diag(x1)
             cov2 = _e(x1.device) if x2o is None else O.cov_diag(x2o)
@@ -88,6 +106,18 @@ class InputFn(torch.autograd.Function):
         gx1 = torch.zeros_like(x1)
         gx2 = None if x2o is None else torch.zeros_like(x2o)
         gn = gn.contiguous()
+        if ctx.ds:
+            n1, k = x1.shape[0], x1.shape[-1]
+            p = int(math.prod(x1.shape[1:-1]))
+            xb = x1 if x2o is None else x2o
+            L.call('ntg_input_ds_bwd', s, L.ptr(gn), L.ptr(x1), L.ptr(xb), L.ptr(gx1),
+                   L.ptr(gx1 if x2o is None else gx2), n1, xb.shape[0], p, k)
+            for gcv, xx, gg in ((gc1, x1, gx1), (gc2, x2o, gx2)):
+                if xx is None or gcv is None:
+                    continue
+                L.call('ntg_input_ds_bwd', s, L.ptr(gcv.contiguous()), L.ptr(xx), None,
+                       L.ptr(gg), None, xx.shape[0], 0, p, k)
+            return gx1, gx2, None, None
         if x1.ndim == 2:
             n1, d = x1.shape
             xb = x1 if x2o is None else x2o
@@ -99,7 +129,7 @@ class InputFn(torch.autograd.Function):
             if x2o is not None:
                 L.call('ntg_cov_diag_bwd', s, L.ptr(gc2.contiguous()), L.ptr(x2o), L.ptr(gx2),
                        n2, d)
-            return gx1, gx2, None
+            return gx1, gx2, None, None
         y1 = x1 if x1.ndim == 4 else x1.unsqueeze(2)
         yb = None if x2o is None else (x2o if x2o.ndim == 4 else x2o.unsqueeze(2))
         gy1 = gx1 if x1.ndim == 4 else gx1.unsqueeze(2)
@@ -114,7 +144,7 @@ class InputFn(torch.autograd.Function):
                 continue
             L.call('ntg_input_fs_bwd2', s, L.ptr(gcv.contiguous()), L.ptr(yy), None, L.ptr(gg),
                    None, yy.shape[0], 0, a, c, k)
-        return gx1, gx2, None
+        return gx1, gx2, None, None
 
 
 # ---------------------------------------------------------------------------
@@ -134,13 +164,16 @@ class AffineFn(torch.autograd.Function):
     """Dense rule (linear.py:899-926) on all four tensors, NTK parameterisation."""
 
     @staticmethod
-    def forward(ctx, w2t, b2t, q, t, c1, c2):
+    def forward(ctx, w2t, b2t, q, t, c1, c2, ds=False):
         w2, b2 = _f(w2t), _f(b2t)
         aff = O.affine(w2, b2, w2)
         zero_t = _zero_ntk(t)
         c2o = _opt(c2)
 
         def aa(x, xt, want_t, bnd):
+            if ds:  # elementwise: the entries as [batch, P] diagonal-spatial kernels
+                return O.affine_act(x.contiguous(), xt, _batch(x, bnd), 0, _positions(x, bnd), 1,
+                                    True, True, aff, O.NO_ACT, O.NO_VAR, O.NO_VAR, want_t)
             a, c = _ac(x, bnd)
             return O.affine_act(x.contiguous(), xt, _batch(x, bnd), 0, a, c, False, True, aff,
                                 O.NO_ACT, O.NO_VAR, O.NO_VAR, want_t)
@@ -177,21 +210,29 @@ class AffineFn(torch.autograd.Function):
         else:
             gw2 = gb2 = None
         return (gw2, gb2, gu.reshape(qn.shape), None if ctx.zero_t else gut.reshape(qn.shape),
-                gc1i, gc2i)
+                gc1i, gc2i, None)
 
 
 class ConvFn(torch.autograd.Function):
     """Full-spatial Conv rule (linear.py:1321-1424), NTK parameterisation."""
 
     @staticmethod
-    def forward(ctx, w2t, b2t, q, t, c1, c2, geom):
+    def forward(ctx, w2t, b2t, q, t, c1, c2, geom, ds=False):
         w2, b2 = _f(w2t), _f(b2t)
         aff = O.affine(w2, b2, w2)
         fh, fw, sh, sw, ph, pw, ao, co, circ, nsp = geom
         zero_t = _zero_ntk(t)
         c2o = _opt(c2)
+        ctx.ds = ds
 
         def conv(x, xt, want_t, bnd):
+            if ds:  # linear.py:3381-3437
+                lead = tuple(x.shape[:bnd])
+                a = x.shape[bnd]
+                c = x.shape[bnd + 1] if nsp == 2 else 1
+                return O.conv_ds(x.contiguous(), None if xt is None else xt.contiguous(),
+                                 _batch(x, bnd), a, c, fh, fw, sh, sw, ph, pw, ao, co, circ, aff,
+                                 want_t, lead, nsp == 2)
             x4 = _as4(x.contiguous(), bnd)
             a, c = _ac(x, bnd)
             n2 = 0 if bnd == 1 else x.shape[1]
@@ -221,6 +262,8 @@ class ConvFn(torch.autograd.Function):
         s = L.stream()
         dev = qn.device
 
+        ds = getattr(ctx, 'ds', False)
+
         def back(g, gtt, in_shape, bnd, want_t_in=True):
             n = int(math.prod(g.shape)) if g is not None else int(math.prod(gtt.shape))
             gu = torch.empty(n, device=dev)
@@ -230,7 +273,7 @@ class ConvFn(torch.autograd.Function):
                    None if gut is None else L.ptr(gut), n, aff, scale)
             lead = in_shape[:bnd]
             a = in_shape[bnd]
-            c = in_shape[bnd + 2] if nsp == 2 else 1
+            c = (in_shape[bnd + 1] if ds else in_shape[bnd + 2]) if nsp == 2 else 1
             batch = int(math.prod(lead))
             outs = []
             for gg in (gu, gut):
@@ -239,7 +282,7 @@ class ConvFn(torch.autograd.Function):
                     continue
                 gin = torch.empty(in_shape, device=dev)
                 L.call('ntg_stencil_bwd', s, L.ptr(gg), L.ptr(gin), batch, a, c, fh, fw, sh, sw,
-                       ph, pw, ao, co, int(circ), 0)
+                       ph, pw, ao, co, int(circ), int(ds))
                 outs.append(gin)
             return outs
 
@@ -267,7 +310,7 @@ class ConvFn(torch.autograd.Function):
                                    O.NO_VAR, O.NO_VAR, True, lead)
             return [gqi_.reshape(in_shape), gti_.reshape(in_shape)]
 
-        symmetric = (sh == 1 and sw == 1 and fh % 2 == 1 and fw % 2 == 1 and
+        symmetric = (not ds and sh == 1 and sw == 1 and fh % 2 == 1 and fw % 2 == 1 and
                      2 * ph + 1 == fh and 2 * pw + 1 == fw and ao == qs[2] and
                      (nsp == 1 or co == qs[4]))
         # the output NTK's cotangent reaches the input nngp through ntk_out = nngp_out + ...
@@ -293,7 +336,7 @@ class ConvFn(torch.autograd.Function):
             gw2, gb2 = acc[0].float(), acc[1].float()
         else:
             gw2 = gb2 = None
-        return gw2, gb2, gqi, gti, gc1i, gc2i, None
+        return gw2, gb2, gqi, gti, gc1i, gc2i, None, None
 
 
 # ---------------------------------------------------------------------------
@@ -305,9 +348,12 @@ class ActFn(torch.autograd.Function):
     """Activation rule (elementwise.py:423-477 ABRelu, :67-112 Erf) on all four tensors."""
 
     @staticmethod
-    def forward(ctx, q, t, c1, c2, act):
+    def forward(ctx, q, t, c1, c2, act, ds=False):
         c2o = _opt(c2)
         zero_t = _zero_ntk(t)
+        ctx.ds = ds
+        if ds:
+            return ActFn._forward_ds(ctx, q, t, c1, c2o, act, zero_t)
         a, c = _ac(q, 2)
         q4, c14 = _as4(q.contiguous(), 2), _as4(c1.contiguous(), 1)
         c24 = None if c2o is None else _as4(c2o.contiguous(), 1)
@@ -332,7 +378,68 @@ class ActFn(torch.autograd.Function):
                 c2n if c2o is None else c2n.reshape(c2o.shape))
 
     @staticmethod
+    def _forward_ds(ctx, q, t, c1, c2o, act, zero_t):
+        """The activation rule on diagonal-spatial kernels [N1, N2, *spatial]: the variances
+        of a position are the per-sample kernels themselves."""
+        p = _positions(q, 2)
+        n1, n2 = q.shape[0], q.shape[1]
+        q, c1 = q.contiguous(), c1.contiguous()
+        c2o = None if c2o is None else c2o.contiguous()
+        v1 = _ds_var(c1)
+        v2 = _ds_var(c2o if c2o is not None else c1)
+        qn, tn = O.affine_act(q, None if zero_t else t.contiguous(), n1 * n2, n2, p, 1, True,
+                              False, O.IDENTITY_AFFINE, act, v1, v2, not zero_t)
+
+        def self_act(cv):
+            vv = _ds_var(cv)
+            return O.affine_act(cv, None, cv.shape[0], 0, p, 1, True, False, O.IDENTITY_AFFINE,
+                                act, vv, vv, False)[0]
+
+        c1n = self_act(c1)
+        c2n = _e(q.device) if c2o is None else self_act(c2o)
+        ctx.save_for_backward(q, t if not zero_t else _e(q.device), c1,
+                              _e(q.device) if c2o is None else c2o)
+        ctx.act, ctx.zero_t = act, zero_t
+        return qn, t.clone() if zero_t else tn, c1n, c2n
+
+    @staticmethod
+    def _backward_ds(ctx, gq, gt, gc1, gc2):
+        q, t, c1, c2 = ctx.saved_tensors
+        act, zero_t = ctx.act, ctx.zero_t
+        c2o = _opt(c2)
+        s = L.stream()
+        p = _positions(q, 2)
+        n1, n2 = q.shape[0], q.shape[1]
+        v1 = _ds_var(c1)
+        v2 = _ds_var(c2o if c2o is not None else c1)
+        gd1 = torch.zeros((n1, p), device=q.device)
+        gd2 = gd1 if c2o is None else torch.zeros((c2o.shape[0], p), device=q.device)
+        gqi = torch.empty_like(q)
+        gti = None if zero_t else torch.empty_like(q)
+        L.call('ntg_act_bwd', s, L.ptr(q), None if zero_t else L.ptr(t),
+               None if gq is None else L.ptr(gq.contiguous()),
+               None if (gt is None or zero_t) else L.ptr(gt.contiguous()), L.ptr(gqi),
+               None if gti is None else L.ptr(gti), n1 * n2, n2, p, 1, 1, act, v1, v2,
+               gd1.data_ptr(), gd2.data_ptr())
+
+        def self_back(cv, gcv, gd):
+            vv = _ds_var(cv)
+            out = torch.empty_like(cv)
+            L.call('ntg_act_bwd', s, L.ptr(cv), None,
+                   None if gcv is None else L.ptr(gcv.contiguous()), None, L.ptr(out), None,
+                   cv.shape[0], 0, p, 1, 1, act, vv, vv, gd.data_ptr(), gd.data_ptr())
+            # every entry of a diagonal-spatial per-sample kernel is a variance
+            L.call('ntg_diag_add', s, gd.data_ptr(), L.ptr(out), cv.shape[0], p, 1, p, 1, 0)
+            return out
+
+        gc1i = self_back(c1, gc1, gd1)
+        gc2i = None if c2o is None else self_back(c2o, gc2, gd2)
+        return gqi, None if zero_t else gti, gc1i, gc2i, None, None
+
+    @staticmethod
     def backward(ctx, gq, gt, gc1, gc2):
+        if getattr(ctx, 'ds', False):
+            return ActFn._backward_ds(ctx, gq, gt, gc1, gc2)
         q, t, c1, c2 = ctx.saved_tensors
         act, zero_t = ctx.act, ctx.zero_t
         c2o = _opt(c2)
@@ -370,7 +477,8 @@ class ActFn(torch.autograd.Function):
         # each self VJP adds its own and folds the total into its diagonal.
         gc1i = self_back(c14, gc1, gd1).reshape(c1.shape)
         gc2i = None if c24 is None else self_back(c24, gc2, gd2).reshape(c2o.shape)
-        return (gqi.reshape(q.shape), None if zero_t else gti.reshape(q.shape), gc1i, gc2i, None)
+        return (gqi.reshape(q.shape), None if zero_t else gti.reshape(q.shape), gc1i, gc2i, None,
+                None)
 
 
 class ActPoolFn(torch.autograd.Function):
@@ -540,18 +648,21 @@ def act_pool_fusable(q: torch.Tensor, pool_geom) -> bool:
 # ---------------------------------------------------------------------------
 class PoolFn(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, q, t, c1, c2, geom):
+    def forward(ctx, q, t, c1, c2, geom, ds=False):
         a, c, wa, wc, sa, sc, pa, pc, ao, co, circ, avg, ne, two_d = geom
 
         def run(x, bnd):
             if x is None or x.ndim == 0 or x.numel() == 0:
                 return x
             lead = tuple(x.shape[:bnd])
-            shape = lead + ((ao, ao, co, co) if two_d else (ao, ao))
+            if ds:
+                shape = lead + ((ao, co) if two_d else (ao,))
+            else:
+                shape = lead + ((ao, ao, co, co) if two_d else (ao, ao))
             return O.pool(x.contiguous(), int(math.prod(lead)), a, c, wa, wc, sa, sc, pa, pc, ao,
-                          co, circ, False, avg, ne, shape)
+                          co, circ, ds, avg, ne, shape)
 
-        ctx.geom = geom
+        ctx.geom, ctx.ds = geom, ds
         ctx.shapes = [None if x is None else tuple(x.shape) for x in (q, t, c1, c2)]
         return run(q, 2), run(t, 2), run(c1, 1), run(c2, 1)
 
@@ -566,26 +677,29 @@ class PoolFn(torch.autograd.Function):
                 continue
             gin = torch.empty(shp, device=g.device)
             L.call('ntg_pool_bwd', s, L.ptr(g.contiguous()), L.ptr(gin),
-                   int(math.prod(shp[:bnd])), a, c, wa, wc, sa, sc, pa, pc, ao, co, int(circ), 0,
-                   int(avg), int(ne))
+                   int(math.prod(shp[:bnd])), a, c, wa, wc, sa, sc, pa, pc, ao, co, int(circ),
+                   int(ctx.ds), int(avg), int(ne))
             outs.append(gin)
-        return (*outs, None)
+        return (*outs, None, None)
 
 
 class ReadoutFn(torch.autograd.Function):
     """GlobalAvgPool / GlobalSumPool (linear.py:1771-1801) and Flatten (:1865-1899)."""
 
     @staticmethod
-    def forward(ctx, q, t, c1, c2, kind):
+    def forward(ctx, q, t, c1, c2, kind, ds=False):
         def run(x, bnd):
             if x is None or x.ndim <= bnd or x.numel() == 0:
                 return x
+            if ds:  # the mean of the positions; GlobalAvgPool scales it by 1 / P once more
+                post = 1. / _positions(x, bnd) if kind == 'avg' else 1.
+                return O.global_pool(x.contiguous(), bnd, kind != 'sum', post)
             if kind == 'flatten':
                 a, c = _ac(x, bnd)
                 return O.flatten_fs(_as4(x.contiguous(), bnd), bnd, a, c)
             return O.global_pool(x.contiguous(), bnd, kind == 'avg', 1.)
 
-        ctx.kind = kind
+        ctx.kind, ctx.ds = kind, ds
         ctx.shapes = [None if x is None else tuple(x.shape) for x in (q, t, c1, c2)]
         return run(q, 2), run(t, 2), run(c1, 1), run(c2, 1)
 
@@ -601,14 +715,18 @@ class ReadoutFn(torch.autograd.Function):
             a = shp[bnd]
             c = shp[bnd + 2] if len(shp) == bnd + 4 else 1
             gin = torch.empty(shp, device=g.device)
-            if ctx.kind == 'flatten':
+            if ctx.ds:
+                sc = (1. / m if ctx.kind != 'sum' else 1.) * (1. / m if ctx.kind == 'avg' else 1.)
+                L.call('ntg_readout_bwd', s, L.ptr(g.contiguous()), L.ptr(gin),
+                       int(math.prod(shp[:bnd])), m, 1, 0, m, sc)
+            elif ctx.kind == 'flatten':
                 L.call('ntg_readout_bwd', s, L.ptr(g.contiguous()), L.ptr(gin),
                        int(math.prod(shp[:bnd])), a, c, 1, m, 1. / (a * c))
             else:
                 L.call('ntg_readout_bwd', s, L.ptr(g.contiguous()), L.ptr(gin),
                        int(math.prod(shp[:bnd])), a, c, 0, m, 1. / m if ctx.kind == 'avg' else 1.)
             outs.append(gin)
-        return (*outs, None)
+        return (*outs, None, None)
 
 
 # ---------------------------------------------------------------------------
@@ -633,6 +751,11 @@ def _sq(v, dev):
     return torch.tensor(float(v) ** 2, device=dev)
 
 
+def _ds_ac(q: torch.Tensor) -> tuple[int, int]:
+    """Spatial sizes (A, C) of a diagonal-spatial pair kernel [N1, N2, A(, C)]."""
+    return q.shape[2], (q.shape[3] if q.ndim > 3 else 1)
+
+
 def _pool_geom(q: torch.Tensor, sp):
     """(a, c, windows, strides, pads, output sizes, circular, average, normalize_edges, two_d)
     of a pooling layer applied to the pair kernel q."""
@@ -655,9 +778,10 @@ def _pool_geom_sizes(a: int, c: int, sp):
 
 
 def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: bool,
-           precision: str = 'fp32') -> Kernel:
+           precision: str = 'fp32', diagonal_spatial: bool = False) -> Kernel:
     """kernel_fn(x1, x2) through the differentiable layer Functions ('mixed': the
-    compensated var1 var2 - q^2 in the activation rules and their VJPs)."""
+    compensated var1 var2 - q^2 in the activation rules and their VJPs;
+    diagonal_spatial: the kernels keep only the (h, h, w, w) entries)."""
     from .stax import Padding, _act_struct, _Ctx, _pads
     dev = x1.device
     ctx = _Ctx(precision)
@@ -668,7 +792,8 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
         x2 = None if x2 is None else x2.reshape(x2.shape[0], -1)
     shape1 = tuple(x1.shape)
     shape2 = shape1 if x2 is None else tuple(x2.shape)
-    q, c1, c2 = InputFn.apply(x1, _e(dev) if x2 is None else x2, ctx.gram_precision)
+    ds = bool(diagonal_spatial) and x1.ndim > 2
+    q, c1, c2 = InputFn.apply(x1, _e(dev) if x2 is None else x2, ctx.gram_precision, ds)
     t = torch.zeros((), device=dev) if compute_ntk else None
     is_gaussian, is_reversed = False, False
     skip_next = 0
@@ -684,12 +809,12 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
             w2, b2 = _sq(p['W_std'], dev), _sq(p['b_std'], dev)
             tt = t if t is not None else torch.zeros((), device=dev)
             if sp.kind == 'dense':
-                q, tt, c1, c2 = AffineFn.apply(w2, b2, q, tt, c1, c2)
+                q, tt, c1, c2 = AffineFn.apply(w2, b2, q, tt, c1, c2, ds)
             else:
                 nsp = len(p['filter_shape'])
                 if nsp > 2:
                     raise NotImplementedError('Conv with 1 or 2 spatial dimensions')
-                a, c = _ac(q, 2)
+                a, c = _ds_ac(q) if ds else _ac(q, 2)
                 fh, sh = p['filter_shape'][0], p['strides'][0]
                 fw, sw = (p['filter_shape'][1], p['strides'][1]) if nsp == 2 else (1, 1)
                 ph, ao = _pads(a, fh, sh, p['padding'])
@@ -712,7 +837,7 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
                     is_reversed = not is_reversed
                     t = tt if t is not None else None
                     continue
-                q, tt, c1, c2 = ConvFn.apply(w2, b2, q, tt, c1, c2, geom)
+                q, tt, c1, c2 = ConvFn.apply(w2, b2, q, tt, c1, c2, geom, ds)
                 is_reversed = not is_reversed
             t = tt if t is not None else None
             is_gaussian = True
@@ -730,30 +855,31 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
                 q, tt, c1, c2 = ActPoolFn.apply(q, tt, c1, c2, _act_struct(p, ctx), geom)
                 skip_next = 1
             else:
-                q, tt, c1, c2 = ActFn.apply(q, tt, c1, c2, _act_struct(p, ctx))
+                q, tt, c1, c2 = ActFn.apply(q, tt, c1, c2, _act_struct(p, ctx), ds)
             t = tt if t is not None else None
             is_gaussian = False
         elif sp.kind == 'pool':
-            geom = _pool_geom(q, sp)
+            geom = _pool_geom_sizes(*_ds_ac(q), sp) if ds else _pool_geom(q, sp)
             tt = t if (t is not None and t.ndim > 0) else None
-            q, tt2, c1, c2 = PoolFn.apply(q, tt, c1, c2, geom)
+            q, tt2, c1, c2 = PoolFn.apply(q, tt, c1, c2, geom, ds)
             t = tt2 if tt is not None else t
         elif sp.kind in ('gpool', 'flatten'):
             kind = 'flatten' if sp.kind == 'flatten' else p['pool']
             tt = t if (t is not None and t.ndim > 0) else None
-            q, tt2, c1, c2 = ReadoutFn.apply(q, tt, c1, c2, kind)
+            q, tt2, c1, c2 = ReadoutFn.apply(q, tt, c1, c2, kind, ds)
             t = tt2 if tt is not None else t
             is_reversed = False
+            ds = False
             if sp.kind == 'flatten':
                 is_gaussian = False
         else:
             raise NotImplementedError(sp.kind)
         shape1, shape2 = sp.shape_fn(shape1), sp.shape_fn(shape2)
     c2o = _opt(c2)
-    return Kernel(nngp=from_physical(q, 2, is_reversed, False),
-                  ntk=from_physical(t, 2, is_reversed, False) if compute_ntk else None,
-                  cov1=from_physical(c1, 1, is_reversed, False),
-                  cov2=None if c2o is None else from_physical(c2o, 1, is_reversed, False),
+    return Kernel(nngp=from_physical(q, 2, is_reversed, ds),
+                  ntk=from_physical(t, 2, is_reversed, ds) if compute_ntk else None,
+                  cov1=from_physical(c1, 1, is_reversed, ds),
+                  cov2=None if c2o is None else from_physical(c2o, 1, is_reversed, ds),
                   x1_is_x2=x2 is None, is_gaussian=is_gaussian, is_reversed=is_reversed,
-                  is_input=False, diagonal_batch=True, diagonal_spatial=False, shape1=shape1,
+                  is_input=False, diagonal_batch=True, diagonal_spatial=ds, shape1=shape1,
                   shape2=shape2)

@@ -63,6 +63,7 @@ SIGNATURES = {
     'ntg_gemm': ([_P, _P, _P, _P, _I64, _I64, _I64, _I32], C.c_int),
     'ntg_cov_diag': ([_P, _P, _I64, _I64, _P], C.c_int),
     'ntg_input_fs': ([_P, _P, _P, _I64, _I64, _I64, _I64, _I64, _I32, _P], C.c_int),
+    'ntg_input_ds': ([_P, _P, _P, _I64, _I64, _I64, _I64, _P], C.c_int),
     'ntg_conv_fs': ([_P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, _I32, _I32, _I32, _I32,
                      _I32, _I32, _I64, _I64, _I32, Affine, Act, Var, Var], C.c_int),
     'ntg_conv_act_fs': ([_P, _P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, Affine, Act, Var,
@@ -95,6 +96,7 @@ SIGNATURES = {
     'ntg_readout_bwd': ([_P, _P, _P, _I64, _I64, _I64, _I32, _I64, _F], C.c_int),
     'ntg_input_fs_bwd': ([_P, _P, _P, _P, _I64, _I64, _I64, _I64, _I64, _I64, _I32], C.c_int),
     'ntg_input_fs_bwd2': ([_P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, _I64], C.c_int),
+    'ntg_input_ds_bwd': ([_P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _I64], C.c_int),
     'ntg_gemm_ex': ([_P, _P, _P, _P, _I64, _I64, _I64, _I32, _F, _I32], C.c_int),
     'ntg_cov_diag_bwd': ([_P, _P, _P, _P, _I64, _I64], C.c_int),
     'ntg_diag_add': ([_P, _P, _P, _I64, _I64, _I64, _I64, _I64, _I64], C.c_int),

@@ -5,6 +5,7 @@ the current torch stream and raises NtgError when the library reports one.
 """
 from __future__ import annotations
 
+import math
 from typing import Optional
 
 import torch
@@ -79,6 +80,23 @@ def gram(x1: torch.Tensor, x2: torch.Tensor, precision: int = 0) -> torch.Tensor
 def cov_diag(x: torch.Tensor) -> torch.Tensor:
     out = torch.empty((x.shape[0],), device=x.device, dtype=torch.float32)
     L.call('ntg_cov_diag', L.stream(), L.ptr(x), x.shape[0], x.shape[1], L.ptr(out))
+    return out
+
+
+def input_ds(x1: torch.Tensor, x2: Optional[torch.Tensor]) -> torch.Tensor:
+    """x [N, *spatial, K] -> [N1, N2, *spatial] (pairs) or [N, *spatial] (x2 None): the
+    diagonal-spatial input covariances."""
+    sp = tuple(x1.shape[1:-1])
+    p, k = int(math.prod(sp)), x1.shape[-1]
+    x1 = x1.contiguous()
+    if x2 is None:
+        out = torch.empty((x1.shape[0],) + sp, device=x1.device, dtype=torch.float32)
+        L.call('ntg_input_ds', L.stream(), L.ptr(x1), None, x1.shape[0], 0, p, k, L.ptr(out))
+    else:
+        x2 = x2.contiguous()
+        out = torch.empty((x1.shape[0], x2.shape[0]) + sp, device=x1.device, dtype=torch.float32)
+        L.call('ntg_input_ds', L.stream(), L.ptr(x1), L.ptr(x2), x1.shape[0], x2.shape[0], p, k,
+               L.ptr(out))
     return out
 
 

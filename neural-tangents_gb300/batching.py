@@ -75,7 +75,8 @@ class _CheckpointedKernel(torch.autograd.Function):
                 with torch.enable_grad():
                     a = x1[r0:r0 + rn].detach().requires_grad_(True)
                     b = xb[c0:c0 + cn].detach().requires_grad_(True)
-                    k = _autograd.run_ad(ctx.kfn.specs, a, b, True, ctx.precision)
+                    k = _autograd.run_ad(ctx.kfn.specs, a, b, True, ctx.precision,
+                                         bool(ctx.kfn.diagonal))
                     outs, grads = [], []
                     for o, g in ((k.nngp, gq), (k.ntk, gt)):
                         if g is not None:

@@ -123,7 +123,8 @@ __device__ __forceinline__ void act_vjp(const ntg_act_t& act, float q, float t, 
     const float a = act.a, b = act.b;
     const float factor = (a - b) * (a - b) / (2.f * kPi);
     const float half = 0.5f * (a * a + b * b);
-    const float d = v1 * v2 - q * q;
+    // rounded like the forward rule, so that a self pair (q == v1 == v2) has d == 0 exactly
+    const float d = prod_minus_sq(v1, v2, q, act.compensated);
     const float s = sqrtf(fmaxf(d, 0.f));
     const float th = (s == 0.f && q == 0.f) ? 0.5f * kPi : atan2f(s, q);
     const float dot = half - factor * th;
@@ -146,7 +147,7 @@ __device__ __forceinline__ void act_vjp(const ntg_act_t& act, float q, float t, 
     const float qb = b2 * q, tb = b2 * t;
     const float d1 = 1.f + 2.f * b2 * v1, d2 = 1.f + 2.f * b2 * v2;
     const float y = 2.f * qb;
-    const float dd = d1 * d2 - y * y;
+    const float dd = prod_minus_sq(d1, d2, y, act.compensated);
     const float s = sqrtf(fmaxf(dd, 0.f));
     const float gq2 = a2 * gq, gt2 = a2 * gt;
     const float dot = (4.f / kPi) / s;
@@ -1234,6 +1235,51 @@ extern "C" int ntg_cov_diag_bwd(void* stream, const float* gcov, const float* x,
                                                                    2.f / (float)d);
   note_launch();
   return check_launch("ntg_cov_diag_bwd");
+}
+
+// Adjoint of ntg_input_ds, ADDING into gx [nself, P, K]:
+//   mode 0: gx[s, p, k] += scale sum_o g[s, o, p] xo[o, p, k]   (g is [nself, nother, P])
+//   mode 1: gx[s, p, k] += scale sum_o g[o, s, p] xo[o, p, k]   (g is [nother, nself, P])
+//   mode 2: gx[s, p, k] += scale g[s, p] xo[s, p, k]             (self covariances)
+__global__ void input_ds_bwd_kernel(const float* __restrict__ g, const float* __restrict__ xo,
+                                    float* __restrict__ gx, int64_t nself, int64_t nother,
+                                    int64_t P, int64_t K, int mode, float scale) {
+  const int64_t total = nself * P * K;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = idx % K, sp = idx / K, p = sp % P, sf = sp / P;
+    float acc = 0.f;
+    if (mode == 2) {
+      acc = g[sf * P + p] * xo[idx];
+    } else {
+      for (int64_t o = 0; o < nother; ++o) {
+        const float gv = mode == 0 ? g[(sf * nother + o) * P + p] : g[(o * nself + sf) * P + p];
+        acc = fmaf(gv, xo[(o * P + p) * K + k], acc);
+      }
+    }
+    gx[idx] += scale * acc;
+  }
+}
+
+extern "C" int ntg_input_ds_bwd(void* stream, const float* g, const float* x1, const float* x2,
+                                float* gx1, float* gx2, int64_t n1, int64_t n2, int64_t p,
+                                int64_t k) {
+  NTG_REQUIRE(g && x1 && gx1 && n1 > 0 && p > 0 && k > 0, "ntg_input_ds_bwd: bad arguments");
+  NTG_REQUIRE(n2 == 0 || (x2 && gx2 && n2 > 0), "ntg_input_ds_bwd: pairs need x2, gx2, n2 > 0");
+  cudaStream_t s = as_stream(stream);
+  const float inv_k = 1.f / (float)k;
+  if (n2 == 0) {
+    input_ds_bwd_kernel<<<grid_for(n1 * p * k), kT, 0, s>>>(g, x1, gx1, n1, 1, p, k, 2,
+                                                            2.f * inv_k);
+    note_launch();
+  } else {
+    // two launches on one stream: gx2 may be gx1 (a symmetric call, x2 == x1)
+    input_ds_bwd_kernel<<<grid_for(n1 * p * k), kT, 0, s>>>(g, x2, gx1, n1, n2, p, k, 0, inv_k);
+    input_ds_bwd_kernel<<<grid_for(n2 * p * k), kT, 0, s>>>(g, x1, gx2, n2, n1, p, k, 1, inv_k);
+    note_launch();
+    note_launch();
+  }
+  return check_launch("ntg_input_ds_bwd");
 }
 
 extern "C" int ntg_diag_add(void* stream, const float* src, float* dst, int64_t n, int64_t a,

@@ -1237,6 +1237,38 @@ extern "C" int ntg_input_fs(void* stream, const float* x1, const float* x2, int6
   return check_launch("ntg_input_fs");
 }
 
+// Diagonal-spatial input covariances (requirements.py:641-830 with
+// diagonal_spatial): out[i, j, p] = sum_k x1[i, p, k] x2[j, p, k] / K over the
+// P spatial positions, or out[i, p] = sum_k x1[i, p, k]^2 / K without x2. Both
+// forms sum the channels in the same order, so a self pair gives
+// var1 * var2 - nngp^2 == 0 exactly.
+__global__ void input_ds_kernel(const float* __restrict__ x1, const float* __restrict__ x2,
+                                int64_t n2, int64_t total, int64_t P, int K, float inv_k,
+                                float* __restrict__ out) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = idx % P, b = idx / P;
+    const int64_t i = n2 > 0 ? b / n2 : b, j = n2 > 0 ? b - i * n2 : b;
+    const float* a = x1 + (i * P + p) * K;
+    const float* c = (n2 > 0 ? x2 : x1) + (j * P + p) * K;
+    float g = 0.f;
+    for (int k = 0; k < K; ++k) g = fmaf(a[k], c[k], g);
+    out[idx] = g * inv_k;
+  }
+}
+
+extern "C" int ntg_input_ds(void* stream, const float* x1, const float* x2, int64_t n1,
+                            int64_t n2, int64_t p, int64_t k, float* out) {
+  NTG_REQUIRE(x1 && out, "ntg_input_ds: null pointer");
+  NTG_REQUIRE(n1 > 0 && p > 0 && k > 0 && k < (1 << 30), "ntg_input_ds: sizes must be positive");
+  NTG_REQUIRE(!x2 == (n2 == 0) && n2 >= 0, "ntg_input_ds: x2 and n2 > 0 go together");
+  const int64_t total = (n2 > 0 ? n1 * n2 : n1) * p;
+  input_ds_kernel<<<grid_for(total), 256, 0, as_stream(stream)>>>(x1, x2, n2, total, p, (int)k,
+                                                                  1.f / (float)k, out);
+  note_launch();
+  return check_launch("ntg_input_ds");
+}
+
 template <bool HAS_T, int RING, int ACTK>
 cudaError_t launch_skew_k(cudaStream_t s, int64_t blocks, size_t sm, const float* in_q,
                           const float* in_t, float* out_q, float* out_t, int64_t batch,

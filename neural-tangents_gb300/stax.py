@@ -544,25 +544,10 @@ def _input_kernel(x1: torch.Tensor, x2: Optional[torch.Tensor], diagonal_spatial
             cov1 = O.cov_diag(x1)
         cov2 = None if x2 is None else O.cov_diag(x2)
     elif diagonal_spatial:
-        kk = x1.shape[-1]
-        sp = x1.shape[1:-1]
-        f1 = x1.reshape(x1.shape[0], -1, kk)
-        fb = xb.reshape(xb.shape[0], -1, kk)
-        # per-position channel dot products: a batched Gram over positions
-        nngp = torch.empty((x1.shape[0], xb.shape[0]) + tuple(sp), device=x1.device)
-        flat = nngp.view(x1.shape[0], xb.shape[0], -1)
-        for pos in range(f1.shape[1]):
-            flat[:, :, pos] = O.gram(f1[:, pos].contiguous(), fb[:, pos].contiguous(), 0)
-        cov1 = torch.empty((x1.shape[0],) + tuple(sp), device=x1.device)
-        cv = cov1.view(x1.shape[0], -1)
-        for pos in range(f1.shape[1]):
-            cv[:, pos] = O.cov_diag(f1[:, pos].contiguous())
-        cov2 = None
-        if x2 is not None:
-            cov2 = torch.empty((x2.shape[0],) + tuple(sp), device=x1.device)
-            cv2 = cov2.view(x2.shape[0], -1)
-            for pos in range(fb.shape[1]):
-                cv2[:, pos] = O.cov_diag(fb[:, pos].contiguous())
+        # per-position channel dot products [N1, N2, *spatial]
+        nngp = O.input_ds(x1, xb)
+        cov1 = O.input_ds(x1, None)
+        cov2 = None if x2 is None else O.input_ds(x2, None)
     else:
         if x1.ndim > 4:
             raise NotImplementedError('nt_gb300 supports at most two spatial dimensions')
@@ -665,9 +650,7 @@ class KernelFn:
                 return self._empty(x1, x2t, get, precision, diagonal_spatial)
             from . import _autograd, _chain
             if _autograd.needs_grad(self.specs, x1, x2t):
-                if ds:
-                    raise NotImplementedError('gradients of diagonal_spatial kernels')
-                k = _autograd.run_ad(self.specs, x1, x2t, compute_ntk, precision)
+                k = _autograd.run_ad(self.specs, x1, x2t, compute_ntk, precision, ds)
                 if names is None:
                     return k
                 vals = tuple(getattr(k, n) for n in names)

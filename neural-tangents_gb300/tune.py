@@ -93,7 +93,8 @@ def _probe(kernel_fn, sample: torch.Tensor, t: int, precision: str):
     for i in range(2):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        k = _autograd.run_ad(kernel_fn.specs, a, b, True, precision)
+        k = _autograd.run_ad(kernel_fn.specs, a, b, True, precision,
+                             bool(getattr(kernel_fn, 'diagonal', False)))
         torch.autograd.backward([k.nngp, k.ntk], [torch.ones_like(k.nngp), torch.ones_like(k.ntk)])
         e1.record()
         torch.cuda.synchronize()

@@ -453,3 +453,76 @@ def test_rare_activation_conv_gradients(nt, kind):
     for idx in [(0, 4, 5, 0)]:
         want = fd(lambda b: loss_oracle(x1, b), x2, idx)
         assert abs(g2[idx] - want) < 3e-3 * scale, (idx, g2[idx], want)
+
+
+def test_diagonal_spatial_gradients(nt):
+    """A CNN without pooling (Flatten readout) runs on diagonal-spatial kernels; its
+    gradients (input covariance, conv and activation adjoints in the diagonal layout) match
+    central finite differences of the oracle and the full-spatial gradients."""
+    rng = np.random.default_rng(23)
+    x1 = rng.standard_normal((2, 6, 5, 2))
+    x2 = rng.standard_normal((3, 6, 5, 2))
+    wq, wt = rng.standard_normal((2, 3)), rng.standard_normal((2, 3))
+
+    def layers(m, w=1.3):
+        return [m.Conv(2, (3, 3), padding='SAME', W_std=w, b_std=0.2), m.Erf(),
+                m.Conv(2, (2, 2), padding='VALID', W_std=1.1, b_std=0.1), m.Relu(),
+                m.Conv(2, (3, 3), strides=(2, 1), padding='SAME', W_std=1.2), m.Gelu(),
+                m.Flatten(), m.Dense(1, 1.2, 0.05)]
+
+    kf = nt.stax.serial(*layers(nt.stax))[2]
+    assert bool(kf.diagonal)
+
+    def loss_oracle(a, b):
+        q, t = o.serial(*layers(o))(a, b, ('nngp', 'ntk'))
+        return float(np.sum(wq * q) + np.sum(wt * t))
+
+    def grads(ds):
+        w = torch.tensor(1.3, device='cuda', requires_grad=True)
+        t1 = torch.tensor(x1, dtype=torch.float32, device='cuda', requires_grad=True)
+        t2 = torch.tensor(x2, dtype=torch.float32, device='cuda', requires_grad=True)
+        f = nt.stax.serial(*layers(nt.stax, w))[2]
+        q, t = f(t1, t2, ('nngp', 'ntk'), diagonal_spatial=ds)
+        loss = (torch.from_numpy(wq).float().cuda() * q).sum() + \
+            (torch.from_numpy(wt).float().cuda() * t).sum()
+        loss.backward()
+        return t1.grad.cpu().numpy(), t2.grad.cpu().numpy(), w.grad.item()
+
+    g1, g2, gw = grads(None)
+    f1, f2, fw = grads(False)
+    scale = max(np.abs(g1).max(), np.abs(g2).max())
+    np.testing.assert_allclose(g1, f1, rtol=0, atol=2e-5 * scale)
+    np.testing.assert_allclose(g2, f2, rtol=0, atol=2e-5 * scale)
+    assert abs(gw - fw) < 2e-5 * abs(fw)
+    for idx in [(0, 0, 0, 0), (1, 3, 2, 1), (0, 5, 4, 1)]:
+        want = fd(lambda a: loss_oracle(a, x2), x1, idx)
+        assert abs(g1[idx] - want) < 3e-3 * scale, (idx, g1[idx], want)
+    for idx in [(2, 4, 1, 0)]:
+        want = fd(lambda b: loss_oracle(x1, b), x2, idx)
+        assert abs(g2[idx] - want) < 3e-3 * scale, (idx, g2[idx], want)
+
+
+def test_diagonal_spatial_output_gradients(nt):
+    """kernel_fn(..., diagonal_spatial=True) without a readout returns [N1, N2, H, W]
+    kernels; their gradients equal those of the diagonal of the full-spatial kernels, and
+    the symmetric call differentiates through the shared input."""
+    rng = np.random.default_rng(24)
+    x = rng.standard_normal((3, 5, 4, 3))
+    w = rng.standard_normal((3, 3, 5, 4))
+    s = nt.stax
+    kf = s.serial(s.Conv(2, (3, 3), padding='SAME', W_std=1.4, b_std=0.1), s.Relu(),
+                  s.Conv(2, (3, 3), padding='SAME', W_std=1.2), s.Sin(1.1, 0.9, 0.2))[2]
+    wt = torch.from_numpy(w).float().cuda()
+
+    def grad(ds):
+        t = torch.tensor(x, dtype=torch.float32, device='cuda', requires_grad=True)
+        q, n = kf(t, None, ('nngp', 'ntk'), diagonal_spatial=ds)
+        if not ds:  # [N1, N2, H, H, W, W] -> its (h, h, w, w) entries
+            q = torch.einsum('abhhww->abhw', q)
+            n = torch.einsum('abhhww->abhw', n)
+        assert q.shape == (3, 3, 5, 4)
+        ((wt * q).sum() + (wt * n).sum()).backward()
+        return t.grad.cpu().numpy()
+
+    gd, gf = grad(True), grad(False)
+    np.testing.assert_allclose(gd, gf, rtol=0, atol=2e-5 * np.abs(gf).max())
