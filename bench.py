@@ -46,6 +46,11 @@ BYTES_PER_ENTRY = (10 * 32 ** 4 + 8 * 16 ** 4 + 8 * 8 ** 4) * 4
 # full-spatial element: Gram 4 FMA + 1 MUL; per conv+act layer 4 adds (A
 # direction) + 4 adds (C direction) x 2 tensors, affine 4, ABRelu rule ~40.
 FLOPS_PER_ELEM_LAYER = 4 * 2 + 4 * 2 + 4 + 40
+# Warp instructions one pair costs in the Myrtle-5 fused kernel: smsp__inst_executed.sum of
+# chain_fwd_kernel<2, 3, 1, 1, 1, 0, 3> over a 32 x 32 tile (ncu), divided by its 1024 pairs.
+WARP_INSTR_PER_PAIR = 4.87e6
+# Instruction issue peak: 152 SMs x 4 warp schedulers, one instruction per cycle each.
+ISSUE_SLOTS_PER_CYCLE = 152 * 4
 
 
 def myrtle5(m):
@@ -283,6 +288,16 @@ def run_gpu(args):
     hbm_peak = peaks.get('hbm_gbs', 6800.0)
     peak_note = 'of measured' if 'hbm_gbs' in peaks else 'of fallback'
     clocks = clk.summary()
+    # The fused kernel's own bound: warp-instruction issue on the CUDA cores, at the SM clock
+    # sampled during the timed steps.
+    sm_mhz = clocks.get('sm_mhz') or 2070.0
+    issue_peak = ISSUE_SLOTS_PER_CYCLE * sm_mhz * 1e6 / 1e9
+    issue_achieved = WARP_INSTR_PER_PAIR * TILE * TILE / (chain_ms / 1e3) / 1e9
+    issue = {'bound': 'issue', 'achieved': round(issue_achieved, 1), 'peak': round(issue_peak, 1),
+             'unit': 'G warp instructions/s', 'frac': round(issue_achieved / issue_peak, 3),
+             'warp_instructions_per_pair': WARP_INSTR_PER_PAIR,
+             'note': 'instructions per pair from an ncu capture; peak = 152 SMs x 4 schedulers '
+                     'x the sampled SM clock'}
     line = {
         'metric': 'Myrtle-5 NTK entries/s mixed vs plain FP32 (<=1e-4 vs FP64); fwd+bwd ms',
         'value': round(value, 1), 'unit': 'entries/s', 'n_gpus': ws, 'steps': args.steps,
@@ -308,7 +323,8 @@ def run_gpu(args):
                      'kernel': 'chain_fwd_kernel', 'kernel_ms': round(chain_ms, 3),
                      'bytes_per_entry': BYTES_PER_ENTRY,
                      'note': f'{peak_note}; algorithmic bytes of the layer-by-layer schedule; '
-                             'the fused kernel keeps them on chip'},
+                             'the fused kernel keeps them on chip',
+                     'issue': issue},
         'compute': {'bound': 'fp32', 'achieved_tflops': round(achieved_tflops, 2),
                     'flops_per_entry': flops_entry},
         'stencil_roofline': st_gbs,
