@@ -288,6 +288,22 @@ int ntg_act_pool_bwd(void* stream, const float* q, const float* t, const float* 
                      const float* gt_pooled, float* oq, float* ot, int64_t batch, int64_t n2,
                      int64_t a, int64_t c, ntg_act_t act, ntg_var_t var1, ntg_var_t var2,
                      float* gvar1, float* gvar2);
+/* Backward of the pair rule ntg_conv_act_fs (3x3 / stride 1 / SAME conv, W_std^2 = w2,
+ * b free, followed by ABRelu) on [B, 32, 32, 32, 32] kernels, fused: the activation
+ * VJP of ntg_act_bwd (pooled == 0; g_q, g_t [B, 32, 32, 32, 32] output cotangents)
+ * or of ntg_act_pool_bwd (pooled != 0; g_q, g_t the AvgPool((2, 2), (2, 2)) output
+ * cotangents [B, 16, 16, 16, 16]) evaluated on pre_q / pre_t (the conv outputs
+ * ntg_conv_act_fs wrote), followed by the conv's transpose: writes the cotangents
+ * of the conv input nngp (gin_q) and ntk (gin_t, NULL when the input NTK is the
+ * zero of an input kernel) and ADDS the variance cotangents into gvar1 / gvar2
+ * (compact [n, 32, 32]; NULL to skip). g_in is bit-identical to the unfused
+ * ntg_act_bwd / ntg_act_pool_bwd + transposed ntg_conv_fs sequence. No reference
+ * counterpart (XLA differentiates the layers separately, linear.py:1321-1424 and
+ * elementwise.py:423-477). All buffers 16-byte aligned. */
+int ntg_conv_act_bwd(void* stream, const float* pre_q, const float* pre_t, const float* g_q,
+                     const float* g_t, int32_t pooled, float* gin_q, float* gin_t, int64_t batch,
+                     int64_t n2, int64_t a, float w2, ntg_act_t act, ntg_var_t var1,
+                     ntg_var_t var2, float* gvar1, float* gvar2);
 /* Cotangents of the unscaled stencil sums U, Ut of an affine rule evaluated
  * as q = aff.w2 * scale * U + b2, t = ntk_w2 * scale * Ut + ... (n entries). */
 int ntg_affine_bwd(void* stream, const float* gq, const float* gt, float* gu, float* gut,

@@ -613,8 +613,60 @@ class ConvActFn(torch.autograd.Function):
         return tuple(outs)
 
     @staticmethod
+    def _backward_fused(ctx, gq, gt, gc1, gc2):
+        """The pair kernels' activation VJP and conv transpose in one pass
+        (ntg_conv_act_bwd); the per-sample kernels take the two rules separately."""
+        qp, tp, c1p, c2p = ctx.saved_tensors
+        w2, b2, zero_t, geom, qs, c1s, c2s = ctx.conv_meta
+        act, pooled = ctx.act, ctx.pool_geom is not None
+        s = L.stream()
+        dev = qp.device
+        n1, n2, a, c = qp.shape[0], qp.shape[1], qp.shape[2], qp.shape[4]
+        c2o = _opt(c2p)
+        v1 = _diag_view(c1p)
+        v2 = _diag_view(c2o if c2o is not None else c1p)
+        gd1 = torch.zeros((n1, a, c), device=dev)
+        gd2 = gd1 if c2o is None else torch.zeros((c2o.shape[0], a, c), device=dev)
+        gqi = torch.empty(qs, device=dev)
+        gti = None if zero_t else torch.empty(qs, device=dev)
+        L.call('ntg_conv_act_bwd', s, L.ptr(qp), L.ptr(tp),
+               None if gq is None else L.ptr(gq.contiguous()),
+               None if gt is None else L.ptr(gt.contiguous()), int(pooled), L.ptr(gqi),
+               None if gti is None else L.ptr(gti), n1 * n2, n2, a, w2, act, v1, v2,
+               gd1.data_ptr(), gd2.data_ptr())
+        vjp = 'ntg_act_pool_bwd' if pooled else 'ntg_act_bwd'
+
+        def self_back(cv, gcv, gd, shape):
+            # activation VJP of a per-sample kernel: its own variance cotangents join the
+            # pair's in gd, which then folds into the kernel's diagonal; then the conv's
+            # transpose (the stride-1 centred stencil is its own transpose)
+            vv = _diag_view(cv)
+            out = torch.empty_like(cv)
+            g = None if gcv is None else L.ptr(gcv.contiguous())
+            if pooled:
+                L.call(vjp, s, L.ptr(cv), None, g, None, L.ptr(out), None, cv.shape[0], 0, a, c,
+                       act, vv, vv, gd.data_ptr(), gd.data_ptr())
+            else:
+                L.call(vjp, s, L.ptr(cv), None, g, None, L.ptr(out), None, cv.shape[0], 0, a, c,
+                       0, act, vv, vv, gd.data_ptr(), gd.data_ptr())
+            L.call('ntg_diag_add', s, gd.data_ptr(), L.ptr(out), cv.shape[0], a, c, vv.s_n,
+                   vv.s_a, vv.s_c)
+            gin, _ = O.conv_fs(out, None, cv.shape[0], 0, a, c, 3, 3, 1, 1, 1, 1, a, c, False,
+                               O.affine(w2, 0., 0., 0., 0., False), O.NO_ACT, O.NO_VAR,
+                               O.NO_VAR, False, (cv.shape[0],))
+            return gin.reshape(shape)
+
+        gc1i = self_back(c1p, gc1, gd1, c1s)
+        gc2i = None if c2s is None else self_back(c2o, gc2, gd2, c2s)
+        return None, None, gqi, gti, gc1i, gc2i, None, None, None
+
+    @staticmethod
     def backward(ctx, gq, gt, gc1, gc2):
         qp, tp, c1p, c2p = ctx.saved_tensors
+        if (ctx.act.kind == L.NTG_ACT_ABRELU and ctx.act.stabilize <= 0.
+                and not (ctx.needs_input_grad[0] or ctx.needs_input_grad[1])
+                and (gq is not None or gt is not None)):
+            return ConvActFn._backward_fused(ctx, gq, gt, gc1, gc2)
         act_ctx = _SubCtx((qp, tp, c1p, c2p), act=ctx.act, zero_t=False)
         if ctx.pool_geom is not None:
             g = ActPoolFn.backward(act_ctx, gq, gt, gc1, gc2)

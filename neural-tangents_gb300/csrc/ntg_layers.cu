@@ -6,6 +6,7 @@
 #include <string>
 
 #include "ntg_common.cuh"
+#include "ntg_vjp.cuh"
 
 namespace ntg {
 namespace {
@@ -871,6 +872,280 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ---------------------------------------------------------------------------
+// Backward of a 3x3 / stride 1 / SAME conv + ABRelu (+ AvgPool(2, 2)) on 32 x 32
+// pair kernels in one pass. The reverse of the pair's forward is
+//   activation VJP: (g_pre_q, g_pre_t) = VJP(pre_q, pre_t, var1, var2; g_q, g_t)
+//   conv transpose: g_in_t = w2/9 S(g_pre_t), g_in_q = w2/9 S(g_pre_q) + w2 S(g_pre_t)/9
+// (S the 3x3 diagonal stencil sum, which a centred stride-1 window makes its own
+// transpose). Separately these move 24 + 16 bytes per entry through HBM; here the
+// VJP runs as each plane of a line enters the CTA (pre-activation and cotangent
+// planes by bulk copy into a shared-memory ring), its results go straight into
+// the stencil's 3-plane register ring, and only g_in leaves: 16 + 8 bytes per
+// entry (8.5 + 8 with the pooled cotangent of AvgPool(2, 2), read at 1/16 size).
+// Same thread layout, operation order and rounding as act_bwd_fs_kernel followed
+// by conv3_skew_kernel with the roles of the two tensors exchanged, so g_in is
+// bit-identical to the two-kernel path. The variance cotangents (sums over the
+// other image's positions) are reduced per plane in shared memory and added to
+// gvar1 / gvar2 ([n, 32, 32]) with one atomic per (plane, position).
+// ---------------------------------------------------------------------------
+constexpr int kVjpRing = 3;
+
+template <bool POOLED>
+__host__ __device__ constexpr int skew_vjp_slot_floats() {
+  return 2 * kSkewPlane + 2 * (POOLED ? kSkewPlane / 4 : kSkewPlane);
+}
+
+template <bool POOLED>
+__host__ __device__ constexpr size_t skew_vjp_smem_bytes() {
+  return sizeof(float) * (kVjpRing * skew_vjp_slot_floats<POOLED>() + 4 * kSkewPlane +
+                          3 * 64 + 3 * 64) +
+         sizeof(uint64_t) * kVjpRing;
+}
+
+template <bool POOLED>
+__global__ void __launch_bounds__(kThreads)
+    conv3_skew_vjp_kernel(const float* __restrict__ pre_q, const float* __restrict__ pre_t,
+                          const float* __restrict__ g_q, const float* __restrict__ g_t,
+                          float* __restrict__ gin_q, float* __restrict__ gin_t, int64_t batch,
+                          int64_t n2, int A, float w2, ntg_act_t act, ntg_var_t var1,
+                          ntg_var_t var2, float* __restrict__ gvar1, float* __restrict__ gvar2) {
+  extern __shared__ __align__(128) float smem[];
+  __shared__ int s_err;
+  constexpr int GP = POOLED ? kSkewPlane / 4 : kSkewPlane;  // floats of a cotangent plane
+  constexpr int SLOT = skew_vjp_slot_floats<POOLED>();
+  float* ring = smem;                                   // [ring][pre_q | pre_t | g_q | g_t]
+  float* stage_q = ring + kVjpRing * SLOT;              // [2][plane]
+  float* stage_t = stage_q + 2 * kSkewPlane;            // [2][plane]
+  float* vrow = stage_t + 2 * kSkewPlane;               // [3][v1[32] | v2[32]]
+  float* sg = vrow + 3 * 64;                            // [3][g v1[32] | g v2[32]]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sg + 3 * 64);
+  const int nlines = 2 * A - 1;
+  const int64_t b = blockIdx.x / nlines;
+  const int delta = (int)(blockIdx.x - b * nlines) - (A - 1);
+  if (b >= batch) return;
+  const int i_lo = delta < 0 ? -delta : 0;
+  const int len = (delta < 0 ? A : A - delta) - i_lo;
+  const int64_t pair_stride = (int64_t)A * A * kSkewPlane;
+  const int Ah = A / 2;
+  const int64_t gpair_stride = POOLED ? (int64_t)Ah * Ah * GP : pair_stride;
+  const uint32_t bytes = (uint32_t)(2 * kSkewPlane * sizeof(float)) +
+                         (uint32_t)((g_q ? 1 : 0) + (g_t ? 1 : 0)) * (uint32_t)(GP * sizeof(float));
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int w0 = (lane & 7) * 4;
+  const int r = (tid >> 5) * 4 + (lane >> 3);
+
+  int u[4], gu[4], wq[4];
+  float mL[4], mR[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int w = w0 + k;
+    wq[k] = (w + r) & (kSkewC - 1);
+    u[k] = w * kSkewC + wq[k];
+    gu[k] = POOLED ? (w >> 1) * (kSkewC / 2) + (wq[k] >> 1) : u[k];
+    mL[k] = (w >= 1 && wq[k] >= 1) ? 1.f : 0.f;
+    mR[k] = (w <= kSkewC - 2 && wq[k] <= kSkewC - 2) ? 1.f : 0.f;
+  }
+  int64_t i1, i2;
+  pair_of(b, n2, i1, i2);
+
+  // variances of plane j (row i = i_lo + j): v1 at (i, w), v2 at (i + delta, w')
+  auto load_vars = [&](int j) {
+    const int i = i_lo + j;
+    float* vb = vrow + (j % 3) * 64;
+    if (tid < kSkewC)
+      vb[tid] = __ldg(var1.base + i1 * var1.s_n + (int64_t)i * var1.s_a + (int64_t)tid * var1.s_c);
+    else if (tid < 2 * kSkewC)
+      vb[tid] = __ldg(var2.base + i2 * var2.s_n + (int64_t)(i + delta) * var2.s_a +
+                      (int64_t)(tid - kSkewC) * var2.s_c);
+  };
+  // adds plane j's variance cotangents to gvar1 / gvar2 and clears its sums
+  auto flush = [&](int j) {
+    float* s = sg + (j % 3) * 64;
+    if (tid < 2 * kSkewC) {
+      const float v = s[tid];
+      s[tid] = 0.f;
+      const int i = i_lo + j;
+      if (tid < kSkewC) {
+        if (gvar1 && v != 0.f) atomicAdd(gvar1 + (i1 * A + i) * kSkewC + tid, v);
+      } else {
+        if (gvar2 && v != 0.f) atomicAdd(gvar2 + (i2 * A + i + delta) * kSkewC + tid - kSkewC, v);
+      }
+    }
+  };
+
+  if (tid == 0) {
+    s_err = 0;
+    for (int sl = 0; sl < kVjpRing; ++sl)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[sl])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (int k = tid; k < 3 * 64; k += kThreads) sg[k] = 0.f;
+  load_vars(0);
+  if (len > 1) load_vars(1);
+  __syncthreads();
+
+  auto issue = [&](int p) {  // plane p of the line into slot p % kVjpRing
+    const int i = i_lo + p;
+    const int sl = p % kVjpRing;
+    const uint32_t bar = smem_addr(&bars[sl]);
+    float* dst = ring + sl * SLOT;
+    const int64_t off = b * pair_stride + ((int64_t)i * A + i + delta) * kSkewPlane;
+    const int64_t goff = POOLED ? b * gpair_stride + ((int64_t)(i >> 1) * Ah + ((i + delta) >> 1)) * GP
+                                : off;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+    const float* src[4] = {pre_q + off, pre_t + off, g_q ? g_q + goff : nullptr,
+                           g_t ? g_t + goff : nullptr};
+    const uint32_t nb[4] = {kSkewPlane * 4u, kSkewPlane * 4u, GP * 4u, GP * 4u};
+    const int dofs[4] = {0, kSkewPlane, 2 * kSkewPlane, 2 * kSkewPlane + GP};
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      if (!src[m]) continue;
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+          ::"r"(smem_addr(dst + dofs[m])), "l"(src[m]), "r"(nb[m]), "r"(bar)
+          : "memory");
+    }
+  };
+  int next = 0;  // next plane thread 0 issues
+  if (tid == 0)
+    for (; next < kVjpRing && next < len; ++next) issue(next);
+
+  const ActC ac = act_consts(act);
+  const float pool_w = 1.f / 16.f;
+  // plane p's activation VJP in this thread's skewed order (zero outside the line):
+  // a = g_pre_t, c = g_pre_q; variance cotangents summed into the plane's shared sums
+  auto take = [&](int p, float (&a)[4], float (&c)[4]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) a[k] = c[k] = 0.f;
+    if (p >= len) return;
+    const int sl = p % kVjpRing;
+    if (!s_err && !bar_wait(smem_addr(&bars[sl]), (uint32_t)((p / kVjpRing) & 1))) s_err = 1;
+    const float* sp = ring + sl * SLOT;
+    const float* vb = vrow + (p % 3) * 64;
+    float qv[4], tv[4], gqv[4], gtv[4], v1[4], v2[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      qv[k] = sp[u[k]];
+      tv[k] = sp[kSkewPlane + u[k]];
+      gqv[k] = g_q ? sp[2 * kSkewPlane + gu[k]] : 0.f;
+      gtv[k] = g_t ? sp[2 * kSkewPlane + GP + gu[k]] : 0.f;
+      if (POOLED) {
+        gqv[k] *= pool_w;
+        gtv[k] *= pool_w;
+      }
+      v1[k] = vb[w0 + k];
+      v2[k] = vb[kSkewC + wq[k]];
+    }
+    float o1[4], o2[4];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      P2 oq2, ot2, a12, a22;
+      abrelu_vjp2(ac, p2(qv[2 * h], qv[2 * h + 1]), p2(tv[2 * h], tv[2 * h + 1]),
+                  p2(v1[2 * h], v1[2 * h + 1]), p2(v2[2 * h], v2[2 * h + 1]),
+                  p2(gqv[2 * h], gqv[2 * h + 1]), p2(gtv[2 * h], gtv[2 * h + 1]), oq2, ot2, a12,
+                  a22);
+      p2u(oq2, c[2 * h], c[2 * h + 1]);
+      p2u(ot2, a[2 * h], a[2 * h + 1]);
+      p2u(a12, o1[2 * h], o1[2 * h + 1]);
+      p2u(a22, o2[2 * h], o2[2 * h + 1]);
+    }
+    float* s = sg + (p % 3) * 64;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      // var1 cotangent at w: the four row groups of the warp share w
+      float x = o1[k];
+      x += __shfl_xor_sync(0xffffffffu, x, 8);
+      x += __shfl_xor_sync(0xffffffffu, x, 16);
+      if (lane < 8) atomicAdd(&s[w0 + k], x);
+      atomicAdd(&s[kSkewC + wq[k]], o2[k]);
+    }
+  };
+
+  const float inv9 = 1.f / 9.f;
+  const P2 W2 = p2s(w2 * inv9), TW = p2s(w2 * inv9), TN = p2s(w2), Z = p2s(0.f);
+  float am[4], cm[4], a0[4], c0[4], ap[4], cp[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) am[k] = cm[k] = 0.f;
+  take(0, a0, c0);
+  for (int j = 0; j < len; ++j) {
+    if (j + 2 < len) load_vars(j + 2);  // buffer (j + 2) % 3 was last read by plane j - 1
+    take(j + 1, ap, cp);
+    const int i = i_lo + j;
+    float ha[4], hc[4], sa[4], sc[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      ha[k] = (am[k] + a0[k]) + ap[k];
+      hc[k] = (cm[k] + c0[k]) + cp[k];
+    }
+    {
+      const float la = __shfl_up_sync(0xffffffffu, ha[3], 1, 8);
+      const float ra = __shfl_down_sync(0xffffffffu, ha[0], 1, 8);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float L = k == 0 ? la : ha[k - 1], R = k == 3 ? ra : ha[k + 1];
+        sa[k] = fmaf(R, mR[k], fmaf(L, mL[k], ha[k]));
+      }
+    }
+    {
+      const float lc = __shfl_up_sync(0xffffffffu, hc[3], 1, 8);
+      const float rc = __shfl_down_sync(0xffffffffu, hc[0], 1, 8);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float L = k == 0 ? lc : hc[k - 1], R = k == 3 ? rc : hc[k + 1];
+        sc[k] = fmaf(R, mR[k], fmaf(L, mL[k], hc[k]));
+      }
+    }
+    // transposed affine rule: g_in_t = W2 S(a), g_in_q = TW S(c) + TN (S(a) / 9)
+    float* oq = stage_q + (j & 1) * kSkewPlane;
+    float* ot = stage_t + (j & 1) * kSkewPlane;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const P2 ca = p2(sa[2 * h], sa[2 * h + 1]), cc = p2(sc[2 * h], sc[2 * h + 1]);
+      const P2 gt_in = fma2(W2, ca, Z);
+      const P2 gq_in = fma2(TW, cc, fma2(TN, mul2(ca, p2s(inv9)), Z));
+      float x0, x1, y0, y1;
+      p2u(gq_in, x0, x1);
+      p2u(gt_in, y0, y1);
+      oq[u[2 * h]] = x0;
+      oq[u[2 * h + 1]] = x1;
+      if (gin_t) {
+        ot[u[2 * h]] = y0;
+        ot[u[2 * h + 1]] = y1;
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    __syncthreads();
+    if (j == 0) flush(0);
+    if (j + 1 < len) flush(j + 1);
+    if (tid == 0) {
+      const int64_t off = b * pair_stride + ((int64_t)i * A + i + delta) * kSkewPlane;
+      bulk_store(gin_q + off, oq, kSkewPlane * 4u);
+      if (gin_t) bulk_store(gin_t + off, ot, kSkewPlane * 4u);
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      // plane j + 1 has been read by every thread: its slot takes plane j + 1 + kVjpRing
+      if (!s_err)
+        for (; next < len && next <= j + 1 + kVjpRing; ++next) issue(next);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      am[k] = a0[k]; cm[k] = c0[k];
+      a0[k] = ap[k]; c0[k] = cp[k];
+    }
+  }
+  if (tid == 0) {
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    if (s_err) {
+      atomicExch(&g_device_error, NTG_ERR_WAIT_TIMEOUT);
+      // let every issued copy land (bounded) before the CTA's shared memory is released
+      for (int p = next > kVjpRing ? next - kVjpRing : 0; p < next; ++p)
+        bar_wait(smem_addr(&bars[p % kVjpRing]), (uint32_t)((p / kVjpRing) & 1));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Diagonal-spatial conv rule: [B, A, C] box filter (linear.py:3381-3437).
 // ---------------------------------------------------------------------------
 __global__ void conv_ds_kernel(const float* __restrict__ in_q, const float* __restrict__ in_t,
@@ -1401,6 +1676,49 @@ extern "C" int ntg_conv_act_fs(void* stream, const float* in_q, const float* in_
   if (e != cudaSuccess) return fail(NTG_ERR_CUDA, std::string("ntg_conv_act_fs: ") + cudaGetErrorString(e));
   note_launch();
   return check_launch("ntg_conv_act_fs");
+}
+
+template <bool POOLED>
+cudaError_t launch_skew_vjp(cudaStream_t s, int64_t blocks, const float* pre_q, const float* pre_t,
+                            const float* g_q, const float* g_t, float* gin_q, float* gin_t,
+                            int64_t batch, int64_t n2, int64_t a, float w2, ntg_act_t act,
+                            ntg_var_t var1, ntg_var_t var2, float* gvar1, float* gvar2) {
+  constexpr size_t sm = skew_vjp_smem_bytes<POOLED>();
+  cudaError_t e = cudaFuncSetAttribute(conv3_skew_vjp_kernel<POOLED>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e == cudaSuccess)
+    conv3_skew_vjp_kernel<POOLED><<<(unsigned)blocks, kThreads, sm, s>>>(
+        pre_q, pre_t, g_q, g_t, gin_q, gin_t, batch, n2, (int)a, w2, act, var1, var2, gvar1,
+        gvar2);
+  return e;
+}
+
+extern "C" int ntg_conv_act_bwd(void* stream, const float* pre_q, const float* pre_t,
+                                const float* g_q, const float* g_t, int32_t pooled, float* gin_q,
+                                float* gin_t, int64_t batch, int64_t n2, int64_t a, float w2,
+                                ntg_act_t act, ntg_var_t var1, ntg_var_t var2, float* gvar1,
+                                float* gvar2) {
+  NTG_REQUIRE(pre_q && pre_t && gin_q && var1.base && var2.base,
+              "ntg_conv_act_bwd: null pointer");
+  NTG_REQUIRE(batch > 0 && a == kSkewC, "ntg_conv_act_bwd: needs [B, 32, 32, 32, 32] kernels");
+  NTG_REQUIRE(act.kind == NTG_ACT_ABRELU && act.stabilize <= 0.f,
+              "ntg_conv_act_bwd: fuses the ABRelu rule (without do_stabilize) only");
+  const bool aligned =
+      ((reinterpret_cast<uintptr_t>(pre_q) | reinterpret_cast<uintptr_t>(pre_t) |
+        reinterpret_cast<uintptr_t>(g_q) | reinterpret_cast<uintptr_t>(g_t) |
+        reinterpret_cast<uintptr_t>(gin_q) | reinterpret_cast<uintptr_t>(gin_t)) & 15) == 0;
+  NTG_REQUIRE(aligned, "ntg_conv_act_bwd: buffers must be 16-byte aligned");
+  const int64_t blocks = batch * (2 * a - 1);
+  NTG_REQUIRE(blocks < (1ll << 31), "ntg_conv_act_bwd: grid too large");
+  const cudaError_t e =
+      pooled ? launch_skew_vjp<true>(as_stream(stream), blocks, pre_q, pre_t, g_q, g_t, gin_q,
+                                     gin_t, batch, n2, a, w2, act, var1, var2, gvar1, gvar2)
+             : launch_skew_vjp<false>(as_stream(stream), blocks, pre_q, pre_t, g_q, g_t, gin_q,
+                                      gin_t, batch, n2, a, w2, act, var1, var2, gvar1, gvar2);
+  if (e != cudaSuccess)
+    return fail(NTG_ERR_CUDA, std::string("ntg_conv_act_bwd: ") + cudaGetErrorString(e));
+  note_launch();
+  return check_launch("ntg_conv_act_bwd");
 }
 
 extern "C" int ntg_conv_input_fs(void* stream, const float* x1, const float* x2, int64_t n1,

@@ -526,3 +526,84 @@ def test_diagonal_spatial_output_gradients(nt):
 
     gd, gf = grad(True), grad(False)
     np.testing.assert_allclose(gd, gf, rtol=0, atol=2e-5 * np.abs(gf).max())
+
+
+@pytest.mark.parametrize('pooled', [False, True])
+@pytest.mark.parametrize('zero_t', [False, True])
+def test_fused_conv_act_backward_matches_two_kernels(nt, pooled, zero_t):
+    """ntg_conv_act_bwd (activation VJP fused into the conv transpose) against the
+    activation VJP kernel followed by the transposed stencil: the image-side cotangents are
+    bit-identical, the variance cotangents equal up to the order of their sums."""
+    from nt_gb300 import _lib as L, _ops as O
+    g = torch.Generator(device='cuda').manual_seed(5)
+    n1, n2, A = 2, 3, 32
+    shp = (n1 * n2, A, A, A, A)
+    cov = torch.rand((n1 + n2, A, A, A, A), device='cuda', generator=g) * 0.2
+    for a in range(A):
+        cov[:, a, a, :, :].diagonal(dim1=-2, dim2=-1).add_(2.)
+    sa = A * A * A + A * A
+    v1 = L.Var(cov[:n1].data_ptr(), A ** 4, sa, A + 1)
+    v2 = L.Var(cov[n1:].data_ptr(), A ** 4, sa, A + 1)
+    act = L.Act(L.NTG_ACT_ABRELU, 0., 1., 0., 0, 0.)
+    pre_q = torch.rand(shp, device='cuda', generator=g) * 2 - 1
+    pre_t = torch.rand(shp, device='cuda', generator=g)
+    gshape = (n1 * n2, 16, 16, 16, 16) if pooled else shp
+    gq = torch.rand(gshape, device='cuda', generator=g) - 0.5
+    gt = torch.rand(gshape, device='cuda', generator=g) - 0.5
+    w2 = 2.0
+    gin_q = torch.empty(shp, device='cuda')
+    gin_t = None if zero_t else torch.empty(shp, device='cuda')
+    gd1, gd2 = torch.zeros((n1, A, A), device='cuda'), torch.zeros((n2, A, A), device='cuda')
+    L.call('ntg_conv_act_bwd', L.stream(), L.ptr(pre_q), L.ptr(pre_t), L.ptr(gq), L.ptr(gt),
+           int(pooled), L.ptr(gin_q), None if gin_t is None else L.ptr(gin_t), n1 * n2, n2, A,
+           w2, act, v1, v2, gd1.data_ptr(), gd2.data_ptr())
+    oq, ot = torch.empty(shp, device='cuda'), torch.empty(shp, device='cuda')
+    hd1, hd2 = torch.zeros((n1, A, A), device='cuda'), torch.zeros((n2, A, A), device='cuda')
+    if pooled:
+        L.call('ntg_act_pool_bwd', L.stream(), L.ptr(pre_q), L.ptr(pre_t), L.ptr(gq), L.ptr(gt),
+               L.ptr(oq), L.ptr(ot), n1 * n2, n2, A, A, act, v1, v2, hd1.data_ptr(),
+               hd2.data_ptr())
+    else:
+        L.call('ntg_act_bwd', L.stream(), L.ptr(pre_q), L.ptr(pre_t), L.ptr(gq), L.ptr(gt),
+               L.ptr(oq), L.ptr(ot), n1 * n2, n2, A, A, 0, act, v1, v2, hd1.data_ptr(),
+               hd2.data_ptr())
+    six = (n1, n2, A, A, A, A)
+    want_t, want_q = O.conv_fs(ot.view(six), oq.view(six), n1 * n2, n2, A, A, 3, 3, 1, 1, 1, 1,
+                               A, A, False, O.affine(w2, 0., w2, w2, 0., False), O.NO_ACT,
+                               O.NO_VAR, O.NO_VAR, True, (n1, n2))
+    torch.cuda.synchronize()
+    assert torch.equal(gin_q, want_q.reshape(shp))
+    if gin_t is not None:
+        assert torch.equal(gin_t, want_t.reshape(shp))
+    for a, b in ((gd1, hd1), (gd2, hd2)):
+        assert float((a - b).abs().max() / b.abs().max()) < 1e-5
+
+
+def test_fused_conv_act_backward_in_network(nt):
+    """A 32 x 32 conv net's input gradients through the fused backward (W_std plain floats)
+    equal those through the unfused rules (W_std tensors that need gradients)."""
+    rng = np.random.default_rng(25)
+    x1 = rng.standard_normal((2, 32, 32, 3))
+    x2 = rng.standard_normal((2, 32, 32, 3))
+    wq, wt = rng.standard_normal((2, 2)), rng.standard_normal((2, 2))
+    s = nt.stax
+
+    def grads(hyper):
+        ws = [torch.tensor(v, device='cuda', requires_grad=True) if hyper else v
+              for v in (1.4, 1.3, 1.2)]
+        net = s.serial(s.Conv(1, (3, 3), padding='SAME', W_std=ws[0], b_std=0.1), s.Relu(),
+                       s.Conv(1, (3, 3), padding='SAME', W_std=ws[1]), s.Relu(),
+                       s.AvgPool((2, 2), (2, 2)), s.Conv(1, (3, 3), padding='SAME', W_std=ws[2]),
+                       s.Relu(), s.GlobalAvgPool(), s.Dense(1, 1.1, 0.05))[2]
+        t1 = torch.tensor(x1, dtype=torch.float32, device='cuda', requires_grad=True)
+        t2 = torch.tensor(x2, dtype=torch.float32, device='cuda', requires_grad=True)
+        q, t = net(t1, t2, ('nngp', 'ntk'))
+        ((torch.from_numpy(wq).float().cuda() * q).sum() +
+         (torch.from_numpy(wt).float().cuda() * t).sum()).backward()
+        return t1.grad.cpu().numpy(), t2.grad.cpu().numpy()
+
+    f1, f2 = grads(False)
+    u1, u2 = grads(True)
+    scale = max(np.abs(u1).max(), np.abs(u2).max())
+    np.testing.assert_allclose(f1, u1, rtol=0, atol=1e-5 * scale)
+    np.testing.assert_allclose(f2, u2, rtol=0, atol=1e-5 * scale)
