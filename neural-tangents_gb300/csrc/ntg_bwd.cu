@@ -614,14 +614,27 @@ struct PlaneIt {  // (i2, h') of a plane in the order the CTA streams them
   int hq;
 };
 
+__device__ int g_bwd_error = 0;
+
+constexpr int kIfRing = 4;
+
+// CTA (i1, h) streams the G planes (i2, h') of its row and the matching rows
+// x2[i2, h', :, :] through a shared-memory ring filled by bulk copies (one
+// thread issues, completion on an mbarrier, every wait bounded), kIfRing planes
+// ahead of the compute. Planes go in cyclic order from a per-CTA start, so that
+// concurrent CTAs add into different gx2 rows.
 template <int K>
 __global__ void __launch_bounds__(256)
     input_fs_t2_kernel(const float* __restrict__ g, const float* __restrict__ x1,
                        const float* __restrict__ x2, float* __restrict__ gx1,
                        float* __restrict__ gx2, int64_t n1, int64_t n2, int A, float inv_k) {
   constexpr int C = kIfC;
-  __shared__ __align__(16) float xs[2][C * 4];      // x2[i2, h', :, :], channels padded to 4
-  __shared__ __align__(16) float cw[2][8][C * 4];   // per-warp gx2 sums of a plane [w'][k]
+  constexpr int XF = C * K;  // floats of a row x[i, h, :, :] (multiple of 32: 16-byte copies)
+  __shared__ __align__(128) float gs[kIfRing][C * C];
+  __shared__ __align__(16) float xs[kIfRing][XF];
+  __shared__ __align__(16) float cw[2][8][C * 4];  // per-warp gx2 sums of a plane [w'][k]
+  __shared__ __align__(8) uint64_t bars[kIfRing];
+  __shared__ int s_err;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t i1 = blockIdx.x / A;
   const int h = (int)(blockIdx.x % A);
@@ -640,43 +653,56 @@ __global__ void __launch_bounds__(256)
   auto advance = [&](PlaneIt& it) {
     if (++it.hq == A) {
       it.hq = 0;
-      ++it.i2;
+      if (!self && ++it.i2 == n2) it.i2 = 0;
     }
   };
-  // G + offset of this thread's 4 entries in plane (i2, h')
-  auto gptr = [&](const PlaneIt& it) {
-    const int64_t b = self ? i1 : i1 * n2 + it.i2;
-    return g + ((b * A + h) * A + it.hq) * (int64_t)(C * C) + w * C + wq0;
+  const int64_t s0 = ((int64_t)blockIdx.x * 7919) % np;
+  PlaneIt cur_it{self ? i1 : s0 / A, (int)(s0 % A)};
+  PlaneIt iss_it = cur_it;  // next plane thread 0 issues
+  int64_t issued = 0;
+  auto issue = [&]() {
+    const int sl = (int)(issued % kIfRing);
+    const uint32_t bar = smem_addr(&bars[sl]);
+    const int64_t b = self ? i1 : i1 * n2 + iss_it.i2;
+    const float* gsrc = g + ((b * A + h) * A + iss_it.hq) * (int64_t)(C * C);
+    const float* xsrc = xo + ((iss_it.i2 * A + iss_it.hq) * C) * K;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
+                 "r"((uint32_t)((C * C + XF) * sizeof(float)))
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_addr(&gs[sl][0])), "l"(gsrc), "r"((uint32_t)(C * C * sizeof(float))), "r"(bar)
+        : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_addr(&xs[sl][0])), "l"(xsrc), "r"((uint32_t)(XF * sizeof(float))), "r"(bar)
+        : "memory");
+    advance(iss_it);
+    ++issued;
   };
-  auto stage = [&](const PlaneIt& it, int buf) {
-    if (tid < C * 4) {
-      const float* src = xo + ((it.i2 * A + it.hq) * C) * K;
-      const int wq = tid >> 2, k = tid & 3;
-      xs[buf][tid] = k < K ? __ldg(src + wq * K + k) : 0.f;
-    }
-  };
-  PlaneIt p0{self ? i1 : 0, 0}, p1 = p0, p2;
-  advance(p1);
-  p2 = p1;
-  advance(p2);
-  stage(p0, 0);
-  float4 G0 = *reinterpret_cast<const float4*>(gptr(p0));
-  float4 G1 = np > 1 ? *reinterpret_cast<const float4*>(gptr(p1)) : G0;
+  if (tid == 0) {
+    s_err = 0;
+    for (int sl = 0; sl < kIfRing; ++sl)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[sl])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
   __syncthreads();
+  if (tid == 0)
+    while (issued < kIfRing && issued < np) issue();
   for (int64_t p = 0; p < np; ++p) {
     const int cur = (int)(p & 1);
-    const float4 G2 = p + 2 < np ? *reinterpret_cast<const float4*>(gptr(p2)) : G1;
-    if (p + 1 < np) stage(p1, cur ^ 1);
-    const float ga[4] = {G0.x, G0.y, G0.z, G0.w};
+    const int sl = (int)(p % kIfRing);
+    if (!s_err && !bar_wait(smem_addr(&bars[sl]), (uint32_t)((p / kIfRing) & 1))) s_err = 1;
+    const float4 G = *reinterpret_cast<const float4*>(&gs[sl][w * C + wq0]);
+    const float ga[4] = {G.x, G.y, G.z, G.w};
     float cp[4][4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const float4 X = *reinterpret_cast<const float4*>(&xs[cur][(wq0 + j) * 4]);
-      const float xv[4] = {X.x, X.y, X.z, X.w};
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         if (k < K) {
-          acc[k] = fmaf(ga[j], xv[k], acc[k]);
+          const float xv = xs[sl][(wq0 + j) * K + k];
+          acc[k] = fmaf(ga[j], xv, acc[k]);
           cp[j][k] = ga[j] * xr[k];
         } else {
           cp[j][k] = 0.f;
@@ -698,18 +724,16 @@ __global__ void __launch_bounds__(256)
             make_float4(cp[j][0], cp[j][1], cp[j][2], cp[j][3]);
     }
     __syncthreads();
+    // every thread has read slot sl: it takes plane p + kIfRing
+    if (tid == 0 && !s_err && issued < np) issue();
     if (tid < C * K) {
       const int wq = tid / K, k = tid - (tid / K) * K;
       float v = 0.f;
 #pragma unroll
       for (int u = 0; u < 8; ++u) v += cw[cur][u][wq * 4 + k];
-      atomicAdd(go + ((p0.i2 * A + p0.hq) * C + wq) * K + k, v * inv_k);
+      atomicAdd(go + ((cur_it.i2 * A + cur_it.hq) * C + wq) * K + k, v * inv_k);
     }
-    G0 = G1;
-    G1 = G2;
-    p0 = p1;
-    p1 = p2;
-    advance(p2);
+    advance(cur_it);
   }
 #pragma unroll
   for (int k = 0; k < K; ++k) {
@@ -720,6 +744,12 @@ __global__ void __launch_bounds__(256)
   if ((lane & 7) == 0) {
 #pragma unroll
     for (int k = 0; k < K; ++k) atomicAdd(gx1 + ((i1 * A + h) * C + w) * K + k, acc[k] * inv_k);
+  }
+  if (tid == 0 && s_err) {
+    atomicExch(&g_bwd_error, NTG_ERR_WAIT_TIMEOUT);
+    // let every issued copy land (bounded) before the CTA's shared memory is released
+    for (int64_t p = issued > kIfRing ? issued - kIfRing : 0; p < issued; ++p)
+      bar_wait(smem_addr(&bars[p % kIfRing]), (uint32_t)((p / kIfRing) & 1));
   }
 }
 
@@ -981,7 +1011,8 @@ extern "C" int ntg_input_fs_bwd2(void* stream, const float* g, const float* x1,
   NTG_REQUIRE(n2 == 0 || (x2 && gx2), "ntg_input_fs_bwd2: pairs need x2 and gx2");
   cudaStream_t s = as_stream(stream);
   const bool fast = c == kIfC && k <= 4 && a <= (1 << 16) && n1 * a < (1ll << 31) &&
-                    (reinterpret_cast<uintptr_t>(g) & 15) == 0;
+                    ((reinterpret_cast<uintptr_t>(g) | reinterpret_cast<uintptr_t>(x1) |
+                      reinterpret_cast<uintptr_t>(x2)) & 15) == 0;
   if (fast) {
     const unsigned grid = (unsigned)(n1 * a);
     const float inv_k = 1.f / (float)k;
@@ -1073,6 +1104,16 @@ extern "C" int ntg_input_ds_bwd(void* stream, const float* g, const float* x1, c
   }
   return check_launch("ntg_input_ds_bwd");
 }
+
+namespace ntg {
+int bwd_take_device_error() {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_bwd_error, sizeof(int)) != cudaSuccess) return -1;
+  const int zero = 0;
+  if (v != 0 && cudaMemcpyToSymbol(g_bwd_error, &zero, sizeof(int)) != cudaSuccess) return -1;
+  return v;
+}
+}  // namespace ntg
 
 extern "C" int ntg_diag_add(void* stream, const float* src, float* dst, int64_t n, int64_t a,
                             int64_t c, int64_t s_n, int64_t s_a, int64_t s_c) {

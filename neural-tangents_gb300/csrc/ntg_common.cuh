@@ -19,6 +19,8 @@ int fail(int code, const std::string& msg);
 int check_launch(const char* what);
 void note_launch(uint64_t n = 1);
 int32_t tune(int32_t knob);  // current value of an NTG_TUNE_* knob
+// Reads and clears the device error word of the adjoint kernels (ntg_bwd.cu).
+int bwd_take_device_error();
 
 // Tensor-core (tcgen05) split-precision Gram; defined in ntg_gram_tc.cu.
 int gram_tc(cudaStream_t stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
@@ -33,6 +35,30 @@ size_t gram_tc_workspace(int64_t n1, int64_t n2, int64_t d);
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 constexpr float kPi = 3.14159265358979323846f;
+
+// ---------------------------------------------------------------------------
+// Bulk-copy rings: shared-memory addresses and bounded mbarrier waits. A wait
+// that runs out returns false; the kernel then raises its device error word.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kLineWaitLimit = 1u << 20;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
+  for (uint32_t it = 0; it < kLineWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
 
 // ---------------------------------------------------------------------------
 // Activation rules.  All products that the reference evaluates as separate

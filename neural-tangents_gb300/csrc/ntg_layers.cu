@@ -384,27 +384,8 @@ __global__ void __launch_bounds__(kThreads)
 // raises the library's device error word and the line is left unwritten.
 // ---------------------------------------------------------------------------
 constexpr int kRing = 4;
-constexpr uint32_t kLineWaitLimit = 1u << 20;
 
 __device__ int g_device_error = 0;
-
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
-  for (uint32_t it = 0; it < kLineWaitLimit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
-}
 
 template <bool HAS_T>
 __global__ void __launch_bounds__(kThreads)
@@ -1839,6 +1820,8 @@ extern "C" int ntg_device_status(void) {
   const int zero = 0;
   if (v != 0 && cudaMemcpyToSymbol(g_device_error, &zero, sizeof(int)) != cudaSuccess)
     return check_launch("ntg_device_status");
+  if (v == 0) v = bwd_take_device_error();
+  if (v < 0) return check_launch("ntg_device_status");
   if (v != 0) return fail(v, "a bounded device wait ran out in a streamed kernel");
   return NTG_OK;
 }
