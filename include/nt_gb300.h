@@ -288,6 +288,17 @@ int ntg_act_pool_bwd(void* stream, const float* q, const float* t, const float* 
                      const float* gt_pooled, float* oq, float* ot, int64_t batch, int64_t n2,
                      int64_t a, int64_t c, ntg_act_t act, ntg_var_t var1, ntg_var_t var2,
                      float* gvar1, float* gvar2);
+/* First layer of a conv net on 32 x 32 images in one pass: the pair input
+ * covariances of x1 [N1, 32, 32, K], x2 [N2, 32, 32, K] (1 <= K <= 4, NHWC;
+ * requirements.py:542-553), the 3x3 SAME conv rule on them (linear.py:1321-1424,
+ * NTK parameterisation: aff.ntk_nn = 1, ntk_c = 0, nn_scaled = 1) and the activation
+ * (variances var1 / var2 of the per-sample conv outputs), without writing the
+ * covariances: out_q / out_t [N1 * N2, 32, 32, 32, 32] are the activated nngp / ntk,
+ * pre_q the conv output (its NTK equals it, the input NTK being zero), all as
+ * ntg_input_fs followed by ntg_conv_act_fs would give them, bit for bit. */
+int ntg_input_conv_act_fs(void* stream, const float* x1, const float* x2, int64_t n1,
+                          int64_t n2, int64_t k, float* out_q, float* out_t, float* pre_q,
+                          ntg_affine_t aff, ntg_act_t act, ntg_var_t var1, ntg_var_t var2);
 /* Backward of the pair rule ntg_conv_act_fs (3x3 / stride 1 / SAME conv, W_std^2 = w2,
  * b free, followed by ABRelu) on [B, 32, 32, 32, 32] kernels, fused: the activation
  * VJP of ntg_act_bwd (pooled == 0; g_q, g_t [B, 32, 32, 32, 32] output cotangents)

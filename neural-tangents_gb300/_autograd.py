@@ -549,6 +549,122 @@ class _SubCtx:
         self.__dict__.update(fields)
 
 
+def _conv_act_self_back(cv, gcv, gd, act, pooled, w2):
+    """Backward of a 3x3 SAME conv + activation (+ AvgPool(2, 2)) on a per-sample kernel
+    cv [n, A, A, C, C] (the conv output): the activation VJP, whose variance cotangents join
+    the pair's already in gd and fold into the kernel's diagonal, then the conv's transpose
+    (the stride-1 centred stencil is its own transpose)."""
+    s = L.stream()
+    n, a, c = cv.shape[0], cv.shape[1], cv.shape[3]
+    vv = _diag_view(cv)
+    out = torch.empty_like(cv)
+    g = None if gcv is None else L.ptr(gcv.contiguous())
+    if pooled:
+        L.call('ntg_act_pool_bwd', s, L.ptr(cv), None, g, None, L.ptr(out), None, n, 0, a, c, act,
+               vv, vv, gd.data_ptr(), gd.data_ptr())
+    else:
+        L.call('ntg_act_bwd', s, L.ptr(cv), None, g, None, L.ptr(out), None, n, 0, a, c, 0, act,
+               vv, vv, gd.data_ptr(), gd.data_ptr())
+    L.call('ntg_diag_add', s, gd.data_ptr(), L.ptr(out), n, a, c, vv.s_n, vv.s_a, vv.s_c)
+    gin, _ = O.conv_fs(out, None, n, 0, a, c, 3, 3, 1, 1, 1, 1, a, c, False,
+                       O.affine(w2, 0., 0., 0., 0., False), O.NO_ACT, O.NO_VAR, O.NO_VAR, False,
+                       (n,))
+    return gin
+
+
+class InputConvActFn(torch.autograd.Function):
+    """Input covariances, a 3x3 / stride 1 / SAME conv (NTK parameterisation) and an ABRelu
+    on 32 x 32 images: the pair kernels take one pass from the images (ntg_input_conv_act_fs,
+    the covariances never written) and one fused backward (ntg_conv_act_bwd with the conv
+    output as both pre-activation tensors: the input NTK is zero, so the conv's NTK equals
+    its NNGP); the per-sample kernels take the layer rules one by one."""
+
+    @staticmethod
+    def forward(ctx, x1, x2, w2t, b2t, act):
+        w2, b2 = _f(w2t), _f(b2t)
+        aff = O.affine(w2, b2, w2)
+        x2o = _opt(x2)
+        xb = x1 if x2o is None else x2o
+        dev = x1.device
+        n1, n2, k = x1.shape[0], xb.shape[0], x1.shape[3]
+        a = c = 32
+
+        def conv_self(cv):
+            return O.conv_fs(cv, None, cv.shape[0], 0, a, c, 3, 3, 1, 1, 1, 1, a, c, False, aff,
+                             O.NO_ACT, O.NO_VAR, O.NO_VAR, False, (cv.shape[0],))[0]
+
+        def act_self(cv):
+            vv = _diag_view(cv)
+            return O.affine_act(cv, None, cv.shape[0], 0, a, c, False, False, O.IDENTITY_AFFINE,
+                                act, vv, vv, False)[0]
+
+        c1p = conv_self(O.input_fs(x1, None))
+        c2p = None if x2o is None else conv_self(O.input_fs(x2o, None))
+        v1 = _diag_view(c1p)
+        v2 = _diag_view(c2p if c2p is not None else c1p)
+        shape = (n1, n2, a, a, c, c)
+        qa, ta = torch.empty(shape, device=dev), torch.empty(shape, device=dev)
+        pre = torch.empty(shape, device=dev)
+        L.call('ntg_input_conv_act_fs', L.stream(), L.ptr(x1), L.ptr(xb), n1, n2, k, L.ptr(qa),
+               L.ptr(ta), L.ptr(pre), aff, act, v1, v2)
+        c1a = act_self(c1p)
+        c2a = _e(dev) if c2p is None else act_self(c2p)
+        ctx.save_for_backward(x1, x2, pre, c1p, _e(dev) if c2p is None else c2p)
+        ctx.w2, ctx.act = w2, act
+        return qa, ta, c1a, c2a
+
+    @staticmethod
+    def backward(ctx, gq, gt, gc1, gc2):
+        x1, x2, pre, c1p, c2p = ctx.saved_tensors
+        x2o, c2o = _opt(x2), _opt(c2p)
+        w2, act = ctx.w2, ctx.act
+        s = L.stream()
+        dev = x1.device
+        n1, n2 = pre.shape[0], pre.shape[1]
+        a, c, k = 32, 32, x1.shape[3]
+        v1 = _diag_view(c1p)
+        v2 = _diag_view(c2o if c2o is not None else c1p)
+        gd1 = torch.zeros((n1, a, c), device=dev)
+        gd2 = gd1 if c2o is None else torch.zeros((n2, a, c), device=dev)
+        gin = torch.empty_like(pre)
+        L.call('ntg_conv_act_bwd', s, L.ptr(pre), L.ptr(pre),
+               None if gq is None else L.ptr(gq.contiguous()),
+               None if gt is None else L.ptr(gt.contiguous()), 0, L.ptr(gin), None, n1 * n2, n2,
+               a, w2, act, v1, v2, gd1.data_ptr(), gd2.data_ptr())
+        gc1i = _conv_act_self_back(c1p, gc1, gd1, act, False, w2)
+        gc2i = None if c2o is None else _conv_act_self_back(c2o, gc2, gd2, act, False, w2)
+        # input covariance adjoint (requirements.py:641-830): the pairs, then each image's own
+        gx1 = torch.zeros_like(x1)
+        gx2 = None if x2o is None else torch.zeros_like(x2o)
+        other = x1 if x2o is None else x2o
+        L.call('ntg_input_fs_bwd2', s, L.ptr(gin), L.ptr(x1), L.ptr(other), L.ptr(gx1),
+               L.ptr(gx1 if x2o is None else gx2), n1, n2, a, c, k)
+        for gcv, xx, gg in ((gc1i, x1, gx1), (gc2i, x2o, gx2)):
+            if xx is None:
+                continue
+            L.call('ntg_input_fs_bwd2', s, L.ptr(gcv), L.ptr(xx), None, L.ptr(gg), None,
+                   xx.shape[0], 0, a, c, k)
+        return gx1, gx2, None, None, None
+
+
+def input_conv_act_fusable(x1: torch.Tensor, specs, ds: bool) -> bool:
+    """Whether the first two layers take InputConvActFn: 32 x 32 NHWC images with 1-4
+    channels, a 3x3 / stride 1 / SAME zero-padded conv in the NTK parameterisation whose
+    W_std / b_std need no gradient, then an ABRelu without do_stabilize."""
+    from .stax import Padding
+    if ds or x1.ndim != 4 or tuple(x1.shape[1:3]) != (32, 32) or not 1 <= x1.shape[3] <= 4:
+        return False
+    if len(specs) < 2 or specs[0].kind != 'conv' or specs[1].kind != 'act':
+        return False
+    p, q = specs[0].params, specs[1].params
+    if (p['parameterization'] != 'ntk' or tuple(p['filter_shape']) != (3, 3)
+            or tuple(p['strides']) != (1, 1) or p['padding'] != Padding.SAME):
+        return False
+    if any(isinstance(p[key], torch.Tensor) and p[key].requires_grad for key in ('W_std', 'b_std')):
+        return False
+    return q['fn'] == 'abrelu' and not q.get('do_stabilize')
+
+
 class ConvActFn(torch.autograd.Function):
     """Conv (3x3, stride 1, SAME, 32 x 32 planes) followed by an activation, and optionally by
     AvgPool((2, 2), (2, 2)): the pair kernels take one pass (ntg_conv_act_fs writes the
@@ -634,30 +750,9 @@ class ConvActFn(torch.autograd.Function):
                None if gt is None else L.ptr(gt.contiguous()), int(pooled), L.ptr(gqi),
                None if gti is None else L.ptr(gti), n1 * n2, n2, a, w2, act, v1, v2,
                gd1.data_ptr(), gd2.data_ptr())
-        vjp = 'ntg_act_pool_bwd' if pooled else 'ntg_act_bwd'
-
-        def self_back(cv, gcv, gd, shape):
-            # activation VJP of a per-sample kernel: its own variance cotangents join the
-            # pair's in gd, which then folds into the kernel's diagonal; then the conv's
-            # transpose (the stride-1 centred stencil is its own transpose)
-            vv = _diag_view(cv)
-            out = torch.empty_like(cv)
-            g = None if gcv is None else L.ptr(gcv.contiguous())
-            if pooled:
-                L.call(vjp, s, L.ptr(cv), None, g, None, L.ptr(out), None, cv.shape[0], 0, a, c,
-                       act, vv, vv, gd.data_ptr(), gd.data_ptr())
-            else:
-                L.call(vjp, s, L.ptr(cv), None, g, None, L.ptr(out), None, cv.shape[0], 0, a, c,
-                       0, act, vv, vv, gd.data_ptr(), gd.data_ptr())
-            L.call('ntg_diag_add', s, gd.data_ptr(), L.ptr(out), cv.shape[0], a, c, vv.s_n,
-                   vv.s_a, vv.s_c)
-            gin, _ = O.conv_fs(out, None, cv.shape[0], 0, a, c, 3, 3, 1, 1, 1, 1, a, c, False,
-                               O.affine(w2, 0., 0., 0., 0., False), O.NO_ACT, O.NO_VAR,
-                               O.NO_VAR, False, (cv.shape[0],))
-            return gin.reshape(shape)
-
-        gc1i = self_back(c1p, gc1, gd1, c1s)
-        gc2i = None if c2s is None else self_back(c2o, gc2, gd2, c2s)
+        gc1i = _conv_act_self_back(c1p, gc1, gd1, act, pooled, w2).reshape(c1s)
+        gc2i = (None if c2s is None else
+                _conv_act_self_back(c2o, gc2, gd2, act, pooled, w2).reshape(c2s))
         return None, None, gqi, gti, gc1i, gc2i, None, None, None
 
     @staticmethod
@@ -845,10 +940,19 @@ def run_ad(specs, x1: torch.Tensor, x2: Optional[torch.Tensor], compute_ntk: boo
     shape1 = tuple(x1.shape)
     shape2 = shape1 if x2 is None else tuple(x2.shape)
     ds = bool(diagonal_spatial) and x1.ndim > 2
-    q, c1, c2 = InputFn.apply(x1, _e(dev) if x2 is None else x2, ctx.gram_precision, ds)
-    t = torch.zeros((), device=dev) if compute_ntk else None
     is_gaussian, is_reversed = False, False
     skip_next = 0
+    if compute_ntk and input_conv_act_fusable(x1, specs, ds):
+        # input covariances, first conv and its activation from the images in one pass
+        p0 = specs[0].params
+        q, t, c1, c2 = InputConvActFn.apply(
+            x1.contiguous(), _e(dev) if x2 is None else x2.contiguous(), _sq(p0['W_std'], dev),
+            _sq(p0['b_std'], dev), _act_struct(specs[1].params, ctx))
+        skip_next = 2
+        is_reversed = True
+    else:
+        q, c1, c2 = InputFn.apply(x1, _e(dev) if x2 is None else x2, ctx.gram_precision, ds)
+        t = torch.zeros((), device=dev) if compute_ntk else None
     for idx, sp in enumerate(specs):
         p = sp.params
         if skip_next:  # layers folded into the rule before them

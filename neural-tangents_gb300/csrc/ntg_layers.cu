@@ -853,6 +853,208 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ---------------------------------------------------------------------------
+// The first layer of a conv net on 32 x 32 images, in one pass per line of a
+// pair: the input covariances G[h, h', w, w'] = sum_k x1[h, w, k] x2[h', w', k] / K
+// (requirements.py:542-553, channels summed in the order of input_fs_vec_kernel,
+// so both round alike), the 3x3 SAME conv rule on them and the activation, as
+// conv3_skew_kernel does on a materialised G. The images of the pair sit in
+// shared memory (planar), so G is never written to or read from HBM. The input
+// NTK is zero and the rule has ntk = nngp_out + W^2 ntk_in, so the conv's NTK
+// equals its NNGP bit for bit: one pre-activation plane (pre_q) serves both.
+// ---------------------------------------------------------------------------
+template <int K>
+__host__ __device__ constexpr size_t skew_input_smem_bytes() {
+  return sizeof(float) * (2 * K * kSkewPlane + 6 * kSkewPlane + 2 * kSkewVars);
+}
+
+template <int K, int ACTK>
+__global__ void __launch_bounds__(kThreads)
+    conv3_skew_input_kernel(const float* __restrict__ x1, const float* __restrict__ x2,
+                            float* __restrict__ out_q, float* __restrict__ out_t,
+                            float* __restrict__ pre_q, int64_t batch, int64_t n2,
+                            ntg_affine_t aff, ntg_act_t act, ntg_var_t var1, ntg_var_t var2,
+                            float inv_k) {
+  extern __shared__ __align__(128) float smem[];
+  constexpr int A = kSkewC;
+  float* im1 = smem;                          // [K][plane] image x1[i1], planar
+  float* im2 = im1 + K * kSkewPlane;          // [K][plane] image x2[i2]
+  float* stage_q = im2 + K * kSkewPlane;      // [2][plane]
+  float* stage_t = stage_q + 2 * kSkewPlane;  // [2][plane]
+  float* stage_p = stage_t + 2 * kSkewPlane;  // [2][plane]
+  float* vrow = stage_p + 2 * kSkewPlane;     // [2][kSkewVars]
+  const int nlines = 2 * A - 1;
+  const int64_t b = blockIdx.x / nlines;
+  const int delta = (int)(blockIdx.x - b * nlines) - (A - 1);
+  if (b >= batch) return;
+  const int i_lo = delta < 0 ? -delta : 0;
+  const int len = (delta < 0 ? A : A - delta) - i_lo;
+  const int64_t pair_stride = (int64_t)A * A * kSkewPlane;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int w0 = (lane & 7) * 4;
+  const int r = (tid >> 5) * 4 + (lane >> 3);
+  const bool has_act = act.kind != NTG_ACT_NONE;
+
+  int u[4], wq[4];
+  float mL[4], mR[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int w = w0 + k;
+    wq[k] = (w + r) & (kSkewC - 1);
+    u[k] = w * kSkewC + wq[k];
+    mL[k] = (w >= 1 && wq[k] >= 1) ? 1.f : 0.f;
+    mR[k] = (w <= kSkewC - 2 && wq[k] <= kSkewC - 2) ? 1.f : 0.f;
+  }
+  int64_t i1, i2;
+  pair_of(b, n2, i1, i2);
+  {  // NHWC images -> planar [K][h * 32 + w]
+    const float* s1 = x1 + i1 * (int64_t)kSkewPlane * K;
+    const float* s2 = x2 + i2 * (int64_t)kSkewPlane * K;
+    for (int e = tid; e < K * kSkewPlane; e += kThreads) {
+      const int pos = e / K, ch = e - pos * K;
+      im1[ch * kSkewPlane + pos] = __ldg(s1 + e);
+      im2[ch * kSkewPlane + pos] = __ldg(s2 + e);
+    }
+  }
+  auto load_vars = [&](int j) {
+    const int i = i_lo + j;
+    float* vb = vrow + (j & 1) * kSkewVars;
+    if (tid < kSkewC) {
+      const float v =
+          __ldg(var1.base + i1 * var1.s_n + (int64_t)i * var1.s_a + (int64_t)tid * var1.s_c);
+      vb[tid] = v;
+      vb[32 + tid] = sqrt_var(v);
+    } else if (tid < 3 * kSkewC) {
+      const int x = tid - kSkewC;
+      const float v = __ldg(var2.base + i2 * var2.s_n + (int64_t)(i + delta) * var2.s_a +
+                            (int64_t)(x & (kSkewC - 1)) * var2.s_c);
+      vb[64 + x] = v;
+      vb[128 + x] = sqrt_var(v);
+    }
+  };
+  if (has_act) load_vars(0);
+  __syncthreads();
+
+  // plane p of the line's input covariance in this thread's skewed order (zero outside)
+  auto take = [&](int p, float (&q)[4]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) q[k] = 0.f;
+    if (p >= len) return;
+    const int h = i_lo + p, hq = h + delta;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      float g = 0.f;
+#pragma unroll
+      for (int ch = 0; ch < K; ++ch)
+        g = fmaf(im1[ch * kSkewPlane + h * kSkewC + w0 + k],
+                 im2[ch * kSkewPlane + hq * kSkewC + wq[k]], g);
+      q[k] = g * inv_k;
+    }
+  };
+
+  const float inv9 = 1.f / 9.f;
+  const ActC ac = act_consts(act);
+  const P2 W2 = p2s(aff.w2 * inv9), B2 = p2s(aff.b2);
+  const P2 TW = p2s(aff.ntk_w2 * inv9), TN = p2s(aff.ntk_nn), TC = p2s(aff.ntk_c);
+  float qm[4], q0[4], qp[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) qm[k] = 0.f;
+  take(0, q0);
+  for (int j = 0; j < len; ++j) {
+    take(j + 1, qp);
+    if (has_act && j + 1 < len) load_vars(j + 1);  // read after the next barrier
+    const int i = i_lo + j;
+    float hq[4], sq[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) hq[k] = (qm[k] + q0[k]) + qp[k];
+    {
+      const float lq = __shfl_up_sync(0xffffffffu, hq[3], 1, 8);
+      const float rq = __shfl_down_sync(0xffffffffu, hq[0], 1, 8);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float L = k == 0 ? lq : hq[k - 1], R = k == 3 ? rq : hq[k + 1];
+        sq[k] = fmaf(R, mR[k], fmaf(L, mL[k], hq[k]));
+      }
+    }
+    // affine rule on packed pairs, the input NTK zero (same rounding as conv3_skew_kernel)
+    P2 q[2], t[2];
+#pragma unroll
+    for (int hh = 0; hh < 2; ++hh) {
+      const P2 cq = p2(sq[2 * hh], sq[2 * hh + 1]), ct = p2s(0.f);
+      q[hh] = fma2(W2, cq, B2);
+      const P2 nn = aff.nn_scaled ? q[hh] : mul2(cq, p2s(inv9));
+      t[hh] = fma2(TW, ct, fma2(TN, nn, TC));
+    }
+    {
+      float* pq = stage_p + (j & 1) * kSkewPlane;
+      float vq[4];
+      p2u(q[0], vq[0], vq[1]);
+      p2u(q[1], vq[2], vq[3]);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) pq[u[k]] = vq[k];
+    }
+    if (has_act) {
+      const float* vb = vrow + (j & 1) * kSkewVars;
+      const float4 v1 = *reinterpret_cast<const float4*>(vb + w0);
+      const float4 s1 = *reinterpret_cast<const float4*>(vb + 32 + w0);
+      float v2[4], s2[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        v2[k] = vb[64 + w0 + r + k];
+        s2[k] = vb[128 + w0 + r + k];
+      }
+      if (ACTK == 1 || (act.kind == NTG_ACT_ABRELU && act.stabilize <= 0.f)) {
+        abrelu2(ac, q[0], t[0], p2(v1.x, v1.y), p2(v2[0], v2[1]), p2(s1.x, s1.y),
+                p2(s2[0], s2[1]));
+        abrelu2(ac, q[1], t[1], p2(v1.z, v1.w), p2(v2[2], v2[3]), p2(s1.z, s1.w),
+                p2(s2[2], s2[3]));
+      } else {
+        const float a1[4] = {v1.x, v1.y, v1.z, v1.w}, b1[4] = {s1.x, s1.y, s1.z, s1.w};
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          float qa, qb, ta, tb;
+          p2u(q[hh], qa, qb);
+          p2u(t[hh], ta, tb);
+          act_apply(ac, qa, ta, a1[2 * hh], v2[2 * hh], b1[2 * hh], s2[2 * hh]);
+          act_apply(ac, qb, tb, a1[2 * hh + 1], v2[2 * hh + 1], b1[2 * hh + 1], s2[2 * hh + 1]);
+          q[hh] = p2(qa, qb);
+          t[hh] = p2(ta, tb);
+        }
+      }
+    }
+    float* gq = stage_q + (j & 1) * kSkewPlane;
+    float* gt = stage_t + (j & 1) * kSkewPlane;
+    {
+      float vq[4], vt[4];
+      p2u(q[0], vq[0], vq[1]);
+      p2u(q[1], vq[2], vq[3]);
+      p2u(t[0], vt[0], vt[1]);
+      p2u(t[1], vt[2], vt[3]);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        gq[u[k]] = vq[k];
+        gt[u[k]] = vt[k];
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      const int64_t off = b * pair_stride + ((int64_t)i * A + i + delta) * kSkewPlane;
+      bulk_store(out_q + off, gq, kSkewPlane * 4u);
+      bulk_store(out_t + off, gt, kSkewPlane * 4u);
+      bulk_store(pre_q + off, stage_p + (j & 1) * kSkewPlane, kSkewPlane * 4u);
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      qm[k] = q0[k];
+      q0[k] = qp[k];
+    }
+  }
+  if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+// ---------------------------------------------------------------------------
 // Backward of a 3x3 / stride 1 / SAME conv + ABRelu (+ AvgPool(2, 2)) on 32 x 32
 // pair kernels in one pass. The reverse of the pair's forward is
 //   activation VJP: (g_pre_q, g_pre_t) = VJP(pre_q, pre_t, var1, var2; g_q, g_t)
@@ -1675,6 +1877,62 @@ extern "C" int ntg_conv_act_fs(void* stream, const float* in_q, const float* in_
   if (e != cudaSuccess) return fail(NTG_ERR_CUDA, std::string("ntg_conv_act_fs: ") + cudaGetErrorString(e));
   note_launch();
   return check_launch("ntg_conv_act_fs");
+}
+
+template <int K, int ACTK>
+cudaError_t launch_skew_input_k(cudaStream_t s, int64_t blocks, const float* x1,
+                                const float* x2, float* out_q, float* out_t, float* pre_q,
+                                int64_t batch, int64_t n2, ntg_affine_t aff, ntg_act_t act,
+                                ntg_var_t var1, ntg_var_t var2) {
+  constexpr size_t sm = skew_input_smem_bytes<K>();
+  cudaError_t e = cudaFuncSetAttribute(conv3_skew_input_kernel<K, ACTK>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e == cudaSuccess)
+    conv3_skew_input_kernel<K, ACTK><<<(unsigned)blocks, kThreads, sm, s>>>(
+        x1, x2, out_q, out_t, pre_q, batch, n2, aff, act, var1, var2, 1.f / (float)K);
+  return e;
+}
+
+template <int K>
+cudaError_t launch_skew_input(bool relu, cudaStream_t s, int64_t blocks, const float* x1,
+                              const float* x2, float* out_q, float* out_t, float* pre_q,
+                              int64_t batch, int64_t n2, ntg_affine_t aff, ntg_act_t act,
+                              ntg_var_t var1, ntg_var_t var2) {
+  return relu ? launch_skew_input_k<K, 1>(s, blocks, x1, x2, out_q, out_t, pre_q, batch, n2, aff,
+                                          act, var1, var2)
+              : launch_skew_input_k<K, 0>(s, blocks, x1, x2, out_q, out_t, pre_q, batch, n2, aff,
+                                          act, var1, var2);
+}
+
+extern "C" int ntg_input_conv_act_fs(void* stream, const float* x1, const float* x2, int64_t n1,
+                                     int64_t n2, int64_t k, float* out_q, float* out_t,
+                                     float* pre_q, ntg_affine_t aff, ntg_act_t act,
+                                     ntg_var_t var1, ntg_var_t var2) {
+  NTG_REQUIRE(x1 && x2 && out_q && out_t && pre_q && var1.base && var2.base,
+              "ntg_input_conv_act_fs: null pointer");
+  NTG_REQUIRE(n1 > 0 && n2 > 0 && k >= 1 && k <= 4, "ntg_input_conv_act_fs: bad sizes");
+  NTG_REQUIRE(aff.ntk_nn == 1.f && aff.ntk_c == 0.f && aff.nn_scaled,
+              "ntg_input_conv_act_fs: needs the NTK rule ntk = nngp_out + W^2 ntk_in");
+  NTG_REQUIRE(act.kind != NTG_ACT_NONE, "ntg_input_conv_act_fs: needs an activation");
+  const bool aligned = ((reinterpret_cast<uintptr_t>(out_q) | reinterpret_cast<uintptr_t>(out_t) |
+                         reinterpret_cast<uintptr_t>(pre_q)) & 15) == 0;
+  NTG_REQUIRE(aligned, "ntg_input_conv_act_fs: outputs must be 16-byte aligned");
+  const int64_t batch = n1 * n2;
+  const int64_t blocks = batch * (2 * kSkewC - 1);
+  NTG_REQUIRE(blocks < (1ll << 31), "ntg_input_conv_act_fs: grid too large");
+  const bool relu = act.kind == NTG_ACT_ABRELU && act.stabilize <= 0.f;
+  cudaStream_t s = as_stream(stream);
+  cudaError_t e;
+  switch (k) {
+    case 1: e = launch_skew_input<1>(relu, s, blocks, x1, x2, out_q, out_t, pre_q, batch, n2, aff, act, var1, var2); break;
+    case 2: e = launch_skew_input<2>(relu, s, blocks, x1, x2, out_q, out_t, pre_q, batch, n2, aff, act, var1, var2); break;
+    case 3: e = launch_skew_input<3>(relu, s, blocks, x1, x2, out_q, out_t, pre_q, batch, n2, aff, act, var1, var2); break;
+    default: e = launch_skew_input<4>(relu, s, blocks, x1, x2, out_q, out_t, pre_q, batch, n2, aff, act, var1, var2); break;
+  }
+  if (e != cudaSuccess)
+    return fail(NTG_ERR_CUDA, std::string("ntg_input_conv_act_fs: ") + cudaGetErrorString(e));
+  note_launch();
+  return check_launch("ntg_input_conv_act_fs");
 }
 
 template <bool POOLED>

@@ -607,3 +607,65 @@ def test_fused_conv_act_backward_in_network(nt):
     scale = max(np.abs(u1).max(), np.abs(u2).max())
     np.testing.assert_allclose(f1, u1, rtol=0, atol=1e-5 * scale)
     np.testing.assert_allclose(f2, u2, rtol=0, atol=1e-5 * scale)
+
+
+def test_input_conv_act_fused_forward_and_backward(nt):
+    """The first conv + ReLU of a 32 x 32 net computed from the images (ntg_input_conv_act_fs)
+    gives the layer-by-layer kernels bit for bit, and its gradients equal those of the unfused
+    rules (W_std a tensor that needs a gradient) and central differences of the oracle."""
+    from nt_gb300 import _lib as L, _ops as O, stax
+    rng = np.random.default_rng(26)
+    x1 = rng.standard_normal((2, 32, 32, 3)).astype(np.float32)
+    x2 = rng.standard_normal((3, 32, 32, 3)).astype(np.float32)
+    t1, t2 = torch.from_numpy(x1).cuda(), torch.from_numpy(x2).cuda()
+    aff = O.affine(2.0, 0.01, 2.0)
+    act = L.Act(L.NTG_ACT_ABRELU, 0., 1., 0., 0, 0.)
+    cv1 = O.conv_fs(O.input_fs(t1, None), None, 2, 0, 32, 32, 3, 3, 1, 1, 1, 1, 32, 32, False, aff,
+                    O.NO_ACT, O.NO_VAR, O.NO_VAR, False, (2,))[0]
+    cv2 = O.conv_fs(O.input_fs(t2, None), None, 3, 0, 32, 32, 3, 3, 1, 1, 1, 1, 32, 32, False, aff,
+                    O.NO_ACT, O.NO_VAR, O.NO_VAR, False, (3,))[0]
+    v1, v2 = O.var_view(cv1, False), O.var_view(cv2, False)
+    shape = (2, 3, 32, 32, 32, 32)
+    qa, ta, pre = (torch.empty(shape, device='cuda') for _ in range(3))
+    L.call('ntg_input_conv_act_fs', L.stream(), L.ptr(t1), L.ptr(t2), 2, 3, 3, L.ptr(qa),
+           L.ptr(ta), L.ptr(pre), aff, act, v1, v2)
+    g = O.input_fs(t1, t2)
+    wq, wt, pq, pt = (torch.empty(shape, device='cuda') for _ in range(4))
+    L.call('ntg_conv_act_fs', L.stream(), L.ptr(g), None, L.ptr(wq), L.ptr(wt), L.ptr(pq),
+           L.ptr(pt), 6, 3, 32, 32, aff, act, v1, v2)
+    torch.cuda.synchronize()
+    assert torch.equal(qa, wq) and torch.equal(ta, wt)
+    assert torch.equal(pre, pq) and torch.equal(pre, pt)
+
+    wq_, wt_ = rng.standard_normal((2, 3)), rng.standard_normal((2, 3))
+
+    def layers(m, w):
+        return [m.Conv(1, (3, 3), padding='SAME', W_std=w, b_std=0.1), m.Relu(),
+                m.AvgPool((2, 2), (2, 2)), m.Conv(1, (3, 3), padding='SAME', W_std=1.2),
+                m.Relu(), m.GlobalAvgPool(), m.Dense(1, 1.1, 0.)]
+
+    def grads(hyper):
+        w = torch.tensor(1.4, device='cuda', requires_grad=True) if hyper else 1.4
+        a = torch.tensor(x1, device='cuda', requires_grad=True)
+        b = torch.tensor(x2, device='cuda', requires_grad=True)
+        q, t = stax.serial(*layers(stax, w))[2](a, b, ('nngp', 'ntk'))
+        ((torch.from_numpy(wq_).float().cuda() * q).sum() +
+         (torch.from_numpy(wt_).float().cuda() * t).sum()).backward()
+        return a.grad.cpu().numpy(), b.grad.cpu().numpy(), q.detach().cpu().numpy()
+
+    f1, f2, fq = grads(False)
+    u1, u2, uq = grads(True)
+    # W_std given as a float is squared in double, as a tensor in float32: W^2 may differ by an ulp
+    np.testing.assert_allclose(fq, uq, rtol=1e-6)
+    scale = max(np.abs(u1).max(), np.abs(u2).max())
+    np.testing.assert_allclose(f1, u1, rtol=0, atol=1e-5 * scale)
+    np.testing.assert_allclose(f2, u2, rtol=0, atol=1e-5 * scale)
+    x1d, x2d = x1.astype(np.float64), x2.astype(np.float64)
+
+    def loss_oracle(a, b):
+        q, t = o.serial(*layers(o, 1.4))(a, b, ('nngp', 'ntk'))
+        return float(np.sum(wq_ * q) + np.sum(wt_ * t))
+
+    for idx in [(0, 0, 0, 0), (1, 17, 9, 2)]:
+        want = fd(lambda a: loss_oracle(a, x2d), x1d, idx)
+        assert abs(f1[idx] - want) < 3e-3 * scale, (idx, f1[idx], want)
