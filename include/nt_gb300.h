@@ -288,6 +288,18 @@ int ntg_act_pool_bwd(void* stream, const float* q, const float* t, const float* 
                      const float* gt_pooled, float* oq, float* ot, int64_t batch, int64_t n2,
                      int64_t a, int64_t c, ntg_act_t act, ntg_var_t var1, ntg_var_t var2,
                      float* gvar1, float* gvar2);
+/* ntg_conv_act_fs followed by AvgPool((2, 2), (2, 2)) without the activated
+ * [B, 32, 32, 32, 32] kernels being written: the conv + activation kernel leaves
+ * the w-direction window sums of each plane in hp_q / hp_t (caller-provided,
+ * [B, 32, 32, 16, 16]) and a second pass adds the planes into out_q / out_t
+ * [B, 16, 16, 16, 16] in the summation order of ntg_pool, so the result equals
+ * ntg_conv_act_fs + ntg_pool bit for bit. pre_q / pre_t receive the conv outputs
+ * (the activation's VJP input). No reference counterpart (linear.py:1631-1664
+ * and :1321-1424 are separate XLA ops). */
+int ntg_conv_act_pool_fs(void* stream, const float* in_q, const float* in_t, float* out_q,
+                         float* out_t, float* pre_q, float* pre_t, float* hp_q, float* hp_t,
+                         int64_t batch, int64_t n2, int64_t a, ntg_affine_t aff, ntg_act_t act,
+                         ntg_var_t var1, ntg_var_t var2);
 /* First layer of a conv net on 32 x 32 images in one pass: the pair input
  * covariances of x1 [N1, 32, 32, K], x2 [N2, 32, 32, K] (1 <= K <= 4, NHWC;
  * requirements.py:542-553), the 3x3 SAME conv rule on them (linear.py:1321-1424,

@@ -698,9 +698,22 @@ class ConvActFn(torch.autograd.Function):
         t4 = None if zero_t else _as4(t.contiguous(), 2)
         shape = (n1, n2, a, a, c, c)
         qp, tp = torch.empty(shape, device=dev), torch.empty(shape, device=dev)
-        qa, ta = torch.empty(shape, device=dev), torch.empty(shape, device=dev)
-        L.call('ntg_conv_act_fs', L.stream(), L.ptr(q4), None if t4 is None else L.ptr(t4),
-               L.ptr(qa), L.ptr(ta), L.ptr(qp), L.ptr(tp), n1 * n2, n2, a, c, aff, act, v1, v2)
+        if pool_geom is not None:
+            # the activated pair kernels go straight into the pool (ntg_conv_act_pool_fs):
+            # only their window sums along w are written, then added plane by plane
+            pshape = (n1, n2, pool_geom[8], pool_geom[8], pool_geom[9], pool_geom[9])
+            qa, ta = torch.empty(pshape, device=dev), torch.empty(pshape, device=dev)
+            hq = torch.empty((n1 * n2, a, a, c // 2, c // 2), device=dev)
+            ht = torch.empty_like(hq)
+            L.call('ntg_conv_act_pool_fs', L.stream(), L.ptr(q4),
+                   None if t4 is None else L.ptr(t4), L.ptr(qa), L.ptr(ta), L.ptr(qp), L.ptr(tp),
+                   L.ptr(hq), L.ptr(ht), n1 * n2, n2, a, aff, act, v1, v2)
+            del hq, ht
+        else:
+            qa, ta = torch.empty(shape, device=dev), torch.empty(shape, device=dev)
+            L.call('ntg_conv_act_fs', L.stream(), L.ptr(q4), None if t4 is None else L.ptr(t4),
+                   L.ptr(qa), L.ptr(ta), L.ptr(qp), L.ptr(tp), n1 * n2, n2, a, c, aff, act, v1,
+                   v2)
 
         def act_self(cv):
             vv = _diag_view(cv)
@@ -725,7 +738,7 @@ class ConvActFn(torch.autograd.Function):
                 return O.pool(x.contiguous(), int(math.prod(lead)), a, c, 2, 2, 2, 2, pa_, pc_,
                               ao2, co2, False, False, True, False, lead + (ao2, ao2, co2, co2))
 
-            outs = [pool(outs[0], 2), pool(outs[1], 2), pool(outs[2], 1), pool(outs[3], 1)]
+            outs = [outs[0], outs[1], pool(outs[2], 1), pool(outs[3], 1)]
         return tuple(outs)
 
     @staticmethod

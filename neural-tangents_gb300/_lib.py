@@ -87,6 +87,8 @@ SIGNATURES = {
                      _P], C.c_int),
     'ntg_act_pool_bwd': ([_P, _P, _P, _P, _P, _P, _P, _I64, _I64, _I64, _I64, Act, Var, Var, _P,
                           _P], C.c_int),
+    'ntg_conv_act_pool_fs': ([_P, _P, _P, _P, _P, _P, _P, _P, _P, _I64, _I64, _I64, Affine, Act,
+                             Var, Var], C.c_int),
     'ntg_input_conv_act_fs': ([_P, _P, _P, _I64, _I64, _I64, _P, _P, _P, Affine, Act, Var, Var],
                               C.c_int),
     'ntg_conv_act_bwd': ([_P, _P, _P, _P, _P, _I32, _P, _P, _I64, _I64, _I64, _F, Act, Var, Var,

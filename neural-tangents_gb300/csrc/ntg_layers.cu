@@ -603,13 +603,15 @@ __device__ __forceinline__ void bulk_store(float* gdst, const float* ssrc, uint3
 }
 
 // ACTK: 1 = the ABRelu family without do_stabilize only (the other rules compiled out),
-// 0 = any activation rule.
-template <bool HAS_T, int RING, int ACTK>
+// 0 = any activation rule. HP: an AvgPool(2, 2) follows; the kernel writes hp_q / hp_t
+// (window sums along w) instead of out_q / out_t.
+template <bool HAS_T, int RING, int ACTK, bool HP = false>
 __global__ void __launch_bounds__(kThreads)
     conv3_skew_kernel(const float* __restrict__ in_q, const float* __restrict__ in_t,
                       float* __restrict__ out_q, float* __restrict__ out_t, int64_t batch,
                       int64_t n2, int A, ntg_affine_t aff, ntg_act_t act, ntg_var_t var1,
-                      ntg_var_t var2, float* __restrict__ pre_q, float* __restrict__ pre_t) {
+                      ntg_var_t var2, float* __restrict__ pre_q, float* __restrict__ pre_t,
+                      float* __restrict__ hp_q, float* __restrict__ hp_t) {
   extern __shared__ __align__(128) float smem[];
   __shared__ int s_err;
   float* ring_q = smem;                           // [RING][plane]
@@ -814,7 +816,7 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         gq[u[k]] = vq[k];
-        if (out_t) gt[u[k]] = vt[k];
+        if (HP ? hp_t != nullptr : out_t != nullptr) gt[u[k]] = vt[k];
       }
     }
     // staging writes -> visible to the bulk-copy engine; the store of plane j - 1
@@ -822,10 +824,26 @@ __global__ void __launch_bounds__(kThreads)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
     __syncthreads();
+    if (HP) {
+      // an AvgPool(2, 2) follows: instead of the activated planes, their w-direction
+      // window sums (x[2j][2j'] + x[2j][2j'+1]) + (x[2j+1][2j'] + x[2j+1][2j'+1]), the
+      // inner sums of pool_kernel's order; pool_planes_kernel adds the planes
+      const int jj = tid >> 4, jp = tid & 15;
+      const int64_t ho = b * (int64_t)A * A * (kSkewPlane / 4) +
+                         ((int64_t)i * A + i + delta) * (kSkewPlane / 4) + tid;
+      const float* xq = gq + (2 * jj) * kSkewC + 2 * jp;
+      hp_q[ho] = (xq[0] + xq[1]) + (xq[kSkewC] + xq[kSkewC + 1]);
+      if (hp_t) {
+        const float* xt = gt + (2 * jj) * kSkewC + 2 * jp;
+        hp_t[ho] = (xt[0] + xt[1]) + (xt[kSkewC] + xt[kSkewC + 1]);
+      }
+    }
     if (tid == 0) {
       const int64_t off = b * pair_stride + ((int64_t)i * A + i + delta) * kSkewPlane;
-      bulk_store(out_q + off, gq, kSkewPlane * 4u);
-      if (out_t) bulk_store(out_t + off, gt, kSkewPlane * 4u);
+      if (!HP) {
+        bulk_store(out_q + off, gq, kSkewPlane * 4u);
+        if (out_t) bulk_store(out_t + off, gt, kSkewPlane * 4u);
+      }
       if (pre_q) {
         bulk_store(pre_q + off, stage_pq + (j & 1) * kSkewPlane, kSkewPlane * 4u);
         if (pre_t) bulk_store(pre_t + off, stage_pt + (j & 1) * kSkewPlane, kSkewPlane * 4u);
@@ -1522,6 +1540,31 @@ struct PoolGeom {
   int wa, wc, sa, sc, pa, pc, circular, diag, average, normalize_edges, pool2;
 };
 
+// Second stage of AvgPool((2, 2), (2, 2)) after conv3_skew_kernel's half-pooled
+// output hp [B, A, A, 16, 16] (w-direction window sums of each (h, h') plane):
+// out[b, i, i', e] = (((hp(2i+1, 2i') + hp(2i, 2i')) + hp(2i+1, 2i'+1)) + hp(2i, 2i'+1)) / 16,
+// pool_kernel's pool2 order, so both paths round alike.
+__global__ void pool_planes_kernel(const float* __restrict__ hp, float* __restrict__ out,
+                                   int64_t batch, int A) {
+  const int Ah = A / 2;
+  const int64_t total = batch * Ah * Ah * 256;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int e = (int)(idx & 255);
+    int64_t r = idx >> 8;
+    const int ip = (int)(r % Ah);
+    r /= Ah;
+    const int i = (int)(r % Ah);
+    const int64_t b = r / Ah;
+    const float* base = hp + b * (int64_t)A * A * 256 + e;
+    auto plane = [&](int u, int up) {
+      return __ldg(base + ((int64_t)(2 * i + u) * A + 2 * ip + up) * 256);
+    };
+    const float sum = ((plane(1, 0) + plane(0, 0)) + plane(1, 1)) + plane(0, 1);
+    out[idx] = sum / 16.f;
+  }
+}
+
 __global__ void pool_kernel(const float* __restrict__ in, float* __restrict__ out, PoolGeom g) {
   const int64_t per_b = g.diag ? g.Ao * g.Co : g.Ao * g.Ao * g.Co * g.Co;
   const int64_t in_b = g.diag ? g.A * g.C : g.A * g.A * g.C * g.C;
@@ -1745,17 +1788,19 @@ extern "C" int ntg_input_ds(void* stream, const float* x1, const float* x2, int6
   return check_launch("ntg_input_ds");
 }
 
-template <bool HAS_T, int RING, int ACTK>
+template <bool HAS_T, int RING, int ACTK, bool HP = false>
 cudaError_t launch_skew_k(cudaStream_t s, int64_t blocks, size_t sm, const float* in_q,
                           const float* in_t, float* out_q, float* out_t, int64_t batch,
                           int64_t n2, int64_t a, ntg_affine_t aff, ntg_act_t act, ntg_var_t var1,
-                          ntg_var_t var2, float* pre_q, float* pre_t) {
-  cudaError_t e = cudaFuncSetAttribute(conv3_skew_kernel<HAS_T, RING, ACTK>,
+                          ntg_var_t var2, float* pre_q, float* pre_t, float* hp_q,
+                          float* hp_t) {
+  cudaError_t e = cudaFuncSetAttribute(conv3_skew_kernel<HAS_T, RING, ACTK, HP>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)skew_smem_bytes_pre<RING>());
   if (e == cudaSuccess)
-    conv3_skew_kernel<HAS_T, RING, ACTK><<<(unsigned)blocks, kThreads, sm, s>>>(
-        in_q, in_t, out_q, out_t, batch, n2, (int)a, aff, act, var1, var2, pre_q, pre_t);
+    conv3_skew_kernel<HAS_T, RING, ACTK, HP><<<(unsigned)blocks, kThreads, sm, s>>>(
+        in_q, in_t, out_q, out_t, batch, n2, (int)a, aff, act, var1, var2, pre_q, pre_t, hp_q,
+        hp_t);
   return e;
 }
 
@@ -1769,13 +1814,40 @@ cudaError_t launch_skew(cudaStream_t s, int64_t blocks, const float* in_q, const
                     (act.kind == NTG_ACT_ABRELU && act.stabilize <= 0.f);
   if (in_t)
     return relu ? launch_skew_k<true, RING, 1>(s, blocks, sm, in_q, in_t, out_q, out_t, batch, n2,
-                                               a, aff, act, var1, var2, pre_q, pre_t)
+                                               a, aff, act, var1, var2, pre_q, pre_t, nullptr,
+                                               nullptr)
                 : launch_skew_k<true, RING, 0>(s, blocks, sm, in_q, in_t, out_q, out_t, batch, n2,
-                                               a, aff, act, var1, var2, pre_q, pre_t);
+                                               a, aff, act, var1, var2, pre_q, pre_t, nullptr,
+                                               nullptr);
   return relu ? launch_skew_k<false, RING, 1>(s, blocks, sm, in_q, nullptr, out_q, out_t, batch,
-                                              n2, a, aff, act, var1, var2, pre_q, pre_t)
+                                              n2, a, aff, act, var1, var2, pre_q, pre_t, nullptr,
+                                              nullptr)
               : launch_skew_k<false, RING, 0>(s, blocks, sm, in_q, nullptr, out_q, out_t, batch,
-                                              n2, a, aff, act, var1, var2, pre_q, pre_t);
+                                              n2, a, aff, act, var1, var2, pre_q, pre_t, nullptr,
+                                              nullptr);
+}
+
+// The conv + activation kernel with the half-pooled output (ring depth 4).
+cudaError_t launch_skew_pool(cudaStream_t s, int64_t blocks, const float* in_q,
+                             const float* in_t, int64_t batch, int64_t n2, int64_t a,
+                             ntg_affine_t aff, ntg_act_t act, ntg_var_t var1, ntg_var_t var2,
+                             float* pre_q, float* pre_t, float* hp_q, float* hp_t) {
+  const size_t sm = skew_smem_bytes_pre<4>();
+  const bool relu = act.kind == NTG_ACT_NONE ||
+                    (act.kind == NTG_ACT_ABRELU && act.stabilize <= 0.f);
+  if (in_t)
+    return relu ? launch_skew_k<true, 4, 1, true>(s, blocks, sm, in_q, in_t, nullptr, nullptr,
+                                                  batch, n2, a, aff, act, var1, var2, pre_q,
+                                                  pre_t, hp_q, hp_t)
+                : launch_skew_k<true, 4, 0, true>(s, blocks, sm, in_q, in_t, nullptr, nullptr,
+                                                  batch, n2, a, aff, act, var1, var2, pre_q,
+                                                  pre_t, hp_q, hp_t);
+  return relu ? launch_skew_k<false, 4, 1, true>(s, blocks, sm, in_q, nullptr, nullptr, nullptr,
+                                                 batch, n2, a, aff, act, var1, var2, pre_q,
+                                                 pre_t, hp_q, hp_t)
+              : launch_skew_k<false, 4, 0, true>(s, blocks, sm, in_q, nullptr, nullptr, nullptr,
+                                                 batch, n2, a, aff, act, var1, var2, pre_q,
+                                                 pre_t, hp_q, hp_t);
 }
 
 extern "C" int ntg_conv_fs(void* stream, const float* in_q, const float* in_t, float* out_q,
@@ -1976,6 +2048,39 @@ extern "C" int ntg_conv_act_bwd(void* stream, const float* pre_q, const float* p
     return fail(NTG_ERR_CUDA, std::string("ntg_conv_act_bwd: ") + cudaGetErrorString(e));
   note_launch();
   return check_launch("ntg_conv_act_bwd");
+}
+
+extern "C" int ntg_conv_act_pool_fs(void* stream, const float* in_q, const float* in_t,
+                                    float* out_q, float* out_t, float* pre_q, float* pre_t,
+                                    float* hp_q, float* hp_t, int64_t batch, int64_t n2,
+                                    int64_t a, ntg_affine_t aff, ntg_act_t act, ntg_var_t var1,
+                                    ntg_var_t var2) {
+  NTG_REQUIRE(in_q && out_q && pre_q && hp_q, "ntg_conv_act_pool_fs: null pointer");
+  NTG_REQUIRE(!out_t == !pre_t && !out_t == !hp_t,
+              "ntg_conv_act_pool_fs: out_t, pre_t and hp_t go together");
+  NTG_REQUIRE(batch > 0 && a == kSkewC, "ntg_conv_act_pool_fs: needs [B, 32, 32, 32, 32] kernels");
+  NTG_REQUIRE(act.kind == NTG_ACT_NONE || (var1.base && var2.base),
+              "ntg_conv_act_pool_fs: activation needs var1/var2");
+  const bool aligned = ((reinterpret_cast<uintptr_t>(in_q) | reinterpret_cast<uintptr_t>(in_t) |
+                         reinterpret_cast<uintptr_t>(pre_q) | reinterpret_cast<uintptr_t>(pre_t)) &
+                        15) == 0;
+  NTG_REQUIRE(aligned, "ntg_conv_act_pool_fs: buffers must be 16-byte aligned");
+  const int64_t blocks = batch * (2 * a - 1);
+  NTG_REQUIRE(blocks < (1ll << 31), "ntg_conv_act_pool_fs: grid too large");
+  cudaStream_t s = as_stream(stream);
+  const cudaError_t e = launch_skew_pool(s, blocks, in_q, in_t, batch, n2, a, aff, act, var1,
+                                         var2, pre_q, pre_t, hp_q, hp_t);
+  if (e != cudaSuccess)
+    return fail(NTG_ERR_CUDA, std::string("ntg_conv_act_pool_fs: ") + cudaGetErrorString(e));
+  note_launch();
+  const int64_t total = batch * (a / 2) * (a / 2) * 256;
+  pool_planes_kernel<<<grid_for(total), kThreads, 0, s>>>(hp_q, out_q, batch, (int)a);
+  note_launch();
+  if (out_t) {
+    pool_planes_kernel<<<grid_for(total), kThreads, 0, s>>>(hp_t, out_t, batch, (int)a);
+    note_launch();
+  }
+  return check_launch("ntg_conv_act_pool_fs");
 }
 
 extern "C" int ntg_conv_input_fs(void* stream, const float* x1, const float* x2, int64_t n1,

@@ -669,3 +669,40 @@ def test_input_conv_act_fused_forward_and_backward(nt):
     for idx in [(0, 0, 0, 0), (1, 17, 9, 2)]:
         want = fd(lambda a: loss_oracle(a, x2d), x1d, idx)
         assert abs(f1[idx] - want) < 3e-3 * scale, (idx, f1[idx], want)
+
+
+@pytest.mark.parametrize('has_t', [False, True])
+def test_conv_act_pool_forward_matches_two_kernels(nt, has_t):
+    """ntg_conv_act_pool_fs (conv + ReLU with the pool's window sums taken in the kernel)
+    equals ntg_conv_act_fs followed by ntg_pool bit for bit, pre-activations included."""
+    from nt_gb300 import _lib as L, _ops as O
+    g = torch.Generator(device='cuda').manual_seed(6)
+    n1, n2, A = 2, 2, 32
+    shp = (n1 * n2, A, A, A, A)
+    cov = torch.rand((n1 + n2, A, A, A, A), device='cuda', generator=g) * 0.2
+    for a in range(A):
+        cov[:, a, a, :, :].diagonal(dim1=-2, dim2=-1).add_(2.)
+    sa = A * A * A + A * A
+    v1 = L.Var(cov[:n1].data_ptr(), A ** 4, sa, A + 1)
+    v2 = L.Var(cov[n1:].data_ptr(), A ** 4, sa, A + 1)
+    act = L.Act(L.NTG_ACT_ABRELU, 0., 1., 0., 0, 0.)
+    aff = O.affine(2.0, 0.05, 2.0)
+    q = torch.rand(shp, device='cuda', generator=g) * 2 - 1
+    t = torch.rand(shp, device='cuda', generator=g) if has_t else None
+    pshape = (n1 * n2, 16, 16, 16, 16)
+    oq, ot = torch.empty(pshape, device='cuda'), torch.empty(pshape, device='cuda')
+    pq, pt = torch.empty(shp, device='cuda'), torch.empty(shp, device='cuda')
+    hq = torch.empty((n1 * n2, A, A, 16, 16), device='cuda')
+    ht = torch.empty_like(hq)
+    L.call('ntg_conv_act_pool_fs', L.stream(), L.ptr(q), None if t is None else L.ptr(t),
+           L.ptr(oq), L.ptr(ot), L.ptr(pq), L.ptr(pt), L.ptr(hq), L.ptr(ht), n1 * n2, n2, A, aff,
+           act, v1, v2)
+    aq, at = torch.empty(shp, device='cuda'), torch.empty(shp, device='cuda')
+    rq, rt = torch.empty(shp, device='cuda'), torch.empty(shp, device='cuda')
+    L.call('ntg_conv_act_fs', L.stream(), L.ptr(q), None if t is None else L.ptr(t), L.ptr(aq),
+           L.ptr(at), L.ptr(rq), L.ptr(rt), n1 * n2, n2, A, A, aff, act, v1, v2)
+    want_q = O.pool(aq, n1 * n2, A, A, 2, 2, 2, 2, 0, 0, 16, 16, False, False, True, False, pshape)
+    want_t = O.pool(at, n1 * n2, A, A, 2, 2, 2, 2, 0, 0, 16, 16, False, False, True, False, pshape)
+    torch.cuda.synchronize()
+    assert torch.equal(pq, rq) and torch.equal(pt, rt)
+    assert torch.equal(oq, want_q) and torch.equal(ot, want_t)
