@@ -1099,7 +1099,7 @@ __host__ __device__ constexpr int skew_vjp_slot_floats() {
 template <bool POOLED>
 __host__ __device__ constexpr size_t skew_vjp_smem_bytes() {
   return sizeof(float) * (kVjpRing * skew_vjp_slot_floats<POOLED>() + 4 * kSkewPlane +
-                          3 * 64 + 3 * 64) +
+                          3 * 64 + 3 * 8 * 64) +
          sizeof(uint64_t) * kVjpRing;
 }
 
@@ -1117,7 +1117,7 @@ __device__ __forceinline__ void skew_vjp_body(
   float* stage_q = ring + kVjpRing * SLOT;              // [2][plane]
   float* stage_t = stage_q + 2 * kSkewPlane;            // [2][plane]
   float* vrow = stage_t + 2 * kSkewPlane;               // [3][v1[32] | v2[32]]
-  float* sg = vrow + 3 * 64;                            // [3][g v1[32] | g v2[32]]
+  float* sg = vrow + 3 * 64;                            // [3][warp][g v1[32] | g v2[32]]
   uint64_t* bars = reinterpret_cast<uint64_t*>(sg + 3 * 64);
   const int nlines = 2 * A - 1;
   const int64_t b = blockIdx.x / nlines;
@@ -1132,7 +1132,8 @@ __device__ __forceinline__ void skew_vjp_body(
                          (uint32_t)((g_q ? 1 : 0) + (g_t ? 1 : 0)) * (uint32_t)(GP * sizeof(float));
   const int tid = threadIdx.x, lane = tid & 31;
   const int w0 = (lane & 7) * 4;
-  const int r = (tid >> 5) * 4 + (lane >> 3);
+  const int r0 = (tid >> 5) * 4;  // first skewed row of this warp
+  const int r = r0 + (lane >> 3);
 
   int u[4], gu[4], wq[4];
   float mL[4], mR[4];
@@ -1158,12 +1159,13 @@ __device__ __forceinline__ void skew_vjp_body(
       vb[tid] = __ldg(var2.base + i2 * var2.s_n + (int64_t)(i + delta) * var2.s_a +
                       (int64_t)(tid - kSkewC) * var2.s_c);
   };
-  // adds plane j's variance cotangents to gvar1 / gvar2 and clears its sums
+  // adds plane j's variance cotangents (the eight warps' partial sums) to gvar1 / gvar2
   auto flush = [&](int j) {
-    float* s = sg + (j % 3) * 64;
+    const float* s = sg + (j % 3) * (8 * 64);
     if (tid < 2 * kSkewC) {
-      const float v = s[tid];
-      s[tid] = 0.f;
+      float v = 0.f;
+#pragma unroll
+      for (int wv = 0; wv < 8; ++wv) v += s[wv * 64 + tid];
       const int i = i_lo + j;
       if (tid < kSkewC) {
         if (gvar1 && v != 0.f) atomicAdd(gvar1 + (i1 * A + i) * kSkewC + tid, v);
@@ -1179,7 +1181,6 @@ __device__ __forceinline__ void skew_vjp_body(
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[sl])));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int k = tid; k < 3 * 64; k += kThreads) sg[k] = 0.f;
   load_vars(0);
   if (len > 1) load_vars(1);
   __syncthreads();
@@ -1250,16 +1251,21 @@ __device__ __forceinline__ void skew_vjp_body(
       p2u(a12, o1[2 * h], o1[2 * h + 1]);
       p2u(a22, o2[2 * h], o2[2 * h + 1]);
     }
-    float* s = sg + (p % 3) * 64;
+    // this warp's partial sums of the plane's variance cotangents, written without atomics:
+    // var1 at w (the warp's four row groups share w), var2 at w' = w + r, gathered so that
+    // lane T holds target T (for element slot k it comes from the lane with 4a + b = T - k - r0)
+    float* s = sg + (p % 3) * (8 * 64) + (tid >> 5) * 64;
+    float y = 0.f;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      // var1 cotangent at w: the four row groups of the warp share w
       float x = o1[k];
       x += __shfl_xor_sync(0xffffffffu, x, 8);
       x += __shfl_xor_sync(0xffffffffu, x, 16);
-      if (lane < 8) atomicAdd(&s[w0 + k], x);
-      atomicAdd(&s[kSkewC + wq[k]], o2[k]);
+      if (lane < 8) s[w0 + k] = x;
+      const int m = (lane - k - r0) & (kSkewC - 1);
+      y += __shfl_sync(0xffffffffu, o2[k], ((m & 3) << 3) | (m >> 2));
     }
+    s[kSkewC + lane] = y;
   };
 
   const float inv9 = 1.f / 9.f;
