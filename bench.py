@@ -487,9 +487,11 @@ def nll_timing(torch, nt, dev):
     X [4096, 3072], Y [4096, 10] (iid N(0,1)) and its gradient with respect to the shared
     (W_std, b_std): input Gram, layer rules and their adjoints, Cholesky and its adjoint."""
     from nt_gb300 import predict, stax
-    x = torch.randn((4096, 3072), device=dev)
-    y = torch.randn((4096, 10), device=dev)
-    out = {'config': 'depth-3 FCN NNGP NLL, X [4096, 3072], d/d(W_std, b_std)'}
+    gen = torch.Generator(device='cpu').manual_seed(3)
+    x = torch.randn((4096, 3072), generator=gen).to(dev)
+    y = torch.randn((4096, 10), generator=gen).to(dev)
+    out = {'config': 'depth-3 FCN NNGP NLL, X [4096, 3072] and Y [4096, 10] iid N(0, 1) '
+                     '(seed 3), d/d(W_std, b_std)'}
     for prec in ('fp32', 'mixed'):
         w = torch.tensor(1.5, device=dev, requires_grad=True)
         b = torch.tensor(0.1, device=dev, requires_grad=True)

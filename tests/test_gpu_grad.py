@@ -706,3 +706,36 @@ def test_conv_act_pool_forward_matches_two_kernels(nt, has_t):
     torch.cuda.synchronize()
     assert torch.equal(pq, rq) and torch.equal(pt, rt)
     assert torch.equal(oq, want_q) and torch.equal(ot, want_t)
+
+
+def test_nll_hyper_gradients_ill_conditioned(nt):
+    """The NLL gradient of the FCN configuration (x [256, 784] on the sphere of radius sqrt(784),
+    diag_reg 1e-4): the self pairs sit at correlation 1, where the activation VJP must see
+    var1 var2 - q^2 == 0 exactly (the _sqrt convention cuts the singular term); a rounding
+    residue there is amplified by the ill-conditioned solve."""
+    import scipy.linalg as sla
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal((256, 784))
+    x *= np.sqrt(784) / np.linalg.norm(x, axis=1, keepdims=True)
+    y = np.eye(10)[rng.integers(0, 10, 256)]
+    hp = np.array([1.5, 0.05])
+
+    def layers(m, w, b):
+        return [m.Dense(512, w, b), m.Relu(), m.Dense(512, w, b), m.Relu(), m.Dense(1, w, b)]
+
+    def nll_oracle(h):
+        k = o.serial(*layers(o, h[0], h[1]))(x, None, 'nngp')
+        a = k + 1e-4 * np.trace(k) / 256 * np.eye(256)
+        c = sla.cho_factor(a)
+        alpha = sla.cho_solve(c, y)
+        # 0.5 y^T A^-1 y + (10 / 2) log det A, log det A = 2 sum log diag(L)
+        return 0.5 * np.sum(y * alpha) + 10 * np.sum(np.log(np.diag(c[0]))) + \
+            0.5 * 256 * 10 * np.log(2 * np.pi)
+
+    w = torch.tensor(hp[0], device='cuda', requires_grad=True)
+    b = torch.tensor(hp[1], device='cuda', requires_grad=True)
+    k = nt.stax.serial(*layers(nt.stax, w, b))[2](x, None, 'nngp')
+    nt.predict.negative_log_likelihood(k, y, diag_reg=1e-4).backward()
+    got = np.array([w.grad.item(), b.grad.item()])
+    want = np.array([fd(nll_oracle, hp, i, h=1e-4) for i in range(2)])
+    np.testing.assert_allclose(got, want, rtol=2e-2, atol=2e-2 * np.abs(want).max())
