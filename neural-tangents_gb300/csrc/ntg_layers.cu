@@ -1351,24 +1351,16 @@ __device__ __forceinline__ void skew_vjp_body(
   }
 }
 
-#define NTG_SKEW_VJP_ARGS                                                                \
-  const float* __restrict__ pre_q, const float* __restrict__ pre_t,                        \
-      const float* __restrict__ g_q, const float* __restrict__ g_t, float* __restrict__ gin_q, \
-      float* __restrict__ gin_t, int64_t batch, int64_t n2, int A, float w2, ntg_act_t act,  \
-      ntg_var_t var1, ntg_var_t var2, float* __restrict__ gvar1, float* __restrict__ gvar2
-
-// The unpooled form keeps the compiler's register choice (79, three CTAs per SM by shared
-// memory); the pooled form's smaller ring fits four CTAs per SM at 64 registers.
-__global__ void __launch_bounds__(kThreads) conv3_skew_vjp_kernel(NTG_SKEW_VJP_ARGS) {
-  skew_vjp_body<false>(pre_q, pre_t, g_q, g_t, gin_q, gin_t, batch, n2, A, w2, act, var1, var2,
-                       gvar1, gvar2);
+template <bool POOLED>
+__global__ void __launch_bounds__(kThreads)
+    conv3_skew_vjp_kernel(const float* __restrict__ pre_q, const float* __restrict__ pre_t,
+                          const float* __restrict__ g_q, const float* __restrict__ g_t,
+                          float* __restrict__ gin_q, float* __restrict__ gin_t, int64_t batch,
+                          int64_t n2, int A, float w2, ntg_act_t act, ntg_var_t var1,
+                          ntg_var_t var2, float* __restrict__ gvar1, float* __restrict__ gvar2) {
+  skew_vjp_body<POOLED>(pre_q, pre_t, g_q, g_t, gin_q, gin_t, batch, n2, A, w2, act, var1, var2,
+                        gvar1, gvar2);
 }
-
-__global__ void __launch_bounds__(kThreads, 4) conv3_skew_vjp_pooled_kernel(NTG_SKEW_VJP_ARGS) {
-  skew_vjp_body<true>(pre_q, pre_t, g_q, g_t, gin_q, gin_t, batch, n2, A, w2, act, var1, var2,
-                      gvar1, gvar2);
-}
-#undef NTG_SKEW_VJP_ARGS
 
 // ---------------------------------------------------------------------------
 // Diagonal-spatial conv rule: [B, A, C] box filter (linear.py:3381-3437).
@@ -2019,12 +2011,12 @@ cudaError_t launch_skew_vjp(cudaStream_t s, int64_t blocks, const float* pre_q, 
                             int64_t batch, int64_t n2, int64_t a, float w2, ntg_act_t act,
                             ntg_var_t var1, ntg_var_t var2, float* gvar1, float* gvar2) {
   constexpr size_t sm = skew_vjp_smem_bytes<POOLED>();
-  auto kernel = POOLED ? conv3_skew_vjp_pooled_kernel : conv3_skew_vjp_kernel;
-  cudaError_t e =
-      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaError_t e = cudaFuncSetAttribute(conv3_skew_vjp_kernel<POOLED>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e == cudaSuccess)
-    kernel<<<(unsigned)blocks, kThreads, sm, s>>>(pre_q, pre_t, g_q, g_t, gin_q, gin_t, batch,
-                                                   n2, (int)a, w2, act, var1, var2, gvar1, gvar2);
+    conv3_skew_vjp_kernel<POOLED><<<(unsigned)blocks, kThreads, sm, s>>>(
+        pre_q, pre_t, g_q, g_t, gin_q, gin_t, batch, n2, (int)a, w2, act, var1, var2, gvar1,
+        gvar2);
   return e;
 }
 
