@@ -1488,7 +1488,7 @@ __global__ void __launch_bounds__(kThreads)
       jn -= P;
       ++bn;
     }
-    if (has_act && ch + gridDim.x < chunks) stage(bn, jn, cur ^ 1);  // read next round
+    if (has_act && ch + gridDim.x < chunks) stage(bn, jn, cur ^ 1);  // read by the next chunk
     const int64_t e = b * M + (int64_t)j * 1024 + 4 * tid;
     b = bn;
     j = jn;
