@@ -346,14 +346,6 @@ __global__ void affine_hyper_kernel(const float* __restrict__ q, const float* __
   }
 }
 
-__device__ __forceinline__ bool wrap_idx(int64_t& i, int64_t n, int circular) {
-  if (i >= 0 && i < n) return true;
-  if (!circular) return false;
-  i %= n;
-  if (i < 0) i += n;
-  return true;
-}
-
 // Outputs i in [0, no) whose window offset `off` lands on input x:
 // i*s + off - p == x (zero padding) or == x mod n (circular). At most 3.
 __device__ __forceinline__ int candidates(int64_t x, int off, int s, int p, int64_t n, int64_t no,
@@ -596,76 +588,66 @@ __global__ void input_fs_t_kernel(const float* __restrict__ g, const float* __re
   }
 }
 
-// Both image cotangents of the full-spatial input covariance in one pass over
-// its cotangent G, for 32 x 32 planes and K <= 4 channels:
+// Image cotangents of the full-spatial input covariance, 32 x 32 planes and
+// K <= 4 channels (requirements.py:542-553, differentiated):
 //   gx1[i1, h, w, k]   += sum_{i2, h', w'} G[i1, i2, h, h', w, w'] x2[i2, h', w', k] / K
 //   gx2[i2, h', w', k] += sum_{i1, h, w}   G[i1, i2, h, h', w, w'] x1[i1, h, w, k] / K
-// One CTA per (i1, h) streams its planes (i2, h') once, two planes of G
-// prefetched in registers; the gx1 sums stay in registers until the end. The
-// gx2 sums of a plane are reduced over a warp's rows by shuffles, written per
-// warp to shared memory and summed over the warps by 32 K threads, which add
-// them to gx2 with one global atomic each. Plane coordinates advance
-// incrementally (no divisions in the loop). n2 == 0: per-sample covariances
-// G[i, h, h', w, w'] of x1 with itself (x2 = x1, gx2 = gx1).
 constexpr int kIfC = 32;
-
-struct PlaneIt {  // (i2, h') of a plane in the order the CTA streams them
-  int64_t i2;
-  int hq;
-};
 
 __device__ int g_bwd_error = 0;
 
 constexpr int kIfRing = 4;
 
-// CTA (i1, h) streams the G planes (i2, h') of its row and the matching rows
-// x2[i2, h', :, :] through a shared-memory ring filled by bulk copies (one
-// thread issues, completion on an mbarrier, every wait bounded), kIfRing planes
-// ahead of the compute. Planes go in cyclic order from a per-CTA start, so that
-// concurrent CTAs add into different gx2 rows.
-template <int K>
+// Two-pass form of the input-covariance adjoint, each pass a pure stream over G
+// with per-thread accumulators and one owner per output row (no atomics):
+//   rows (COLS = false): CTA (i1, h) streams the planes (i2, h') of its rows,
+//     gx1[i1, h, w, k] += sum_{i2, h', w'} G[i1, i2, h, h', w, w'] x2[i2, h', w', k] / K;
+//   cols (COLS = true): CTA (i2, h') streams the planes (i1, h) of its columns,
+//     gx2[i2, h', w', k] += sum_{i1, h, w} G[i1, i2, h, h', w, w'] x1[i1, h, w, k] / K.
+// With n2 == 0 (the per-sample covariances of x1) both passes run over G[i, h, h']
+// and add into gx1. G planes and the matching image rows come through a bulk-copy
+// ring (one thread issues, completion on an mbarrier, every wait bounded).
+template <int K, bool COLS>
 __global__ void __launch_bounds__(256)
-    input_fs_t2_kernel(const float* __restrict__ g, const float* __restrict__ x1,
-                       const float* __restrict__ x2, float* __restrict__ gx1,
-                       float* __restrict__ gx2, int64_t n1, int64_t n2, int A, float inv_k) {
+    input_fs_pass_kernel(const float* __restrict__ g, const float* __restrict__ x1,
+                         const float* __restrict__ x2, float* __restrict__ gx, int64_t n1,
+                         int64_t n2, int A, float inv_k) {
   constexpr int C = kIfC;
-  constexpr int XF = C * K;  // floats of a row x[i, h, :, :] (multiple of 32: 16-byte copies)
+  constexpr int XF = C * K;
   __shared__ __align__(128) float gs[kIfRing][C * C];
   __shared__ __align__(16) float xs[kIfRing][XF];
-  __shared__ __align__(16) float cw[2][8][C * 4];  // per-warp gx2 sums of a plane [w'][k]
+  __shared__ float red[8][C * K];
   __shared__ __align__(8) uint64_t bars[kIfRing];
   __shared__ int s_err;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t i1 = blockIdx.x / A;
-  const int h = (int)(blockIdx.x % A);
-  if (i1 >= n1) return;
   const bool self = n2 == 0;
-  const float* xo = self ? x1 : x2;
-  float* go = self ? gx1 : gx2;
-  const int64_t np = (self ? 1 : n2) * A;
+  const int64_t nown = COLS ? (self ? n1 : n2) : n1;  // images owning the output rows
+  const int64_t own = blockIdx.x / A;                 // i1 (rows) or i2 (cols)
+  const int hown = (int)(blockIdx.x % A);             // h (rows) or h' (cols)
+  if (own >= nown) return;
+  const int64_t nother = self ? 1 : (COLS ? n1 : n2);
+  const int64_t np = nother * A;
+  // rows read x2 rows (x1's own rows when self); cols read x1 rows
+  const float* xo = COLS ? x1 : (self ? x1 : x2);
   const int w = tid >> 3, wq0 = (tid & 7) * 4;
-  float xr[K], acc[K];
+  float acc[4][K];
 #pragma unroll
-  for (int k = 0; k < K; ++k) {
-    xr[k] = __ldg(x1 + ((i1 * A + h) * C + w) * K + k);
-    acc[k] = 0.f;
-  }
-  auto advance = [&](PlaneIt& it) {
-    if (++it.hq == A) {
-      it.hq = 0;
-      if (!self && ++it.i2 == n2) it.i2 = 0;
-    }
-  };
-  const int64_t s0 = ((int64_t)blockIdx.x * 7919) % np;
-  PlaneIt cur_it{self ? i1 : s0 / A, (int)(s0 % A)};
-  PlaneIt iss_it = cur_it;  // next plane thread 0 issues
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc[j][k] = 0.f;
   int64_t issued = 0;
   auto issue = [&]() {
     const int sl = (int)(issued % kIfRing);
+    const int64_t o = self ? own : issued / A;  // the other image
+    const int hq = (int)(issued % A);           // the other position row
     const uint32_t bar = smem_addr(&bars[sl]);
-    const int64_t b = self ? i1 : i1 * n2 + iss_it.i2;
-    const float* gsrc = g + ((b * A + h) * A + iss_it.hq) * (int64_t)(C * C);
-    const float* xsrc = xo + ((iss_it.i2 * A + iss_it.hq) * C) * K;
+    int64_t plane;
+    if (!COLS)
+      plane = self ? (own * A + hown) * A + hq : ((own * n2 + o) * A + hown) * A + hq;
+    else
+      plane = self ? (own * A + hq) * A + hown : ((o * n2 + own) * A + hq) * A + hown;
+    const float* gsrc = g + plane * (int64_t)(C * C);
+    const float* xsrc = xo + ((o * A + hq) * C) * K;
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar),
                  "r"((uint32_t)((C * C + XF) * sizeof(float)))
                  : "memory");
@@ -677,7 +659,6 @@ __global__ void __launch_bounds__(256)
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
         ::"r"(smem_addr(&xs[sl][0])), "l"(xsrc), "r"((uint32_t)(XF * sizeof(float))), "r"(bar)
         : "memory");
-    advance(iss_it);
     ++issued;
   };
   if (tid == 0) {
@@ -690,64 +671,70 @@ __global__ void __launch_bounds__(256)
   if (tid == 0)
     while (issued < kIfRing && issued < np) issue();
   for (int64_t p = 0; p < np; ++p) {
-    const int cur = (int)(p & 1);
     const int sl = (int)(p % kIfRing);
     if (!s_err && !bar_wait(smem_addr(&bars[sl]), (uint32_t)((p / kIfRing) & 1))) s_err = 1;
     const float4 G = *reinterpret_cast<const float4*>(&gs[sl][w * C + wq0]);
     const float ga[4] = {G.x, G.y, G.z, G.w};
-    float cp[4][4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (k < K) {
-          const float xv = xs[sl][(wq0 + j) * K + k];
-          acc[k] = fmaf(ga[j], xv, acc[k]);
-          cp[j][k] = ga[j] * xr[k];
-        } else {
-          cp[j][k] = 0.f;
-        }
-      }
-    }
-    // sums over the 4 rows w of this warp (lanes 8 apart), then one row per warp
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int k = 0; k < K; ++k) {
-        cp[j][k] += __shfl_xor_sync(0xffffffffu, cp[j][k], 8);
-        cp[j][k] += __shfl_xor_sync(0xffffffffu, cp[j][k], 16);
-      }
-    if (lane < 8) {
+    if (!COLS) {
+      // acc[0][k]: sum over the row's columns w' of G[w, w'] x[w', k]
 #pragma unroll
       for (int j = 0; j < 4; ++j)
-        *reinterpret_cast<float4*>(&cw[cur][warp][(wq0 + j) * 4]) =
-            make_float4(cp[j][0], cp[j][1], cp[j][2], cp[j][3]);
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[0][k] = fmaf(ga[j], xs[sl][(wq0 + j) * K + k], acc[0][k]);
+    } else {
+      // acc[j][k]: column w' = wq0 + j, summed over rows w of G[w, w'] x[w, k]
+      float xv[K];
+#pragma unroll
+      for (int k = 0; k < K; ++k) xv[k] = xs[sl][w * K + k];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int k = 0; k < K; ++k) acc[j][k] = fmaf(ga[j], xv[k], acc[j][k]);
     }
     __syncthreads();
     // every thread has read slot sl: it takes plane p + kIfRing
     if (tid == 0 && !s_err && issued < np) issue();
+  }
+  float* out;
+  if (!COLS) {
+    // the 8 threads of a row w hold the row's partial sums over disjoint columns
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      acc[0][k] += __shfl_xor_sync(0xffffffffu, acc[0][k], 1);
+      acc[0][k] += __shfl_xor_sync(0xffffffffu, acc[0][k], 2);
+      acc[0][k] += __shfl_xor_sync(0xffffffffu, acc[0][k], 4);
+    }
+    out = gx + ((own * A + hown) * C + w) * K;
+    if ((lane & 7) == 0) {
+#pragma unroll
+      for (int k = 0; k < K; ++k) out[k] += acc[0][k] * inv_k;
+    }
+  } else {
+    // sums over the 4 rows of the warp (lanes 8 apart), then over the 8 warps
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        acc[j][k] += __shfl_xor_sync(0xffffffffu, acc[j][k], 8);
+        acc[j][k] += __shfl_xor_sync(0xffffffffu, acc[j][k], 16);
+      }
+    if (lane < 8) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int k = 0; k < K; ++k) red[warp][(wq0 + j) * K + k] = acc[j][k];
+    }
+    __syncthreads();
+    out = gx + ((own * A + hown) * C) * K;
     if (tid < C * K) {
-      const int wq = tid / K, k = tid - (tid / K) * K;
       float v = 0.f;
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v += cw[cur][u][wq * 4 + k];
-      atomicAdd(go + ((cur_it.i2 * A + cur_it.hq) * C + wq) * K + k, v * inv_k);
+      for (int u = 0; u < 8; ++u) v += red[u][tid];
+      out[tid] += v * inv_k;
     }
-    advance(cur_it);
-  }
-#pragma unroll
-  for (int k = 0; k < K; ++k) {
-    acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], 1);
-    acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], 2);
-    acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], 4);
-  }
-  if ((lane & 7) == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) atomicAdd(gx1 + ((i1 * A + h) * C + w) * K + k, acc[k] * inv_k);
   }
   if (tid == 0 && s_err) {
     atomicExch(&g_bwd_error, NTG_ERR_WAIT_TIMEOUT);
-    // let every issued copy land (bounded) before the CTA's shared memory is released
     for (int64_t p = issued > kIfRing ? issued - kIfRing : 0; p < issued; ++p)
       bar_wait(smem_addr(&bars[p % kIfRing]), (uint32_t)((p / kIfRing) & 1));
   }
@@ -1013,15 +1000,32 @@ extern "C" int ntg_input_fs_bwd2(void* stream, const float* g, const float* x1,
   const bool fast = c == kIfC && k <= 4 && a <= (1 << 16) && n1 * a < (1ll << 31) &&
                     ((reinterpret_cast<uintptr_t>(g) | reinterpret_cast<uintptr_t>(x1) |
                       reinterpret_cast<uintptr_t>(x2)) & 15) == 0;
-  if (fast) {
-    const unsigned grid = (unsigned)(n1 * a);
+  if (fast && n2 * a < (1ll << 31)) {
     const float inv_k = 1.f / (float)k;
+    // rows into gx1, then columns into gx2 (gx1 for the per-sample covariances, or when
+    // x2 is x1); two launches on one stream, so a shared gx is never written concurrently
+    const unsigned grid_r = (unsigned)(n1 * a);
+    const unsigned grid_c = (unsigned)((n2 > 0 ? n2 : n1) * a);
+    float* gc = n2 > 0 ? gx2 : gx1;
     switch (k) {
-      case 1: input_fs_t2_kernel<1><<<grid, 256, 0, s>>>(g, x1, x2, gx1, gx2, n1, n2, (int)a, inv_k); break;
-      case 2: input_fs_t2_kernel<2><<<grid, 256, 0, s>>>(g, x1, x2, gx1, gx2, n1, n2, (int)a, inv_k); break;
-      case 3: input_fs_t2_kernel<3><<<grid, 256, 0, s>>>(g, x1, x2, gx1, gx2, n1, n2, (int)a, inv_k); break;
-      default: input_fs_t2_kernel<4><<<grid, 256, 0, s>>>(g, x1, x2, gx1, gx2, n1, n2, (int)a, inv_k); break;
+      case 1:
+        input_fs_pass_kernel<1, false><<<grid_r, 256, 0, s>>>(g, x1, x2, gx1, n1, n2, (int)a, inv_k);
+        input_fs_pass_kernel<1, true><<<grid_c, 256, 0, s>>>(g, x1, x2, gc, n1, n2, (int)a, inv_k);
+        break;
+      case 2:
+        input_fs_pass_kernel<2, false><<<grid_r, 256, 0, s>>>(g, x1, x2, gx1, n1, n2, (int)a, inv_k);
+        input_fs_pass_kernel<2, true><<<grid_c, 256, 0, s>>>(g, x1, x2, gc, n1, n2, (int)a, inv_k);
+        break;
+      case 3:
+        input_fs_pass_kernel<3, false><<<grid_r, 256, 0, s>>>(g, x1, x2, gx1, n1, n2, (int)a, inv_k);
+        input_fs_pass_kernel<3, true><<<grid_c, 256, 0, s>>>(g, x1, x2, gc, n1, n2, (int)a, inv_k);
+        break;
+      default:
+        input_fs_pass_kernel<4, false><<<grid_r, 256, 0, s>>>(g, x1, x2, gx1, n1, n2, (int)a, inv_k);
+        input_fs_pass_kernel<4, true><<<grid_c, 256, 0, s>>>(g, x1, x2, gc, n1, n2, (int)a, inv_k);
+        break;
     }
+    note_launch();
     note_launch();
     return check_launch("ntg_input_fs_bwd2");
   }
