@@ -358,3 +358,24 @@ def test_more_dual_activations_vs_oracle(nt, act, cifar_like):
     k = kf.apply_kernel(k, ctx)
     assert rel_err(got[0], cpu(k.nngp)) < 2e-6
     assert rel_err(got[1], cpu(k.ntk)) < 2e-6
+
+
+def test_argument_swap_symmetry(nt, cifar_like):
+    """elementwise_test.py:639-732 (argument-swap symmetry): K(x2, x1) is K(x1, x2) transposed,
+    on the fused whole-network kernel and on the layer-by-layer kernels (an Erf network)."""
+    x1, x2 = cifar_like
+    s = nt.stax
+    kf = s.serial(*myrtle(s, 5))[2]
+    a = kf(x1, x2, ('nngp', 'ntk'))
+    b = kf(x2, x1, ('nngp', 'ntk'))
+    for u, v in zip(a, b):
+        np.testing.assert_allclose(cpu(u), cpu(v).T, rtol=2e-6)
+    ke = s.serial(s.Conv(2, (3, 3), padding='SAME', W_std=1.3, b_std=0.1), s.Erf(),
+                  s.Conv(2, (2, 2), padding='VALID', W_std=1.2), s.Relu(), s.GlobalAvgPool(),
+                  s.Dense(1, 1.1, 0.))[2]
+    rng = np.random.default_rng(9)
+    y1, y2 = rng.standard_normal((3, 7, 6, 2)), rng.standard_normal((2, 7, 6, 2))
+    a = ke(y1, y2, ('nngp', 'ntk'))
+    b = ke(y2, y1, ('nngp', 'ntk'))
+    for u, v in zip(a, b):
+        np.testing.assert_allclose(cpu(u), cpu(v).T, rtol=2e-6)

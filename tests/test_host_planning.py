@@ -111,3 +111,17 @@ def test_fused_entries_check_arguments_before_any_launch():
     assert rc == 1 and b'go together' in lib.ntg_last_error()
     rc = lib.ntg_input_ds(None, fake, None, 2, 3, 10, 3, fake)
     assert rc == 1 and b'go together' in lib.ntg_last_error()
+
+
+def test_diagonal_spatial_request_rejected_for_pooled_readout():
+    """stax_test.py:636-687: asking for diagonal_spatial=True from a network whose pooling needs
+    the full spatial kernel raises ValueError before any kernel runs."""
+    from nt_gb300 import stax
+    kf = stax.serial(stax.Conv(1, (3, 3), padding='SAME'), stax.Relu(),
+                     stax.AvgPool((2, 2), (2, 2)), stax.Flatten(), stax.Dense(1))[2]
+    assert not bool(kf.diagonal)
+    with pytest.raises(ValueError, match='diagonal_spatial'):
+        kf(torch.zeros((2, 8, 8, 3)), None, 'nngp', diagonal_spatial=True)
+    gap = stax.serial(stax.Conv(1, (3, 3), padding='SAME'), stax.Relu(), stax.GlobalAvgPool())[2]
+    with pytest.raises(ValueError, match='diagonal_spatial'):
+        gap(torch.zeros((2, 8, 8, 3)), None, 'nngp', diagonal_spatial=True)
