@@ -29,6 +29,14 @@ def tile_grid(n1: int, n2: int, b: int):
     return [(r0, rn, c0, cn) for r0, rn in _tiles(n1, b) for c0, cn in _tiles(n2, b)]
 
 
+def rank_rows(n: int, b: int, world_size: int, rank: int):
+    """The contiguous rows [start, stop) of an n-row kernel that one rank computes when whole
+    tile rows (b rows each, the last one ragged) are split evenly across ranks."""
+    t = (n + b - 1) // b
+    lo, hi = rank * t // world_size, (rank + 1) * t // world_size
+    return min(lo * b, n), min(hi * b, n)
+
+
 def rank_tiles(tiles, world_size: int, rank: int, steps=None):
     """Tiles of one rank when the grid is sharded across ranks (tile k -> rank k % world_size,
     batching.py:505-644 shards x1 rows the same way). Every tile of the grid is independent, so

@@ -61,3 +61,15 @@ def test_rank_tiles_wraps_for_steps():
     assert rank_tiles(tiles, 4, 1, steps=5) == [tiles[1], tiles[5], tiles[0], tiles[4], tiles[8]]
     assert sorted(rank_tiles(tiles, 4, 0) + rank_tiles(tiles, 4, 1) + rank_tiles(tiles, 4, 2) +
                   rank_tiles(tiles, 4, 3)) == sorted(tiles)
+
+
+@pytest.mark.parametrize('n,b,world', [(2000, 100, 2), (2000, 100, 8), (250, 40, 4), (7, 100, 3)])
+def test_rank_rows_cover_every_row_once(n, b, world):
+    """The end-to-end job under torchrun: each rank's contiguous block of tile rows."""
+    from nt_gb300.batching import rank_rows
+    rows = [rank_rows(n, b, world, r) for r in range(world)]
+    assert rows[0][0] == 0 and rows[-1][1] == n
+    for (a0, a1), (b0, b1) in zip(rows, rows[1:]):
+        assert a1 == b0 and a0 <= a1
+    for a0, a1 in rows:
+        assert a0 % b == 0 or a0 == n
