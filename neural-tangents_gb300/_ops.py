@@ -122,16 +122,6 @@ def conv_fs(q, t, batch, n2, a, c, fh, fw, sh, sw, ph, pw, ao, co, circular, aff
     return out_q, out_t
 
 
-def conv_input_fs(x1, x2, aff, act, var1, var2):
-    n1, a, c, k = x1.shape
-    n2 = x2.shape[0]
-    out_q = torch.empty((n1, n2, a, a, c, c), device=x1.device, dtype=torch.float32)
-    out_t = torch.empty_like(out_q)
-    L.call('ntg_conv_input_fs', L.stream(), L.ptr(x1), L.ptr(x2), n1, n2, a, c, k, L.ptr(out_q),
-           L.ptr(out_t), aff, act, var1, var2)
-    return out_q, out_t
-
-
 def conv_ds(q, t, batch, a, c, fh, fw, sh, sw, ph, pw, ao, co, circular, aff, want_t, lead,
             has_c):
     shape = lead + ((ao, co) if has_c else (ao,))
