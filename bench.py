@@ -9,8 +9,10 @@ Because K(x, x) is symmetric, the job is the per-sample chains of the 2000
 inputs plus the upper triangle of the 20 x 20 tile grid: 20 diagonal tiles
 (pairs i <= j) and 190 off-diagonal tiles whose results are also written at
 the mirrored position, 210 tiles in all. Step k is tile k of the triangle plus
-1/210 of the per-sample chains; each step is credited 2000^2 / 210 entries, so
-`value` is the throughput of the whole job. Steps are spread evenly over the
+1/210 of the per-sample chains, credited with the output entries its tile
+produces (2 x 100^2 for an off-diagonal tile, 100^2 for a diagonal one; the 210
+credits add up to 2000^2), so `value` estimates the throughput of the whole job
+from any sample of steps. Steps are spread evenly over the
 triangle; under torchrun rank r takes tiles r, r+N, ... (weak scaling).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
@@ -51,6 +53,13 @@ FLOPS_PER_ELEM_LAYER = 4 * 2 + 4 * 2 + 4 + 40
 WARP_INSTR_PER_PAIR = 4.87e6
 # Instruction issue peak: 152 SMs x 4 warp schedulers, one instruction per cycle each.
 ISSUE_SLOTS_PER_CYCLE = 152 * 4
+
+
+def tile_entries(tile) -> int:
+    """Output entries of tile (r, c) of the upper triangle of the TILE x TILE grid: an
+    off-diagonal tile is written at (r, c) and mirrored at (c, r)."""
+    r, c = tile
+    return TILE * TILE * (1 if r == c else 2)
 
 
 def myrtle5(m):
@@ -152,7 +161,8 @@ def run_gpu(args):
     # per-sample chains of the 2000 inputs and the upper triangle of the 20 x 20 tile grid
     # (20 diagonal tiles with only i <= j evaluated, 190 off-diagonal tiles written at (i, j)
     # and (j, i)). Step k is tile k of the triangle plus the per-sample chains of samples
-    # [k N / 210, (k + 1) N / 210): the 210 steps are the whole job, each credited N^2 / 210
+    # [k N / 210, (k + 1) N / 210): the 210 steps are the whole job, each credited with its
+    # tile's output entries (tile_entries; N^2 over the 210 steps)
     # entries. Steps are spread evenly over a rank's share of the tiles (tile k -> rank k % N).
     nt_ = N_SAMPLES // TILE
     tiles = [(r, c) for r in range(nt_) for c in range(r, nt_)]
@@ -221,9 +231,11 @@ def run_gpu(args):
     if ws > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     ms_max = float(t.item())
-    per_step = N_SAMPLES * N_SAMPLES / njob
-    entries = per_step * args.steps * ws
-    value = entries / (ms_max / 1e3)
+    e = torch.tensor([float(sum(tile_entries(tiles[mine[args.warmup + s]])
+                                for s in range(args.steps)))], device=dev)
+    if ws > 1:
+        dist.all_reduce(e)
+    value = float(e.item()) / (ms_max / 1e3)
 
     # Dominant kernel alone: the fused chain launch of one off-diagonal tile (10 000 pairs
     # evaluated), CUDA events on the launching stream, L2 flushed before each launch.
@@ -265,7 +277,8 @@ def run_gpu(args):
         b.record(stream)
         torch.cuda.synchronize()
         em.append(a.elapsed_time(b))
-    mixed_value = per_step / (statistics.mean(em) / 1e3)
+    mixed_value = (sum(tile_entries(tiles[mine[args.warmup + s]]) for s in range(len(em))) /
+                   (sum(em) / 1e3))
 
     # End to end through the public API: the whole job nt.batch(kf, 100)(x, None) from pinned
     # host inputs, nngp and ntk read back to the host.
@@ -321,7 +334,8 @@ def run_gpu(args):
                                'nt.batch(batch_size=100); the job is the per-sample chains and '
                                'the upper triangle of the 20x20 tile grid (210 tiles, '
                                'off-diagonal tiles mirrored); step = one tile of the triangle '
-                               'plus 1/210 of the per-sample chains, credited 2000^2/210 entries',
+                               'plus 1/210 of the per-sample chains, credited with the output '
+                               'entries of its tile (2x100^2 off the diagonal, 100^2 on it)',
                    'n_samples': N_SAMPLES, 'batch_size': TILE, 'input': list(IMG),
                    'precision': 'fp32 (plain)', 'l2': 'flushed before every step (256 MiB write)',
                    'path': 'fused chain kernel (ntg_chain_fwd_sym) + per-sample chains'},

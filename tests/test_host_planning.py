@@ -125,3 +125,13 @@ def test_diagonal_spatial_request_rejected_for_pooled_readout():
     gap = stax.serial(stax.Conv(1, (3, 3), padding='SAME'), stax.Relu(), stax.GlobalAvgPool())[2]
     with pytest.raises(ValueError, match='diagonal_spatial'):
         gap(torch.zeros((2, 8, 8, 3)), None, 'nngp', diagonal_spatial=True)
+
+
+def test_bench_step_credits_add_up_to_the_job():
+    """bench.py credits each step of the symmetric job with the entries its tile produces; the
+    210 tiles of the 2000 x 2000 triangle add up to the whole kernel."""
+    import bench
+    n = bench.N_SAMPLES // bench.TILE
+    tiles = [(r, c) for r in range(n) for c in range(r, n)]
+    assert len(tiles) == 210
+    assert sum(bench.tile_entries(t) for t in tiles) == bench.N_SAMPLES ** 2
