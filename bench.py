@@ -162,8 +162,8 @@ def run_gpu(args):
     # (20 diagonal tiles with only i <= j evaluated, 190 off-diagonal tiles written at (i, j)
     # and (j, i)). Step k is tile k of the triangle plus the per-sample chains of samples
     # [k N / 210, (k + 1) N / 210): the 210 steps are the whole job, each credited with its
-    # tile's output entries (tile_entries; N^2 over the 210 steps)
-    # entries. Steps are spread evenly over a rank's share of the tiles (tile k -> rank k % N).
+    # tile's output entries (tile_entries; N^2 over the 210 steps). Steps are spread evenly
+    # over a rank's share of the tiles (tile k -> rank k % N).
     nt_ = N_SAMPLES // TILE
     tiles = [(r, c) for r in range(nt_) for c in range(r, nt_)]
     njob = len(tiles)
