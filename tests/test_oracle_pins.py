@@ -315,3 +315,25 @@ def test_dual_activations_match_gaussian_expectations(case):
                          (c2[0, 0], phi(np.sqrt(v2) * z[:, 1]) ** 2)):
         mean, err = samples.mean(), samples.std() / np.sqrt(n)
         assert abs(got - mean) < 6 * err + 1e-12, (got, mean, err)
+
+
+@pytest.mark.parametrize('act', ['relu', 'erf', 'gelu', 'sin', 'rbf'])
+def test_diagonal_spatial_is_the_diagonal_of_the_full_kernel(act):
+    """requirements_test.py:55-137 (diagonal_batch / diagonal_spatial consistency): for a CNN
+    without pooling the diagonal-spatial kernels equal the (h, h, w, w) entries of the
+    full-spatial ones, nngp, ntk and the per-sample covariances alike."""
+    mk = {'relu': lambda: o.Relu(), 'erf': lambda: o.Erf(), 'gelu': lambda: o.Gelu(),
+          'sin': lambda: o.Sin(1.1, 0.9, 0.3), 'rbf': lambda: o.Rbf(0.4)}[act]
+    kf = o.serial(o.Conv(2, (3, 3), padding='SAME', W_std=1.3, b_std=0.2), mk(),
+                  o.Conv(2, (2, 3), strides=(1, 2), padding='VALID', W_std=1.1, b_std=0.1), mk())
+    rng = np.random.default_rng(12)
+    x1, x2 = rng.standard_normal((2, 6, 7, 3)), rng.standard_normal((3, 6, 7, 3))
+    full = kf(x1, x2, None, diagonal_spatial=False)
+    diag = kf(x1, x2, None, diagonal_spatial=True)
+    assert not full.is_reversed and full.nngp.ndim == 6 and diag.nngp.ndim == 4
+    pick2 = lambda k: np.einsum('abhhww->abhw', k)
+    pick1 = lambda k: np.einsum('ahhww->ahw', k)
+    np.testing.assert_allclose(diag.nngp, pick2(full.nngp), rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(diag.ntk, pick2(full.ntk), rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(diag.cov1, pick1(full.cov1), rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(diag.cov2, pick1(full.cov2), rtol=1e-12, atol=1e-12)
