@@ -135,3 +135,13 @@ def test_bench_step_credits_add_up_to_the_job():
     tiles = [(r, c) for r in range(n) for c in range(r, n)]
     assert len(tiles) == 210
     assert sum(bench.tile_entries(t) for t in tiles) == bench.N_SAMPLES ** 2
+
+
+@pytest.mark.skipif(torch.cuda.is_available(), reason='checks the behaviour without a GPU')
+def test_no_cpu_fallback():
+    """Without a CUDA device the product path raises instead of computing on the host."""
+    import numpy as np
+    from nt_gb300 import stax
+    kf = stax.serial(stax.Dense(4, 1.5, 0.05), stax.Relu(), stax.Dense(1))[2]
+    with pytest.raises(RuntimeError, match='no CPU fallback'):
+        kf(np.ones((2, 3), np.float32), None, 'nngp')
