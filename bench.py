@@ -306,6 +306,29 @@ def run_gpu(args):
     h2d = ws * N_SAMPLES * int(np.prod(IMG)) * 4
     d2h = 2 * N_SAMPLES * N_SAMPLES * 4
 
+    # Parity sample of the benchmarked job: PARITY_PAIRS seeded entries of the 2000 x 2000
+    # result (some on the diagonal, where the correlation is 1), fp32 as the e2e call returned
+    # them, mixed from the same entries evaluated with precision='mixed'; the float64 oracle
+    # values are computed in the CPU leg below.
+    checks = []
+    if ws == 1:
+        pairs = parity_pairs(N_SAMPLES, PARITY_PAIRS, seed=7)
+        ii = [i for i, _ in pairs]
+        jj = [j for _, j in pairs]
+        km = kf(xd[ii], xd[jj], ('nngp', 'ntk'), precision='mixed')
+        k = torch.arange(len(pairs))
+        checks.append({
+            'name': 'myrtle5_2000', 'net': 'myrtle5', 'x': x, 'pairs': pairs,
+            'got': {'fp32': (q[ii, jj].numpy(), tt[ii, jj].numpy()),
+                    'mixed': (km.nngp[k, k].cpu().numpy(), km.ntk[k, k].cpu().numpy())}})
+    full = {}
+    if ws == 1 and args.full_configs:
+        full['config1_fcn'], chk = config1_timing(torch, nt, dev)
+        checks.append(chk)
+        full['config5_krr'] = config5_timing(torch, nt, kf)
+        full['config3_myrtle10'], chk = config3_timing(torch, nt, dev)
+        checks.append(chk)
+
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
@@ -363,8 +386,15 @@ def run_gpu(args):
         'gpu_launches': int(launches),
         'clocks': clocks,
     }
+    if full:
+        line['configs'] = full
     if args.cpu_baseline and rank == 0 and ws == 1:
         line['cpu_baseline'] = cpu_baseline(x, args.cpu_seconds)
+        parity = cpu_checks(checks)
+        line['parity'] = parity.pop('myrtle5_2000')
+        for name, res in parity.items():
+            key = {'config1_fcn': 'config1_fcn', 'myrtle10_5000': 'config3_myrtle10'}[name]
+            full[key]['parity'] = res
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:
@@ -401,7 +431,7 @@ def stencil_roofline(torch, O, dev, pairs=256, reps=4):
 
 
 def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=64, precision='fp32', reps=2,
-                   tile=None):
+                   tile=None, xs_in=None, xt_in=None):
     """Kernel-ridge loss of the Myrtle-5 NTK, ||y_t - K_ts (K_ss + 1e-6 tr(K_ss)/n I)^-1 y_s||^2,
     and its gradient with respect to the support set x_s (forward through nt.batch's fused
     grid, backward through its checkpointed tiles and the hand-written adjoints; the solve
@@ -412,11 +442,12 @@ def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=64, precision='fp32', 
     g = torch.Generator(device='cpu').manual_seed(2)
     ys = torch.nn.functional.one_hot(torch.randint(0, 10, (n_s,), generator=g), 10).float().cuda()
     yt = torch.nn.functional.one_hot(torch.randint(0, 10, (n_t,), generator=g), 10).float().cuda()
-    xt = xd[:n_t].contiguous()
+    xt = xd[:n_t].contiguous() if xt_in is None else xt_in
     batched = nt.batch(kf, batch_size=bs, recompute_tile=tile)
     ts, grad = [], None
     for i in range(reps + 1):
-        xs = xd[1000:1000 + n_s].clone().requires_grad_(True)
+        src = xd[1000:1000 + n_s] if xs_in is None else xs_in
+        xs = src.clone().requires_grad_(True)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
         kss = batched(xs, None, 'ntk', precision=precision)
@@ -433,7 +464,7 @@ def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=64, precision='fp32', 
     entries = n_s * n_s + n_t * n_s
     if tile is None:
         tile = nt.tune.recompute_tile(kf, tuple(xs.shape), precision)
-    return {'ms': round(ms, 2), 'entries': entries,
+    return {'ms': round(ms, 2), 'entries': entries, 'loss': float(loss),
             'entries_per_s': round(entries / (ms / 1e3), 1), 'precision': precision,
             'recompute_tile': min(tile, bs),
             'config': f'Myrtle-5 NTK kernel-ridge loss, d/dx_s; x_s [{n_s}], x_t [{n_t}], '
@@ -554,6 +585,231 @@ def gram_roofline(torch, O, dev):
     return {'kernel': 'gram_tc_kernel (+ bf16 split)', 'shape': [4096, 4096, 3072], 'ms': round(ms, 3),
             'tflops_fp32_equivalent': round(flops / (ms / 1e3) / 1e12, 1),
             'tensor_tflops_issued': round(3 * flops / (ms / 1e3) / 1e12, 1), 'unit': 'TFLOP/s'}
+
+
+PARITY_PAIRS = 48
+
+
+def parity_pairs(n, count, seed):
+    """`count` seeded (i, j) entries of an n x n kernel, one in six on the diagonal."""
+    rng = np.random.default_rng(seed)
+    pairs = [(int(i), int(i)) for i in rng.choice(n, count // 6, replace=False)]
+    while len(pairs) < count:
+        i, j = (int(v) for v in rng.integers(0, n, 2))
+        if i != j:
+            pairs.append((i, j))
+    return pairs
+
+
+def fcn_layers(m):
+    return [m.Dense(512, W_std=1.5, b_std=0.05), m.Relu(), m.Dense(512, W_std=1.5, b_std=0.05),
+            m.Relu(), m.Dense(1, W_std=1.5, b_std=0.05)]
+
+
+def fcn_inputs():
+    """Configuration 1: x1, x2 [256, 784] iid N(0, 1) (seeds 0 and 1), rows rescaled to norm
+    sqrt(784); y [256, 10] one-hot labels drawn uniformly (seed 2)."""
+    xs = []
+    for seed in (0, 1):
+        v = np.random.default_rng(seed).standard_normal((256, 784))
+        xs.append((v / np.linalg.norm(v, axis=1, keepdims=True) * math.sqrt(784)).astype(np.float32))
+    y = np.eye(10, dtype=np.float32)[np.random.default_rng(2).integers(0, 10, 256)]
+    return xs[0], xs[1], y
+
+
+def config1_timing(torch, nt, dev, reps=5):
+    """Configuration 1 end to end on the device: kernel_fn(x1, x2, ('nngp', 'ntk')) of the
+    three-layer ReLU FCN, then gradient_descent_mse(k_train_train, y, diag_reg=1e-4) at
+    t = None and t = inf (test predictions on x2 with fx_train_0 = fx_test_0 = 0); the
+    train-train and test-train NTKs come from the same kernel_fn. Times are medians of
+    `reps` calls (CUDA events, inputs resident)."""
+    from nt_gb300 import stax
+    x1h, x2h, yh = fcn_inputs()
+    x1, x2, y = (torch.from_numpy(v).to(dev) for v in (x1h, x2h, yh))
+    kf = stax.serial(*fcn_layers(stax))[2]
+    out = {'config': 'FCN Dense(512,1.5,0.05)-Relu x2-Dense(1); x1, x2 [256, 784] on the sphere '
+                     'of radius sqrt(784) (seeds 0, 1); y one-hot [256, 10] (seed 2); '
+                     'gradient_descent_mse diag_reg=1e-4'}
+    res = {}
+
+    def kernels():
+        res['k12'] = kf(x1, x2, ('nngp', 'ntk'))
+    out['kernel_fn_us'] = round(_timed(torch, kernels, reps) * 1e3, 1)
+    ktt = kf(x1, None, 'ntk')
+    kts = kf(x2, x1, 'ntk')
+    for t, name in ((None, 't_none'), (float('inf'), 't_inf')):
+        def solve():
+            res[name] = nt.predict.gradient_descent_mse(ktt, y, diag_reg=1e-4)(t, 0., 0., kts)
+        out[f'gradient_descent_mse_{name}_us'] = round(_timed(torch, solve, reps) * 1e3, 1)
+
+    def whole():
+        k = kf(x1, None, 'ntk')
+        nt.predict.gradient_descent_mse(k, y, diag_reg=1e-4)(float('inf'), 0., 0.,
+                                                              kf(x2, x1, 'ntk'))
+    out['end_to_end_us'] = round(_timed(torch, whole, reps) * 1e3, 1)
+    check = {'name': 'config1_fcn', 'kind': 'fcn', 'x1': x1h, 'x2': x2h, 'y': yh,
+             'got': {'nngp': res['k12'].nngp.cpu().numpy(), 'ntk': res['k12'].ntk.cpu().numpy(),
+                     'fx_test_t_none': res['t_none'][1].cpu().numpy(),
+                     'fx_test_t_inf': res['t_inf'][1].cpu().numpy()}}
+    return out, check
+
+
+def config5_timing(torch, nt, kf):
+    """Configuration 5 at its stated size: the Myrtle-5 NTK kernel-ridge loss
+    ||y_t - K_ts (K_ss + 1e-6 tr(K_ss)/n I)^-1 y_s||^2 and d loss / d x_s for x_s [200]
+    (iid N(0, 1), seed 5) and x_t [2000] (seed 6), one-hot y_s, y_t over 10 classes
+    (seed 2), in the plain FP32 and the mixed forms (one warm-up evaluation, one timed).
+    Parity of these gradients against float64 finite differences of the oracle is checked
+    at reduced sizes in the test suite (the oracle would need days at this size); here the
+    gradient is checked against a central difference of the loss along a seeded direction
+    through the same forward path."""
+    dev = torch.device('cuda', torch.cuda.current_device())
+    xs = torch.from_numpy(np.random.default_rng(5).standard_normal((200,) + IMG).astype(
+        np.float32)).to(dev)
+    xt = torch.from_numpy(np.random.default_rng(6).standard_normal((2000,) + IMG).astype(
+        np.float32)).to(dev)
+    out = {}
+    grads = {}
+    for prec in ('fp32', 'mixed'):
+        r, g = fwd_bwd_timing(torch, nt, kf, None, n_t=2000, n_s=200, bs=200, precision=prec,
+                              reps=1, xs_in=xs, xt_in=xt)
+        out[prec] = r
+        grads[prec] = g
+    out['mixed']['grad_rel_diff_vs_fp32'] = float(
+        (grads['mixed'] - grads['fp32']).abs().max() / grads['fp32'].abs().max())
+    # directional derivative check of the fp32 gradient: (L(x + h v) - L(x - h v)) / 2h
+    v = torch.from_numpy(np.random.default_rng(8).standard_normal((200,) + IMG).astype(
+        np.float32)).to(dev)
+    h = 1e-2
+    with torch.no_grad():
+        lp = krr_loss(torch, nt, kf, xs + h * v, xt, 'fp32')
+        lm = krr_loss(torch, nt, kf, xs - h * v, xt, 'fp32')
+    fd_dir = (lp - lm) / (2 * h)
+    an = float((grads['fp32'].double() * v.double()).sum())
+    out['fp32']['directional_fd_rel_diff'] = abs(an - fd_dir) / abs(fd_dir)
+    out['config'] = ('Myrtle-5 NTK kernel-ridge loss, d/dx_s; x_s [200] (seed 5), x_t [2000] '
+                     '(seed 6) iid N(0,1); y one-hot over 10 classes (seed 2); '
+                     'nt.batch(batch_size=200) with the autotuned recompute tile')
+    return out
+
+
+def krr_loss(torch, nt, kf, xs, xt, precision, bs=200):
+    """The configuration-5 loss value (float64 on the host) without gradients."""
+    from nt_gb300 import predict
+    n_s, n_t = xs.shape[0], xt.shape[0]
+    g = torch.Generator(device='cpu').manual_seed(2)
+    ys = torch.nn.functional.one_hot(torch.randint(0, 10, (n_s,), generator=g), 10).float().cuda()
+    yt = torch.nn.functional.one_hot(torch.randint(0, 10, (n_t,), generator=g), 10).float().cuda()
+    batched = nt.batch(kf, batch_size=bs)
+    kss = batched(xs, None, 'ntk', precision=precision)
+    kts = batched(xt, xs, 'ntk', precision=precision)
+    alpha = predict.kernel_ridge_solve(kss, ys, diag_reg=1e-6)
+    return float(((yt - predict.matmul(kts, alpha)) ** 2).double().sum())
+
+
+def config3_timing(torch, nt, dev, n=5000, bs=128):
+    """Configuration 3 at its stated size: the Myrtle-10 NTK and NNGP K(x, x) of x
+    [5000, 32, 32, 3] iid N(0, 1) (seed 0) in the mixed form (split-precision first layer,
+    compensated arccos) through nt.batch(batch_size=128) (ragged: 5000 = 39 x 128 + 8, one
+    fused launch over the symmetric grid), then gradient_descent_mse(ntk, y, diag_reg=1e-4)
+    at t = None (FP32 Cholesky of the 5000 x 5000 kernel, FP64 refinement) with y one-hot over
+    10 classes (seed 2), predicting the first 100 training points. Wall-clock seconds, the job
+    once; the kernel entries and the predictions are checked in the CPU leg against the
+    float64 oracle."""
+    from nt_gb300 import stax
+    xh = np.random.default_rng(0).standard_normal((n,) + IMG).astype(np.float32)
+    yh = np.eye(10, dtype=np.float32)[np.random.default_rng(2).integers(0, 10, n)]
+    x, y = torch.from_numpy(xh).to(dev), torch.from_numpy(yh).to(dev)
+    kf = stax.serial(*myrtle10(stax))[2]
+    batched = nt.batch(kf, batch_size=bs)
+    batched(x[:256], None, ('nngp', 'ntk'), precision='mixed')  # warm-up (library, planner)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    k = batched(x, None, ('nngp', 'ntk'), precision='mixed')
+    torch.cuda.synchronize()
+    kernel_s = time.perf_counter() - t0
+    kts = k.ntk[:100].contiguous()
+    t0 = time.perf_counter()
+    pred = nt.predict.gradient_descent_mse(k.ntk, y, diag_reg=1e-4)
+    fx = pred(None, 0., 0., kts)[1]
+    torch.cuda.synchronize()
+    solve_s = time.perf_counter() - t0
+    pairs = parity_pairs(n, 24, seed=9)
+    ii = [i for i, _ in pairs]
+    jj = [j for _, j in pairs]
+    out = {'config': f'Myrtle-10 [3,3,3] + GlobalAvgPool + Dense, K(x, x), x [{n}, 32, 32, 3] '
+                     f'iid N(0,1) (seed 0), mixed form, nt.batch(batch_size={bs}) ragged; then '
+                     'gradient_descent_mse(ntk, one-hot y (seed 2), diag_reg=1e-4) at t=None, '
+                     'predictions for the first 100 training points',
+           'kernel_s': round(kernel_s, 2), 'entries_per_s': round(n * n / kernel_s, 1),
+           'solve_ms': round(solve_s * 1e3, 2)}
+    check = {'name': 'myrtle10_5000', 'net': 'myrtle10', 'x': xh, 'pairs': pairs,
+             'got': {'mixed': (k.nngp[ii, jj].cpu().numpy(), k.ntk[ii, jj].cpu().numpy())},
+             'solve': {'k': k.ntk.cpu().numpy(), 'y': yh, 'fx_test': fx.cpu().numpy()}}
+    return out, check
+
+
+def _oracle_pair(args):
+    """float64 oracle (nngp, ntk) of one pair of images through a Myrtle network."""
+    net, a, b = args
+    sys.path.insert(0, ROOT)
+    from oracle import nt_oracle as o
+    layers = myrtle5(o) if net == 'myrtle5' else myrtle10(o)
+    q, t = o.serial(*layers)(a[None], b[None], ('nngp', 'ntk'))
+    return float(q.reshape(())), float(t.reshape(()))
+
+
+def _rel(got, want):
+    return float(np.max(np.abs(np.asarray(got, np.float64) - want) / np.abs(want)))
+
+
+def cpu_checks(checks, procs=None):
+    """The checker half of the CPU leg: the float64 oracle on the sampled entries (and the
+    FCN and solve configurations) of what the GPU computed; max relative errors per form."""
+    import multiprocessing as mp
+    sys.path.insert(0, ROOT)
+    from oracle import nt_oracle as o
+    procs = procs or os.cpu_count() or 1
+    out = {}
+    tasks, owners = [], []
+    for c in checks:
+        if 'pairs' in c:
+            for (i, j) in c['pairs']:
+                tasks.append((c['net'], c['x'][i], c['x'][j]))
+                owners.append(c['name'])
+    t0 = time.perf_counter()
+    with mp.get_context('spawn').Pool(procs) as pool:
+        vals = pool.map(_oracle_pair, tasks, chunksize=1)
+    pair_s = time.perf_counter() - t0
+    for c in checks:
+        if 'pairs' in c:
+            want = np.array([v for v, name in zip(vals, owners) if name == c['name']])
+            res = {'entries': len(c['pairs']), 'reference': 'float64 oracle (CPU restatement)',
+                   'oracle_s': round(pair_s, 1)}
+            for form, (gq, gt) in c['got'].items():
+                res[f'max_rel_err_{form}'] = max(_rel(gq, want[:, 0]), _rel(gt, want[:, 1]))
+            if 'solve' in c:
+                sv = c['solve']
+                ref = o.gradient_descent_mse(sv['k'], sv['y'], diag_reg=1e-4)(
+                    None, 0., 0., np.asarray(sv['k'][:100], np.float64))[1]
+                res['predictions_max_rel_err_vs_float64_solve'] = float(
+                    np.max(np.abs(sv['fx_test'] - ref)) / np.max(np.abs(ref)))
+            out[c['name']] = res
+        elif c.get('kind') == 'fcn':
+            kf = o.serial(*fcn_layers(o))
+            q, t = kf(c['x1'], c['x2'], ('nngp', 'ntk'))
+            ktt = kf(c['x1'], None, 'ntk')
+            kts = kf(c['x2'], c['x1'], 'ntk')
+            pred = o.gradient_descent_mse(ktt, c['y'], diag_reg=1e-4)
+            g = c['got']
+            res = {'reference': 'float64 oracle (CPU restatement)',
+                   'max_rel_err_nngp': _rel(g['nngp'], q), 'max_rel_err_ntk': _rel(g['ntk'], t)}
+            for name, t_ in (('t_none', None), ('t_inf', np.inf)):
+                want = pred(t_, 0., 0., kts)[1]
+                res[f'fx_test_{name}_max_err_rel_to_max'] = float(
+                    np.max(np.abs(g[f'fx_test_{name}'] - want)) / np.max(np.abs(want)))
+            out[c['name']] = res
+    return out
 
 
 REF_TILE = 4
@@ -685,6 +941,8 @@ def main():
     ap.add_argument('--no-cpu-baseline', dest='cpu_baseline', action='store_false')
     ap.add_argument('--cpu-seconds', type=float, default=15.0)
     ap.add_argument('--ref-step-seconds', type=float, default=5.0)
+    ap.add_argument('--no-full-configs', dest='full_configs', action='store_false',
+                    help='skip configurations 1, 3 and 5 at their stated sizes')
     args = ap.parse_args()
     if args.profile_tile:
         profile_tile(args.profile_tile)

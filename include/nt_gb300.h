@@ -394,15 +394,20 @@ int ntg_nll_grad(void* stream, const float* kinv, const float* alpha, int64_t n,
 
 /* No counterpart in the reference. ntg_chol_solve without a caller workspace,
  * for callers that cannot allocate device memory where they call the solve
- * (a handler inside a captured CUDA graph, a server that reserved all device
- * memory up front). The refinement workspace is a fixed device array of
+ * (an XLA FFI handler, which only receives the buffers XLA allocated for it;
+ * a server that reserved all device memory up front for its own pool). The refinement workspace is a fixed device array of
  * NTG_NOALLOC_SCRATCH_BYTES owned by the library: each GPU that loads the
  * library holds it until the process exits, and the call fails with
  * NTG_ERR_INVALID_ARG when ntg_chol_workspace_bytes(n, m) exceeds it (about
  * n * m <= 87,000). The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture. All calls share the array: calls that overlap on the GPU (other
- * streams, other threads) race and must be serialised by the caller. No
+ * address (cudaGetSymbolAddress) and caches it per device ordinal; make that
+ * first call before any stream capture. The cached address belongs to the
+ * device's primary context (the one the CUDA runtime and PyTorch use): it is
+ * not valid in another context made current through the driver API, nor after
+ * cudaDeviceReset. n must be at most 46340 (the factorisation's limit) and
+ * n * m at most (NTG_NOALLOC_SCRATCH_BYTES - 256) / 12; both are checked before
+ * any size is computed. All calls share the array: calls that overlap on the
+ * GPU (other streams, other threads) race and must be serialised by the caller. No
  * cudaMalloc, cudaFree or allocating library routine is called. Arguments
  * and results are those of ntg_chol_solve. */
 #define NTG_NOALLOC_SCRATCH_BYTES (1u << 20)

@@ -100,6 +100,12 @@ class InputFn(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, gn, gc1, gc2):
+        # the input rule's backward runs last in a network's backward pass
+        with L.boundary('kernel_fn backward'):
+            return InputFn._backward(ctx, gn, gc1, gc2)
+
+    @staticmethod
+    def _backward(ctx, gn, gc1, gc2):
         x1, x2 = ctx.saved_tensors
         x2o = _opt(x2)
         s = L.stream()
@@ -615,6 +621,12 @@ class InputConvActFn(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, gq, gt, gc1, gc2):
+        # the first layers' backward runs last in a network's backward pass
+        with L.boundary('kernel_fn backward'):
+            return InputConvActFn._backward(ctx, gq, gt, gc1, gc2)
+
+    @staticmethod
+    def _backward(ctx, gq, gt, gc1, gc2):
         x1, x2, pre, c1p, c2p = ctx.saved_tensors
         x2o, c2o = _opt(x2), _opt(c2p)
         w2, act = ctx.w2, ctx.act

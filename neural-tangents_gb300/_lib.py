@@ -6,6 +6,7 @@ kernel of this package.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes as C
 import os
 import threading
@@ -170,6 +171,40 @@ def call(name: str, *args) -> None:
     if rc != 0:
         msg = lib.ntg_last_error().decode()
         raise NtgError(f'{name} failed ({ERRORS.get(rc, rc)}): {msg}')
+
+
+_depth = threading.local()
+
+
+def check_device(where: str) -> None:
+    """Raises NtgError when a bounded wait of a device kernel ran out since the last check.
+
+    The streamed, adjoint and tensor-core kernels bound every pipeline wait; one that runs
+    out sets a device error word and the kernel winds down with its results incomplete.
+    The current stream is synchronised first, so that every kernel it carries has finished,
+    then ntg_device_status reads and clears the words (one 4-byte read per word)."""
+    if not torch.cuda.is_available():
+        return  # nothing of this library can have run
+    torch.cuda.current_stream().synchronize()
+    lib = load()
+    rc = lib.ntg_device_status()
+    if rc != 0:
+        raise NtgError(f'{where}: {ERRORS.get(rc, rc)}: {lib.ntg_last_error().decode()}')
+
+
+@contextlib.contextmanager
+def boundary(where: str):
+    """A public call of the package: on its normal exit, and only at the outermost level
+    (calls nest, e.g. nt.batch calls kernel_fn per tile), the device error words are
+    checked with check_device."""
+    d = getattr(_depth, 'n', 0)
+    _depth.n = d + 1
+    try:
+        yield
+    finally:
+        _depth.n = d
+    if d == 0:
+        check_device(where)
 
 
 def launch_count() -> int:

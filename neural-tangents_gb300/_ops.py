@@ -68,12 +68,10 @@ def gram(x1: torch.Tensor, x2: torch.Tensor, precision: int = 0) -> torch.Tensor
     if precision == 1:
         nbytes = int(L.load().ntg_gram_workspace_bytes(n1, n2, d))
         ws = torch.empty((nbytes,), device=x1.device, dtype=torch.uint8)
+    # a tensor-core pipeline wait that runs out raises the library's device error word,
+    # which the public call around this one reads (L.boundary)
     L.call('ntg_gram', L.stream(), L.ptr(x1), L.ptr(x2), n1, n2, d, L.ptr(out), precision,
            None if ws is None else ws.data_ptr(), nbytes)
-    if precision == 1:
-        code = int(ws[:4].view(torch.int32).item())
-        if code:
-            raise L.NtgError(f'ntg_gram: tensor-core pipeline wait timed out (code {code})')
     return out
 
 

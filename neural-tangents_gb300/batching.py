@@ -16,6 +16,7 @@ import numpy as np
 import torch
 
 from . import _chain
+from . import _lib as L
 from .kernel import Kernel, analytic_kernel
 from .stax import KernelFn, _Ctx, _as_input, _normalize_get
 
@@ -66,6 +67,11 @@ class _CheckpointedKernel(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, gq, gt):
+        with L.boundary('nt.batch backward'):
+            return _CheckpointedKernel._backward(ctx, gq, gt)
+
+    @staticmethod
+    def _backward(ctx, gq, gt):
         from . import _autograd
         x1, x2 = ctx.saved_tensors
         x2o = None if x2.numel() == 0 else x2
@@ -134,6 +140,10 @@ def batch(kernel_fn, batch_size: int = 0, device_count: int = -1, store_on_devic
         raise NotImplementedError('nt_gb300 runs on one GPU; device_count must be -1, 0 or 1')
 
     def batched(x1, x2=None, get=None, *, precision='fp32', **kwargs):
+        with L.boundary('nt.batch'):
+            return _batched(x1, x2, get, precision=precision, **kwargs)
+
+    def _batched(x1, x2=None, get=None, *, precision='fp32', **kwargs):
         if isinstance(x1, Kernel):
             return kernel_fn(x1, x2, get, **kwargs)
         x1t = _as_input(x1)
@@ -238,7 +248,6 @@ class CapturedBatch:
 
     def __init__(self, kernel_fn, x1_shape, x2_shape=None, get=('nngp', 'ntk'),
                  batch_size: int = 0, precision: str = 'fp32'):
-        from . import _lib as L
         dev = L.require_cuda()
         if not isinstance(kernel_fn, KernelFn):
             raise TypeError('CapturedBatch needs a kernel_fn from nt_gb300.stax.serial')
@@ -282,5 +291,6 @@ class CapturedBatch:
             self.x2.copy_(_as_input(x2), non_blocking=True)
         elif x2 is not None:
             raise ValueError('this capture was made with x2=None')
-        self.graph.replay()
+        with L.boundary('CapturedBatch'):
+            self.graph.replay()
         return self.out

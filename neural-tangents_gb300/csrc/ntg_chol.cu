@@ -414,9 +414,14 @@ int trsv(cudaStream_t s, const float* L, int64_t n, float* X, int64_t m, int tra
 using namespace ntg;
 
 extern "C" size_t ntg_chol_workspace_bytes(int64_t n, int64_t m) {
-  // trace + lambda + rnorm (3 doubles), x64 [n*m] doubles, residual [n*m] floats
-  size_t b = 256 + sizeof(double) * (size_t)(n * m) + sizeof(float) * (size_t)(n * m);
-  return (b + 255) & ~(size_t)255;
+  // trace + lambda + rnorm (3 doubles), x64 [n*m] doubles, residual [n*m] floats.
+  // Sizes whose byte count would not fit in 63 bits report SIZE_MAX, which no
+  // workspace satisfies (the product n * m itself must not wrap).
+  if (n <= 0 || m <= 0) return 256;
+  const uint64_t per = sizeof(double) + sizeof(float);
+  if ((uint64_t)n > ((uint64_t)INT64_MAX / per) / (uint64_t)m) return SIZE_MAX;
+  const uint64_t b = 256 + per * (uint64_t)n * (uint64_t)m;
+  return (size_t)((b + 255) & ~(uint64_t)255);
 }
 
 extern "C" int ntg_chol_factor(void* stream, const float* A, int64_t n, double diag_reg,

@@ -19,8 +19,10 @@ int fail(int code, const std::string& msg);
 int check_launch(const char* what);
 void note_launch(uint64_t n = 1);
 int32_t tune(int32_t knob);  // current value of an NTG_TUNE_* knob
-// Reads and clears the device error word of the adjoint kernels (ntg_bwd.cu).
+// Read and clear the device error words of the adjoint kernels (ntg_bwd.cu)
+// and of the tensor-core Gram (ntg_gram_tc.cu); -1 if the read failed.
 int bwd_take_device_error();
+int gram_take_device_error();
 
 // Tensor-core (tcgen05) split-precision Gram; defined in ntg_gram_tc.cu.
 int gram_tc(cudaStream_t stream, const float* x1, const float* x2, int64_t n1, int64_t n2,

@@ -7,7 +7,9 @@
 // swizzled row) moved by TMA into a 3-stage shared-memory ring; one thread
 // issues tcgen05.mma (M=128, N=128, K=16) and tcgen05.commit frees each stage;
 // four warps drain the accumulator with tcgen05.ld. Every mbarrier wait is
-// bounded: a wait that runs out sets the error word and the CTA winds down.
+// bounded: a wait that runs out sets the error words (the workspace word and
+// the library's device word read by ntg_device_status), waits (bounded) for the
+// copies and MMAs already issued, frees its tensor memory and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -27,6 +29,8 @@ constexpr int STAGE_BYTES = 4 * TILE_BYTES;   // A_hi, A_lo, B_hi, B_lo
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr uint32_t TMEM_COLS = 128;
 constexpr uint64_t WAIT_LIMIT = 1ull << 20;   // about a second of polling
+
+__device__ int g_gram_error = 0;
 
 __global__ void split_bf16_kernel(const float* __restrict__ x, int64_t n, int64_t d,
                                   int64_t npad, int64_t dpad, __nv_bfloat16* __restrict__ hi,
@@ -144,6 +148,10 @@ __global__ void __launch_bounds__(128, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   bool ok = true;
+  __shared__ int s_fail;
+  if (threadIdx.x == 0) s_fail = 0;
+  __syncthreads();
+  int issued = 0;  // TMA stages issued by the producer thread
 
   if (warp == 0 && lane == 0) {
     // TMA producer
@@ -159,8 +167,13 @@ __global__ void __launch_bounds__(128, 1)
       tma_load_2d(smem_u32(st + TILE_BYTES), &ta_lo, full, x, (int32_t)m0);
       tma_load_2d(smem_u32(st + 2 * TILE_BYTES), &tb_hi, full, x, (int32_t)n0);
       tma_load_2d(smem_u32(st + 3 * TILE_BYTES), &tb_lo, full, x, (int32_t)n0);
+      issued = kc + 1;
     }
-    if (!ok) atomicExch(err, 1);
+    if (!ok) {
+      atomicExch(err, 1);
+      atomicExch(&g_gram_error, NTG_ERR_WAIT_TIMEOUT);
+      s_fail = 1;
+    }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
     for (int kc = 0; kc < nk && ok; ++kc) {
@@ -180,14 +193,22 @@ __global__ void __launch_bounds__(128, 1)
       }
       mma_commit(smem_u32(&bars[STAGES + s]));  // frees the stage once these MMAs finish
     }
-    mma_commit(smem_u32(&bars[2 * STAGES]));  // accumulator complete
-    if (!ok) atomicExch(err, 2);
+    mma_commit(smem_u32(&bars[2 * STAGES]));  // accumulator complete (or all issued MMAs)
+    if (!ok) {
+      atomicExch(err, 2);
+      atomicExch(&g_gram_error, NTG_ERR_WAIT_TIMEOUT);
+      s_fail = 1;
+    }
   }
   __syncwarp();
 
   // Epilogue: warp w drains TMEM lanes 32 (w % 4) .. + 31 (rows of the tile).
   const bool ready = mbar_wait(smem_u32(&bars[2 * STAGES]), 0);
-  if (!ready && lane == 0) atomicExch(err, 3);
+  if (!ready && lane == 0) {
+    atomicExch(err, 3);
+    atomicExch(&g_gram_error, NTG_ERR_WAIT_TIMEOUT);
+    s_fail = 1;
+  }
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ready) {
     const int rq = warp & 3;
@@ -218,6 +239,16 @@ __global__ void __launch_bounds__(128, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  if (s_fail) {
+    // A wait ran out: let the TMA loads still in flight land (the last use of
+    // each stage; bounded) before the shared memory is released. The MMAs the
+    // issuer started are tracked by its final commit, waited on above.
+    if (warp == 0 && lane == 0)
+      for (int kc = issued > STAGES ? issued - STAGES : 0; kc < issued; ++kc)
+        mbar_wait(smem_u32(&bars[kc % STAGES]), (kc / STAGES) & 1);
+    if (!ready && warp == 1 && lane == 0) mbar_wait(smem_u32(&bars[2 * STAGES]), 0);
+    __syncthreads();
+  }
   if (warp == 1) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(TMEM_COLS));
@@ -253,6 +284,14 @@ int make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t dpad) {
 }
 
 }  // namespace
+
+int gram_take_device_error() {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_gram_error, sizeof(int)) != cudaSuccess) return -1;
+  const int zero = 0;
+  if (v != 0 && cudaMemcpyToSymbol(g_gram_error, &zero, sizeof(int)) != cudaSuccess) return -1;
+  return v;
+}
 
 size_t gram_tc_workspace(int64_t n1, int64_t n2, int64_t d) {
   const int64_t dpad = ceil_div(d, BK) * BK;

@@ -2199,8 +2199,11 @@ extern "C" int ntg_device_status(void) {
   const int zero = 0;
   if (v != 0 && cudaMemcpyToSymbol(g_device_error, &zero, sizeof(int)) != cudaSuccess)
     return check_launch("ntg_device_status");
-  if (v == 0) v = bwd_take_device_error();
-  if (v < 0) return check_launch("ntg_device_status");
+  // every word is read and cleared, so one timeout is reported once
+  const int vb = bwd_take_device_error();
+  const int vg = gram_take_device_error();
+  if (vb < 0 || vg < 0) return check_launch("ntg_device_status");
+  if (v == 0) v = vb ? vb : vg;
   if (v != 0) return fail(v, "a bounded device wait ran out in a streamed kernel");
   return NTG_OK;
 }

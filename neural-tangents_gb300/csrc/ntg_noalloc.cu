@@ -1,8 +1,8 @@
 // Allocation-free variant of ntg_chol_solve.
 //
 // Some callers cannot allocate device memory at the point where they need the
-// kernel-regression solve: an XLA FFI handler running inside a captured CUDA
-// graph (cudaMalloc would break the capture), a serving process that reserves
+// kernel-regression solve: an XLA FFI handler (XLA owns device memory and
+// hands the handler only its operand and result buffers), a serving process that reserves
 // all device memory up front, or a host runtime whose allocator is not
 // reachable from the call site. ntg_chol_solve_noalloc takes the refinement
 // workspace from a fixed device array owned by this library instead of a
@@ -53,6 +53,15 @@ extern "C" int ntg_chol_solve_noalloc(void* stream, const float* A, const float*
                                       const double* lambda, int64_t n, const float* B, int64_t m,
                                       float* X, int32_t refine_iters, double* final_residual) {
   NTG_REQUIRE(n > 0 && m > 0, "ntg_chol_solve_noalloc: sizes must be positive");
+  // Bound n and m before any product is formed, so no size can wrap past the
+  // check below: n at the factorisation's own limit, n * m at what the fixed
+  // array can hold (12 bytes per entry after a 256-byte header).
+  constexpr int64_t kMaxEntries = ((int64_t)NTG_NOALLOC_SCRATCH_BYTES - 256) / 12;
+  if (n > 46340 || m > kMaxEntries / n)
+    return ntg::fail(NTG_ERR_INVALID_ARG,
+                     "ntg_chol_solve_noalloc: n * m too large for the fixed scratch (n * m "
+                     "must be at most " + std::to_string(kMaxEntries) +
+                     " with n <= 46340); use ntg_chol_solve with a workspace");
   const size_t need = ntg_chol_workspace_bytes(n, m);
   if (need > (size_t)NTG_NOALLOC_SCRATCH_BYTES)
     return ntg::fail(NTG_ERR_INVALID_ARG,

@@ -5,8 +5,8 @@ NNGP / NTK / NTKGP posterior and the infinite-ensemble predictions on the same k
 
 ``gradient_descent_mse(k_train_train, y_train, ...)`` keeps the reference
 signature (predict.py:71-278) and returns ``predict_fn(t=None, fx_train_0=0.,
-fx_test_0=None, k_test_train=None)``. ``t=None`` (infinite time) is the
-Cholesky path: an FP32 Cholesky of K + lambda I on the GPU, FP32 triangular
+fx_test_0=None, k_test_train=None)``. ``t=None`` (infinite time) and a scalar
+``t=inf`` take the Cholesky path: an FP32 Cholesky of K + lambda I on the GPU, FP32 triangular
 solves and FP64 iterative refinement (`refine_iters`, default 2; 0 gives the
 plain FP32 solve), all in libntgb300.so. The factorisation is computed once
 and cached, as the reference caches it (predict.py:163). Finite ``t`` uses the
@@ -123,6 +123,11 @@ def gradient_descent_mse(k_train_train, y_train, learning_rate: float = 1.,
     def predict_fn(t=None, fx_train_0=0., fx_test_0=None, k_test_train=None):
         if fx_test_0 is not None and k_test_train is None:
             raise ValueError('`k_test_train` must be specified when `fx_test_0` is not `None`.')
+        # A scalar t = inf is the limit t=None computes (predict.py:236-239, pinned by
+        # predict_test.py:396-428): it takes the Cholesky path too, unless the regularised
+        # kernel is not positive definite, where the eigenbasis path's |lambda| applies.
+        if _is_inf(t) and solver().info == 0:
+            t = None
         if t is None:
             fx_train_t = y
             if fx_test_0 is None:
@@ -156,6 +161,14 @@ def gradient_descent_mse(k_train_train, y_train, learning_rate: float = 1.,
         return outs[0] if outs else y
 
     return predict_fn
+
+
+def _is_inf(t) -> bool:
+    """Whether t is the scalar +inf (a Python number or a 0-d array)."""
+    if t is None:
+        return False
+    a = np.asarray(t.cpu() if isinstance(t, torch.Tensor) else t)
+    return a.ndim == 0 and bool(np.isposinf(a))
 
 
 def _as_like(v, like: Optional[torch.Tensor]):
@@ -451,6 +464,8 @@ def gradient_descent_mse_ensemble(kernel_fn, x_train, y_train, learning_rate: fl
             k = kernel_fn(x_test, x_train, dep if len(dep) > 1 else dep[0], **kw_tt)
             k_td = {g: _dev(getattr(k, g) if len(dep) > 1 else k) for g in dep}
             nngp_tt = _dev(kernel_fn(x_test, None, 'nngp', **kw_tt)) if compute_cov else None
+        if _is_inf(t):
+            t = None  # the limit gp_inference computes (predict.py:860-905 at t = inf)
         if t is None:
             if dep not in inf_cache:
                 inf_cache[dep] = gp_inference(kd, y, diag_reg, diag_reg_absolute_scale)

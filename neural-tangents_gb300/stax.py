@@ -629,6 +629,13 @@ class KernelFn:
 
     def __call__(self, x1_or_kernel, x2=None, get=None, *, pattern=None, mask_constant=None,
                  diagonal_batch=None, diagonal_spatial=None, precision='fp32', **kwargs):
+        with L.boundary('kernel_fn'):
+            return self._call(x1_or_kernel, x2, get, pattern=pattern,
+                              mask_constant=mask_constant, diagonal_batch=diagonal_batch,
+                              diagonal_spatial=diagonal_spatial, precision=precision, **kwargs)
+
+    def _call(self, x1_or_kernel, x2=None, get=None, *, pattern=None, mask_constant=None,
+              diagonal_batch=None, diagonal_spatial=None, precision='fp32', **kwargs):
         if mask_constant is not None:
             raise NotImplementedError('masked inputs are not supported by nt_gb300')
         if diagonal_batch is False:

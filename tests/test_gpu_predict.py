@@ -58,6 +58,31 @@ def test_cholesky_equals_eigh_at_infinite_time(nt):
     a = pred(None, 0., 0., kts)[1].cpu().numpy()
     b = pred(np.inf, 0., 0., kts)[1].cpu().numpy()
     np.testing.assert_allclose(a, b, rtol=2e-4, atol=2e-5)
+    # a time far past every eigenvalue's decay takes the eigenbasis path and meets the limit
+    c = pred(1e12, 0., 0., kts)[1].cpu().numpy()
+    np.testing.assert_allclose(c, a, rtol=2e-4, atol=2e-5)
+
+
+def test_scalar_infinite_time_takes_the_cholesky_path(nt, monkeypatch):
+    """A scalar t = inf is served by the Cholesky kernels (the limit t=None computes); an
+    array of times containing inf keeps the eigenbasis path, where expm1(-inf) = -1."""
+    x1, x2 = rows(6, 48, 20), rows(7, 8, 20)
+    y = onehot(8, 48)
+    kf = nt.stax.serial(*fcn(nt.stax))[2]
+    ktt, kts = kf(x1, None, 'ntk'), kf(x2, x1, 'ntk')
+    calls = []
+    real = nt.predict.CholeskySolver.solve
+    monkeypatch.setattr(nt.predict.CholeskySolver, 'solve',
+                        lambda self, *a, **k: calls.append(1) or real(self, *a, **k))
+    pred = nt.predict.gradient_descent_mse(ktt, y, diag_reg=1e-3)
+    fx_train, fx_test = pred(np.inf, 0., 0., kts)
+    assert calls, 'scalar t = inf did not reach the Cholesky solve'
+    torch.testing.assert_close(fx_train, torch.tensor(y, dtype=torch.float32).cuda())
+    want = pred(None, 0., 0., kts)[1]
+    torch.testing.assert_close(fx_test, want, rtol=0, atol=0)
+    both = pred(np.array([1., np.inf]), 0., 0., kts)[1]
+    assert both.shape == (2, 8, 10)
+    np.testing.assert_allclose(both[1].cpu().numpy(), want.cpu().numpy(), rtol=2e-4, atol=2e-5)
 
 
 @pytest.mark.parametrize('n,m', [(33, 1), (100, 10), (1000, 7), (2048, 10), (300, 2500), (517, 129)])

@@ -1,7 +1,8 @@
 """The allocation-free solve (ntg_chol_solve_noalloc) against the workspace solve.
 
-Callers that cannot allocate device memory at the call site (a handler inside
-a captured CUDA graph, a server with a pre-reserved memory pool) use
+Callers that cannot allocate device memory at the call site (an XLA FFI
+handler, which only receives the buffers XLA allocated; a server whose device
+memory is all reserved up front in its own pool) use
 ntg_chol_solve_noalloc, whose refinement workspace is a fixed device array of
 the library. This test calls it through the C ABI twice in a row, on two
 different right-hand sides, and compares each result with ntg_chol_solve run
