@@ -263,6 +263,46 @@ int ntg_chol_solve(void* stream, const float* A, const float* L, const double* l
                    const float* B, int64_t m, float* X, int32_t refine_iters, void* workspace,
                    size_t workspace_bytes, double* final_residual);
 
+/* FP32-accurate GEMM on the tcgen05 tensor cores: C = alpha A B^T + beta C with
+ * A [m, k] (row pitch lda) and B [n, k] (row pitch ldb) row-major float32, C [m, n]
+ * (row pitch ldc). Each operand is split into tf32 hi + lo parts in shared memory
+ * and hi hi + hi lo + lo hi are accumulated in FP32 (about 22 significant bits per
+ * operand). lda and ldb multiples of 4, A and B 16-byte aligned (TMA). lower != 0
+ * (m == n): only C's lower triangle (col <= row) is computed and written, the
+ * symmetric rank-k update of a Cholesky factorisation. C may alias A when n <= 128.
+ * Serves the trailing updates of ntg_chol_factor_tc and the solves of
+ * ntg_chol_solve_tc (predict.py:1235-1258, cuSOLVER potrf/potrs in the reference). */
+int ntg_gemm_tc(void* stream, const float* a, int64_t lda, const float* b, int64_t ldb, float* c,
+                int64_t ldc, int64_t m, int64_t n, int64_t k, float alpha, float beta,
+                int32_t lower);
+
+/* The tensor-core Cholesky of predict.gradient_descent_mse (predict.py:1224-1258,
+ * cho_factor / cho_solve): A = K + lambda I = L L^T in FP32 with 128-wide panels
+ * (diagonal block factored and inverted by one CTA, the panel below by forward
+ * substitution, the trailing update by ntg_gemm_tc). K [n, n] float32 contiguous;
+ * L [n, ldl] row-major (ldl >= n, a multiple of 4, L 16-byte aligned) receives the
+ * lower factor, zeros above the diagonal; lambda and info as ntg_chol_factor.
+ * factor_workspace (ntg_chol_factor_tc_workspace_bytes) receives the inverses of
+ * the diagonal blocks and L^T, which ntg_chol_solve_tc reads. */
+size_t ntg_chol_factor_tc_workspace_bytes(int64_t n, int64_t ldl);
+int ntg_chol_factor_tc(void* stream, const float* A, int64_t n, double diag_reg, int32_t absolute,
+                       float* L, int64_t ldl, double* lambda, int* info, void* factor_workspace,
+                       size_t factor_workspace_bytes);
+/* X = (K + lambda I)^{-1} B, B and X [n, m] row-major, from a factor of
+ * ntg_chol_factor_tc: for m <= 16 two cooperative launches (block-triangular
+ * solves with the stored inverses of the diagonal blocks, blocks handed on by
+ * flags under bounded waits), for more right-hand sides blocked solves whose
+ * updates run on ntg_gemm_tc. refine_iters steps of iterative refinement keep X in
+ * FP64 with the residual accumulated in FP64 (m <= 16) or double-float arithmetic
+ * (two FP32 words; m > 16). final_residual as ntg_chol_solve. */
+size_t ntg_chol_solve_tc_workspace_bytes(int64_t n, int64_t m, int64_t ldl);
+int ntg_chol_solve_tc(void* stream, const float* A, const float* L, int64_t ldl,
+                      const void* factor_workspace, const double* lambda, int64_t n,
+                      const float* B, int64_t m, float* X, int32_t refine_iters, void* workspace,
+                      size_t workspace_bytes, double* final_residual);
+/* log det(L L^T) of a factor of ntg_chol_factor_tc -> out[0] (device double). */
+int ntg_chol_logdet_tc(void* stream, const float* L, int64_t n, int64_t ldl, double* out);
+
 /* ---- adjoints (reverse mode; the jax.custom_vjp backward rules) -------- */
 /* Derivative conventions follow the reference's custom JVPs: the square root
  * of elementwise.py:1278-1290 has derivative 0 at arguments <= 1e-30, and the

@@ -113,6 +113,14 @@ SIGNATURES = {
     'ntg_chol_workspace_bytes': ([_I64, _I64], C.c_size_t),
     'ntg_chol_solve': ([_P, _P, _P, _P, _I64, _P, _I64, _P, _I32, _P, C.c_size_t, _P], C.c_int),
     'ntg_chol_solve_noalloc': ([_P, _P, _P, _P, _I64, _P, _I64, _P, _I32, _P], C.c_int),
+    'ntg_gemm_tc': ([_P, _P, _I64, _P, _I64, _P, _I64, _I64, _I64, _I64, _F, _F, _I32], C.c_int),
+    'ntg_chol_factor_tc_workspace_bytes': ([_I64, _I64], C.c_size_t),
+    'ntg_chol_factor_tc': ([_P, _P, _I64, C.c_double, _I32, _P, _I64, _P, _P, _P, C.c_size_t],
+                           C.c_int),
+    'ntg_chol_solve_tc_workspace_bytes': ([_I64, _I64, _I64], C.c_size_t),
+    'ntg_chol_solve_tc': ([_P, _P, _P, _I64, _P, _P, _I64, _P, _I64, _P, _I32, _P, C.c_size_t,
+                           _P], C.c_int),
+    'ntg_chol_logdet_tc': ([_P, _P, _I64, _I64, _P], C.c_int),
 }
 
 _lib = None

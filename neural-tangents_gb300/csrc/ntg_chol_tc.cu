@@ -1,0 +1,792 @@
+// Blocked Cholesky factorisation and solves of predict.gradient_descent_mse on
+// the sm_103a tensor cores (neural_tangents/_src/predict.py:1224-1258 restated
+// for the GPU): A = K + lambda I = L L^T in FP32 with 128-wide panels.
+//
+// Per panel k:
+//   diag_block_kernel   one CTA factors the 128 x 128 diagonal block (four
+//                       32-wide steps, each a warp-level Cholesky + inverse in
+//                       registers, then the sub-panel solve and rank-32 update in
+//                       shared memory) and writes the block's inverse;
+//   panel_trsm_kernel   the rows below: L21 = A21 L11^-T by forward substitution
+//                       (a warp per row, backward stable);
+//   gemm_tf32x3 lower   the trailing update A22 -= L21 L21^T on the tensor cores
+//                       (3xTF32 products, FP32 accumulation; tiles on or below the
+//                       diagonal only).
+// Solves: for up to kSmallM right-hand sides, one cooperative launch per
+// triangle in which the CTA of block b folds in each solved block j < b as
+// soon as its flag is set (bounded waits) and applies the stored inverse of its
+// diagonal block; for more right-hand sides, blocked right-looking solves on the
+// transposed right-hand sides whose updates are 3xTF32 tensor-core GEMMs.
+// Iterative refinement x <- x + A^{-1} (b - A x) keeps x in FP64; the residual
+// is accumulated in FP64 for up to kSmallM right-hand sides and in double-float
+// (two-FP32, error-free products and sums) for more, where FP64 throughput
+// would make the n^2 m residual the dominant cost.
+#include <cooperative_groups.h>
+
+#include <mutex>
+#include <string>
+
+#include "ntg_common.cuh"
+
+namespace ntg {
+int gemm_tf32x3(cudaStream_t s, const float* a, int64_t lda, const float* b, int64_t ldb,
+                float* c, int64_t ldc, int64_t m, int64_t n, int64_t k, float alpha, float beta,
+                int lower);
+
+namespace {
+
+constexpr int PB = 128;        // panel / diagonal block
+constexpr int PBS = PB + 1;    // padded shared-memory row
+constexpr int kSmallM = 16;    // right-hand sides of the cooperative solves
+constexpr uint32_t kFlagWait = 1u << 22;
+
+__device__ int g_chol_error = 0;
+
+__host__ __device__ __forceinline__ int64_t mini(int64_t a, int64_t b) { return a < b ? a : b; }
+
+// ---------------------------------------------------------------------------
+// Set-up
+// ---------------------------------------------------------------------------
+
+__global__ void trace_tc_kernel(const float* __restrict__ A, int64_t n, double* __restrict__ out) {
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += (double)A[i * n + i];
+  __shared__ double part[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+    out[0] = t;
+  }
+}
+
+// L[i, j] = A[i, j] (j < i), A[i, i] + lambda (j == i), 0 above the diagonal and in the
+// padding columns n <= j < ldl.
+__global__ void init_factor_ld_kernel(const float* __restrict__ A, int64_t n, int64_t ldl,
+                                      double reg, int absolute, const double* __restrict__ trace,
+                                      float* __restrict__ L, double* __restrict__ lambda) {
+  const double lam = absolute ? reg : reg * trace[0] / (double)n;
+  if (blockIdx.x == 0 && threadIdx.x == 0) lambda[0] = lam;
+  const int64_t total = n * ldl;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx / ldl, j = idx - i * ldl;
+    float v = 0.f;
+    if (j < i) v = A[i * n + j];
+    else if (j == i) v = (float)((double)A[i * n + i] + lam);
+    L[idx] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Diagonal block: factor + inverse (one CTA of 512 threads)
+// ---------------------------------------------------------------------------
+
+// Warp-level Cholesky of the 32 x 32 block at (o, o) of `a` (lower part used) and the
+// inverse of the factor into dinv (lower, row-major 32 x 33). Lane r holds row r.
+__device__ void warp_potrf_inv32(float (*a)[PBS], int o, float (*dinv)[33], int* info,
+                                 int64_t col0) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  float v[32];
+#pragma unroll
+  for (int c = 0; c < 32; ++c) v[c] = a[o + lane][o + c];
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    float d = __shfl_sync(full, v[j], j);
+    if (!(d > 0.f)) {  // uniform across the warp
+      if (lane == 0) atomicCAS(info, 0, (int)(col0 + o + j + 1));
+      d = 1.f;
+    }
+    const float s = sqrtf(d);
+    const float lrj = (lane == j) ? s : v[j] / s;
+    v[j] = lrj;
+#pragma unroll
+    for (int c = j + 1; c < 32; ++c) {
+      const float lcj = __shfl_sync(full, lrj, c);
+      if (lane >= c) v[c] = fmaf(-lrj, lcj, v[c]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 32; ++c) a[o + lane][o + c] = (c <= lane) ? v[c] : 0.f;
+  // X = L^-1, lane c computes column c: x_i = (delta_ic - sum_{p<i} L[i][p] x_p) / L[i][i]
+  float x[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    float s = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+    for (int p = 0; p < i; ++p) s = fmaf(-__shfl_sync(full, v[p], i), x[p], s);
+    x[i] = s / __shfl_sync(full, v[i], i);
+  }
+#pragma unroll
+  for (int i = 0; i < 32; ++i) dinv[i][lane] = x[i];
+}
+
+// Factors L[k:k+nb, k:k+nb] in place (upper part zeroed) and writes the inverse of the
+// factor, zero-padded to 128 x 128, to linv (row-major) and its transpose to linvT.
+__global__ void __launch_bounds__(512, 1)
+    diag_block_kernel(float* __restrict__ L, int64_t ldl, int64_t n, int64_t k, int* info,
+                      float* __restrict__ linv, float* __restrict__ linvT) {
+  extern __shared__ float sm[];
+  float(*a)[PBS] = reinterpret_cast<float(*)[PBS]>(sm);
+  float(*x)[PBS] = reinterpret_cast<float(*)[PBS]>(sm + PB * PBS);
+  float(*t)[33] = reinterpret_cast<float(*)[33]>(sm + 2 * PB * PBS);        // 128 x 33
+  float(*dinv)[32][33] = reinterpret_cast<float(*)[32][33]>(sm + 2 * PB * PBS + PB * 33);
+  const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5;
+  const int nb = (int)mini(PB, n - k);
+  // padding beyond nb: identity (factors to the identity, inverse identity, cut later)
+  for (int idx = tid; idx < PB * PB; idx += nth) {
+    const int i = idx / PB, j = idx % PB;
+    float v;
+    if (i < nb && j < nb) v = (j <= i) ? L[(k + i) * ldl + k + j] : 0.f;
+    else v = (i == j) ? 1.f : 0.f;
+    a[i][j] = v;
+  }
+  __syncthreads();
+  for (int sb = 0; sb < 4; ++sb) {
+    const int o = sb * 32;
+    if (warp == 0) warp_potrf_inv32(a, o, dinv[sb], info, k);
+    __syncthreads();
+    const int rows = PB - o - 32;
+    if (rows > 0) {
+      // sub-panel solve: L[r][o+c] = sum_{p <= c} A[r][o+p] Dinv[c][p], r >= o + 32
+      for (int idx = tid; idx < rows * 32; idx += nth) {
+        const int r = o + 32 + idx / 32, c = idx % 32;
+        float s = 0.f;
+        for (int p = 0; p <= c; ++p) s = fmaf(a[r][o + p], dinv[sb][c][p], s);
+        t[r][c] = s;
+      }
+      __syncthreads();
+      for (int idx = tid; idx < rows * 32; idx += nth) {
+        const int r = o + 32 + idx / 32, c = idx % 32;
+        a[r][o + c] = t[r][c];
+      }
+      __syncthreads();
+      // trailing rank-32 update of the lower part
+      for (int idx = tid; idx < rows * rows; idx += nth) {
+        const int r = o + 32 + idx / rows, c = o + 32 + idx % rows;
+        if (c > r) continue;
+        float s = a[r][c];
+#pragma unroll 8
+        for (int p = 0; p < 32; ++p) s = fmaf(-a[r][o + p], a[c][o + p], s);
+        a[r][c] = s;
+      }
+      __syncthreads();
+    }
+  }
+  // write the factor back (lower incl. the diagonal; upper zero)
+  for (int idx = tid; idx < nb * nb; idx += nth) {
+    const int i = idx / nb, j = idx % nb;
+    L[(k + i) * ldl + k + j] = (j <= i) ? a[i][j] : 0.f;
+  }
+  // inverse, 32-blocks: X_ii = Dinv_i, X_ij = -Dinv_i sum_{q=j}^{i-1} L_iq X_qj
+  for (int idx = tid; idx < PB * PB; idx += nth) {
+    const int i = idx / PB, j = idx % PB;
+    const int bi = i >> 5, bj = j >> 5;
+    x[i][j] = (bi == bj) ? dinv[bi][i & 31][j & 31] : 0.f;
+  }
+  __syncthreads();
+  for (int bi = 1; bi < 4; ++bi) {
+    // T[r][c'] over the bi blocks j < bi: T_j = sum_{q=j}^{bi-1} L_{bi,q} X_{q,j}, into t
+    // (t holds 128 rows x 32: rows j*32 + r' for block j)
+    for (int idx = tid; idx < bi * 1024; idx += nth) {
+      const int bj = idx / 1024, r = (idx % 1024) / 32, c = idx % 32;
+      float s = 0.f;
+      for (int q = bj * 32; q < bi * 32; ++q) s = fmaf(a[bi * 32 + r][q], x[q][bj * 32 + c], s);
+      t[bj * 32 + r][c] = s;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < bi * 1024; idx += nth) {
+      const int bj = idx / 1024, r = (idx % 1024) / 32, c = idx % 32;
+      float s = 0.f;
+      for (int p = 0; p <= r; ++p) s = fmaf(dinv[bi][r][p], t[bj * 32 + p][c], s);
+      x[bi * 32 + r][bj * 32 + c] = -s;
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < PB * PB; idx += nth) {
+    const int i = idx / PB, j = idx % PB;
+    const bool in = i < nb && j < nb;
+    linv[idx] = in ? x[i][j] : 0.f;
+    linvT[idx] = in ? x[j][i] : 0.f;
+  }
+}
+
+constexpr size_t kDiagSmem = (size_t)(2 * PB * PBS + PB * 33 + 4 * 32 * 33) * sizeof(float);
+
+// ---------------------------------------------------------------------------
+// Panel solve below the diagonal block: x L11^T = a for rows r >= k + 128, a warp per
+// row; lane l holds columns l, l + 32, l + 64, l + 96.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(512)
+    panel_trsm_kernel(float* __restrict__ L, int64_t ldl, int64_t n, int64_t k) {
+  extern __shared__ float sm[];
+  float(*l11)[PBS] = reinterpret_cast<float(*)[PBS]>(sm);
+  for (int idx = threadIdx.x; idx < PB * PB; idx += blockDim.x) {
+    const int i = idx / PB, j = idx % PB;
+    l11[i][j] = (j <= i) ? L[(k + i) * ldl + k + j] : 0.f;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const unsigned full = 0xffffffffu;
+  for (int64_t r = k + PB + (int64_t)blockIdx.x * nw + warp; r < n; r += (int64_t)gridDim.x * nw) {
+    float* row = L + r * ldl + k;
+    float x[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) x[s] = row[lane + 32 * s];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+#pragma unroll 4
+      for (int cc = 0; cc < 32; ++cc) {
+        const int c = 32 * s + cc;
+        const float xc = __shfl_sync(full, x[s], cc) / l11[c][c];
+        if (lane == cc) x[s] = xc;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int p = lane + 32 * u;
+          if (p > c) x[u] = fmaf(-xc, l11[p][c], x[u]);
+        }
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < 4; ++s) row[lane + 32 * s] = x[s];
+  }
+}
+
+constexpr size_t kPanelSmem = (size_t)PB * PBS * sizeof(float);
+
+// out[j, i] = in[i, j] for an [rows, cols] block (row pitches ld_in, ld_out).
+__global__ void transpose_kernel(const float* __restrict__ in, int64_t ld_in, float* __restrict__ out,
+                                 int64_t ld_out, int64_t rows, int64_t cols) {
+  __shared__ float tile[32][33];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, c0 = (int64_t)blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  for (int i = ty; i < 32; i += 8) {
+    const int64_t r = r0 + i, c = c0 + tx;
+    tile[i][tx] = (r < rows && c < cols) ? in[r * ld_in + c] : 0.f;
+  }
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    const int64_t c = c0 + i, r = r0 + tx;
+    if (c < cols && r < rows) out[c * ld_out + r] = tile[tx][i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Cooperative triangular solves for up to kSmallM right-hand sides.
+// X [n, m] row-major in place: forward L y = b, or backward L^T x = y.
+// Block b's CTA waits (bounded) for the flags of the blocks it depends on; a
+// flag is set once the block's solution is in global memory.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool wait_flag(const int* flag, int want) {
+  for (uint32_t it = 0; it < kFlagWait; ++it) {
+    if (*reinterpret_cast<const volatile int*>(flag) >= want) {
+      __threadfence();
+      return true;
+    }
+    __nanosleep(64);
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(256)
+    trsv_coop_kernel(const float* __restrict__ L, int64_t ldl, const float* __restrict__ linv,
+                     const float* __restrict__ linvT, int64_t n, float* X, int64_t m,
+                     int* flags, int backward) {
+  extern __shared__ float sm[];
+  float(*blk)[PBS] = reinterpret_cast<float(*)[PBS]>(sm);        // an L block or Linv
+  float(*yj)[kSmallM + 1] = reinterpret_cast<float(*)[kSmallM + 1]>(sm + PB * PBS);
+  float(*acc)[kSmallM + 1] = reinterpret_cast<float(*)[kSmallM + 1]>(sm + PB * PBS + PB * (kSmallM + 1));
+  __shared__ int s_ok;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int64_t nblk = (n + PB - 1) / PB;
+  // thread -> (row r, columns c0 .. c0 + m/2)
+  const int r = tid & (PB - 1), half = tid >> 7;
+  for (int64_t ord = blockIdx.x; ord < nblk; ord += gridDim.x) {
+    const int64_t b = backward ? nblk - 1 - ord : ord;
+    const int64_t r0 = b * PB;
+    const int nb = (int)mini(PB, n - r0);
+    for (int idx = tid; idx < PB * (int)m; idx += nth) {
+      const int i = idx / (int)m, c = idx % (int)m;
+      acc[i][c] = i < nb ? X[(r0 + i) * m + c] : 0.f;
+    }
+    if (tid == 0) s_ok = 1;
+    __syncthreads();
+    // fold in every solved block j this block depends on
+    for (int64_t jo = 0; jo < ord; ++jo) {
+      const int64_t j = backward ? nblk - 1 - jo : jo;
+      const int64_t j0 = j * PB;
+      const int nj = (int)mini(PB, n - j0);
+      if (tid == 0 && s_ok && !wait_flag(flags + j, 1)) {
+        s_ok = 0;
+        atomicExch(&g_chol_error, NTG_ERR_WAIT_TIMEOUT);
+      }
+      __syncthreads();
+      if (!s_ok) break;
+      // forward: acc -= L[b rows, j cols] y_j; backward: acc -= L[j rows, b cols]^T x_j
+      // blk[i][q] multiplies y_j[q] into row i; both loads walk contiguous global rows
+      if (!backward) {
+        for (int idx = tid; idx < PB * PB; idx += nth) {
+          const int i = idx / PB, q = idx % PB;
+          blk[i][q] = (i < nb && q < nj) ? L[(r0 + i) * ldl + j0 + q] : 0.f;
+        }
+      } else {
+        for (int idx = tid; idx < PB * PB; idx += nth) {
+          const int q = idx / PB, i = idx % PB;
+          blk[i][q] = (q < nj && i < nb) ? L[(j0 + q) * ldl + r0 + i] : 0.f;
+        }
+      }
+      for (int idx = tid; idx < PB * (int)m; idx += nth) {
+        const int q = idx / (int)m, c = idx % (int)m;
+        yj[q][c] = q < nj ? __ldcg(X + (j0 + q) * m + c) : 0.f;
+      }
+      __syncthreads();
+      for (int c = half; c < (int)m; c += 2) {
+        float s = 0.f;
+#pragma unroll 8
+        for (int q = 0; q < PB; ++q) s = fmaf(blk[r][q], yj[q][c], s);
+        acc[r][c] -= s;
+      }
+      __syncthreads();
+    }
+    if (!s_ok) return;
+    // x_b = Linv acc (forward) or Linv^T acc (backward)
+    const float* li = (backward ? linvT : linv) + b * PB * PB;
+    for (int idx = tid; idx < PB * PB; idx += nth) blk[idx / PB][idx % PB] = li[idx];
+    __syncthreads();
+    for (int c = half; c < (int)m; c += 2) {
+      float s = 0.f;
+#pragma unroll 8
+      for (int q = 0; q < PB; ++q) s = fmaf(blk[r][q], acc[q][c], s);
+      if (r < nb) X[(r0 + r) * m + c] = s;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicExch(flags + b, 1);
+  }
+}
+
+constexpr size_t kTrsvSmem = (size_t)(PB * PBS + 2 * PB * (kSmallM + 1)) * sizeof(float);
+
+// ---------------------------------------------------------------------------
+// Residuals R = B - (A + lambda I) X with X in FP64.
+// ---------------------------------------------------------------------------
+
+// FP64, one warp per row, up to MR right-hand sides in registers.
+template <int MR>
+__global__ void __launch_bounds__(256)
+    residual64_rows_kernel(const float* __restrict__ A, int64_t n, const double* lambda,
+                           const float* __restrict__ B, const double* __restrict__ X, int64_t m,
+                           float* __restrict__ R, double* __restrict__ rnorm) {
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float* ar = A + row * n;
+  double acc[MR];
+#pragma unroll
+  for (int c = 0; c < MR; ++c) acc[c] = 0.0;
+  for (int64_t j = lane; j < n; j += 32) {
+    const double a = (double)ar[j];
+    const double* xr = X + j * m;
+#pragma unroll
+    for (int c = 0; c < MR; ++c)
+      if (c < m) acc[c] = fma(a, xr[c], acc[c]);
+  }
+  double rmax = 0.0;
+#pragma unroll
+  for (int c = 0; c < MR; ++c) {
+    double v = acc[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (c < m && lane == 0) {
+      const double r = (double)B[row * m + c] - v - lambda[0] * X[row * m + c];
+      R[row * m + c] = (float)r;
+      rmax = fmax(rmax, fabs(r));
+    }
+  }
+  if (lane == 0 && rmax > 0.0)
+    atomicMax(reinterpret_cast<unsigned long long*>(rnorm),
+              (unsigned long long)__double_as_longlong(rmax));
+}
+
+// Double-float accumulation (s_hi, s_lo) += a * (x_hi + x_lo): a * x_hi is split
+// error-free (product and fused remainder), its high part added with a two-sum.
+__device__ __forceinline__ void df_fma(float a, float xh, float xl, float& sh, float& sl) {
+  const float ph = a * xh;
+  float pl = fmaf(a, xh, -ph);
+  pl = fmaf(a, xl, pl);
+  const float s = sh + ph;
+  const float bv = s - sh;
+  const float e = (sh - (s - bv)) + (ph - bv);
+  sl += e + pl;
+  sh = s;
+}
+
+// Double-float residual over 64 x 64 tiles of (row, column): X (FP64) is split into
+// FP32 (hi, lo) as it is staged; each thread keeps 4 x 4 double-float sums.
+__global__ void __launch_bounds__(256)
+    residual_df_kernel(const float* __restrict__ A, int64_t n, const double* lambda,
+                       const float* __restrict__ B, const double* __restrict__ X, int64_t m,
+                       float* __restrict__ R, double* __restrict__ rnorm) {
+  __shared__ float As[16][64 + 1];   // [k][i]
+  __shared__ float Xh[16][64 + 1];   // [k][j]
+  __shared__ float Xl[16][64 + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t i0 = (int64_t)blockIdx.y * 64, j0 = (int64_t)blockIdx.x * 64;
+  float sh[4][4] = {}, sl[4][4] = {};
+  for (int64_t k0 = 0; k0 < n; k0 += 16) {
+    for (int idx = threadIdx.x; idx < 16 * 64; idx += 256) {
+      const int i = idx / 16, k = idx % 16;
+      As[k][i] = (i0 + i < n && k0 + k < n) ? A[(i0 + i) * n + k0 + k] : 0.f;
+      const int kk = idx / 64, j = idx % 64;
+      const double xv = (k0 + kk < n && j0 + j < m) ? X[(k0 + kk) * m + j0 + j] : 0.0;
+      const float xh = (float)xv;
+      Xh[kk][j] = xh;
+      Xl[kk][j] = (float)(xv - (double)xh);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      float av[4], hv[4], lv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        av[u] = As[k][ty * 4 + u];
+        hv[u] = Xh[k][tx * 4 + u];
+        lv[u] = Xl[k][tx * 4 + u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) df_fma(av[u], hv[v], lv[v], sh[u][v], sl[u][v]);
+    }
+    __syncthreads();
+  }
+  double rmax = 0.0;
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int64_t i = i0 + ty * 4 + u;
+    if (i >= n) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int64_t j = j0 + tx * 4 + v;
+      if (j >= m) continue;
+      const double ax = (double)sh[u][v] + (double)sl[u][v];
+      const double r = (double)B[i * m + j] - ax - lambda[0] * X[i * m + j];
+      R[i * m + j] = (float)r;
+      rmax = fmax(rmax, fabs(r));
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+  if ((threadIdx.x & 31) == 0 && rmax > 0.0)
+    atomicMax(reinterpret_cast<unsigned long long*>(rnorm),
+              (unsigned long long)__double_as_longlong(rmax));
+}
+
+__global__ void to_double_tc_kernel(const float* __restrict__ a, double* __restrict__ b,
+                                    int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+
+__global__ void accumulate_tc_kernel(double* __restrict__ x, const float* __restrict__ dx,
+                                     float* __restrict__ x32, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += (double)dx[i];
+    x32[i] = (float)x[i];
+  }
+}
+
+__global__ void logdet_ld_kernel(const float* __restrict__ L, int64_t n, int64_t ldl,
+                                 double* __restrict__ out) {
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += log((double)L[i * ldl + i]);
+  __shared__ double part[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+    out[0] = 2.0 * t;
+  }
+}
+
+int grid_for(int64_t n) {
+  int64_t g = (n + 255) / 256;
+  return (int)(g > 152 * 32 ? 152 * 32 : (g < 1 ? 1 : g));
+}
+
+int set_smem(const void* fn, size_t bytes) {
+  const cudaError_t e =
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) return fail(NTG_ERR_CUDA, std::string("chol: ") + cudaGetErrorString(e));
+  return NTG_OK;
+}
+
+int attrs_once() {
+  static std::once_flag once;
+  static int rc = NTG_OK;
+  std::call_once(once, [] {
+    rc = set_smem((const void*)diag_block_kernel, kDiagSmem);
+    if (!rc) rc = set_smem((const void*)panel_trsm_kernel, kPanelSmem);
+    if (!rc) rc = set_smem((const void*)trsv_coop_kernel, kTrsvSmem);
+  });
+  return rc;
+}
+
+// Factor workspace layout (bytes): linv [nblk * 128 * 128] f32, linvT [same],
+// U = L^T [n * ldl] f32 (for the many-right-hand-side backward solve).
+struct FactorWs {
+  float* linv;
+  float* linvT;
+  float* u;
+};
+
+size_t factor_ws_bytes(int64_t n, int64_t ldl) {
+  const int64_t nblk = (n + PB - 1) / PB;
+  return (size_t)(2 * nblk * PB * PB + n * ldl) * sizeof(float) + 256;
+}
+
+FactorWs factor_ws(void* ws, int64_t n) {
+  const int64_t nblk = (n + PB - 1) / PB;
+  char* p = static_cast<char*>(ws);
+  p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 255) & ~(uintptr_t)255);
+  FactorWs f;
+  f.linv = reinterpret_cast<float*>(p);
+  f.linvT = f.linv + nblk * PB * PB;
+  f.u = f.linvT + nblk * PB * PB;
+  return f;
+}
+
+// Solve workspace: rnorm (256 B), x64 [n m] f64, r32 [n m] f32, flags [2 nblk] i32,
+// z [m_pad * ldz] f32 for the many-right-hand-side path (ldz = ldl).
+size_t solve_ws_bytes(int64_t n, int64_t m, int64_t ldl) {
+  const int64_t nblk = (n + PB - 1) / PB;
+  size_t b = 256 + (size_t)n * m * (sizeof(double) + sizeof(float)) + 2 * nblk * sizeof(int) + 256;
+  if (m > kSmallM) b += (size_t)m * ldl * sizeof(float) + 256;
+  return (b + 255) & ~(size_t)255;
+}
+
+int coop_trsv(cudaStream_t s, const float* L, int64_t ldl, const FactorWs& f, int64_t n,
+              float* X, int64_t m, int* flags, int backward) {
+  const int64_t nblk = (n + PB - 1) / PB;
+  if (cudaMemsetAsync(flags, 0, sizeof(int) * nblk, s) != cudaSuccess)
+    return check_launch("ntg_chol_solve_tc flags");
+  static int max_ctas = 0;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int per_sm = 0, dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trsv_coop_kernel, 256, kTrsvSmem);
+    max_ctas = per_sm * sms;
+  });
+  if (max_ctas <= 0) return fail(NTG_ERR_CUDA, "ntg_chol_solve_tc: no co-resident CTAs");
+  const int grid = (int)mini(nblk, max_ctas);
+  const float* linv = f.linv;
+  const float* linvT = f.linvT;
+  int bw = backward;
+  void* args[] = {(void*)&L, (void*)&ldl, (void*)&linv, (void*)&linvT, (void*)&n, (void*)&X,
+                  (void*)&m, (void*)&flags, (void*)&bw};
+  const cudaError_t e = cudaLaunchCooperativeKernel((const void*)trsv_coop_kernel, grid, 256,
+                                                    args, kTrsvSmem, s);
+  note_launch();
+  if (e != cudaSuccess)
+    return fail(NTG_ERR_CUDA, std::string("ntg_chol_solve_tc: ") + cudaGetErrorString(e));
+  return NTG_OK;
+}
+
+// Many right-hand sides: Z = X^T [m, ldz]; forward Z_b = (Z_b) Linv_b^T then
+// Z[:, >b] -= Z_b L[>b rows, b]^T; backward Z_b = Z_b Linv_b then Z[:, <b] -= Z_b U[<b, b]^T.
+int gemm_trsm(cudaStream_t s, const float* L, int64_t ldl, const FactorWs& f, int64_t n,
+              float* X, int64_t m, float* z, int64_t ldz) {
+  const int64_t nblk = (n + PB - 1) / PB;
+  {
+    dim3 g((unsigned)ceil_div(m, 32), (unsigned)ceil_div(n, 32));
+    transpose_kernel<<<g, 256, 0, s>>>(X, m, z, ldz, n, m);
+    note_launch();
+  }
+  int rc;
+  for (int64_t bb = 0; bb < nblk; ++bb) {
+    const int64_t b = bb;
+    const int64_t r0 = b * PB;
+    const int64_t nb = mini(PB, n - r0);
+    rc = gemm_tf32x3(s, z + r0, ldz, f.linv + b * PB * PB, PB, z + r0, ldz, m, nb, nb, 1.f, 0.f, 0);
+    if (rc) return rc;
+    const int64_t rest = n - r0 - nb;
+    if (rest > 0) {
+      rc = gemm_tf32x3(s, z + r0, ldz, L + (r0 + nb) * ldl + r0, ldl, z + r0 + nb, ldz, m, rest,
+                       nb, -1.f, 1.f, 0);
+      if (rc) return rc;
+    }
+  }
+  for (int64_t bb = 0; bb < nblk; ++bb) {
+    const int64_t b = nblk - 1 - bb;
+    const int64_t r0 = b * PB;
+    const int64_t nb = mini(PB, n - r0);
+    rc = gemm_tf32x3(s, z + r0, ldz, f.linvT + b * PB * PB, PB, z + r0, ldz, m, nb, nb, 1.f, 0.f,
+                     0);
+    if (rc) return rc;
+    if (r0 > 0) {
+      rc = gemm_tf32x3(s, z + r0, ldz, f.u + r0, ldl, z, ldz, m, r0, nb, -1.f, 1.f, 0);
+      if (rc) return rc;
+    }
+  }
+  {
+    dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(m, 32));
+    transpose_kernel<<<g, 256, 0, s>>>(z, ldz, X, m, m, n);
+    note_launch();
+  }
+  return check_launch("ntg_chol_solve_tc trsm");
+}
+
+}  // namespace
+
+int chol_take_device_error() {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_chol_error, sizeof(int)) != cudaSuccess) return -1;
+  const int zero = 0;
+  if (v != 0 && cudaMemcpyToSymbol(g_chol_error, &zero, sizeof(int)) != cudaSuccess) return -1;
+  return v;
+}
+
+}  // namespace ntg
+
+using namespace ntg;
+
+extern "C" size_t ntg_chol_factor_tc_workspace_bytes(int64_t n, int64_t ldl) {
+  if (n <= 0 || ldl < n || n > 46340 || ldl > 46340 + 128) return SIZE_MAX;
+  return factor_ws_bytes(n, ldl);
+}
+
+extern "C" int ntg_chol_factor_tc(void* stream, const float* A, int64_t n, double diag_reg,
+                                  int32_t absolute, float* L, int64_t ldl, double* lambda,
+                                  int* info, void* workspace, size_t workspace_bytes) {
+  NTG_REQUIRE(A && L && lambda && info && workspace, "ntg_chol_factor_tc: null pointer");
+  NTG_REQUIRE(n > 0 && n <= 46340, "ntg_chol_factor_tc: n must be in [1, 46340]");
+  NTG_REQUIRE(ldl >= n && ldl % 4 == 0 && ldl <= 46340 + 128,
+              "ntg_chol_factor_tc: ldl must be >= n and a multiple of 4");
+  NTG_REQUIRE((reinterpret_cast<uintptr_t>(L) & 15) == 0, "ntg_chol_factor_tc: L must be 16-byte aligned");
+  NTG_REQUIRE(workspace_bytes >= factor_ws_bytes(n, ldl),
+              "ntg_chol_factor_tc: workspace smaller than ntg_chol_factor_tc_workspace_bytes");
+  int rc = attrs_once();
+  if (rc) return rc;
+  cudaStream_t s = as_stream(stream);
+  const FactorWs f = factor_ws(workspace, n);
+  if (cudaMemsetAsync(info, 0, sizeof(int), s) != cudaSuccess)
+    return check_launch("ntg_chol_factor_tc memset");
+  trace_tc_kernel<<<1, 1024, 0, s>>>(A, n, lambda + 1);
+  init_factor_ld_kernel<<<grid_for(n * ldl), 256, 0, s>>>(A, n, ldl, diag_reg, absolute,
+                                                          lambda + 1, L, lambda);
+  note_launch(2);
+  const int64_t nblk = (n + PB - 1) / PB;
+  for (int64_t b = 0; b < nblk; ++b) {
+    const int64_t k = b * PB;
+    diag_block_kernel<<<1, 512, kDiagSmem, s>>>(L, ldl, n, k, info, f.linv + b * PB * PB,
+                                                f.linvT + b * PB * PB);
+    note_launch();
+    const int64_t rest = n - k - PB;
+    if (rest > 0) {
+      const int64_t grid = mini(ceil_div(rest, 16), 2 * 152);
+      panel_trsm_kernel<<<(unsigned)grid, 512, kPanelSmem, s>>>(L, ldl, n, k);
+      note_launch();
+      float* l21 = L + (k + PB) * ldl + k;
+      rc = gemm_tf32x3(s, l21, ldl, l21, ldl, L + (k + PB) * ldl + k + PB, ldl, rest, rest, PB,
+                       -1.f, 1.f, 1);
+      if (rc) return rc;
+    }
+  }
+  dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
+  transpose_kernel<<<g, 256, 0, s>>>(L, ldl, f.u, ldl, n, n);
+  note_launch();
+  return check_launch("ntg_chol_factor_tc");
+}
+
+extern "C" size_t ntg_chol_solve_tc_workspace_bytes(int64_t n, int64_t m, int64_t ldl) {
+  if (n <= 0 || m <= 0 || ldl < n || n > 46340) return SIZE_MAX;
+  const uint64_t per = sizeof(double) + sizeof(float) + sizeof(float);
+  if ((uint64_t)m > ((uint64_t)INT64_MAX / per) / (uint64_t)ldl) return SIZE_MAX;
+  return solve_ws_bytes(n, m, ldl);
+}
+
+extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, int64_t ldl,
+                                 const void* factor_workspace, const double* lambda, int64_t n,
+                                 const float* B, int64_t m, float* X, int32_t refine_iters,
+                                 void* workspace, size_t workspace_bytes,
+                                 double* final_residual) {
+  NTG_REQUIRE(A && L && factor_workspace && lambda && B && X && workspace,
+              "ntg_chol_solve_tc: null pointer");
+  NTG_REQUIRE(n > 0 && n <= 46340 && m > 0, "ntg_chol_solve_tc: bad sizes");
+  NTG_REQUIRE(ldl >= n && ldl % 4 == 0, "ntg_chol_solve_tc: bad ldl");
+  NTG_REQUIRE(refine_iters >= 0 && refine_iters <= 16, "ntg_chol_solve_tc: 0..16 refinement steps");
+  NTG_REQUIRE(m <= (1ll << 31) / 64, "ntg_chol_solve_tc: too many right-hand sides");
+  NTG_REQUIRE(workspace_bytes >= ntg_chol_solve_tc_workspace_bytes(n, m, ldl),
+              "ntg_chol_solve_tc: workspace smaller than ntg_chol_solve_tc_workspace_bytes");
+  int rc = attrs_once();
+  if (rc) return rc;
+  cudaStream_t s = as_stream(stream);
+  const FactorWs f = factor_ws(const_cast<void*>(factor_workspace), n);
+  char* ws = static_cast<char*>(workspace);
+  const int64_t nblk = (n + PB - 1) / PB;
+  double* rnorm = reinterpret_cast<double*>(ws);
+  double* x64 = reinterpret_cast<double*>(ws + 256);
+  float* r32 = reinterpret_cast<float*>(x64 + n * m);
+  int* flags = reinterpret_cast<int*>(r32 + n * m);
+  float* z = reinterpret_cast<float*>(
+      (reinterpret_cast<uintptr_t>(flags + 2 * nblk) + 255) & ~(uintptr_t)255);
+  auto solve = [&](float* xx) -> int {
+    if (m <= kSmallM) {
+      int r = coop_trsv(s, L, ldl, f, n, xx, m, flags, 0);
+      if (r) return r;
+      return coop_trsv(s, L, ldl, f, n, xx, m, flags + nblk, 1);
+    }
+    return gemm_trsm(s, L, ldl, f, n, xx, m, z, ldl);
+  };
+  if (cudaMemcpyAsync(X, B, sizeof(float) * n * m, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return check_launch("ntg_chol_solve_tc copy");
+  rc = solve(X);
+  if (rc) return rc;
+  if (refine_iters == 0 && !final_residual) return check_launch("ntg_chol_solve_tc");
+  to_double_tc_kernel<<<grid_for(n * m), 256, 0, s>>>(X, x64, n * m);
+  note_launch();
+  for (int it = 0; it <= refine_iters; ++it) {
+    if (it == refine_iters && !final_residual) break;
+    if (cudaMemsetAsync(rnorm, 0, sizeof(double), s) != cudaSuccess)
+      return check_launch("ntg_chol_solve_tc memset");
+    if (m <= 4)
+      residual64_rows_kernel<4><<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(A, n, lambda, B, x64, m,
+                                                                         r32, rnorm);
+    else if (m <= kSmallM)
+      residual64_rows_kernel<kSmallM><<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(
+          A, n, lambda, B, x64, m, r32, rnorm);
+    else
+      residual_df_kernel<<<dim3((unsigned)ceil_div(m, 64), (unsigned)ceil_div(n, 64)), 256, 0,
+                           s>>>(A, n, lambda, B, x64, m, r32, rnorm);
+    note_launch();
+    if (it == refine_iters) break;
+    rc = solve(r32);
+    if (rc) return rc;
+    accumulate_tc_kernel<<<grid_for(n * m), 256, 0, s>>>(x64, r32, X, n * m);
+    note_launch();
+  }
+  if (final_residual &&
+      cudaMemcpyAsync(final_residual, rnorm, sizeof(double), cudaMemcpyDeviceToDevice, s) !=
+          cudaSuccess)
+    return check_launch("ntg_chol_solve_tc residual copy");
+  return check_launch("ntg_chol_solve_tc");
+}
+
+extern "C" int ntg_chol_logdet_tc(void* stream, const float* L, int64_t n, int64_t ldl,
+                                  double* out) {
+  NTG_REQUIRE(L && out && n > 0 && ldl >= n, "ntg_chol_logdet_tc: bad arguments");
+  logdet_ld_kernel<<<1, 1024, 0, as_stream(stream)>>>(L, n, ldl, out);
+  note_launch();
+  return check_launch("ntg_chol_logdet_tc");
+}

@@ -23,6 +23,8 @@ int32_t tune(int32_t knob);  // current value of an NTG_TUNE_* knob
 // and of the tensor-core Gram (ntg_gram_tc.cu); -1 if the read failed.
 int bwd_take_device_error();
 int gram_take_device_error();
+int gemm_take_device_error();  // ntg_gemm_tc.cu
+int chol_take_device_error();  // ntg_chol_tc.cu
 
 // Tensor-core (tcgen05) split-precision Gram; defined in ntg_gram_tc.cu.
 int gram_tc(cudaStream_t stream, const float* x1, const float* x2, int64_t n1, int64_t n2,

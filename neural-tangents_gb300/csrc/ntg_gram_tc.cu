@@ -10,14 +10,12 @@
 // bounded: a wait that runs out sets the error words (the workspace word and
 // the library's device word read by ntg_device_status), waits (bounded) for the
 // copies and MMAs already issued, frees its tensor memory and returns.
-#include <cuda.h>
 #include <cuda_bf16.h>
-#include <cudaTypedefs.h>
 
 #include <mutex>
 #include <string>
 
-#include "ntg_common.cuh"
+#include "ntg_tc.cuh"
 
 namespace ntg {
 namespace {
@@ -46,58 +44,20 @@ __global__ void split_bf16_kernel(const float* __restrict__ x, int64_t n, int64_
   }
 }
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
+using tc::commit;
+using tc::mbar_expect_tx;
+using tc::mbar_init;
+using tc::smem_u32;
+using tc::tma_load_2d;
 
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-               : "memory");
-}
-
-// Bounded wait for the phase with the given parity; false on timeout.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (uint64_t it = 0; it < WAIT_LIMIT; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
+  return tc::mbar_wait(bar, parity, WAIT_LIMIT);
 }
 
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar,
-                                            int32_t x, int32_t y) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
-      : "memory");
-}
-
-// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row
-// groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-  uint64_t d = 0;
-  d |= (uint64_t)((addr & 0x3FFFF) >> 4);        // start address
-  d |= (uint64_t)1 << 16;                        // leading byte offset (unused for SW128 K-major)
-  d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset
-  d |= (uint64_t)1 << 46;                        // descriptor version
-  d |= (uint64_t)2 << 61;                        // SWIZZLE_128B
-  return d;
-}
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) { return tc::smem_desc_sw128(addr); }
 
 // Instruction descriptor, kind::f16: D F32, A/B BF16, both K-major, M=128, N=128.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+constexpr uint32_t IDESC = tc::idesc(1, BM, BN);
 
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t acc) {
   asm volatile(
@@ -106,11 +66,7 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b
       "l"(a), "l"(b), "r"(IDESC), "r"(acc));
 }
 
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-      : "memory");
-}
+__device__ __forceinline__ void mma_commit(uint32_t bar) { commit(bar); }
 
 __global__ void __launch_bounds__(128, 1)
     gram_tc_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
@@ -255,32 +211,9 @@ __global__ void __launch_bounds__(128, 1)
   }
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static std::once_flag once;
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  std::call_once(once, [] {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                         &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  });
-  return fn;
-}
-
 int make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t dpad) {
-  auto fn = encode_fn();
-  if (!fn) return fail(NTG_ERR_CUDA, "ntg_gram: cuTensorMapEncodeTiled unavailable");
-  cuuint64_t dims[2] = {(cuuint64_t)dpad, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)(dpad * 2)};
-  cuuint32_t box[2] = {BK, BM};
-  cuuint32_t es[2] = {1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
-                  box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return fail(NTG_ERR_CUDA, "ntg_gram: cuTensorMapEncodeTiled failed");
-  return NTG_OK;
+  return tc::make_map_2d(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, rows, dpad, dpad, BM, BK,
+                         "ntg_gram");
 }
 
 }  // namespace

@@ -2200,10 +2200,12 @@ extern "C" int ntg_device_status(void) {
   if (v != 0 && cudaMemcpyToSymbol(g_device_error, &zero, sizeof(int)) != cudaSuccess)
     return check_launch("ntg_device_status");
   // every word is read and cleared, so one timeout is reported once
-  const int vb = bwd_take_device_error();
-  const int vg = gram_take_device_error();
-  if (vb < 0 || vg < 0) return check_launch("ntg_device_status");
-  if (v == 0) v = vb ? vb : vg;
+  const int others[4] = {bwd_take_device_error(), gram_take_device_error(),
+                         gemm_take_device_error(), chol_take_device_error()};
+  for (int o : others) {
+    if (o < 0) return check_launch("ntg_device_status");
+    if (v == 0) v = o;
+  }
   if (v != 0) return fail(v, "a bounded device wait ran out in a streamed kernel");
   return NTG_OK;
 }

@@ -6,9 +6,11 @@ NNGP / NTK / NTKGP posterior and the infinite-ensemble predictions on the same k
 ``gradient_descent_mse(k_train_train, y_train, ...)`` keeps the reference
 signature (predict.py:71-278) and returns ``predict_fn(t=None, fx_train_0=0.,
 fx_test_0=None, k_test_train=None)``. ``t=None`` (infinite time) and a scalar
-``t=inf`` take the Cholesky path: an FP32 Cholesky of K + lambda I on the GPU, FP32 triangular
-solves and FP64 iterative refinement (`refine_iters`, default 2; 0 gives the
-plain FP32 solve), all in libntgb300.so. The factorisation is computed once
+``t=inf`` take the Cholesky path: an FP32 Cholesky of K + lambda I on the GPU (128-wide panels,
+trailing updates on the tcgen05 tensor cores), FP32 triangular solves and
+iterative refinement with the residual accumulated in FP64 (or double-float for
+more than 16 right-hand sides; `refine_iters`, default 2; 0 gives the plain
+FP32 solve), all in libntgb300.so. The factorisation is computed once
 and cached, as the reference caches it (predict.py:163). Finite ``t`` uses the
 eigendecomposition of predict.py:185-229 through torch.linalg.eigh (a cuSOLVER
 library call) in float64. Only 2-D ``k_train_train`` with ``trace_axes=(-1,)``
@@ -42,18 +44,26 @@ def _gemm(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
 
 
 class CholeskySolver:
-    """Cached factorisation of K + lambda I (predict.py:1224-1258)."""
+    """Cached factorisation of K + lambda I (predict.py:1224-1258) on the tensor-core
+    Cholesky kernels: L lives in a [n, ldl] buffer (ldl = n rounded up to 32, the row
+    pitch the TMA loads of the trailing updates need); the factor workspace keeps the
+    inverses of the 128-wide diagonal blocks and L^T for the solves."""
 
     def __init__(self, k: torch.Tensor, diag_reg: float, absolute: bool, refine_iters: int = 2):
         n = k.shape[0]
         if k.ndim != 2 or k.shape[1] != n:
             raise NotImplementedError('nt_gb300 supports a 2-D square k_train_train')
+        lib = L.load()
         self.k, self.n, self.refine = k, n, int(refine_iters)
-        self.L = torch.empty_like(k)
+        self.ldl = (n + 31) // 32 * 32
+        self.Lbuf = torch.empty((n, self.ldl), device=k.device, dtype=torch.float32)
+        fws = int(lib.ntg_chol_factor_tc_workspace_bytes(n, self.ldl))
+        self.fws = torch.empty((fws,), device=k.device, dtype=torch.uint8)
         self.lam = torch.zeros((2,), device=k.device, dtype=torch.float64)
         info = torch.zeros((1,), device=k.device, dtype=torch.int32)
-        L.call('ntg_chol_factor', L.stream(), L.ptr(k), n, float(diag_reg), int(bool(absolute)),
-               L.ptr(self.L), self.lam.data_ptr(), info.data_ptr())
+        L.call('ntg_chol_factor_tc', L.stream(), L.ptr(k), n, float(diag_reg),
+               int(bool(absolute)), self.Lbuf.data_ptr(), self.ldl, self.lam.data_ptr(),
+               info.data_ptr(), self.fws.data_ptr(), fws)
         self.info = int(info.item())
         if self.info:
             warnings.warn(f'k_train_train + diag_reg * I is not positive definite (pivot '
@@ -61,31 +71,41 @@ class CholeskySolver:
                           f'would return.')
         self.residual = None
 
-    COLS = 2048  # right-hand sides per ntg_chol_solve call (bounds the FP64 workspace)
+    @property
+    def L(self) -> torch.Tensor:
+        """The lower factor as an [n, n] view of its padded buffer."""
+        return self.Lbuf[:, :self.n]
+
+    def logdet(self) -> torch.Tensor:
+        """log det(K + lambda I) = 2 sum log L_ii (device float64, shape [1])."""
+        out = torch.zeros(1, device=self.k.device, dtype=torch.float64)
+        L.call('ntg_chol_logdet_tc', L.stream(), self.Lbuf.data_ptr(), self.n, self.ldl,
+               out.data_ptr())
+        return out
+
+    COLS = 4096  # right-hand sides per ntg_chol_solve_tc call (bounds its workspace)
 
     def solve(self, b: torch.Tensor, refine_iters: Optional[int] = None,
               residual: bool = True) -> torch.Tensor:
-        """A^{-1} b; refine_iters overrides the solver's FP64 refinement steps;
-        residual=False skips the final FP64 residual kept in self.residual."""
+        """A^{-1} b; refine_iters overrides the solver's refinement steps; residual=False
+        skips the final residual kept in self.residual."""
         refine = self.refine if refine_iters is None else int(refine_iters)
         b = b.reshape(self.n, -1).contiguous()
         if self.info:
             return torch.full_like(b, float('nan'))
         out = torch.empty_like(b)
         cols = min(b.shape[1], self.COLS)
-        if refine or residual:
-            ws_bytes = int(L.load().ntg_chol_workspace_bytes(self.n, cols))
-            ws = torch.empty((ws_bytes,), device=b.device, dtype=torch.uint8)
-        else:  # plain FP32 solve: no workspace
-            ws_bytes, ws = 0, None
+        lib = L.load()
+        ws_bytes = int(lib.ntg_chol_solve_tc_workspace_bytes(self.n, cols, self.ldl))
+        ws = torch.empty((ws_bytes,), device=b.device, dtype=torch.uint8)
         res = torch.zeros((1,), device=b.device, dtype=torch.float64) if residual else None
         single = b.shape[1] <= cols
         for c0 in range(0, b.shape[1], cols):
             bc = b if single else b[:, c0:c0 + cols].contiguous()
             xc = out if single else torch.empty_like(bc)
-            L.call('ntg_chol_solve', L.stream(), L.ptr(self.k), L.ptr(self.L),
-                   self.lam.data_ptr(), self.n, L.ptr(bc), bc.shape[1], L.ptr(xc), refine,
-                   None if ws is None else ws.data_ptr(), ws_bytes,
+            L.call('ntg_chol_solve_tc', L.stream(), L.ptr(self.k), self.Lbuf.data_ptr(), self.ldl,
+                   self.fws.data_ptr(), self.lam.data_ptr(), self.n, L.ptr(bc), bc.shape[1],
+                   L.ptr(xc), refine, ws.data_ptr(), ws_bytes,
                    None if res is None else res.data_ptr())
             if not single:
                 out[:, c0:c0 + cols] = xc
@@ -192,8 +212,7 @@ class _NLL(torch.autograd.Function):
         n, m = y.shape
         solver = CholeskySolver(k, diag_reg, absolute, refine_iters)
         alpha = solver.solve(y)
-        ld = torch.zeros(1, device=k.device, dtype=torch.float64)
-        L.call('ntg_chol_logdet', L.stream(), L.ptr(solver.L), n, ld.data_ptr())
+        ld = solver.logdet()
         quad = _gemm(y.reshape(1, -1).contiguous(), alpha.reshape(-1, 1).contiguous())
         nll = 0.5 * quad.reshape(()).double() + 0.5 * m * ld[0] + 0.5 * n * m * math.log(2 * math.pi)
         ctx.solver, ctx.alpha, ctx.meta = solver, alpha, (diag_reg, absolute, n, m)
