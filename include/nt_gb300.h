@@ -289,12 +289,17 @@ int ntg_chol_factor_tc(void* stream, const float* A, int64_t n, double diag_reg,
                        float* L, int64_t ldl, double* lambda, int* info, void* factor_workspace,
                        size_t factor_workspace_bytes);
 /* X = (K + lambda I)^{-1} B, B and X [n, m] row-major, from a factor of
- * ntg_chol_factor_tc: for m <= 16 two cooperative launches (block-triangular
- * solves with the stored inverses of the diagonal blocks, blocks handed on by
- * flags under bounded waits), for more right-hand sides blocked solves whose
- * updates run on ntg_gemm_tc. refine_iters steps of iterative refinement keep X in
- * FP64 with the residual accumulated in FP64 (m <= 16) or double-float arithmetic
- * (two FP32 words; m > 16). final_residual as ntg_chol_solve. */
+ * ntg_chol_factor_tc. Triangular solves: for m <= 16 two cooperative launches
+ * (block-triangular solves with the stored inverses of the diagonal blocks, blocks
+ * handed on by flags under bounded waits), for more right-hand sides blocked solves
+ * whose updates run on ntg_gemm_tc. Refinement keeps X in FP64 and accumulates the
+ * products with K in double-float arithmetic (two FP32 words, about 44 significant
+ * bits): for m <= 16 at most refine_iters iterations of conjugate gradients
+ * preconditioned by the FP32 factor, each column stopping once max |residual| <=
+ * 1e-13 max |b| (converges where plain refinement stalls, cond(K) * u > 1); for
+ * m > 16 refine_iters steps of x <- x + (L L^T)^{-1} (b - (K + lambda I) x).
+ * final_residual (device double, optional) receives max |b - (K + lambda I) X| of
+ * the returned X. */
 size_t ntg_chol_solve_tc_workspace_bytes(int64_t n, int64_t m, int64_t ldl);
 int ntg_chol_solve_tc(void* stream, const float* A, const float* L, int64_t ldl,
                       const void* factor_workspace, const double* lambda, int64_t n,
@@ -302,6 +307,28 @@ int ntg_chol_solve_tc(void* stream, const float* A, const float* L, int64_t ldl,
                       size_t workspace_bytes, double* final_residual);
 /* log det(L L^T) of a factor of ntg_chol_factor_tc -> out[0] (device double). */
 int ntg_chol_logdet_tc(void* stream, const float* L, int64_t n, int64_t ldl, double* out);
+
+/* ---- finite-time predictions (predict.py:185-229, 860-1005, 1180-1294) ---- */
+/* Eigendecomposition of the symmetric K + shift I (K [n, n] float32), the eigh of
+ * the reference's _get_fns_in_eigenbasis: two-sided block Jacobi in FP32 (32-wide
+ * blocks, every pair of blocks diagonalised per round by one CTA, the rotations
+ * applied to K and to the eigenvectors tile by tile). Sweeps run until the
+ * off-diagonal Frobenius norm is at most tol times the whole norm, or max_sweeps;
+ * evals [n] (not sorted) and evecs [n, n] (column j belongs to evals[j]) are
+ * written, *sweeps_out (host int, may be NULL) receives the sweeps run. Reads one
+ * 16-byte norm back after each sweep: synchronises the stream once per sweep. */
+size_t ntg_eigh_workspace_bytes(int64_t n);
+int ntg_eigh(void* stream, const float* K, int64_t n, double shift, float* evals, float* evecs,
+             int32_t max_sweeps, double tol, void* workspace, size_t workspace_bytes,
+             int32_t* sweeps_out);
+/* out[i, t, c] = w(lambda_i, t_t) x[i, c] for x [n, m], times t [nt] (device doubles,
+ * already scaled by the learning rate) and the spectral function `kind` (pos =
+ * max(lambda, 0), N = norm): 0 expm1(-pos t/N), 1 expm1(-pos t/N)/|lambda|,
+ * 2 pos exp(-2 pos t/N), 3 exp(-pos t/N), 4 -expm1(-2 pos t/N)/|lambda|,
+ * 5 -expm1(-pos t/N), 6 -expm1(-pos t/N)/|lambda| (predict.py:1277-1294 and the
+ * ensemble covariances of :860-1005), evaluated in FP64. */
+int ntg_spectral_scale(void* stream, const float* evals, const double* ts, int64_t nt, int32_t kind,
+                       double norm, const float* x, int64_t n, int64_t m, float* out);
 
 /* ---- adjoints (reverse mode; the jax.custom_vjp backward rules) -------- */
 /* Derivative conventions follow the reference's custom JVPs: the square root

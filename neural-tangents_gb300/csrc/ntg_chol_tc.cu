@@ -17,10 +17,12 @@
 // soon as its flag is set (bounded waits) and applies the stored inverse of its
 // diagonal block; for more right-hand sides, blocked right-looking solves on the
 // transposed right-hand sides whose updates are 3xTF32 tensor-core GEMMs.
-// Iterative refinement x <- x + A^{-1} (b - A x) keeps x in FP64; the residual
-// is accumulated in FP64 for up to kSmallM right-hand sides and in double-float
-// (two-FP32, error-free products and sums) for more, where FP64 throughput
-// would make the n^2 m residual the dominant cost.
+// Refinement keeps x in FP64 and accumulates every product with K in
+// double-float (two FP32 words, error-free products and sums; about 44
+// significant bits), which the GB300's FP32 rate makes about 6x cheaper than
+// FP64: for up to kSmallM right-hand sides preconditioned conjugate gradients
+// (the FP32 factor as preconditioner; converges where plain refinement stalls,
+// kappa u > 1), for more, refine_iters steps of x <- x + A^{-1} (b - A x).
 #include <cooperative_groups.h>
 
 #include <mutex>
@@ -295,7 +297,8 @@ __device__ __forceinline__ bool wait_flag(const int* flag, int want) {
 __global__ void __launch_bounds__(256)
     trsv_coop_kernel(const float* __restrict__ L, int64_t ldl, const float* __restrict__ linv,
                      const float* __restrict__ linvT, int64_t n, float* X, int64_t m,
-                     int* flags, int backward) {
+                     int* flags, int backward, const int* skip) {
+  if (skip && *reinterpret_cast<const volatile int*>(skip)) return;  // uniform: no CTA waits
   extern __shared__ float sm[];
   float(*blk)[PBS] = reinterpret_cast<float(*)[PBS]>(sm);        // an L block or Linv
   float(*yj)[kSmallM + 1] = reinterpret_cast<float(*)[kSmallM + 1]>(sm + PB * PBS);
@@ -375,41 +378,16 @@ constexpr size_t kTrsvSmem = (size_t)(PB * PBS + 2 * PB * (kSmallM + 1)) * sizeo
 // Residuals R = B - (A + lambda I) X with X in FP64.
 // ---------------------------------------------------------------------------
 
-// FP64, one warp per row, up to MR right-hand sides in registers.
-template <int MR>
-__global__ void __launch_bounds__(256)
-    residual64_rows_kernel(const float* __restrict__ A, int64_t n, const double* lambda,
-                           const float* __restrict__ B, const double* __restrict__ X, int64_t m,
-                           float* __restrict__ R, double* __restrict__ rnorm) {
-  const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-  const int lane = threadIdx.x & 31;
-  if (row >= n) return;
-  const float* ar = A + row * n;
-  double acc[MR];
+__global__ void max_abs64_kernel(const double* __restrict__ v, int64_t n, double* __restrict__ out) {
+  double mx = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    mx = fmax(mx, fabs(v[i]));
 #pragma unroll
-  for (int c = 0; c < MR; ++c) acc[c] = 0.0;
-  for (int64_t j = lane; j < n; j += 32) {
-    const double a = (double)ar[j];
-    const double* xr = X + j * m;
-#pragma unroll
-    for (int c = 0; c < MR; ++c)
-      if (c < m) acc[c] = fma(a, xr[c], acc[c]);
-  }
-  double rmax = 0.0;
-#pragma unroll
-  for (int c = 0; c < MR; ++c) {
-    double v = acc[c];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (c < m && lane == 0) {
-      const double r = (double)B[row * m + c] - v - lambda[0] * X[row * m + c];
-      R[row * m + c] = (float)r;
-      rmax = fmax(rmax, fabs(r));
-    }
-  }
-  if (lane == 0 && rmax > 0.0)
-    atomicMax(reinterpret_cast<unsigned long long*>(rnorm),
-              (unsigned long long)__double_as_longlong(rmax));
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0 && mx > 0.0)
+    atomicMax(reinterpret_cast<unsigned long long*>(out),
+              (unsigned long long)__double_as_longlong(mx));
 }
 
 // Double-float accumulation (s_hi, s_lo) += a * (x_hi + x_lo): a * x_hi is split
@@ -502,6 +480,219 @@ __global__ void accumulate_tc_kernel(double* __restrict__ x, const float* __rest
   }
 }
 
+// ---------------------------------------------------------------------------
+// Preconditioned conjugate gradients for up to kSmallM right-hand sides: the
+// FP32 factor L L^T preconditions (K + lambda I) d = r, with x, r, p, q in FP64
+// and the products (K + lambda I) v accumulated in double-float. Each column
+// stops (its step sizes become 0) once max |r| <= kPcgTol max |b|; when every
+// column has stopped the remaining launches return at once.
+// ---------------------------------------------------------------------------
+constexpr double kPcgTol = 1e-13;
+constexpr int kDotBlocks = 128;
+
+struct PcgState {
+  double rho[2][kSmallM];   // r.z of the current / next iteration
+  double bnorm[kSmallM];    // max |b_j|
+  double rmax[kSmallM];     // max |r_j| of the last residual
+  int active[kSmallM];
+  int all_done;
+};
+
+__device__ __forceinline__ void df_add(float& sh, float& sl, float bh, float bl) {
+  const float s = sh + bh;
+  const float bv = s - sh;
+  const float e = (sh - (s - bv)) + (bh - bv);
+  sl += e + bl;
+  sh = s;
+}
+
+// out = B - (K + lambda I) X (subtract = 1) or (K + lambda I) X (subtract = 0), X FP64
+// [n, m]; one warp per row, double-float sums of the m <= MR products kept per lane.
+template <int MR>
+__global__ void __launch_bounds__(256)
+    matvec_df_rows_kernel(const float* __restrict__ A, int64_t n, const double* lambda,
+                          const float* __restrict__ B, const double* __restrict__ X, int64_t m,
+                          int subtract, double* __restrict__ out, float* __restrict__ out32,
+                          const PcgState* st) {
+  if (st && st->all_done) return;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float* ar = A + row * n;
+  float sh[MR], sl[MR];
+#pragma unroll
+  for (int c = 0; c < MR; ++c) sh[c] = sl[c] = 0.f;
+  for (int64_t j = lane; j < n; j += 32) {
+    const float a = ar[j];
+    const double* xr = X + j * m;
+#pragma unroll
+    for (int c = 0; c < MR; ++c)
+      if (c < m) {
+        const double xv = xr[c];
+        const float xh = (float)xv;
+        df_fma(a, xh, (float)(xv - (double)xh), sh[c], sl[c]);
+      }
+  }
+#pragma unroll
+  for (int c = 0; c < MR; ++c) {
+    if (c >= m) break;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, sh[c], o);
+      const float ol = __shfl_xor_sync(0xffffffffu, sl[c], o);
+      df_add(sh[c], sl[c], oh, ol);
+    }
+    if (lane == 0) {
+      const double v = (double)sh[c] + (double)sl[c] + lambda[0] * X[row * m + c];
+      const double r = subtract ? (double)B[row * m + c] - v : v;
+      out[row * m + c] = r;
+      if (out32) out32[row * m + c] = (float)r;
+    }
+  }
+}
+
+// part[blk][j] = sum over the block's rows of u[i, j] * v[i, j] (v FP64, or vf FP32).
+__global__ void __launch_bounds__(256)
+    col_dots_kernel(const double* __restrict__ u, const double* __restrict__ v,
+                    const float* __restrict__ vf, int64_t n, int64_t m, double* __restrict__ part,
+                    const PcgState* st) {
+  if (st->all_done) return;
+  __shared__ double red[8][kSmallM];
+  double acc[kSmallM];
+#pragma unroll
+  for (int c = 0; c < kSmallM; ++c) acc[c] = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+#pragma unroll
+    for (int c = 0; c < kSmallM; ++c)
+      if (c < m) acc[c] = fma(u[i * m + c], vf ? (double)vf[i * m + c] : v[i * m + c], acc[c]);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < kSmallM; ++c) {
+    double x = acc[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp][c] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < m) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w][threadIdx.x];
+    part[blockIdx.x * kSmallM + threadIdx.x] = t;
+  }
+}
+
+__device__ __forceinline__ double sum_parts(const double* part, int c) {
+  double t = 0.0;
+  for (int b = 0; b < kDotBlocks; ++b) t += part[b * kSmallM + c];
+  return t;
+}
+
+// Set-up: bnorm, rho[0] = r.z (from part), p = z, every column active.
+__global__ void pcg_init_kernel(const float* __restrict__ B, const float* __restrict__ z,
+                                double* __restrict__ p, int64_t n, int64_t m,
+                                const double* __restrict__ part, PcgState* st) {
+  __shared__ double bmax[kSmallM];
+  if (threadIdx.x < kSmallM) bmax[threadIdx.x] = 0.0;
+  __syncthreads();
+  for (int64_t i = threadIdx.x; i < n * m; i += blockDim.x) {
+    p[i] = (double)z[i];
+    const int c = (int)(i % m);
+    atomicMax(reinterpret_cast<unsigned long long*>(&bmax[c]),
+              (unsigned long long)__double_as_longlong(fabs((double)B[i])));
+  }
+  __syncthreads();
+  if (threadIdx.x < m) {
+    const int c = threadIdx.x;
+    st->bnorm[c] = bmax[c];
+    st->rho[0][c] = sum_parts(part, c);
+    st->rmax[c] = 0.0;
+    st->active[c] = 1;
+  }
+  if (threadIdx.x == 0) st->all_done = 0;
+}
+
+// x += alpha p, r -= alpha q (alpha_c = rho_c / p.q), r32 = (float) r; the block's
+// max |r_c| into rpart.
+__global__ void __launch_bounds__(256)
+    pcg_step_kernel(double* __restrict__ x, double* __restrict__ r, float* __restrict__ r32,
+                    const double* __restrict__ p, const double* __restrict__ q, int64_t n,
+                    int64_t m, const double* __restrict__ pq_part, double* __restrict__ rpart,
+                    PcgState* st, int cur) {
+  if (st->all_done) return;
+  __shared__ double alpha[kSmallM];
+  __shared__ double rmax[kSmallM];
+  if (threadIdx.x < m) {
+    const int c = threadIdx.x;
+    const double pq = sum_parts(pq_part, c);
+    alpha[c] = (st->active[c] && pq != 0.0) ? st->rho[cur][c] / pq : 0.0;
+    rmax[c] = 0.0;
+  }
+  __syncthreads();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * m; i += stride) {
+    const int c = (int)(i % m);
+    const double a = alpha[c];
+    x[i] = fma(a, p[i], x[i]);
+    const double rv = fma(-a, q[i], r[i]);
+    r[i] = rv;
+    r32[i] = (float)rv;
+    atomicMax(reinterpret_cast<unsigned long long*>(&rmax[c]),
+              (unsigned long long)__double_as_longlong(fabs(rv)));
+  }
+  __syncthreads();
+  if (threadIdx.x < m) rpart[blockIdx.x * kSmallM + threadIdx.x] = rmax[threadIdx.x];
+}
+
+// Convergence: max |r_c| over the blocks' maxima; a column at or below kPcgTol max |b_c|
+// stops; all_done once none is left.
+__global__ void pcg_check_kernel(const double* __restrict__ rpart, int64_t m, int nblocks,
+                                 PcgState* st) {
+  if (st->all_done) return;
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  if (threadIdx.x < m) {
+    const int c = threadIdx.x;
+    double mx = 0.0;
+    for (int b = 0; b < nblocks; ++b) mx = fmax(mx, rpart[b * kSmallM + c]);
+    st->rmax[c] = mx;
+    if (st->active[c] && mx <= kPcgTol * st->bnorm[c]) st->active[c] = 0;
+    if (st->active[c]) atomicOr(&any, 1);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && !any) st->all_done = 1;
+}
+
+// beta_c = (r.z)_new / rho_c; p = z + beta p; rho[nxt] = (r.z)_new.
+__global__ void __launch_bounds__(256)
+    pcg_dir_kernel(double* __restrict__ p, const float* __restrict__ z, int64_t n, int64_t m,
+                   const double* __restrict__ rz_part, PcgState* st, int cur) {
+  if (st->all_done) return;
+  __shared__ double beta[kSmallM];
+  const int nxt = cur ^ 1;
+  if (threadIdx.x < m) {
+    const int c = threadIdx.x;
+    const double rz = sum_parts(rz_part, c);
+    beta[c] = st->rho[cur][c] != 0.0 ? rz / st->rho[cur][c] : 0.0;
+    if (blockIdx.x == 0) st->rho[nxt][c] = rz;
+  }
+  __syncthreads();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * m; i += stride) {
+    const int c = (int)(i % m);
+    if (st->active[c]) p[i] = fma(beta[c], p[i], (double)z[i]);
+  }
+}
+
+__global__ void copy_to_float_kernel(const double* __restrict__ a, float* __restrict__ b,
+                                     int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
 __global__ void logdet_ld_kernel(const float* __restrict__ L, int64_t n, int64_t ldl,
                                  double* __restrict__ out) {
   double s = 0.0;
@@ -567,15 +758,19 @@ FactorWs factor_ws(void* ws, int64_t n) {
 
 // Solve workspace: rnorm (256 B), x64 [n m] f64, r32 [n m] f32, flags [2 nblk] i32,
 // z [m_pad * ldz] f32 for the many-right-hand-side path (ldz = ldl).
+// For m <= kSmallM the PCG vectors follow: r64, p64, q64 [n m] f64, three dot-product
+// partial arrays [kDotBlocks * kSmallM] f64 and the PcgState.
 size_t solve_ws_bytes(int64_t n, int64_t m, int64_t ldl) {
   const int64_t nblk = (n + PB - 1) / PB;
   size_t b = 256 + (size_t)n * m * (sizeof(double) + sizeof(float)) + 2 * nblk * sizeof(int) + 256;
   if (m > kSmallM) b += (size_t)m * ldl * sizeof(float) + 256;
+  else b += (size_t)3 * n * m * sizeof(double) + 3 * kDotBlocks * kSmallM * sizeof(double) +
+            sizeof(PcgState) + 256;
   return (b + 255) & ~(size_t)255;
 }
 
 int coop_trsv(cudaStream_t s, const float* L, int64_t ldl, const FactorWs& f, int64_t n,
-              float* X, int64_t m, int* flags, int backward) {
+              float* X, int64_t m, int* flags, int backward, const int* skip = nullptr) {
   const int64_t nblk = (n + PB - 1) / PB;
   if (cudaMemsetAsync(flags, 0, sizeof(int) * nblk, s) != cudaSuccess)
     return check_launch("ntg_chol_solve_tc flags");
@@ -594,7 +789,7 @@ int coop_trsv(cudaStream_t s, const float* L, int64_t ldl, const FactorWs& f, in
   const float* linvT = f.linvT;
   int bw = backward;
   void* args[] = {(void*)&L, (void*)&ldl, (void*)&linv, (void*)&linvT, (void*)&n, (void*)&X,
-                  (void*)&m, (void*)&flags, (void*)&bw};
+                  (void*)&m, (void*)&flags, (void*)&bw, (void*)&skip};
   const cudaError_t e = cudaLaunchCooperativeKernel((const void*)trsv_coop_kernel, grid, 256,
                                                     args, kTrsvSmem, s);
   note_launch();
@@ -741,37 +936,83 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
   int* flags = reinterpret_cast<int*>(r32 + n * m);
   float* z = reinterpret_cast<float*>(
       (reinterpret_cast<uintptr_t>(flags + 2 * nblk) + 255) & ~(uintptr_t)255);
-  auto solve = [&](float* xx) -> int {
+  auto solve = [&](float* xx, const int* skip) -> int {
     if (m <= kSmallM) {
-      int r = coop_trsv(s, L, ldl, f, n, xx, m, flags, 0);
+      int r = coop_trsv(s, L, ldl, f, n, xx, m, flags, 0, skip);
       if (r) return r;
-      return coop_trsv(s, L, ldl, f, n, xx, m, flags + nblk, 1);
+      return coop_trsv(s, L, ldl, f, n, xx, m, flags + nblk, 1, skip);
     }
     return gemm_trsm(s, L, ldl, f, n, xx, m, z, ldl);
   };
   if (cudaMemcpyAsync(X, B, sizeof(float) * n * m, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
     return check_launch("ntg_chol_solve_tc copy");
-  rc = solve(X);
+  rc = solve(X, nullptr);
   if (rc) return rc;
   if (refine_iters == 0 && !final_residual) return check_launch("ntg_chol_solve_tc");
   to_double_tc_kernel<<<grid_for(n * m), 256, 0, s>>>(X, x64, n * m);
   note_launch();
+  if (m <= kSmallM) {
+    // preconditioned conjugate gradients on (K + lambda I) x = b from x0 = (L L^T)^-1 b
+    double* r64 = reinterpret_cast<double*>(
+        (reinterpret_cast<uintptr_t>(flags + 2 * nblk) + 255) & ~(uintptr_t)255);
+    double* p64 = r64 + n * m;
+    double* q64 = p64 + n * m;
+    double* part = q64 + n * m;
+    double* part_rz = part + kDotBlocks * kSmallM;
+    double* part_r = part_rz + kDotBlocks * kSmallM;
+    PcgState* st = reinterpret_cast<PcgState*>(part_r + kDotBlocks * kSmallM);
+    const unsigned rows_grid = (unsigned)ceil_div(n, 8);
+    matvec_df_rows_kernel<kSmallM><<<rows_grid, 256, 0, s>>>(A, n, lambda, B, x64, m, 1, r64,
+                                                              r32, nullptr);
+    note_launch();
+    if (refine_iters > 0) {
+      rc = solve(r32, nullptr);  // z0
+      if (rc) return rc;
+      col_dots_kernel<<<kDotBlocks, 256, 0, s>>>(r64, nullptr, r32, n, m, part_rz, nullptr);
+      pcg_init_kernel<<<1, 1024, 0, s>>>(B, r32, p64, n, m, part_rz, st);
+      note_launch(2);
+      for (int it = 0; it < refine_iters; ++it) {
+        const int cur = it & 1;
+        matvec_df_rows_kernel<kSmallM><<<rows_grid, 256, 0, s>>>(A, n, lambda, nullptr, p64, m,
+                                                                  0, q64, nullptr, st);
+        col_dots_kernel<<<kDotBlocks, 256, 0, s>>>(p64, q64, nullptr, n, m, part, st);
+        pcg_step_kernel<<<kDotBlocks, 256, 0, s>>>(x64, r64, r32, p64, q64, n, m, part, part_r,
+                                                   st, cur);
+        pcg_check_kernel<<<1, 32, 0, s>>>(part_r, m, kDotBlocks, st);
+        note_launch(4);
+        rc = solve(r32, &st->all_done);
+        if (rc) return rc;
+        col_dots_kernel<<<kDotBlocks, 256, 0, s>>>(r64, nullptr, r32, n, m, part_rz, st);
+        pcg_dir_kernel<<<kDotBlocks, 256, 0, s>>>(p64, r32, n, m, part_rz, st, cur);
+        note_launch(2);
+      }
+      copy_to_float_kernel<<<grid_for(n * m), 256, 0, s>>>(x64, X, n * m);
+      note_launch();
+    }
+    if (final_residual) {
+      // the true residual of the returned solution
+      matvec_df_rows_kernel<kSmallM><<<rows_grid, 256, 0, s>>>(A, n, lambda, B, x64, m, 1, r64,
+                                                                nullptr, nullptr);
+      if (cudaMemsetAsync(rnorm, 0, sizeof(double), s) != cudaSuccess)
+        return check_launch("ntg_chol_solve_tc memset");
+      max_abs64_kernel<<<grid_for(n * m), 256, 0, s>>>(r64, n * m, rnorm);
+      note_launch(2);
+      if (cudaMemcpyAsync(final_residual, rnorm, sizeof(double), cudaMemcpyDeviceToDevice, s) !=
+          cudaSuccess)
+        return check_launch("ntg_chol_solve_tc residual copy");
+    }
+    return check_launch("ntg_chol_solve_tc");
+  }
+  // many right-hand sides: refine_iters steps of iterative refinement
   for (int it = 0; it <= refine_iters; ++it) {
     if (it == refine_iters && !final_residual) break;
     if (cudaMemsetAsync(rnorm, 0, sizeof(double), s) != cudaSuccess)
       return check_launch("ntg_chol_solve_tc memset");
-    if (m <= 4)
-      residual64_rows_kernel<4><<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(A, n, lambda, B, x64, m,
-                                                                         r32, rnorm);
-    else if (m <= kSmallM)
-      residual64_rows_kernel<kSmallM><<<(unsigned)ceil_div(n, 8), 256, 0, s>>>(
-          A, n, lambda, B, x64, m, r32, rnorm);
-    else
-      residual_df_kernel<<<dim3((unsigned)ceil_div(m, 64), (unsigned)ceil_div(n, 64)), 256, 0,
-                           s>>>(A, n, lambda, B, x64, m, r32, rnorm);
+    residual_df_kernel<<<dim3((unsigned)ceil_div(m, 64), (unsigned)ceil_div(n, 64)), 256, 0, s>>>(
+        A, n, lambda, B, x64, m, r32, rnorm);
     note_launch();
     if (it == refine_iters) break;
-    rc = solve(r32);
+    rc = solve(r32, nullptr);
     if (rc) return rc;
     accumulate_tc_kernel<<<grid_for(n * m), 256, 0, s>>>(x64, r32, X, n * m);
     note_launch();

@@ -12,9 +12,9 @@ iterative refinement with the residual accumulated in FP64 (or double-float for
 more than 16 right-hand sides; `refine_iters`, default 2; 0 gives the plain
 FP32 solve), all in libntgb300.so. The factorisation is computed once
 and cached, as the reference caches it (predict.py:163). Finite ``t`` uses the
-eigendecomposition of predict.py:185-229 through torch.linalg.eigh (a cuSOLVER
-library call) in float64. Only 2-D ``k_train_train`` with ``trace_axes=(-1,)``
-is supported.
+eigenbasis of predict.py:185-229 with this library's own eigensolver (two-sided
+block Jacobi in FP32, ntg_eigh), its spectral-weight kernel and FP32 GEMMs.
+Only 2-D ``k_train_train`` with ``trace_axes=(-1,)`` is supported.
 """
 from __future__ import annotations
 
@@ -43,18 +43,73 @@ def _gemm(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     return out
 
 
+def _gemm_tn(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """a^T @ b for a [k, m], b [k, n] on the library's FP32 GEMM."""
+    out = torch.empty((a.shape[1], b.shape[1]), device=a.device, dtype=torch.float32)
+    L.call('ntg_gemm_ex', L.stream(), L.ptr(a), L.ptr(b), L.ptr(out), a.shape[1], b.shape[1],
+           a.shape[0], 1, 1., 0)
+    return out
+
+
+def _eigh(k: torch.Tensor, shift: float, max_sweeps: int = 20, tol: float = 2e-7):
+    """Eigenpairs of k + shift I on this library's block-Jacobi kernels (FP32):
+    (evals [n], evecs [n, n], column j for evals[j]), evals not sorted."""
+    n = k.shape[0]
+    lib = L.load()
+    nbytes = int(lib.ntg_eigh_workspace_bytes(n))
+    ws = torch.empty((nbytes,), device=k.device, dtype=torch.uint8)
+    evals = torch.empty((n,), device=k.device, dtype=torch.float32)
+    evecs = torch.empty((n, n), device=k.device, dtype=torch.float32)
+    L.call('ntg_eigh', L.stream(), L.ptr(k), n, float(shift), L.ptr(evals), L.ptr(evecs),
+           int(max_sweeps), float(tol), ws.data_ptr(), nbytes, None)
+    return evals, evecs
+
+
+# spectral functions of ntg_spectral_scale (predict.py:1277-1294 and the ensemble's)
+_EXPM1, _INV_EXPM1, _POS_EXP2, _EXP, _NEG_INV_EXPM1_2, _NEG_EXPM1, _NEG_INV_EXPM1 = range(7)
+
+
+def _spectral(evals: torch.Tensor, ts: torch.Tensor, kind: int, norm: float,
+              x: torch.Tensor) -> torch.Tensor:
+    """out [n, T, m] = w_kind(lambda_i, t) x[i, :] for x [n, m] and the times ts [T]."""
+    n, m = x.shape
+    out = torch.empty((n, ts.numel(), m), device=x.device, dtype=torch.float32)
+    L.call('ntg_spectral_scale', L.stream(), L.ptr(evals), ts.data_ptr(), ts.numel(), kind,
+           float(norm), L.ptr(x.contiguous()), n, m, L.ptr(out))
+    return out
+
+
+def _spectral_apply(evecs, evals, ts, kind, norm, x):
+    """sum_i evecs[:, i] w_kind(lambda_i, t) x[i, :] for every t: [T, n, m]."""
+    w = _spectral(evals, ts, kind, norm, x)                    # [n, T, m]
+    n, nt, m = w.shape
+    return _gemm(evecs, w.reshape(n, nt * m)).reshape(evecs.shape[0], nt, m).permute(1, 0, 2)
+
+
+def _times(t, learning_rate, dev):
+    tt = np.asarray(t, np.float64) * learning_rate
+    return tt.shape, torch.as_tensor(tt.reshape(-1), dtype=torch.float64, device=dev)
+
+
 class CholeskySolver:
     """Cached factorisation of K + lambda I (predict.py:1224-1258) on the tensor-core
     Cholesky kernels: L lives in a [n, ldl] buffer (ldl = n rounded up to 32, the row
     pitch the TMA loads of the trailing updates need); the factor workspace keeps the
     inverses of the 128-wide diagonal blocks and L^T for the solves."""
 
-    def __init__(self, k: torch.Tensor, diag_reg: float, absolute: bool, refine_iters: int = 2):
+    # refinement per solve when the caller gives none: at most 16 preconditioned CG
+    # iterations for up to 16 right-hand sides (they stop once converged), 2 plain
+    # refinement steps for more
+    REFINE_FEW, REFINE_MANY, FEW = 16, 2, 16
+
+    def __init__(self, k: torch.Tensor, diag_reg: float, absolute: bool,
+                 refine_iters: Optional[int] = None):
         n = k.shape[0]
         if k.ndim != 2 or k.shape[1] != n:
             raise NotImplementedError('nt_gb300 supports a 2-D square k_train_train')
         lib = L.load()
-        self.k, self.n, self.refine = k, n, int(refine_iters)
+        self.k, self.n = k, n
+        self.refine = None if refine_iters is None else int(refine_iters)
         self.ldl = (n + 31) // 32 * 32
         self.Lbuf = torch.empty((n, self.ldl), device=k.device, dtype=torch.float32)
         fws = int(lib.ntg_chol_factor_tc_workspace_bytes(n, self.ldl))
@@ -89,8 +144,10 @@ class CholeskySolver:
               residual: bool = True) -> torch.Tensor:
         """A^{-1} b; refine_iters overrides the solver's refinement steps; residual=False
         skips the final residual kept in self.residual."""
-        refine = self.refine if refine_iters is None else int(refine_iters)
         b = b.reshape(self.n, -1).contiguous()
+        refine = self.refine if refine_iters is None else int(refine_iters)
+        if refine is None:
+            refine = self.REFINE_FEW if b.shape[1] <= self.FEW else self.REFINE_MANY
         if self.info:
             return torch.full_like(b, float('nan'))
         out = torch.empty_like(b)
@@ -116,7 +173,7 @@ class CholeskySolver:
 
 def gradient_descent_mse(k_train_train, y_train, learning_rate: float = 1.,
                          diag_reg: float = 0., diag_reg_absolute_scale: bool = False,
-                         trace_axes=(-1,), refine_iters: int = 2):
+                         trace_axes=(-1,), refine_iters: Optional[int] = None):
     """predict.py:71-278."""
     if tuple(trace_axes) not in ((-1,), (1,)):
         raise NotImplementedError('nt_gb300 supports trace_axes=(-1,)')
@@ -133,11 +190,10 @@ def gradient_descent_mse(k_train_train, y_train, learning_rate: float = 1.,
 
     def eig():
         if 'eig' not in state:
-            a = k.double()
-            n = a.shape[0]
-            reg = diag_reg if diag_reg_absolute_scale else diag_reg * torch.trace(a) / n
-            a = a + reg * torch.eye(n, device=a.device, dtype=a.dtype)
-            state['eig'] = torch.linalg.eigh(a)
+            n = k.shape[0]
+            reg = diag_reg if diag_reg_absolute_scale else \
+                diag_reg * float(k.diagonal().double().sum()) / n
+            state['eig'] = _eigh(k, reg)
         return state['eig']
 
     def predict_fn(t=None, fx_train_0=0., fx_test_0=None, k_test_train=None):
@@ -158,24 +214,25 @@ def gradient_descent_mse(k_train_train, y_train, learning_rate: float = 1.,
             if fx_train_0 is None:
                 return fx_test_t
             return fx_train_t, fx_test_t
+        # eigenbasis path (predict.py:185-229): own block-Jacobi eigenpairs, spectral
+        # weights and products on this library's kernels, FP32
         evals, evecs = eig()
-        tt = torch.as_tensor(np.asarray(t, dtype=np.float64), device=k.device) * learning_rate
-        yd = y.double()
-        rhs = -yd if fx_train_0 is None else _t64(fx_train_0, y) - yd
-        proj = evecs.T @ rhs
-        tshape = tuple(tt.shape)
-        tf = tt.reshape(-1, 1)
-        expm1 = torch.expm1(-torch.clamp(evals, min=0)[None] * tf / y.numel())
+        tshape, ts = _times(t, learning_rate, k.device)
+        rhs = -y if fx_train_0 is None else _as_tensor(fx_train_0, y) - y
+        proj = _gemm_tn(evecs, rhs.contiguous())                    # [n, m]
+        norm = y.numel()
         outs = []
         if fx_train_0 is not None:
-            dfx = torch.einsum('ji,ti,ik->tjk', evecs, expm1, proj)
-            outs.append((_t64(fx_train_0, y) + dfx).reshape(tshape + y.shape).float())
+            dfx = _spectral_apply(evecs, evals, ts, _EXPM1, norm, proj)   # [T, n, m]
+            outs.append((_as_tensor(fx_train_0, y) + dfx).reshape(tshape + tuple(y.shape)))
         if fx_test_0 is not None:
-            inv = expm1 / torch.abs(evals)[None]
-            dfx = torch.einsum('ji,ti,ik->tjk', evecs, inv, proj)
-            kt = _dev(k_test_train).double()
-            test = _t64(fx_test_0, y) + torch.einsum('sj,tjk->tsk', kt, dfx)
-            outs.append(test.reshape(tshape + (kt.shape[0], y.shape[1])).float())
+            dfx = _spectral_apply(evecs, evals, ts, _INV_EXPM1, norm, proj)
+            kt = _dev(k_test_train)
+            nt_, n, m = dfx.shape
+            flat = dfx.permute(1, 0, 2).reshape(n, nt_ * m).contiguous()
+            test = _gemm(kt, flat).reshape(kt.shape[0], nt_, m).permute(1, 0, 2)
+            test = _as_tensor(fx_test_0, y) + test
+            outs.append(test.reshape(tshape + (kt.shape[0], y.shape[1])))
         if len(outs) == 2:
             return tuple(outs)
         return outs[0] if outs else y
@@ -192,6 +249,13 @@ def _is_inf(t) -> bool:
 
 
 def _as_like(v, like: Optional[torch.Tensor]):
+    if isinstance(v, (int, float)):
+        return v
+    return _dev(v)
+
+
+def _as_tensor(v, like: torch.Tensor):
+    """A scalar stays a Python number; arrays become float32 device tensors."""
     if isinstance(v, (int, float)):
         return v
     return _dev(v)
@@ -236,7 +300,8 @@ class _NLL(torch.autograd.Function):
 
 
 def negative_log_likelihood(k_train_train, y_train, diag_reg: float = 0.,
-                            diag_reg_absolute_scale: bool = False, refine_iters: int = 2):
+                            diag_reg_absolute_scale: bool = False,
+                            refine_iters: Optional[int] = None):
     """NNGP negative log marginal likelihood, differentiable with respect to the kernel.
 
     A helper for hyper-parameter learning (not part of the reference's predict
@@ -247,7 +312,7 @@ def negative_log_likelihood(k_train_train, y_train, diag_reg: float = 0.,
     """
     k = k_train_train if isinstance(k_train_train, torch.Tensor) else _dev(k_train_train)
     y = _dev(y_train)
-    return _NLL.apply(k, y, float(diag_reg), bool(diag_reg_absolute_scale), int(refine_iters))
+    return _NLL.apply(k, y, float(diag_reg), bool(diag_reg_absolute_scale), refine_iters)
 
 
 class _RidgeSolve(torch.autograd.Function):
@@ -278,7 +343,8 @@ class _RidgeSolve(torch.autograd.Function):
 
 
 def kernel_ridge_solve(k_train_train, y_train, diag_reg: float = 0.,
-                       diag_reg_absolute_scale: bool = False, refine_iters: int = 2):
+                       diag_reg_absolute_scale: bool = False,
+                       refine_iters: Optional[int] = None):
     """(K + diag_reg * trace(K) / n * I)^{-1} y on this module's Cholesky kernels,
     differentiable with respect to K and y (a helper for kernel-ridge losses such
     as the support-set objective of dataset distillation; the reference computes
@@ -288,7 +354,7 @@ def kernel_ridge_solve(k_train_train, y_train, diag_reg: float = 0.,
     k = k_train_train if isinstance(k_train_train, torch.Tensor) else _dev(k_train_train)
     y = y_train if isinstance(y_train, torch.Tensor) else _dev(y_train)
     return _RidgeSolve.apply(k, y, float(diag_reg), bool(diag_reg_absolute_scale),
-                             int(refine_iters))
+                             refine_iters)
 
 
 class _MatMul(torch.autograd.Function):
@@ -352,7 +418,8 @@ def _gaussians(get, names, out):
 
 
 def gp_inference(k_train_train, y_train, diag_reg: float = 0.,
-                 diag_reg_absolute_scale: bool = False, trace_axes=(-1,), refine_iters: int = 2):
+                 diag_reg_absolute_scale: bool = False, trace_axes=(-1,),
+                 refine_iters: Optional[int] = None):
     """predict.py:566-745: ``predict_fn(get, k_test_train, k_test_test)`` with the
     NNGP / NTK / NTKGP posterior mean and, given ``k_test_test``, covariance.
 
@@ -439,9 +506,9 @@ def gradient_descent_mse_ensemble(kernel_fn, x_train, y_train, learning_rate: fl
     """predict.py:753-1005: ``predict_fn(t=None, x_test=None, get=None, compute_cov=False)``,
     the mean (and covariance) of the infinite ensemble of infinite-width networks
     trained by gradient flow on the MSE loss. ``t=None`` is the Cholesky path of
-    ``gp_inference`` (this library's kernels); finite ``t`` uses the eigendecomposition of
-    the regularised train-train kernel (``torch.linalg.eigh`` in FP64) and the expm1
-    spectral functions of predict.py:1277-1294, contracted in FP64."""
+    ``gp_inference`` (this library's kernels); finite ``t`` uses the library's own
+    eigendecomposition of the regularised train-train kernel (block Jacobi, FP32), the
+    expm1 spectral functions of predict.py:1277-1294 as a kernel, and its FP32 GEMMs."""
     if tuple(trace_axes) not in ((-1,), (1,)):
         raise NotImplementedError('nt_gb300 supports trace_axes=(-1,)')
     y = _dev(y_train)
@@ -462,10 +529,11 @@ def gradient_descent_mse_ensemble(kernel_fn, x_train, y_train, learning_rate: fl
 
     def eigenspace(g):
         if g not in eig:
-            a = k_train((g,))[g].double()
+            a = k_train((g,))[g]
             n = a.shape[0]
-            reg = diag_reg if diag_reg_absolute_scale else diag_reg * torch.trace(a) / n
-            eig[g] = torch.linalg.eigh(a + reg * torch.eye(n, device=a.device, dtype=a.dtype))
+            reg = diag_reg if diag_reg_absolute_scale else \
+                diag_reg * float(a.diagonal().double().sum()) / n
+            eig[g] = _eigh(a, reg)
         return eig[g]
 
     inf_cache = {}
@@ -489,51 +557,64 @@ def gradient_descent_mse_ensemble(kernel_fn, x_train, y_train, learning_rate: fl
             if dep not in inf_cache:
                 inf_cache[dep] = gp_inference(kd, y, diag_reg, diag_reg_absolute_scale)
             return inf_cache[dep](get=get, k_test_train=k_td, k_test_test=nngp_tt)
-        tt = torch.as_tensor(np.asarray(t, np.float64), device=y.device) * learning_rate
-        t_shape = tuple(tt.shape)
-        tf = tt.reshape(-1, 1)
-        y64 = y.double()
+        # eigenbasis path: own block-Jacobi eigenpairs, the spectral weights of
+        # predict.py:1277-1294 and every product on this library's kernels (FP32)
+        t_shape, ts = _times(t, learning_rate, y.device)
+        nt_ = ts.numel()
         norm = y.numel()
         out = {}
+
+        def per_t(x):  # [T, a, b] -> t_shape + [a, b]
+            return x.reshape(t_shape + tuple(x.shape[1:]))
+
+        def sym_apply(evecs, evals, kind, x_t):
+            # evecs diag(w_kind(t)) evecs^T for every t: [T, n, n]
+            return _spectral_apply(evecs, evals, ts, kind, norm, evecs.t().contiguous())
+
         for g in names:
             evals, evecs = eigenspace(g)
-            ev = evals[None, :]
-            pos = torch.clamp(ev, min=0.)
-            neg_expm1 = -torch.expm1(-pos * tf / norm)
-            neg_inv = neg_expm1 / torch.abs(ev)
-            proj = evecs.t() @ y64                                   # [i, m]
+            proj = _gemm_tn(evecs, y)                                   # [n, m]
             if k_td is None:
-                mean = torch.einsum('ji,ti,im->tjm', evecs, neg_expm1, proj)
+                mean = _spectral_apply(evecs, evals, ts, _NEG_EXPM1, norm, proj)
             else:
-                ktd = k_td[g].double()
-                mean = torch.einsum('lj,ji,ti,im->tlm', ktd, evecs, neg_inv, proj)
-            mean = mean.reshape(t_shape + tuple(mean.shape[1:])).float()
+                ktd = k_td[g]
+                w = _spectral_apply(evecs, evals, ts, _NEG_INV_EXPM1, norm, proj)  # [T, n, m]
+                n, m = proj.shape
+                flat = w.permute(1, 0, 2).reshape(n, nt_ * m).contiguous()
+                mean = _gemm(ktd, flat).reshape(ktd.shape[0], nt_, m).permute(1, 0, 2)
+            mean = per_t(mean.contiguous())
             if nngp_tt is None:
                 out[g] = mean
                 continue
-            nngp_dd = kd['nngp'].double()
+            nngp_dd = kd['nngp']
             if k_td is None:
                 if g == 'nngp':
-                    cov = torch.einsum('ji,ti,ki->tjk', evecs,
-                                       pos * torch.exp(-2 * pos * tf / norm), evecs)
+                    cov = sym_apply(evecs, evals, _POS_EXP2, None)
                 else:
-                    ex = torch.einsum('mi,ti,ki->tmk', evecs, torch.exp(-pos * tf / norm), evecs)
-                    cov = torch.einsum('tmk,kl,tnl->tmn', ex, nngp_dd, ex)
+                    ex = sym_apply(evecs, evals, _EXP, None)              # [T, n, n]
+                    cov = torch.stack([_gemm(_gemm(e.contiguous(), nngp_dd), e.contiguous())
+                                       for e in ex])
             else:
-                tt_k = nngp_tt.double()[None]
+                tt_k = nngp_tt[None]
+                a = _gemm(ktd, evecs)                                     # [s, n]
+                at = a.t().contiguous()                                   # [n, s]
+                s_ = a.shape[0]
                 if g == 'nngp':
-                    neg_inv2 = -torch.expm1(-pos * 2 * tf / norm) / torch.abs(ev)
-                    a = ktd @ evecs                                    # [m, i]
-                    cov = tt_k - torch.einsum('mi,ti,li->tml', a, neg_inv2, a)
+                    w = _spectral(evals, ts, _NEG_INV_EXPM1_2, norm, at)   # [n, T, s]
+                    flat = w.reshape(at.shape[0], nt_ * s_)
+                    quad = _gemm(a, flat).reshape(s_, nt_, s_).permute(1, 0, 2)
+                    cov = tt_k - quad
                 else:
-                    b = evecs.t() @ ktd.t()                            # [i, l]
-                    term_1 = torch.einsum('mi,ti,il->tml', evecs, neg_inv, b)
-                    c = evecs.t() @ k_td['nngp'].double().t()         # [i, l]
-                    term_2 = torch.einsum('mi,ti,il->tml', ktd @ evecs, neg_inv, c)
+                    term_1 = _spectral_apply(evecs, evals, ts, _NEG_INV_EXPM1, norm, at)
+                    c = _gemm_tn(evecs, k_td['nngp'].t().contiguous())    # [n, s]
+                    w = _spectral(evals, ts, _NEG_INV_EXPM1, norm, c)     # [n, T, s]
+                    term_2 = _gemm(a, w.reshape(c.shape[0], nt_ * s_)).reshape(
+                        s_, nt_, s_).permute(1, 0, 2)
                     term_2 = term_2 + term_2.transpose(1, 2)
-                    cov = torch.einsum('tji,jk,tkl->til', term_1, nngp_dd, term_1) - term_2 + tt_k
-            cov = cov.reshape(t_shape + tuple(cov.shape[1:])).float()
-            out[g] = Gaussian(mean, cov)
+                    quad = torch.stack([_gemm_tn(t1.contiguous(), _gemm(nngp_dd, t1.contiguous()))
+                                        for t1 in term_1])
+                    cov = quad - term_2 + tt_k
+            out[g] = Gaussian(mean, per_t(cov.contiguous()))
         return _gaussians(get, names, out)
 
     return predict_fn
