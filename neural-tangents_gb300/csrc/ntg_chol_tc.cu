@@ -556,7 +556,7 @@ __global__ void __launch_bounds__(256)
     col_dots_kernel(const double* __restrict__ u, const double* __restrict__ v,
                     const float* __restrict__ vf, int64_t n, int64_t m, double* __restrict__ part,
                     const PcgState* st) {
-  if (st->all_done) return;
+  if (st && st->all_done) return;  // st == nullptr: the set-up product, always computed
   __shared__ double red[8][kSmallM];
   double acc[kSmallM];
 #pragma unroll
