@@ -283,20 +283,23 @@ int ntg_gemm_tc(void* stream, const float* a, int64_t lda, const float* b, int64
  * L [n, ldl] row-major (ldl >= n, a multiple of 4, L 16-byte aligned) receives the
  * lower factor, zeros above the diagonal; lambda and info as ntg_chol_factor.
  * factor_workspace (ntg_chol_factor_tc_workspace_bytes) receives the inverses of
- * the diagonal blocks and L^T, which ntg_chol_solve_tc reads. */
+ * the diagonal blocks and the explicit inverse factors L^-1 and L^-T (a forward
+ * block solve of L Y = I whose updates run on ntg_gemm_tc), which
+ * ntg_chol_solve_tc reads. */
 size_t ntg_chol_factor_tc_workspace_bytes(int64_t n, int64_t ldl);
 int ntg_chol_factor_tc(void* stream, const float* A, int64_t n, double diag_reg, int32_t absolute,
                        float* L, int64_t ldl, double* lambda, int* info, void* factor_workspace,
                        size_t factor_workspace_bytes);
 /* X = (K + lambda I)^{-1} B, B and X [n, m] row-major, from a factor of
- * ntg_chol_factor_tc. Triangular solves: for m <= 16 two cooperative launches
- * (block-triangular solves with the stored inverses of the diagonal blocks, blocks
- * handed on by flags under bounded waits), for more right-hand sides blocked solves
- * whose updates run on ntg_gemm_tc. Refinement keeps X in FP64 and accumulates the
+ * ntg_chol_factor_tc (L itself is not read: the solves multiply by the inverse
+ * factors of the factor workspace): for m <= 16 two triangular matrix-vector
+ * products (a warp per row), for more right-hand sides two ntg_gemm_tc products on
+ * the transposed right-hand sides. Refinement keeps X in FP64 and accumulates the
  * products with K in double-float arithmetic (two FP32 words, about 44 significant
  * bits): for m <= 16 at most refine_iters iterations of conjugate gradients
- * preconditioned by the FP32 factor, each column stopping once max |residual| <=
- * 1e-13 max |b| (converges where plain refinement stalls, cond(K) * u > 1); for
+ * preconditioned by the FP32 factor, each column stopping once its max |residual|
+ * fell 1e10-fold or below 1e-15 max |b| (converges where plain refinement stalls,
+ * cond(K) * u > 1); for
  * m > 16 refine_iters steps of x <- x + (L L^T)^{-1} (b - (K + lambda I) x).
  * final_residual (device double, optional) receives max |b - (K + lambda I) X| of
  * the returned X. */
@@ -315,12 +318,16 @@ int ntg_chol_logdet_tc(void* stream, const float* L, int64_t n, int64_t ldl, dou
  * applied to K and to the eigenvectors tile by tile). Sweeps run until the
  * off-diagonal Frobenius norm is at most tol times the whole norm, or max_sweeps;
  * evals [n] (not sorted) and evecs [n, n] (column j belongs to evals[j]) are
- * written, *sweeps_out (host int, may be NULL) receives the sweeps run. Reads one
- * 16-byte norm back after each sweep: synchronises the stream once per sweep. */
+ * written, *sweeps_out (host int, may be NULL) receives the sweeps run. Then
+ * refine_steps (0-4) steps of the Ogita-Aishima refinement of all pairs, with
+ * X^T X and X^T (K + shift I) X accumulated in double-float (two FP32 words): the
+ * Jacobi rounds leave about 1e-5 relative error at n = 1000, a step squares it
+ * down to the FP32 rounding of the output. Reads one 16-byte norm back after each
+ * sweep: synchronises the stream once per sweep. */
 size_t ntg_eigh_workspace_bytes(int64_t n);
 int ntg_eigh(void* stream, const float* K, int64_t n, double shift, float* evals, float* evecs,
-             int32_t max_sweeps, double tol, void* workspace, size_t workspace_bytes,
-             int32_t* sweeps_out);
+             int32_t max_sweeps, double tol, int32_t refine_steps, void* workspace,
+             size_t workspace_bytes, int32_t* sweeps_out);
 /* out[i, t, c] = w(lambda_i, t_t) x[i, c] for x [n, m], times t [nt] (device doubles,
  * already scaled by the learning rate) and the spectral function `kind` (pos =
  * max(lambda, 0), N = norm): 0 expm1(-pos t/N), 1 expm1(-pos t/N)/|lambda|,

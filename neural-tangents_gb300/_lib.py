@@ -122,8 +122,8 @@ SIGNATURES = {
                            _P], C.c_int),
     'ntg_chol_logdet_tc': ([_P, _P, _I64, _I64, _P], C.c_int),
     'ntg_eigh_workspace_bytes': ([_I64], C.c_size_t),
-    'ntg_eigh': ([_P, _P, _I64, C.c_double, _P, _P, _I32, C.c_double, _P, C.c_size_t, _P],
-                 C.c_int),
+    'ntg_eigh': ([_P, _P, _I64, C.c_double, _P, _P, _I32, C.c_double, _I32, _P, C.c_size_t,
+                  _P], C.c_int),
     'ntg_spectral_scale': ([_P, _P, _P, _I64, _I32, C.c_double, _P, _I64, _I64, _P], C.c_int),
 }
 

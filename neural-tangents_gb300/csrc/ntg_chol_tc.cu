@@ -12,19 +12,18 @@
 //   gemm_tf32x3 lower   the trailing update A22 -= L21 L21^T on the tensor cores
 //                       (3xTF32 products, FP32 accumulation; tiles on or below the
 //                       diagonal only).
-// Solves: for up to kSmallM right-hand sides, one cooperative launch per
-// triangle in which the CTA of block b folds in each solved block j < b as
-// soon as its flag is set (bounded waits) and applies the stored inverse of its
-// diagonal block; for more right-hand sides, blocked right-looking solves on the
-// transposed right-hand sides whose updates are 3xTF32 tensor-core GEMMs.
+// After the panels, the explicit inverse factors L^-T (a forward block solve of
+// L Y = I on the tensor cores, only the non-zero rows of each block column) and
+// L^-1 (its transpose) are kept in the factor workspace: a solve is then two
+// triangular products, GEMV-shaped for up to kSmallM right-hand sides (a warp
+// per row, bandwidth-bound) and tensor-core GEMMs for more.
 // Refinement keeps x in FP64 and accumulates every product with K in
 // double-float (two FP32 words, error-free products and sums; about 44
 // significant bits), which the GB300's FP32 rate makes about 6x cheaper than
 // FP64: for up to kSmallM right-hand sides preconditioned conjugate gradients
-// (the FP32 factor as preconditioner; converges where plain refinement stalls,
-// kappa u > 1), for more, refine_iters steps of x <- x + A^{-1} (b - A x).
-#include <cooperative_groups.h>
-
+// (the factor as preconditioner; converges where plain refinement stalls,
+// kappa u > 1, each column stopping once its residual fell by kPcgTol), for
+// more, refine_iters steps of x <- x + (L L^T)^-1 (b - A x).
 #include <mutex>
 #include <string>
 
@@ -40,7 +39,6 @@ namespace {
 constexpr int PB = 128;        // panel / diagonal block
 constexpr int PBS = PB + 1;    // padded shared-memory row
 constexpr int kSmallM = 16;    // right-hand sides of the cooperative solves
-constexpr uint32_t kFlagWait = 1u << 22;
 
 __device__ int g_chol_error = 0;
 
@@ -128,10 +126,10 @@ __device__ void warp_potrf_inv32(float (*a)[PBS], int o, float (*dinv)[33], int*
 }
 
 // Factors L[k:k+nb, k:k+nb] in place (upper part zeroed) and writes the inverse of the
-// factor, zero-padded to 128 x 128, to linv (row-major) and its transpose to linvT.
+// factor, zero-padded to 128 x 128, to linv (row-major).
 __global__ void __launch_bounds__(512, 1)
     diag_block_kernel(float* __restrict__ L, int64_t ldl, int64_t n, int64_t k, int* info,
-                      float* __restrict__ linv, float* __restrict__ linvT) {
+                      float* __restrict__ linv) {
   extern __shared__ float sm[];
   float(*a)[PBS] = reinterpret_cast<float(*)[PBS]>(sm);
   float(*x)[PBS] = reinterpret_cast<float(*)[PBS]>(sm + PB * PBS);
@@ -213,7 +211,6 @@ __global__ void __launch_bounds__(512, 1)
     const int i = idx / PB, j = idx % PB;
     const bool in = i < nb && j < nb;
     linv[idx] = in ? x[i][j] : 0.f;
-    linvT[idx] = in ? x[j][i] : 0.f;
   }
 }
 
@@ -278,101 +275,50 @@ __global__ void transpose_kernel(const float* __restrict__ in, int64_t ld_in, fl
 }
 
 // ---------------------------------------------------------------------------
-// Cooperative triangular solves for up to kSmallM right-hand sides.
-// X [n, m] row-major in place: forward L y = b, or backward L^T x = y.
-// Block b's CTA waits (bounded) for the flags of the blocks it depends on; a
-// flag is set once the block's solution is in global memory.
+// Triangular products with the explicit inverse factors, for up to kSmallM
+// right-hand sides: Y[i, c] = sum_{j in range(i)} M[i, j] X[j, c] with range
+// j <= i (M = L^-1, lower) or j >= i (M = L^-T, upper). One warp per row.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool wait_flag(const int* flag, int want) {
-  for (uint32_t it = 0; it < kFlagWait; ++it) {
-    if (*reinterpret_cast<const volatile int*>(flag) >= want) {
-      __threadfence();
-      return true;
-    }
-    __nanosleep(64);
-  }
-  return false;
-}
-
+template <int MR>
 __global__ void __launch_bounds__(256)
-    trsv_coop_kernel(const float* __restrict__ L, int64_t ldl, const float* __restrict__ linv,
-                     const float* __restrict__ linvT, int64_t n, float* X, int64_t m,
-                     int* flags, int backward, const int* skip) {
-  if (skip && *reinterpret_cast<const volatile int*>(skip)) return;  // uniform: no CTA waits
-  extern __shared__ float sm[];
-  float(*blk)[PBS] = reinterpret_cast<float(*)[PBS]>(sm);        // an L block or Linv
-  float(*yj)[kSmallM + 1] = reinterpret_cast<float(*)[kSmallM + 1]>(sm + PB * PBS);
-  float(*acc)[kSmallM + 1] = reinterpret_cast<float(*)[kSmallM + 1]>(sm + PB * PBS + PB * (kSmallM + 1));
-  __shared__ int s_ok;
-  const int tid = threadIdx.x, nth = blockDim.x;
-  const int64_t nblk = (n + PB - 1) / PB;
-  // thread -> (row r, columns c0 .. c0 + m/2)
-  const int r = tid & (PB - 1), half = tid >> 7;
-  for (int64_t ord = blockIdx.x; ord < nblk; ord += gridDim.x) {
-    const int64_t b = backward ? nblk - 1 - ord : ord;
-    const int64_t r0 = b * PB;
-    const int nb = (int)mini(PB, n - r0);
-    for (int idx = tid; idx < PB * (int)m; idx += nth) {
-      const int i = idx / (int)m, c = idx % (int)m;
-      acc[i][c] = i < nb ? X[(r0 + i) * m + c] : 0.f;
-    }
-    if (tid == 0) s_ok = 1;
-    __syncthreads();
-    // fold in every solved block j this block depends on
-    for (int64_t jo = 0; jo < ord; ++jo) {
-      const int64_t j = backward ? nblk - 1 - jo : jo;
-      const int64_t j0 = j * PB;
-      const int nj = (int)mini(PB, n - j0);
-      if (tid == 0 && s_ok && !wait_flag(flags + j, 1)) {
-        s_ok = 0;
-        atomicExch(&g_chol_error, NTG_ERR_WAIT_TIMEOUT);
-      }
-      __syncthreads();
-      if (!s_ok) break;
-      // forward: acc -= L[b rows, j cols] y_j; backward: acc -= L[j rows, b cols]^T x_j
-      // blk[i][q] multiplies y_j[q] into row i; both loads walk contiguous global rows
-      if (!backward) {
-        for (int idx = tid; idx < PB * PB; idx += nth) {
-          const int i = idx / PB, q = idx % PB;
-          blk[i][q] = (i < nb && q < nj) ? L[(r0 + i) * ldl + j0 + q] : 0.f;
-        }
-      } else {
-        for (int idx = tid; idx < PB * PB; idx += nth) {
-          const int q = idx / PB, i = idx % PB;
-          blk[i][q] = (q < nj && i < nb) ? L[(j0 + q) * ldl + r0 + i] : 0.f;
-        }
-      }
-      for (int idx = tid; idx < PB * (int)m; idx += nth) {
-        const int q = idx / (int)m, c = idx % (int)m;
-        yj[q][c] = q < nj ? __ldcg(X + (j0 + q) * m + c) : 0.f;
-      }
-      __syncthreads();
-      for (int c = half; c < (int)m; c += 2) {
-        float s = 0.f;
-#pragma unroll 8
-        for (int q = 0; q < PB; ++q) s = fmaf(blk[r][q], yj[q][c], s);
-        acc[r][c] -= s;
-      }
-      __syncthreads();
-    }
-    if (!s_ok) return;
-    // x_b = Linv acc (forward) or Linv^T acc (backward)
-    const float* li = (backward ? linvT : linv) + b * PB * PB;
-    for (int idx = tid; idx < PB * PB; idx += nth) blk[idx / PB][idx % PB] = li[idx];
-    __syncthreads();
-    for (int c = half; c < (int)m; c += 2) {
-      float s = 0.f;
-#pragma unroll 8
-      for (int q = 0; q < PB; ++q) s = fmaf(blk[r][q], acc[q][c], s);
-      if (r < nb) X[(r0 + r) * m + c] = s;
-    }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) atomicExch(flags + b, 1);
+    tri_gemv_kernel(const float* __restrict__ M, int64_t ld, int64_t n, int upper,
+                    const float* __restrict__ X, int64_t m, float* __restrict__ Y,
+                    const int* skip) {
+  if (skip && *skip) return;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float* mr = M + row * ld;
+  float acc[MR];
+#pragma unroll
+  for (int c = 0; c < MR; ++c) acc[c] = 0.f;
+  const int64_t j0 = upper ? row : 0, j1 = upper ? n : row + 1;
+  for (int64_t j = j0 + lane; j < j1; j += 32) {
+    const float a = mr[j];
+    const float* xr = X + j * m;
+#pragma unroll
+    for (int c = 0; c < MR; ++c)
+      if (c < m) acc[c] = fmaf(a, xr[c], acc[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < MR; ++c) {
+    if (c >= m) break;
+    float v = acc[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) Y[row * m + c] = v;
   }
 }
 
-constexpr size_t kTrsvSmem = (size_t)(PB * PBS + 2 * PB * (kSmallM + 1)) * sizeof(float);
+// I [n, ld]: ones on the diagonal, zeros elsewhere (padding columns included).
+__global__ void identity_kernel(float* __restrict__ Z, int64_t n, int64_t ld) {
+  const int64_t total = n * ld;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx / ld, j = idx - i * ld;
+    Z[idx] = (i == j) ? 1.f : 0.f;
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Residuals R = B - (A + lambda I) X with X in FP64.
@@ -487,12 +433,14 @@ __global__ void accumulate_tc_kernel(double* __restrict__ x, const float* __rest
 // stops (its step sizes become 0) once max |r| <= kPcgTol max |b|; when every
 // column has stopped the remaining launches return at once.
 // ---------------------------------------------------------------------------
-constexpr double kPcgTol = 1e-13;
+constexpr double kPcgTol = 1e-10;   // residual reduction from the starting point
+constexpr double kPcgFloor = 1e-15; // or residual below this times max |b|
 constexpr int kDotBlocks = 128;
 
 struct PcgState {
   double rho[2][kSmallM];   // r.z of the current / next iteration
   double bnorm[kSmallM];    // max |b_j|
+  double r0norm[kSmallM];   // max |r_j| of the starting point
   double rmax[kSmallM];     // max |r_j| of the last residual
   int active[kSmallM];
   int all_done;
@@ -589,26 +537,29 @@ __device__ __forceinline__ double sum_parts(const double* part, int c) {
   return t;
 }
 
-// Set-up: bnorm, rho[0] = r.z (from part), p = z, every column active.
+// Set-up: bnorm, r0norm, rho[0] = r.z (from part), p = z, every column active.
 __global__ void pcg_init_kernel(const float* __restrict__ B, const float* __restrict__ z,
-                                double* __restrict__ p, int64_t n, int64_t m,
-                                const double* __restrict__ part, PcgState* st) {
-  __shared__ double bmax[kSmallM];
-  if (threadIdx.x < kSmallM) bmax[threadIdx.x] = 0.0;
+                                double* __restrict__ p, const double* __restrict__ r, int64_t n,
+                                int64_t m, const double* __restrict__ part, PcgState* st) {
+  __shared__ double bmax[kSmallM], rmax[kSmallM];
+  if (threadIdx.x < kSmallM) bmax[threadIdx.x] = rmax[threadIdx.x] = 0.0;
   __syncthreads();
   for (int64_t i = threadIdx.x; i < n * m; i += blockDim.x) {
     p[i] = (double)z[i];
     const int c = (int)(i % m);
     atomicMax(reinterpret_cast<unsigned long long*>(&bmax[c]),
               (unsigned long long)__double_as_longlong(fabs((double)B[i])));
+    atomicMax(reinterpret_cast<unsigned long long*>(&rmax[c]),
+              (unsigned long long)__double_as_longlong(fabs(r[i])));
   }
   __syncthreads();
   if (threadIdx.x < m) {
     const int c = threadIdx.x;
     st->bnorm[c] = bmax[c];
+    st->r0norm[c] = rmax[c];
     st->rho[0][c] = sum_parts(part, c);
-    st->rmax[c] = 0.0;
-    st->active[c] = 1;
+    st->rmax[c] = rmax[c];
+    st->active[c] = rmax[c] > kPcgFloor * bmax[c];
   }
   if (threadIdx.x == 0) st->all_done = 0;
 }
@@ -626,7 +577,7 @@ __global__ void __launch_bounds__(256)
   if (threadIdx.x < m) {
     const int c = threadIdx.x;
     const double pq = sum_parts(pq_part, c);
-    alpha[c] = (st->active[c] && pq != 0.0) ? st->rho[cur][c] / pq : 0.0;
+    alpha[c] = (st->active[c] && pq > 0.0) ? st->rho[cur][c] / pq : 0.0;
     rmax[c] = 0.0;
   }
   __syncthreads();
@@ -658,7 +609,8 @@ __global__ void pcg_check_kernel(const double* __restrict__ rpart, int64_t m, in
     double mx = 0.0;
     for (int b = 0; b < nblocks; ++b) mx = fmax(mx, rpart[b * kSmallM + c]);
     st->rmax[c] = mx;
-    if (st->active[c] && mx <= kPcgTol * st->bnorm[c]) st->active[c] = 0;
+    if (st->active[c] && (mx <= kPcgTol * st->r0norm[c] || mx <= kPcgFloor * st->bnorm[c]))
+      st->active[c] = 0;
     if (st->active[c]) atomicOr(&any, 1);
   }
   __syncthreads();
@@ -727,119 +679,77 @@ int attrs_once() {
   std::call_once(once, [] {
     rc = set_smem((const void*)diag_block_kernel, kDiagSmem);
     if (!rc) rc = set_smem((const void*)panel_trsm_kernel, kPanelSmem);
-    if (!rc) rc = set_smem((const void*)trsv_coop_kernel, kTrsvSmem);
   });
   return rc;
 }
 
-// Factor workspace layout (bytes): linv [nblk * 128 * 128] f32, linvT [same],
-// U = L^T [n * ldl] f32 (for the many-right-hand-side backward solve).
+// Factor workspace layout: linv [nblk * 128 * 128] f32 (inverses of the diagonal
+// blocks), uinv = L^-T [n * ldl] f32 (upper), linvf = L^-1 [n * ldl] f32 (lower).
 struct FactorWs {
   float* linv;
-  float* linvT;
-  float* u;
+  float* uinv;
+  float* linvf;
 };
 
 size_t factor_ws_bytes(int64_t n, int64_t ldl) {
   const int64_t nblk = (n + PB - 1) / PB;
-  return (size_t)(2 * nblk * PB * PB + n * ldl) * sizeof(float) + 256;
+  return (size_t)(nblk * PB * PB + 2 * n * ldl) * sizeof(float) + 256;
 }
 
-FactorWs factor_ws(void* ws, int64_t n) {
+FactorWs factor_ws(void* ws, int64_t n, int64_t ldl) {
   const int64_t nblk = (n + PB - 1) / PB;
   char* p = static_cast<char*>(ws);
   p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 255) & ~(uintptr_t)255);
   FactorWs f;
   f.linv = reinterpret_cast<float*>(p);
-  f.linvT = f.linv + nblk * PB * PB;
-  f.u = f.linvT + nblk * PB * PB;
+  f.uinv = f.linv + nblk * PB * PB;
+  f.linvf = f.uinv + n * ldl;
   return f;
 }
 
-// Solve workspace: rnorm (256 B), x64 [n m] f64, r32 [n m] f32, flags [2 nblk] i32,
-// z [m_pad * ldz] f32 for the many-right-hand-side path (ldz = ldl).
-// For m <= kSmallM the PCG vectors follow: r64, p64, q64 [n m] f64, three dot-product
-// partial arrays [kDotBlocks * kSmallM] f64 and the PcgState.
+// Solve workspace: rnorm (256 B), x64 [n m] f64, r32 [n m] f32, t32 [n m] f32, then
+// for m <= kSmallM the PCG vectors r64, p64, q64 [n m] f64, three dot-product partial
+// arrays [kDotBlocks * kSmallM] f64 and the PcgState; for more, z [m * ldl] f32 and
+// y [m * ldl] f32 (the transposed right-hand sides and their half-solved form).
 size_t solve_ws_bytes(int64_t n, int64_t m, int64_t ldl) {
-  const int64_t nblk = (n + PB - 1) / PB;
-  size_t b = 256 + (size_t)n * m * (sizeof(double) + sizeof(float)) + 2 * nblk * sizeof(int) + 256;
-  if (m > kSmallM) b += (size_t)m * ldl * sizeof(float) + 256;
+  size_t b = 256 + (size_t)n * m * (sizeof(double) + 2 * sizeof(float)) + 256;
+  if (m > kSmallM) b += 2 * (size_t)m * ldl * sizeof(float) + 512;
   else b += (size_t)3 * n * m * sizeof(double) + 3 * kDotBlocks * kSmallM * sizeof(double) +
             sizeof(PcgState) + 256;
   return (b + 255) & ~(size_t)255;
 }
 
-int coop_trsv(cudaStream_t s, const float* L, int64_t ldl, const FactorWs& f, int64_t n,
-              float* X, int64_t m, int* flags, int backward, const int* skip = nullptr) {
-  const int64_t nblk = (n + PB - 1) / PB;
-  if (cudaMemsetAsync(flags, 0, sizeof(int) * nblk, s) != cudaSuccess)
-    return check_launch("ntg_chol_solve_tc flags");
-  static int max_ctas = 0;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    int per_sm = 0, dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trsv_coop_kernel, 256, kTrsvSmem);
-    max_ctas = per_sm * sms;
-  });
-  if (max_ctas <= 0) return fail(NTG_ERR_CUDA, "ntg_chol_solve_tc: no co-resident CTAs");
-  const int grid = (int)mini(nblk, max_ctas);
-  const float* linv = f.linv;
-  const float* linvT = f.linvT;
-  int bw = backward;
-  void* args[] = {(void*)&L, (void*)&ldl, (void*)&linv, (void*)&linvT, (void*)&n, (void*)&X,
-                  (void*)&m, (void*)&flags, (void*)&bw, (void*)&skip};
-  const cudaError_t e = cudaLaunchCooperativeKernel((const void*)trsv_coop_kernel, grid, 256,
-                                                    args, kTrsvSmem, s);
-  note_launch();
-  if (e != cudaSuccess)
-    return fail(NTG_ERR_CUDA, std::string("ntg_chol_solve_tc: ") + cudaGetErrorString(e));
-  return NTG_OK;
+// X = (L L^T)^-1 X for up to kSmallM right-hand sides: t = L^-1 X, X = L^-T t.
+int inv_apply_small(cudaStream_t s, const FactorWs& f, int64_t ldl, int64_t n, float* X, int64_t m,
+                    float* t, const int* skip) {
+  const unsigned g = (unsigned)ceil_div(n, 8);
+  tri_gemv_kernel<kSmallM><<<g, 256, 0, s>>>(f.linvf, ldl, n, 0, X, m, t, skip);
+  tri_gemv_kernel<kSmallM><<<g, 256, 0, s>>>(f.uinv, ldl, n, 1, t, m, X, skip);
+  note_launch(2);
+  return check_launch("ntg_chol_solve_tc apply");
 }
 
-// Many right-hand sides: Z = X^T [m, ldz]; forward Z_b = (Z_b) Linv_b^T then
-// Z[:, >b] -= Z_b L[>b rows, b]^T; backward Z_b = Z_b Linv_b then Z[:, <b] -= Z_b U[<b, b]^T.
-int gemm_trsm(cudaStream_t s, const float* L, int64_t ldl, const FactorWs& f, int64_t n,
-              float* X, int64_t m, float* z, int64_t ldz) {
-  const int64_t nblk = (n + PB - 1) / PB;
+// X = (L L^T)^-1 X for many right-hand sides on the tensor cores, through the transposed
+// right-hand sides z = X^T [m, ldl]: y = z L^-T (= (L^-1 X)^T), z = y L^-1 (= X'^T).
+int inv_apply_many(cudaStream_t s, const FactorWs& f, int64_t ldl, int64_t n, float* X, int64_t m,
+                   float* z, float* y) {
   {
     dim3 g((unsigned)ceil_div(m, 32), (unsigned)ceil_div(n, 32));
-    transpose_kernel<<<g, 256, 0, s>>>(X, m, z, ldz, n, m);
+    transpose_kernel<<<g, 256, 0, s>>>(X, m, z, ldl, n, m);
     note_launch();
   }
-  int rc;
-  for (int64_t bb = 0; bb < nblk; ++bb) {
-    const int64_t b = bb;
-    const int64_t r0 = b * PB;
-    const int64_t nb = mini(PB, n - r0);
-    rc = gemm_tf32x3(s, z + r0, ldz, f.linv + b * PB * PB, PB, z + r0, ldz, m, nb, nb, 1.f, 0.f, 0);
-    if (rc) return rc;
-    const int64_t rest = n - r0 - nb;
-    if (rest > 0) {
-      rc = gemm_tf32x3(s, z + r0, ldz, L + (r0 + nb) * ldl + r0, ldl, z + r0 + nb, ldz, m, rest,
-                       nb, -1.f, 1.f, 0);
-      if (rc) return rc;
-    }
-  }
-  for (int64_t bb = 0; bb < nblk; ++bb) {
-    const int64_t b = nblk - 1 - bb;
-    const int64_t r0 = b * PB;
-    const int64_t nb = mini(PB, n - r0);
-    rc = gemm_tf32x3(s, z + r0, ldz, f.linvT + b * PB * PB, PB, z + r0, ldz, m, nb, nb, 1.f, 0.f,
-                     0);
-    if (rc) return rc;
-    if (r0 > 0) {
-      rc = gemm_tf32x3(s, z + r0, ldz, f.u + r0, ldl, z, ldz, m, r0, nb, -1.f, 1.f, 0);
-      if (rc) return rc;
-    }
-  }
+  // y[c, j] = sum_i z[c, i] L^-1[j, i]: NT with B = L^-1 (row-major)
+  int rc = gemm_tf32x3(s, z, ldl, f.linvf, ldl, y, ldl, m, n, n, 1.f, 0.f, 0);
+  if (rc) return rc;
+  // z[c, i] = sum_j y[c, j] L^-T[i, j]: NT with B = L^-T (row-major)
+  rc = gemm_tf32x3(s, y, ldl, f.uinv, ldl, z, ldl, m, n, n, 1.f, 0.f, 0);
+  if (rc) return rc;
   {
     dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(m, 32));
-    transpose_kernel<<<g, 256, 0, s>>>(z, ldz, X, m, m, n);
+    transpose_kernel<<<g, 256, 0, s>>>(z, ldl, X, m, m, n);
     note_launch();
   }
-  return check_launch("ntg_chol_solve_tc trsm");
+  return check_launch("ntg_chol_solve_tc apply");
 }
 
 }  // namespace
@@ -874,7 +784,7 @@ extern "C" int ntg_chol_factor_tc(void* stream, const float* A, int64_t n, doubl
   int rc = attrs_once();
   if (rc) return rc;
   cudaStream_t s = as_stream(stream);
-  const FactorWs f = factor_ws(workspace, n);
+  const FactorWs f = factor_ws(workspace, n, ldl);
   if (cudaMemsetAsync(info, 0, sizeof(int), s) != cudaSuccess)
     return check_launch("ntg_chol_factor_tc memset");
   trace_tc_kernel<<<1, 1024, 0, s>>>(A, n, lambda + 1);
@@ -884,8 +794,7 @@ extern "C" int ntg_chol_factor_tc(void* stream, const float* A, int64_t n, doubl
   const int64_t nblk = (n + PB - 1) / PB;
   for (int64_t b = 0; b < nblk; ++b) {
     const int64_t k = b * PB;
-    diag_block_kernel<<<1, 512, kDiagSmem, s>>>(L, ldl, n, k, info, f.linv + b * PB * PB,
-                                                f.linvT + b * PB * PB);
+    diag_block_kernel<<<1, 512, kDiagSmem, s>>>(L, ldl, n, k, info, f.linv + b * PB * PB);
     note_launch();
     const int64_t rest = n - k - PB;
     if (rest > 0) {
@@ -898,8 +807,25 @@ extern "C" int ntg_chol_factor_tc(void* stream, const float* A, int64_t n, doubl
       if (rc) return rc;
     }
   }
+  // L^-T by the forward block solve of L Y = I on the transposed side, Z = Y^T: per
+  // block b, Z[:, b] <- Z[:, b] Linv_b^T, then Z[:, >b] -= Z[:, b] L[>b, b]^T, where only
+  // the rows [0, r0 + nb) of Z[:, b] are non-zero (Z is upper triangular)
+  identity_kernel<<<grid_for(n * ldl), 256, 0, s>>>(f.uinv, n, ldl);
+  note_launch();
+  for (int64_t b = 0; b < nblk; ++b) {
+    const int64_t r0 = b * PB, nb = mini(PB, n - r0), rows = r0 + nb;
+    rc = gemm_tf32x3(s, f.uinv + r0, ldl, f.linv + b * PB * PB, PB, f.uinv + r0, ldl, rows, nb,
+                     nb, 1.f, 0.f, 0);
+    if (rc) return rc;
+    const int64_t rest = n - rows;
+    if (rest > 0) {
+      rc = gemm_tf32x3(s, f.uinv + r0, ldl, L + rows * ldl + r0, ldl, f.uinv + rows, ldl, rows,
+                       rest, nb, -1.f, 1.f, 0);
+      if (rc) return rc;
+    }
+  }
   dim3 g((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n, 32));
-  transpose_kernel<<<g, 256, 0, s>>>(L, ldl, f.u, ldl, n, n);
+  transpose_kernel<<<g, 256, 0, s>>>(f.uinv, ldl, f.linvf, ldl, n, n);
   note_launch();
   return check_launch("ntg_chol_factor_tc");
 }
@@ -920,41 +846,39 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
               "ntg_chol_solve_tc: null pointer");
   NTG_REQUIRE(n > 0 && n <= 46340 && m > 0, "ntg_chol_solve_tc: bad sizes");
   NTG_REQUIRE(ldl >= n && ldl % 4 == 0, "ntg_chol_solve_tc: bad ldl");
-  NTG_REQUIRE(refine_iters >= 0 && refine_iters <= 16, "ntg_chol_solve_tc: 0..16 refinement steps");
+  NTG_REQUIRE(refine_iters >= 0 && refine_iters <= 64, "ntg_chol_solve_tc: 0..64 refinement steps");
   NTG_REQUIRE(m <= (1ll << 31) / 64, "ntg_chol_solve_tc: too many right-hand sides");
   NTG_REQUIRE(workspace_bytes >= ntg_chol_solve_tc_workspace_bytes(n, m, ldl),
               "ntg_chol_solve_tc: workspace smaller than ntg_chol_solve_tc_workspace_bytes");
+  (void)L;  // the solves use the inverse factors kept in factor_workspace
   int rc = attrs_once();
   if (rc) return rc;
   cudaStream_t s = as_stream(stream);
-  const FactorWs f = factor_ws(const_cast<void*>(factor_workspace), n);
+  const FactorWs f = factor_ws(const_cast<void*>(factor_workspace), n, ldl);
   char* ws = static_cast<char*>(workspace);
-  const int64_t nblk = (n + PB - 1) / PB;
   double* rnorm = reinterpret_cast<double*>(ws);
   double* x64 = reinterpret_cast<double*>(ws + 256);
   float* r32 = reinterpret_cast<float*>(x64 + n * m);
-  int* flags = reinterpret_cast<int*>(r32 + n * m);
-  float* z = reinterpret_cast<float*>(
-      (reinterpret_cast<uintptr_t>(flags + 2 * nblk) + 255) & ~(uintptr_t)255);
-  auto solve = [&](float* xx, const int* skip) -> int {
-    if (m <= kSmallM) {
-      int r = coop_trsv(s, L, ldl, f, n, xx, m, flags, 0, skip);
-      if (r) return r;
-      return coop_trsv(s, L, ldl, f, n, xx, m, flags + nblk, 1, skip);
-    }
-    return gemm_trsm(s, L, ldl, f, n, xx, m, z, ldl);
+  float* t32 = r32 + n * m;
+  char* tail = reinterpret_cast<char*>(
+      (reinterpret_cast<uintptr_t>(t32 + n * m) + 255) & ~(uintptr_t)255);
+  float* z = reinterpret_cast<float*>(tail);
+  float* y = reinterpret_cast<float*>(
+      (reinterpret_cast<uintptr_t>(z + m * ldl) + 255) & ~(uintptr_t)255);
+  auto apply = [&](float* xx, const int* skip) -> int {
+    if (m <= kSmallM) return inv_apply_small(s, f, ldl, n, xx, m, t32, skip);
+    return inv_apply_many(s, f, ldl, n, xx, m, z, y);
   };
   if (cudaMemcpyAsync(X, B, sizeof(float) * n * m, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
     return check_launch("ntg_chol_solve_tc copy");
-  rc = solve(X, nullptr);
+  rc = apply(X, nullptr);
   if (rc) return rc;
   if (refine_iters == 0 && !final_residual) return check_launch("ntg_chol_solve_tc");
   to_double_tc_kernel<<<grid_for(n * m), 256, 0, s>>>(X, x64, n * m);
   note_launch();
   if (m <= kSmallM) {
     // preconditioned conjugate gradients on (K + lambda I) x = b from x0 = (L L^T)^-1 b
-    double* r64 = reinterpret_cast<double*>(
-        (reinterpret_cast<uintptr_t>(flags + 2 * nblk) + 255) & ~(uintptr_t)255);
+    double* r64 = reinterpret_cast<double*>(tail);
     double* p64 = r64 + n * m;
     double* q64 = p64 + n * m;
     double* part = q64 + n * m;
@@ -966,10 +890,10 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
                                                               r32, nullptr);
     note_launch();
     if (refine_iters > 0) {
-      rc = solve(r32, nullptr);  // z0
+      rc = apply(r32, nullptr);  // z0
       if (rc) return rc;
       col_dots_kernel<<<kDotBlocks, 256, 0, s>>>(r64, nullptr, r32, n, m, part_rz, nullptr);
-      pcg_init_kernel<<<1, 1024, 0, s>>>(B, r32, p64, n, m, part_rz, st);
+      pcg_init_kernel<<<1, 1024, 0, s>>>(B, r32, p64, r64, n, m, part_rz, st);
       note_launch(2);
       for (int it = 0; it < refine_iters; ++it) {
         const int cur = it & 1;
@@ -980,7 +904,7 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
                                                    st, cur);
         pcg_check_kernel<<<1, 32, 0, s>>>(part_r, m, kDotBlocks, st);
         note_launch(4);
-        rc = solve(r32, &st->all_done);
+        rc = apply(r32, &st->all_done);
         if (rc) return rc;
         col_dots_kernel<<<kDotBlocks, 256, 0, s>>>(r64, nullptr, r32, n, m, part_rz, st);
         pcg_dir_kernel<<<kDotBlocks, 256, 0, s>>>(p64, r32, n, m, part_rz, st, cur);
@@ -1012,7 +936,7 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
         A, n, lambda, B, x64, m, r32, rnorm);
     note_launch();
     if (it == refine_iters) break;
-    rc = solve(r32, nullptr);
+    rc = apply(r32, nullptr);
     if (rc) return rc;
     accumulate_tc_kernel<<<grid_for(n * m), 256, 0, s>>>(x64, r32, X, n * m);
     note_launch();

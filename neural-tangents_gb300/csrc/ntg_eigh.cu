@@ -15,6 +15,8 @@
 //   jacobi_apply_v_kernel V <- V U.
 // After each sweep off(A) / ||A||_F is read back (one 16-byte copy) and the sweeps
 // stop below the tolerance. Eigenvalues are the diagonal of the final A, not sorted.
+// FP32 rounding accumulates over the rounds (about 1e-5 relative at n = 1000), so the
+// pairs are then refined with double-float products (see the refinement below).
 #include <cmath>
 #include <string>
 #include <vector>
@@ -348,6 +350,128 @@ __global__ void spectral_scale_kernel(const float* __restrict__ evals, const dou
   }
 }
 
+// ---------------------------------------------------------------------------
+// Refinement of the Jacobi eigenpairs (Ogita & Aishima, "Iterative refinement for
+// symmetric eigenvalue decomposition", Japan J. Indust. Appl. Math. 35 (2018)):
+// with X the approximate eigenvectors, R = I - X^T X and S = X^T (A X) formed in
+// double-float, lambda_i = S_ii / (1 - R_ii) and X <- X + X E with
+// E_ij = (S_ij + lambda_j R_ij) / (lambda_j - lambda_i) for separated pairs,
+// E_ij = R_ij / 2 for pairs whose gap is not large against that numerator (a
+// cluster: only orthogonalised), E_ii = R_ii / 2.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void df_fma_e(float a, float xh, float xl, float& sh, float& sl) {
+  const float ph = a * xh;
+  float pl = fmaf(a, xh, -ph);
+  pl = fmaf(a, xl, pl);
+  const float s2 = sh + ph;
+  const float bv = s2 - sh;
+  const float e = (sh - (s2 - bv)) + (ph - bv);
+  sl += e + pl;
+  sh = s2;
+}
+
+// C[i, j] = sum_k P[k, i] (Qh[k, j] + Ql[k, j]) + shift (Qh[i, j] + Ql[i, j]) over 64 x 64
+// tiles, double-float sums; P, Qh, Ql [n, n] row-major (Ql may be NULL). Output as
+// FP64 (c64) or as a double-float pair (ch, cl).
+__global__ void __launch_bounds__(256)
+    df_gemm_tn_kernel(const float* __restrict__ P, const float* __restrict__ Qh,
+                      const float* __restrict__ Ql, int64_t n, double shift,
+                      double* __restrict__ c64, float* __restrict__ ch, float* __restrict__ cl) {
+  __shared__ float Ps[16][64 + 1];
+  __shared__ float Hs[16][64 + 1];
+  __shared__ float Ls[16][64 + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t i0 = (int64_t)blockIdx.y * 64, j0 = (int64_t)blockIdx.x * 64;
+  float sh[4][4] = {}, sl[4][4] = {};
+  for (int64_t k0 = 0; k0 < n; k0 += 16) {
+    for (int idx = threadIdx.x; idx < 16 * 64; idx += 256) {
+      const int kk = idx / 64, c = idx % 64;
+      const bool kin = k0 + kk < n;
+      Ps[kk][c] = (kin && i0 + c < n) ? P[(k0 + kk) * n + i0 + c] : 0.f;
+      Hs[kk][c] = (kin && j0 + c < n) ? Qh[(k0 + kk) * n + j0 + c] : 0.f;
+      Ls[kk][c] = (Ql && kin && j0 + c < n) ? Ql[(k0 + kk) * n + j0 + c] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      float av[4], hv[4], lv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        av[u] = Ps[k][ty * 4 + u];
+        hv[u] = Hs[k][tx * 4 + u];
+        lv[u] = Ls[k][tx * 4 + u];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) df_fma_e(av[u], hv[v], lv[v], sh[u][v], sl[u][v]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    const int64_t i = i0 + ty * 4 + u;
+    if (i >= n) continue;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int64_t j = j0 + tx * 4 + v;
+      if (j >= n) continue;
+      double val = (double)sh[u][v] + (double)sl[u][v];
+      if (shift != 0.0)
+        val += shift * ((double)Qh[i * n + j] + (Ql ? (double)Ql[i * n + j] : 0.0));
+      if (c64) c64[i * n + j] = val;
+      if (ch) {
+        const float h = (float)val;
+        ch[i * n + j] = h;
+        cl[i * n + j] = (float)(val - (double)h);
+      }
+    }
+  }
+}
+
+// R <- I - R
+__global__ void identity_minus_kernel(double* __restrict__ R, int64_t n) {
+  const int64_t total = n * n;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx / n, j = idx - i * n;
+    R[idx] = (i == j ? 1.0 : 0.0) - R[idx];
+  }
+}
+
+__global__ void refine_lambda_kernel(const double* __restrict__ S, const double* __restrict__ R,
+                                     int64_t n, double* __restrict__ lam) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    lam[i] = S[i * n + i] / (1.0 - R[i * n + i]);
+}
+
+// E = the correction of X (see above); X1 = X (for the accumulate of X + X E).
+__global__ void refine_e_kernel(const double* __restrict__ S, const double* __restrict__ R,
+                                const double* __restrict__ lam, int64_t n, float* __restrict__ E) {
+  const int64_t total = n * n;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = idx / n, j = idx - i * n;
+    const double r = R[idx];
+    double e = 0.5 * r;
+    if (i != j) {
+      const double num = S[idx] + lam[j] * r;
+      const double gap = lam[j] - lam[i];
+      if (fabs(gap) > 1e3 * fabs(num)) e = num / gap;
+    }
+    E[idx] = (float)e;
+  }
+}
+
+__global__ void lam_to_float_kernel(const double* __restrict__ lam, int64_t n,
+                                    float* __restrict__ evals) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    evals[i] = (float)lam[i];
+}
+
 int egrid(int64_t n) {
   int64_t g = (n + 255) / 256;
   return (int)(g > 152 * 16 ? 152 * 16 : (g < 1 ? 1 : g));
@@ -379,19 +503,25 @@ EighWs eigh_ws(void* ws, int64_t npad) {
 
 using namespace ntg;
 
+// Refinement buffers after the Jacobi ones: S, R [n n] f64, lam [n] f64, Yh, Yl, E [n n] f32.
+size_t refine_bytes(int64_t n) {
+  return (size_t)(2 * n * n + n) * sizeof(double) + (size_t)3 * n * n * sizeof(float) + 1024;
+}
+
 extern "C" size_t ntg_eigh_workspace_bytes(int64_t n) {
   if (n <= 0 || n > 32768) return SIZE_MAX;
   const int64_t npad = (n + JP - 1) / JP * JP;
   return (size_t)(2 * npad * npad + (npad / JP) * JP * JP) * sizeof(float) + 2 * sizeof(double) +
-         sizeof(int) + 512;
+         sizeof(int) + 512 + refine_bytes(n);
 }
 
 extern "C" int ntg_eigh(void* stream, const float* A, int64_t n, double shift, float* evals,
-                        float* evecs, int32_t max_sweeps, double tol, void* workspace,
-                        size_t workspace_bytes, int32_t* sweeps_out) {
+                        float* evecs, int32_t max_sweeps, double tol, int32_t refine_steps,
+                        void* workspace, size_t workspace_bytes, int32_t* sweeps_out) {
   NTG_REQUIRE(A && evals && evecs && workspace, "ntg_eigh: null pointer");
   NTG_REQUIRE(n > 0 && n <= 32768, "ntg_eigh: n must be in [1, 32768]");
   NTG_REQUIRE(max_sweeps > 0 && max_sweeps <= 100, "ntg_eigh: max_sweeps in [1, 100]");
+  NTG_REQUIRE(refine_steps >= 0 && refine_steps <= 4, "ntg_eigh: refine_steps in [0, 4]");
   NTG_REQUIRE(workspace_bytes >= ntg_eigh_workspace_bytes(n),
               "ntg_eigh: workspace smaller than ntg_eigh_workspace_bytes(n)");
   cudaStream_t s = as_stream(stream);
@@ -425,6 +555,35 @@ extern "C" int ntg_eigh(void* stream, const float* A, int64_t n, double shift, f
   }
   eigh_extract_kernel<<<egrid(n * n), 256, 0, s>>>(e.w, e.v, npad, n, evals, evecs);
   note_launch();
+  if (refine_steps > 0) {
+    char* rp = reinterpret_cast<char*>(
+        (reinterpret_cast<uintptr_t>(e.done + 1) + 255) & ~(uintptr_t)255);
+    double* S = reinterpret_cast<double*>(rp);
+    double* R = S + n * n;
+    double* lam = R + n * n;
+    float* yh = reinterpret_cast<float*>(lam + n);
+    float* yl = yh + n * n;
+    float* E = yl + n * n;
+    const dim3 g((unsigned)ceil_div(n, 64), (unsigned)ceil_div(n, 64));
+    for (int it = 0; it < refine_steps; ++it) {
+      // Y = (K + shift I) X (K symmetric: K^T X), S = X^T Y, R = X^T X (as -R + I below)
+      df_gemm_tn_kernel<<<g, 256, 0, s>>>(A, evecs, nullptr, n, shift, nullptr, yh, yl);
+      df_gemm_tn_kernel<<<g, 256, 0, s>>>(evecs, yh, yl, n, 0.0, S, nullptr, nullptr);
+      df_gemm_tn_kernel<<<g, 256, 0, s>>>(evecs, evecs, nullptr, n, 0.0, R, nullptr, nullptr);
+      identity_minus_kernel<<<egrid(n * n), 256, 0, s>>>(R, n);
+      refine_lambda_kernel<<<egrid(n), 256, 0, s>>>(S, R, n, lam);
+      refine_e_kernel<<<egrid(n * n), 256, 0, s>>>(S, R, lam, n, E);
+      note_launch(6);
+      // X <- X + X E (the product reads a copy of X)
+      if (cudaMemcpyAsync(yh, evecs, sizeof(float) * n * n, cudaMemcpyDeviceToDevice, s) !=
+          cudaSuccess)
+        return check_launch("ntg_eigh refine copy");
+      const int rc = ntg_gemm(stream, yh, E, evecs, n, n, n, 1);
+      if (rc) return rc;
+    }
+    lam_to_float_kernel<<<egrid(n), 256, 0, s>>>(lam, n, evals);
+    note_launch();
+  }
   if (sweeps_out) *sweeps_out = sweeps;
   return check_launch("ntg_eigh");
 }

@@ -9,7 +9,8 @@
 // four converter warps split each tile in place (hi) and into a second buffer
 // (lo) and hand the stage to the MMA thread, which issues 12 MMAs per stage and
 // frees it with tcgen05.commit; the converter warps then drain the accumulator
-// with tcgen05.ld and apply alpha, beta. With `lower` set only the tiles on or
+// with tcgen05.ld into the idle ring, from which all warps write C row by row
+// (coalesced) with alpha, beta applied. With `lower` set only the tiles on or
 // below the diagonal are computed and only entries with col <= row written (the
 // symmetric rank-k update of a Cholesky factorisation). Every wait is bounded:
 // one that runs out raises the device error word, lets the copies and MMAs in
@@ -225,36 +226,45 @@ __global__ void __launch_bounds__(GTHREADS, 1)
     }
     ready = tc::mbar_wait(tc::smem_u32(&bars[3 * GSTAGES]), 0, GWAIT);
     ready = __all_sync(0xffffffffu, ready);
-    tc::fence_after();
-    if (!ready) {
-      if (lane == 0) {
-        atomicExch(&g_gemm_error, NTG_ERR_WAIT_TIMEOUT);
-        s_fail = 1;
-      }
-    } else {
-      // warp w reads TMEM lanes 32 (w % 4) .. + 31: rows of the tile
-      const int q = warp & 3;
-      const int64_t row = m0 + q * 32 + lane;
-#pragma unroll 1
-      for (int c0 = 0; c0 < GN; c0 += 32) {
-        uint32_t v[32];
-        tc::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
-        if (row < p.m) {
-          float* crow = p.c + row * p.ldc + n0 + c0;
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int64_t col = n0 + c0 + j;
-            if (col < p.n && (!p.lower || col <= row)) {
-              float r = p.alpha * __uint_as_float(v[j]);
-              if (p.beta != 0.f) r = fmaf(p.beta, crow[j], r);
-              crow[j] = r;
-            }
-          }
-        }
-      }
+    if (!ready && lane == 0) {
+      atomicExch(&g_gemm_error, NTG_ERR_WAIT_TIMEOUT);
+      s_fail = 1;
     }
   }
 
+  // Epilogue through shared memory: the split warps move the accumulator from TMEM into
+  // the (now idle) stage buffers, then all six warps write C row by row, coalesced.
+  tc::fence_before();
+  __syncthreads();
+  const bool acc_ok = !s_fail;
+  float* stile = reinterpret_cast<float*>(smem);  // [128][129] floats, 66 KB of the ring
+  constexpr int SP = GN + 1;
+  if (acc_ok && warp >= 2) {
+    tc::fence_after();
+    const int q = warp & 3;
+#pragma unroll 1
+    for (int c0 = 0; c0 < GN; c0 += 32) {
+      uint32_t v[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, v);
+      float* dst = stile + (q * 32 + lane) * SP + c0;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) dst[j] = __uint_as_float(v[j]);
+    }
+  }
+  __syncthreads();
+  if (acc_ok) {
+    const int nthr = GTHREADS;
+    for (int idx = threadIdx.x; idx < GM * GN; idx += nthr) {
+      const int r = idx / GN, cc = idx % GN;
+      const int64_t row = m0 + r, col = n0 + cc;
+      if (row < p.m && col < p.n && (!p.lower || col <= row)) {
+        float* cp = p.c + row * p.ldc + col;
+        float val = p.alpha * stile[r * SP + cc];
+        if (p.beta != 0.f) val = fmaf(p.beta, *cp, val);
+        *cp = val;
+      }
+    }
+  }
   tc::fence_before();
   __syncthreads();
   if (s_fail) {

@@ -51,17 +51,20 @@ def _gemm_tn(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     return out
 
 
-def _eigh(k: torch.Tensor, shift: float, max_sweeps: int = 20, tol: float = 2e-7):
-    """Eigenpairs of k + shift I on this library's block-Jacobi kernels (FP32):
-    (evals [n], evecs [n, n], column j for evals[j]), evals not sorted."""
+def _eigh(k: torch.Tensor, shift: float, max_sweeps: int = 20, tol: float = 2e-7,
+          refine_steps: int = 2):
+    """Eigenpairs of k + shift I on this library's block-Jacobi kernels (FP32) with
+    `refine_steps` double-float refinement steps: (evals [n], evecs [n, n], column j
+    for evals[j]), evals not sorted."""
     n = k.shape[0]
     lib = L.load()
     nbytes = int(lib.ntg_eigh_workspace_bytes(n))
     ws = torch.empty((nbytes,), device=k.device, dtype=torch.uint8)
     evals = torch.empty((n,), device=k.device, dtype=torch.float32)
     evecs = torch.empty((n, n), device=k.device, dtype=torch.float32)
-    L.call('ntg_eigh', L.stream(), L.ptr(k), n, float(shift), L.ptr(evals), L.ptr(evecs),
-           int(max_sweeps), float(tol), ws.data_ptr(), nbytes, None)
+    L.call('ntg_eigh', L.stream(), L.ptr(k.contiguous()), n, float(shift), L.ptr(evals),
+           L.ptr(evecs), int(max_sweeps), float(tol), int(refine_steps), ws.data_ptr(), nbytes,
+           None)
     return evals, evecs
 
 

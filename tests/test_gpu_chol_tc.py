@@ -107,4 +107,5 @@ def test_logdet_matches_float64(nt):
     s = _factor(nt, k, 1e-3)
     a = k.astype(np.float64) + 1e-3 * np.trace(k.astype(np.float64)) / 400 * np.eye(400)
     want = np.linalg.slogdet(a)[1]
-    assert abs(float(s.logdet().item()) - want) < 1e-5 * abs(want)
+    # each pivot carries the float32 factor's rounding (cond ~ 1e3 here)
+    assert abs(float(s.logdet().item()) - want) < 5e-5 * abs(want)
