@@ -356,8 +356,8 @@ __global__ void spectral_scale_kernel(const float* __restrict__ evals, const dou
 // with X the approximate eigenvectors, R = I - X^T X and S = X^T (A X) formed in
 // double-float, lambda_i = S_ii / (1 - R_ii) and X <- X + X E with
 // E_ij = (S_ij + lambda_j R_ij) / (lambda_j - lambda_i) for separated pairs,
-// E_ij = R_ij / 2 for pairs whose gap is not large against that numerator (a
-// cluster: only orthogonalised), E_ii = R_ii / 2.
+// E_ij = R_ij / 2 for pairs whose gap is not large against that numerator or is
+// below 1e-6 of the largest |lambda| (a cluster: only orthogonalised), E_ii = R_ii / 2.
 // ---------------------------------------------------------------------------
 
 __device__ __forceinline__ void df_fma_e(float a, float xh, float xl, float& sh, float& sl) {
@@ -440,11 +440,20 @@ __global__ void identity_minus_kernel(double* __restrict__ R, int64_t n) {
   }
 }
 
+// lam_i = S_ii / (1 - R_ii); lam[n] receives max |lam_i| (zeroed by the caller).
 __global__ void refine_lambda_kernel(const double* __restrict__ S, const double* __restrict__ R,
                                      int64_t n, double* __restrict__ lam) {
+  double mx = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
+       i += (int64_t)gridDim.x * blockDim.x) {
     lam[i] = S[i * n + i] / (1.0 - R[i * n + i]);
+    mx = fmax(mx, fabs(lam[i]));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0 && mx > 0.0)
+    atomicMax(reinterpret_cast<unsigned long long*>(lam + n),
+              (unsigned long long)__double_as_longlong(mx));
 }
 
 // E = the correction of X (see above); X1 = X (for the accumulate of X + X E).
@@ -457,9 +466,11 @@ __global__ void refine_e_kernel(const double* __restrict__ S, const double* __re
     const double r = R[idx];
     double e = 0.5 * r;
     if (i != j) {
+      // separated: the gap is large against the coupling and above the resolution of the
+      // float32 eigenvalues (1e-6 of the largest); closer pairs are a cluster
       const double num = S[idx] + lam[j] * r;
       const double gap = lam[j] - lam[i];
-      if (fabs(gap) > 1e3 * fabs(num)) e = num / gap;
+      if (fabs(gap) > 1e3 * fabs(num) && fabs(gap) > 1e-6 * lam[n]) e = num / gap;
     }
     E[idx] = (float)e;
   }
@@ -505,7 +516,7 @@ using namespace ntg;
 
 // Refinement buffers after the Jacobi ones: S, R [n n] f64, lam [n] f64, Yh, Yl, E [n n] f32.
 size_t refine_bytes(int64_t n) {
-  return (size_t)(2 * n * n + n) * sizeof(double) + (size_t)3 * n * n * sizeof(float) + 1024;
+  return (size_t)(2 * n * n + n + 1) * sizeof(double) + (size_t)3 * n * n * sizeof(float) + 1024;
 }
 
 extern "C" size_t ntg_eigh_workspace_bytes(int64_t n) {
@@ -561,7 +572,7 @@ extern "C" int ntg_eigh(void* stream, const float* A, int64_t n, double shift, f
     double* S = reinterpret_cast<double*>(rp);
     double* R = S + n * n;
     double* lam = R + n * n;
-    float* yh = reinterpret_cast<float*>(lam + n);
+    float* yh = reinterpret_cast<float*>(lam + n + 1);
     float* yl = yh + n * n;
     float* E = yl + n * n;
     const dim3 g((unsigned)ceil_div(n, 64), (unsigned)ceil_div(n, 64));
@@ -571,6 +582,8 @@ extern "C" int ntg_eigh(void* stream, const float* A, int64_t n, double shift, f
       df_gemm_tn_kernel<<<g, 256, 0, s>>>(evecs, yh, yl, n, 0.0, S, nullptr, nullptr);
       df_gemm_tn_kernel<<<g, 256, 0, s>>>(evecs, evecs, nullptr, n, 0.0, R, nullptr, nullptr);
       identity_minus_kernel<<<egrid(n * n), 256, 0, s>>>(R, n);
+      if (cudaMemsetAsync(lam + n, 0, sizeof(double), s) != cudaSuccess)
+        return check_launch("ntg_eigh refine");
       refine_lambda_kernel<<<egrid(n), 256, 0, s>>>(S, R, n, lam);
       refine_e_kernel<<<egrid(n * n), 256, 0, s>>>(S, R, lam, n, E);
       note_launch(6);
