@@ -454,13 +454,28 @@ __device__ __forceinline__ void df_add(float& sh, float& sl, float bh, float bl)
   sh = s;
 }
 
-// out = B - (K + lambda I) X (subtract = 1) or (K + lambda I) X (subtract = 0), X FP64
-// [n, m]; one warp per row, double-float sums of the m <= MR products kept per lane.
+// X (FP64 [n, m]) as double-float pairs xs[j, c] = (hi, lo), split once per product so
+// that the row kernel below runs on the FP32 pipes only.
+__global__ void split_df_kernel(const double* __restrict__ X, int64_t total,
+                                float2* __restrict__ xs, const PcgState* st) {
+  if (st && st->all_done) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = X[i];
+    const float h = (float)v;
+    xs[i] = make_float2(h, (float)(v - (double)h));
+  }
+}
+
+// out = B - (K + lambda I) X (subtract = 1) or (K + lambda I) X (subtract = 0) with X FP64
+// [n, m] given also as its double-float split xs; one warp per row, double-float sums of
+// the m <= MR products kept per lane.
 template <int MR>
 __global__ void __launch_bounds__(256)
     matvec_df_rows_kernel(const float* __restrict__ A, int64_t n, const double* lambda,
-                          const float* __restrict__ B, const double* __restrict__ X, int64_t m,
-                          int subtract, double* __restrict__ out, float* __restrict__ out32,
+                          const float* __restrict__ B, const double* __restrict__ X,
+                          const float2* __restrict__ xs, int64_t m, int subtract,
+                          double* __restrict__ out, float* __restrict__ out32,
                           const PcgState* st) {
   if (st && st->all_done) return;
   const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
@@ -472,13 +487,12 @@ __global__ void __launch_bounds__(256)
   for (int c = 0; c < MR; ++c) sh[c] = sl[c] = 0.f;
   for (int64_t j = lane; j < n; j += 32) {
     const float a = ar[j];
-    const double* xr = X + j * m;
+    const float2* xr = xs + j * m;
 #pragma unroll
     for (int c = 0; c < MR; ++c)
       if (c < m) {
-        const double xv = xr[c];
-        const float xh = (float)xv;
-        df_fma(a, xh, (float)(xv - (double)xh), sh[c], sl[c]);
+        const float2 xv = xr[c];
+        df_fma(a, xv.x, xv.y, sh[c], sl[c]);
       }
   }
 #pragma unroll
@@ -709,13 +723,14 @@ FactorWs factor_ws(void* ws, int64_t n, int64_t ldl) {
 
 // Solve workspace: rnorm (256 B), x64 [n m] f64, r32 [n m] f32, t32 [n m] f32, then
 // for m <= kSmallM the PCG vectors r64, p64, q64 [n m] f64, three dot-product partial
-// arrays [kDotBlocks * kSmallM] f64 and the PcgState; for more, z [m * ldl] f32 and
+// arrays [kDotBlocks * kSmallM] f64, the PcgState and the double-float split of the
+// current vector [n m] float2; for more, z [m * ldl] f32 and
 // y [m * ldl] f32 (the transposed right-hand sides and their half-solved form).
 size_t solve_ws_bytes(int64_t n, int64_t m, int64_t ldl) {
   size_t b = 256 + (size_t)n * m * (sizeof(double) + 2 * sizeof(float)) + 256;
   if (m > kSmallM) b += 2 * (size_t)m * ldl * sizeof(float) + 512;
   else b += (size_t)3 * n * m * sizeof(double) + 3 * kDotBlocks * kSmallM * sizeof(double) +
-            sizeof(PcgState) + 256;
+            sizeof(PcgState) + 256 + (size_t)n * m * sizeof(float2) + 256;
   return (b + 255) & ~(size_t)255;
 }
 
@@ -885,10 +900,18 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
     double* part_rz = part + kDotBlocks * kSmallM;
     double* part_r = part_rz + kDotBlocks * kSmallM;
     PcgState* st = reinterpret_cast<PcgState*>(part_r + kDotBlocks * kSmallM);
+    float2* xs = reinterpret_cast<float2*>(
+        (reinterpret_cast<uintptr_t>(st + 1) + 255) & ~(uintptr_t)255);
     const unsigned rows_grid = (unsigned)ceil_div(n, 8);
-    matvec_df_rows_kernel<kSmallM><<<rows_grid, 256, 0, s>>>(A, n, lambda, B, x64, m, 1, r64,
-                                                              r32, nullptr);
-    note_launch();
+    // (K + lambda I) v for v = x64 or p64 (subtract: b - ...), through the split of v
+    auto matvec = [&](const double* v, int subtract, const float* bb, double* out, float* o32,
+                      const PcgState* stp) {
+      split_df_kernel<<<grid_for(n * m), 256, 0, s>>>(v, n * m, xs, stp);
+      matvec_df_rows_kernel<kSmallM><<<rows_grid, 256, 0, s>>>(A, n, lambda, bb, v, xs, m,
+                                                                subtract, out, o32, stp);
+      note_launch(2);
+    };
+    matvec(x64, 1, B, r64, r32, nullptr);
     if (refine_iters > 0) {
       rc = apply(r32, nullptr);  // z0
       if (rc) return rc;
@@ -897,8 +920,7 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
       note_launch(2);
       for (int it = 0; it < refine_iters; ++it) {
         const int cur = it & 1;
-        matvec_df_rows_kernel<kSmallM><<<rows_grid, 256, 0, s>>>(A, n, lambda, nullptr, p64, m,
-                                                                  0, q64, nullptr, st);
+        matvec(p64, 0, nullptr, q64, nullptr, st);
         col_dots_kernel<<<kDotBlocks, 256, 0, s>>>(p64, q64, nullptr, n, m, part, st);
         pcg_step_kernel<<<kDotBlocks, 256, 0, s>>>(x64, r64, r32, p64, q64, n, m, part, part_r,
                                                    st, cur);
@@ -915,8 +937,7 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
     }
     if (final_residual) {
       // the true residual of the returned solution
-      matvec_df_rows_kernel<kSmallM><<<rows_grid, 256, 0, s>>>(A, n, lambda, B, x64, m, 1, r64,
-                                                                nullptr, nullptr);
+      matvec(x64, 1, B, r64, nullptr, nullptr);
       if (cudaMemsetAsync(rnorm, 0, sizeof(double), s) != cudaSuccess)
         return check_launch("ntg_chol_solve_tc memset");
       max_abs64_kernel<<<grid_for(n * m), 256, 0, s>>>(r64, n * m, rnorm);
