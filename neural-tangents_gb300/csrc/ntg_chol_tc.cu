@@ -86,43 +86,40 @@ __global__ void init_factor_ld_kernel(const float* __restrict__ A, int64_t n, in
 // ---------------------------------------------------------------------------
 
 // Warp-level Cholesky of the 32 x 32 block at (o, o) of `a` (lower part used) and the
-// inverse of the factor into dinv (lower, row-major 32 x 33). Lane r holds row r.
+// inverse of the factor into dinv (lower, row-major 32 x 33). Lane r owns row r; the
+// pivot column and the solved rows are read from shared memory as broadcasts.
 __device__ void warp_potrf_inv32(float (*a)[PBS], int o, float (*dinv)[33], int* info,
                                  int64_t col0) {
-  const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  float v[32];
-#pragma unroll
-  for (int c = 0; c < 32; ++c) v[c] = a[o + lane][o + c];
-#pragma unroll
+  float* row = &a[o + lane][o];
   for (int j = 0; j < 32; ++j) {
-    float d = __shfl_sync(full, v[j], j);
-    if (!(d > 0.f)) {  // uniform across the warp
+    float d = a[o + j][o + j];
+    if (!(d > 0.f)) {  // the same value in every lane
       if (lane == 0) atomicCAS(info, 0, (int)(col0 + o + j + 1));
       d = 1.f;
     }
-    const float s = sqrtf(d);
-    const float lrj = (lane == j) ? s : v[j] / s;
-    v[j] = lrj;
-#pragma unroll
-    for (int c = j + 1; c < 32; ++c) {
-      const float lcj = __shfl_sync(full, lrj, c);
-      if (lane >= c) v[c] = fmaf(-lrj, lcj, v[c]);
+    const float piv = sqrtf(d);
+    __syncwarp();
+    float l = 0.f;
+    if (lane == j) row[j] = piv;
+    if (lane > j) {
+      l = row[j] / piv;
+      row[j] = l;
     }
+    __syncwarp();
+    if (lane > j)
+      for (int c = j + 1; c <= lane; ++c) row[c] = fmaf(-l, a[o + c][o + j], row[c]);
+    __syncwarp();
   }
-#pragma unroll
-  for (int c = 0; c < 32; ++c) a[o + lane][o + c] = (c <= lane) ? v[c] : 0.f;
+  for (int c = lane + 1; c < 32; ++c) row[c] = 0.f;
+  __syncwarp();
   // X = L^-1, lane c computes column c: x_i = (delta_ic - sum_{p<i} L[i][p] x_p) / L[i][i]
-  float x[32];
-#pragma unroll
   for (int i = 0; i < 32; ++i) {
-    float s = (i == lane) ? 1.f : 0.f;
-#pragma unroll
-    for (int p = 0; p < i; ++p) s = fmaf(-__shfl_sync(full, v[p], i), x[p], s);
-    x[i] = s / __shfl_sync(full, v[i], i);
+    float sacc = (i == lane) ? 1.f : 0.f;
+    for (int p = lane; p < i; ++p) sacc = fmaf(-a[o + i][o + p], dinv[p][lane], sacc);
+    dinv[i][lane] = (i < lane) ? 0.f : sacc / a[o + i][o + i];
   }
-#pragma unroll
-  for (int i = 0; i < 32; ++i) dinv[i][lane] = x[i];
+  __syncwarp();
 }
 
 // Factors L[k:k+nb, k:k+nb] in place (upper part zeroed) and writes the inverse of the
@@ -435,12 +432,15 @@ __global__ void accumulate_tc_kernel(double* __restrict__ x, const float* __rest
 // ---------------------------------------------------------------------------
 constexpr double kPcgTol = 1e-10;   // residual reduction from the starting point
 constexpr double kPcgFloor = 1e-15; // or residual below this times max |b|
+constexpr int kPcgStall = 2;        // or no halving of the best residual for this many steps
 constexpr int kDotBlocks = 128;
 
 struct PcgState {
   double rho[2][kSmallM];   // r.z of the current / next iteration
   double bnorm[kSmallM];    // max |b_j|
   double r0norm[kSmallM];   // max |r_j| of the starting point
+  double rbest[kSmallM];    // smallest max |r_j| so far
+  int stall[kSmallM];       // iterations since rbest last halved
   double rmax[kSmallM];     // max |r_j| of the last residual
   int active[kSmallM];
   int all_done;
@@ -513,6 +513,29 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The row kernel instantiated for the exact number of right-hand sides (1..kSmallM), so
+// no lane issues work for absent columns.
+template <int MR>
+void launch_matvec_t(unsigned grid, cudaStream_t s, const float* A, int64_t n,
+                     const double* lambda, const float* B, const double* X, const float2* xs,
+                     int64_t m, int subtract, double* out, float* out32, const PcgState* st) {
+  matvec_df_rows_kernel<MR><<<grid, 256, 0, s>>>(A, n, lambda, B, X, xs, m, subtract, out,
+                                                 out32, st);
+}
+
+void launch_matvec(int64_t m, unsigned grid, cudaStream_t s, const float* A, int64_t n,
+                   const double* lambda, const float* B, const double* X, const float2* xs,
+                   int subtract, double* out, float* out32, const PcgState* st) {
+  switch (m) {
+#define NTG_MV(k) \
+  case k: launch_matvec_t<k>(grid, s, A, n, lambda, B, X, xs, m, subtract, out, out32, st); break;
+    NTG_MV(1) NTG_MV(2) NTG_MV(3) NTG_MV(4) NTG_MV(5) NTG_MV(6) NTG_MV(7) NTG_MV(8)
+    NTG_MV(9) NTG_MV(10) NTG_MV(11) NTG_MV(12) NTG_MV(13) NTG_MV(14) NTG_MV(15)
+#undef NTG_MV
+    default: launch_matvec_t<kSmallM>(grid, s, A, n, lambda, B, X, xs, m, subtract, out, out32, st);
+  }
+}
+
 // part[blk][j] = sum over the block's rows of u[i, j] * v[i, j] (v FP64, or vf FP32).
 __global__ void __launch_bounds__(256)
     col_dots_kernel(const double* __restrict__ u, const double* __restrict__ v,
@@ -571,6 +594,8 @@ __global__ void pcg_init_kernel(const float* __restrict__ B, const float* __rest
     const int c = threadIdx.x;
     st->bnorm[c] = bmax[c];
     st->r0norm[c] = rmax[c];
+    st->rbest[c] = rmax[c];
+    st->stall[c] = 0;
     st->rho[0][c] = sum_parts(part, c);
     st->rmax[c] = rmax[c];
     st->active[c] = rmax[c] > kPcgFloor * bmax[c];
@@ -623,7 +648,16 @@ __global__ void pcg_check_kernel(const double* __restrict__ rpart, int64_t m, in
     double mx = 0.0;
     for (int b = 0; b < nblocks; ++b) mx = fmax(mx, rpart[b * kSmallM + c]);
     st->rmax[c] = mx;
-    if (st->active[c] && (mx <= kPcgTol * st->r0norm[c] || mx <= kPcgFloor * st->bnorm[c]))
+    // the double-float products put a floor under the residual: a column whose best
+    // residual has not halved in kPcgStall iterations has reached it and stops
+    if (mx < 0.5 * st->rbest[c]) {
+      st->rbest[c] = mx;
+      st->stall[c] = 0;
+    } else {
+      ++st->stall[c];
+    }
+    if (st->active[c] && (mx <= kPcgTol * st->r0norm[c] || mx <= kPcgFloor * st->bnorm[c] ||
+                          st->stall[c] >= kPcgStall))
       st->active[c] = 0;
     if (st->active[c]) atomicOr(&any, 1);
   }
@@ -907,8 +941,7 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
     auto matvec = [&](const double* v, int subtract, const float* bb, double* out, float* o32,
                       const PcgState* stp) {
       split_df_kernel<<<grid_for(n * m), 256, 0, s>>>(v, n * m, xs, stp);
-      matvec_df_rows_kernel<kSmallM><<<rows_grid, 256, 0, s>>>(A, n, lambda, bb, v, xs, m,
-                                                                subtract, out, o32, stp);
+      launch_matvec(m, rows_grid, s, A, n, lambda, bb, v, xs, subtract, out, o32, stp);
       note_launch(2);
     };
     matvec(x64, 1, B, r64, r32, nullptr);

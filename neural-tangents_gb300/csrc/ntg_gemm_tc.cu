@@ -253,15 +253,49 @@ __global__ void __launch_bounds__(GTHREADS, 1)
   }
   __syncthreads();
   if (acc_ok) {
-    const int nthr = GTHREADS;
-    for (int idx = threadIdx.x; idx < GM * GN; idx += nthr) {
-      const int r = idx / GN, cc = idx % GN;
-      const int64_t row = m0 + r, col = n0 + cc;
-      if (row < p.m && col < p.n && (!p.lower || col <= row)) {
-        float* cp = p.c + row * p.ldc + col;
-        float val = p.alpha * stile[r * SP + cc];
-        if (p.beta != 0.f) val = fmaf(p.beta, *cp, val);
-        *cp = val;
+    // groups of 4 columns; four groups per thread in flight (the read of C for beta != 0
+    // is latency-bound otherwise); whole groups move as float4 when C allows it
+    const bool vec = ((p.ldc & 3) == 0) && ((reinterpret_cast<uintptr_t>(p.c) & 15) == 0);
+    constexpr int G = GM * GN / 4, GPR = GN / 4;
+    for (int g0 = threadIdx.x; g0 < G; g0 += 4 * GTHREADS) {
+      float4 cv[4];
+      bool whole[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int g = g0 + u * GTHREADS;
+        const int r = g / GPR, c4 = (g % GPR) * 4;
+        const int64_t row = m0 + r, col = n0 + c4;
+        whole[u] = g < G && vec && row < p.m && col + 3 < p.n && (!p.lower || col + 3 <= row);
+        cv[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (whole[u] && p.beta != 0.f)
+          cv[u] = *reinterpret_cast<const float4*>(p.c + row * p.ldc + col);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int g = g0 + u * GTHREADS;
+        if (g >= G) continue;
+        const int r = g / GPR, c4 = (g % GPR) * 4;
+        const int64_t row = m0 + r, col = n0 + c4;
+        const float* sv = stile + r * SP + c4;
+        if (whole[u]) {
+          float4 o;
+          o.x = fmaf(p.beta, cv[u].x, p.alpha * sv[0]);
+          o.y = fmaf(p.beta, cv[u].y, p.alpha * sv[1]);
+          o.z = fmaf(p.beta, cv[u].z, p.alpha * sv[2]);
+          o.w = fmaf(p.beta, cv[u].w, p.alpha * sv[3]);
+          *reinterpret_cast<float4*>(p.c + row * p.ldc + col) = o;
+        } else if (row < p.m) {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int64_t cl = col + e;
+            if (cl < p.n && (!p.lower || cl <= row)) {
+              float* cp = p.c + row * p.ldc + cl;
+              float val = p.alpha * sv[e];
+              if (p.beta != 0.f) val = fmaf(p.beta, *cp, val);
+              *cp = val;
+            }
+          }
+        }
       }
     }
   }
