@@ -276,27 +276,46 @@ __global__ void transpose_kernel(const float* __restrict__ in, int64_t ld_in, fl
 // right-hand sides: Y[i, c] = sum_{j in range(i)} M[i, j] X[j, c] with range
 // j <= i (M = L^-1, lower) or j >= i (M = L^-T, upper). One warp per row.
 // ---------------------------------------------------------------------------
+constexpr int kRowWarps = 16;  // rows (one warp each) per CTA of the row kernels
+constexpr int kChunk = 256;    // right-hand-side rows staged in shared memory at a time
+
 template <int MR>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kRowWarps * 32)
     tri_gemv_kernel(const float* __restrict__ M, int64_t ld, int64_t n, int upper,
                     const float* __restrict__ X, int64_t m, float* __restrict__ Y,
                     const int* skip) {
   if (skip && *skip) return;
-  const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  // X rows staged column-major, so that the lanes of a warp read consecutive words
+  __shared__ float sx[MR][kChunk];
+  const int64_t r0 = (int64_t)blockIdx.x * kRowWarps;
+  const int64_t row = r0 + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
-  if (row >= n) return;
-  const float* mr = M + row * ld;
+  const bool live = row < n;
+  const float* mr = M + (live ? row : 0) * ld;
   float acc[MR];
 #pragma unroll
   for (int c = 0; c < MR; ++c) acc[c] = 0.f;
-  const int64_t j0 = upper ? row : 0, j1 = upper ? n : row + 1;
-  for (int64_t j = j0 + lane; j < j1; j += 32) {
-    const float a = mr[j];
-    const float* xr = X + j * m;
+  // the CTA's column range: lower rows need j <= row, upper rows j >= row
+  const int64_t jb = upper ? r0 : 0;
+  const int64_t je = upper ? n : mini(n, r0 + kRowWarps);
+  for (int64_t j0 = jb; j0 < je; j0 += kChunk) {
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < kChunk * MR; idx += blockDim.x) {
+      const int jj = idx / MR, c = idx % MR;
+      const int64_t j = j0 + jj;
+      sx[c][jj] = (c < m && j < je) ? X[j * m + c] : 0.f;
+    }
+    __syncthreads();
+    if (!live) continue;
+    for (int jj = lane; jj < kChunk; jj += 32) {
+      const int64_t j = j0 + jj;
+      if (j >= je || (upper ? j < row : j > row)) continue;
+      const float a = mr[j];
 #pragma unroll
-    for (int c = 0; c < MR; ++c)
-      if (c < m) acc[c] = fmaf(a, xr[c], acc[c]);
+      for (int c = 0; c < MR; ++c) acc[c] = fmaf(a, sx[c][jj], acc[c]);
+    }
   }
+  if (!live) return;
 #pragma unroll
   for (int c = 0; c < MR; ++c) {
     if (c >= m) break;
@@ -471,33 +490,44 @@ __global__ void split_df_kernel(const double* __restrict__ X, int64_t total,
 // [n, m] given also as its double-float split xs; one warp per row, double-float sums of
 // the m <= MR products kept per lane.
 template <int MR>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kRowWarps * 32)
     matvec_df_rows_kernel(const float* __restrict__ A, int64_t n, const double* lambda,
                           const float* __restrict__ B, const double* __restrict__ X,
                           const float2* __restrict__ xs, int64_t m, int subtract,
                           double* __restrict__ out, float* __restrict__ out32,
                           const PcgState* st) {
   if (st && st->all_done) return;
-  const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+  // the split of X staged column-major per chunk (lanes read consecutive words)
+  __shared__ float2 sx[MR][kChunk];
+  const int64_t row = (int64_t)blockIdx.x * kRowWarps + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
-  if (row >= n) return;
-  const float* ar = A + row * n;
+  const bool live = row < n;
+  const float* ar = A + (live ? row : 0) * n;
   float sh[MR], sl[MR];
 #pragma unroll
   for (int c = 0; c < MR; ++c) sh[c] = sl[c] = 0.f;
-  for (int64_t j = lane; j < n; j += 32) {
-    const float a = ar[j];
-    const float2* xr = xs + j * m;
+  for (int64_t j0 = 0; j0 < n; j0 += kChunk) {
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < kChunk * MR; idx += blockDim.x) {
+      const int jj = idx / MR, c = idx % MR;
+      const int64_t j = j0 + jj;
+      sx[c][jj] = (j < n) ? xs[j * m + c] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    if (!live) continue;
+    const int lim = (int)mini(kChunk, n - j0);
+    for (int jj = lane; jj < lim; jj += 32) {
+      const float a = ar[j0 + jj];
 #pragma unroll
-    for (int c = 0; c < MR; ++c)
-      if (c < m) {
-        const float2 xv = xr[c];
+      for (int c = 0; c < MR; ++c) {
+        const float2 xv = sx[c][jj];
         df_fma(a, xv.x, xv.y, sh[c], sl[c]);
       }
+    }
   }
+  if (!live) return;
 #pragma unroll
   for (int c = 0; c < MR; ++c) {
-    if (c >= m) break;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const float oh = __shfl_xor_sync(0xffffffffu, sh[c], o);
@@ -519,8 +549,8 @@ template <int MR>
 void launch_matvec_t(unsigned grid, cudaStream_t s, const float* A, int64_t n,
                      const double* lambda, const float* B, const double* X, const float2* xs,
                      int64_t m, int subtract, double* out, float* out32, const PcgState* st) {
-  matvec_df_rows_kernel<MR><<<grid, 256, 0, s>>>(A, n, lambda, B, X, xs, m, subtract, out,
-                                                 out32, st);
+  matvec_df_rows_kernel<MR><<<grid, kRowWarps * 32, 0, s>>>(A, n, lambda, B, X, xs, m,
+                                                            subtract, out, out32, st);
 }
 
 void launch_matvec(int64_t m, unsigned grid, cudaStream_t s, const float* A, int64_t n,
@@ -771,9 +801,21 @@ size_t solve_ws_bytes(int64_t n, int64_t m, int64_t ldl) {
 // X = (L L^T)^-1 X for up to kSmallM right-hand sides: t = L^-1 X, X = L^-T t.
 int inv_apply_small(cudaStream_t s, const FactorWs& f, int64_t ldl, int64_t n, float* X, int64_t m,
                     float* t, const int* skip) {
-  const unsigned g = (unsigned)ceil_div(n, 8);
-  tri_gemv_kernel<kSmallM><<<g, 256, 0, s>>>(f.linvf, ldl, n, 0, X, m, t, skip);
-  tri_gemv_kernel<kSmallM><<<g, 256, 0, s>>>(f.uinv, ldl, n, 1, t, m, X, skip);
+  const unsigned g = (unsigned)ceil_div(n, kRowWarps);
+  const unsigned nt = kRowWarps * 32;
+  if (m == 1) {
+    tri_gemv_kernel<1><<<g, nt, 0, s>>>(f.linvf, ldl, n, 0, X, m, t, skip);
+    tri_gemv_kernel<1><<<g, nt, 0, s>>>(f.uinv, ldl, n, 1, t, m, X, skip);
+  } else if (m <= 4) {
+    tri_gemv_kernel<4><<<g, nt, 0, s>>>(f.linvf, ldl, n, 0, X, m, t, skip);
+    tri_gemv_kernel<4><<<g, nt, 0, s>>>(f.uinv, ldl, n, 1, t, m, X, skip);
+  } else if (m <= 10) {
+    tri_gemv_kernel<10><<<g, nt, 0, s>>>(f.linvf, ldl, n, 0, X, m, t, skip);
+    tri_gemv_kernel<10><<<g, nt, 0, s>>>(f.uinv, ldl, n, 1, t, m, X, skip);
+  } else {
+    tri_gemv_kernel<kSmallM><<<g, nt, 0, s>>>(f.linvf, ldl, n, 0, X, m, t, skip);
+    tri_gemv_kernel<kSmallM><<<g, nt, 0, s>>>(f.uinv, ldl, n, 1, t, m, X, skip);
+  }
   note_launch(2);
   return check_launch("ntg_chol_solve_tc apply");
 }
@@ -936,7 +978,7 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
     PcgState* st = reinterpret_cast<PcgState*>(part_r + kDotBlocks * kSmallM);
     float2* xs = reinterpret_cast<float2*>(
         (reinterpret_cast<uintptr_t>(st + 1) + 255) & ~(uintptr_t)255);
-    const unsigned rows_grid = (unsigned)ceil_div(n, 8);
+    const unsigned rows_grid = (unsigned)ceil_div(n, kRowWarps);
     // (K + lambda I) v for v = x64 or p64 (subtract: b - ...), through the split of v
     auto matvec = [&](const double* v, int subtract, const float* bb, double* out, float* o32,
                       const PcgState* stp) {
