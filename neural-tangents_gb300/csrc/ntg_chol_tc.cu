@@ -86,39 +86,56 @@ __global__ void init_factor_ld_kernel(const float* __restrict__ A, int64_t n, in
 // ---------------------------------------------------------------------------
 
 // Warp-level Cholesky of the 32 x 32 block at (o, o) of `a` (lower part used) and the
-// inverse of the factor into dinv (lower, row-major 32 x 33). Lane r owns row r; the
-// pivot column and the solved rows are read from shared memory as broadcasts.
+// inverse of the factor into dinv (lower, row-major 32 x 33). Lane r holds row r in
+// registers; each pivot column is broadcast through shared memory. The pivot uses the
+// hardware reciprocal square root (2 ulp): L_jj = d rsqrt(d), L_rj = A_rj rsqrt(d), and
+// the reciprocal pivots are kept for the inverse, which then needs no division (the
+// factor is refined against the exact kernel by the solves; measured on GB300, the IEEE
+// square root and divisions were 40 % of this routine).
 __device__ void warp_potrf_inv32(float (*a)[PBS], int o, float (*dinv)[33], int* info,
                                  int64_t col0) {
+  __shared__ float colbuf[33];
+  __shared__ float rpiv[32];
   const int lane = threadIdx.x & 31;
-  float* row = &a[o + lane][o];
+  float v[32];
+#pragma unroll
+  for (int c = 0; c < 32; ++c) v[c] = a[o + lane][o + c];
+#pragma unroll
   for (int j = 0; j < 32; ++j) {
-    float d = a[o + j][o + j];
+    if (lane == j) colbuf[32] = v[j];
+    __syncwarp();
+    float d = colbuf[32];
     if (!(d > 0.f)) {  // the same value in every lane
       if (lane == 0) atomicCAS(info, 0, (int)(col0 + o + j + 1));
       d = 1.f;
     }
-    const float piv = sqrtf(d);
+    const float rs = rsqrtf(d);
+    const float l = (lane == j) ? d * rs : v[j] * rs;
+    v[j] = l;
+    colbuf[lane] = l;
+    if (lane == 0) rpiv[j] = rs;
     __syncwarp();
-    float l = 0.f;
-    if (lane == j) row[j] = piv;
-    if (lane > j) {
-      l = row[j] / piv;
-      row[j] = l;
+#pragma unroll
+    for (int c = j + 1; c < 32; ++c) {
+      const float lc = colbuf[c];
+      if (lane >= c) v[c] = fmaf(-l, lc, v[c]);
     }
     __syncwarp();
-    if (lane > j)
-      for (int c = j + 1; c <= lane; ++c) row[c] = fmaf(-l, a[o + c][o + j], row[c]);
-    __syncwarp();
   }
-  for (int c = lane + 1; c < 32; ++c) row[c] = 0.f;
+#pragma unroll
+  for (int c = 0; c < 32; ++c) a[o + lane][o + c] = (c <= lane) ? v[c] : 0.f;
   __syncwarp();
   // X = L^-1, lane c computes column c: x_i = (delta_ic - sum_{p<i} L[i][p] x_p) / L[i][i]
+  float x[32];
+#pragma unroll
   for (int i = 0; i < 32; ++i) {
-    float sacc = (i == lane) ? 1.f : 0.f;
-    for (int p = lane; p < i; ++p) sacc = fmaf(-a[o + i][o + p], dinv[p][lane], sacc);
-    dinv[i][lane] = (i < lane) ? 0.f : sacc / a[o + i][o + i];
+    float s = (i == lane) ? 1.f : 0.f;
+#pragma unroll
+    for (int p = 0; p < i; ++p) s = fmaf(-a[o + i][o + p], x[p], s);
+    x[i] = s * rpiv[i];
   }
+#pragma unroll
+  for (int i = 0; i < 32; ++i) dinv[i][lane] = x[i];
   __syncwarp();
 }
 
@@ -221,10 +238,13 @@ __global__ void __launch_bounds__(512)
     panel_trsm_kernel(float* __restrict__ L, int64_t ldl, int64_t n, int64_t k) {
   extern __shared__ float sm[];
   float(*l11)[PBS] = reinterpret_cast<float(*)[PBS]>(sm);
+  float* rdiag = sm + PB * PBS;  // 1 / L11[c][c]: a multiplication on the dependent chain
   for (int idx = threadIdx.x; idx < PB * PB; idx += blockDim.x) {
     const int i = idx / PB, j = idx % PB;
     l11[i][j] = (j <= i) ? L[(k + i) * ldl + k + j] : 0.f;
   }
+  __syncthreads();
+  if (threadIdx.x < PB) rdiag[threadIdx.x] = 1.f / l11[threadIdx.x][threadIdx.x];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const unsigned full = 0xffffffffu;
@@ -238,7 +258,7 @@ __global__ void __launch_bounds__(512)
 #pragma unroll 4
       for (int cc = 0; cc < 32; ++cc) {
         const int c = 32 * s + cc;
-        const float xc = __shfl_sync(full, x[s], cc) / l11[c][c];
+        const float xc = __shfl_sync(full, x[s], cc) * rdiag[c];
         if (lane == cc) x[s] = xc;
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -252,7 +272,7 @@ __global__ void __launch_bounds__(512)
   }
 }
 
-constexpr size_t kPanelSmem = (size_t)PB * PBS * sizeof(float);
+constexpr size_t kPanelSmem = (size_t)(PB * PBS + PB) * sizeof(float);
 
 // out[j, i] = in[i, j] for an [rows, cols] block (row pitches ld_in, ld_out).
 __global__ void transpose_kernel(const float* __restrict__ in, int64_t ld_in, float* __restrict__ out,
@@ -276,46 +296,27 @@ __global__ void transpose_kernel(const float* __restrict__ in, int64_t ld_in, fl
 // right-hand sides: Y[i, c] = sum_{j in range(i)} M[i, j] X[j, c] with range
 // j <= i (M = L^-1, lower) or j >= i (M = L^-T, upper). One warp per row.
 // ---------------------------------------------------------------------------
-constexpr int kRowWarps = 16;  // rows (one warp each) per CTA of the row kernels
-constexpr int kChunk = 256;    // right-hand-side rows staged in shared memory at a time
-
 template <int MR>
-__global__ void __launch_bounds__(kRowWarps * 32)
+__global__ void __launch_bounds__(256)
     tri_gemv_kernel(const float* __restrict__ M, int64_t ld, int64_t n, int upper,
                     const float* __restrict__ X, int64_t m, float* __restrict__ Y,
                     const int* skip) {
   if (skip && *skip) return;
-  // X rows staged column-major, so that the lanes of a warp read consecutive words
-  __shared__ float sx[MR][kChunk];
-  const int64_t r0 = (int64_t)blockIdx.x * kRowWarps;
-  const int64_t row = r0 + threadIdx.x / 32;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
-  const bool live = row < n;
-  const float* mr = M + (live ? row : 0) * ld;
+  if (row >= n) return;
+  const float* mr = M + row * ld;
   float acc[MR];
 #pragma unroll
   for (int c = 0; c < MR; ++c) acc[c] = 0.f;
-  // the CTA's column range: lower rows need j <= row, upper rows j >= row
-  const int64_t jb = upper ? r0 : 0;
-  const int64_t je = upper ? n : mini(n, r0 + kRowWarps);
-  for (int64_t j0 = jb; j0 < je; j0 += kChunk) {
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < kChunk * MR; idx += blockDim.x) {
-      const int jj = idx / MR, c = idx % MR;
-      const int64_t j = j0 + jj;
-      sx[c][jj] = (c < m && j < je) ? X[j * m + c] : 0.f;
-    }
-    __syncthreads();
-    if (!live) continue;
-    for (int jj = lane; jj < kChunk; jj += 32) {
-      const int64_t j = j0 + jj;
-      if (j >= je || (upper ? j < row : j > row)) continue;
-      const float a = mr[j];
+  const int64_t j0 = upper ? row : 0, j1 = upper ? n : row + 1;
+  for (int64_t j = j0 + lane; j < j1; j += 32) {
+    const float a = mr[j];
+    const float* xr = X + j * m;
 #pragma unroll
-      for (int c = 0; c < MR; ++c) acc[c] = fmaf(a, sx[c][jj], acc[c]);
-    }
+    for (int c = 0; c < MR; ++c)
+      if (c < m) acc[c] = fmaf(a, xr[c], acc[c]);
   }
-  if (!live) return;
 #pragma unroll
   for (int c = 0; c < MR; ++c) {
     if (c >= m) break;
@@ -490,42 +491,29 @@ __global__ void split_df_kernel(const double* __restrict__ X, int64_t total,
 // [n, m] given also as its double-float split xs; one warp per row, double-float sums of
 // the m <= MR products kept per lane.
 template <int MR>
-__global__ void __launch_bounds__(kRowWarps * 32)
+__global__ void __launch_bounds__(256)
     matvec_df_rows_kernel(const float* __restrict__ A, int64_t n, const double* lambda,
                           const float* __restrict__ B, const double* __restrict__ X,
                           const float2* __restrict__ xs, int64_t m, int subtract,
                           double* __restrict__ out, float* __restrict__ out32,
                           const PcgState* st) {
   if (st && st->all_done) return;
-  // the split of X staged column-major per chunk (lanes read consecutive words)
-  __shared__ float2 sx[MR][kChunk];
-  const int64_t row = (int64_t)blockIdx.x * kRowWarps + threadIdx.x / 32;
+  const int64_t row = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
   const int lane = threadIdx.x & 31;
-  const bool live = row < n;
-  const float* ar = A + (live ? row : 0) * n;
+  if (row >= n) return;
+  const float* ar = A + row * n;
   float sh[MR], sl[MR];
 #pragma unroll
   for (int c = 0; c < MR; ++c) sh[c] = sl[c] = 0.f;
-  for (int64_t j0 = 0; j0 < n; j0 += kChunk) {
-    __syncthreads();
-    for (int idx = threadIdx.x; idx < kChunk * MR; idx += blockDim.x) {
-      const int jj = idx / MR, c = idx % MR;
-      const int64_t j = j0 + jj;
-      sx[c][jj] = (j < n) ? xs[j * m + c] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    if (!live) continue;
-    const int lim = (int)mini(kChunk, n - j0);
-    for (int jj = lane; jj < lim; jj += 32) {
-      const float a = ar[j0 + jj];
+  for (int64_t j = lane; j < n; j += 32) {
+    const float a = ar[j];
+    const float2* xr = xs + j * m;
 #pragma unroll
-      for (int c = 0; c < MR; ++c) {
-        const float2 xv = sx[c][jj];
-        df_fma(a, xv.x, xv.y, sh[c], sl[c]);
-      }
+    for (int c = 0; c < MR; ++c) {
+      const float2 xv = xr[c];
+      df_fma(a, xv.x, xv.y, sh[c], sl[c]);
     }
   }
-  if (!live) return;
 #pragma unroll
   for (int c = 0; c < MR; ++c) {
 #pragma unroll
@@ -549,8 +537,8 @@ template <int MR>
 void launch_matvec_t(unsigned grid, cudaStream_t s, const float* A, int64_t n,
                      const double* lambda, const float* B, const double* X, const float2* xs,
                      int64_t m, int subtract, double* out, float* out32, const PcgState* st) {
-  matvec_df_rows_kernel<MR><<<grid, kRowWarps * 32, 0, s>>>(A, n, lambda, B, X, xs, m,
-                                                            subtract, out, out32, st);
+  matvec_df_rows_kernel<MR><<<grid, 256, 0, s>>>(A, n, lambda, B, X, xs, m, subtract, out,
+                                                 out32, st);
 }
 
 void launch_matvec(int64_t m, unsigned grid, cudaStream_t s, const float* A, int64_t n,
@@ -801,8 +789,8 @@ size_t solve_ws_bytes(int64_t n, int64_t m, int64_t ldl) {
 // X = (L L^T)^-1 X for up to kSmallM right-hand sides: t = L^-1 X, X = L^-T t.
 int inv_apply_small(cudaStream_t s, const FactorWs& f, int64_t ldl, int64_t n, float* X, int64_t m,
                     float* t, const int* skip) {
-  const unsigned g = (unsigned)ceil_div(n, kRowWarps);
-  const unsigned nt = kRowWarps * 32;
+  const unsigned g = (unsigned)ceil_div(n, 8);
+  const unsigned nt = 256;
   if (m == 1) {
     tri_gemv_kernel<1><<<g, nt, 0, s>>>(f.linvf, ldl, n, 0, X, m, t, skip);
     tri_gemv_kernel<1><<<g, nt, 0, s>>>(f.uinv, ldl, n, 1, t, m, X, skip);
@@ -978,7 +966,7 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
     PcgState* st = reinterpret_cast<PcgState*>(part_r + kDotBlocks * kSmallM);
     float2* xs = reinterpret_cast<float2*>(
         (reinterpret_cast<uintptr_t>(st + 1) + 255) & ~(uintptr_t)255);
-    const unsigned rows_grid = (unsigned)ceil_div(n, kRowWarps);
+    const unsigned rows_grid = (unsigned)ceil_div(n, 8);
     // (K + lambda I) v for v = x64 or p64 (subtract: b - ...), through the split of v
     auto matvec = [&](const double* v, int subtract, const float* bb, double* out, float* o32,
                       const PcgState* stp) {
