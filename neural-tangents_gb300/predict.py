@@ -100,10 +100,10 @@ class CholeskySolver:
     pitch the TMA loads of the trailing updates need); the factor workspace keeps the
     inverses of the 128-wide diagonal blocks and L^T for the solves."""
 
-    # refinement per solve when the caller gives none: at most 16 preconditioned CG
-    # iterations for up to 16 right-hand sides (they stop once converged), 2 plain
-    # refinement steps for more
-    REFINE_FEW, REFINE_MANY, FEW = 16, 2, 16
+    # refinement per solve when the caller gives none: at most 8 preconditioned CG
+    # iterations for up to 16 right-hand sides (they stop once converged, typically after
+    # two; the rest of the launches return at once), 2 plain refinement steps for more
+    REFINE_FEW, REFINE_MANY, FEW = 8, 2, 16
 
     def __init__(self, k: torch.Tensor, diag_reg: float, absolute: bool,
                  refine_iters: Optional[int] = None):
