@@ -724,14 +724,16 @@ def config3_timing(torch, nt, dev, n=5000, bs=128):
     [5000, 32, 32, 3] iid N(0, 1) (seed 0) in the mixed form (split-precision first layer,
     compensated arccos) through nt.batch(batch_size=128) (ragged: 5000 = 39 x 128 + 8, one
     fused launch over the symmetric grid), then gradient_descent_mse(ntk, y, diag_reg=1e-4)
-    at t = None (FP32 Cholesky of the 5000 x 5000 kernel, FP64 refinement) with y one-hot over
-    10 classes (seed 2), predicting the first 100 training points. Wall-clock seconds, the job
-    once; the kernel entries and the predictions are checked in the CPU leg against the
-    float64 oracle."""
+    at t = None (FP32 Cholesky of the 5000 x 5000 kernel on the tensor cores, refinement by
+    conjugate gradients) with y one-hot over 10 classes (seed 2), predicting 100 held-out
+    inputs (iid N(0, 1), seed 1). Wall-clock seconds, the job once; the kernel entries, the
+    solve A^-1 y and the predictions are checked in the CPU leg against float64."""
     from nt_gb300 import stax
     xh = np.random.default_rng(0).standard_normal((n,) + IMG).astype(np.float32)
+    xth = np.random.default_rng(1).standard_normal((100,) + IMG).astype(np.float32)
     yh = np.eye(10, dtype=np.float32)[np.random.default_rng(2).integers(0, 10, n)]
     x, y = torch.from_numpy(xh).to(dev), torch.from_numpy(yh).to(dev)
+    xt = torch.from_numpy(xth).to(dev)
     kf = stax.serial(*myrtle10(stax))[2]
     batched = nt.batch(kf, batch_size=bs)
     batched(x[:256], None, ('nngp', 'ntk'), precision='mixed')  # warm-up (library, planner)
@@ -740,24 +742,26 @@ def config3_timing(torch, nt, dev, n=5000, bs=128):
     k = batched(x, None, ('nngp', 'ntk'), precision='mixed')
     torch.cuda.synchronize()
     kernel_s = time.perf_counter() - t0
-    kts = k.ntk[:100].contiguous()
+    kts = batched(xt, x, 'ntk', precision='mixed')
     t0 = time.perf_counter()
     pred = nt.predict.gradient_descent_mse(k.ntk, y, diag_reg=1e-4)
     fx = pred(None, 0., 0., kts)[1]
     torch.cuda.synchronize()
     solve_s = time.perf_counter() - t0
+    alpha = nt.predict.CholeskySolver(k.ntk, 1e-4, False).solve(y)
     pairs = parity_pairs(n, 24, seed=9)
     ii = [i for i, _ in pairs]
     jj = [j for _, j in pairs]
     out = {'config': f'Myrtle-10 [3,3,3] + GlobalAvgPool + Dense, K(x, x), x [{n}, 32, 32, 3] '
                      f'iid N(0,1) (seed 0), mixed form, nt.batch(batch_size={bs}) ragged; then '
                      'gradient_descent_mse(ntk, one-hot y (seed 2), diag_reg=1e-4) at t=None, '
-                     'predictions for the first 100 training points',
+                     'predictions for 100 held-out inputs (seed 1)',
            'kernel_s': round(kernel_s, 2), 'entries_per_s': round(n * n / kernel_s, 1),
            'solve_ms': round(solve_s * 1e3, 2)}
     check = {'name': 'myrtle10_5000', 'net': 'myrtle10', 'x': xh, 'pairs': pairs,
              'got': {'mixed': (k.nngp[ii, jj].cpu().numpy(), k.ntk[ii, jj].cpu().numpy())},
-             'solve': {'k': k.ntk.cpu().numpy(), 'y': yh, 'fx_test': fx.cpu().numpy()}}
+             'solve': {'k': k.ntk.cpu().numpy(), 'y': yh, 'kts': kts.cpu().numpy(),
+                       'fx_test': fx.cpu().numpy(), 'alpha': alpha.cpu().numpy()}}
     return out, check
 
 
@@ -801,10 +805,16 @@ def cpu_checks(checks, procs=None):
             for form, (gq, gt) in c['got'].items():
                 res[f'max_rel_err_{form}'] = max(_rel(gq, want[:, 0]), _rel(gt, want[:, 1]))
             if 'solve' in c:
+                # the solve and the predictions against float64 on the same GPU kernel matrix
+                import scipy.linalg as sla
                 sv = c['solve']
-                ref = o.gradient_descent_mse(sv['k'], sv['y'], diag_reg=1e-4)(
-                    None, 0., 0., np.asarray(sv['k'][:100], np.float64))[1]
-                res['predictions_max_rel_err_vs_float64_solve'] = float(
+                k64 = np.asarray(sv['k'], np.float64)
+                a = k64 + 1e-4 * np.trace(k64) / k64.shape[0] * np.eye(k64.shape[0])
+                alpha = sla.cho_solve(sla.cho_factor(a), np.asarray(sv['y'], np.float64))
+                res['solve_max_rel_err_vs_float64'] = float(
+                    np.max(np.abs(sv['alpha'] - alpha)) / np.max(np.abs(alpha)))
+                ref = np.asarray(sv['kts'], np.float64) @ alpha
+                res['predictions_max_rel_err_vs_float64'] = float(
                     np.max(np.abs(sv['fx_test'] - ref)) / np.max(np.abs(ref)))
             out[c['name']] = res
         elif c.get('kind') == 'fcn':

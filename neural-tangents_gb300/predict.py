@@ -280,8 +280,8 @@ class _NLL(torch.autograd.Function):
         solver = CholeskySolver(k, diag_reg, absolute, refine_iters)
         alpha = solver.solve(y)
         ld = solver.logdet()
-        quad = _gemm(y.reshape(1, -1).contiguous(), alpha.reshape(-1, 1).contiguous())
-        nll = 0.5 * quad.reshape(()).double() + 0.5 * m * ld[0] + 0.5 * n * m * math.log(2 * math.pi)
+        quad = (y.double() * alpha.double()).sum()
+        nll = 0.5 * quad + 0.5 * m * ld[0] + 0.5 * n * m * math.log(2 * math.pi)
         ctx.solver, ctx.alpha, ctx.meta = solver, alpha, (diag_reg, absolute, n, m)
         return nll.float()
 
@@ -291,10 +291,10 @@ class _NLL(torch.autograd.Function):
         solver, alpha = ctx.solver, ctx.alpha
         eye = torch.zeros((n, n), device=alpha.device)
         eye.view(-1)[::n + 1] = 1.
-        # A^{-1} for the log-determinant term, refined like the solve itself: on the
-        # ill-conditioned kernels of wide, deep FCNs the plain FP32 inverse moves this
-        # gradient term by tens of percent
-        kinv = solver.solve(eye, residual=False)
+        # A^{-1} for the log-determinant term, with one refinement step (double-float
+        # residual): on the ill-conditioned kernels of wide, deep FCNs the plain FP32
+        # inverse moves this gradient term by tens of percent, one step squares that error
+        kinv = solver.solve(eye, refine_iters=1, residual=False)
         out = torch.empty((n, n), device=alpha.device)
         tr = torch.zeros(1, device=alpha.device, dtype=torch.float64)
         L.call('ntg_nll_grad', L.stream(), L.ptr(kinv), L.ptr(alpha.contiguous()), n, m,
