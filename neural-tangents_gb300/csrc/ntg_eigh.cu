@@ -105,7 +105,11 @@ __global__ void __launch_bounds__(256)
         const float apq = S[p][q];
         const float thr = fmaxf(tiny, 1e-7f * sqrtf(fabsf(S[p][p] * S[q][q])));
         sym_schur2(S[p][p], S[q][q], apq, thr, c, s);
-        if (s != 0.f) rotated = 1;
+        // another sweep is needed while some coupling is still above 1e-5 of its pivots
+        // (the smaller ones are rotated too, but leave the rest to the outer sweeps and
+        // the refinement)
+        if (fabsf(apq) > 1e-5f * sqrtf(fabsf(S[p][p] * S[q][q])) && fabsf(apq) > tiny)
+          rotated = 1;
         cs[tid][0] = c;
         cs[tid][1] = s;
         pq[tid][0] = p;

@@ -51,11 +51,12 @@ def _gemm_tn(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     return out
 
 
-def _eigh(k: torch.Tensor, shift: float, max_sweeps: int = 20, tol: float = 2e-7,
+def _eigh(k: torch.Tensor, shift: float, max_sweeps: int = 20, tol: float = 1e-5,
           refine_steps: int = 2):
     """Eigenpairs of k + shift I on this library's block-Jacobi kernels (FP32) with
     `refine_steps` double-float refinement steps: (evals [n], evecs [n, n], column j
-    for evals[j]), evals not sorted."""
+    for evals[j]), evals not sorted. The Jacobi sweeps stop at an off-diagonal norm of
+    `tol` (relative); the refinement steps take the pairs from there to FP32 accuracy."""
     n = k.shape[0]
     lib = L.load()
     nbytes = int(lib.ntg_eigh_workspace_bytes(n))
