@@ -950,12 +950,74 @@ def profile_gram(n: int):
     print(json.dumps({'profile_gram': n, 'mean': float(g.mean())}))
 
 
+def profile_chol(n: int):
+    """Factor + solve of gradient_descent_mse's Cholesky path on an SPD kernel of order n (the
+    Gram of iid N(0, 1) features [n, 6144] / 6144, diag_reg 1e-4, 10 one-hot targets), after
+    a warm-up factorisation; NVTX ranges 'factor' and 'solve' select the launches."""
+    import torch
+    from nt_gb300 import _ops as O, predict
+    dev = torch.device('cuda')
+    g = torch.Generator(device='cpu').manual_seed(2)
+    x = torch.randn((n, 6144), device=dev)
+    k = O.gram(x, x, 0)
+    y = torch.nn.functional.one_hot(torch.randint(0, 10, (n,), generator=g), 10).float().to(dev)
+    predict.CholeskySolver(k, 1e-4, False)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push('factor')
+    s = predict.CholeskySolver(k, 1e-4, False)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.nvtx.range_push('solve')
+    s.solve(y)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    print(json.dumps({'profile_chol': n, 'residual': float(s.residual.item()), 'info': s.info}))
+
+
+def profile_nll():
+    """The NLL forward + backward of the bench's depth-3 FCN (X [4096, 3072]), twice (the
+    first a warm-up; autograd runs the backward on its own thread, so select by launch
+    count rather than NVTX)."""
+    import torch
+    from nt_gb300 import predict, stax
+    dev = torch.device('cuda')
+    gen = torch.Generator(device='cpu').manual_seed(3)
+    x = torch.randn((4096, 3072), generator=gen).to(dev)
+    y = torch.randn((4096, 10), generator=gen).to(dev)
+    w = torch.tensor(1.5, device=dev, requires_grad=True)
+    b = torch.tensor(0.1, device=dev, requires_grad=True)
+    kf = stax.serial(stax.Dense(512, w, b), stax.Relu(), stax.Dense(512, w, b), stax.Relu(),
+                     stax.Dense(512, w, b), stax.Relu(), stax.Dense(1, w, b))[2]
+    for _ in range(2):
+        w.grad = b.grad = None
+        predict.negative_log_likelihood(kf(x, None, 'nngp'), y, diag_reg=1e-4).backward()
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_nll': 4096, 'grad': [float(w.grad), float(b.grad)]}))
+
+
+def profile_gemm(n: int):
+    """Two n x n x n calls of the 3xTF32 tensor-core GEMM (ntg_gemm_tc), C = A B^T."""
+    import torch
+    from nt_gb300 import _lib as L
+    a = torch.randn((n, n), device='cuda')
+    b = torch.randn((n, n), device='cuda')
+    c = torch.empty((n, n), device='cuda')
+    for _ in range(2):
+        L.call('ntg_gemm_tc', L.stream(), a.data_ptr(), n, b.data_ptr(), n, c.data_ptr(), n, n,
+               n, n, 1., 0., 0)
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_gemm': n, 'c00': float(c[0, 0])}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--profile-tile', type=int, default=0)
     ap.add_argument('--profile-stencil', type=int, default=0)
     ap.add_argument('--profile-fwd-bwd', type=int, default=0)
     ap.add_argument('--profile-gram', type=int, default=0)
+    ap.add_argument('--profile-chol', type=int, default=0)
+    ap.add_argument('--profile-nll', action='store_true')
+    ap.add_argument('--profile-gemm', type=int, default=0)
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=3)
@@ -974,6 +1036,12 @@ def main():
         profile_fwd_bwd(args.profile_fwd_bwd)
     elif args.profile_gram:
         profile_gram(args.profile_gram)
+    elif args.profile_chol:
+        profile_chol(args.profile_chol)
+    elif args.profile_nll:
+        profile_nll()
+    elif args.profile_gemm:
+        profile_gemm(args.profile_gemm)
     elif args.impl == 'reference':
         run_reference(args)
     else:
