@@ -27,6 +27,7 @@ constexpr int NT = 512;
 struct ChainCtx {
   const float* img1;  // [K][S0*S0] channel planes
   const float* img2;
+  const float* img2s;  // img2 planes shifted one column left (segment-0 paired loads)
   int K;
   float* stage;        // [2 buffers][2 tensors][S0*S0]
   float inv_k;
@@ -260,6 +261,11 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
   const P2 MR = p2((c0 != S - 1 - r) ? 1.f : 0.f,
                    (c0 + 1 <= S - 2 && c0 + 1 != S - 1 - r) ? 1.f : 0.f);
   const int wp0 = (c0 + r) & (S - 1), wp1 = (c0 + 1 + r) & (S - 1);
+  // Sample-2 entries at the skewed columns (wp0, wp1 = wp0 + 1 mod 32) as one aligned
+  // 8-byte load: from the plane itself for even rows (wp0 even), from its copy shifted
+  // one column left (shifted[j] = plane[j + 1 mod 32]) at wp0 - 1 for odd rows.
+  const int wpo = (r & 1) ? wp0 - 1 : wp0;
+  const float* img2v = (r & 1) ? cx.img2s : cx.img2;
   const P2 zero = p2s(0.f);
 
   ActC acs[NC];
@@ -289,14 +295,12 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
     P2 nq = zero, nt = zero;
     if (s < hi) {
       const float* x1r = cx.img1 + s * S + c0;
-      const float* x2r = cx.img2 + (s + delta) * S;
+      const float* x2r = img2v + (s + delta) * S + wpo;
       P2 g = zero;
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
-        if (KC > 0 ? k < KC : k < cx.K) {  // KC > 0: channel count fixed at compile time
-          const float* b = x2r + k * (S * S);
-          g = fma2(p2ld(x1r + k * (S * S)), p2(b[wp0], b[wp1]), g);
-        }
+        if (KC > 0 ? k < KC : k < cx.K)  // KC > 0: channel count fixed at compile time
+          g = fma2(p2ld(x1r + k * (S * S)), p2ld(x2r + k * (S * S)), g);
       }
       nq = mul2(g, INVK);
     }
@@ -323,13 +327,16 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
         P2 t = fma2(TW[k], ct, fma2(TN[k], nn, TC[k]));
         const ActC& ac = acs[k];
         if (ac.kind != NTG_ACT_NONE) {
-          const float* vm = vmaps + 4 * k * S * S;
+          // six maps per layer: v1, v2, sqrt v1, sqrt v2, and v2, sqrt v2 shifted
+          const float* vm = vmaps + 6 * k * S * S;
           const int i1 = p * S + c0, i2 = (p + delta) * S;
           const P2 v1 = p2ld(vm + i1), sv1 = p2ld(vm + 2 * S * S + i1);
           const float* v2r = vm + S * S + i2;
           const float* s2r = vm + 3 * S * S + i2;
           if (RO == 1 || (ac.kind == NTG_ACT_ABRELU && ac.stab <= 0.f)) {
-            abrelu2<COMP>(ac, q, t, v1, p2(v2r[wp0], v2r[wp1]), sv1, p2(s2r[wp0], s2r[wp1]));
+            // odd rows read the shifted copies: v2 at map 4, sqrt v2 at map 5
+            const int shv = (r & 1) ? 3 * S * S : 0, shs = (r & 1) ? 2 * S * S : 0;
+            abrelu2<COMP>(ac, q, t, v1, p2ld(v2r + shv + wpo), sv1, p2ld(s2r + shs + wpo));
           } else {
             float qa, qb, ta, tb, va, vb, sa, sb;
             p2u(q, qa, qb);
@@ -441,7 +448,8 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
   ChainCtx cx;
   float* img1 = smem;                 // [4][S0*S0]
   float* img2 = img1 + 4 * S0 * S0;
-  float* p = img2 + 4 * S0 * S0;
+  float* img2s = img2 + 4 * S0 * S0;
+  float* p = img2s + 4 * S0 * S0;
   // per-layer variance maps of both samples, segment by segment
   float* vseg[3] = {nullptr, nullptr, nullptr};
   {
@@ -458,8 +466,14 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
           p[S * S + e] = b;
           p[2 * S * S + e] = sqrt_var(a);
           p[3 * S * S + e] = sqrt_var(b);
+          if (sgi == 0) {  // shifted copies of the sample-2 maps: [row][j] = [row][j + 1]
+            const int row = e / S, col = e % S;
+            const float bs = __ldg(g2 + row * S + ((col + 1) & (S - 1)));
+            p[4 * S * S + e] = bs;
+            p[5 * S * S + e] = sqrt_var(bs);
+          }
         }
-        p += 4 * S * S;
+        p += (sgi == 0 ? 6 : 4) * S * S;
       }
     }
   }
@@ -478,10 +492,13 @@ __device__ __forceinline__ void chain_pair(const ntg_chain_t& pg, const float* _
     for (int k = 0; k < K; ++k) {
       img1[k * S0 * S0 + e] = __ldg(im1 + e * K + k);
       img2[k * S0 * S0 + e] = __ldg(im2 + e * K + k);
+      const int es = (e & ~(S0 - 1)) | ((e + 1) & (S0 - 1));  // same row, next column
+      img2s[k * S0 * S0 + e] = __ldg(im2 + es * K + k);
     }
   }
   cx.img1 = img1;
   cx.img2 = img2;
+  cx.img2s = img2s;
   cx.K = K;
   cx.inv_k = 1.f / (float)K;
   cx.acc_q = cx.acc_t = 0.f;
@@ -590,10 +607,10 @@ __global__ void __launch_bounds__(NT, 1)
 }
 
 size_t chain_smem_bytes(const ntg_chain_t& pg) {
-  size_t f = 2 * 4 * 32 * 32;  // images (4 channel planes each)
+  size_t f = 3 * 4 * 32 * 32;  // images (4 channel planes each), image 2 shifted
   for (int sgi = 0; sgi < pg.nseg; ++sgi) {
     size_t S = 32 >> sgi;
-    f += 4 * S * S * pg.nconv[sgi];
+    f += (sgi == 0 ? 6 : 4) * S * S * pg.nconv[sgi];
     if (sgi > 0) f += 4 * S * S * S;
   }
   f += 4 * 32 * 32;  // staging
@@ -684,6 +701,7 @@ int launch_chain(const char* who, void* stream, const ntg_chain_t* prog, const f
   NTG_REQUIRE(total < (1ll << 31), w + ": too many pairs for one launch");
   const unsigned grid = (unsigned)total;  // one CTA per pair
   size_t sm = chain_smem_bytes(pg);
+  NTG_REQUIRE(sm <= 232448, w + ": network needs more shared memory than a CTA has");
   cudaStream_t s = as_stream(stream);
   const int n0 = pg.nconv[0];
   const int c1 = pg.nseg > 1 ? pg.nconv[1] : -1, c2 = pg.nseg > 2 ? pg.nconv[2] : -1;
