@@ -788,6 +788,11 @@ def serial(*layers: Layer):
     diag = fold_diagonal(layers)
 
     def kernel_fn(x1, x2=None, get=None, *, diagonal_spatial=None, dtype=np.float64):
+        # requirements.py:884-900: a diagonal-spatial output can only be asked of a network
+        # that does not need the full spatial covariance.
+        if diagonal_spatial is True and diag.input == Bool.NO:
+            raise ValueError('Asked to compute `kernel_fn` output with `diagonal_spatial == '
+                             f'True`, while `kernel_fn` requires `diagonal_spatial == {diag}`.')
         ds = bool(diag) if diagonal_spatial is None else diagonal_spatial
         compute_ntk = get is None or 'ntk' in (get if isinstance(get, tuple) else (get,))
         k = inputs_to_kernel(x1, x2, diagonal_spatial=ds, compute_ntk=compute_ntk, dtype=dtype)
@@ -803,6 +808,11 @@ def serial(*layers: Layer):
         return tuple(getattr(k, g) for g in get)
 
     def apply_to_kernel(k: Kernel) -> Kernel:
+        # requirements.py:100-112: an input kernel that holds only the spatial diagonal lacks
+        # what a network needing the full spatial covariance reads.
+        if k.diagonal_spatial and diag.input == Bool.NO:
+            raise ValueError(f'the network requires `diagonal_spatial == {diag}`, but the input '
+                             'kernel has `diagonal_spatial == True`.')
         for l in layers:
             k = l.kernel_fn(k)
         return k

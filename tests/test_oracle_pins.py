@@ -94,6 +94,39 @@ def test_serial_composition():
     np.testing.assert_allclose(kbb.ntk, kb2.ntk, rtol=1e-12)
 
 
+@pytest.mark.parametrize('avg_pool', [True, False])
+@pytest.mark.parametrize('same_inputs', [True, False])
+def test_serial_composition_conv_readouts(avg_pool, same_inputs):
+    """tests/stax/stax_test.py:654-685: a conv block followed by a readout. Composed ==
+    readout o block with the block's kernel full-spatial or by default; a diagonal-spatial
+    block kernel is enough for Flatten, and a ValueError for a Conv + GlobalAvgPool readout,
+    which needs the full spatial covariance (requirements.py:100-112)."""
+    rng = np.random.default_rng(11)
+    x1 = rng.standard_normal((3, 5, 5, 3))
+    x2 = None if same_inputs else rng.standard_normal((4, 5, 5, 3))
+    block = [o.Conv(1, (3, 3)), o.Relu()]
+    readout = ([o.Conv(1, (3, 3)), o.GlobalAvgPool(), o.Dense(1)] if avg_pool
+               else [o.Flatten(), o.Dense(1)])
+    composed = o.serial(*block, *readout)(x1, x2)
+    rf, bf = o.serial(*readout), o.serial(*block)
+    # the default block kernel is diagonal-spatial for the Flatten readout: its Relu runs on the
+    # diagonal entries alone, where correlations near 1 make the arc-cosine lose ~1e-10
+    tol = 1e-12 if avg_pool else 1e-8
+    for k in (rf.apply_to_kernel(bf(x1, x2, diagonal_spatial=False)),
+              rf.apply_to_kernel(bf(x1, x2))):
+        np.testing.assert_allclose(k.nngp, composed.nngp, rtol=tol)
+        np.testing.assert_allclose(k.ntk, composed.ntk, rtol=tol)
+    if avg_pool:
+        with pytest.raises(ValueError):
+            rf.apply_to_kernel(bf(x1, x2, diagonal_spatial=True))
+        with pytest.raises(ValueError):
+            o.serial(*block, *readout)(x1, x2, diagonal_spatial=True)
+    else:
+        k = rf.apply_to_kernel(bf(x1, x2, diagonal_spatial=True))
+        np.testing.assert_allclose(k.nngp, composed.nngp, rtol=1e-8)
+        np.testing.assert_allclose(k.ntk, composed.ntk, rtol=1e-8)
+
+
 def _conv_expectation(x1, x2, W_std, b_std, fs=3):
     """E[f(x1)[h,w] f(x2)[h',w']] of one SAME conv layer, written out directly."""
     n1, H, W, C = x1.shape
