@@ -278,8 +278,12 @@ int ntg_gemm_tc(void* stream, const float* a, int64_t lda, const float* b, int64
 
 /* The tensor-core Cholesky of predict.gradient_descent_mse (predict.py:1224-1258,
  * cho_factor / cho_solve): A = K + lambda I = L L^T in FP32 with 128-wide panels
- * (diagonal block factored and inverted by one CTA, the panel below by forward
- * substitution, the trailing update by ntg_gemm_tc). K [n, n] float32 contiguous;
+ * (diagonal block factored and inverted by one CTA, the panel below as the product
+ * with that inverse and the trailing update both by ntg_gemm_tc). The work runs on
+ * three library streams forked from `stream` and joined back into it before the
+ * call's work ends: the diagonal blocks, panels and next column block on a
+ * high-priority stream, the rest of each trailing update one panel behind on a
+ * second, the inverse factors below on a third. K [n, n] float32 contiguous;
  * L [n, ldl] row-major (ldl >= n, a multiple of 4, L 16-byte aligned) receives the
  * lower factor, zeros above the diagonal; lambda and info as ntg_chol_factor.
  * factor_workspace (ntg_chol_factor_tc_workspace_bytes) receives the inverses of
@@ -293,7 +297,7 @@ int ntg_chol_factor_tc(void* stream, const float* A, int64_t n, double diag_reg,
 /* X = (K + lambda I)^{-1} B, B and X [n, m] row-major, from a factor of
  * ntg_chol_factor_tc (L itself is not read: the solves multiply by the inverse
  * factors of the factor workspace): for m <= 16 two triangular matrix-vector
- * products (a warp per row), for more right-hand sides two ntg_gemm_tc products on
+ * products (two rows per warp), for more right-hand sides two ntg_gemm_tc products on
  * the transposed right-hand sides. Refinement keeps X in FP64 and accumulates the
  * products with K in double-float arithmetic (two FP32 words, about 44 significant
  * bits): for m <= 16 at most refine_iters iterations of conjugate gradients
@@ -302,12 +306,24 @@ int ntg_chol_factor_tc(void* stream, const float* A, int64_t n, double diag_reg,
  * cond(K) * u > 1); for
  * m > 16 refine_iters steps of x <- x + (L L^T)^{-1} (b - (K + lambda I) x).
  * final_residual (device double, optional) receives max |b - (K + lambda I) X| of
- * the returned X. */
+ * the returned X; x64_out (device double [n, m], optional) the solution before its
+ * rounding to FP32, for products that keep its precision (ntg_gemm_df). */
 size_t ntg_chol_solve_tc_workspace_bytes(int64_t n, int64_t m, int64_t ldl);
 int ntg_chol_solve_tc(void* stream, const float* A, const float* L, int64_t ldl,
                       const void* factor_workspace, const double* lambda, int64_t n,
                       const float* B, int64_t m, float* X, int32_t refine_iters, void* workspace,
-                      size_t workspace_bytes, double* final_residual);
+                      size_t workspace_bytes, double* final_residual, double* x64_out);
+/* Y = Y0 + A X in double-float arithmetic (two FP32 words, about 44 significant
+ * bits), rounded to FP32: A [rows, n] float32 (row pitch lda), X [n, m] FP64
+ * row-major, Y0 (optional) and Y [rows, m] float32. The mean prediction
+ * k_test_train (K + lambda I)^{-1} y of predict.py:236-276 and 566-745: with an
+ * ill-conditioned K the product cancels, and an FP32 product of the FP32-rounded
+ * solution loses cond-many digits that the FP64 solution of ntg_chol_solve_tc
+ * keeps. workspace: ntg_gemm_df_workspace_bytes(rows, n, m). */
+size_t ntg_gemm_df_workspace_bytes(int64_t rows, int64_t n, int64_t m);
+int ntg_gemm_df(void* stream, const float* A, int64_t lda, int64_t rows, int64_t n,
+                const double* X, int64_t m, const float* Y0, float* Y, void* workspace,
+                size_t workspace_bytes);
 /* log det(L L^T) of a factor of ntg_chol_factor_tc -> out[0] (device double). */
 int ntg_chol_logdet_tc(void* stream, const float* L, int64_t n, int64_t ldl, double* out);
 

@@ -7,13 +7,15 @@ NNGP / NTK / NTKGP posterior and the infinite-ensemble predictions on the same k
 signature (predict.py:71-278) and returns ``predict_fn(t=None, fx_train_0=0.,
 fx_test_0=None, k_test_train=None)``. ``t=None`` (infinite time) and a scalar
 ``t=inf`` take the Cholesky path: an FP32 Cholesky of K + lambda I on the GPU (128-wide panels,
-trailing updates on the tcgen05 tensor cores), FP32 triangular solves and
-iterative refinement with the residual accumulated in FP64 (or double-float for
-more than 16 right-hand sides; `refine_iters`, default 2; 0 gives the plain
-FP32 solve), all in libntgb300.so. The factorisation is computed once
-and cached, as the reference caches it (predict.py:163). Finite ``t`` uses the
-eigenbasis of predict.py:185-229 with this library's own eigensolver (two-sided
-block Jacobi in FP32, ntg_eigh), its spectral-weight kernel and FP32 GEMMs.
+the panel solves and trailing updates on the tcgen05 tensor cores), solves by the
+explicit inverse factors and a refinement whose products with K are accumulated in
+double-float (preconditioned conjugate gradients for up to 16 right-hand sides, plain
+refinement steps for more; `refine_iters` overrides the default, 0 gives the plain FP32
+solve), all in libntgb300.so. The mean predictions multiply k_test_train by the FP64
+solution in double-float (ntg_gemm_df). The factorisation is computed once and cached,
+as the reference caches it (predict.py:163). Finite ``t`` uses the eigenbasis of
+predict.py:185-229 with this library's own eigensolver (two-sided block Jacobi in FP32
+with double-float refinement, ntg_eigh), its spectral-weight kernel and FP32 GEMMs.
 Only 2-D ``k_train_train`` with ``trace_axes=(-1,)`` is supported.
 """
 from __future__ import annotations
@@ -40,6 +42,21 @@ def _gemm(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     out = torch.empty((a.shape[0], b.shape[1]), device=a.device, dtype=torch.float32)
     L.call('ntg_gemm', L.stream(), L.ptr(a), L.ptr(b), L.ptr(out), a.shape[0], b.shape[1],
            a.shape[1], 0)
+    return out
+
+
+def _gemm_df(a: torch.Tensor, x64: torch.Tensor) -> torch.Tensor:
+    """a @ x64 for a [rows, n] float32 and x64 [n, m] float64, accumulated in double-float
+    and rounded to float32 (ntg_gemm_df): the mean predictions k_test_train A^{-1} y, whose
+    products cancel when A is ill-conditioned, keep the digits of the FP64 solution."""
+    a = a.contiguous()
+    rows, n = a.shape
+    m = x64.shape[1]
+    out = torch.empty((rows, m), device=a.device, dtype=torch.float32)
+    ws_bytes = int(L.load().ntg_gemm_df_workspace_bytes(rows, n, m))
+    ws = torch.empty((ws_bytes,), device=a.device, dtype=torch.uint8)
+    L.call('ntg_gemm_df', L.stream(), L.ptr(a), n, rows, n, x64.data_ptr(), m, None,
+           out.data_ptr(), ws.data_ptr(), ws_bytes)
     return out
 
 
@@ -145,16 +162,19 @@ class CholeskySolver:
     COLS = 4096  # right-hand sides per ntg_chol_solve_tc call (bounds its workspace)
 
     def solve(self, b: torch.Tensor, refine_iters: Optional[int] = None,
-              residual: bool = True) -> torch.Tensor:
+              residual: bool = True, want_x64: bool = False):
         """A^{-1} b; refine_iters overrides the solver's refinement steps; residual=False
-        skips the final residual kept in self.residual."""
+        skips the final residual kept in self.residual. want_x64: also return the FP64
+        solution before its rounding to float32, as (x, x64)."""
         b = b.reshape(self.n, -1).contiguous()
         refine = self.refine if refine_iters is None else int(refine_iters)
         if refine is None:
             refine = self.REFINE_FEW if b.shape[1] <= self.FEW else self.REFINE_MANY
         if self.info:
-            return torch.full_like(b, float('nan'))
+            nan = torch.full_like(b, float('nan'))
+            return (nan, nan.double()) if want_x64 else nan
         out = torch.empty_like(b)
+        x64 = torch.empty(b.shape, device=b.device, dtype=torch.float64) if want_x64 else None
         cols = min(b.shape[1], self.COLS)
         lib = L.load()
         ws_bytes = int(lib.ntg_chol_solve_tc_workspace_bytes(self.n, cols, self.ldl))
@@ -164,15 +184,20 @@ class CholeskySolver:
         for c0 in range(0, b.shape[1], cols):
             bc = b if single else b[:, c0:c0 + cols].contiguous()
             xc = out if single else torch.empty_like(bc)
+            x64c = x64 if (single or x64 is None) else torch.empty(bc.shape, device=b.device,
+                                                                     dtype=torch.float64)
             L.call('ntg_chol_solve_tc', L.stream(), L.ptr(self.k), self.Lbuf.data_ptr(), self.ldl,
                    self.fws.data_ptr(), self.lam.data_ptr(), self.n, L.ptr(bc), bc.shape[1],
                    L.ptr(xc), refine, ws.data_ptr(), ws_bytes,
-                   None if res is None else res.data_ptr())
+                   None if res is None else res.data_ptr(),
+                   None if x64c is None else x64c.data_ptr())
             if not single:
                 out[:, c0:c0 + cols] = xc
+                if x64 is not None:
+                    x64[:, c0:c0 + cols] = x64c
         if res is not None:
             self.residual = res
-        return out
+        return (out, x64) if want_x64 else out
 
 
 def gradient_descent_mse(k_train_train, y_train, learning_rate: float = 1.,
@@ -213,8 +238,8 @@ def gradient_descent_mse(k_train_train, y_train, learning_rate: float = 1.,
             if fx_test_0 is None:
                 return fx_train_t
             rhs = y if fx_train_0 is None else y - _as_like(fx_train_0, y)
-            x = solver().solve(rhs)
-            fx_test_t = _as_like(fx_test_0, None) + _gemm(_dev(k_test_train), x)
+            _, x64 = solver().solve(rhs, want_x64=True)
+            fx_test_t = _as_like(fx_test_0, None) + _gemm_df(_dev(k_test_train), x64)
             if fx_train_0 is None:
                 return fx_test_t
             return fx_train_t, fx_test_t
@@ -428,8 +453,9 @@ def gp_inference(k_train_train, y_train, diag_reg: float = 0.,
     NNGP / NTK / NTKGP posterior mean and, given ``k_test_test``, covariance.
 
     Every solve runs on this module's Cholesky kernels (FP32 factorisation cached per
-    kernel, blocked triangular solves with FP64 refinement) and every product on its
-    GEMM kernel; 2-D kernels with ``trace_axes=(-1,)``."""
+    kernel, solves refined in double-float), the means on the double-float product with
+    the FP64 solution and every other product on its GEMM kernel; 2-D kernels with
+    ``trace_axes=(-1,)``."""
     if tuple(trace_axes) not in ((-1,), (1,)):
         raise NotImplementedError('nt_gb300 supports trace_axes=(-1,)')
     y = _dev(y_train)
@@ -453,9 +479,9 @@ def gp_inference(k_train_train, y_train, diag_reg: float = 0.,
             if k_td is None:
                 mean = y
             else:
-                if k not in k_inv_y:
-                    k_inv_y[k] = solve(k).solve(y, residual=False)
-                mean = _gemm(k_td, k_inv_y[k].reshape(y.shape[0], -1)).reshape(
+                if k not in k_inv_y:  # the FP64 solution: the product below cancels
+                    k_inv_y[k] = solve(k).solve(y, residual=False, want_x64=True)[1]
+                mean = _gemm_df(k_td, k_inv_y[k].reshape(y.shape[0], -1)).reshape(
                     (k_td.shape[0],) + tuple(y.shape[1:]))
             if k_test_test is None:
                 out[g] = mean

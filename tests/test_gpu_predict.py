@@ -178,3 +178,50 @@ def test_gp_inference_ntkgp_and_errors(nt):
         nt.predict.gp_inference({'ntk': k_dd.ntk}, y_train)(get='ntk',
                                                            k_test_train={'ntk': k_td.ntk},
                                                            k_test_test=k_tt.nngp)
+
+
+def _power_law_features(seed, n, d=256, p=1.5):
+    """Rows with a power-law feature spectrum: their Gram matrix is ill-conditioned like a
+    deep-network NTK (eigenvalues ~ i^-2p)."""
+    rng = np.random.default_rng(seed)
+    scale = np.arange(1, d + 1, dtype=np.float64) ** -p
+    return rng.standard_normal((n, d)) * scale
+
+
+def test_infinite_time_mean_is_float64_accurate_on_an_ill_conditioned_kernel(nt):
+    """predict.py:236-276 at t=None: k_test_train (K + lambda I)^{-1} y cancels when K is
+    ill-conditioned (here cond ~ 7e4); the mean is formed from the FP64 solution in
+    double-float, so it matches float64 to FP32 rounding rather than losing cond-many
+    digits in an FP32 product. gp_inference's mean takes the same path."""
+    feats = _power_law_features(7, 900)
+    xtr, xte = feats[:800], feats[800:]
+    k = (xtr @ xtr.T).astype(np.float32)
+    kts = (xte @ xtr.T).astype(np.float32)
+    y = onehot(3, 800)
+    reg = 1e-2
+    a = k.astype(np.float64) + reg * np.trace(k.astype(np.float64)) / 800 * np.eye(800)
+    assert np.linalg.cond(a) > 1e4
+    want = kts.astype(np.float64) @ sla.cho_solve(sla.cho_factor(a), y)
+    scale = np.max(np.abs(want))
+    fx = nt.predict.gradient_descent_mse(k, y, diag_reg=reg)(None, 0., 0., kts)[1]
+    assert np.max(np.abs(fx.cpu().numpy() - want)) / scale < 1e-5
+    mean = nt.predict.gp_inference(k, y, diag_reg=reg)(get='nngp', k_test_train=kts)
+    assert np.max(np.abs(mean.cpu().numpy() - want)) / scale < 1e-5
+
+
+def test_gemm_df_keeps_a_cancelling_product(nt):
+    """ntg_gemm_df: A X with X = X1 + 1e6 X2, A X2 ~ 0 (X2 in A's null space): an FP32
+    product would lose ~6 digits; double-float keeps the result to FP32 rounding."""
+    from nt_gb300 import predict
+    rng = np.random.default_rng(4)
+    rows_, n, m = 37, 1000, 3
+    a = rng.standard_normal((rows_, n)).astype(np.float32)
+    a64 = a.astype(np.float64)
+    null = sla.null_space(a64)[:, :m]
+    x = rng.standard_normal((n, m)) + 1e6 * null
+    want = a64 @ x
+    got = predict._gemm_df(torch.from_numpy(a).cuda(), torch.from_numpy(x).cuda())
+    got = got.cpu().numpy().astype(np.float64)
+    assert np.max(np.abs(got - want) / np.abs(want)) < 1e-6
+    # the FP32 product of the same operands, for scale: far off
+    assert np.max(np.abs(a @ x.astype(np.float32) - want) / np.abs(want)) > 1e-4
