@@ -434,8 +434,9 @@ def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=64, precision='fp32', 
                    tile=None, xs_in=None, xt_in=None, diag_reg=1e-6):
     """Kernel-ridge loss of the Myrtle-5 NTK, ||y_t - K_ts (K_ss + 1e-6 tr(K_ss)/n I)^-1 y_s||^2,
     and its gradient with respect to the support set x_s (forward through nt.batch's fused
-    grid, backward through its checkpointed tiles and the hand-written adjoints; the solve
-    and its adjoint on the library's Cholesky kernels). A bounded sample of the
+    grid, backward through its checkpointed tiles and the hand-written adjoints; the
+    prediction K_ts A^-1 y_s and its adjoint on the library's Cholesky kernels and the
+    double-float product, predict.kernel_ridge_predict). A bounded sample of the
     [200]-support / [2000]-target configuration: x_s [n_s], x_t [n_t] from the synthetic
     inputs, one-hot labels over 10 classes (seed 2)."""
     from nt_gb300 import predict
@@ -452,8 +453,8 @@ def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=64, precision='fp32', 
         a.record()
         kss = batched(xs, None, 'ntk', precision=precision)
         kts = batched(xt, xs, 'ntk', precision=precision)
-        alpha = predict.kernel_ridge_solve(kss, ys, diag_reg=diag_reg)
-        loss = ((yt - predict.matmul(kts, alpha)) ** 2).sum()
+        pred = predict.kernel_ridge_predict(kts, kss, ys, diag_reg=diag_reg)
+        loss = ((yt - pred) ** 2).sum()
         loss.backward()
         b.record()
         torch.cuda.synchronize()
@@ -661,8 +662,10 @@ def config5_timing(torch, nt, kf):
     (seed 2), in the plain FP32 and the mixed forms (one warm-up evaluation, one timed).
     Parity of these gradients against float64 finite differences of the oracle is checked
     at reduced sizes in the test suite (the oracle would need days at this size); here the
-    gradient is checked against a central difference of the loss along a seeded direction
-    through the same forward path."""
+    gradient is checked against central differences of the loss along its own direction
+    through the same forward path, Richardson-extrapolated from steps h and 2h that move the
+    loss by about 1 % and 2 % (the float32 kernels fix the loss to about cond(A) u, which
+    bounds any such check at diag_reg = 1e-6)."""
     dev = torch.device('cuda', torch.cuda.current_device())
     xs = torch.from_numpy(np.random.default_rng(5).standard_normal((200,) + IMG).astype(
         np.float32)).to(dev)
@@ -693,10 +696,14 @@ def config5_timing(torch, nt, kf):
         v = (g / g.norm()).to(dev)
         with torch.no_grad():
             l0 = krr_loss(torch, nt, kf, xs, xt, 'fp32', diag_reg=reg)
-            h = 5e-4 * abs(l0) / float(g.norm())
-            lp = krr_loss(torch, nt, kf, xs + h * v, xt, 'fp32', diag_reg=reg)
-            lm = krr_loss(torch, nt, kf, xs - h * v, xt, 'fp32', diag_reg=reg)
-        fd_dir = (lp - lm) / (2 * h)
+            h = 1e-2 * abs(l0) / float(g.norm())
+
+            def central(step):
+                lp = krr_loss(torch, nt, kf, xs + step * v, xt, 'fp32', diag_reg=reg)
+                lm = krr_loss(torch, nt, kf, xs - step * v, xt, 'fp32', diag_reg=reg)
+                return (lp - lm) / (2 * step)
+            d1, d2 = central(h), central(2 * h)
+        fd_dir = (4 * d1 - d2) / 3
         an = float(g.norm())
         out['fp32'][f'directional_fd_rel_diff_diag_reg_{reg:g}'] = abs(an - fd_dir) / abs(fd_dir)
     out['config'] = ('Myrtle-5 NTK kernel-ridge loss, d/dx_s; x_s [200] (seed 5), x_t [2000] '
@@ -715,8 +722,8 @@ def krr_loss(torch, nt, kf, xs, xt, precision, bs=200, diag_reg=1e-6):
     batched = nt.batch(kf, batch_size=bs)
     kss = batched(xs, None, 'ntk', precision=precision)
     kts = batched(xt, xs, 'ntk', precision=precision)
-    alpha = predict.kernel_ridge_solve(kss, ys, diag_reg=diag_reg)
-    return float(((yt - predict.matmul(kts, alpha)) ** 2).double().sum())
+    pred = predict.kernel_ridge_predict(kts, kss, ys, diag_reg=diag_reg)
+    return float(((yt - pred).double() ** 2).sum())
 
 
 def config3_timing(torch, nt, dev, n=5000, bs=128):
@@ -995,6 +1002,42 @@ def profile_nll():
     print(json.dumps({'profile_nll': 4096, 'grad': [float(w.grad), float(b.grad)]}))
 
 
+def profile_predict(n: int):
+    """Finite-time predictions (the eigenbasis paths of predict.py:185-229 and 860-1005) of
+    the FCN configuration on n training inputs [n, 784] (seed 0) and 64 test inputs (seed 1):
+    gradient_descent_mse at t = [1, 10, 100] with the test predictions, then the infinite
+    ensemble's NNGP/NTK means and covariances at t = 10; an NVTX range 'predict' selects the
+    launches after a warm-up of the same calls."""
+    import torch
+    import nt_gb300 as nt
+    from nt_gb300 import stax
+    dev = torch.device('cuda')
+    rows = []
+    for seed, count in ((0, n), (1, 64)):
+        v = np.random.default_rng(seed).standard_normal((count, 784))
+        rows.append(torch.from_numpy((v / np.linalg.norm(v, axis=1, keepdims=True) *
+                                      math.sqrt(784)).astype(np.float32)).to(dev))
+    x, xt = rows
+    y = torch.nn.functional.one_hot(torch.arange(n) % 10, 10).float().to(dev)
+    kf = stax.serial(*fcn_layers(stax))[2]
+    ktt = kf(x, None, 'ntk')
+    kts = kf(xt, x, 'ntk')
+
+    def run():
+        pred = nt.predict.gradient_descent_mse(ktt, y, diag_reg=1e-4)
+        out = pred([1., 10., 100.], 0., 0., kts)
+        ens = nt.predict.gradient_descent_mse_ensemble(kf, x, y, diag_reg=1e-4)
+        mean_cov = ens(10., xt, ('nngp', 'ntk'), compute_cov=True)
+        return out, mean_cov
+    run()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push('predict')
+    out, mean_cov = run()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    print(json.dumps({'profile_predict': n, 'fx_test_sum': float(out[1].sum())}))
+
+
 def profile_gemm(n: int):
     """Two n x n x n calls of the 3xTF32 tensor-core GEMM (ntg_gemm_tc), C = A B^T."""
     import torch
@@ -1018,6 +1061,7 @@ def main():
     ap.add_argument('--profile-chol', type=int, default=0)
     ap.add_argument('--profile-nll', action='store_true')
     ap.add_argument('--profile-gemm', type=int, default=0)
+    ap.add_argument('--profile-predict', type=int, default=0)
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=3)
@@ -1042,6 +1086,8 @@ def main():
         profile_nll()
     elif args.profile_gemm:
         profile_gemm(args.profile_gemm)
+    elif args.profile_predict:
+        profile_predict(args.profile_predict)
     elif args.impl == 'reference':
         run_reference(args)
     else:

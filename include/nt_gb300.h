@@ -307,23 +307,27 @@ int ntg_chol_factor_tc(void* stream, const float* A, int64_t n, double diag_reg,
  * m > 16 refine_iters steps of x <- x + (L L^T)^{-1} (b - (K + lambda I) x).
  * final_residual (device double, optional) receives max |b - (K + lambda I) X| of
  * the returned X; x64_out (device double [n, m], optional) the solution before its
- * rounding to FP32, for products that keep its precision (ntg_gemm_df). */
+ * rounding to FP32, for products that keep its precision (ntg_gemm_df). B64 (device
+ * double [n, m], optional): the right-hand side in FP64, whose digits beyond B's
+ * float32 rounding the refinement then resolves (B still gives the first solve). */
 size_t ntg_chol_solve_tc_workspace_bytes(int64_t n, int64_t m, int64_t ldl);
 int ntg_chol_solve_tc(void* stream, const float* A, const float* L, int64_t ldl,
                       const void* factor_workspace, const double* lambda, int64_t n,
                       const float* B, int64_t m, float* X, int32_t refine_iters, void* workspace,
-                      size_t workspace_bytes, double* final_residual, double* x64_out);
+                      size_t workspace_bytes, double* final_residual, double* x64_out,
+                      const double* B64);
 /* Y = Y0 + A X in double-float arithmetic (two FP32 words, about 44 significant
- * bits), rounded to FP32: A [rows, n] float32 (row pitch lda), X [n, m] FP64
- * row-major, Y0 (optional) and Y [rows, m] float32. The mean prediction
+ * bits), rounded to FP32 into Y and / or stored in FP64 into Y64 (either may be
+ * NULL, not both): A [rows, n] float32 (row pitch lda), X [n, m] FP64 row-major,
+ * Y0 (optional) and Y [rows, m] float32, Y64 [rows, m] double. The mean prediction
  * k_test_train (K + lambda I)^{-1} y of predict.py:236-276 and 566-745: with an
  * ill-conditioned K the product cancels, and an FP32 product of the FP32-rounded
  * solution loses cond-many digits that the FP64 solution of ntg_chol_solve_tc
  * keeps. workspace: ntg_gemm_df_workspace_bytes(rows, n, m). */
 size_t ntg_gemm_df_workspace_bytes(int64_t rows, int64_t n, int64_t m);
 int ntg_gemm_df(void* stream, const float* A, int64_t lda, int64_t rows, int64_t n,
-                const double* X, int64_t m, const float* Y0, float* Y, void* workspace,
-                size_t workspace_bytes);
+                const double* X, int64_t m, const float* Y0, float* Y, double* Y64,
+                void* workspace, size_t workspace_bytes);
 /* log det(L L^T) of a factor of ntg_chol_factor_tc -> out[0] (device double). */
 int ntg_chol_logdet_tc(void* stream, const float* L, int64_t n, int64_t ldl, double* out);
 

@@ -119,9 +119,9 @@ SIGNATURES = {
                            C.c_int),
     'ntg_chol_solve_tc_workspace_bytes': ([_I64, _I64, _I64], C.c_size_t),
     'ntg_chol_solve_tc': ([_P, _P, _P, _I64, _P, _P, _I64, _P, _I64, _P, _I32, _P, C.c_size_t,
-                           _P, _P], C.c_int),
+                           _P, _P, _P], C.c_int),
     'ntg_gemm_df_workspace_bytes': ([_I64, _I64, _I64], C.c_size_t),
-    'ntg_gemm_df': ([_P, _P, _I64, _I64, _I64, _P, _I64, _P, _P, _P, C.c_size_t], C.c_int),
+    'ntg_gemm_df': ([_P, _P, _I64, _I64, _I64, _P, _I64, _P, _P, _P, _P, C.c_size_t], C.c_int),
     'ntg_chol_logdet_tc': ([_P, _P, _I64, _I64, _P], C.c_int),
     'ntg_eigh_workspace_bytes': ([_I64], C.c_size_t),
     'ntg_eigh': ([_P, _P, _I64, C.c_double, _P, _P, _I32, C.c_double, _I32, _P, C.c_size_t,

@@ -430,13 +430,15 @@ __device__ __forceinline__ void df_fma2(P2 a, P2 xh, P2 xl, P2& sh, P2& sl) {
   sh = sum;
 }
 
-// Double-float residual over 64 x 64 tiles of (row, column): R = B - (A + lambda I) X,
+// Double-float residual over 64 x 64 tiles of (row, column): R = B - (A + lambda I) X
+// (B64 in place of B when given),
 // the products taken with X's double-float split xs (split_df_kernel: split once, not
 // once per tile). Each thread keeps 4 x 4 sums as 4 x 2 packed pairs of columns
 // (df_fma2); rnorm receives max |R|.
 __global__ void __launch_bounds__(256)
     residual_df_kernel(const float* __restrict__ A, int64_t n, const double* lambda,
-                       const float* __restrict__ B, const double* __restrict__ X,
+                       const float* __restrict__ B, const double* __restrict__ B64,
+                       const double* __restrict__ X,
                        const float2* __restrict__ xs, int64_t m, float* __restrict__ R,
                        double* __restrict__ rnorm) {
   __shared__ float As[16][64 + 1];   // [k][i]
@@ -490,7 +492,8 @@ __global__ void __launch_bounds__(256)
       p2u(sh[u][v >> 1], h0, h1);
       p2u(sl[u][v >> 1], l0, l1);
       const double ax = (v & 1) ? (double)h1 + (double)l1 : (double)h0 + (double)l0;
-      const double r = (double)B[i * m + j] - ax - lambda[0] * X[i * m + j];
+      const double b = B64 ? B64[i * m + j] : (double)B[i * m + j];
+      const double r = b - ax - lambda[0] * X[i * m + j];
       R[i * m + j] = (float)r;
       rmax = fmax(rmax, fabs(r));
     }
@@ -730,12 +733,13 @@ __global__ void gemv_reduce_kernel(const float* __restrict__ part, int64_t rows,
 }
 
 // Double-float products, finished: v = sum of the row's tiles (+ lambda X[i, c] when
-// lambda is given: the square (K + lambda I) x), then out = v (mode 0), B - v (mode 1)
-// or B + v (mode 2, B nullable), as FP64 (out) and / or FP32 (out32). B, X, out and
-// out32 have row pitch ldo (the tiles' pitch is m).
+// lambda is given: the square (K + lambda I) x), then out = v (mode 0), b - v (mode 1)
+// or b + v (mode 2), b = B64 when given, else B (nullable: 0), as FP64 (out) and / or
+// FP32 (out32). B, B64, X, out and out32 have row pitch ldo (the tiles' pitch is m).
 __global__ void df_reduce_kernel(const float2* __restrict__ part2, int64_t rows, int64_t m,
                                  int64_t nkb, const double* lambda, const float* __restrict__ B,
-                                 const double* __restrict__ X, int64_t ldo, int mode,
+                                 const double* __restrict__ B64, const double* __restrict__ X,
+                                 int64_t ldo, int mode,
                                  double* __restrict__ out, float* __restrict__ out32,
                                  const int* skip) {
   if (skip && *skip) return;
@@ -749,7 +753,8 @@ __global__ void df_reduce_kernel(const float2* __restrict__ part2, int64_t rows,
     }
     double v = (double)hi + (double)lo;
     if (lambda) v += lambda[0] * X[o];
-    const double r = mode == 1 ? (double)B[o] - v : (mode == 2 && B) ? (double)B[o] + v : v;
+    const double b = B64 ? B64[o] : B ? (double)B[o] : 0.0;
+    const double r = mode == 1 ? b - v : mode == 2 ? b + v : v;
     if (out) out[o] = r;
     if (out32) out32[o] = (float)r;
   }
@@ -774,7 +779,8 @@ size_t df_part_bytes(int64_t rows, int64_t ncols, int64_t m) {
 // out = mode(B, (A + [lambda I]) x) for x [ncols, m <= kSmallM] given as its split xs:
 // gemv_part_kernel in double-float, then df_reduce_kernel. part2: df_part_bytes.
 void launch_matvec(cudaStream_t s, const float* A, int64_t lda, int64_t rows, int64_t ncols,
-                   const double* lambda, const float* B, const double* X, const float2* xs,
+                   const double* lambda, const float* B, const double* B64, const double* X,
+                   const float2* xs,
                    int64_t m, int64_t ldo, int mode, double* out, float* out32, float2* part2,
                    const PcgState* st) {
   const int* skip = st ? &st->all_done : nullptr;
@@ -788,8 +794,8 @@ void launch_matvec(cudaStream_t s, const float* A, int64_t lda, int64_t rows, in
 #undef NTG_MV
     default: launch_df_part<kSmallM>(s, grid, A, lda, rows, ncols, ks, xs, m, part2, skip);
   }
-  df_reduce_kernel<<<grid_for(rows * m), 256, 0, s>>>(part2, rows, m, nkb, lambda, B, X, ldo,
-                                                      mode, out, out32, skip);
+  df_reduce_kernel<<<grid_for(rows * m), 256, 0, s>>>(part2, rows, m, nkb, lambda, B, B64, X,
+                                                      ldo, mode, out, out32, skip);
 }
 // part[blk][j] = sum over the block's rows of u[i, j] * v[i, j] (v FP64, or vf FP32).
 __global__ void __launch_bounds__(256)
@@ -1237,7 +1243,7 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
                                  const void* factor_workspace, const double* lambda, int64_t n,
                                  const float* B, int64_t m, float* X, int32_t refine_iters,
                                  void* workspace, size_t workspace_bytes,
-                                 double* final_residual, double* x64_out) {
+                                 double* final_residual, double* x64_out, const double* B64) {
   NTG_REQUIRE(A && L && factor_workspace && lambda && B && X && workspace,
               "ntg_chol_solve_tc: null pointer");
   NTG_REQUIRE(n > 0 && n <= 46340 && m > 0, "ntg_chol_solve_tc: bad sizes");
@@ -1306,7 +1312,8 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
     auto matvec = [&](const double* v, int subtract, const float* bb, double* out, float* o32,
                       const PcgState* stp) {
       split_df_kernel<<<grid_for(n * m), 256, 0, s>>>(v, m, n, m, xs, stp);
-      launch_matvec(s, A, n, n, n, lambda, bb, v, xs, m, m, subtract, out, o32, dpart, stp);
+      launch_matvec(s, A, n, n, n, lambda, bb, bb ? B64 : nullptr, v, xs, m, m, subtract, out, o32,
+                    dpart, stp);
       note_launch(3);
     };
     matvec(x64, 1, B, r64, r32, nullptr);
@@ -1356,7 +1363,7 @@ extern "C" int ntg_chol_solve_tc(void* stream, const float* A, const float* L, i
       return check_launch("ntg_chol_solve_tc memset");
     split_df_kernel<<<grid_for(n * m), 256, 0, s>>>(x64, m, n, m, xsplit, nullptr);
     residual_df_kernel<<<dim3((unsigned)ceil_div(m, 64), (unsigned)ceil_div(n, 64)), 256, 0, s>>>(
-        A, n, lambda, B, x64, xsplit, m, r32, rnorm);
+        A, n, lambda, B, B64, x64, xsplit, m, r32, rnorm);
     note_launch(2);
     if (it == refine_iters) break;
     rc = apply(r32, nullptr);
@@ -1380,9 +1387,9 @@ extern "C" size_t ntg_gemm_df_workspace_bytes(int64_t rows, int64_t n, int64_t m
 }
 
 extern "C" int ntg_gemm_df(void* stream, const float* A, int64_t lda, int64_t rows, int64_t n,
-                           const double* X, int64_t m, const float* Y0, float* Y,
+                           const double* X, int64_t m, const float* Y0, float* Y, double* Y64,
                            void* workspace, size_t workspace_bytes) {
-  NTG_REQUIRE(A && X && Y && workspace, "ntg_gemm_df: null pointer");
+  NTG_REQUIRE(A && X && (Y || Y64) && workspace, "ntg_gemm_df: null pointer");
   NTG_REQUIRE(rows > 0 && n > 0 && m > 0 && lda >= n, "ntg_gemm_df: bad sizes");
   NTG_REQUIRE(workspace_bytes >= ntg_gemm_df_workspace_bytes(rows, n, m),
               "ntg_gemm_df: workspace smaller than ntg_gemm_df_workspace_bytes");
@@ -1394,8 +1401,8 @@ extern "C" int ntg_gemm_df(void* stream, const float* A, int64_t lda, int64_t ro
   for (int64_t c0 = 0; c0 < m; c0 += kSmallM) {
     const int64_t mc = mini(kSmallM, m - c0);
     split_df_kernel<<<grid_for(n * mc), 256, 0, s>>>(X + c0, m, n, mc, xs, nullptr);
-    launch_matvec(s, A, lda, rows, n, nullptr, Y0 ? Y0 + c0 : nullptr, nullptr, xs, mc, m, 2,
-                  nullptr, Y + c0, dpart, nullptr);
+    launch_matvec(s, A, lda, rows, n, nullptr, Y0 ? Y0 + c0 : nullptr, nullptr, nullptr, xs, mc,
+                  m, 2, Y64 ? Y64 + c0 : nullptr, Y ? Y + c0 : nullptr, dpart, nullptr);
     note_launch(3);
   }
   return check_launch("ntg_gemm_df");

@@ -45,19 +45,22 @@ def _gemm(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     return out
 
 
-def _gemm_df(a: torch.Tensor, x64: torch.Tensor) -> torch.Tensor:
+def _gemm_df(a: torch.Tensor, x64: torch.Tensor, out64: bool = False):
     """a @ x64 for a [rows, n] float32 and x64 [n, m] float64, accumulated in double-float
     and rounded to float32 (ntg_gemm_df): the mean predictions k_test_train A^{-1} y, whose
-    products cancel when A is ill-conditioned, keep the digits of the FP64 solution."""
+    products cancel when A is ill-conditioned, keep the digits of the FP64 solution.
+    out64: return (float32, float64) results."""
     a = a.contiguous()
+    x64 = x64.contiguous()
     rows, n = a.shape
     m = x64.shape[1]
     out = torch.empty((rows, m), device=a.device, dtype=torch.float32)
+    o64 = torch.empty((rows, m), device=a.device, dtype=torch.float64) if out64 else None
     ws_bytes = int(L.load().ntg_gemm_df_workspace_bytes(rows, n, m))
     ws = torch.empty((ws_bytes,), device=a.device, dtype=torch.uint8)
     L.call('ntg_gemm_df', L.stream(), L.ptr(a), n, rows, n, x64.data_ptr(), m, None,
-           out.data_ptr(), ws.data_ptr(), ws_bytes)
-    return out
+           out.data_ptr(), None if o64 is None else o64.data_ptr(), ws.data_ptr(), ws_bytes)
+    return (out, o64) if out64 else out
 
 
 def _gemm_tn(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
@@ -162,11 +165,15 @@ class CholeskySolver:
     COLS = 4096  # right-hand sides per ntg_chol_solve_tc call (bounds its workspace)
 
     def solve(self, b: torch.Tensor, refine_iters: Optional[int] = None,
-              residual: bool = True, want_x64: bool = False):
+              residual: bool = True, want_x64: bool = False,
+              b64: Optional[torch.Tensor] = None):
         """A^{-1} b; refine_iters overrides the solver's refinement steps; residual=False
         skips the final residual kept in self.residual. want_x64: also return the FP64
-        solution before its rounding to float32, as (x, x64)."""
+        solution before its rounding to float32, as (x, x64). b64: the right-hand side in
+        FP64 (b its float32 rounding), which the refinement then solves for."""
         b = b.reshape(self.n, -1).contiguous()
+        if b64 is not None:
+            b64 = b64.reshape(self.n, -1).contiguous()
         refine = self.refine if refine_iters is None else int(refine_iters)
         if refine is None:
             refine = self.REFINE_FEW if b.shape[1] <= self.FEW else self.REFINE_MANY
@@ -183,6 +190,7 @@ class CholeskySolver:
         single = b.shape[1] <= cols
         for c0 in range(0, b.shape[1], cols):
             bc = b if single else b[:, c0:c0 + cols].contiguous()
+            b64c = b64 if (single or b64 is None) else b64[:, c0:c0 + cols].contiguous()
             xc = out if single else torch.empty_like(bc)
             x64c = x64 if (single or x64 is None) else torch.empty(bc.shape, device=b.device,
                                                                      dtype=torch.float64)
@@ -190,7 +198,8 @@ class CholeskySolver:
                    self.fws.data_ptr(), self.lam.data_ptr(), self.n, L.ptr(bc), bc.shape[1],
                    L.ptr(xc), refine, ws.data_ptr(), ws_bytes,
                    None if res is None else res.data_ptr(),
-                   None if x64c is None else x64c.data_ptr())
+                   None if x64c is None else x64c.data_ptr(),
+                   None if b64c is None else b64c.data_ptr())
             if not single:
                 out[:, c0:c0 + cols] = xc
                 if x64 is not None:
@@ -238,8 +247,10 @@ def gradient_descent_mse(k_train_train, y_train, learning_rate: float = 1.,
             if fx_test_0 is None:
                 return fx_train_t
             rhs = y if fx_train_0 is None else y - _as_like(fx_train_0, y)
-            _, x64 = solver().solve(rhs, want_x64=True)
-            fx_test_t = _as_like(fx_test_0, None) + _gemm_df(_dev(k_test_train), x64)
+            # differentiable in k_train_train, k_test_train, y and the initial outputs
+            fx_test_t = _as_like(fx_test_0, None) + _RidgePredict.apply(
+                k, _dev(k_test_train), rhs, float(diag_reg), bool(diag_reg_absolute_scale),
+                refine_iters, solver())
             if fx_train_0 is None:
                 return fx_test_t
             return fx_train_t, fx_test_t
@@ -384,6 +395,70 @@ def kernel_ridge_solve(k_train_train, y_train, diag_reg: float = 0.,
     y = y_train if isinstance(y_train, torch.Tensor) else _dev(y_train)
     return _RidgeSolve.apply(k, y, float(diag_reg), bool(diag_reg_absolute_scale),
                              refine_iters)
+
+
+class _RidgePredict(torch.autograd.Function):
+    """k_test_train A^{-1} y, A = K + lambda I, from the FP64 solution and a double-float
+    product (ntg_gemm_df): with an ill-conditioned A the product cancels, and an FP32
+    product of the rounded solution would lose cond(A)-many of its digits. Backward,
+    with alpha = A^{-1} y and the cotangent g: gK_td = g alpha^T, gY = A^{-1} K_td^T g
+    (the right-hand side in double-float, solved for in FP64),
+    gK = -gY alpha^T - [relative lambda] (r / n) <gY, alpha> I."""
+
+    @staticmethod
+    def forward(ctx, k, k_td, y, diag_reg, absolute, refine_iters, solver):
+        n = k.shape[0]
+        y2 = y.reshape(n, -1).contiguous()
+        if solver is None:
+            solver = CholeskySolver(k.contiguous(), diag_reg, absolute, refine_iters)
+        alpha, alpha64 = solver.solve(y2, want_x64=True)
+        k_td = k_td.contiguous()
+        out = _gemm_df(k_td, alpha64)
+        ctx.solver, ctx.alpha, ctx.meta = solver, alpha, (diag_reg, absolute, tuple(y.shape))
+        ctx.save_for_backward(k_td)
+        return out.reshape((k_td.shape[0],) + tuple(y.shape[1:]))
+
+    @staticmethod
+    def backward(ctx, g):
+        diag_reg, absolute, yshape = ctx.meta
+        solver, alpha = ctx.solver, ctx.alpha
+        (k_td,) = ctx.saved_tensors
+        n = alpha.shape[0]
+        g2 = g.reshape(k_td.shape[0], -1).contiguous()
+        gk = gk_td = gy = None
+        if ctx.needs_input_grad[1]:
+            gk_td = _gemm(g2, alpha.t().contiguous())
+        if ctx.needs_input_grad[0] or ctx.needs_input_grad[2]:
+            # K_td^T g in double-float and solved for in FP64: its float32 rounding alone
+            # would move gY by cond(A) u
+            r32, r64 = _gemm_df(k_td.t().contiguous(), g2.double(), out64=True)
+            gy = solver.solve(r32, residual=False, b64=r64)
+            if ctx.needs_input_grad[0]:
+                gk = torch.empty((n, n), device=alpha.device)
+                L.call('ntg_gemm_ex', L.stream(), L.ptr(gy), L.ptr(alpha.t().contiguous()),
+                       L.ptr(gk), n, n, alpha.shape[1], 0, -1., 0)
+                if not absolute and diag_reg:
+                    gk.diagonal().sub_((diag_reg / n) *
+                                       (gy.double() * alpha.double()).sum().float())
+            gy = gy.reshape(yshape)
+        return gk, gk_td, gy, None, None, None, None
+
+
+def kernel_ridge_predict(k_test_train, k_train_train, y_train, diag_reg: float = 0.,
+                         diag_reg_absolute_scale: bool = False,
+                         refine_iters: Optional[int] = None):
+    """k_test_train (K + diag_reg * trace(K) / n * I)^{-1} y, differentiable with respect to
+    both kernels and y: the mean prediction of gradient_descent_mse at t = None
+    (predict.py:236-276), and the prediction of kernel-ridge losses such as
+    ||y_t - K_ts (K_ss + lambda I)^{-1} y_s||^2 (dataset distillation). The product
+    is formed from the FP64 solution in double-float, so an ill-conditioned K costs
+    no digits beyond those of the kernels themselves; the backward reuses the
+    factorisation (see _RidgePredict)."""
+    k = k_train_train if isinstance(k_train_train, torch.Tensor) else _dev(k_train_train)
+    kt = k_test_train if isinstance(k_test_train, torch.Tensor) else _dev(k_test_train)
+    y = y_train if isinstance(y_train, torch.Tensor) else _dev(y_train)
+    return _RidgePredict.apply(k, kt, y, float(diag_reg), bool(diag_reg_absolute_scale),
+                               refine_iters, None)
 
 
 class _MatMul(torch.autograd.Function):

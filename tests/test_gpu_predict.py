@@ -225,3 +225,42 @@ def test_gemm_df_keeps_a_cancelling_product(nt):
     assert np.max(np.abs(got - want) / np.abs(want)) < 1e-6
     # the FP32 product of the same operands, for scale: far off
     assert np.max(np.abs(a @ x.astype(np.float32) - want) / np.abs(want)) > 1e-4
+
+
+def test_kernel_ridge_predict_and_its_gradients_vs_float64(nt):
+    """kernel_ridge_predict (the t=None mean of predict.py:236-276 as a differentiable op) on
+    an ill-conditioned kernel: forward and d/d(K_td, K, y) of <w, pred> against the float64
+    closed forms gK_td = w alpha^T, gY = A^-1 K_td^T w, gK = -gY alpha^T - (r/n) <gY, alpha> I."""
+    feats = _power_law_features(11, 136, d=96)
+    xtr, xte = feats[:96], feats[96:]
+    k = (xtr @ xtr.T).astype(np.float32)
+    kts = (xte @ xtr.T).astype(np.float32)
+    y = np.random.default_rng(5).standard_normal((96, 3)).astype(np.float32)
+    w = np.random.default_rng(6).standard_normal((40, 3))
+    reg = 1e-3
+    k64 = k.astype(np.float64)
+    a = k64 + reg * np.trace(k64) / 96 * np.eye(96)
+    assert np.linalg.cond(a) > 1e3
+    alpha = np.linalg.solve(a, y.astype(np.float64))
+    want = kts.astype(np.float64) @ alpha
+    gy_want = np.linalg.solve(a, kts.astype(np.float64).T @ w)
+    gk_want = -gy_want @ alpha.T - reg / 96 * np.sum(gy_want * alpha) * np.eye(96)
+    gkt_want = w @ alpha.T
+    tk = torch.from_numpy(k).cuda().requires_grad_(True)
+    tkt = torch.from_numpy(kts).cuda().requires_grad_(True)
+    ty = torch.from_numpy(y).cuda().requires_grad_(True)
+    pred = nt.predict.kernel_ridge_predict(tkt, tk, ty, diag_reg=reg)
+    (pred.double() * torch.from_numpy(w).cuda()).sum().backward()
+
+    def rel(got, ref):
+        return np.max(np.abs(got.detach().cpu().numpy().astype(np.float64) - ref)) / np.max(np.abs(ref))
+    assert rel(pred, want) < 1e-6
+    assert rel(tkt.grad, gkt_want) < 1e-5
+    assert rel(ty.grad, gy_want) < 1e-5
+    assert rel(tk.grad, gk_want) < 1e-5
+    # gradient_descent_mse's t=None test prediction is the same differentiable op
+    tkt2 = torch.from_numpy(kts).cuda().requires_grad_(True)
+    fx = nt.predict.gradient_descent_mse(k, y, diag_reg=reg)(None, 0., 0., tkt2)[1]
+    assert rel(fx, want) < 1e-6
+    (fx.double() * torch.from_numpy(w).cuda()).sum().backward()
+    assert rel(tkt2.grad, gkt_want) < 1e-5
