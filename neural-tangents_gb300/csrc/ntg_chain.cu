@@ -257,9 +257,10 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
   const int r = tid >> 4, c0 = (tid & 15) * 2;
   const int lo = delta < 0 ? -delta : 0;
   const int hi = delta < 0 ? S : S - delta;
-  const P2 ML = p2((c0 >= 1 && c0 != S - r) ? 1.f : 0.f, (c0 + 1 != S - r) ? 1.f : 0.f);
-  const P2 MR = p2((c0 != S - 1 - r) ? 1.f : 0.f,
-                   (c0 + 1 <= S - 2 && c0 + 1 != S - 1 - r) ? 1.f : 0.f);
+  // 1/0 weights of the left / right neighbours of the thread's two columns
+  const float ml0 = (c0 >= 1 && c0 != S - r) ? 1.f : 0.f, ml1 = (c0 + 1 != S - r) ? 1.f : 0.f;
+  const float mr0 = (c0 != S - 1 - r) ? 1.f : 0.f;
+  const float mr1 = (c0 + 1 <= S - 2 && c0 + 1 != S - 1 - r) ? 1.f : 0.f;
   const int wp0 = (c0 + r) & (S - 1), wp1 = (c0 + 1 + r) & (S - 1);
   // Sample-2 entries at the skewed columns (wp0, wp1 = wp0 + 1 mod 32) as one aligned
   // 8-byte load: from the plane itself for even rows (wp0 even), from its copy shifted
@@ -291,6 +292,9 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
 
   int buf = 0;
   __syncthreads();
+  // unrolled by the period of the (A, B, new) plane ring, so that its rotation is a
+  // renaming of registers rather than moves
+#pragma unroll 3
   for (int s = lo; s < hi + NC; ++s) {
     P2 nq = zero, nt = zero;
     if (s < hi) {
@@ -310,15 +314,17 @@ __device__ __forceinline__ void line_s32(ChainCtx& cx, const ntg_chain_t& pg, co
       const bool has_t = k > 0;
       const P2 hq = add2(add2(Aq[k], Bq[k]), nq);
       const P2 ht = has_t ? add2(add2(At[k], Bt[k]), nt) : zero;
+      // the w-direction stencil per lane, in the order of the packed form
+      // (h + ml * left) + mr * right, from the two shuffled neighbours
       float h0, h1, e0 = 0.f, e1 = 0.f;
       p2u(hq, h0, h1);
       const float lq = wshift_left(h1), rq = wshift_right(h0);
-      const P2 cq = fma2(MR, p2(h1, rq), fma2(ML, p2(lq, h0), hq));
+      const P2 cq = p2(fmaf(mr0, h1, fmaf(ml0, lq, h0)), fmaf(mr1, rq, fmaf(ml1, h0, h1)));
       P2 ct = zero;
       if (has_t) {
         p2u(ht, e0, e1);
         const float lt = wshift_left(e1), rt = wshift_right(e0);
-        ct = fma2(MR, p2(e1, rt), fma2(ML, p2(lt, e0), ht));
+        ct = p2(fmaf(mr0, e1, fmaf(ml0, lt, e0)), fmaf(mr1, rt, fmaf(ml1, e0, e1)));
       }
       P2 oq = zero, ot = zero;
       if (p >= lo && p < hi) {  // uniform across the CTA
