@@ -257,6 +257,8 @@ def run_gpu(args):
 
     # Materialised per-layer stencil (conv + Relu epilogue) on a 16 x 16 tile at S = 32.
     st_gbs = stencil_roofline(torch, O, dev)
+    # the fused backward of conv + ReLU (+ AvgPool) layers: VJP + transposed stencil
+    vjp = [vjp_roofline(torch, dev, pooled) for pooled in (True, False)]
     gram_tc = gram_roofline(torch, O, dev)
     fb32, g32 = fwd_bwd_timing(torch, nt, kf, xd, precision='fp32')
     fbmx, gmx = fwd_bwd_timing(torch, nt, kf, xd, precision='mixed')
@@ -380,6 +382,7 @@ def run_gpu(args):
         'compute': {'bound': 'fp32', 'achieved_tflops': round(achieved_tflops, 2),
                     'flops_per_entry': flops_entry},
         'stencil_roofline': st_gbs,
+        'vjp_roofline': vjp,
         'gram_tc': gram_tc,
         'fwd_bwd': fwd_bwd,
         'side': side,
@@ -428,6 +431,46 @@ def stencil_roofline(torch, O, dev, pairs=256, reps=4):
     gbs = nbytes / (ms / 1e3) / 1e9
     return {'kernel': 'conv3_skew_kernel', 'pairs': B, 'bytes': nbytes, 'ms': round(ms, 3),
             'achieved': round(gbs, 1), 'unit': 'GB/s'}
+
+
+def vjp_roofline(torch, dev, pooled, n1=16, n2=32, reps=4):
+    """Fused ReLU VJP + transposed 3x3 stencil (ntg_conv_act_bwd) on [B, 32, 32, 32, 32]
+    pair kernels, B = n1 n2 = 512 pairs, both input cotangents written. Algorithmic bytes per
+    entry: pre-activations 8, output cotangents 8 (0.5 after the 2x2 AvgPool, which pools
+    both (h, h') and (w, w'): one cotangent entry per 16), input cotangents 8."""
+    from nt_gb300 import _lib as L
+    A = 32
+    B = n1 * n2
+    shp = (B, A, A, A, A)
+    pre_q = torch.rand(shp, device=dev) * 2 - 1
+    pre_t = torch.rand(shp, device=dev)
+    gshape = (B, 16, 16, 16, 16) if pooled else shp
+    gq = torch.rand(gshape, device=dev) - 0.5
+    gt = torch.rand(gshape, device=dev) - 0.5
+    var = torch.rand((n1 + n2, A, A), device=dev) + 2.
+    v1 = L.Var(var[:n1].data_ptr(), A * A, A, 1)
+    v2 = L.Var(var[n1:].data_ptr(), A * A, A, 1)
+    act = L.Act(L.NTG_ACT_ABRELU, 0., 1., 0., 0, 0.)
+    gin_q, gin_t = torch.empty(shp, device=dev), torch.empty(shp, device=dev)
+    gd1, gd2 = torch.zeros((n1, A, A), device=dev), torch.zeros((n2, A, A), device=dev)
+    ts = []
+    for i in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        L.call('ntg_conv_act_bwd', L.stream(), L.ptr(pre_q), L.ptr(pre_t), L.ptr(gq), L.ptr(gt),
+               int(pooled), L.ptr(gin_q), L.ptr(gin_t), B, n2, A, 2.0, act, v1, v2,
+               gd1.data_ptr(), gd2.data_ptr())
+        b.record()
+        torch.cuda.synchronize()
+        if i:
+            ts.append(a.elapsed_time(b))
+    ms = statistics.median(ts)
+    entries = B * A ** 4
+    per_entry = 8 + (0.5 if pooled else 8) + 8
+    nbytes = int(entries * per_entry)
+    return {'kernel': f'conv3_skew_vjp_kernel<{int(pooled)}>', 'pairs': B, 'bytes': nbytes,
+            'bytes_per_entry': per_entry, 'ms': round(ms, 3),
+            'achieved': round(nbytes / (ms / 1e3) / 1e9, 1), 'unit': 'GB/s'}
 
 
 def fwd_bwd_timing(torch, nt, kf, xd, n_t=128, n_s=64, bs=64, precision='fp32', reps=2,
@@ -1062,6 +1105,8 @@ def main():
     ap.add_argument('--profile-nll', action='store_true')
     ap.add_argument('--profile-gemm', type=int, default=0)
     ap.add_argument('--profile-predict', type=int, default=0)
+    ap.add_argument('--profile-vjp', action='store_true',
+                    help='time the fused backward (pooled and plain) and exit')
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=20)
     ap.add_argument('--warmup', type=int, default=3)
@@ -1088,6 +1133,10 @@ def main():
         profile_gemm(args.profile_gemm)
     elif args.profile_predict:
         profile_predict(args.profile_predict)
+    elif args.profile_vjp:
+        import torch
+        print(json.dumps({'vjp_roofline': [vjp_roofline(torch, torch.device('cuda'), p)
+                                           for p in (True, False)]}))
     elif args.impl == 'reference':
         run_reference(args)
     else:

@@ -2013,6 +2013,10 @@ cudaError_t launch_skew_vjp(cudaStream_t s, int64_t blocks, const float* pre_q, 
   constexpr size_t sm = skew_vjp_smem_bytes<POOLED>();
   cudaError_t e = cudaFuncSetAttribute(conv3_skew_vjp_kernel<POOLED>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  // all of the unified L1 / shared memory as shared memory: the resident CTAs' rings
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(conv3_skew_vjp_kernel<POOLED>,
+                             cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e == cudaSuccess)
     conv3_skew_vjp_kernel<POOLED><<<(unsigned)blocks, kThreads, sm, s>>>(
         pre_q, pre_t, g_q, g_t, gin_q, gin_t, batch, n2, (int)a, w2, act, var1, var2, gvar1,
