@@ -613,22 +613,31 @@ def nll_timing(torch, nt, dev):
 
 
 def gram_roofline(torch, O, dev):
-    """tcgen05 split-BF16 Gram of the NLL configuration, X [4096, 3072]: X X^T / D."""
+    """tcgen05 split-BF16 Gram of the NLL configuration, X [4096, 3072]: X X^T / D, as the
+    kernel computes it for x1 is x2 (the 528 tiles on or below the diagonal, mirrored) and for
+    two distinct operands (all 1024 tiles). FP32-equivalent rate: 2 n^2 d over the call;
+    tensor rate: the three BF16 products of the tiles computed."""
     x = torch.randn((4096, 3072), device=dev)
-    ts = []
-    for i in range(4):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
-        O.gram(x, x, 1)
-        b.record()
-        torch.cuda.synchronize()
-        if i:
-            ts.append(a.elapsed_time(b))
-    ms = statistics.median(ts)
-    flops = 2 * 4096 * 4096 * 3072
-    return {'kernel': 'gram_tc_kernel (+ bf16 split)', 'shape': [4096, 4096, 3072], 'ms': round(ms, 3),
-            'tflops_fp32_equivalent': round(flops / (ms / 1e3) / 1e12, 1),
-            'tensor_tflops_issued': round(3 * flops / (ms / 1e3) / 1e12, 1), 'unit': 'TFLOP/s'}
+    y = x.clone()
+    n, d, nb = 4096, 3072, 4096 // 128
+    out = {'kernel': 'gram_tc_kernel (+ bf16 split)', 'shape': [n, n, d], 'unit': 'TFLOP/s'}
+    for name, other, tiles in (('symmetric', x, nb * (nb + 1) // 2), ('general', y, nb * nb)):
+        ts = []
+        for i in range(4):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            O.gram(x, other, 1)
+            b.record()
+            torch.cuda.synchronize()
+            if i:
+                ts.append(a.elapsed_time(b))
+        ms = statistics.median(ts)
+        issued = 3 * 2 * tiles * 128 * 128 * d
+        out[name] = {'ms': round(ms, 3),
+                     'tflops_fp32_equivalent': round(2 * n * n * d / (ms / 1e3) / 1e12, 1),
+                     'tensor_tflops_issued': round(issued / (ms / 1e3) / 1e12, 1)}
+    out['ms'] = out['symmetric']['ms']
+    return out
 
 
 PARITY_PAIRS = 48
@@ -1105,6 +1114,8 @@ def main():
     ap.add_argument('--profile-nll', action='store_true')
     ap.add_argument('--profile-gemm', type=int, default=0)
     ap.add_argument('--profile-predict', type=int, default=0)
+    ap.add_argument('--profile-gram-timing', action='store_true',
+                    help='time the tensor-core Gram (symmetric and general) and exit')
     ap.add_argument('--profile-vjp', action='store_true',
                     help='time the fused backward (pooled and plain) and exit')
     ap.add_argument('--gpus', type=int, default=1)
@@ -1133,6 +1144,10 @@ def main():
         profile_gemm(args.profile_gemm)
     elif args.profile_predict:
         profile_predict(args.profile_predict)
+    elif args.profile_gram_timing:
+        import torch
+        from nt_gb300 import _ops as O
+        print(json.dumps({'gram_tc': gram_roofline(torch, O, torch.device('cuda'))}))
     elif args.profile_vjp:
         import torch
         print(json.dumps({'vjp_roofline': [vjp_roofline(torch, torch.device('cuda'), p)

@@ -3,7 +3,8 @@
 // Each float32 input is split into bf16 hi = bf16(x) and lo = bf16(x - hi);
 // x1 x2^T ~ hi1 hi2^T + hi1 lo2^T + lo1 hi2^T, the three products accumulated
 // in FP32 in tensor memory (the lo lo^T term is below float32 resolution of
-// the sum). Tiles: 128 x 128 outputs per CTA, K chunks of 64 bf16 (one 128-byte
+// the sum). For x1 == x2 only the tiles on or below the diagonal are computed and
+// the output is mirrored, so that it is exactly symmetric. Tiles: 128 x 128 outputs per CTA, K chunks of 64 bf16 (one 128-byte
 // swizzled row) moved by TMA into a 3-stage shared-memory ring; one thread
 // issues tcgen05.mma (M=128, N=128, K=16) and tcgen05.commit frees each stage;
 // four warps drain the accumulator with tcgen05.ld. Every mbarrier wait is
@@ -30,17 +31,35 @@ constexpr uint64_t WAIT_LIMIT = 1ull << 20;   // about a second of polling
 
 __device__ int g_gram_error = 0;
 
+// hi = bf16(x), lo = bf16(x - hi) for x [n, d] into [npad, dpad] (zero padding), eight
+// consecutive entries of a row per thread: two 16-byte loads (when rows are 16-byte
+// aligned) and one 16-byte store into each of hi and lo.
 __global__ void split_bf16_kernel(const float* __restrict__ x, int64_t n, int64_t d,
                                   int64_t npad, int64_t dpad, __nv_bfloat16* __restrict__ hi,
                                   __nv_bfloat16* __restrict__ lo) {
-  const int64_t total = npad * dpad;
+  const int64_t groups = dpad / 8, total = npad * groups;
+  const bool vec = (d & 3) == 0 && (reinterpret_cast<uintptr_t>(x) & 15) == 0;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = idx / dpad, c = idx - r * dpad;
-    const float v = (r < n && c < d) ? __ldg(x + r * d + c) : 0.f;
-    const __nv_bfloat16 h = __float2bfloat16_rn(v);
-    hi[idx] = h;
-    lo[idx] = __float2bfloat16_rn(v - __bfloat162float(h));
+    const int64_t r = idx / groups, c = (idx - r * groups) * 8;
+    float v[8];
+    if (r < n && vec && c + 8 <= d) {
+      const float4 a = __ldg(reinterpret_cast<const float4*>(x + r * d + c));
+      const float4 b = __ldg(reinterpret_cast<const float4*>(x + r * d + c + 4));
+      v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+      v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+    } else {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = (r < n && c + u < d) ? __ldg(x + r * d + c + u) : 0.f;
+    }
+    __align__(16) __nv_bfloat16 h[8], l[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      h[u] = __float2bfloat16_rn(v[u]);
+      l[u] = __float2bfloat16_rn(v[u] - __bfloat162float(h[u]));
+    }
+    *reinterpret_cast<uint4*>(hi + r * dpad + c) = *reinterpret_cast<const uint4*>(h);
+    *reinterpret_cast<uint4*>(lo + r * dpad + c) = *reinterpret_cast<const uint4*>(l);
   }
 }
 
@@ -68,11 +87,13 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b
 
 __device__ __forceinline__ void mma_commit(uint32_t bar) { commit(bar); }
 
+// Tile (blockIdx.y, blockIdx.x) of the output, or with sym (x1 == x2) tile t = blockIdx.x of
+// the lower triangle of the tile grid, written at (i, j) and mirrored at (j, i).
 __global__ void __launch_bounds__(128, 1)
     gram_tc_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
                    const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
                    float* __restrict__ out, int64_t n1, int64_t n2, int64_t dpad, float inv_d,
-                   int* err) {
+                   int sym, int* err) {
   extern __shared__ uint8_t smem_raw[];
   // 1024-byte alignment for the swizzled tiles
   uint8_t* smem = reinterpret_cast<uint8_t*>(
@@ -82,7 +103,18 @@ __global__ void __launch_bounds__(128, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
+  int64_t ti = blockIdx.y, tj = blockIdx.x;
+  if (sym) {  // t = i (i + 1) / 2 + j, j <= i
+    const int64_t t = blockIdx.x;
+    ti = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (ti * (ti + 1) / 2 > t) --ti;
+    while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+    tj = t - ti * (ti + 1) / 2;
+  }
+  const int64_t m0 = ti * BM, n0 = tj * BN;
+  // sym: an off-diagonal tile is written at (i, j) and transposed at (j, i); a diagonal
+  // tile's upper half is its lower half transposed, so the whole output is symmetric
+  const bool diag = sym && ti == tj;
   const int nk = (int)(dpad / BK);
 
   if (threadIdx.x == 0) {
@@ -168,7 +200,10 @@ __global__ void __launch_bounds__(128, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ready) {
     const int rq = warp & 3;
-    const int64_t row = m0 + rq * 32 + lane;
+    // every stage has been consumed by the finished MMAs: the ring's shared memory stages
+    // each warp's 32 x 32 block for row-coalesced stores
+    float* stg = reinterpret_cast<float*>(smem) + warp * 32 * 33;
+    const int64_t rbase = m0 + rq * 32;
 #pragma unroll 1
     for (int c0 = 0; c0 < BN; c0 += 32) {
       uint32_t v[32];
@@ -185,12 +220,24 @@ __global__ void __launch_bounds__(128, 1)
             "=r"(v[31])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (row < n1) {
-        float* o = out + row * n2 + n0 + c0;
+      // lane = row rbase + lane of the tile, v[j] = column n0 + c0 + j
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
-          if (n0 + c0 + j < n2) o[j] = __uint_as_float(v[j]) * inv_d;
+      for (int j = 0; j < 32; ++j) stg[lane * 33 + j] = __uint_as_float(v[j]) * inv_d;
+      __syncwarp();
+      const int64_t col = n0 + c0 + lane;
+      if (col < n2) {
+#pragma unroll 4
+        for (int rr = 0; rr < 32; ++rr)
+          if (rbase + rr < n1 && (!diag || col <= rbase + rr))
+            out[(rbase + rr) * n2 + col] = stg[rr * 33 + lane];
       }
+      if (sym && rbase + lane < n1) {  // out[n0 + c0 + j][rbase + lane] = tile[lane][j]
+#pragma unroll 4
+        for (int j = 0; j < 32; ++j)
+          if (n0 + c0 + j < n1 && (!diag || n0 + c0 + j < rbase + lane))
+            out[(n0 + c0 + j) * n2 + rbase + lane] = stg[lane * 33 + j];
+      }
+      __syncwarp();
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -246,10 +293,18 @@ int gram_tc(cudaStream_t s, const float* x1, const float* x2, int64_t n1, int64_
   __nv_bfloat16* b_hi = a_lo + p1 * dpad;
   __nv_bfloat16* b_lo = b_hi + p2 * dpad;
   if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return check_launch("ntg_gram memset");
+  // x1 == x2: one split, the lower triangle of tiles, mirrored (the result exactly symmetric)
+  const bool sym = x1 == x2 && n1 == n2;
   auto grid = [](int64_t n) { return (unsigned)std::min<int64_t>(ceil_div(n, 256), 152 * 32); };
-  split_bf16_kernel<<<grid(p1 * dpad), 256, 0, s>>>(x1, n1, d, p1, dpad, a_hi, a_lo);
-  split_bf16_kernel<<<grid(p2 * dpad), 256, 0, s>>>(x2, n2, d, p2, dpad, b_hi, b_lo);
-  note_launch(2);
+  split_bf16_kernel<<<grid(p1 * dpad / 8), 256, 0, s>>>(x1, n1, d, p1, dpad, a_hi, a_lo);
+  note_launch();
+  if (!sym) {
+    split_bf16_kernel<<<grid(p2 * dpad / 8), 256, 0, s>>>(x2, n2, d, p2, dpad, b_hi, b_lo);
+    note_launch();
+  } else {
+    b_hi = a_hi;
+    b_lo = a_lo;
+  }
   CUtensorMap m[4];
   int rc;
   if ((rc = make_map(&m[0], a_hi, p1, dpad)) || (rc = make_map(&m[1], a_lo, p1, dpad)) ||
@@ -263,9 +318,10 @@ int gram_tc(cudaStream_t s, const float* x1, const float* x2, int64_t n1, int64_
   });
   if (attr_err != cudaSuccess)
     return fail(NTG_ERR_CUDA, std::string("ntg_gram: ") + cudaGetErrorString(attr_err));
-  dim3 g((unsigned)(p2 / BN), (unsigned)(p1 / BM));
+  const int64_t nb1 = p1 / BM;
+  dim3 g = sym ? dim3((unsigned)(nb1 * (nb1 + 1) / 2), 1) : dim3((unsigned)(p2 / BN), (unsigned)nb1);
   gram_tc_kernel<<<g, 128, SMEM_BYTES, s>>>(m[0], m[1], m[2], m[3], out, n1, n2, dpad,
-                                            1.f / (float)d, err);
+                                            1.f / (float)d, sym ? 1 : 0, err);
   note_launch();
   return check_launch("ntg_gram (tcgen05)");
 }

@@ -41,3 +41,21 @@ def test_fcn_mixed_precision_vs_oracle(nt):
     want = o.serial(*lay(o))(x[:128], x[128:], ('nngp', 'ntk'))
     for g, w in zip(got, want):
         assert np.max(np.abs(g.cpu().numpy() - w) / np.abs(w)) < 1e-4
+
+
+@pytest.mark.parametrize('n,d', [(128, 64), (300, 99), (1000, 3072), (129, 784)])
+def test_tc_gram_symmetric_inputs(nt, n, d):
+    """x1 is x2: the lower triangle of tiles, each off-diagonal tile mirrored. The result is
+    exactly symmetric, within the mixed-precision bound of float64 and no less accurate than
+    the general path on two copies of x (d = 99: rows not 16-byte aligned, the split's scalar
+    path). On the diagonal every partial sum is positive, so the tensor cores' FP32
+    accumulation error grows with d there (about 2e-5 at d = 3072) in both paths."""
+    from nt_gb300 import _ops as O
+    rng = np.random.default_rng(n + d)
+    x = rng.standard_normal((n, d)).astype(np.float32)
+    t = torch.from_numpy(x).cuda()
+    got = O.gram(t, t, 1).cpu().numpy()
+    assert np.array_equal(got, got.T)
+    assert cs_err(got, x, x) < 1e-4
+    other = O.gram(t, t.clone(), 1).cpu().numpy()
+    assert cs_err(got, x, x) <= cs_err(other, x, x) + 1e-7
