@@ -25,7 +25,6 @@ constexpr int BM = 128, BN = 128, BK = 64;
 constexpr int STAGES = 3;
 constexpr int TILE_BYTES = BM * BK * 2;       // one operand tile: 16 KB
 constexpr int STAGE_BYTES = 4 * TILE_BYTES;   // A_hi, A_lo, B_hi, B_lo
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr uint32_t TMEM_COLS = 128;
 constexpr uint64_t WAIT_LIMIT = 1ull << 20;   // about a second of polling
 
@@ -87,174 +86,207 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b
 
 __device__ __forceinline__ void mma_commit(uint32_t bar) { commit(bar); }
 
-// Tile (blockIdx.y, blockIdx.x) of the output, or with sym (x1 == x2) tile t = blockIdx.x of
-// the lower triangle of the tile grid, written at (i, j) and mirrored at (j, i).
-__global__ void __launch_bounds__(128, 1)
-    gram_tc_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
-                   const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
-                   float* __restrict__ out, int64_t n1, int64_t n2, int64_t dpad, float inv_d,
-                   int sym, int* err) {
-  extern __shared__ uint8_t smem_raw[];
-  // 1024-byte alignment for the swizzled tiles
-  uint8_t* smem = reinterpret_cast<uint8_t*>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
-  // bars[0..S): full, bars[S..2S): empty, bars[2S]: accumulator ready
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+constexpr int kThreads = 192;            // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr uint32_t TMEM_ALLOC = 2 * TMEM_COLS;  // two accumulators
+constexpr int STG_FLOATS = 4 * 32 * 33;  // each epilogue warp's 32 x 32 staging block
+constexpr int P_SMEM_BYTES = STAGES * STAGE_BYTES + STG_FLOATS * 4 + 1024 + 256;
 
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int64_t ti = blockIdx.y, tj = blockIdx.x;
-  if (sym) {  // t = i (i + 1) / 2 + j, j <= i
-    const int64_t t = blockIdx.x;
+// Output tile t of the schedule: with sym (x1 == x2) t enumerates the tiles (i, j <= i) of
+// the lower triangle row by row, else the nbn-wide grid row by row.
+__device__ __forceinline__ void tile_of(int64_t t, int sym, int64_t nbn, int64_t& ti,
+                                        int64_t& tj) {
+  if (sym) {  // t = i (i + 1) / 2 + j
     ti = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
     while (ti * (ti + 1) / 2 > t) --ti;
     while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
     tj = t - ti * (ti + 1) / 2;
+  } else {
+    ti = t / nbn;
+    tj = t - ti * nbn;
   }
-  const int64_t m0 = ti * BM, n0 = tj * BN;
-  // sym: an off-diagonal tile is written at (i, j) and transposed at (j, i); a diagonal
-  // tile's upper half is its lower half transposed, so the whole output is symmetric
-  const bool diag = sym && ti == tj;
+}
+
+// Persistent: CTA c computes the tiles c, c + gridDim.x, ... of the schedule. The TMA
+// producer and the MMA issuer run through the tiles' K chunks in one continuous ring; the
+// MMAs of a tile go to one of two TMEM accumulators while the four epilogue warps drain
+// the other (tcgen05.ld -> shared-memory staging -> row-coalesced stores), so that a tile's
+// epilogue overlaps the next tile's MMAs. With sym each off-diagonal tile is also written
+// transposed at (j, i), and a diagonal tile's upper half is its lower half transposed.
+__global__ void __launch_bounds__(kThreads, 1)
+    gram_tc_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
+                   const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
+                   float* __restrict__ out, int64_t n1, int64_t n2, int64_t dpad, float inv_d,
+                   int sym, int64_t ntiles, int64_t nbn, int* err) {
+  extern __shared__ uint8_t smem_raw[];
+  // 1024-byte alignment for the swizzled tiles
+  uint8_t* smem = reinterpret_cast<uint8_t*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  float* stg_all = reinterpret_cast<float*>(smem + STAGES * STAGE_BYTES);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(stg_all + STG_FLOATS);
+  // bars[0..S) full, [S..2S) empty, 2S + b: accumulator b full, 2S + 2 + b: accumulator b
+  // drained, 2S + 4: all MMAs retired
+  uint64_t* tfull = bars + 2 * STAGES;
+  uint64_t* tempty = bars + 2 * STAGES + 2;
+  uint64_t* drain = bars + 2 * STAGES + 4;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
+  __shared__ int s_fail;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nk = (int)(dpad / BK);
 
   if (threadIdx.x == 0) {
+    s_fail = 0;
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(smem_u32(&bars[s]), 1);
       mbar_init(smem_u32(&bars[STAGES + s]), 1);
     }
-    mbar_init(smem_u32(&bars[2 * STAGES]), 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&tfull[b]), 1);
+      mbar_init(smem_u32(&tempty[b]), 4);  // one arrival per epilogue warp
+    }
+    mbar_init(smem_u32(drain), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(TMEM_COLS));
+                 "r"(TMEM_ALLOC));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  tc::fence_before();
   __syncthreads();
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  tc::fence_after();
   const uint32_t tmem = *tmem_slot;
-  bool ok = true;
-  __shared__ int s_fail;
-  if (threadIdx.x == 0) s_fail = 0;
-  __syncthreads();
-  int issued = 0;  // TMA stages issued by the producer thread
+  int64_t issued = 0;  // K chunks whose TMA loads the producer issued
 
-  if (warp == 0 && lane == 0) {
-    // TMA producer
-    for (int kc = 0; kc < nk && ok; ++kc) {
-      const int s = kc % STAGES;
-      if (kc >= STAGES) ok = mbar_wait(smem_u32(&bars[STAGES + s]), ((kc / STAGES) - 1) & 1);
-      if (!ok) break;
-      const uint32_t full = smem_u32(&bars[s]);
-      uint8_t* st = smem + s * STAGE_BYTES;
-      mbar_expect_tx(full, STAGE_BYTES);
-      const int32_t x = kc * BK;
-      tma_load_2d(smem_u32(st), &ta_hi, full, x, (int32_t)m0);
-      tma_load_2d(smem_u32(st + TILE_BYTES), &ta_lo, full, x, (int32_t)m0);
-      tma_load_2d(smem_u32(st + 2 * TILE_BYTES), &tb_hi, full, x, (int32_t)n0);
-      tma_load_2d(smem_u32(st + 3 * TILE_BYTES), &tb_lo, full, x, (int32_t)n0);
-      issued = kc + 1;
-    }
-    if (!ok) {
-      atomicExch(err, 1);
-      atomicExch(&g_gram_error, NTG_ERR_WAIT_TIMEOUT);
-      s_fail = 1;
-    }
-  } else if (warp == 1 && lane == 0) {
-    // MMA issuer
-    for (int kc = 0; kc < nk && ok; ++kc) {
-      const int s = kc % STAGES;
-      ok = mbar_wait(smem_u32(&bars[s]), (kc / STAGES) & 1);
-      if (!ok) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
-      const uint32_t a_hi = st, a_lo = st + TILE_BYTES, b_hi = st + 2 * TILE_BYTES,
-                     b_lo = st + 3 * TILE_BYTES;
-#pragma unroll
-      for (int kk = 0; kk < BK / 16; ++kk) {
-        const uint32_t off = kk * 32;  // 16 bf16 along K
-        mma_bf16(tmem, smem_desc(a_hi + off), smem_desc(b_hi + off), (kc | kk) ? 1u : 0u);
-        mma_bf16(tmem, smem_desc(a_hi + off), smem_desc(b_lo + off), 1u);
-        mma_bf16(tmem, smem_desc(a_lo + off), smem_desc(b_hi + off), 1u);
+  if (warp == 0) {
+    if (lane == 0) {  // TMA producer
+      bool ok = true;
+      int64_t g = 0;
+      for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        int64_t ti, tj;
+        tile_of(t, sym, nbn, ti, tj);
+        for (int kc = 0; kc < nk; ++kc, ++g) {
+          const int s = (int)(g % STAGES);
+          if (g >= STAGES && !(ok = mbar_wait(smem_u32(&bars[STAGES + s]),
+                                              (uint32_t)(((g / STAGES) - 1) & 1))))
+            break;
+          const uint32_t full = smem_u32(&bars[s]);
+          uint8_t* st = smem + s * STAGE_BYTES;
+          mbar_expect_tx(full, STAGE_BYTES);
+          const int32_t x = kc * BK;
+          tma_load_2d(smem_u32(st), &ta_hi, full, x, (int32_t)(ti * BM));
+          tma_load_2d(smem_u32(st + TILE_BYTES), &ta_lo, full, x, (int32_t)(ti * BM));
+          tma_load_2d(smem_u32(st + 2 * TILE_BYTES), &tb_hi, full, x, (int32_t)(tj * BN));
+          tma_load_2d(smem_u32(st + 3 * TILE_BYTES), &tb_lo, full, x, (int32_t)(tj * BN));
+          issued = g + 1;
+        }
       }
-      mma_commit(smem_u32(&bars[STAGES + s]));  // frees the stage once these MMAs finish
+      if (!ok) {
+        atomicExch(err, 1);
+        atomicExch(&g_gram_error, NTG_ERR_WAIT_TIMEOUT);
+        s_fail = 1;
+      }
     }
-    mma_commit(smem_u32(&bars[2 * STAGES]));  // accumulator complete (or all issued MMAs)
-    if (!ok) {
-      atomicExch(err, 2);
-      atomicExch(&g_gram_error, NTG_ERR_WAIT_TIMEOUT);
-      s_fail = 1;
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      bool ok = true;
+      int64_t g = 0;
+      int it = 0;
+      for (int64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++it) {
+        const int b = it & 1;
+        // the accumulator's previous tile has been drained (its first use passes at once)
+        if (!(ok = mbar_wait(smem_u32(&tempty[b]), (uint32_t)(((it >> 1) & 1) ^ 1)))) break;
+        tc::fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * TMEM_COLS);
+        for (int kc = 0; kc < nk; ++kc, ++g) {
+          const int s = (int)(g % STAGES);
+          if (!(ok = mbar_wait(smem_u32(&bars[s]), (uint32_t)((g / STAGES) & 1)))) break;
+          tc::fence_after();
+          const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
+          const uint32_t a_hi = st, a_lo = st + TILE_BYTES, b_hi = st + 2 * TILE_BYTES,
+                         b_lo = st + 3 * TILE_BYTES;
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; ++kk) {
+            const uint32_t off = kk * 32;  // 16 bf16 along K
+            mma_bf16(acc, smem_desc(a_hi + off), smem_desc(b_hi + off), (kc | kk) ? 1u : 0u);
+            mma_bf16(acc, smem_desc(a_hi + off), smem_desc(b_lo + off), 1u);
+            mma_bf16(acc, smem_desc(a_lo + off), smem_desc(b_hi + off), 1u);
+          }
+          mma_commit(smem_u32(&bars[STAGES + s]));  // frees the stage once these MMAs finish
+        }
+        if (!ok) break;
+        mma_commit(smem_u32(&tfull[b]));  // the tile's accumulator is complete
+      }
+      mma_commit(smem_u32(drain));  // every MMA issued, retired before TMEM is freed
+      if (!ok) {
+        atomicExch(err, 2);
+        atomicExch(&g_gram_error, NTG_ERR_WAIT_TIMEOUT);
+        s_fail = 1;
+      }
     }
-  }
-  __syncwarp();
-
-  // Epilogue: warp w drains TMEM lanes 32 (w % 4) .. + 31 (rows of the tile).
-  const bool ready = mbar_wait(smem_u32(&bars[2 * STAGES]), 0);
-  if (!ready && lane == 0) {
-    atomicExch(err, 3);
-    atomicExch(&g_gram_error, NTG_ERR_WAIT_TIMEOUT);
-    s_fail = 1;
-  }
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (ready) {
+  } else {  // epilogue: warp w drains TMEM lanes 32 (w % 4) .. + 31 (rows of the tile)
     const int rq = warp & 3;
-    // every stage has been consumed by the finished MMAs: the ring's shared memory stages
-    // each warp's 32 x 32 block for row-coalesced stores
-    float* stg = reinterpret_cast<float*>(smem) + warp * 32 * 33;
-    const int64_t rbase = m0 + rq * 32;
+    float* stg = stg_all + (warp - 2) * 32 * 33;
+    int it = 0;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
+      const int b = it & 1;
+      if (!mbar_wait(smem_u32(&tfull[b]), (uint32_t)((it >> 1) & 1))) {
+        if (lane == 0) {
+          atomicExch(err, 3);
+          atomicExch(&g_gram_error, NTG_ERR_WAIT_TIMEOUT);
+          s_fail = 1;
+        }
+        break;
+      }
+      tc::fence_after();
+      int64_t ti, tj;
+      tile_of(t, sym, nbn, ti, tj);
+      const int64_t m0 = ti * BM, n0 = tj * BN;
+      const bool diag = sym && ti == tj;
+      const int64_t rbase = m0 + rq * 32;
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 32) {
-      uint32_t v[32];
-      const uint32_t taddr = tmem + ((uint32_t)(rq * 32) << 16) + (uint32_t)c0;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-          "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
-          "%28, %29, %30, %31}, [%32];"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-            "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
-            "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]),
-            "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
-            "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]),
-            "=r"(v[31])
-          : "r"(taddr));
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      // lane = row rbase + lane of the tile, v[j] = column n0 + c0 + j
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t v[32];
+        tc::tmem_ld32(tmem + ((uint32_t)(rq * 32) << 16) + (uint32_t)(b * TMEM_COLS + c0), v);
+        // lane = row rbase + lane of the tile, v[j] = column n0 + c0 + j
 #pragma unroll
-      for (int j = 0; j < 32; ++j) stg[lane * 33 + j] = __uint_as_float(v[j]) * inv_d;
-      __syncwarp();
-      const int64_t col = n0 + c0 + lane;
-      if (col < n2) {
+        for (int j = 0; j < 32; ++j) stg[lane * 33 + j] = __uint_as_float(v[j]) * inv_d;
+        __syncwarp();
+        const int64_t col = n0 + c0 + lane;
+        if (col < n2) {
 #pragma unroll 4
-        for (int rr = 0; rr < 32; ++rr)
-          if (rbase + rr < n1 && (!diag || col <= rbase + rr))
-            out[(rbase + rr) * n2 + col] = stg[rr * 33 + lane];
-      }
-      if (sym && rbase + lane < n1) {  // out[n0 + c0 + j][rbase + lane] = tile[lane][j]
+          for (int rr = 0; rr < 32; ++rr)
+            if (rbase + rr < n1 && (!diag || col <= rbase + rr))
+              out[(rbase + rr) * n2 + col] = stg[rr * 33 + lane];
+        }
+        if (sym && rbase + lane < n1) {  // out[n0 + c0 + j][rbase + lane] = tile[lane][j]
 #pragma unroll 4
-        for (int j = 0; j < 32; ++j)
-          if (n0 + c0 + j < n1 && (!diag || n0 + c0 + j < rbase + lane))
-            out[(n0 + c0 + j) * n2 + rbase + lane] = stg[lane * 33 + j];
+          for (int j = 0; j < 32; ++j)
+            if (n0 + c0 + j < n1 && (!diag || n0 + c0 + j < rbase + lane))
+              out[(n0 + c0 + j) * n2 + rbase + lane] = stg[lane * 33 + j];
+        }
+        __syncwarp();
       }
+      tc::fence_before();
       __syncwarp();
+      if (lane == 0) tc::mbar_arrive(smem_u32(&tempty[b]));
     }
   }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (s_fail) {
-    // A wait ran out: let the TMA loads still in flight land (the last use of
-    // each stage; bounded) before the shared memory is released. The MMAs the
-    // issuer started are tracked by its final commit, waited on above.
-    if (warp == 0 && lane == 0)
-      for (int kc = issued > STAGES ? issued - STAGES : 0; kc < issued; ++kc)
-        mbar_wait(smem_u32(&bars[kc % STAGES]), (kc / STAGES) & 1);
-    if (!ready && warp == 1 && lane == 0) mbar_wait(smem_u32(&bars[2 * STAGES]), 0);
-    __syncthreads();
+  if (warp == 1 && lane == 0) mbar_wait(smem_u32(drain), 0);  // bounded
+  if (s_fail && warp == 0 && lane == 0) {
+    // a wait ran out: let the TMA loads still in flight land (the last use of each stage;
+    // bounded) before the shared memory is released
+    for (int64_t g = issued > STAGES ? issued - STAGES : 0; g < issued; ++g)
+      mbar_wait(smem_u32(&bars[g % STAGES]), (uint32_t)((g / STAGES) & 1));
   }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
   if (warp == 1) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(TMEM_COLS));
+                 "r"(TMEM_ALLOC));
   }
 }
 
@@ -312,16 +344,23 @@ int gram_tc(cudaStream_t s, const float* x1, const float* x2, int64_t n1, int64_
     return rc;
   static std::once_flag attr_once;
   static cudaError_t attr_err = cudaSuccess;
+  static int num_sms = 0;
   std::call_once(attr_once, [] {
     attr_err = cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    SMEM_BYTES);
+                                    P_SMEM_BYTES);
+    int dev = 0;
+    if (attr_err == cudaSuccess) attr_err = cudaGetDevice(&dev);
+    if (attr_err == cudaSuccess)
+      attr_err = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
   });
   if (attr_err != cudaSuccess)
     return fail(NTG_ERR_CUDA, std::string("ntg_gram: ") + cudaGetErrorString(attr_err));
-  const int64_t nb1 = p1 / BM;
-  dim3 g = sym ? dim3((unsigned)(nb1 * (nb1 + 1) / 2), 1) : dim3((unsigned)(p2 / BN), (unsigned)nb1);
-  gram_tc_kernel<<<g, 128, SMEM_BYTES, s>>>(m[0], m[1], m[2], m[3], out, n1, n2, dpad,
-                                            1.f / (float)d, sym ? 1 : 0, err);
+  const int64_t nb1 = p1 / BM, nbn = p2 / BN;
+  const int64_t ntiles = sym ? nb1 * (nb1 + 1) / 2 : nb1 * nbn;
+  const unsigned ctas = (unsigned)std::min<int64_t>(ntiles, num_sms > 0 ? num_sms : 148);
+  gram_tc_kernel<<<ctas, kThreads, P_SMEM_BYTES, s>>>(m[0], m[1], m[2], m[3], out, n1, n2, dpad,
+                                                      1.f / (float)d, sym ? 1 : 0, ntiles, nbn,
+                                                      err);
   note_launch();
   return check_launch("ntg_gram (tcgen05)");
 }
