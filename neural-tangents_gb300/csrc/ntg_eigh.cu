@@ -78,7 +78,6 @@ __global__ void __launch_bounds__(256)
   __shared__ float U[JP][JPS];
   __shared__ float cs[JP / 2][2];
   __shared__ int pq[JP / 2][2];
-  __shared__ int rotated;
   __shared__ float smax;
   int pa, pb;
   rr_pair(nblk, round, blockIdx.x, pa, pb);
@@ -95,8 +94,7 @@ __global__ void __launch_bounds__(256)
   // couplings below this are already zero at float32 resolution of the pair's matrix
   const float tiny = 1e-9f * smax;
   for (int sw = 0; sw < inner_sweeps; ++sw) {
-    if (tid == 0) rotated = 0;
-    __syncthreads();
+    int rotated = 0;  // this thread's rotations of the sweep (combined below)
     for (int r = 0; r < JP - 1; ++r) {
       if (tid < JP / 2) {
         int p, q;
@@ -148,7 +146,9 @@ __global__ void __launch_bounds__(256)
       }
       __syncthreads();
     }
-    if (!rotated) break;
+    // every thread's flag, combined at a barrier (no shared flag for thread 0 to reset
+    // while another warp still reads it)
+    if (!__syncthreads_or(rotated)) break;
   }
   float* u = Uout + (int64_t)blockIdx.x * JP * JP;
   for (int idx = tid; idx < JP * JP; idx += blockDim.x) u[idx] = U[idx / JP][idx % JP];
@@ -216,16 +216,14 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], b[v], acc[u][v]);
   }
-  const bool diag = blockIdx.x == blockIdx.y;
+  // the pair's own tile keeps what the inner sweeps left of its couplings (they need not
+  // have run to convergence): the outer sweeps and the off-diagonal norm see them
 #pragma unroll
   for (int u = 0; u < 4; ++u)
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const int r = 4 * ty + u, c = tx + 16 * v;
-      // the pair's own tile is diagonal up to rounding: keep the off-diagonal zero
-      const float val = (diag && r != c) ? 0.f : acc[u][v];
-      A[(int64_t)pair_index(ia, ib, r) * lda + pair_index(ja, jb, c)] = val;
-    }
+    for (int v = 0; v < 4; ++v)
+      A[(int64_t)pair_index(ia, ib, 4 * ty + u) * lda + pair_index(ja, jb, tx + 16 * v)] =
+          acc[u][v];
 }
 
 // V[rows, cols_j] <- V[rows, cols_j] U_j for 64 consecutive rows (blockIdx.y) and pair j.
@@ -550,7 +548,9 @@ extern "C" int ntg_eigh(void* stream, const float* A, int64_t n, double shift, f
   int sweeps = 0;
   for (int sw = 0; sw < max_sweeps; ++sw) {
     for (int r = 0; r < nblk - 1; ++r) {
-      jacobi_inner_kernel<<<npairs, 256, 0, s>>>(e.w, npad, nblk, r, 10, e.u, e.done);
+      // two inner sweeps per pair and round: the outer sweeps converge as fast, and an
+      // inner problem driven to convergence early on is undone by the next rounds
+      jacobi_inner_kernel<<<npairs, 256, 0, s>>>(e.w, npad, nblk, r, 2, e.u, e.done);
       jacobi_apply_kernel<<<dim3(npairs, npairs), 256, 0, s>>>(e.w, npad, nblk, r, e.u, e.done);
       jacobi_apply_v_kernel<<<dim3(npairs, (unsigned)(npad / JP)), 256, 0, s>>>(
           e.v, npad, nblk, r, e.u, e.done);
