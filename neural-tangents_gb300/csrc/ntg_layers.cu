@@ -24,49 +24,103 @@ __device__ __forceinline__ void pair_of(int64_t b, int64_t n2, int64_t& i1, int6
 }
 
 // ---------------------------------------------------------------------------
-// Flat Gram on CUDA cores: out[i, j] = sum_d x1[i, d] x2[j, d] / D.
-// 64x64 output tile per CTA, 16x16 threads, 4x4 outputs per thread.
+// Flat Gram on CUDA cores: out[i, j] = sum_d x1[i, d] x2[j, d] / D, every output
+// accumulated by fmaf in ascending d (the order of the per-sample variances, so that
+// the diagonal of x x^T equals them bit for bit). 128 x 128 output tile per CTA, 16 x 16
+// threads, 8 x 8 outputs per thread (rows 4 ty + u and 64 + 4 ty + u, columns likewise
+// in tx) read from shared memory as 16-byte words. SYM (x1 == x2): the tiles on or below
+// the diagonal only (blockIdx.x enumerates them row by row), each off-diagonal one also
+// stored transposed: fmaf(a, b, c) == fmaf(b, a, c), so the mirror is exactly the value
+// the tile (j, i) would hold.
 // ---------------------------------------------------------------------------
+template <bool SYM>
 __global__ void __launch_bounds__(256) gram_simt_kernel(const float* __restrict__ x1,
                                                         const float* __restrict__ x2,
                                                         int64_t n1, int64_t n2, int64_t d,
                                                         float inv_d, float* __restrict__ out) {
-  __shared__ float As[16][64 + 4];
-  __shared__ float Bs[16][64 + 4];
+  __shared__ __align__(16) float As[16][128 + 4];
+  __shared__ __align__(16) float Bs[16][128 + 4];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int64_t row0 = (int64_t)blockIdx.y * 64, col0 = (int64_t)blockIdx.x * 64;
-  float acc[4][4] = {};
+  int64_t ti = blockIdx.y, tj = blockIdx.x;
+  if (SYM) {  // t = i (i + 1) / 2 + j, j <= i
+    const int64_t t = blockIdx.x;
+    ti = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (ti * (ti + 1) / 2 > t) --ti;
+    while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+    tj = t - ti * (ti + 1) / 2;
+  }
+  const int64_t row0 = ti * 128, col0 = tj * 128;
+  float acc[8][8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u)
+#pragma unroll
+    for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
   for (int64_t k0 = 0; k0 < d; k0 += 16) {
-    for (int idx = threadIdx.x; idx < 16 * 64; idx += 256) {
-      int r = idx / 16, kk = idx % 16;
-      int64_t gi = row0 + r, gk = k0 + kk;
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int idx = threadIdx.x + 256 * e;
+      const int r = idx >> 4, kk = idx & 15;
+      const int64_t gk = k0 + kk;
+      const int64_t gi = row0 + r, gj = col0 + r;
       As[kk][r] = (gi < n1 && gk < d) ? __ldg(x1 + gi * d + gk) : 0.f;
-      int64_t gj = col0 + r;
       Bs[kk][r] = (gj < n2 && gk < d) ? __ldg(x2 + gj * d + gk) : 0.f;
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < 16; ++kk) {
-      float a[4], bb[4];
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[kk][4 * ty]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[kk][64 + 4 * ty]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[kk][4 * tx]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[kk][64 + 4 * tx]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        a[u] = As[kk][ty * 4 + u];
-        bb[u] = Bs[kk][tx * 4 + u];
-      }
+      for (int u = 0; u < 8; ++u)
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(a[u], bb[v], acc[u][v]);
+        for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(a[u], bb[v], acc[u][v]);
     }
     __syncthreads();
   }
+  const bool vec = (n2 & 3) == 0 && (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+  const bool mirror = SYM && ti != tj;
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < 8; ++u) {
+    const int64_t gi = row0 + (u < 4 ? 4 * ty + u : 64 + 4 * ty + u - 4);
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      int64_t gi = row0 + ty * 4 + u, gj = col0 + tx * 4 + v;
-      if (gi < n1 && gj < n2) out[gi * n2 + gj] = acc[u][v] * inv_d;
+    for (int h = 0; h < 2; ++h) {
+      const int64_t gj = col0 + 64 * h + 4 * tx;
+      if (gi >= n1) continue;
+      if (vec && gj + 3 < n2) {
+        *reinterpret_cast<float4*>(out + gi * n2 + gj) =
+            make_float4(acc[u][4 * h] * inv_d, acc[u][4 * h + 1] * inv_d,
+                        acc[u][4 * h + 2] * inv_d, acc[u][4 * h + 3] * inv_d);
+      } else {
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+          if (gj + v < n2) out[gi * n2 + gj + v] = acc[u][4 * h + v] * inv_d;
+      }
     }
+  }
+  if (mirror) {  // out[gj][gi] = tile[gi][gj]
+#pragma unroll
+    for (int v = 0; v < 8; ++v) {
+      const int64_t gj = col0 + (v < 4 ? 4 * tx + v : 64 + 4 * tx + v - 4);
+      if (gj >= n1) continue;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int64_t gi = row0 + 64 * h + 4 * ty;
+        if (vec && gi + 3 < n1) {
+          *reinterpret_cast<float4*>(out + gj * n2 + gi) =
+              make_float4(acc[4 * h][v] * inv_d, acc[4 * h + 1][v] * inv_d,
+                          acc[4 * h + 2][v] * inv_d, acc[4 * h + 3][v] * inv_d);
+        } else {
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (gi + u < n1) out[gj * n2 + gi + u] = acc[4 * h + u][v] * inv_d;
+        }
+      }
+    }
+  }
 }
 
 // C[M, N] = A[M, K] B[K, N] (+ C_in when accumulate): 64x64 tiles, 4x4 per thread.
@@ -1704,9 +1758,16 @@ extern "C" int ntg_gram(void* stream, const float* x1, const float* x2, int64_t 
     return gram_tc(as_stream(stream), x1, x2, n1, n2, d, nngp, workspace, workspace_bytes);
   }
   NTG_REQUIRE(precision == 0, "ntg_gram: precision must be 0 or 1");
-  NTG_REQUIRE(ceil_div(n1, 64) <= 65535, "ntg_gram: n1 too large");
-  dim3 grid((unsigned)ceil_div(n2, 64), (unsigned)ceil_div(n1, 64));
-  gram_simt_kernel<<<grid, 256, 0, as_stream(stream)>>>(x1, x2, n1, n2, d, 1.f / (float)d, nngp);
+  NTG_REQUIRE(ceil_div(n1, 128) <= 65535, "ntg_gram: n1 too large");
+  const int64_t nb1 = ceil_div(n1, 128);
+  if (x1 == x2 && n1 == n2) {  // the lower triangle of tiles, mirrored
+    gram_simt_kernel<true><<<(unsigned)(nb1 * (nb1 + 1) / 2), 256, 0, as_stream(stream)>>>(
+        x1, x2, n1, n2, d, 1.f / (float)d, nngp);
+  } else {
+    dim3 grid((unsigned)ceil_div(n2, 128), (unsigned)nb1);
+    gram_simt_kernel<false><<<grid, 256, 0, as_stream(stream)>>>(x1, x2, n1, n2, d,
+                                                                 1.f / (float)d, nngp);
+  }
   note_launch();
   return check_launch("ntg_gram");
 }

@@ -59,3 +59,19 @@ def test_tc_gram_symmetric_inputs(nt, n, d):
     assert cs_err(got, x, x) < 1e-4
     other = O.gram(t, t.clone(), 1).cpu().numpy()
     assert cs_err(got, x, x) <= cs_err(other, x, x) + 1e-7
+
+
+@pytest.mark.parametrize('n,d', [(128, 64), (300, 99), (1000, 3072), (130, 784)])
+def test_fp32_gram_symmetric_inputs_bit_identical(nt, n, d):
+    """The FP32 Gram (precision 0) for x1 is x2 computes the lower triangle of tiles and
+    mirrors it: bit for bit the general path's result (every entry a fmaf chain in ascending
+    d, fmaf commutative in its product), and within float32 accuracy of float64 (the
+    diagonal's sums of squares carry the sequential sum's rounding, ~2.5e-6 at d = 3072)."""
+    from nt_gb300 import _ops as O
+    rng = np.random.default_rng(n * d)
+    x = rng.standard_normal((n, d)).astype(np.float32)
+    t = torch.from_numpy(x).cuda()
+    got = O.gram(t, t, 0).cpu().numpy()
+    assert np.array_equal(got, got.T)
+    assert np.array_equal(got, O.gram(t, t.clone(), 0).cpu().numpy())
+    assert cs_err(got, x, x) < 1e-5
