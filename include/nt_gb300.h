@@ -103,12 +103,16 @@ int32_t ntg_tune_get(int32_t knob);
 
 /* ---- input kernels (requirements.py:518-638, 641-830) ---------------- */
 /* Flat inputs x1 [N1, D], x2 [N2, D] -> nngp [N1, N2] = x1 x2^T / D
- * (requirements.py:542-564). precision 0: FP32 on CUDA cores (workspace
- * unused, may be NULL); 1: x = hi + lo split into BF16, hi1 hi2^T + hi1 lo2^T
- * + lo1 hi2^T on the tcgen05 tensor cores with FP32 accumulation, fed by TMA;
- * needs ntg_gram_workspace_bytes(n1, n2, d) bytes of workspace, whose first
- * int32 is set non-zero if a bounded pipeline wait ran out (read it back to
- * check). */
+ * (requirements.py:542-564). precision 0: FP32 on CUDA cores, every entry an
+ * fmaf chain in ascending D (workspace unused, may be NULL); 1: x = hi + lo
+ * split into BF16, hi1 hi2^T + hi1 lo2^T + lo1 hi2^T on the tcgen05 tensor
+ * cores with FP32 accumulation, fed by TMA (a persistent kernel, one CTA per
+ * SM); needs ntg_gram_workspace_bytes(n1, n2, d) bytes of workspace, whose
+ * first int32 is set non-zero if a bounded pipeline wait ran out (read it
+ * back, or ntg_device_status). When x1 == x2 (the same pointer) and n1 == n2
+ * both precisions compute the tiles on or below the diagonal only and store
+ * each also transposed: the output is exactly symmetric (for precision 0 bit
+ * for bit what two distinct copies of x would give). */
 int ntg_gram(void* stream, const float* x1, const float* x2, int64_t n1, int64_t n2,
              int64_t d, float* nngp, int32_t precision, void* workspace, size_t workspace_bytes);
 size_t ntg_gram_workspace_bytes(int64_t n1, int64_t n2, int64_t d);
