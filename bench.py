@@ -609,6 +609,36 @@ def nll_timing(torch, nt, dev):
 
         ms = _timed(torch, run)
         out[prec] = {'ms': round(ms, 2), 'grad': [float(w.grad), float(b.grad)]}
+        if prec == 'fp32':
+            # central differences in W_std and b_std, steps h and 2h, Richardson-extrapolated,
+            # of the NLL evaluated in FP64 from the same kernel, factorisation and refined
+            # solve (the forward returns it rounded to float32); h = 1e-2: the float32 kernel's
+            # rounding moves this NLL by about n cond(A) u, which a 1e-3 step would resolve
+            # only to ~1e-3 of b_std's gradient
+            def nll_at(wv, bv):
+                with torch.no_grad():
+                    kf2 = stax.serial(stax.Dense(512, wv, bv), stax.Relu(), stax.Dense(512, wv, bv),
+                                      stax.Relu(), stax.Dense(512, wv, bv), stax.Relu(),
+                                      stax.Dense(1, wv, bv))[2]
+                    solver = predict.CholeskySolver(kf2(x, None, 'nngp'), 1e-4, False)
+                    _, a64 = solver.solve(y, want_x64=True, residual=False)
+                    n, m = y.shape
+                    return (0.5 * float((y.double() * a64).sum()) +
+                            0.5 * m * float(solver.logdet()[0]) +
+                            0.5 * n * m * math.log(2 * math.pi))
+            fd = []
+            for which in (0, 1):
+                base = [1.5, 0.1]
+
+                def central(h):
+                    hi, lo = list(base), list(base)
+                    hi[which] += h
+                    lo[which] -= h
+                    return (nll_at(*hi) - nll_at(*lo)) / (2 * h)
+                fd.append((4 * central(1e-2) - central(2e-2)) / 3)
+            out[prec]['fd_grad'] = fd
+            out[prec]['grad_rel_diff_vs_fd'] = max(
+                abs(g - f) / abs(f) for g, f in zip(out[prec]['grad'], fd))
     return out
 
 
