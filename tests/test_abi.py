@@ -90,3 +90,37 @@ def test_argument_checks_before_any_launch(lib):
     rc = lib.ntg_chol_solve(None, fake, fake, fake, i64(4), fake, i64(2), fake, 17, None,
                             ctypes.c_size_t(0), None)
     assert rc == 1 and b'refinement' in lib.ntg_last_error()
+
+
+def test_tensor_core_solver_entries_check_arguments(lib):
+    """The tensor-core Cholesky, its solve, the double-float product and the eigensolver reject
+    bad sizes, pointers and workspaces with an error code and message before any launch."""
+    lib.ntg_last_error.restype = ctypes.c_char_p
+    i64, sz = ctypes.c_int64, ctypes.c_size_t
+    fake = ctypes.c_void_p(256)
+    for fn in ('ntg_gemm_df_workspace_bytes', 'ntg_chol_factor_tc_workspace_bytes',
+               'ntg_chol_solve_tc_workspace_bytes', 'ntg_eigh_workspace_bytes'):
+        getattr(lib, fn).restype = ctypes.c_size_t
+    size_max = ctypes.c_size_t(-1).value
+    assert lib.ntg_gemm_df_workspace_bytes(i64(0), i64(5), i64(3)) == size_max
+    assert lib.ntg_gemm_df_workspace_bytes(i64(7), i64(5), i64(3)) > 5 * 3 * 8
+    assert lib.ntg_chol_factor_tc_workspace_bytes(i64(100), i64(99)) == size_max  # ldl < n
+    # ntg_gemm_df: no output at all, then a workspace too small for rows x n x m
+    rc = lib.ntg_gemm_df(None, fake, i64(8), i64(4), i64(8), fake, i64(2), None, None, None,
+                         fake, sz(1 << 20))
+    assert rc == 1 and b'null pointer' in lib.ntg_last_error()
+    rc = lib.ntg_gemm_df(None, fake, i64(8), i64(4), i64(8), fake, i64(2), None, fake, None,
+                         fake, sz(16))
+    assert rc == 1 and b'workspace' in lib.ntg_last_error()
+    # ntg_chol_factor_tc: ldl not a multiple of 4
+    rc = lib.ntg_chol_factor_tc(None, fake, i64(10), ctypes.c_double(1e-4), 0, fake, i64(11),
+                                fake, fake, fake, sz(1 << 30))
+    assert rc == 1 and b'ldl' in lib.ntg_last_error()
+    # ntg_chol_solve_tc: refinement steps out of range
+    rc = lib.ntg_chol_solve_tc(None, fake, fake, i64(12), fake, fake, i64(10), fake, i64(2), fake,
+                               65, fake, sz(1 << 30), None, None, None)
+    assert rc == 1 and b'refinement' in lib.ntg_last_error()
+    # ntg_eigh: sweeps out of range
+    rc = lib.ntg_eigh(None, fake, i64(10), ctypes.c_double(0.), fake, fake, 0,
+                      ctypes.c_double(1e-5), 2, fake, sz(1 << 30), None)
+    assert rc == 1 and b'max_sweeps' in lib.ntg_last_error()
