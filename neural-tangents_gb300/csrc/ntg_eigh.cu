@@ -7,9 +7,10 @@
 // to the others, so they stay exact unit vectors) is split into 32-wide blocks.
 // A sweep pairs every two blocks once, in the round-robin order of a tournament
 // (nb - 1 rounds of nb / 2 disjoint pairs). In a round:
-//   jacobi_inner_kernel   one CTA per pair diagonalises the 64 x 64 matrix of its
-//                         two blocks by cyclic parallel Jacobi in shared memory
-//                         and writes the accumulated rotation U (64 x 64);
+//   jacobi_inner_kernel   one CTA per pair runs up to two sweeps of cyclic parallel
+//                         Jacobi on the 64 x 64 matrix of its two blocks in shared
+//                         memory and writes the accumulated rotation U (64 x 64);
+//                         what couplings remain stay in A for the next sweeps;
 //   jacobi_apply_kernel   A <- U^T A U tile by tile (a 64 x 64 tile of A couples
 //                         two pairs and depends only on their rotations);
 //   jacobi_apply_v_kernel V <- V U.
@@ -66,10 +67,10 @@ __device__ __forceinline__ void sym_schur2(float app, float aqq, float apq, floa
   s = t * c;
 }
 
-// One CTA per pair of blocks: S = A[idx, idx] (64 x 64), diagonalised in place by cyclic
+// One CTA per pair of blocks: S = A[idx, idx] (64 x 64), rotated in place by cyclic
 // parallel Jacobi (32 disjoint rotations per round, 63 rounds per sweep) until a sweep
-// rotates nothing or `inner_sweeps` sweeps ran; U (64 x 64, row-major) accumulates the
-// rotations.
+// leaves no coupling above 1e-5 of its pivots or `inner_sweeps` sweeps ran; U (64 x 64,
+// row-major) accumulates the rotations.
 __global__ void __launch_bounds__(256)
     jacobi_inner_kernel(const float* __restrict__ A, int64_t lda, int nblk, int round,
                         int inner_sweeps, float* __restrict__ Uout, const int* done) {
