@@ -21,7 +21,15 @@ Prints one JSON line. `value` is device-timed throughput (inputs resident);
 `e2e` is the same metric through the public API from pinned host buffers
 with host<->device copies inside the timed region; `--impl reference` times
 the CPU restatement of the reference's kernel rules (oracle/nt_oracle.py,
-float32, one process per host core) on the same workload.
+float32, one process per host core) on the same workload. Beside them:
+`parity` (sampled entries of the timed job against the float64 oracle),
+`configs` (configurations 1, 3 and 5 at their stated sizes with their errors
+against float64; `--no-full-configs` skips them), `roofline` / `compute` of
+the fused kernel, the rooflines of the materialised stencil, the fused
+backward (`vjp_roofline`) and the tensor-core Gram (`gram_tc`), and `side`
+figures (Myrtle-10 block, Cholesky solve, NLL with its finite-difference
+check). The `--profile-*` modes run one small case of a kernel for ncu and
+exit.
 """
 from __future__ import annotations
 
