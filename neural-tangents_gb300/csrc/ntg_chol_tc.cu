@@ -995,6 +995,10 @@ struct SideStream {
   cudaStream_t hi = nullptr, trail = nullptr, side = nullptr;
   cudaEvent_t fork = nullptr, panel = nullptr, trail_done = nullptr;
   cudaEvent_t join[3] = {nullptr, nullptr, nullptr};
+  // held while one factorisation enqueues its work: the events are re-recorded per panel,
+  // and two host threads interleaving their records and waits would order each other's
+  // launches (a wait, once enqueued, is not affected by a later record)
+  std::mutex enqueue;
 };
 
 int side_stream(SideStream** out) {
@@ -1156,6 +1160,7 @@ extern "C" int ntg_chol_factor_tc(void* stream, const float* A, int64_t n, doubl
   SideStream* ss = nullptr;
   rc = side_stream(&ss);
   if (rc) return rc;
+  std::lock_guard<std::mutex> enqueue_lock(ss->enqueue);
   // L^-T by the forward block solve of L Y = I on the transposed side, Z = Y^T: per
   // block b, Z[:, b] <- Z[:, b] Linv_b^T, then Z[:, >b] -= Z[:, b] L[>b, b]^T, where only
   // the rows [0, r0 + nb) of Z[:, b] are non-zero (Z is upper triangular). Step b reads

@@ -109,3 +109,35 @@ def test_logdet_matches_float64(nt):
     want = np.linalg.slogdet(a)[1]
     # each pivot carries the float32 factor's rounding (cond ~ 1e3 here)
     assert abs(float(s.logdet().item()) - want) < 5e-5 * abs(want)
+
+
+def test_concurrent_factorisations_on_two_streams(nt):
+    """Two host threads, each on its own stream, factorise different matrices at once: the
+    library's per-device streams and events are taken by one factorisation at a time, so
+    each factor is that of its own matrix."""
+    import threading
+    from nt_gb300 import predict
+    ks = [_spd(700, 41 + i) for i in range(2)]
+    out, errs = [None, None], []
+
+    def work(i):
+        try:
+            st = torch.cuda.Stream()
+            with torch.cuda.stream(st):
+                for _ in range(3):
+                    s = predict.CholeskySolver(_t(ks[i]), 1e-3, False)
+                    out[i] = s.L.clone()
+            st.synchronize()
+        except Exception as e:  # reported below
+            errs.append(e)
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errs
+    for i in range(2):
+        a = ks[i].astype(np.float64)
+        a = a + 1e-3 * np.trace(a) / 700 * np.eye(700)
+        lf = out[i].cpu().numpy().astype(np.float64)
+        assert np.max(np.abs(lf @ lf.T - a)) / np.max(np.abs(a)) < 1e-5
