@@ -652,14 +652,15 @@ def nll_timing(torch, nt, dev):
 
 def gram_roofline(torch, O, dev):
     """tcgen05 split-BF16 Gram of the NLL configuration, X [4096, 3072]: X X^T / D, as the
-    kernel computes it for x1 is x2 (the 528 tiles on or below the diagonal, mirrored) and for
-    two distinct operands (all 1024 tiles). FP32-equivalent rate: 2 n^2 d over the call;
-    tensor rate: the three BF16 products of the tiles computed."""
+    kernel computes it for x1 is x2 (the 272 tiles of 128 x 256 that reach the diagonal or lie
+    below it, mirrored) and for two distinct operands (all 512 tiles). FP32-equivalent rate:
+    2 n^2 d over the call; tensor rate: the three BF16 products of the tiles computed."""
     x = torch.randn((4096, 3072), device=dev)
     y = x.clone()
     n, d, nb = 4096, 3072, 4096 // 128
     out = {'kernel': 'gram_tc_kernel (+ bf16 split)', 'shape': [n, n, d], 'unit': 'TFLOP/s'}
-    for name, other, tiles in (('symmetric', x, nb * (nb + 1) // 2), ('general', y, nb * nb)):
+    sym_tiles = (nb // 2) * (nb // 2 + 1) if nb % 2 == 0 else (nb // 2 + 1) ** 2
+    for name, other, tiles in (('symmetric', x, sym_tiles), ('general', y, nb * (n // 256))):
         ts = []
         for i in range(4):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -670,7 +671,7 @@ def gram_roofline(torch, O, dev):
             if i:
                 ts.append(a.elapsed_time(b))
         ms = statistics.median(ts)
-        issued = 3 * 2 * tiles * 128 * 128 * d
+        issued = 3 * 2 * tiles * 128 * 256 * d
         out[name] = {'ms': round(ms, 3),
                      'tflops_fp32_equivalent': round(2 * n * n * d / (ms / 1e3) / 1e12, 1),
                      'tensor_tflops_issued': round(issued / (ms / 1e3) / 1e12, 1)}

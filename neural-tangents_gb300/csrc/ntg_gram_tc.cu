@@ -21,11 +21,12 @@
 namespace ntg {
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64;
-constexpr int STAGES = 3;
-constexpr int TILE_BYTES = BM * BK * 2;       // one operand tile: 16 KB
-constexpr int STAGE_BYTES = 4 * TILE_BYTES;   // A_hi, A_lo, B_hi, B_lo
-constexpr uint32_t TMEM_COLS = 128;
+constexpr int BM = 128, BN = 256, BK = 64;
+constexpr int STAGES = 2;
+constexpr int A_BYTES = BM * BK * 2;              // an A operand tile: 16 KB
+constexpr int B_BYTES = BN * BK * 2;              // a B operand tile: 32 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * B_BYTES;  // A_hi, A_lo, B_hi, B_lo: 96 KB
+constexpr uint32_t TMEM_COLS = BN;
 constexpr uint64_t WAIT_LIMIT = 1ull << 20;   // about a second of polling
 
 __device__ int g_gram_error = 0;
@@ -91,15 +92,23 @@ constexpr uint32_t TMEM_ALLOC = 2 * TMEM_COLS;  // two accumulators
 constexpr int STG_FLOATS = 4 * 32 * 33;  // each epilogue warp's 32 x 32 staging block
 constexpr int P_SMEM_BYTES = STAGES * STAGE_BYTES + STG_FLOATS * 4 + 1024 + 256;
 
-// Output tile t of the schedule: with sym (x1 == x2) t enumerates the tiles (i, j <= i) of
-// the lower triangle row by row, else the nbn-wide grid row by row.
+// Output tile t of the schedule (128-row x 256-column tiles): with sym (x1 == x2) t
+// enumerates, row tile by row tile, the column tiles j <= i / 2 that reach the diagonal
+// or below it (row tile i has i / 2 + 1 of them: S(2a) = a (a + 1) and S(2a + 1) =
+// (a + 1)^2 tiles precede row tiles 2a and 2a + 1), else the nbn-wide grid row by row.
 __device__ __forceinline__ void tile_of(int64_t t, int sym, int64_t nbn, int64_t& ti,
                                         int64_t& tj) {
-  if (sym) {  // t = i (i + 1) / 2 + j
-    ti = (int64_t)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while (ti * (ti + 1) / 2 > t) --ti;
-    while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
-    tj = t - ti * (ti + 1) / 2;
+  if (sym) {
+    int64_t a = (int64_t)((sqrt(4.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (a * (a + 1) > t) --a;
+    while ((a + 1) * (a + 2) <= t) ++a;
+    if (t >= (a + 1) * (a + 1)) {
+      ti = 2 * a + 1;
+      tj = t - (a + 1) * (a + 1);
+    } else {
+      ti = 2 * a;
+      tj = t - a * (a + 1);
+    }
   } else {
     ti = t / nbn;
     tj = t - ti * nbn;
@@ -111,7 +120,8 @@ __device__ __forceinline__ void tile_of(int64_t t, int sym, int64_t nbn, int64_t
 // MMAs of a tile go to one of two TMEM accumulators while the four epilogue warps drain
 // the other (tcgen05.ld -> shared-memory staging -> row-coalesced stores), so that a tile's
 // epilogue overlaps the next tile's MMAs. With sym each off-diagonal tile is also written
-// transposed at (j, i), and a diagonal tile's upper half is its lower half transposed.
+// transposed: the entries on or below the diagonal are stored directly and those strictly
+// below it also at their mirrored position, so that the output is exactly symmetric.
 __global__ void __launch_bounds__(kThreads, 1)
     gram_tc_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
                    const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo,
@@ -176,9 +186,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           mbar_expect_tx(full, STAGE_BYTES);
           const int32_t x = kc * BK;
           tma_load_2d(smem_u32(st), &ta_hi, full, x, (int32_t)(ti * BM));
-          tma_load_2d(smem_u32(st + TILE_BYTES), &ta_lo, full, x, (int32_t)(ti * BM));
-          tma_load_2d(smem_u32(st + 2 * TILE_BYTES), &tb_hi, full, x, (int32_t)(tj * BN));
-          tma_load_2d(smem_u32(st + 3 * TILE_BYTES), &tb_lo, full, x, (int32_t)(tj * BN));
+          tma_load_2d(smem_u32(st + A_BYTES), &ta_lo, full, x, (int32_t)(ti * BM));
+          tma_load_2d(smem_u32(st + 2 * A_BYTES), &tb_hi, full, x, (int32_t)(tj * BN));
+          tma_load_2d(smem_u32(st + 2 * A_BYTES + B_BYTES), &tb_lo, full, x, (int32_t)(tj * BN));
           issued = g + 1;
         }
       }
@@ -204,8 +214,8 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (!(ok = mbar_wait(smem_u32(&bars[s]), (uint32_t)((g / STAGES) & 1)))) break;
           tc::fence_after();
           const uint32_t st = smem_u32(smem + s * STAGE_BYTES);
-          const uint32_t a_hi = st, a_lo = st + TILE_BYTES, b_hi = st + 2 * TILE_BYTES,
-                         b_lo = st + 3 * TILE_BYTES;
+          const uint32_t a_hi = st, a_lo = st + A_BYTES, b_hi = st + 2 * A_BYTES,
+                         b_lo = st + 2 * A_BYTES + B_BYTES;
 #pragma unroll
           for (int kk = 0; kk < BK / 16; ++kk) {
             const uint32_t off = kk * 32;  // 16 bf16 along K
@@ -243,7 +253,6 @@ __global__ void __launch_bounds__(kThreads, 1)
       int64_t ti, tj;
       tile_of(t, sym, nbn, ti, tj);
       const int64_t m0 = ti * BM, n0 = tj * BN;
-      const bool diag = sym && ti == tj;
       const int64_t rbase = m0 + rq * 32;
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 32) {
@@ -257,13 +266,13 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (col < n2) {
 #pragma unroll 4
           for (int rr = 0; rr < 32; ++rr)
-            if (rbase + rr < n1 && (!diag || col <= rbase + rr))
+            if (rbase + rr < n1 && (!sym || col <= rbase + rr))
               out[(rbase + rr) * n2 + col] = stg[rr * 33 + lane];
         }
         if (sym && rbase + lane < n1) {  // out[n0 + c0 + j][rbase + lane] = tile[lane][j]
 #pragma unroll 4
           for (int j = 0; j < 32; ++j)
-            if (n0 + c0 + j < n1 && (!diag || n0 + c0 + j < rbase + lane))
+            if (n0 + c0 + j < rbase + lane)  // strictly below the diagonal (and < n1)
               out[(n0 + c0 + j) * n2 + rbase + lane] = stg[lane * 33 + j];
         }
         __syncwarp();
@@ -290,9 +299,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
-int make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t dpad) {
-  return tc::make_map_2d(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, rows, dpad, dpad, BM, BK,
-                         "ntg_gram");
+int make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t dpad, int box_rows) {
+  return tc::make_map_2d(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, rows, dpad, dpad,
+                         box_rows, BK, "ntg_gram");
 }
 
 }  // namespace
@@ -339,8 +348,11 @@ int gram_tc(cudaStream_t s, const float* x1, const float* x2, int64_t n1, int64_
   }
   CUtensorMap m[4];
   int rc;
-  if ((rc = make_map(&m[0], a_hi, p1, dpad)) || (rc = make_map(&m[1], a_lo, p1, dpad)) ||
-      (rc = make_map(&m[2], b_hi, p2, dpad)) || (rc = make_map(&m[3], b_lo, p2, dpad)))
+  // B tiles are 256 rows: for sym the A buffers (rows padded to 128) serve as B, the rows
+  // beyond them read as zero
+  const int64_t brows = sym ? p1 : p2;
+  if ((rc = make_map(&m[0], a_hi, p1, dpad, BM)) || (rc = make_map(&m[1], a_lo, p1, dpad, BM)) ||
+      (rc = make_map(&m[2], b_hi, brows, dpad, BN)) || (rc = make_map(&m[3], b_lo, brows, dpad, BN)))
     return rc;
   static std::once_flag attr_once;
   static cudaError_t attr_err = cudaSuccess;
@@ -356,7 +368,9 @@ int gram_tc(cudaStream_t s, const float* x1, const float* x2, int64_t n1, int64_
   if (attr_err != cudaSuccess)
     return fail(NTG_ERR_CUDA, std::string("ntg_gram: ") + cudaGetErrorString(attr_err));
   const int64_t nb1 = p1 / BM, nbn = p2 / BN;
-  const int64_t ntiles = sym ? nb1 * (nb1 + 1) / 2 : nb1 * nbn;
+  // sym: S(nb1) tiles, S(2a) = a (a + 1), S(2a + 1) = (a + 1)^2
+  const int64_t ha = nb1 / 2;
+  const int64_t ntiles = sym ? ((nb1 & 1) ? (ha + 1) * (ha + 1) : ha * (ha + 1)) : nb1 * nbn;
   const unsigned ctas = (unsigned)std::min<int64_t>(ntiles, num_sms > 0 ? num_sms : 148);
   gram_tc_kernel<<<ctas, kThreads, P_SMEM_BYTES, s>>>(m[0], m[1], m[2], m[3], out, n1, n2, dpad,
                                                       1.f / (float)d, sym ? 1 : 0, ntiles, nbn,
