@@ -574,8 +574,9 @@ def symmetric_grid_timing(torch, nt, kf, xd, n=1000):
 
 def cholesky_timing(torch, O, dev, n=5000, m=10):
     """predict.gradient_descent_mse at t = None for n = 5000 training points and 10 one-hot
-    targets: FP32 Cholesky of K + 1e-4 tr(K)/n I, FP32 triangular solves, two FP64 refinement
-    steps, and the test prediction for 100 points. K is a synthetic SPD kernel (the Gram of
+    targets: FP32 Cholesky of K + 1e-4 tr(K)/n I on the tensor cores, the solve by the explicit
+    inverse factors refined by conjugate gradients with double-float products, and the test
+    prediction for 100 points (double-float product with the FP64 solution). K is a synthetic SPD kernel (the Gram of
     iid N(0,1) features of width 6144)."""
     from nt_gb300 import predict
     g = torch.Generator(device='cpu').manual_seed(2)

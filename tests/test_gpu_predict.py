@@ -1,4 +1,5 @@
-"""GPU parity of predict.gradient_descent_mse (Cholesky + FP64 refinement)."""
+"""GPU parity of predict.gradient_descent_mse, gp_inference and the ensemble (tensor-core Cholesky with
+double-float refinement at t = None / inf, the library's eigensolver at finite t)."""
 import math
 
 import numpy as np
