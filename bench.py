@@ -472,6 +472,7 @@ def vjp_roofline(torch, dev, pooled, n1=16, n2=32, reps=4):
         torch.cuda.synchronize()
         if i:
             ts.append(a.elapsed_time(b))
+    L.check_device('ntg_conv_act_bwd')  # a timed call whose ring wait ran out would raise here
     ms = statistics.median(ts)
     entries = B * A ** 4
     per_entry = 8 + (0.5 if pooled else 8) + 8

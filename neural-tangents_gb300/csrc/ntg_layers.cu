@@ -1144,6 +1144,7 @@ __global__ void __launch_bounds__(kThreads)
 // gvar1 / gvar2 ([n, 32, 32]) with one atomic per (plane, position).
 // ---------------------------------------------------------------------------
 constexpr int kVjpRing = 3;
+constexpr int kVjpWarps = kThreads / 32;  // each keeps its own variance-cotangent partials
 
 template <bool POOLED>
 __host__ __device__ constexpr int skew_vjp_slot_floats() {
@@ -1153,7 +1154,7 @@ __host__ __device__ constexpr int skew_vjp_slot_floats() {
 template <bool POOLED>
 __host__ __device__ constexpr size_t skew_vjp_smem_bytes() {
   return sizeof(float) * (kVjpRing * skew_vjp_slot_floats<POOLED>() + 4 * kSkewPlane +
-                          3 * 64 + 3 * 8 * 64) +
+                          3 * 64 + 3 * kVjpWarps * 64) +
          sizeof(uint64_t) * kVjpRing;
 }
 
@@ -1172,7 +1173,7 @@ __device__ __forceinline__ void skew_vjp_body(
   float* stage_t = stage_q + 2 * kSkewPlane;            // [2][plane]
   float* vrow = stage_t + 2 * kSkewPlane;               // [3][v1[32] | v2[32]]
   float* sg = vrow + 3 * 64;                            // [3][warp][g v1[32] | g v2[32]]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sg + 3 * 64);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sg + 3 * kVjpWarps * 64);  // after all of sg
   const int nlines = 2 * A - 1;
   const int64_t b = blockIdx.x / nlines;
   const int delta = (int)(blockIdx.x - b * nlines) - (A - 1);
@@ -1215,11 +1216,11 @@ __device__ __forceinline__ void skew_vjp_body(
   };
   // adds plane j's variance cotangents (the eight warps' partial sums) to gvar1 / gvar2
   auto flush = [&](int j) {
-    const float* s = sg + (j % 3) * (8 * 64);
+    const float* s = sg + (j % 3) * (kVjpWarps * 64);
     if (tid < 2 * kSkewC) {
       float v = 0.f;
 #pragma unroll
-      for (int wv = 0; wv < 8; ++wv) v += s[wv * 64 + tid];
+      for (int wv = 0; wv < kVjpWarps; ++wv) v += s[wv * 64 + tid];
       const int i = i_lo + j;
       if (tid < kSkewC) {
         if (gvar1 && v != 0.f) atomicAdd(gvar1 + (i1 * A + i) * kSkewC + tid, v);
@@ -1308,7 +1309,7 @@ __device__ __forceinline__ void skew_vjp_body(
     // this warp's partial sums of the plane's variance cotangents, written without atomics:
     // var1 at w (the warp's four row groups share w), var2 at w' = w + r, gathered so that
     // lane T holds target T (for element slot k it comes from the lane with 4a + b = T - k - r0)
-    float* s = sg + (p % 3) * (8 * 64) + (tid >> 5) * 64;
+    float* s = sg + (p % 3) * (kVjpWarps * 64) + (tid >> 5) * 64;
     float y = 0.f;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
