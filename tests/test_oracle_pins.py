@@ -370,3 +370,73 @@ def test_diagonal_spatial_is_the_diagonal_of_the_full_kernel(act):
     np.testing.assert_allclose(diag.ntk, pick2(full.ntk), rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose(diag.cov1, pick1(full.cov1), rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose(diag.cov2, pick1(full.cov2), rtol=1e-12, atol=1e-12)
+
+
+# ---------------------------------------------------------------------------
+# The same rules against a deterministic quadrature: the check of the reference's
+# ElementwiseNumericalTest (tests/stax/elementwise_test.py:480-538), which compares each
+# closed-form rule with its Gauss-Hermite rule (ElementwiseNumerical,
+# elementwise.py:1134-1247). For the smooth activations a 120-point tensor rule is
+# exact to ~1e-12 at these variances, so the closed forms are pinned far tighter than
+# by sampling.
+# ---------------------------------------------------------------------------
+def _gauss_hermite_2d(f, v1, v2, q, deg=120):
+    """E[f(u, v)] for (u, v) ~ N(0, [[v1, q], [q, v2]]): probabilists' Gauss-Hermite
+    nodes in each of two independent standard normals, u = a z1, v = b z1 + c z2."""
+    z, w = np.polynomial.hermite_e.hermegauss(deg)
+    w = w / math.sqrt(2 * math.pi)
+    a = math.sqrt(v1)
+    b = q / a
+    c = math.sqrt(max(v2 - b * b, 0.))
+    u = a * z[:, None] + 0. * z[None, :]
+    v = b * z[:, None] + c * z[None, :]
+    return float(np.sum(w[:, None] * w[None, :] * f(u, v)))
+
+
+def _smooth_cases():
+    from scipy.special import erf
+    erf_case = (o.Erf(), lambda x: erf(x), lambda x: 2 / math.sqrt(math.pi) * np.exp(-x * x))
+    return _phi_pairs() + [erf_case]
+
+
+@pytest.mark.parametrize('case', range(5))
+def test_dual_activations_match_gauss_hermite_quadrature(case):
+    """Second layer of Dense -> phi -> Dense -> phi: nngp, ntk and both per-sample
+    variances of the rule equal the quadrature of phi(u) phi(v) (and ntk_in E[phi'(u)
+    phi'(v)]) over the first three layers' kernel, as the reference's numerical test
+    composes them (depth 2, W_std 1, b_std 0.01 there; other scales here)."""
+    layer, phi, dphi = _smooth_cases()[case]
+    rng = np.random.default_rng(60 + case)
+    x1, x2 = rng.standard_normal((3, 7)), rng.standard_normal((2, 7))
+    body = [o.Dense(1, 1.2, 0.1), layer, o.Dense(1, 0.9, 0.2)]
+    kin = o.serial(*body)(x1, x2)
+    kout = o.serial(*body, layer)(x1, x2)
+    pp = lambda u, v: phi(u) * phi(v)
+    dd = lambda u, v: dphi(u) * dphi(v)
+    for i in range(3):
+        v1 = float(kin.cov1[i])
+        np.testing.assert_allclose(kout.cov1[i], _gauss_hermite_2d(pp, v1, v1, v1),
+                                   rtol=1e-10, atol=1e-13)
+        for j in range(2):
+            v2, q, t = float(kin.cov2[j]), float(kin.nngp[i, j]), float(kin.ntk[i, j])
+            np.testing.assert_allclose(kout.nngp[i, j], _gauss_hermite_2d(pp, v1, v2, q),
+                                       rtol=1e-10, atol=1e-13)
+            np.testing.assert_allclose(kout.ntk[i, j], t * _gauss_hermite_2d(dd, v1, v2, q),
+                                       rtol=1e-10, atol=1e-13)
+    for j in range(2):
+        v2 = float(kin.cov2[j])
+        np.testing.assert_allclose(kout.cov2[j], _gauss_hermite_2d(pp, v2, v2, v2),
+                                   rtol=1e-10, atol=1e-13)
+
+
+def test_sin_closed_form():
+    """tests/stax/elementwise_test.py:428-437: Sin with its default a = b = 1, c = 0 has
+    nngp = (exp(-(v1 + v2) / 2 + q) - exp(-(v1 + v2) / 2 - q)) / 2."""
+    rng = np.random.default_rng(61)
+    x1, x2 = rng.standard_normal((4, 5)), rng.standard_normal((3, 5))
+    pre = o.serial(o.Dense(1, 1.1, 0.2))
+    kin = pre(x1, x2)
+    k = o.serial(o.Dense(1, 1.1, 0.2), o.Sin())(x1, x2)
+    s = -0.5 * (kin.cov1[:, None] + kin.cov2[None, :])
+    want = (np.exp(s + kin.nngp) - np.exp(s - kin.nngp)) / 2
+    np.testing.assert_allclose(k.nngp, want, rtol=1e-12)
