@@ -32,9 +32,12 @@ instead by the reference's own known-answer and identity tests, re-run here by
 (``tests/stax/elementwise_test.py:541-636``), ``serial(B, B) == B o B``
 (``tests/stax/stax_test.py:636-687``), batching equals the unbatched kernel
 (``tests/batching_test.py:139-360``) and Cholesky ``t=None`` equals eigh
-``t=inf`` (``tests/predict_test.py:396-428``), plus closed forms derived from
-the mathematics (the arc-cosine kernel of Cho & Saul, the arcsine kernel of
-Williams) and brute-force finite-width Monte Carlo checks. The golden fixtures
+``t=inf`` (``tests/predict_test.py:396-428``), the zero / multi / infinite time
+predictions and the agreement with a trained (here exactly linear) network
+(``tests/predict_test.py:108-160, 192-273``), the dual activations against
+Gauss-Hermite quadrature (``tests/stax/elementwise_test.py:480-538``), plus
+closed forms derived from the mathematics (the arc-cosine kernel of Cho & Saul,
+the arcsine kernel of Williams) and brute-force finite-width Monte Carlo checks. The golden fixtures
 under ``tests/golden/`` are outputs of this restatement, regenerated by
 ``tests/golden/make_golden.py``.
 """
@@ -859,7 +862,8 @@ def _add_diagonal_regularizer(A, diag_reg, absolute):
 
 def gradient_descent_mse(k_train_train, y_train, learning_rate=1., diag_reg=0.,
                          diag_reg_absolute_scale=False):
-    """Infinite (t=None, Cholesky) and finite/infinite (eigh) time predictions.
+    """predict.py:71-278: infinite (t=None, Cholesky) and finite/infinite (eigh) time
+    predictions of gradient flow on the MSE loss.
 
     Restricted to a 2-D ``k_train_train`` and ``trace_axes=(-1,)``.
     """
@@ -881,18 +885,24 @@ def gradient_descent_mse(k_train_train, y_train, learning_rate=1., diag_reg=0.,
                 return fx_test_t
             return fx_train_t, fx_test_t
         evals, evecs = np.linalg.eigh(A)
+        # predict.py:197-229: t of any shape; the outputs are t.shape + the fx shape
         t = np.asarray(t, np.float64) * learning_rate
+        t_shape = t.shape
+        ts = t.reshape(-1, 1)
         rhs = -y if fx_train_0 is None else fx_train_0 - y
         # predict.py:1277-1294: expm1 / inv-expm1 spectral functions with
         # normalisation y_train.size and negative eigenvalues clipped to 0.
-        expm1 = np.expm1(-np.maximum(evals, 0.) * t / y.size)
-        inv = expm1 / np.abs(evals)
+        expm1 = np.expm1(-np.maximum(evals, 0.)[None, :] * ts / y.size)  # [T, n]
+        inv = expm1 / np.abs(evals)[None, :]
+        proj = evecs.T @ rhs
         out_train = out_test = None
         if fx_train_0 is not None:
-            out_train = fx_train_0 + evecs @ (expm1[:, None] * (evecs.T @ rhs))
+            d = np.einsum('ji,ti,ik->tjk', evecs, expm1, proj)
+            out_train = fx_train_0 + d.reshape(t_shape + d.shape[1:])
         if fx_test_0 is not None:
-            out_test = fx_test_0 + np.asarray(k_test_train, np.float64) @ (
-                evecs @ (inv[:, None] * (evecs.T @ rhs)))
+            d = np.einsum('ji,ti,ik->tjk', evecs, inv, proj)
+            d = np.einsum('mj,tjk->tmk', np.asarray(k_test_train, np.float64), d)
+            out_test = fx_test_0 + d.reshape(t_shape + d.shape[1:])
         if out_train is not None and out_test is not None:
             return out_train, out_test
         return out_test if out_train is None else out_train

@@ -440,3 +440,68 @@ def test_sin_closed_form():
     s = -0.5 * (kin.cov1[:, None] + kin.cov2[None, :])
     want = (np.exp(s + kin.nngp) - np.exp(s - kin.nngp)) / 2
     np.testing.assert_allclose(k.nngp, want, rtol=1e-12)
+
+
+# ---------------------------------------------------------------------------
+# gradient_descent_mse in time (tests/predict_test.py:108-160, 192-273)
+# ---------------------------------------------------------------------------
+def _linear_model(n=12, m=5, p=30, k=3, seed=70):
+    """A network that is its own linearisation: f(x) = phi(x) w with fixed features, so
+    its NTK is phi phi^T exactly and gradient flow on the MSE loss is a linear ODE."""
+    rng = np.random.default_rng(seed)
+    ph, pt = rng.standard_normal((n, p)), rng.standard_normal((m, p))
+    w0 = rng.standard_normal((p, k)) * 0.3
+    y = rng.standard_normal((n, k))
+    return ph, pt, w0, y
+
+
+def test_gd_mse_zero_multi_and_infinite_time():
+    """predict_test.py:108-160: t = 0 returns the initial outputs; an array of times equals
+    the stacked single-time predictions, shape t.shape + fx.shape; t = inf on the train set
+    returns y and equals the t = None (Cholesky) predictions."""
+    ph, pt, w0, y = _linear_model()
+    k_dd, k_td = ph @ ph.T, pt @ ph.T
+    f0, g0 = ph @ w0, pt @ w0
+    pred = o.gradient_descent_mse(k_dd, y, learning_rate=0.7)
+    a, b = pred(0., f0, g0, k_td)
+    np.testing.assert_allclose(a, f0, rtol=0, atol=1e-13)
+    np.testing.assert_allclose(b, g0, rtol=0, atol=1e-13)
+    np.testing.assert_allclose(pred(0., f0), f0, rtol=0, atol=1e-13)
+    ts = np.arange(6.).reshape(2, 1, 3) * 40.
+    a, b = pred(ts, f0, g0, k_td)
+    assert a.shape == ts.shape + f0.shape and b.shape == ts.shape + g0.shape
+    for idx in np.ndindex(ts.shape):
+        sa, sb = pred(ts[idx], f0, g0, k_td)
+        np.testing.assert_allclose(a[idx], sa, rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(b[idx], sb, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(pred(np.inf, f0), y, rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(pred(np.inf, f0), pred(None, f0, None, None), rtol=1e-10)
+    for u, v in zip(pred(np.inf, f0, g0, k_td), pred(None, f0, g0, k_td)):
+        np.testing.assert_allclose(u, v, rtol=1e-9, atol=1e-11)
+
+
+def test_gd_mse_equals_gradient_flow_of_a_linearised_network():
+    """predict_test.py:192-273 (testNTKGDPrediction, loss 'mse_analytic'): the analytic
+    predictions at time t equal the network trained by gradient descent for time t on
+    0.5 mean((f - y)^2). Here the network is exactly linear in its parameters, and its
+    gradient flow dw/dt = -lr phi^T (phi w - y) / y.size is integrated in parameter space
+    by the exponential of the augmented [[A, b], [0, 0]] matrix, independently of the
+    eigenbasis in function space that the predictor uses."""
+    import scipy.linalg as sla
+    ph, pt, w0, y = _linear_model()
+    lr, T = 0.7, 35.
+    n, k = y.shape
+    p = ph.shape[1]
+    A = -lr * ph.T @ ph / y.size
+    wT = np.empty_like(w0)
+    for c in range(k):
+        M = np.zeros((p + 1, p + 1))
+        M[:p, :p] = A
+        M[:p, p] = lr * ph.T @ y[:, c] / y.size
+        wT[:, c] = (sla.expm(T * M) @ np.append(w0[:, c], 1.))[:p]
+    pred = o.gradient_descent_mse(ph @ ph.T, y, learning_rate=lr)
+    ftr, fte = pred(T, ph @ w0, pt @ w0, pt @ ph.T)
+    np.testing.assert_allclose(ftr, ph @ wT, rtol=1e-9, atol=1e-11)
+    np.testing.assert_allclose(fte, pt @ wT, rtol=1e-9, atol=1e-11)
+    # and the trajectory moved: the initial outputs are far from the trained ones
+    assert np.abs(ftr - ph @ w0).max() > 0.1
