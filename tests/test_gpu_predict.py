@@ -123,6 +123,26 @@ def test_finite_time_matches_oracle(nt):
         np.testing.assert_allclose(g.cpu().numpy(), w, rtol=1e-4, atol=1e-6)
 
 
+def test_finite_time_array_of_times_matches_oracle(nt):
+    """predict_test.py:135-160 (_test_multi_step): t of shape (2, 1, 3) gives outputs of
+    shape t.shape + fx.shape, each slice the prediction at that time; against the float64
+    oracle, with nonzero initial outputs and held-out test inputs."""
+    rng = np.random.default_rng(8)
+    x, xt = rows(6, 40, 12), rows(9, 15, 12)
+    y = rng.standard_normal((40, 2))
+    f0, g0 = rng.standard_normal((40, 2)) * 0.3, rng.standard_normal((15, 2)) * 0.3
+    kf = nt.stax.serial(*fcn(nt.stax))[2]
+    kdd, ktd = kf(x, None, 'ntk'), kf(xt, x, 'ntk')
+    ts = np.arange(6.).reshape(2, 1, 3) * 0.8
+    got = nt.predict.gradient_descent_mse(kdd, y, learning_rate=1.5, diag_reg=1e-3)(
+        ts, f0, g0, ktd)
+    want = o.gradient_descent_mse(kdd.double().cpu().numpy(), y, learning_rate=1.5,
+                                  diag_reg=1e-3)(ts, f0, g0, ktd.double().cpu().numpy())
+    assert tuple(got[0].shape) == (2, 1, 3, 40, 2) and tuple(got[1].shape) == (2, 1, 3, 15, 2)
+    for g, w in zip(got, want):
+        np.testing.assert_allclose(g.cpu().numpy(), w, rtol=1e-4, atol=1e-6)
+
+
 def _leaves(x):
     if isinstance(x, tuple):
         return [a for v in x for a in _leaves(v)]
