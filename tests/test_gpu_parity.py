@@ -73,6 +73,68 @@ def test_fcn_erf_and_abrelu(nt):
         assert elem_rel_err(g, w) < RTOL
 
 
+
+@pytest.mark.parametrize('same_inputs', [True, False])
+@pytest.mark.parametrize('do_stabilize', [True, False])
+def test_abrelu_family_identities(nt, same_inputs, do_stabilize):
+    """tests/stax/elementwise_test.py:541-636 on the CUDA path: ABRelu(0, 1), (0, -1),
+    (-1, 0) and (1, 0) all give ReLU's kernels; ABRelu(a, a) is a times the identity;
+    LeakyRelu(a) is ABRelu(a, 1) and Abs is ABRelu(-1, 1); every kernel also against the
+    float64 oracle."""
+    rng = np.random.default_rng(1)
+    x1 = rng.standard_normal((3, 2))
+    x2 = None if same_inputs else rng.standard_normal((4, 2))
+    fc = lambda m: m.Dense(5, 1., 0.)
+
+    def k(layers_fn, a=x1, b=x2, get=('nngp', 'ntk')):
+        got, want = both(nt, layers_fn, a, b, get)
+        for g, w in zip(got, want):
+            assert rel_err(g, w) < RTOL
+        return got
+
+    relu = k(lambda m: [fc(m), m.Relu(do_stabilize)])
+    for a, b in [(0, 1), (0, -1), (-1, 0), (1, 0)]:
+        got = k(lambda m: [fc(m), m.ABRelu(a, b, do_stabilize)])
+        for g, w in zip(got, relu):
+            assert rel_err(g, w) < RTOL, (a, b)
+    for a in [-5, -1, -0.5, 0.5, 1, 5]:
+        kid = k(lambda m: [fc(m), m.Identity()], x1 * a, None if x2 is None else x2 * a,
+                ('nngp', 'ntk', 'cov1'))
+        kab = k(lambda m: [fc(m), m.ABRelu(a, a, do_stabilize)], get=('nngp', 'ntk', 'cov1'))
+        for g, w in zip(kab, kid):
+            assert rel_err(g, w) < RTOL, a
+    for a in [-2, -1, 0, 1, 2]:
+        kl = k(lambda m: [fc(m), m.LeakyRelu(a, do_stabilize)])
+        ka = k(lambda m: [fc(m), m.ABRelu(a, 1, do_stabilize)])
+        for g, w in zip(kl, ka):
+            assert np.array_equal(g, w), a
+    kabs = k(lambda m: [fc(m), m.Abs(do_stabilize)])
+    kab = k(lambda m: [fc(m), m.ABRelu(-1, 1, do_stabilize)])
+    for g, w in zip(kabs, kab):
+        assert np.array_equal(g, w)
+
+
+@pytest.mark.parametrize('avg_pool', [True, False])
+@pytest.mark.parametrize('same_inputs', [True, False])
+def test_serial_composition_through_a_kernel(nt, avg_pool, same_inputs):
+    """tests/stax/stax_test.py:636-687 on the CUDA path: serial(block, readout) equals the
+    readout's kernel_fn applied to the Kernel the block's kernel_fn returns (full spatial),
+    and the composed kernels match the float64 oracle."""
+    s = nt.stax
+    rng = np.random.default_rng(11)
+    x1 = rng.standard_normal((3, 5, 5, 3))
+    x2 = None if same_inputs else rng.standard_normal((4, 5, 5, 3))
+    block = lambda m: [m.Conv(1, (3, 3)), m.Relu()]
+    readout = lambda m: ([m.Conv(1, (3, 3)), m.GlobalAvgPool(), m.Dense(1)] if avg_pool
+                         else [m.Flatten(), m.Dense(1)])
+    composed = s.serial(*block(s), *readout(s))[2](x1, x2, ('nngp', 'ntk'))
+    bk = s.serial(*block(s))[2](x1, x2, diagonal_spatial=False)
+    via = s.serial(*readout(s))[2](bk, None, ('nngp', 'ntk'))
+    want = o.serial(*block(o), *readout(o))(x1, x2, ('nngp', 'ntk'))
+    for g, c, w in zip(via, composed, want):
+        assert rel_err(cpu(g), cpu(c)) < 1e-6
+        assert elem_rel_err(cpu(c), w) < RTOL
+
 CONV_CASES = [
     dict(filter_shape=(3, 3), padding='SAME'),
     dict(filter_shape=(3, 3), padding='VALID'),
