@@ -135,6 +135,43 @@ def test_serial_composition_through_a_kernel(nt, avg_pool, same_inputs):
         assert rel_err(cpu(g), cpu(c)) < 1e-6
         assert elem_rel_err(cpu(c), w) < RTOL
 
+
+@pytest.mark.parametrize('act', ['relu', 'relu_stab', 'erf'])
+def test_zero_inputs_give_finite_kernels(nt, act):
+    """tests/stax/stax_test.py:587-634 (sparse inputs): rows of zeros have zero variance
+    at every layer; the activation rules must return finite kernels (no 0/0) equal to the
+    float64 oracle's."""
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((4, 3))
+    x[:2] = 0.
+    for get in ('nngp', 'ntk'):
+        lay = lambda m: [m.Dense(1024), m.Relu(act == 'relu_stab') if act != 'erf' else m.Erf(),
+                         m.Dense(1 if get == 'ntk' else 1024)]
+        got = cpu(nt.stax.serial(*lay(nt.stax))[2](x, None, get))
+        want = o.serial(*lay(o))(x, None, get)
+        assert np.all(np.isfinite(got)), get
+        assert rel_err(got, want) < RTOL, get
+
+
+@pytest.mark.parametrize('normalize_edges', [False, True])
+def test_avg_pool_all_ones_kat(nt, normalize_edges):
+    """tests/stax/stax_test.py:494-551 on the CUDA path: AvgPool((2, 2), (1, 1), 'SAME') of
+    all-ones inputs. With normalize_edges every kernel entry is 1; without, the window
+    averages are out_unnorm = [[1, 1, 0.5], [0.5, 0.5, 0.25]] and the kernels their outer
+    products in the zipped layout."""
+    X1, X2 = np.ones((4, 2, 3, 2)), np.ones((3, 2, 3, 2))
+    k = nt.stax.AvgPool((2, 2), (1, 1), 'SAME', normalize_edges=normalize_edges)[2](X1, X2)
+    nngp, cov1, cov2 = cpu(k.nngp), cpu(k.cov1), cpu(k.cov2)
+    if normalize_edges:
+        want = np.ones((2, 2, 3, 3))
+    else:
+        out_unnorm = np.array([[1., 1., 0.5], [0.5, 0.5, 0.25]])
+        want = np.transpose(np.outer(out_unnorm, out_unnorm).reshape(2, 3, 2, 3), (0, 2, 1, 3))
+    assert nngp.shape == (4, 3, 2, 2, 3, 3) and cov1.shape == (4, 2, 2, 3, 3)
+    np.testing.assert_allclose(nngp, np.broadcast_to(want, nngp.shape), rtol=1e-6)
+    np.testing.assert_allclose(cov1, np.broadcast_to(want, cov1.shape), rtol=1e-6)
+    np.testing.assert_allclose(cov2, np.broadcast_to(want, cov2.shape), rtol=1e-6)
+
 CONV_CASES = [
     dict(filter_shape=(3, 3), padding='SAME'),
     dict(filter_shape=(3, 3), padding='VALID'),
