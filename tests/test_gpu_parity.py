@@ -172,6 +172,24 @@ def test_avg_pool_all_ones_kat(nt, normalize_edges):
     np.testing.assert_allclose(cov1, np.broadcast_to(want, cov1.shape), rtol=1e-6)
     np.testing.assert_allclose(cov2, np.broadcast_to(want, cov2.shape), rtol=1e-6)
 
+
+@pytest.mark.parametrize('same_inputs', [True, False])
+def test_flatten_at_the_bottom_equals_dense_on_flattened_inputs(nt, same_inputs):
+    """tests/stax/linear_test.py:53-100 on the CUDA path: serial(Flatten, Dense, Erf, Dense)
+    on images equals serial(Dense, Erf, Dense) on the flattened images, and the float64
+    oracle's kernels (relative to the largest entry: the Erf kernel changes sign, and
+    entries near zero carry no relative accuracy)."""
+    rng = np.random.default_rng(13)
+    x1 = rng.standard_normal((4, 4, 3, 2))
+    x2 = None if same_inputs else rng.standard_normal((2, 4, 3, 2))
+    flat = lambda x: None if x is None else x.reshape(x.shape[0], -1)
+    top = lambda m: [m.Dense(512, 1.7, 0.1), m.Erf(), m.Dense(512, 1.7, 0.1)]
+    k = nt.stax.serial(*top(nt.stax))[2](flat(x1), flat(x2), ('nngp', 'ntk'))
+    got, want = both(nt, lambda m: [m.Flatten()] + top(m), x1, x2, ('nngp', 'ntk'))
+    for g, a, w in zip(got, k, want):
+        assert rel_err(g, cpu(a)) < 1e-6
+        assert rel_err(g, w) < RTOL
+
 CONV_CASES = [
     dict(filter_shape=(3, 3), padding='SAME'),
     dict(filter_shape=(3, 3), padding='VALID'),

@@ -505,3 +505,18 @@ def test_gd_mse_equals_gradient_flow_of_a_linearised_network():
     np.testing.assert_allclose(fte, pt @ wT, rtol=1e-9, atol=1e-11)
     # and the trajectory moved: the initial outputs are far from the trained ones
     assert np.abs(ftr - ph @ w0).max() > 0.1
+
+
+@pytest.mark.parametrize('same_inputs', [True, False])
+def test_flatten_at_the_bottom_equals_dense_on_flattened_inputs(same_inputs):
+    """tests/stax/linear_test.py:53-100: serial(Flatten, Dense, Erf, Dense) on images equals
+    serial(Dense, Erf, Dense) on the flattened images, nngp and ntk."""
+    rng = np.random.default_rng(13)
+    x1 = rng.standard_normal((4, 4, 3, 2))
+    x2 = None if same_inputs else rng.standard_normal((2, 4, 3, 2))
+    flat = lambda x: None if x is None else x.reshape(x.shape[0], -1)
+    dense = lambda: o.Dense(512, 1.7, 0.1)
+    k = o.serial(dense(), o.Erf(), dense())(flat(x1), flat(x2), ('nngp', 'ntk'))
+    kb = o.serial(o.Flatten(), dense(), o.Erf(), dense())(x1, x2, ('nngp', 'ntk'))
+    for a, b in zip(kb, k):
+        np.testing.assert_allclose(a, b, rtol=1e-12)
