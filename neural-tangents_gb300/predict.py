@@ -301,12 +301,6 @@ def _as_tensor(v, like: torch.Tensor):
     return _dev(v)
 
 
-def _t64(v, like: torch.Tensor) -> torch.Tensor:
-    if isinstance(v, (int, float)):
-        return torch.tensor(float(v), dtype=torch.float64, device=like.device)
-    return _dev(v, torch.float64)
-
-
 class _NLL(torch.autograd.Function):
     """1/2 tr(Y^T A^{-1} Y) + m/2 log det A + n m/2 log 2 pi, A = K + lambda I."""
 
