@@ -112,11 +112,22 @@ def test_symmetric_call_gradient(nt):
         assert abs(g[idx] - want) < TOL * np.abs(g).max(), (idx, g[idx], want)
 
 
-def test_zero_input_gradient_is_finite(nt):
-    """tests/stax/elementwise_test.py:949-1036 (issue 123): zero inputs give finite gradients."""
-    x = torch.zeros((2, 4), device='cuda', requires_grad=True)
-    q = nt.stax.serial(nt.stax.Dense(3, 1., 0.), nt.stax.Relu(), nt.stax.Dense(1))[2](x, None, 'nngp')
-    q.sum().backward()
+@pytest.mark.parametrize('arch', ['dense', 'conv'])
+@pytest.mark.parametrize('get', ['nngp', 'ntk'])
+def test_zero_input_gradient_is_finite(nt, arch, get):
+    """tests/stax/elementwise_test.py:949-1036 (issue 123): zero inputs give a finite kernel
+    and a zero gradient, for a Dense + Relu network and for the issue's Conv(1, (3, 3)) +
+    Relu + Flatten on [1, 8, 8, 3] zeros (the full-spatial rules and their adjoints)."""
+    s = nt.stax
+    if arch == 'dense':
+        x = torch.zeros((2, 4), device='cuda', requires_grad=True)
+        kf = s.serial(s.Dense(3, 1., 0.), s.Relu(), s.Dense(1))[2]
+    else:
+        x = torch.zeros((1, 8, 8, 3), device='cuda', requires_grad=True)
+        kf = s.serial(s.Conv(1, (3, 3)), s.Relu(), s.Flatten())[2]
+    k = kf(x, x, get)
+    assert torch.isfinite(k).all()
+    k[0, 0].backward()
     assert torch.isfinite(x.grad).all()
     assert (x.grad == 0).all()
 
