@@ -520,3 +520,37 @@ def test_flatten_at_the_bottom_equals_dense_on_flattened_inputs(same_inputs):
     kb = o.serial(o.Flatten(), dense(), o.Erf(), dense())(x1, x2, ('nngp', 'ntk'))
     for a, b in zip(kb, k):
         np.testing.assert_allclose(a, b, rtol=1e-12)
+
+
+@pytest.mark.parametrize('with_t', [False, True])
+@pytest.mark.parametrize('with_x', [False, True])
+def test_ensemble_ntk_nngp_agreement(with_t, with_x):
+    """predict_test.py:493-584 (testNTK_NTKNNGPAgreement): an array of times equals the
+    stacked single-time predictions; the NTK mean equals the NNGP equations run on a kernel
+    function that always returns the NTK; and the NNGP covariance equals the NTK equations
+    run on one that always returns the NNGP (the reference checks this one roughly:
+    ~5e-7 here at diag_reg 1e-7)."""
+    rng = np.random.default_rng(80)
+    x_train, x_test = rng.standard_normal((8, 6)), rng.standard_normal((4, 6))
+    y = (rng.random((8, 2)) > 0.5).astype(np.float64)
+    kf = o.serial(o.Dense(64, W_std=1.2, b_std=0.05), o.Erf(), o.Dense(2, W_std=1.2, b_std=0.05))
+    reg = 1e-7
+    ts = np.logspace(-2, 8, 10).reshape(5, 2) if with_t else None
+    x = x_test if with_x else None
+    pred = o.gradient_descent_mse_ensemble(kf, x_train, y, diag_reg=reg)
+    ntk = np.asarray(pred(t=ts, get='ntk', x_test=x))
+    if ts is not None:
+        each = np.array([pred(t=t, get='ntk', x_test=x) for t in ts.ravel()])
+        np.testing.assert_allclose(each.reshape(ts.shape + ntk.shape[2:]), ntk, rtol=1e-12,
+                                   atol=1e-14)
+    always_ntk = lambda a, b, get: kf(a, b, 'ntk')
+    always_nngp = lambda a, b, get: kf(a, b, 'nngp')
+    ntk_nngp = o.gradient_descent_mse_ensemble(always_ntk, x_train, y, diag_reg=reg)(
+        t=ts, get='nngp', x_test=x)
+    np.testing.assert_allclose(np.asarray(ntk_nngp), ntk, rtol=1e-10, atol=1e-12)
+    nngp_cov = pred(t=ts, get='nngp', x_test=x, compute_cov=True).covariance
+    ntk_cov = o.gradient_descent_mse_ensemble(always_nngp, x_train, y, diag_reg=reg)(
+        t=ts, get='ntk', x_test=x, compute_cov=True).covariance
+    assert ntk_cov.shape == nngp_cov.shape
+    np.testing.assert_allclose(ntk_cov, nngp_cov, rtol=0,
+                               atol=5e-6 * max(np.abs(nngp_cov).max(), 1e-3))
