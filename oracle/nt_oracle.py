@@ -34,7 +34,9 @@ instead by the reference's own known-answer and identity tests, re-run here by
 (``tests/batching_test.py:139-360``) and Cholesky ``t=None`` equals eigh
 ``t=inf`` (``tests/predict_test.py:396-428``), the zero / multi / infinite time
 predictions and the agreement with a trained (here exactly linear) network
-(``tests/predict_test.py:108-160, 192-273``), the dual activations against
+(``tests/predict_test.py:108-160, 192-273``), the ensemble's NTK / NNGP agreement
+and its mean and covariance against an exactly linear network ensemble
+(``tests/predict_test.py:493-584, 622-686``), the dual activations against
 Gauss-Hermite quadrature (``tests/stax/elementwise_test.py:480-538``), plus
 closed forms derived from the mathematics (the arc-cosine kernel of Cho & Saul,
 the arcsine kernel of Williams) and brute-force finite-width Monte Carlo checks. The golden fixtures

@@ -554,3 +554,41 @@ def test_ensemble_ntk_nngp_agreement(with_t, with_x):
     assert ntk_cov.shape == nngp_cov.shape
     np.testing.assert_allclose(ntk_cov, nngp_cov, rtol=0,
                                atol=5e-6 * max(np.abs(nngp_cov).max(), 1e-3))
+
+
+@pytest.mark.parametrize('get', ['ntk', 'nngp'])
+def test_ensemble_mean_and_covariance_of_an_exactly_linear_network(get):
+    """predict_test.py:622-686 (testTrainedEnsemblePredCov) made exact: an ensemble of
+    networks f(x) = phi(x) w / sqrt(p), w0 ~ N(0, I), is its own linearisation with
+    NNGP = NTK = phi phi^T / p. Gradient flow on 0.5 mean((f - y)^2) maps w0 to
+    w(T) = E w0 + c (E, c from the exponential of the augmented parameter-space system), so
+    the ensemble of outputs at time T has mean phi c / sqrt(p) and covariance
+    phi E E^T phi^T / p, independently of the function-space equations of
+    gradient_descent_mse_ensemble, on the training and the test inputs."""
+    import scipy.linalg as sla
+    rng = np.random.default_rng(90)
+    n, m, p, k = 10, 4, 25, 2
+    ph, pt = rng.standard_normal((n, p)), rng.standard_normal((m, p))
+    y = rng.standard_normal((n, k))
+    feats = np.concatenate([ph, pt])
+
+    def kf(a, b, get):  # inputs are row indices into the feature table
+        fa = feats[np.asarray(a, int)]
+        fb = fa if b is None else feats[np.asarray(b, int)]
+        return fa @ fb.T / p
+
+    lr, T = 0.9, 40.
+    A = -lr * ph.T @ ph / (y.size * p)
+    E = sla.expm(T * A)
+    c = np.empty((p, k))
+    for j in range(k):
+        M = np.zeros((p + 1, p + 1))
+        M[:p, :p] = A
+        M[:p, p] = lr * ph.T @ y[:, j] / (y.size * math.sqrt(p))
+        c[:, j] = (sla.expm(T * M) @ np.append(np.zeros(p), 1.))[:p]
+    pred = o.gradient_descent_mse_ensemble(kf, np.arange(n), y, learning_rate=lr)
+    for x, f in ((np.arange(n, n + m), pt), (None, ph)):
+        r = pred(t=T, x_test=x, get=get, compute_cov=True)
+        np.testing.assert_allclose(r.mean, f @ c / math.sqrt(p), rtol=1e-10, atol=1e-13)
+        np.testing.assert_allclose(r.covariance, f @ E @ E.T @ f.T / p, rtol=1e-10, atol=1e-13)
+    assert np.abs(f @ c).max() > 0.1  # the ensemble has moved towards y
