@@ -30,8 +30,7 @@ instead by the reference's own known-answer and identity tests, re-run here by
 ``tests/test_oracle_pins.py``: the AvgPool all-ones closed form
 (``tests/stax/stax_test.py:494-539``), the ABRelu identities
 (``tests/stax/elementwise_test.py:541-636``), ``serial(B, B) == B o B``
-(``tests/stax/stax_test.py:636-687``), batching equals the unbatched kernel
-(``tests/batching_test.py:139-360``) and Cholesky ``t=None`` equals eigh
+(``tests/stax/stax_test.py:636-687``), Cholesky ``t=None`` equals eigh
 ``t=inf`` (``tests/predict_test.py:396-428``), the zero / multi / infinite time
 predictions and the agreement with a trained (here exactly linear) network
 (``tests/predict_test.py:108-160, 192-273``), the ensemble's NTK / NNGP agreement
@@ -39,8 +38,10 @@ and its mean and covariance against an exactly linear network ensemble
 (``tests/predict_test.py:493-584, 622-686``), the dual activations against
 Gauss-Hermite quadrature (``tests/stax/elementwise_test.py:480-538``), plus
 closed forms derived from the mathematics (the arc-cosine kernel of Cho & Saul,
-the arcsine kernel of Williams) and brute-force finite-width Monte Carlo checks. The golden fixtures
-under ``tests/golden/`` are outputs of this restatement, regenerated by
+the arcsine kernel of Williams) and brute-force finite-width Monte Carlo checks.
+(Batched equals unbatched, ``tests/batching_test.py:139-360``, is a property of
+the product's tiling and is checked on its GPU path, not here.) The golden
+fixtures under ``tests/golden/`` are outputs of this restatement, regenerated by
 ``tests/golden/make_golden.py``.
 """
 from __future__ import annotations
