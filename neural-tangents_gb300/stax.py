@@ -34,13 +34,21 @@ from .kernel import Kernel, analytic_kernel, from_physical, to_physical
 
 
 class Bool(enum.IntEnum):
+    """Three-valued requirement flag; `&` is the smaller of the two (requirements.py)."""
     NO = 0
     MAYBE = 1
     YES = 2
 
+    def __and__(self, other: 'Bool') -> 'Bool':
+        return Bool(min(int(self), int(other)))
+
+    __rand__ = __and__
+
 
 @dataclasses.dataclass(frozen=True)
 class Diagonal:
+    """Whether a layer accepts, and keeps, diagonal-only kernels: `a >> b` (and `b << a`) is
+    the requirement of b applied after a, `a & b` that of parallel branches."""
     input: Bool = Bool.YES
     output: Bool = Bool.NO
 
@@ -54,6 +62,15 @@ class Diagonal:
         else:
             inp = min(self.input, other.input)
         return Diagonal(input=inp, output=other.output)
+
+    def __lshift__(self, other: 'Diagonal') -> 'Diagonal':
+        return other >> self
+
+    def __and__(self, other: 'Diagonal') -> 'Diagonal':
+        return Diagonal(input=Bool(self.input) & Bool(other.input),
+                        output=Bool(self.output) & Bool(other.output))
+
+    __rand__ = __and__
 
     def __bool__(self) -> bool:
         return self.input == Bool.YES and self.output > Bool.NO

@@ -145,3 +145,19 @@ def test_no_cpu_fallback():
     kf = stax.serial(stax.Dense(4, 1.5, 0.05), stax.Relu(), stax.Dense(1))[2]
     with pytest.raises(RuntimeError, match='no CPU fallback'):
         kf(np.ones((2, 3), np.float32), None, 'nngp')
+
+
+def test_diagonal_requirement_algebra():
+    """tests/stax/requirements_test.py:116-132: composition of the diagonal requirements is
+    associative (`>>` and `<<` alike, and they agree); `&` is commutative, associative and
+    idempotent (requirements.py:432-515). For the product's `stax.Diagonal` and the oracle's."""
+    import itertools
+    from nt_gb300 import stax
+    from oracle import nt_oracle as o
+    for B, D in ((stax.Bool, stax.Diagonal), (o.Bool, o.Diagonal)):
+        vals = [D(i, j) for i, j in itertools.product(B, repeat=2)]
+        for a, b, c in itertools.product(vals, repeat=3):
+            assert (a >> b) >> c == a >> (b >> c)
+            if D is stax.Diagonal:
+                assert c << (b << a) == (c << b) << a == (a >> b) >> c
+                assert (a & b) == (b & a) and (a & b) & c == a & (b & c) and (a & a) == a
