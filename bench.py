@@ -22,6 +22,10 @@ Prints one JSON line. `value` is device-timed throughput (inputs resident);
 with host<->device copies inside the timed region; `--impl reference` times
 the CPU restatement of the reference's kernel rules (oracle/nt_oracle.py,
 float32, one process per host core) on the same workload. Beside them:
+`mixed` (the same job in the mixed form), `fwd_bwd` (a bounded sample of the
+kernel-ridge forward + backward, fp32 and mixed), `clocks` (SM clock and
+throttle reasons sampled during the timed steps), `gpu_launches` (this
+library's kernels launched in the timed steps),
 `parity` (sampled entries of the timed job against the float64 oracle),
 `configs` (configurations 1, 3 and 5 at their stated sizes with their errors
 against float64; `--no-full-configs` skips them), `roofline` / `compute` of
