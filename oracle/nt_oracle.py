@@ -24,9 +24,12 @@ What it restates (paths are inside the neural-tangents 0.6.6 project):
   ``:566-745`` ``gp_inference``, ``:753-1005`` ``gradient_descent_mse_ensemble``,
   ``:1180-1294`` eigen / Cholesky / expm1 helpers.
 
-Parity pinning. The reference ships no stored golden vectors and cannot be
-imported in this environment (it needs jax/jaxlib). This restatement is pinned
-instead by the reference's own known-answer and identity tests, re-run here by
+Parity pinning. The reference ships no stored golden vectors, and JAX is not
+installed here. Its own stax / predict code is run on a numpy stand-in for the
+JAX primitives it calls (``oracle/jax_stand_in``) by
+``tests/golden/make_reference_golden.py``; this restatement reproduces those
+outputs to 1e-12 (``tests/test_golden.py``). It is also pinned by the
+reference's own known-answer and identity tests, re-run here by
 ``tests/test_oracle_pins.py``: the AvgPool all-ones closed form
 (``tests/stax/stax_test.py:494-539``), the ABRelu identities
 (``tests/stax/elementwise_test.py:541-636``), ``serial(B, B) == B o B``

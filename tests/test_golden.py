@@ -34,3 +34,104 @@ def test_gpu_matches_fixture(nt, name):
         want = f[g]
         err = np.max(np.abs(got - want) / np.maximum(np.abs(want), 1e-30))
         assert err < 1e-5, (g, err)
+
+
+# ---------------------------------------------------------------------------
+# Outputs of the reference itself (neural-tangents 0.6.6's own stax / predict code, run here on
+# the numpy JAX stand-in by tests/golden/make_reference_golden.py): the oracle reproduces them.
+# ---------------------------------------------------------------------------
+_rspec = importlib.util.spec_from_file_location(
+    'make_reference_golden', os.path.join(HERE, 'make_reference_golden.py'))
+R = importlib.util.module_from_spec(_rspec)
+_rspec.loader.exec_module(R)
+
+REF_TOL = 1e-12  # relative to the largest entry; float64 on both sides
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize('name', sorted(G.CASES))
+def test_oracle_matches_reference_fixture(name):
+    layers, _, _, get = G.CASES[name]
+    f = np.load(os.path.join(HERE, f'{name}_reference.npz'))
+    out = o.serial(*layers(o))(f['x1'], f['x2'], get)
+    for g, v in zip(get, out):
+        assert _rel(v, f[g]) < REF_TOL, (g, _rel(v, f[g]))
+
+
+@pytest.mark.parametrize('case', sorted(R.KERNEL_CASES))
+def test_oracle_matches_reference_kernels(case):
+    """Activations, paddings, strides, pools, readouts, full- and diagonal-spatial kernels.
+    With x2 = None the NTK of a self pair (the diagonal) sits at correlation 1, where the
+    ReLU rule's derivative term (pi - theta) / 2 pi with theta = atan2(sqrt(q11 q22 - q12^2),
+    q12) turns the float64 rounding of q11 q22 - q12^2 (~1e-16) into theta ~ 1e-8: there the
+    two implementations agree to 1e-7, everywhere else to REF_TOL."""
+    layers, _, s2, get, kw = R.KERNEL_CASES[case]
+    x1, x2 = R.kernel_inputs(case)
+    ref = np.load(os.path.join(HERE, 'reference_cases.npz'))
+    out = o.serial(*layers(o))(x1, x2, get, **kw)
+    for g, v in zip(get, out):
+        want = ref[f'{case}/{g}']
+        assert np.shape(v) == want.shape, (g, np.shape(v), want.shape)
+        if s2 is None and g == 'ntk':
+            d = np.abs(np.asarray(v) - want) / np.abs(want).max()
+            assert np.diag(d).max() < 1e-7
+            assert (d - np.diag(np.diag(d))).max() < REF_TOL
+        else:
+            assert _rel(v, want) < REF_TOL, (g, _rel(v, want))
+
+
+def test_oracle_predictions_match_reference():
+    """gradient_descent_mse (t = None, inf, a scalar, a 2 x 2 array of times),
+    gradient_descent_mse_ensemble (t = None, a scalar, an array; means and covariances) and
+    gp_inference, from the same kernel matrices as the reference's run."""
+    P = np.load(os.path.join(HERE, 'reference_predictions.npz'))
+    xtr, xte, y, f0, g0 = R.prediction_inputs()
+    kdd = {g: P[f'kernels/dd_{g}'] for g in ('nngp', 'ntk')}
+    ktd = {g: P[f'kernels/td_{g}'] for g in ('nngp', 'ntk')}
+    ktt = P['kernels/tt_nngp']
+    kf = o.serial(*R._pred_net(o))
+    for g in ('nngp', 'ntk'):  # the kernels themselves (no self-pair NTK diagonal among them)
+        assert _rel(kf(xte, xtr, g), ktd[g]) < REF_TOL
+    assert _rel(kf(xtr, None, 'nngp'), kdd['nngp']) < REF_TOL
+    for g in ('nngp', 'ntk'):
+        pred = o.gradient_descent_mse(kdd[g], y, learning_rate=1.5, diag_reg=1e-3)
+        for tn, t in R.PRED_TIMES.items():
+            a, b = pred(t, f0, g0, ktd[g])
+            assert _rel(a, P[f'gd_{g}_{tn}/train']) < 1e-11, (g, tn)
+            assert _rel(b, P[f'gd_{g}_{tn}/test']) < 1e-11, (g, tn)
+
+    def saved_kernels(a, b, get):  # the reference's kernel matrices for the three calls
+        if b is None:
+            return kdd[get] if a is xtr else ktt
+        return ktd[get]
+
+    ens = o.gradient_descent_mse_ensemble(saved_kernels, xtr, y, learning_rate=1.5,
+                                          diag_reg=1e-3)
+    for tn, t in R.ENS_TIMES.items():
+        for g in ('nngp', 'ntk'):
+            r = ens(t=t, x_test=xte, get=g, compute_cov=True)
+            assert _rel(r.mean, P[f'ens_{g}_{tn}/mean']) < 1e-11, (g, tn)
+            assert _rel(r.covariance, P[f'ens_{g}_{tn}/cov']) < 1e-11, (g, tn)
+    gp = o.gp_inference(kdd, y, diag_reg=1e-3)(get=('nngp', 'ntk'), k_test_train=ktd,
+                                                 k_test_test=ktt)
+    for g, v in zip(('nngp', 'ntk'), gp):
+        assert _rel(v.mean, P[f'gp_{g}/mean']) < 1e-11
+        assert _rel(v.covariance, P[f'gp_{g}/cov']) < 1e-11
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize('name', sorted(G.CASES))
+def test_gpu_matches_reference_fixture(nt, name):
+    """The CUDA path against the reference's own outputs on the fixtures' inputs."""
+    layers, _, _, get = G.CASES[name]
+    f = np.load(os.path.join(HERE, f'{name}_reference.npz'))
+    out = nt.stax.serial(*layers(nt.stax))[2](f['x1'], f['x2'], get)
+    for g, v in zip(get, out):
+        got = v.detach().cpu().numpy()
+        want = f[g]
+        err = np.max(np.abs(got - want) / np.maximum(np.abs(want), 1e-30))
+        assert err < 1e-5, (g, err)
