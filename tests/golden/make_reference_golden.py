@@ -86,7 +86,22 @@ KERNEL_CASES = {
                    m.Conv(1, (3, 3), padding='SAME', W_std=math.sqrt(2.), b_std=0.), m.Relu(),
                    m.AvgPool((2, 2), (2, 2)), m.Flatten(), m.Dense(10, math.sqrt(2.), 0.)],
         (3, 16, 16, 3), None, ('nngp', 'ntk', 'cov1'), {}),
+    'myrtle10_32': (lambda m: _myrtle10(m), (2, 32, 32, 3), (1, 32, 32, 3),
+                    ('nngp', 'ntk', 'cov1', 'cov2'), {}),
 }
+
+
+def _myrtle10(m):
+    """Myrtle-10: Conv3x3 + Relu blocks [3, 3, 3] with AvgPool(2, 2) between them,
+    GlobalAvgPool, Dense (W_std = sqrt 2, b_std = 0)."""
+    conv = lambda: m.Conv(1, (3, 3), padding='SAME', W_std=math.sqrt(2.), b_std=0.)
+    layers = []
+    for i in range(3):
+        for _ in range(3):
+            layers += [conv(), m.Relu()]
+        if i < 2:
+            layers.append(m.AvgPool((2, 2), (2, 2)))
+    return layers + [m.GlobalAvgPool(), m.Dense(10, math.sqrt(2.), 0.)]
 
 
 def kernel_inputs(name):
