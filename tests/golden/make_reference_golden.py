@@ -10,6 +10,9 @@ Writes, in float64 (the reference under jax_enable_x64, inputs cast to float64):
                          oracle's fixtures): x1, x2 and the reference's nngp / ntk / cov1 / cov2;
   reference_cases.npz    KERNEL_CASES below (activations, paddings, strides, pools, readouts,
                          x2 = None, full- and diagonal-spatial kernels), keys '<case>/<name>';
+  reference_random.npz   nngp / ntk of the 40 seeded random networks of random_networks()
+                         (their specs and inputs are regenerated from the seed), keys
+                         'net<i>/<name>';
   reference_predictions.npz  gradient_descent_mse at t = None / inf / a scalar / an array of
                          times, gradient_descent_mse_ensemble and gp_inference (means and
                          covariances), keys '<case>/<name>', and the kernels they were
@@ -112,6 +115,61 @@ def kernel_inputs(name):
     return x1, x2
 
 
+_ACTS = [('Relu', {}), ('Erf', {'a': 0.7, 'b': 1.2, 'c': 0.1}), ('ABRelu', {'a': -0.4, 'b': 0.9}),
+         ('Gelu', {}), ('Sin', {'a': 1.2, 'b': 0.8, 'c': 0.3}), ('Cos', {'a': 0.9, 'b': 1.1, 'c': -0.2}),
+         ('Rbf', {'gamma': 0.5}), ('LeakyRelu', {'alpha': 0.1}), ('Abs', {}),
+         ('Relu', {'do_stabilize': True}), ('Identity', {})]
+
+
+def random_networks(count=40, seed=123):
+    """Seeded random networks as layer specs [(name, kwargs)] that both the reference's stax
+    and the oracle build alike: Dense stacks, or Conv stacks with filters of 1-3, strides,
+    SAME / VALID / CIRCULAR padding and Avg / Sum / circular pools, each with a random
+    activation and a Flatten / GlobalAvgPool / GlobalSumPool readout; x2 given or None."""
+    rs = np.random.default_rng(seed)
+    nets = []
+    for _ in range(count):
+        spec = []
+        if rs.random() < 0.3:
+            for _ in range(int(rs.integers(1, 4))):
+                spec.append(('Dense', {'out_dim': 4, 'W_std': float(rs.uniform(0.8, 1.6)),
+                                       'b_std': float(rs.uniform(0., 0.3))}))
+                spec.append(_ACTS[int(rs.integers(len(_ACTS)))])
+            shape = (int(rs.integers(5, 9)),)
+        else:
+            for _ in range(int(rs.integers(1, 3))):
+                spec.append(('Conv', {
+                    'out_chan': 1, 'filter_shape': (int(rs.integers(1, 4)), int(rs.integers(1, 4))),
+                    'strides': (int(rs.integers(1, 3)), 1) if rs.random() < 0.3 else (1, 1),
+                    'padding': ['SAME', 'VALID', 'CIRCULAR'][int(rs.integers(3))],
+                    'W_std': float(rs.uniform(0.8, 1.6)), 'b_std': float(rs.uniform(0., 0.3))}))
+                spec.append(_ACTS[int(rs.integers(len(_ACTS)))])
+                if rs.random() < 0.4:
+                    win = (int(rs.integers(1, 3)), int(rs.integers(1, 3)))
+                    kind = int(rs.integers(3))
+                    pad = ['SAME', 'VALID'][int(rs.integers(2))]
+                    if kind == 0:
+                        spec.append(('AvgPool', {'window_shape': win, 'strides': win, 'padding': pad,
+                                                 'normalize_edges': bool(rs.random() < 0.5)}))
+                    elif kind == 1:
+                        spec.append(('SumPool', {'window_shape': win, 'strides': (1, 1),
+                                                 'padding': pad}))
+                    else:
+                        spec.append(('AvgPool', {'window_shape': win, 'strides': (1, 1),
+                                                 'padding': 'CIRCULAR'}))
+            spec.append((['Flatten', 'GlobalAvgPool', 'GlobalSumPool'][int(rs.integers(3))], {}))
+            shape = (int(rs.integers(5, 9)), int(rs.integers(5, 9)), 2)
+        spec.append(('Dense', {'out_dim': 1, 'W_std': 1.2, 'b_std': 0.1}))
+        x1 = rs.standard_normal((2,) + shape)
+        x2 = rs.standard_normal((3,) + shape) if rs.random() < 0.7 else None
+        nets.append((spec, x1, x2))
+    return nets
+
+
+def build(m, spec):
+    return [getattr(m, name)(**kw) for name, kw in spec]
+
+
 def _pred_net(m):
     return [m.Dense(64, 1.3, 0.1), m.Erf(), m.Dense(64, 1.2, 0.05), m.Relu(), m.Dense(2, 1.2, 0.05)]
 
@@ -159,6 +217,14 @@ def main(path=DEFAULT_REFERENCE):
             arrays[f'{name}/{g}'] = np.asarray(v)
         print(name, [np.asarray(v).shape for v in out])
     np.savez_compressed(os.path.join(HERE, 'reference_cases.npz'), **arrays)
+
+    arrays = {}
+    for i, (spec, x1, x2) in enumerate(random_networks()):
+        q, t = stax.serial(*build(stax, spec))[2](x1, x2, ('nngp', 'ntk'))
+        arrays[f'net{i}/nngp'] = np.asarray(q)
+        arrays[f'net{i}/ntk'] = np.asarray(t)
+    np.savez_compressed(os.path.join(HERE, 'reference_random.npz'), **arrays)
+    print('random networks', len(arrays) // 2)
 
     xtr, xte, y, f0, g0 = prediction_inputs()
     kf = stax.serial(*_pred_net(stax))[2]

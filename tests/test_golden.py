@@ -84,6 +84,23 @@ def test_oracle_matches_reference_kernels(case):
             assert _rel(v, want) < REF_TOL, (g, _rel(v, want))
 
 
+def test_oracle_matches_reference_on_random_networks():
+    """Forty seeded random Dense / Conv networks (filters 1-3, strides, SAME / VALID /
+    CIRCULAR padding, Avg / Sum / circular pools, all eleven activations, three readouts,
+    x2 given or None): the oracle against the reference's outputs. Self-pair NTK entries of
+    x2 = None kernels to 1e-7 (see test_oracle_matches_reference_kernels)."""
+    ref = np.load(os.path.join(HERE, 'reference_random.npz'))
+    for i, (spec, x1, x2) in enumerate(R.random_networks()):
+        q, t = o.serial(*R.build(o, spec))(x1, x2, ('nngp', 'ntk'))
+        assert _rel(q, ref[f'net{i}/nngp']) < REF_TOL, (i, spec)
+        want = ref[f'net{i}/ntk']
+        d = np.abs(np.asarray(t) - want) / max(np.abs(want).max(), 1e-300)
+        if x2 is None:
+            assert np.diag(d).max() < 1e-7, (i, spec)
+            d = d - np.diag(np.diag(d))
+        assert d.max() < REF_TOL, (i, spec, d.max())
+
+
 def test_oracle_predictions_match_reference():
     """gradient_descent_mse (t = None, inf, a scalar, a 2 x 2 array of times),
     gradient_descent_mse_ensemble (t = None, a scalar, an array; means and covariances) and
