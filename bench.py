@@ -48,6 +48,9 @@ import time
 
 import numpy as np
 
+ORACLE_LABEL = ('float64 oracle (CPU restatement of the reference\'s rules; it reproduces '
+                'outputs of the reference\'s own code to 1e-12: tests/golden)')
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -904,7 +907,7 @@ def cpu_checks(checks, procs=None):
     for c in checks:
         if 'pairs' in c:
             want = np.array([v for v, name in zip(vals, owners) if name == c['name']])
-            res = {'entries': len(c['pairs']), 'reference': 'float64 oracle (CPU restatement)',
+            res = {'entries': len(c['pairs']), 'reference': ORACLE_LABEL,
                    'oracle_s': round(pair_s, 1)}
             for form, (gq, gt) in c['got'].items():
                 res[f'max_rel_err_{form}'] = max(_rel(gq, want[:, 0]), _rel(gt, want[:, 1]))
@@ -928,7 +931,7 @@ def cpu_checks(checks, procs=None):
             kts = kf(c['x2'], c['x1'], 'ntk')
             pred = o.gradient_descent_mse(ktt, c['y'], diag_reg=1e-4)
             g = c['got']
-            res = {'reference': 'float64 oracle (CPU restatement)',
+            res = {'reference': ORACLE_LABEL,
                    'max_rel_err_nngp': _rel(g['nngp'], q), 'max_rel_err_ntk': _rel(g['ntk'], t)}
             for name, t_ in (('t_none', None), ('t_inf', np.inf)):
                 want = pred(t_, 0., 0., kts)[1]
