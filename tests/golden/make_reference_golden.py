@@ -91,6 +91,18 @@ KERNEL_CASES = {
         (3, 16, 16, 3), None, ('nngp', 'ntk', 'cov1'), {}),
     'myrtle10_32': (lambda m: _myrtle10(m), (2, 32, 32, 3), (1, 32, 32, 3),
                     ('nngp', 'ntk', 'cov1', 'cov2'), {}),
+    'fc_standard_parameterization': (
+        lambda m: [m.Dense(8, W_std=1.3, b_std=0.1, parameterization='standard', s=(2, 3)),
+                   m.Relu(), m.Dense(8, W_std=1.2, b_std=0.2, parameterization='standard'),
+                   m.Erf(), m.Dense(1, W_std=1.1, b_std=0.05, parameterization='standard', s=(3, 1))],
+        (5, 7), (4, 7), ('nngp', 'ntk', 'cov1', 'cov2'), {}),
+    'conv_standard_parameterization': (
+        lambda m: [m.Conv(1, (3, 3), padding='SAME', W_std=1.3, b_std=0.1,
+                          parameterization='standard', s=(1, 2)), m.Relu(),
+                   m.Conv(1, (2, 2), padding='VALID', W_std=1.2, b_std=0.05,
+                          parameterization='standard', s=(2, 1)), m.Relu(),
+                   m.GlobalAvgPool(), m.Dense(1, 1.1, 0.05, parameterization='standard')],
+        (2, 6, 6, 3), (3, 6, 6, 3), ('nngp', 'ntk', 'cov1', 'cov2'), {}),
 }
 
 
