@@ -11,8 +11,9 @@ Writes, in float64 (the reference under jax_enable_x64, inputs cast to float64):
   reference_cases.npz    KERNEL_CASES below (activations, paddings, strides, pools, readouts,
                          x2 = None, full- and diagonal-spatial kernels), keys '<case>/<name>';
   reference_random.npz   nngp / ntk of the 40 seeded random networks of random_networks()
-                         (their specs and inputs are regenerated from the seed), keys
-                         'net<i>/<name>';
+                         (their specs and inputs are regenerated from the seed) and the
+                         diagonal_spatial requirement the reference derives for each
+                         (input, output as Bool values), keys 'net<i>/<name>';
   reference_predictions.npz  gradient_descent_mse at t = None / inf / a scalar / an array of
                          times, gradient_descent_mse_ensemble and gp_inference (means and
                          covariances), keys '<case>/<name>', and the kernels they were
@@ -232,9 +233,12 @@ def main(path=DEFAULT_REFERENCE):
 
     arrays = {}
     for i, (spec, x1, x2) in enumerate(random_networks()):
-        q, t = stax.serial(*build(stax, spec))[2](x1, x2, ('nngp', 'ntk'))
+        kf = stax.serial(*build(stax, spec))[2]
+        q, t = kf(x1, x2, ('nngp', 'ntk'))
         arrays[f'net{i}/nngp'] = np.asarray(q)
         arrays[f'net{i}/ntk'] = np.asarray(t)
+        req = kf.input_req['diagonal_spatial']
+        arrays[f'net{i}/diagonal_spatial_req'] = np.array([int(req.input), int(req.output)])
     np.savez_compressed(os.path.join(HERE, 'reference_random.npz'), **arrays)
     print('random networks', len(arrays) // 2)
 

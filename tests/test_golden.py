@@ -101,6 +101,18 @@ def test_oracle_matches_reference_on_random_networks():
         assert d.max() < REF_TOL, (i, spec, d.max())
 
 
+def test_product_requirements_match_reference():
+    """Host planning: for each random network the product's serial() derives the same
+    diagonal_spatial requirement (requirements.py:401-515 folded over the layers) as the
+    reference did, which decides the kernel layout every rule then runs on."""
+    from nt_gb300 import stax
+    ref = np.load(os.path.join(HERE, 'reference_random.npz'))
+    for i, (spec, _, _) in enumerate(R.random_networks()):
+        d = stax.serial(*R.build(stax, spec))[2].input_req['diagonal_spatial']
+        assert (int(d.input), int(d.output)) == tuple(ref[f'net{i}/diagonal_spatial_req']), \
+            (i, spec)
+
+
 def test_oracle_predictions_match_reference():
     """gradient_descent_mse (t = None, inf, a scalar, a 2 x 2 array of times),
     gradient_descent_mse_ensemble (t = None, a scalar, an array; means and covariances) and
