@@ -13,7 +13,8 @@ Writes, in float64 (the reference under jax_enable_x64, inputs cast to float64):
   reference_random.npz   nngp / ntk of the 40 seeded random networks of random_networks()
                          (their specs and inputs are regenerated from the seed) and the
                          diagonal_spatial requirement the reference derives for each
-                         (input, output as Bool values), keys 'net<i>/<name>';
+                         (input, output as Bool values) and its init_fn's output shape for
+                         x1, keys 'net<i>/<name>';
   reference_predictions.npz  gradient_descent_mse at t = None / inf / a scalar / an array of
                          times, gradient_descent_mse_ensemble and gp_inference (means and
                          covariances), keys '<case>/<name>', and the kernels they were
@@ -199,6 +200,11 @@ def prediction_inputs():
             0.1 * rng.standard_normal((5, 2)))
 
 
+def jax_key():
+    import jax
+    return jax.random.PRNGKey(0)
+
+
 def _load_reference(path):
     sys.path.insert(0, os.path.join(ROOT, 'oracle', 'jax_stand_in'))
     pkg = types.ModuleType('neural_tangents')
@@ -239,6 +245,8 @@ def main(path=DEFAULT_REFERENCE):
         arrays[f'net{i}/ntk'] = np.asarray(t)
         req = kf.input_req['diagonal_spatial']
         arrays[f'net{i}/diagonal_spatial_req'] = np.array([int(req.input), int(req.output)])
+        init_fn = stax.serial(*build(stax, spec))[0]
+        arrays[f'net{i}/out_shape'] = np.array(init_fn(jax_key(), x1.shape)[0])
     np.savez_compressed(os.path.join(HERE, 'reference_random.npz'), **arrays)
     print('random networks', len(arrays) // 2)
 

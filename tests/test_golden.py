@@ -104,13 +104,17 @@ def test_oracle_matches_reference_on_random_networks():
 def test_product_requirements_match_reference():
     """Host planning: for each random network the product's serial() derives the same
     diagonal_spatial requirement (requirements.py:401-515 folded over the layers) as the
-    reference did, which decides the kernel layout every rule then runs on."""
+    reference did, which decides the kernel layout every rule then runs on, and its init_fn
+    the same output shape."""
     from nt_gb300 import stax
     ref = np.load(os.path.join(HERE, 'reference_random.npz'))
-    for i, (spec, _, _) in enumerate(R.random_networks()):
-        d = stax.serial(*R.build(stax, spec))[2].input_req['diagonal_spatial']
+    for i, (spec, x1, _) in enumerate(R.random_networks()):
+        init_fn, _, kernel_fn = stax.serial(*R.build(stax, spec))
+        d = kernel_fn.input_req['diagonal_spatial']
         assert (int(d.input), int(d.output)) == tuple(ref[f'net{i}/diagonal_spatial_req']), \
             (i, spec)
+        # and the same output shape from init_fn (padding, strides and pools alike)
+        assert tuple(init_fn(0, x1.shape)[0]) == tuple(ref[f'net{i}/out_shape']), (i, spec)
 
 
 def test_oracle_predictions_match_reference():
