@@ -93,6 +93,15 @@ KERNEL_CASES = {
         (3, 16, 16, 3), None, ('nngp', 'ntk', 'cov1'), {}),
     'myrtle10_32': (lambda m: _myrtle10(m), (2, 32, 32, 3), (1, 32, 32, 3),
                     ('nngp', 'ntk', 'cov1', 'cov2'), {}),
+    'conv1d_pool_gap': (
+        lambda m: [m.Conv(1, (3,), padding='SAME', W_std=1.3, b_std=0.1), m.Relu(),
+                   m.AvgPool((2,), (2,)), m.Conv(1, (2,), padding='VALID', W_std=1.2, b_std=0.05),
+                   m.Erf(), m.GlobalAvgPool(), m.Dense(1, 1.1, 0.1)],
+        (2, 9, 3), (3, 9, 3), ('nngp', 'ntk', 'cov1', 'cov2'), {}),
+    'conv1d_circular_strided_same_inputs': (
+        lambda m: [m.Conv(1, (3,), strides=(2,), padding='CIRCULAR', W_std=1.3, b_std=0.1),
+                   m.Gelu(), m.Flatten(), m.Dense(1, 1.1, 0.1)],
+        (3, 9, 3), None, ('nngp', 'ntk', 'cov1'), {}),
     'fc_standard_parameterization': (
         lambda m: [m.Dense(8, W_std=1.3, b_std=0.1, parameterization='standard', s=(2, 3)),
                    m.Relu(), m.Dense(8, W_std=1.2, b_std=0.2, parameterization='standard'),
