@@ -168,3 +168,81 @@ def test_gpu_matches_reference_fixture(nt, name):
         want = f[g]
         err = np.max(np.abs(got - want) / np.maximum(np.abs(want), 1e-30))
         assert err < 1e-5, (g, err)
+
+
+# ---------------------------------------------------------------------------
+# The stand-in's convolution and pooling, against direct loops: the primitives on which the
+# reference's outputs above were computed (loaded under a private name, not as `jax`).
+# ---------------------------------------------------------------------------
+def _stand_in():
+    import sys
+    name = 'ntg_jax_stand_in'
+    if name not in sys.modules:
+        path = os.path.join(os.path.dirname(HERE), '..', 'oracle', 'jax_stand_in', 'jax')
+        spec = importlib.util.spec_from_file_location(
+            name, os.path.join(path, '__init__.py'), submodule_search_locations=[path])
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
+def _direct_conv_nchw(x, w, strides, pads, groups):
+    n, c, h, wd = x.shape
+    o_, i_, kh, kw = w.shape
+    xp = np.pad(x, ((0, 0), (0, 0), pads[0], pads[1]))
+    oh = (xp.shape[2] - kh) // strides[0] + 1
+    ow = (xp.shape[3] - kw) // strides[1] + 1
+    out = np.zeros((n, o_, oh, ow))
+    per = o_ // groups
+    for b in range(n):
+        for oc in range(o_):
+            g = oc // per
+            for p in range(oh):
+                for q in range(ow):
+                    win = xp[b, g * i_:(g + 1) * i_, p * strides[0]:p * strides[0] + kh,
+                             q * strides[1]:q * strides[1] + kw]
+                    out[b, oc, p, q] = np.sum(win * w[oc])
+    return out
+
+
+@pytest.mark.parametrize('padding', ['SAME', 'VALID', ((1, 2), (0, 1))])
+@pytest.mark.parametrize('strides', [(1, 1), (2, 1)])
+def test_stand_in_convolution_is_lax_cross_correlation(padding, strides):
+    """NCHW / OIHW and NHWC / HWIO layouts, feature groups, lax's SAME rule (output
+    ceil(n / s), the smaller half of the padding first) and explicit padding."""
+    lax = _stand_in().lax
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((2, 4, 7, 6))
+    for groups in (1, 2):
+        w = rng.standard_normal((4, 4 // groups, 3, 2))
+        pads = lax.padtype_to_pads((7, 6), (3, 2), strides, padding)
+        if padding == 'SAME':
+            for n, k, s_, (lo, hi) in zip((7, 6), (3, 2), strides, pads):
+                total = max((-(-n // s_) - 1) * s_ + k - n, 0)
+                assert (lo, hi) == (total // 2, total - total // 2)
+        want = _direct_conv_nchw(x, w, strides, pads, groups)
+        got = lax.conv_general_dilated(x, w, strides, padding, feature_group_count=groups,
+                                       dimension_numbers=('NCHW', 'OIHW', 'NCHW'))
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12)
+        got = lax.conv_general_dilated(np.transpose(x, (0, 2, 3, 1)), np.transpose(w, (2, 3, 1, 0)),
+                                       strides, padding, feature_group_count=groups,
+                                       dimension_numbers=('NHWC', 'HWIO', 'NHWC'))
+        np.testing.assert_allclose(np.transpose(got, (0, 3, 1, 2)), want, rtol=1e-12, atol=1e-12)
+
+
+def test_stand_in_window_sums_and_dot_general():
+    lax = _stand_in().lax
+    rng = np.random.default_rng(6)
+    x = rng.standard_normal((2, 5, 6, 3))
+    got = lax.reduce_window(x, 0., lax.add, (1, 2, 3, 1), (1, 2, 1, 1), 'SAME')
+    pads = lax.padtype_to_pads(x.shape, (1, 2, 3, 1), (1, 2, 1, 1), 'SAME')
+    xp = np.pad(x, pads)
+    want = np.zeros(got.shape)
+    for i in range(got.shape[1]):
+        for j in range(got.shape[2]):
+            want[:, i, j, :] = xp[:, 2 * i:2 * i + 2, j:j + 3, :].sum(axis=(1, 2))
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12)
+    a, b = rng.standard_normal((3, 4, 5)), rng.standard_normal((3, 5, 6))
+    np.testing.assert_allclose(lax.dot_general(a, b, (((2,), (1,)), ((0,), (0,)))),
+                               np.einsum('bij,bjk->bik', a, b), rtol=1e-12)
