@@ -13,8 +13,9 @@ Writes, in float64 (the reference under jax_enable_x64, inputs cast to float64):
   reference_random.npz   nngp / ntk of the 40 seeded random networks of random_networks()
                          (their specs and inputs are regenerated from the seed) and the
                          diagonal_spatial requirement the reference derives for each
-                         (input, output as Bool values) and its init_fn's output shape for
-                         x1, keys 'net<i>/<name>';
+                         (input, output as Bool values), its init_fn's output shape for x1
+                         and the ValueError text of a diagonal_spatial=True request ('' when
+                         the network serves it), keys 'net<i>/<name>';
   reference_predictions.npz  gradient_descent_mse at t = None / inf / a scalar / an array of
                          times, gradient_descent_mse_ensemble and gp_inference (means and
                          covariances), keys '<case>/<name>', and the kernels they were
@@ -256,6 +257,12 @@ def main(path=DEFAULT_REFERENCE):
         arrays[f'net{i}/diagonal_spatial_req'] = np.array([int(req.input), int(req.output)])
         init_fn = stax.serial(*build(stax, spec))[0]
         arrays[f'net{i}/out_shape'] = np.array(init_fn(jax_key(), x1.shape)[0])
+        try:  # a diagonal-spatial request the network cannot serve
+            kf(x1, x2, 'nngp', diagonal_spatial=True)
+            msg = ''
+        except ValueError as e:
+            msg = str(e)
+        arrays[f'net{i}/diagonal_spatial_error'] = np.array(msg)
     np.savez_compressed(os.path.join(HERE, 'reference_random.npz'), **arrays)
     print('random networks', len(arrays) // 2)
 

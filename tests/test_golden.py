@@ -115,6 +115,13 @@ def test_product_requirements_match_reference():
             (i, spec)
         # and the same output shape from init_fn (padding, strides and pools alike)
         assert tuple(init_fn(0, x1.shape)[0]) == tuple(ref[f'net{i}/out_shape']), (i, spec)
+        # a diagonal-spatial request the network cannot serve: the reference's ValueError,
+        # word for word, raised before any kernel runs
+        msg = str(ref[f'net{i}/diagonal_spatial_error'])
+        if msg:
+            with pytest.raises(ValueError) as err:
+                kernel_fn(x1, None, 'nngp', diagonal_spatial=True)
+            assert str(err.value) == msg, (i, str(err.value), msg)
 
 
 def test_oracle_predictions_match_reference():
