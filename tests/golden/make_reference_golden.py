@@ -94,6 +94,8 @@ KERNEL_CASES = {
         (3, 16, 16, 3), None, ('nngp', 'ntk', 'cov1'), {}),
     'myrtle10_32': (lambda m: _myrtle10(m), (2, 32, 32, 3), (1, 32, 32, 3),
                     ('nngp', 'ntk', 'cov1', 'cov2'), {}),
+    'myrtle5_32_same_inputs': (lambda m: _myrtle5(m), (3, 32, 32, 3), None,
+                               ('nngp', 'ntk', 'cov1'), {}),
     'conv1d_pool_gap': (
         lambda m: [m.Conv(1, (3,), padding='SAME', W_std=1.3, b_std=0.1), m.Relu(),
                    m.AvgPool((2,), (2,)), m.Conv(1, (2,), padding='VALID', W_std=1.2, b_std=0.05),
@@ -116,6 +118,15 @@ KERNEL_CASES = {
                    m.GlobalAvgPool(), m.Dense(1, 1.1, 0.05, parameterization='standard')],
         (2, 6, 6, 3), (3, 6, 6, 3), ('nngp', 'ntk', 'cov1', 'cov2'), {}),
 }
+
+
+def _myrtle5(m):
+    """Myrtle-5 as benchmarked: Conv3x3 + Relu x2, AvgPool, Conv + Relu, AvgPool, Conv + Relu,
+    AvgPool x3, Flatten, Dense (W_std = sqrt 2, b_std = 0)."""
+    conv = lambda: m.Conv(1, (3, 3), padding='SAME', W_std=math.sqrt(2.), b_std=0.)
+    pool = lambda: m.AvgPool((2, 2), (2, 2))
+    return [conv(), m.Relu(), conv(), m.Relu(), pool(), conv(), m.Relu(), pool(), conv(),
+            m.Relu(), pool(), pool(), pool(), m.Flatten(), m.Dense(10, math.sqrt(2.), 0.)]
 
 
 def _myrtle10(m):
